@@ -1,0 +1,1206 @@
+/* FP64 CPU restatement of the reference's Monte Carlo energy path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the oracle). Loaded by tests/, the smoke check
+ * and bench.py's CPU-baseline leg; never by the product.
+ *
+ * Each function names the reference lines it restates. Arithmetic is kept in
+ * the reference's evaluation order wherever the result feeds a comparison
+ * (rejection loops, cut-offs, the Metropolis test), so the draw sequence and
+ * accept/reject decisions match the reference for the same mt19937 stream.
+ * The reciprocal Ewald term is the one deliberate rewrite: the reference sums
+ * (4 pi lB q_i q_j / V) sum_k e^{-k^2/4a}/k^2 cos(k.r_ij) over pairs
+ * (potential_ewald_coul.cc:198-225); here it is (4 pi lB / V) sum over the
+ * half k-space of e^{-k^2/4a}/k^2 |S(k)|^2 on the identical k-set, which is
+ * the same quantity.
+ */
+#include "plum_oracle.h"
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* utilities/constants.h:5-62 */
+#define K_EWALD_CUTOFF 1e-7
+#define K_VERY_LARGE 1e8
+#define K_PI 3.14159265359
+#define K213 1.25992104989
+#define K216 1.12246204831
+#define K_DI_CORRECTION 3
+#define K_NO_MOVE_TYPE 5
+#define K_MED_SMALL 1e-4
+#define MAXT 64
+/* M_PI as <cmath> defines it; the crankshaft angle uses it (molecule.cc:247). */
+#define M_PI_LIBM 3.14159265358979323846
+
+/* ------------------------------------------------------------------ mt19937 */
+/* Matsumoto & Nishimura (1998) MT19937 with the standard initialisation and
+ * tempering; std::mt19937 (used by the reference, simulation.h:148) is this
+ * generator. */
+typedef struct {
+  uint32_t mt[624];
+  int idx;
+} mt_t;
+
+static void mt_seed(mt_t* g, uint32_t s) {
+  g->mt[0] = s;
+  for (int i = 1; i < 624; i++)
+    g->mt[i] = 1812433253u * (g->mt[i - 1] ^ (g->mt[i - 1] >> 30)) + (uint32_t)i;
+  g->idx = 624;
+}
+
+static uint32_t mt_next(mt_t* g) {
+  if (g->idx >= 624) {
+    for (int i = 0; i < 624; i++) {
+      uint32_t y = (g->mt[i] & 0x80000000u) | (g->mt[(i + 1) % 624] & 0x7fffffffu);
+      uint32_t v = g->mt[(i + 397) % 624] ^ (y >> 1);
+      if (y & 1u) v ^= 0x9908b0dfu;
+      g->mt[i] = v;
+    }
+    g->idx = 0;
+  }
+  uint32_t y = g->mt[g->idx++];
+  y ^= y >> 11;
+  y ^= (y << 7) & 0x9d2c5680u;
+  y ^= (y << 15) & 0xefc60000u;
+  y ^= y >> 18;
+  return y;
+}
+
+void po_mt19937(uint32_t seed, long n, uint32_t* out) {
+  mt_t g;
+  mt_seed(&g, seed);
+  for (long i = 0; i < n; i++) out[i] = mt_next(&g);
+}
+
+/* Draw source: the internal generator or a recorded stream. */
+typedef struct {
+  mt_t* g;
+  const uint32_t* s;
+  long n, pos;
+  int overrun;
+} rng_t;
+
+static uint32_t rng_u32(rng_t* r) {
+  if (r->s) {
+    if (r->pos >= r->n) {
+      r->overrun = 1;
+      return 0;
+    }
+    return r->s[r->pos++];
+  }
+  r->pos++;
+  return mt_next(r->g);
+}
+static const double MT_MAX = 4294967295.0;
+
+/* ---------------------------------------------------------------- context */
+struct po_ctx {
+  int n_bead, n_mol, n_type;
+  double* x;   /* current xyz, unwrapped */
+  double* t;   /* trial xyz */
+  double* q;
+  int* type;
+  int* mol_start; /* n_mol+1 */
+  char sym[MAXT][16];
+  /* run.in: simulation.cc:30-50 */
+  double box[3];
+  int npbc;
+  double beta, move_size;
+  int calc_chem_pot, phantom, coion, grafted, grafted_counterion;
+  double move_prob[5];
+  /* force_field.cc:65-103 */
+  int use_pair, use_ewald, use_bond, use_rigid, use_angle, use_dihed, use_ext,
+      use_gc;
+  double rigid;
+  double lj_cut, lj_sig[MAXT], lj_eps[MAXT];
+  double lB, dielectric, alpha;
+  int dipole;
+  double ebox[3], evol, real_cut, kc2;
+  int real_cell[3], kcell[3];
+  int n_k;
+  double *kv, *kw, *sk; /* kv: n_k*3, kw: e^{-k2/4a}/k2, sk: n_k*2 */
+  double kpref;         /* lB/(kPi V) * 4 kPi^2 */
+  double k_bond, r0;
+  double wall_cut, wall_sig[MAXT], wall_eps[MAXT];
+  int graft[MAXT]; /* 0 none, 1 "L", 2 "R" */
+  /* running totals (force_field.cc:1201-1219) */
+  double e_pair, e_ewald, e_bond, e_ext, dipl_cur;
+  double* bond_mol;
+  /* counts (simulation.cc:1066-1094) */
+  int n_chain, n_cion, n_aion, n_nion;
+  mt_t g;
+};
+
+int po_n_bead(const po_ctx* c) { return c->n_bead; }
+int po_n_mol(const po_ctx* c) { return c->n_mol; }
+int po_n_kvec(const po_ctx* c) { return c->n_k; }
+
+/* ------------------------------------------------------------- tokenizer */
+typedef struct {
+  char* buf;
+  char* p;
+} tok_t;
+
+static int tok_open(tok_t* t, const char* path) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return -1;
+  fseek(f, 0, SEEK_END);
+  long n = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  t->buf = (char*)malloc((size_t)n + 1);
+  size_t got = fread(t->buf, 1, (size_t)n, f);
+  t->buf[got] = 0;
+  fclose(f);
+  t->p = t->buf;
+  return 0;
+}
+
+static const char* tok_next(tok_t* t) {
+  while (*t->p && (*t->p == ' ' || *t->p == '\t' || *t->p == '\n' || *t->p == '\r'))
+    t->p++;
+  if (!*t->p) return NULL;
+  char* s = t->p;
+  while (*t->p && !(*t->p == ' ' || *t->p == '\t' || *t->p == '\n' || *t->p == '\r'))
+    t->p++;
+  if (*t->p) *t->p++ = 0;
+  return s;
+}
+
+typedef struct {
+  tok_t* t;
+  char* err;
+  int cap;
+  int bad;
+} rd_t;
+
+static void rd_fail(rd_t* r, const char* fmt, ...) {
+  if (r->bad) return;
+  r->bad = 1;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(r->err, (size_t)r->cap, fmt, ap);
+  va_end(ap);
+}
+
+/* `flag value` item: skips the flag, returns the value token. */
+static const char* rd_item(rd_t* r, const char* what) {
+  if (r->bad) return "0";
+  const char* f = tok_next(r->t);
+  const char* v = f ? tok_next(r->t) : NULL;
+  if (!v) {
+    rd_fail(r, "run.in ended while reading %s", what);
+    return "0";
+  }
+  return v;
+}
+static double rd_d(rd_t* r, const char* w) { return atof(rd_item(r, w)); }
+static int rd_i(rd_t* r, const char* w) { return atoi(rd_item(r, w)); }
+
+static int type_of(po_ctx* c, const char* s) {
+  for (int i = 0; i < c->n_type; i++)
+    if (!strcmp(c->sym[i], s)) return i;
+  if (c->n_type >= MAXT) return -1;
+  snprintf(c->sym[c->n_type], 16, "%s", s);
+  c->lj_sig[c->n_type] = c->lj_eps[c->n_type] = 0.0;
+  c->wall_sig[c->n_type] = c->wall_eps[c->n_type] = 0.0;
+  c->graft[c->n_type] = !strcmp(s, "L") ? 1 : (!strcmp(s, "R") ? 2 : 0);
+  return c->n_type++;
+}
+
+/* {symbol sigma epsilon}... end  (potential_truncated_lj.cc:31-45,
+ * potential_truncated_lj_wall.cc:29-43). Symbols absent from the table keep
+ * sigma = epsilon = 0, as std::map::operator[] gives the reference. */
+static void rd_table(rd_t* r, po_ctx* c, double* sig, double* eps) {
+  for (int guard = 0; guard < 100000 && !r->bad; guard++) {
+    const char* s = rd_item(r, "bead type symbol");
+    if (r->bad) return;
+    if (!strcmp(s, "end")) return;
+    char name[16];
+    snprintf(name, 16, "%s", s);
+    double sg = rd_d(r, "sigma"), ep = rd_d(r, "epsilon");
+    int ti = type_of(c, name);
+    if (ti < 0) {
+      rd_fail(r, "too many bead types");
+      return;
+    }
+    sig[ti] = sg;
+    eps[ti] = ep;
+  }
+}
+
+static char* join_path(const char* dir, const char* name) {
+  size_t n = strlen(dir) + strlen(name) + 2;
+  char* p = (char*)malloc(n);
+  if (name[0] == '/')
+    snprintf(p, n, "%s", name);
+  else
+    snprintf(p, n, "%s/%s", dir, name);
+  return p;
+}
+
+/* ------------------------------------------------------------ geometry */
+/* Bead::BBDist on two coordinate triples (bead.cc:162-176). */
+static double bbdist(const double* a, const double* b, const double* box,
+                     int npbc) {
+  double dist = 0;
+  for (int i = 0; i < 3; i++) {
+    double di = a[i] - b[i];
+    if (i < npbc) {
+      di -= box[i] * round(di / box[i]);
+      if (fabs(di) > 0.5 * box[i]) di = box[i] - fabs(di);
+    }
+    dist += (di * di);
+  }
+  return sqrt(dist);
+}
+
+/* PotentialTruncatedLJ::PairEnergy (potential_truncated_lj.cc:49-85). */
+static double lj_pair(const po_ctx* c, const double* a, int ta, const double* b,
+                      int tb) {
+  double energy = 0;
+  double r = bbdist(a, b, c->box, c->npbc);
+  double sigma = (c->lj_sig[ta] + c->lj_sig[tb]) / 2;
+  double epsilon = sqrt((c->lj_eps[ta] * c->lj_eps[tb]));
+  if (r <= 0) return K_VERY_LARGE;
+  if (c->lj_cut < 0) {
+    double r6_ref = pow((1.0 / K216), 6);
+    double energy_ref = 4 * epsilon * (r6_ref * r6_ref - r6_ref);
+    if (r < K216 * sigma) {
+      double r6 = pow((sigma / r), 6);
+      energy = 4 * epsilon * (r6 * r6 - r6) - energy_ref;
+    }
+  } else if (r < c->lj_cut) {
+    double r6_ref = pow((sigma / c->lj_cut), 6);
+    double energy_ref = 4 * epsilon * (r6_ref * r6_ref - r6_ref);
+    double r6 = pow((sigma / r), 6);
+    energy = 4 * epsilon * (r6 * r6 - r6) - energy_ref;
+  }
+  return energy;
+}
+
+/* PotentialEwaldCoul::PairEnergyReal (potential_ewald_coul.cc:134-164) with
+ * GetDistVector (misc.cc:43-56) on the Ewald box. */
+static double ew_real_pair(const po_ctx* c, const double* a, double qa,
+                           const double* b, double qb) {
+  double energy = 0;
+  if (qa * qb == 0) return energy;
+  double dist[3];
+  for (int i = 0; i < 3; i++) {
+    double di = b[i] - a[i];
+    if (i < c->npbc) di -= c->ebox[i] * round(di / c->ebox[i]);
+    dist[i] = di;
+  }
+  double prefactor = c->lB * qa * qb;
+  for (int i = -c->real_cell[0]; i <= c->real_cell[0]; i++)
+    for (int j = -c->real_cell[1]; j <= c->real_cell[1]; j++)
+      for (int k = -c->real_cell[2]; k <= c->real_cell[2]; k++) {
+        double rv0 = dist[0] + i * c->ebox[0];
+        double rv1 = dist[1] + j * c->ebox[1];
+        double rv2 = dist[2] + k * c->ebox[2];
+        double r = sqrt(rv0 * rv0 + rv1 * rv1 + rv2 * rv2);
+        if (r > 0 && r <= c->real_cut)
+          energy += prefactor * erfc(sqrt(c->alpha) * r) / r;
+      }
+  return energy;
+}
+
+/* SelfEnergy (potential_ewald_coul.cc:253-257). */
+static double ew_self(const po_ctx* c, double q) {
+  return -c->lB * sqrt(c->alpha / K_PI) * q * q;
+}
+
+/* DipoleE on current z (potential_ewald_coul.cc:415-428). */
+static double ew_dipole(const po_ctx* c) {
+  double mz = 0;
+  for (int i = 0; i < c->n_bead; i++) mz += c->q[i] * c->x[3 * i + 2];
+  return c->lB * 2 * K_PI / (c->evol / 1.0) * mz * mz;
+}
+
+/* PotentialSpring::MoleculeEnergy (potential_spring.cc:22-48) on coords p. */
+static double bond_mol_energy(const po_ctx* c, int m, const double* p) {
+  double e = 0;
+  for (int i = c->mol_start[m]; i < c->mol_start[m + 1] - 1; i++) {
+    double r = bbdist(p + 3 * i, p + 3 * (i + 1), c->box, 0);
+    e += 0.5 * c->k_bond * (r - c->r0) * (r - c->r0);
+  }
+  return e;
+}
+
+/* PotentialTruncatedLJWall::BeadEnergy (potential_truncated_lj_wall.cc:46-134). */
+static double wall_energy(const po_ctx* c, double z, int ty) {
+  double energy = 0;
+  double sigma = c->wall_sig[ty], epsilon = c->wall_eps[ty];
+  double R0 = 3 * K213 * sigma, K = 1;
+  double lz = c->box[2];
+  int g = c->graft[ty];
+  if (epsilon == 0) return 0;
+  if (z <= 0 || z >= lz) return K_VERY_LARGE;
+  if (c->wall_cut < 0 && g == 0) {
+    double r3_ref = pow((1.0 / K213), 3);
+    double energy_ref = 2.59807621135 * epsilon * (r3_ref * r3_ref - r3_ref);
+    if (z < K213 * sigma) {
+      double r3 = pow((sigma / z), 3);
+      energy += 2.59807621135 * epsilon * (r3 * r3 - r3) - energy_ref;
+    }
+    if (lz - z < K213 * sigma) {
+      double r3 = pow((sigma / (lz - z)), 3);
+      energy += 2.59807621135 * epsilon * (r3 * r3 - r3) - energy_ref;
+    }
+  } else if (g == 1) {
+    double r3 = pow((sigma / z), 3);
+    energy += 2.59807621135 * epsilon * (r3 * r3 - r3);
+    energy += -0.5 * K * R0 * R0 * log(1 - pow(z / R0, 2));
+    if (lz - z < K213 * sigma) {
+      r3 = pow((sigma / (lz - z)), 3);
+      energy += 2.59807621135 * epsilon * (r3 * r3 - r3);
+    } else {
+      r3 = pow((1.0 / K213), 3);
+      energy += 2.59807621135 * epsilon * (r3 * r3 - r3);
+    }
+  } else if (g == 2) {
+    double r3 = pow((sigma / (lz - z)), 3);
+    energy += 2.59807621135 * epsilon * (r3 * r3 - r3);
+    energy += -0.5 * K * R0 * R0 * log(1 - pow((lz - z) / R0, 2));
+    if (z < K213 * sigma) {
+      r3 = pow((sigma / z), 3);
+      energy += 2.59807621135 * epsilon * (r3 * r3 - r3);
+    } else {
+      r3 = pow((1.0 / K213), 3);
+      energy += 2.59807621135 * epsilon * (r3 * r3 - r3);
+    }
+  } else {
+    double r3_ref = pow((1.0 / c->wall_cut), 3);
+    double energy_ref = 2.59807621135 * epsilon * (r3_ref * r3_ref - r3_ref);
+    if (z < c->wall_cut) {
+      double r3 = pow((sigma / z), 3);
+      energy += 2.59807621135 * epsilon * (r3 * r3 - r3) - energy_ref;
+    }
+    if (lz - z < c->wall_cut) {
+      double r3 = pow((sigma / (lz - z)), 3);
+      energy += 2.59807621135 * epsilon * (r3 * r3 - r3) - energy_ref;
+    }
+  }
+  return energy;
+}
+
+/* Structure factor contribution of one bead: q e^{i k.r} for every k in the
+ * half space, positions wrapped into the primary cell on periodic axes. */
+static void sk_add(const po_ctx* c, const double* p, double q, double sign,
+                   double* acc) {
+  double w[3];
+  for (int a = 0; a < 3; a++) {
+    w[a] = p[a];
+    if (a < c->npbc) w[a] -= c->ebox[a] * floor(p[a] / c->ebox[a]);
+  }
+  for (int k = 0; k < c->n_k; k++) {
+    double ph = c->kv[3 * k] * w[0] + c->kv[3 * k + 1] * w[1] + c->kv[3 * k + 2] * w[2];
+    acc[2 * k] += sign * q * cos(ph);
+    acc[2 * k + 1] += sign * q * sin(ph);
+  }
+}
+
+static double sk_energy(const po_ctx* c, const double* s) {
+  double e = 0;
+  for (int k = 0; k < c->n_k; k++)
+    e += c->kw[k] * (s[2 * k] * s[2 * k] + s[2 * k + 1] * s[2 * k + 1]);
+  return c->kpref * e;
+}
+
+/* ----------------------------------------------------------- Ewald setup */
+/* PotentialEwaldCoul::ReadParameters (potential_ewald_coul.cc:38-115), with
+ * optional overrides from the trailing extension block. */
+static void ewald_setup(po_ctx* c, double rc_over, int kmax_over, double kc2_over,
+                        int have_kc2) {
+  for (int i = 0; i < 3; i++) c->ebox[i] = c->box[i];
+  if (c->dipole) {
+    double min_padding = 150;
+    if (c->ebox[2] * K_DI_CORRECTION > min_padding)
+      c->ebox[2] = c->ebox[2] * K_DI_CORRECTION;
+    else
+      c->ebox[2] += min_padding;
+  }
+  c->evol = c->ebox[0] * c->ebox[1] * c->ebox[2];
+  c->real_cut = 1;
+  while (0.5 * c->lB * 1 * 1 * erfc(sqrt(c->alpha) * c->real_cut) / c->real_cut >
+         K_EWALD_CUTOFF)
+    c->real_cut += 1;
+  if (rc_over > 0) c->real_cut = rc_over;
+  for (int i = 0; i < 3; i++) c->real_cell[i] = (int)ceil(c->real_cut / c->ebox[i]);
+  c->kc2 = c->alpha;
+  double min_box_vol = pow(c->ebox[0], 3);
+  while (c->lB * 1 * 1 / (2 * K_PI * min_box_vol) * (4 * K_PI * K_PI) *
+             exp(-c->kc2 / (4 * c->alpha)) / c->kc2 >
+         K_EWALD_CUTOFF)
+    c->kc2 += c->alpha;
+  for (int i = 0; i < 3; i++)
+    c->kcell[i] = (int)ceil(sqrt(c->kc2) * c->ebox[i] / (2 * K_PI));
+  if (kmax_over > 0) {
+    for (int i = 0; i < 3; i++) c->kcell[i] = kmax_over;
+    if (!have_kc2) c->kc2 = INFINITY;
+  }
+  if (have_kc2) c->kc2 = kc2_over > 0 ? kc2_over : INFINITY;
+  int cap = (2 * c->kcell[0] + 1) * (2 * c->kcell[1] + 1) * (2 * c->kcell[2] + 1);
+  c->kv = (double*)malloc(sizeof(double) * 3 * (size_t)cap);
+  c->kw = (double*)malloc(sizeof(double) * (size_t)cap);
+  c->n_k = 0;
+  for (int lx = -c->kcell[0]; lx <= c->kcell[0]; lx++)
+    for (int ly = -c->kcell[1]; ly <= c->kcell[1]; ly++)
+      for (int lz = -c->kcell[2]; lz <= c->kcell[2]; lz++) {
+        int half = lx > 0 || (lx == 0 && ly > 0) || (lx == 0 && ly == 0 && lz > 0);
+        if (!half) continue;
+        double kx = lx * 2 * K_PI / c->ebox[0];
+        double ky = ly * 2 * K_PI / c->ebox[1];
+        double kz = lz * 2 * K_PI / c->ebox[2];
+        double k2 = kx * kx + ky * ky + kz * kz;
+        if (!(k2 > 0 && k2 <= c->kc2)) continue;
+        c->kv[3 * c->n_k] = kx;
+        c->kv[3 * c->n_k + 1] = ky;
+        c->kv[3 * c->n_k + 2] = kz;
+        c->kw[c->n_k] = exp(-k2 / (4 * c->alpha)) / k2;
+        c->n_k++;
+      }
+  c->kpref = c->lB / (K_PI * c->evol) * (4 * K_PI * K_PI);
+  c->sk = (double*)calloc((size_t)2 * (c->n_k > 0 ? c->n_k : 1), sizeof(double));
+}
+
+void po_ewald_info(const po_ctx* c, double* out) {
+  out[0] = c->real_cut;
+  out[1] = c->kc2;
+  for (int i = 0; i < 3; i++) out[2 + i] = c->real_cell[i];
+  for (int i = 0; i < 3; i++) out[5 + i] = c->kcell[i];
+  for (int i = 0; i < 3; i++) out[8 + i] = c->ebox[i];
+  out[11] = c->alpha;
+  out[12] = c->lB;
+  out[13] = c->evol;
+  out[14] = c->dipole;
+}
+
+/* simulation.cc:1066-1094 */
+static void update_counts(po_ctx* c) {
+  c->n_chain = c->n_cion = c->n_aion = c->n_nion = 0;
+  for (int m = c->phantom; m < c->n_mol; m++) {
+    int sz = c->mol_start[m + 1] - c->mol_start[m];
+    double q0 = c->q[c->mol_start[m]];
+    if (sz > 1)
+      c->n_chain++;
+    else if (q0 > 0)
+      c->n_cion++;
+    else if (q0 < 0)
+      c->n_aion++;
+    else
+      c->n_nion++;
+  }
+  c->n_chain -= c->grafted;
+}
+
+/* ------------------------------------------------------------- creation */
+po_ctx* po_create(const char* dir, const char* runin, uint32_t seed, char* err,
+                  int cap) {
+  po_ctx* c = (po_ctx*)calloc(1, sizeof(po_ctx));
+  tok_t tr, tt, tc;
+  memset(&tr, 0, sizeof(tr));
+  memset(&tt, 0, sizeof(tt));
+  memset(&tc, 0, sizeof(tc));
+  rd_t r = {&tr, err, cap, 0};
+  char* p = join_path(dir, runin);
+  if (tok_open(&tr, p)) {
+    snprintf(err, (size_t)cap, "cannot open %s", p);
+    free(p);
+    free(c);
+    return NULL;
+  }
+  free(p);
+  char crd[512], top[512];
+  snprintf(crd, sizeof crd, "%s", rd_item(&r, "crd name"));
+  snprintf(top, sizeof top, "%s", rd_item(&r, "top name"));
+  rd_item(&r, "run name");
+  rd_item(&r, "steps");
+  rd_item(&r, "steps_eq");
+  rd_item(&r, "sample_freq");
+  rd_item(&r, "stat_out_freq");
+  rd_item(&r, "traj_out_freq");
+  c->npbc = rd_i(&r, "npbc");
+  c->beta = rd_d(&r, "beta");
+  c->move_size = rd_d(&r, "move_size");
+  c->calc_chem_pot = rd_i(&r, "calc_chem_pot");
+  c->phantom = rd_i(&r, "phantom");
+  c->coion = rd_i(&r, "coion");
+  c->grafted = rd_i(&r, "grafted");
+  c->grafted_counterion = rd_i(&r, "grafted_counterion");
+  for (int i = 0; i < 5; i++) c->move_prob[i] = rd_d(&r, "move_prob");
+  rd_item(&r, "vp_el_res");
+  rd_item(&r, "vp_bead_size");
+  c->use_pair = rd_i(&r, "use_pair");
+  c->use_ewald = rd_i(&r, "use_ewald");
+  c->use_bond = rd_i(&r, "use_bond");
+  c->use_rigid = rd_i(&r, "use_bond_rigid");
+  c->use_angle = rd_i(&r, "use_angle");
+  c->use_dihed = rd_i(&r, "use_dihed");
+  c->use_ext = rd_i(&r, "use_ext");
+  c->use_gc = rd_i(&r, "use_gc");
+  if (c->use_gc) {
+    for (int i = 0; i < 7; i++) rd_item(&r, "gc parameter");
+  }
+  c->rigid = -1;
+  if (c->use_pair) {
+    const char* nm = rd_item(&r, "pair potential");
+    if (strcmp(nm, "TruncatedLJ")) rd_fail(&r, "unsupported pair potential %s", nm);
+    c->lj_cut = rd_d(&r, "LJ cutoff");
+    rd_table(&r, c, c->lj_sig, c->lj_eps);
+  }
+  if (c->use_ewald) {
+    const char* nm = rd_item(&r, "Ewald potential");
+    if (strcmp(nm, "Coul")) rd_fail(&r, "unsupported Ewald potential %s", nm);
+    c->lB = rd_d(&r, "lB");
+    c->dielectric = rd_d(&r, "dielectric");
+    c->alpha = rd_d(&r, "alpha");
+    c->dipole = rd_i(&r, "dipole correction");
+  }
+  if (c->use_bond) {
+    const char* nm = rd_item(&r, "bond potential");
+    if (strcmp(nm, "Spring")) rd_fail(&r, "unsupported bond potential %s", nm);
+    c->k_bond = rd_d(&r, "k");
+    c->r0 = rd_d(&r, "r0");
+  }
+  if (c->use_rigid) c->rigid = rd_d(&r, "rigid bond");
+  if (c->use_ext) {
+    const char* nm = rd_item(&r, "external potential");
+    if (strcmp(nm, "TruncatedLJWall")) rd_fail(&r, "unsupported external potential %s", nm);
+    c->wall_cut = rd_d(&r, "wall cutoff");
+    rd_item(&r, "wall sigma");
+    rd_item(&r, "wall epsilon");
+    rd_table(&r, c, c->wall_sig, c->wall_eps);
+  }
+  /* Trailing extension block (never read by the reference). */
+  double rc_over = -1, kc2_over = -1;
+  int kmax_over = -1, have_kc2 = 0;
+  for (;;) {
+    const char* key = tok_next(&tr);
+    const char* val = key ? tok_next(&tr) : NULL;
+    if (!val) break;
+    if (!strcmp(key, "plum_ewald_real_cutoff")) rc_over = atof(val);
+    if (!strcmp(key, "plum_ewald_kmax")) kmax_over = atoi(val);
+    if (!strcmp(key, "plum_ewald_kcut2")) {
+      kc2_over = atof(val);
+      have_kc2 = 1;
+    }
+  }
+  if (r.bad) goto fail;
+  /* top file: simulation.cc:610-646 */
+  p = join_path(dir, top);
+  if (tok_open(&tt, p)) {
+    snprintf(err, (size_t)cap, "cannot open %s", p);
+    free(p);
+    goto fail;
+  }
+  free(p);
+  {
+    rd_t rt = {&tt, err, cap, 0};
+    rd_item(&rt, "n_bead");
+    c->n_mol = rd_i(&rt, "n_mol");
+    for (int i = 0; i < 3; i++) c->box[i] = rd_d(&rt, "box");
+    if (rt.bad || c->n_mol <= 0) {
+      if (!rt.bad) snprintf(err, (size_t)cap, "bad molecule count");
+      goto fail;
+    }
+  }
+  /* crd file: simulation.cc:582-608 */
+  p = join_path(dir, crd);
+  {
+    FILE* f = fopen(p, "r");
+    free(p);
+    if (!f) {
+      snprintf(err, (size_t)cap, "cannot open coordinate file");
+      goto fail;
+    }
+    char line[1024];
+    if (!fgets(line, sizeof line, f) || !fgets(line, sizeof line, f)) {
+      fclose(f);
+      snprintf(err, (size_t)cap, "coordinate file too short");
+      goto fail;
+    }
+    int capb = 1024, nb = 0;
+    int* mol = (int*)malloc(sizeof(int) * capb);
+    double* xyz = (double*)malloc(sizeof(double) * 3 * capb);
+    double* qq = (double*)malloc(sizeof(double) * capb);
+    int* ty = (int*)malloc(sizeof(int) * capb);
+    int mid;
+    char s[64];
+    double x, y, z, q;
+    while (fscanf(f, "%d %63s %lf %lf %lf %lf", &mid, s, &x, &y, &z, &q) == 6) {
+      if (mid < 0 || mid >= c->n_mol) {
+        snprintf(err, (size_t)cap, "Molecule ID %d is out of bounds", mid);
+        fclose(f);
+        free(mol), free(xyz), free(qq), free(ty);
+        goto fail;
+      }
+      if (nb == capb) {
+        capb *= 2;
+        mol = (int*)realloc(mol, sizeof(int) * capb);
+        xyz = (double*)realloc(xyz, sizeof(double) * 3 * capb);
+        qq = (double*)realloc(qq, sizeof(double) * capb);
+        ty = (int*)realloc(ty, sizeof(int) * capb);
+      }
+      mol[nb] = mid;
+      xyz[3 * nb] = x, xyz[3 * nb + 1] = y, xyz[3 * nb + 2] = z;
+      qq[nb] = q;
+      ty[nb] = type_of(c, s);
+      nb++;
+    }
+    fclose(f);
+    /* Molecules are stored in molecule order; beads keep file order within a
+     * molecule (Molecule::AddBead, molecule.cc:47-52). */
+    c->n_bead = nb;
+    c->mol_start = (int*)calloc((size_t)c->n_mol + 1, sizeof(int));
+    for (int i = 0; i < nb; i++) c->mol_start[mol[i] + 1]++;
+    for (int m = 0; m < c->n_mol; m++) {
+      if (c->mol_start[m + 1] == 0) {
+        snprintf(err, (size_t)cap, "molecule %d has no beads", m);
+        free(mol), free(xyz), free(qq), free(ty);
+        goto fail;
+      }
+      c->mol_start[m + 1] += c->mol_start[m];
+    }
+    int* fill = (int*)calloc((size_t)c->n_mol, sizeof(int));
+    c->x = (double*)malloc(sizeof(double) * 3 * nb);
+    c->t = (double*)malloc(sizeof(double) * 3 * nb);
+    c->q = (double*)malloc(sizeof(double) * nb);
+    c->type = (int*)malloc(sizeof(int) * nb);
+    for (int i = 0; i < nb; i++) {
+      int k = c->mol_start[mol[i]] + fill[mol[i]]++;
+      memcpy(c->x + 3 * k, xyz + 3 * i, 3 * sizeof(double));
+      c->q[k] = qq[i];
+      c->type[k] = ty[i];
+    }
+    memcpy(c->t, c->x, sizeof(double) * 3 * nb);
+    free(fill), free(mol), free(xyz), free(qq), free(ty);
+  }
+  if (c->use_ewald) ewald_setup(c, rc_over, kmax_over, kc2_over, have_kc2);
+  c->bond_mol = (double*)calloc((size_t)c->n_mol, sizeof(double));
+  update_counts(c);
+  mt_seed(&c->g, seed);
+  {
+    double e[8];
+    po_total_energy(c, e);
+  }
+  free(tr.buf), free(tt.buf), free(tc.buf);
+  return c;
+fail:
+  free(tr.buf), free(tt.buf), free(tc.buf);
+  po_destroy(c);
+  return NULL;
+}
+
+void po_destroy(po_ctx* c) {
+  if (!c) return;
+  free(c->x), free(c->t), free(c->q), free(c->type), free(c->mol_start);
+  free(c->kv), free(c->kw), free(c->sk), free(c->bond_mol);
+  free(c);
+}
+
+static int mol_of(const po_ctx* c, int bead) {
+  int lo = 0, hi = c->n_mol - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) / 2;
+    if (c->mol_start[mid] <= bead)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+/* ------------------------------------------------------- total energy */
+/* ForceField::InitializeEnergy (force_field.cc:365-381) through the
+ * potentials' EnergyInitialization; pairs in the reference's loop order
+ * (intramolecular first, then molecule pairs), potential_pair.cc:55-100. */
+void po_total_energy(po_ctx* c, double* out) {
+  double ep = 0, er = 0, ek = 0, es = 0, ed = 0, eb = 0, ee = 0;
+  if (c->use_pair) {
+    for (int m = 0; m < c->n_mol; m++)
+      for (int j = c->mol_start[m]; j < c->mol_start[m + 1] - 1; j++)
+        for (int k = j + 1; k < c->mol_start[m + 1]; k++)
+          ep += lj_pair(c, c->x + 3 * j, c->type[j], c->x + 3 * k, c->type[k]);
+    for (int m = 0; m < c->n_mol - 1; m++)
+      for (int i = c->mol_start[m]; i < c->mol_start[m + 1]; i++)
+        for (int j = c->mol_start[m + 1]; j < c->n_bead; j++)
+          ep += lj_pair(c, c->x + 3 * i, c->type[i], c->x + 3 * j, c->type[j]);
+  }
+  if (c->use_ewald) {
+    for (int i = 0; i < c->n_bead; i++) {
+      er += 0.5 * ew_real_pair(c, c->x + 3 * i, c->q[i], c->x + 3 * i, c->q[i]);
+      for (int j = i + 1; j < c->n_bead; j++)
+        er += ew_real_pair(c, c->x + 3 * i, c->q[i], c->x + 3 * j, c->q[j]);
+    }
+    memset(c->sk, 0, sizeof(double) * 2 * (size_t)c->n_k);
+    for (int i = 0; i < c->n_bead; i++) sk_add(c, c->x + 3 * i, c->q[i], 1.0, c->sk);
+    ek = sk_energy(c, c->sk);
+    for (int i = 0; i < c->n_bead; i++) es += ew_self(c, c->q[i]);
+    if (c->dipole) ed = ew_dipole(c);
+    c->dipl_cur = ed;
+  }
+  if (c->use_bond)
+    for (int m = 0; m < c->n_mol; m++) {
+      c->bond_mol[m] = bond_mol_energy(c, m, c->x);
+      eb += c->bond_mol[m];
+    }
+  if (c->use_ext)
+    for (int i = 0; i < c->n_bead; i++) ee += wall_energy(c, c->x[3 * i + 2], c->type[i]);
+  c->e_pair = ep;
+  c->e_ewald = er + ek + es + ed;
+  c->e_bond = eb;
+  c->e_ext = ee;
+  if (out) {
+    out[0] = ep, out[1] = c->e_ewald, out[2] = eb, out[3] = ee;
+    out[4] = er, out[5] = ek, out[6] = es, out[7] = ed;
+  }
+}
+
+void po_energies(const po_ctx* c, double* out) {
+  out[0] = c->e_pair, out[1] = c->e_ewald, out[2] = c->e_bond, out[3] = c->e_ext;
+}
+
+/* ----------------------------------------------------- energy difference */
+typedef struct {
+  double de, pair, ewald, bond, ext, dip_trial, bond_trial;
+  double* dsk;
+} de_t;
+
+/* ForceField::EnergyDifference (force_field.cc:407-434) for molecule m with
+ * trial coordinates c->t and flags mv (indexed by bead). */
+static void energy_difference(po_ctx* c, int m, const int* mv, de_t* d) {
+  int b0 = c->mol_start[m], b1 = c->mol_start[m + 1];
+  d->pair = d->ewald = d->bond = d->ext = 0;
+  d->de = 0;
+  if (c->use_pair) {
+    double de = 0;
+    /* potential_pair.cc:152-201 */
+    for (int i = b0; i < b1 - 1; i++)
+      for (int j = i + 1; j < b1; j++)
+        if (mv[i] || mv[j])
+          de += lj_pair(c, c->t + 3 * i, c->type[i], c->t + 3 * j, c->type[j]) -
+                lj_pair(c, c->x + 3 * i, c->type[i], c->x + 3 * j, c->type[j]);
+    for (int o = 0; o < c->n_mol; o++) {
+      if (o == m) continue;
+      for (int j = c->mol_start[o]; j < c->mol_start[o + 1]; j++)
+        for (int k = b0; k < b1; k++)
+          if (mv[k])
+            de += lj_pair(c, c->t + 3 * k, c->type[k], c->x + 3 * j, c->type[j]) -
+                  lj_pair(c, c->x + 3 * k, c->type[k], c->x + 3 * j, c->type[j]);
+    }
+    d->pair = de;
+    d->de += de;
+    if (d->de >= K_VERY_LARGE) return;
+  }
+  if (c->use_ext) {
+    /* potential_external.cc:100-117 */
+    double de = 0;
+    for (int i = b0; i < b1; i++) {
+      if (!mv[i]) continue;
+      double en = wall_energy(c, c->t[3 * i + 2], c->type[i]);
+      if (en >= K_VERY_LARGE) {
+        de = K_VERY_LARGE;
+        break;
+      }
+      de += en - wall_energy(c, c->x[3 * i + 2], c->type[i]);
+    }
+    d->ext = de;
+    d->de += de;
+    if (d->de >= K_VERY_LARGE) return;
+  }
+  if (c->use_ewald) {
+    /* potential_ewald.cc:429-535: real space pairwise (the i == j terms cancel
+     * exactly), reciprocal space through S(k), self energy unchanged, dipole
+     * from the current z (the reference evaluates DipoleE before commit). */
+    double de = 0;
+    for (int i = b0; i < b1; i++)
+      for (int j = i + 1; j < b1; j++)
+        if (mv[i] || mv[j])
+          de += ew_real_pair(c, c->t + 3 * i, c->q[i], c->t + 3 * j, c->q[j]) -
+                ew_real_pair(c, c->x + 3 * i, c->q[i], c->x + 3 * j, c->q[j]);
+    for (int o = 0; o < c->n_mol; o++) {
+      if (o == m) continue;
+      for (int j = c->mol_start[o]; j < c->mol_start[o + 1]; j++)
+        for (int k = b0; k < b1; k++)
+          if (mv[k])
+            de += ew_real_pair(c, c->t + 3 * k, c->q[k], c->x + 3 * j, c->q[j]) -
+                  ew_real_pair(c, c->x + 3 * k, c->q[k], c->x + 3 * j, c->q[j]);
+    }
+    memset(d->dsk, 0, sizeof(double) * 2 * (size_t)c->n_k);
+    for (int i = b0; i < b1; i++)
+      if (mv[i] && c->q[i] != 0) {
+        sk_add(c, c->t + 3 * i, c->q[i], 1.0, d->dsk);
+        sk_add(c, c->x + 3 * i, c->q[i], -1.0, d->dsk);
+      }
+    double ek = 0;
+    for (int k = 0; k < c->n_k; k++) {
+      double sr = c->sk[2 * k], si = c->sk[2 * k + 1];
+      double nr = sr + d->dsk[2 * k], ni = si + d->dsk[2 * k + 1];
+      ek += c->kw[k] * ((nr * nr + ni * ni) - (sr * sr + si * si));
+    }
+    de += c->kpref * ek;
+    if (c->dipole) {
+      d->dip_trial = ew_dipole(c);
+      de += d->dip_trial - c->dipl_cur;
+    }
+    d->ewald = de;
+    d->de += de;
+  }
+  if (c->use_bond) {
+    /* potential_spring.cc:63-80 */
+    if (b1 - b0 > 1) {
+      d->bond_trial = bond_mol_energy(c, m, c->t);
+      d->bond = d->bond_trial - c->bond_mol[m];
+      d->de += d->bond;
+    }
+  }
+}
+
+static void finalize(po_ctx* c, int m, const int* mv, const de_t* d, int accept) {
+  int b0 = c->mol_start[m], b1 = c->mol_start[m + 1];
+  if (accept) {
+    c->e_pair += d->pair;
+    c->e_ext += d->ext;
+    c->e_ewald += d->ewald;
+    c->e_bond += d->bond;
+    if (c->use_ewald) {
+      for (int k = 0; k < 2 * c->n_k; k++) c->sk[k] += d->dsk[k];
+      if (c->dipole) c->dipl_cur = d->dip_trial;
+    }
+    if (c->use_bond && b1 - b0 > 1) c->bond_mol[m] = d->bond_trial;
+    memcpy(c->x + 3 * b0, c->t + 3 * b0, sizeof(double) * 3 * (size_t)(b1 - b0));
+  } else {
+    memcpy(c->t + 3 * b0, c->x + 3 * b0, sizeof(double) * 3 * (size_t)(b1 - b0));
+  }
+  (void)mv;
+}
+
+void po_delta_energy(po_ctx* c, int mol, const double* trial, const int* moved,
+                     double* out) {
+  int b0 = c->mol_start[mol], b1 = c->mol_start[mol + 1];
+  int* mv = (int*)calloc((size_t)c->n_bead, sizeof(int));
+  for (int i = b0; i < b1; i++) {
+    memcpy(c->t + 3 * i, trial + 3 * (i - b0), 3 * sizeof(double));
+    mv[i] = moved[i - b0];
+  }
+  de_t d;
+  memset(&d, 0, sizeof d);
+  d.dsk = (double*)calloc((size_t)2 * (c->n_k > 0 ? c->n_k : 1), sizeof(double));
+  energy_difference(c, mol, mv, &d);
+  out[0] = d.de, out[1] = d.pair, out[2] = d.ewald, out[3] = d.bond, out[4] = d.ext;
+  finalize(c, mol, mv, &d, 0);
+  free(d.dsk);
+  free(mv);
+}
+
+/* ------------------------------------------------------------------ moves */
+/* randSphere (misc.cc:95-109) */
+static void rand_sphere(rng_t* r, double* vec) {
+  double rand_square = 2, r1 = 0, r2 = 0;
+  while (rand_square > 1) {
+    r1 = 1 - 2 * ((double)rng_u32(r) / MT_MAX);
+    r2 = 1 - 2 * ((double)rng_u32(r) / MT_MAX);
+    rand_square = r1 * r1 + r2 * r2;
+    if (r->overrun) return;
+  }
+  double ranh = 2 * sqrt(1 - rand_square);
+  vec[0] = r1 * ranh;
+  vec[1] = r2 * ranh;
+  vec[2] = (1 - 2 * rand_square);
+}
+
+#define TX(i, d) c->t[3 * (i) + (d)]
+#define CX(i, d) c->x[3 * (i) + (d)]
+
+/* Molecule::BeadTranslate (molecule.cc:103-133) */
+static void mv_bead(po_ctx* c, rng_t* r, int b0, int* mv) {
+  double vec[3];
+  rand_sphere(r, vec);
+  double vec_len = sqrt(vec[0] * vec[0] + vec[1] * vec[1] + vec[2] * vec[2]);
+  if (vec_len > 0) vec_len = 3 * c->move_size / vec_len;
+  mv[b0] = 1;
+  for (int i = 0; i < 3; i++) TX(b0, i) = CX(b0, i) + vec_len * vec[i];
+}
+
+/* Molecule::COMTranslate (molecule.cc:135-151) */
+static void mv_com(po_ctx* c, rng_t* r, int b0, int b1, int* mv) {
+  double vec[3];
+  for (int i = 0; i < 3; i++) vec[i] = 0.5 * c->move_size * (double)rng_u32(r) / MT_MAX;
+  for (int i = 0; i < 3; i++)
+    if (rng_u32(r) % 2 == 0) vec[i] = -vec[i];
+  for (int i = b0; i < b1; i++) {
+    for (int j = 0; j < 3; j++) TX(i, j) = CX(i, j) + vec[j];
+    mv[i] = 1;
+  }
+}
+
+/* Molecule::Pivot (molecule.cc:153-237) */
+static void mv_pivot(po_ctx* c, rng_t* r, int b0, int b1, double eq, int vary,
+                     int* mv) {
+  int len = b1 - b0;
+  int pivot = (int)floor(len * (double)rng_u32(r) / MT_MAX);
+  if (pivot == len) pivot--;
+  double s = c->move_size * (double)rng_u32(r) / MT_MAX;
+  for (int i = pivot + 1; i < len; i++) {
+    double vec[3];
+    rand_sphere(r, vec);
+    int bi = b0 + i, bp = b0 + i - 1;
+    double x = TX(bi, 0) + s * vec[0];
+    double y = TX(bi, 1) + s * vec[1];
+    double z = TX(bi, 2) + s * vec[2];
+    double dx = x - TX(bp, 0), dy = y - TX(bp, 1), dz = z - TX(bp, 2);
+    double bl = eq;
+    if (vary) bl += (eq / 5.0) * ((double)rng_u32(r) / MT_MAX - 0.5);
+    double norm = bl / sqrt(dx * dx + dy * dy + dz * dz);
+    double cx = norm * dx + TX(bp, 0), cy = norm * dy + TX(bp, 1),
+           cz = norm * dz + TX(bp, 2);
+    double mx = cx - TX(bi, 0), my = cy - TX(bi, 1), mz = cz - TX(bi, 2);
+    for (int j = i; j < len; j++) {
+      TX(b0 + j, 0) = TX(b0 + j, 0) + mx;
+      TX(b0 + j, 1) = TX(b0 + j, 1) + my;
+      TX(b0 + j, 2) = TX(b0 + j, 2) + mz;
+    }
+  }
+  for (int i = pivot - 1; i >= 0; i--) {
+    double vec[3];
+    rand_sphere(r, vec);
+    int bi = b0 + i, bp = b0 + i + 1;
+    double x = TX(bi, 0) + s * vec[0];
+    double y = TX(bi, 1) + s * vec[1];
+    double z = TX(bi, 2) + s * vec[2];
+    double dx = x - TX(bp, 0), dy = y - TX(bp, 1), dz = z - TX(bp, 2);
+    double bl = eq;
+    if (vary) bl += (eq / 5.0) * ((double)rng_u32(r) / MT_MAX - 0.5);
+    double norm = bl / sqrt(dx * dx + dy * dy + dz * dz);
+    double cx = norm * dx + TX(bp, 0), cy = norm * dy + TX(bp, 1),
+           cz = norm * dz + TX(bp, 2);
+    double mx = cx - TX(bi, 0), my = cy - TX(bi, 1), mz = cz - TX(bi, 2);
+    for (int j = i; j >= 0; j--) {
+      TX(b0 + j, 0) = TX(b0 + j, 0) + mx;
+      TX(b0 + j, 1) = TX(b0 + j, 1) + my;
+      TX(b0 + j, 2) = TX(b0 + j, 2) + mz;
+    }
+  }
+  for (int i = b0; i < b1; i++) mv[i] = 1;
+}
+
+/* Molecule::Crankshaft (molecule.cc:239-265). The rotation is Rodrigues'
+ * formula in the per-entry grouping of Eigen's AngleAxis::toRotationMatrix. */
+static void mv_crank(po_ctx* c, rng_t* r, int b0, int b1, int* mv) {
+  int len = b1 - b0;
+  int first = (int)floor((len - 2) * (double)rng_u32(r) / MT_MAX);
+  int last = (int)floor((len - first) * (double)rng_u32(r) / MT_MAX) + first;
+  if (last > len - 1) last = len - 1; /* the reference reads past the chain here */
+  double ax[3];
+  for (int i = 0; i < 3; i++) ax[i] = CX(b0 + last, i) - CX(b0 + first, i);
+  double z = ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2];
+  if (z > 0) {
+    double n = sqrt(z);
+    for (int i = 0; i < 3; i++) ax[i] /= n;
+  }
+  double angle = c->move_size * ((double)rng_u32(r) / MT_MAX * 2 * M_PI_LIBM - M_PI_LIBM);
+  double sn = sin(angle), cs = cos(angle);
+  double sa[3] = {sn * ax[0], sn * ax[1], sn * ax[2]};
+  double ca[3] = {(1.0 - cs) * ax[0], (1.0 - cs) * ax[1], (1.0 - cs) * ax[2]};
+  double R[3][3];
+  double tt = ca[0] * ax[1];
+  R[0][1] = tt - sa[2];
+  R[1][0] = tt + sa[2];
+  tt = ca[0] * ax[2];
+  R[0][2] = tt + sa[1];
+  R[2][0] = tt - sa[1];
+  tt = ca[1] * ax[2];
+  R[1][2] = tt - sa[0];
+  R[2][1] = tt + sa[0];
+  for (int i = 0; i < 3; i++) R[i][i] = ca[i] * ax[i] + cs;
+  for (int i = first + 1; i < last; i++) {
+    int bi = b0 + i;
+    mv[bi] = 1;
+    double v[3];
+    for (int k = 0; k < 3; k++) v[k] = CX(bi, k) - CX(b0 + first, k);
+    for (int k = 0; k < 3; k++)
+      TX(bi, k) = ((R[k][0] * v[0] + R[k][1] * v[1]) + R[k][2] * v[2]) + CX(b0 + first, k);
+  }
+}
+
+/* Molecule::RandomReptation (molecule.cc:267-312) */
+static void mv_rept(po_ctx* c, rng_t* r, int b0, int b1, double eq, int vary,
+                    int* mv) {
+  int len = b1 - b0;
+  double bl = eq;
+  if (vary) bl += (eq / 5.0) * ((double)rng_u32(r) / MT_MAX - 0.5);
+  int dir = 1, begin = 0, end = len - 1;
+  if (rng_u32(r) % 2 == 0) {
+    dir = -1;
+    begin = len - 1;
+    end = 0;
+  }
+  for (int i = begin; i != end; i += dir)
+    for (int j = 0; j < 3; j++) TX(b0 + i, j) = CX(b0 + i + dir, j);
+  double vec[3];
+  rand_sphere(r, vec);
+  double vl = sqrt(vec[0] * vec[0] + vec[1] * vec[1] + vec[2] * vec[2]);
+  for (int i = 0; i < 3; i++) TX(b0 + end, i) = CX(b0 + end, i) + bl * vec[i] / vl;
+  for (int i = b0; i < b1; i++) mv[i] = 1;
+}
+
+/* Simulation::TranslationalMove (simulation.cc:241-355). Returns the move
+ * type attempted (-1 if none); *acc receives the decision. */
+static int translational_move(po_ctx* c, rng_t* r, int* mv, de_t* d, int* acc) {
+  *acc = 0;
+  if (c->n_mol - c->phantom <= 0) return -1;
+  int n_ch = c->grafted + c->n_chain;
+  int n_io = c->n_cion + c->n_aion + c->n_nion;
+  int chain_id = -1, ion_id = -1;
+  int which_chain = (int)floor((double)rng_u32(r) / MT_MAX * n_ch);
+  int which_ion = (int)floor((double)rng_u32(r) / MT_MAX * n_io);
+  if (which_chain == n_ch) which_chain--;
+  if (which_ion == n_io) which_ion--;
+  int ccount = -1, icount = -1;
+  for (int i = c->phantom; i < c->n_mol; i++) {
+    if (c->mol_start[i + 1] - c->mol_start[i] > 1)
+      ccount++;
+    else
+      icount++;
+    if (ccount == which_chain) {
+      chain_id = i;
+      which_chain = -2;
+    }
+    if (icount == which_ion) {
+      ion_id = i;
+      which_ion = -2;
+    }
+  }
+  int move_type = 0;
+  double u = (double)rng_u32(r) / MT_MAX;
+  double cur = c->move_prob[0];
+  while (cur < u && move_type < K_NO_MOVE_TYPE - 1) {
+    move_type++;
+    cur += c->move_prob[move_type];
+  }
+  if (cur < u) move_type++;
+  if (move_type >= K_NO_MOVE_TYPE) move_type = K_NO_MOVE_TYPE - 1;
+  int mol = -1;
+  if (move_type == 0 && n_io > 0) {
+    mol = ion_id;
+    mv_bead(c, r, c->mol_start[mol], mv);
+  } else if (n_ch > 0) {
+    mol = chain_id;
+    double bl = 0;
+    int vary = 0;
+    if (c->use_rigid) bl = c->rigid;
+    if (c->use_bond) {
+      bl = c->r0;
+      vary = 1;
+    }
+    int b0 = c->mol_start[mol], b1 = c->mol_start[mol + 1];
+    switch (move_type) {
+      case 1: mv_com(c, r, b0, b1, mv); break;
+      case 2: mv_pivot(c, r, b0, b1, bl, vary, mv); break;
+      case 3: mv_crank(c, r, b0, b1, mv); break;
+      case 4: mv_rept(c, r, b0, b1, bl, vary, mv); break;
+    }
+  }
+  if (!((move_type == 0 && n_io > 0) || (move_type > 0 && n_ch > 0))) return -1;
+  if (r->overrun) return -1;
+  energy_difference(c, mol, mv, d);
+  int accept = 0;
+  if (d->de < K_VERY_LARGE) accept = ((double)rng_u32(r) / MT_MAX < exp(-c->beta * d->de));
+  finalize(c, mol, mv, d, accept);
+  for (int i = c->mol_start[mol]; i < c->mol_start[mol + 1]; i++) mv[i] = 0;
+  *acc = accept;
+  return move_type;
+}
+
+static long run_loop(po_ctx* c, rng_t* r, int n, int* move_type, int* accept,
+                     int* draws, double* etot) {
+  int* mv = (int*)calloc((size_t)c->n_bead, sizeof(int));
+  de_t d;
+  memset(&d, 0, sizeof d);
+  d.dsk = (double*)calloc((size_t)2 * (c->n_k > 0 ? c->n_k : 1), sizeof(double));
+  for (int s = 0; s < n; s++) {
+    long p0 = r->pos;
+    (void)rng_u32(r); /* simulation.cc:221 */
+    int acc = 0;
+    int mt = translational_move(c, r, mv, &d, &acc);
+    if (r->overrun) break;
+    if (move_type) move_type[s] = mt;
+    if (accept) accept[s] = acc;
+    if (draws) draws[s] = (int)(r->pos - p0);
+    if (etot) etot[s] = c->e_pair + c->e_ewald + c->e_bond + c->e_ext;
+  }
+  free(d.dsk);
+  free(mv);
+  return r->overrun ? -1 : r->pos;
+}
+
+int po_run(po_ctx* c, int n, int* move_type, int* accept, int* draws,
+           double* etot) {
+  rng_t r = {&c->g, NULL, 0, 0, 0};
+  run_loop(c, &r, n, move_type, accept, draws, etot);
+  return n;
+}
+
+long po_run_stream(po_ctx* c, int n, const uint32_t* stream, long n_stream,
+                   int* move_type, int* accept, double* etot) {
+  rng_t r = {NULL, stream, n_stream, 0, 0};
+  return run_loop(c, &r, n, move_type, accept, NULL, etot);
+}
+
+void po_coords(const po_ctx* c, double* out) {
+  memcpy(out, c->x, sizeof(double) * 3 * (size_t)c->n_bead);
+}
+
+void po_set_coords(po_ctx* c, const double* xyz) {
+  memcpy(c->x, xyz, sizeof(double) * 3 * (size_t)c->n_bead);
+  memcpy(c->t, xyz, sizeof(double) * 3 * (size_t)c->n_bead);
+  po_total_energy(c, NULL);
+}
+
+/* RadiusOfGyration / RadiusOfGyrationXYZ / EndToEndDistance
+ * (simulation.cc:406-500). */
+void po_observables(const po_ctx* c, double* out) {
+  double rg = 0, rx = 0, ry = 0, rz = 0, ete = 0;
+  for (int m = 0; m < c->n_mol; m++) {
+    int b0 = c->mol_start[m], n = c->mol_start[m + 1] - b0;
+    if (n <= 1) continue;
+    double g = 0, gx = 0, gy = 0, gz = 0;
+    for (int j = 0; j < n - 1; j++)
+      for (int k = j + 1; k < n; k++) {
+        double r = bbdist(c->x + 3 * (b0 + j), c->x + 3 * (b0 + k), c->box, 0);
+        g += r * r;
+        double x = fabs(CX(b0 + j, 0) - CX(b0 + k, 0));
+        double y = fabs(CX(b0 + j, 1) - CX(b0 + k, 1));
+        double z = fabs(CX(b0 + j, 2) - CX(b0 + k, 2));
+        gx += x * x, gy += y * y, gz += z * z;
+      }
+    rg += g / (n * n), rx += gx / (n * n), ry += gy / (n * n), rz += gz / (n * n);
+    double e = bbdist(c->x + 3 * b0, c->x + 3 * (b0 + n - 1), c->box, 0);
+    ete += e * e;
+  }
+  int nc = c->grafted + c->n_chain;
+  if (nc > 0) rg /= nc, rx /= nc, ry /= nc, rz /= nc, ete /= nc;
+  out[0] = rg, out[1] = rx, out[2] = ry, out[3] = rz, out[4] = ete;
+}
+
+/* CalcRhoZ (simulation.cc:1029-1045), one pass on a zeroed histogram. */
+int po_rhoz(const po_ctx* c, double* out, int cap) {
+  double res = 0.02;
+  int nb = (int)ceil(c->box[2] / res);
+  int n = 3 * nb < cap ? 3 * nb : cap;
+  for (int i = 0; i < n; i++) out[i] = 0;
+  for (int m = c->phantom; m < c->n_mol; m++) {
+    int b0 = c->mol_start[m], sz = c->mol_start[m + 1] - b0;
+    int id = sz > 1 ? 0 : (c->q[b0] >= 0 ? 1 : 2);
+    for (int j = b0; j < b0 + sz; j++) {
+      double z = c->x[3 * j + 2];
+      z -= c->box[2] * floor(z / c->box[2]);
+      int bz = (int)floor(z / res);
+      if (bz >= 0 && bz < nb && 3 * bz + id < n)
+        out[3 * bz + id] += 1.0 / (c->box[0] * c->box[1] * res);
+    }
+  }
+  return nb;
+}
