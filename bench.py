@@ -1,0 +1,372 @@
+#!/usr/bin/env python
+"""Benchmark of the Monte Carlo energy-difference hot path on one GB300.
+
+Workload (default ``bulk_20000_pinned``): 100 chains x 100 beads (charge -1)
+plus 10,000 +1 counterions, periodic cube L = 80, LJ eps = sigma = 1 cut at
+2.5, harmonic bonds k = 400 r0 = 1, lB = 3, Ewald alpha = (5.6/L)^2 with the
+real-space cut-off at L/2 and |n| <= 12 per axis (7,812 half-space k-vectors),
+move mix ion 0.3 / COM 0.1 / pivot 0.2 / crankshaft 0.2 / reptation 0.2.
+Seeded synthetic initial configuration (self-avoiding chains, uniform ions,
+no pair closer than 0.8 sigma), written in the reference's input formats.
+
+A "step" is a batch of Monte Carlo moves run on the device. Reported:
+  value        moves/s of the precision form (FP32 pair/k arithmetic, FP64
+               accumulators, FP64 recompute every 1e4 moves), device time
+  plain_fp64   moves/s of the plain FP64 form on the same system
+  e2e          moves/s through the C ABI with host buffers: the recorded
+               mt19937 stream copied in and the per-move logs copied out
+               inside the timed region
+  samples      Rg-decorrelated samples/s (tau_int of the chain-averaged Rg^2
+               series, Sokal window c = 5) when --samples-seconds > 0
+  roofline     FP32 pipe: algorithmic FLOPs per move x moves/s over the FP32
+               FMA peak measured on this GPU by a probe kernel
+  cpu_baseline the FP64 CPU restatement of the reference (the reference
+               itself cannot hold 20,000 particles: O(N^2) std::map storage)
+               on a bounded sample of moves, one core
+
+``--impl reference`` times the reference's CPU path (oracle/_ref where the
+reference compiled, else the CPU restatement) with one process per host core.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MC moves/s and Rg-decorrelated samples/s: plain FP64 vs chosen form, 1 GB300"
+
+
+def mt19937_stream(seed: int, n: int):
+    """std::mt19937 output words for `seed` (classic init_genrand seeding)."""
+    import numpy as np
+    key = np.zeros(624, dtype=np.uint32)
+    x = seed & 0xFFFFFFFF
+    key[0] = x
+    for i in range(1, 624):
+        x = (1812433253 * (x ^ (x >> 30)) + i) & 0xFFFFFFFF
+        key[i] = x
+    bg = np.random.MT19937()
+    bg.state = {"bit_generator": "MT19937", "state": {"key": key, "pos": 624}}
+    return bg.random_raw(n).astype(np.uint32)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        mhz, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                mhz.append(float(r[1]))
+                mx = float(r[2])
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(mhz) if mhz else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def tau_int(x, c=5.0):
+    """Integrated autocorrelation time with Sokal's automatic window."""
+    import numpy as np
+    x = np.asarray(x, dtype=np.float64)
+    n = len(x)
+    if n < 8:
+        return float("nan")
+    x = x - x.mean()
+    f = np.fft.rfft(x, 2 * n)
+    acf = np.fft.irfft(f * np.conj(f))[:n]
+    if acf[0] <= 0:
+        return float("nan")
+    rho = acf / acf[0]
+    tau = 0.5
+    for w in range(1, n):
+        tau += rho[w]
+        if w >= c * tau:
+            break
+    return float(tau)
+
+
+def alg_flops_per_move(n_bead, mean_moved, n_k, frac_in_rc, mean_bonds):
+    """Algorithmic FP32 work per attempted move, with the weights fixed before
+    measuring: 20 per (moved, other) pair for distance and wrap, 8 per image
+    check (one image per pair when r_c = L/2), 25 per in-cut-off erfc term,
+    12 per in-cut-off LJ pair (negligible at these densities), 16 per (moved
+    bead, half-space k) phase pair, 10 per k for the |S|^2 change, 15 per bond.
+    Counted once per pair (new configuration), as the reference's algorithm
+    does; the kernel evaluates both old and new."""
+    pairs = mean_moved * (n_bead - 1)
+    return (pairs * (20 + 8) + pairs * frac_in_rc * 25 + mean_moved * n_k * 16
+            + n_k * 10 + 15 * mean_bonds)
+
+
+def run_reference_arm(args, rank, world):
+    """The reference's CPU path on the host cores: one process per core, each
+    timing a bounded sample of moves on its own copy of the workload."""
+    if rank != 0:
+        return 0
+    from oracle import bindings as ob  # CPU baseline leg only
+    d = make_workload(args.workload)
+    cores = max(1, min(os.cpu_count() or 1, 16))
+    moves = args.ref_moves
+    code = (
+        "import sys,time; sys.path.insert(0,%r)\n"
+        "from oracle import bindings as ob\n"
+        "o=ob.Oracle(%r, seed=int(sys.argv[1]), fast_init=True)\n"
+        "t=time.time(); o.run(%d); print(time.time()-t)\n" % (ROOT, d, moves))
+    steps = []
+    for s in range(args.warmup + args.steps):
+        procs = [subprocess.Popen([sys.executable, "-c", code, str(1000 + s * 97 + p)],
+                                  stdout=subprocess.PIPE, text=True) for p in range(cores)]
+        t = [float(p.communicate()[0].strip().splitlines()[-1]) for p in procs]
+        if s >= args.warmup:
+            steps.append(cores * moves / max(t))
+    v = statistics.mean(steps)
+    kind = "reference" if ob.have_ref() else "port"
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "moves/s",
+            "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": args.workload, "moves_per_step": moves * cores,
+                       "note": "the reference cannot hold this system; the FP64 CPU "
+                               "restatement of its algorithm is timed"},
+            "cpu_baseline": {"value": v, "unit": "moves/s", "cores": cores, "kind": kind,
+                             "sample": "%d moves per process per step" % moves},
+            "e2e": {"value": v, "unit": "moves/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def make_workload(name):
+    from plum_gb300 import systems
+    d = os.path.join(tempfile.gettempdir(), "plum_bench_" + name)
+    if not os.path.exists(os.path.join(d, "run.in")):
+        systems.write_bulk(d, systems.CONFIGS[name], seed=20261203)
+    return d
+
+
+def cpu_baseline_sample(d, moves):
+    code = ("import sys,time; sys.path.insert(0,%r)\n"
+            "from oracle import bindings as ob\n"
+            "o=ob.Oracle(%r, seed=7, fast_init=True)\n"
+            "t=time.time(); o.run(%d); print(time.time()-t)\n" % (ROOT, d, moves))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
+    t = float(out.stdout.strip().splitlines()[-1])
+    return moves / t
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="bulk_20000_pinned")
+    ap.add_argument("--moves-per-step", type=int, default=2000)
+    ap.add_argument("--plain-moves-per-step", type=int, default=200)
+    ap.add_argument("--samples-seconds", type=float, default=0.0)
+    ap.add_argument("--cpu-moves", type=int, default=20)
+    ap.add_argument("--ref-moves", type=int, default=10)
+    ap.add_argument("--only", default=None, choices=[None, "fp32", "fp64"],
+                    help="profiling runs: time one form only, no baselines or e2e")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference_arm(args, rank, world)
+
+    import numpy as np
+    import torch
+    import plum_gb300 as pg
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    d = make_workload(args.workload)
+    M = args.moves_per_step
+    s32 = pg.System(d, form=pg.FORM_FP32, device=local)
+    s64 = pg.System(d, form=pg.FORM_FP64, device=local)
+    info = s32.info
+    s32.seed(1234 + rank)
+    s64.seed(1234 + rank)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    if args.only:
+        s = s32 if args.only == "fp32" else s64
+        for _ in range(args.warmup + args.steps):
+            s.run(M)
+        torch.cuda.synchronize()
+        ms, k = s.last_timing()
+        print(json.dumps({"profile_run": args.only, "moves_per_step": M, "last_ms": ms,
+                          "moves_per_s": M / (ms / 1e3)}), flush=True)
+        return 0
+
+    for _ in range(args.warmup):
+        s32.run(M)
+        s64.run(args.plain_moves_per_step)
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    dev_ms, kernels = [], 0
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()          # L2 flush between steps (outside the step's events)
+        torch.cuda.synchronize()
+        s32.run(M)
+        ms, k = s32.last_timing()
+        dev_ms.append(ms)
+        kernels += k
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    step_ms = statistics.mean(dev_ms)
+    if dist:
+        t = torch.tensor([step_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms = float(t.item())
+    value = world * M / (step_ms / 1e3)
+
+    # plain FP64 on the same system
+    p_ms = []
+    for _ in range(max(3, args.steps // 2)):
+        s64.run(args.plain_moves_per_step)
+        p_ms.append(s64.last_timing()[0])
+    plain = args.plain_moves_per_step / (statistics.mean(p_ms) / 1e3)
+
+    # e2e through the C ABI with host buffers (stream in, logs out)
+    n_e2e = M
+    words = n_e2e * (24 + 4 * 100)
+    stream = mt19937_stream(99 + rank, words)
+    e2e_t = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        used, mt, ac, et = s32.run_moves(stream, n_e2e)
+        e2e_t.append(time.perf_counter() - t1)
+    e2e = n_e2e / statistics.median(e2e_t)
+    h2d = stream.nbytes
+    d2h = n_e2e * (4 + 4 + 8)
+
+    # algorithmic work per move (mean moved beads from the move mix)
+    prob = (0.3, 0.1, 0.2, 0.2, 0.2)
+    L = 100
+    crank_mean = sum(max(0, ((L - f) * u) // 1 - 1) for f in range(L - 1)
+                     for u in (0.25, 0.5, 0.75)) / (3 * (L - 1))
+    mean_moved = prob[0] * 1 + (prob[1] + prob[2] + prob[4]) * L + prob[3] * crank_mean
+    mean_bonds = (1 - prob[0]) * (L - 1)
+    frac_in = (4.0 / 3.0) * math.pi * info.real_cutoff ** 3 / (info.box[0] ** 3)
+    W = alg_flops_per_move(info.n_bead, mean_moved, info.n_kvec, min(1.0, frac_in), mean_bonds)
+    peak, peak64 = pg.probe_peaks(local)
+    achieved = W * (M / (step_ms / 1e3)) / 1e12
+
+    samples = None
+    if args.samples_seconds > 0:
+        every = 1000
+        rg = []
+        t_end = time.perf_counter() + args.samples_seconds
+        while time.perf_counter() < t_end:
+            s32.run(every)
+            rg.append(s32.observables()[0])
+        tau = tau_int(rg)
+        samples = {"tau_int_samples": tau, "moves_per_sample": every, "n_samples": len(rg),
+                   "fp32_samples_per_s": value / (every * 2 * tau) if tau == tau else None,
+                   "fp64_samples_per_s": plain / (every * 2 * tau) if tau == tau else None}
+
+    cpu = None
+    if rank == 0:
+        try:
+            v = cpu_baseline_sample(d, args.cpu_moves)
+            cpu = {"value": v, "unit": "moves/s", "cores": 1, "kind": "port",
+                   "sample": "%d moves of the FP64 CPU restatement on this workload "
+                             "(the reference cannot hold 20,000 particles)" % args.cpu_moves}
+        except Exception as e:  # noqa: BLE001
+            cpu = {"value": None, "unit": "moves/s", "cores": 1, "kind": "port",
+                   "sample": "failed: %s" % e}
+
+    drift = s32.drift()
+    line = {
+        "metric": METRIC, "value": value, "unit": "moves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": args.workload, "n_bead": info.n_bead, "n_kvec_half": info.n_kvec,
+                   "real_cutoff": info.real_cutoff, "moves_per_step": M,
+                   "form": "precision (FP32 pair/k, FP64 S(k) and totals)",
+                   "l2": "flushed between steps (256 MB write)", "parallelism": "replicas"},
+        "plain_fp64": {"value": plain, "unit": "moves/s",
+                       "moves_per_step": args.plain_moves_per_step},
+        "speedup_vs_plain_fp64": value / plain,
+        "e2e": {"value": e2e, "unit": "moves/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(kernels),
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": "FP32 FMA probe kernel on this GPU (measured; the "
+                                    "measured-peaks file has no FP32 entry)",
+                     "fp64_peak_tflops": peak64,
+                     "alg_flops_per_move": W},
+        "samples": samples,
+        "drift_fp32": {"last": list(drift[:4]), "max_abs_total": drift[4]},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "wall_s": wall,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

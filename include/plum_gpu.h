@@ -1,0 +1,151 @@
+/* plum_gpu.h -- C ABI of the GB300 Monte Carlo energy engine.
+ *
+ * One context holds one system (or a batch of replicas) resident on one GPU:
+ * bead positions, charges and types, the Ewald structure factor S(k), and the
+ * running energy totals. Every entry point takes plain pointers and sizes;
+ * host buffers are copied in and out by the call.
+ *
+ * The reference (nuwapi/Plum) has no FFI: its hot path sits behind C++ class
+ * methods called by Simulation. Each entry point below replaces one of those
+ * methods (file:line in the reference's src/ tree); the C++ host classes in
+ * plum_gb300/csrc/host/ keep the reference's method names and call these.
+ *
+ * Error convention: every call returns PLUM_OK (0) or a PLUM_ERR_* code;
+ * plum_last_error() returns a message for the calling thread. The reference
+ * exits the process on bad input (e.g. simulation.cc:142-156, 594-597); this
+ * library returns PLUM_ERR_INPUT instead. Energies keep the reference's 1e8
+ * overlap sentinel (utilities/constants.h:15) and its "no Metropolis draw when
+ * dE >= 1e8" rule (simulation.cc:327-332).
+ *
+ * Threading: a context binds one CUDA stream; calls on one context must not
+ * overlap. Distinct contexts are independent.
+ */
+#ifndef PLUM_GPU_H_
+#define PLUM_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PLUM_OK 0
+#define PLUM_ERR_INPUT 1     /* malformed or unsupported input */
+#define PLUM_ERR_CUDA 2      /* a CUDA call failed */
+#define PLUM_ERR_TIMEOUT 3   /* a device-side bounded wait gave up */
+#define PLUM_ERR_NONFINITE 4 /* NaN/Inf energy detected on the device */
+#define PLUM_ERR_STATE 5     /* call out of order (e.g. finalize without delta) */
+#define PLUM_ERR_STREAM 6    /* recorded random stream exhausted */
+
+/* Arithmetic of the pair and k-space sums. */
+#define PLUM_FORM_FP64 0 /* plain form: FP64 everywhere (the drop-in) */
+#define PLUM_FORM_FP32 1 /* precision form: FP32 pair/k arithmetic, FP64
+                            S(k) and energy accumulators */
+
+typedef struct plum_ctx plum_ctx;
+
+typedef struct {
+  int n_bead, n_mol, n_type, n_kvec; /* n_kvec: half-space k-vectors */
+  int npbc, form;
+  double box[3];      /* simulation box */
+  double ewald_box[3]; /* Ewald box (z padded when the dipole correction is on) */
+  double real_cutoff, kcut2, alpha, lB;
+  int real_cell[3], k_cell[3];
+} plum_info;
+
+/* Message for the last failing call on this thread ("" if none). */
+const char* plum_last_error(void);
+
+/* Creates a context from the reference's own inputs: `runin` (relative to
+ * `dir`) in the positional grammar of simulation.cc:30-50 and
+ * force_field.cc:64-195, plus the coordinate and topology files it names
+ * (simulation.cc:582-646). Replaces Simulation::Simulation's reading and
+ * ForceField::Initialize + InitializeEnergy (force_field.cc:46-405).
+ * The total energy is computed on the device before returning. */
+int plum_ctx_create(const char* dir, const char* runin, int form, int device,
+                    plum_ctx** out);
+int plum_ctx_destroy(plum_ctx* ctx);
+int plum_ctx_info(const plum_ctx* ctx, plum_info* out);
+
+/* Recomputes every energy term of the current configuration from scratch on
+ * the device in FP64 and resets the running totals and S(k) to it.
+ * out[8] = {pair, ewald, bond, ext, ewald_real, ewald_recip, ewald_self,
+ * ewald_dipole}. Replaces ForceField::InitializeEnergy
+ * (force_field.cc:365-405) and the potentials' EnergyInitialization
+ * (potential_pair.cc:55-100, potential_ewald.cc:176-231,
+ * potential_bond.cc:16-27, potential_external.cc:48-61). */
+int plum_total_energy(plum_ctx* ctx, double* out);
+
+/* Running totals out[4] = {pair, ewald, bond, ext}. Replaces
+ * ForceField::TotPairEnergy/TotEwaldEnergy/TotBondEnergy/TotExtEnergy
+ * (force_field.cc:1201-1219). */
+int plum_energies(const plum_ctx* ctx, double* out);
+
+/* Energy difference of a trial configuration of molecule `mol`:
+ * trial_xyz[size*3] and moved[size] (host buffers, the molecule's beads in
+ * order). out[5] = {dE, dE_pair, dE_ewald, dE_bond, dE_ext}. The trial is
+ * kept pending until plum_finalize. Replaces ForceField::EnergyDifference
+ * (force_field.cc:407-434). */
+int plum_delta_energy(plum_ctx* ctx, int mol, const double* trial_xyz,
+                      const int* moved, double* out);
+
+/* Accepts (commit trial, update S(k) and totals) or rejects the pending
+ * trial. Replaces ForceField::FinalizeEnergies (force_field.cc:436-451) plus
+ * the coordinate update of Simulation::TranslationalMove
+ * (simulation.cc:336-351). */
+int plum_finalize(plum_ctx* ctx, int accept);
+
+/* Runs `n_moves` Monte Carlo steps entirely on the device: per step one draw
+ * for the grand-canonical check (simulation.cc:221), molecule and move-type
+ * choice, the trial move, dE and the Metropolis test, consuming the recorded
+ * mt19937 output `stream[n_stream]` (host buffer) in the reference's draw
+ * order. Replaces Simulation::Run's translational branch
+ * (simulation.cc:216-355) with the Molecule moves (molecule.cc:103-312).
+ * Optional per-step logs (host buffers of n_moves, may be NULL): move type
+ * (0..4, -1 none), accept flag, total energy after the step.
+ * *draws_used receives the number of stream words consumed. */
+int plum_run_moves(plum_ctx* ctx, const uint32_t* stream, long n_stream,
+                   int n_moves, int* move_type, int* accept, double* etot,
+                   long* draws_used);
+
+/* Same loop with the mt19937 stream generated on the device from `seed`
+ * (std::mt19937 semantics) instead of a host buffer: the throughput path.
+ * Continues the device generator across calls; plum_seed resets it. */
+int plum_seed(plum_ctx* ctx, uint32_t seed);
+int plum_run(plum_ctx* ctx, int n_moves, int* accepted_out);
+
+/* Current coordinates, n_bead*3 doubles (host buffer), molecule order. */
+int plum_get_positions(const plum_ctx* ctx, double* xyz);
+/* Replaces the current coordinates (n_bead*3) and recomputes the energy. */
+int plum_set_positions(plum_ctx* ctx, const double* xyz);
+
+/* out[5] = {Rg^2 averaged over chains, Rg_x^2, Rg_y^2, Rg_z^2, end-to-end^2}
+ * of the current configuration. Replaces Simulation::RadiusOfGyration,
+ * RadiusOfGyrationXYZ and EndToEndDistance (simulation.cc:406-500). */
+int plum_observables(const plum_ctx* ctx, double* out);
+
+/* Full FP64 recompute cadence of plum_run, in moves (0 = never). The
+ * precision form defaults to 10000: every 10^4 moves (at the next batch
+ * boundary of 256) the totals, S(k) and the fixed-point mirror are rebuilt
+ * from the FP64 positions, which resets FP32 drift. No reference counterpart
+ * (the reference never recomputes, force_field.cc:1201-1219). */
+int plum_set_recompute(plum_ctx* ctx, long every);
+/* Drift found at the last recompute: out[5] = {pair, ewald, bond, ext}
+ * running-minus-recomputed, and the largest |total drift| seen so far. */
+int plum_drift(const plum_ctx* ctx, double* out);
+
+/* Measured duration (ms) of the last plum_run/plum_run_moves call's device
+ * work, and the number of kernels it launched. */
+int plum_last_timing(const plum_ctx* ctx, double* ms, long* kernels);
+
+/* Measures the FP32 and FP64 FMA throughput of `device` (TFLOP/s, an FMA
+ * counted as 2 FLOPs) with a short probe kernel: the roofline denominator of
+ * the pair and k-space kernels, which run on the FP32/FP64 pipes rather than
+ * the tensor cores. No reference counterpart. */
+int plum_probe_peaks(int device, double* fp32_tflops, double* fp64_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -100,6 +100,7 @@ def _load_oracle():
         L.po_rhoz.argtypes = [C.c_void_p, _dp, C.c_int]
         L.po_rhoz.restype = C.c_int
         L.po_mt19937.argtypes = [C.c_uint32, C.c_long, _up]
+        L.po_set_fast_init.argtypes = [C.c_int]
         _orc_lib = L
     return _orc_lib
 
@@ -190,10 +191,13 @@ class Ref(_Base):
 class Oracle(_Base):
     """The FP64 CPU restatement (oracle/_ref/liboracle.so)."""
 
-    def __init__(self, dirpath: str, runin: str = "run.in", seed: int = 1):
+    def __init__(self, dirpath: str, runin: str = "run.in", seed: int = 1,
+                 fast_init: bool = False):
         self.L = _load_oracle()
         err = C.create_string_buffer(512)
+        self.L.po_set_fast_init(int(fast_init))
         self.h = self.L.po_create(dirpath.encode(), runin.encode(), seed, err, 512)
+        self.L.po_set_fast_init(0)
         if not self.h:
             raise ValueError(err.value.decode())
         self.n_bead = self.L.po_n_bead(self.h)

@@ -496,6 +496,10 @@ static void update_counts(po_ctx* c) {
 }
 
 /* ------------------------------------------------------------- creation */
+static int g_skip_pair_totals = 0;
+
+void po_set_fast_init(int on) { g_skip_pair_totals = on; }
+
 po_ctx* po_create(const char* dir, const char* runin, uint32_t seed, char* err,
                   int cap) {
   po_ctx* c = (po_ctx*)calloc(1, sizeof(po_ctx));
@@ -718,7 +722,8 @@ static int mol_of(const po_ctx* c, int bead) {
  * (intramolecular first, then molecule pairs), potential_pair.cc:55-100. */
 void po_total_energy(po_ctx* c, double* out) {
   double ep = 0, er = 0, ek = 0, es = 0, ed = 0, eb = 0, ee = 0;
-  if (c->use_pair) {
+  const int skip = g_skip_pair_totals;
+  if (c->use_pair && !skip) {
     for (int m = 0; m < c->n_mol; m++)
       for (int j = c->mol_start[m]; j < c->mol_start[m + 1] - 1; j++)
         for (int k = j + 1; k < c->mol_start[m + 1]; k++)
@@ -729,7 +734,7 @@ void po_total_energy(po_ctx* c, double* out) {
           ep += lj_pair(c, c->x + 3 * i, c->type[i], c->x + 3 * j, c->type[j]);
   }
   if (c->use_ewald) {
-    for (int i = 0; i < c->n_bead; i++) {
+    for (int i = 0; i < c->n_bead && !skip; i++) {
       er += 0.5 * ew_real_pair(c, c->x + 3 * i, c->q[i], c->x + 3 * i, c->q[i]);
       for (int j = i + 1; j < c->n_bead; j++)
         er += ew_real_pair(c, c->x + 3 * i, c->q[i], c->x + 3 * j, c->q[j]);
@@ -1107,7 +1112,8 @@ static int translational_move(po_ctx* c, rng_t* r, int* mv, de_t* d, int* acc) {
   if (r->overrun) return -1;
   energy_difference(c, mol, mv, d);
   int accept = 0;
-  if (d->de < K_VERY_LARGE) accept = ((double)rng_u32(r) / MT_MAX < exp(-c->beta * d->de));
+  /* simulation.cc:327-332: no draw only when dE >= 1e8 (a NaN dE still draws) */
+  if (!(d->de >= K_VERY_LARGE)) accept = ((double)rng_u32(r) / MT_MAX < exp(-c->beta * d->de));
   finalize(c, mol, mv, d, accept);
   for (int i = c->mol_start[mol]; i < c->mol_start[mol + 1]; i++) mv[i] = 0;
   *acc = accept;

@@ -37,6 +37,10 @@ typedef struct po_ctx po_ctx;
 po_ctx* po_create(const char* dir, const char* runin, uint32_t seed, char* err,
                   int cap);
 void po_destroy(po_ctx* c);
+/* When on, po_create skips the O(N^2) pair and real-space totals (their
+ * running values start at 0); S(k), bonds, walls and self terms are still
+ * built. For timing moves on systems too large for an all-pairs sum. */
+void po_set_fast_init(int on);
 
 int po_n_bead(const po_ctx* c);
 int po_n_mol(const po_ctx* c);

@@ -1,0 +1,186 @@
+"""GB300 Monte Carlo energy engine for Plum-format polyelectrolyte systems.
+
+The compute path is the CUDA library ``plum_gb300/_lib/libplumgpu.so`` (built
+from ``plum_gb300/csrc`` for sm_103a). This module is a thin ctypes layer over
+its C ABI (``include/plum_gpu.h``); it has no CPU implementation of any
+energy term and raises if the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libplumgpu.so")
+
+PLUM_OK = 0
+FORM_FP64 = 0
+FORM_FP32 = 1
+ERRORS = {1: "input", 2: "cuda", 3: "timeout", 4: "nonfinite", 5: "state", 6: "stream"}
+
+_lib = None
+
+
+class PlumError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s error (%d): %s" % (ERRORS.get(code, "unknown"), code, msg))
+        self.code = code
+
+
+class Info(C.Structure):
+    _fields_ = [("n_bead", C.c_int), ("n_mol", C.c_int), ("n_type", C.c_int),
+                ("n_kvec", C.c_int), ("npbc", C.c_int), ("form", C.c_int),
+                ("box", C.c_double * 3), ("ewald_box", C.c_double * 3),
+                ("real_cutoff", C.c_double), ("kcut2", C.c_double),
+                ("alpha", C.c_double), ("lB", C.c_double),
+                ("real_cell", C.c_int * 3), ("k_cell", C.c_int * 3)]
+
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_up = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+
+
+def lib():
+    """Loads the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("plum_gb300 CUDA library not built: %s (run __graft_entry__.build())"
+                              % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        L.plum_last_error.restype = C.c_char_p
+        L.plum_ctx_create.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int,
+                                      C.POINTER(C.c_void_p)]
+        L.plum_ctx_destroy.argtypes = [C.c_void_p]
+        L.plum_ctx_info.argtypes = [C.c_void_p, C.POINTER(Info)]
+        L.plum_total_energy.argtypes = [C.c_void_p, _dp]
+        L.plum_energies.argtypes = [C.c_void_p, _dp]
+        L.plum_delta_energy.argtypes = [C.c_void_p, C.c_int, _dp, _ip, _dp]
+        L.plum_finalize.argtypes = [C.c_void_p, C.c_int]
+        L.plum_run_moves.argtypes = [C.c_void_p, _up, C.c_long, C.c_int, C.c_void_p,
+                                     C.c_void_p, C.c_void_p, C.POINTER(C.c_long)]
+        L.plum_seed.argtypes = [C.c_void_p, C.c_uint32]
+        L.plum_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
+        L.plum_get_positions.argtypes = [C.c_void_p, _dp]
+        L.plum_set_positions.argtypes = [C.c_void_p, _dp]
+        L.plum_observables.argtypes = [C.c_void_p, _dp]
+        L.plum_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_long)]
+        L.plum_set_recompute.argtypes = [C.c_void_p, C.c_long]
+        L.plum_drift.argtypes = [C.c_void_p, _dp]
+        L.plum_probe_peaks.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _lib = L
+    return _lib
+
+
+def probe_peaks(device: int = 0):
+    """Measured (FP32, FP64) FMA throughput of the GPU in TFLOP/s."""
+    a, b = C.c_double(0), C.c_double(0)
+    _check(lib().plum_probe_peaks(device, C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
+def _check(rc):
+    if rc != PLUM_OK:
+        raise PlumError(rc, lib().plum_last_error().decode())
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class System:
+    """One system resident on a GPU, read from the reference's input files.
+
+    Mirrors the reference's ForceField energy surface: ``total_energy``
+    (InitializeEnergy), ``energies`` (Tot*Energy), ``energy_difference``
+    (EnergyDifference) and ``finalize`` (FinalizeEnergies)."""
+
+    def __init__(self, dirpath: str, runin: str = "run.in", form: int = FORM_FP64,
+                 device: int = 0):
+        L = lib()
+        h = C.c_void_p()
+        _check(L.plum_ctx_create(dirpath.encode(), runin.encode(), form, device, C.byref(h)))
+        self.h = h
+        info = Info()
+        _check(L.plum_ctx_info(self.h, C.byref(info)))
+        self.info = info
+        self.n_bead = info.n_bead
+        self.n_mol = info.n_mol
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().plum_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def total_energy(self):
+        o = np.zeros(8)
+        _check(lib().plum_total_energy(self.h, o))
+        return o
+
+    def energies(self):
+        o = np.zeros(4)
+        _check(lib().plum_energies(self.h, o))
+        return o
+
+    def energy_difference(self, mol, trial, moved):
+        o = np.zeros(5)
+        _check(lib().plum_delta_energy(self.h, mol,
+                                       np.ascontiguousarray(trial, np.float64).ravel(),
+                                       np.ascontiguousarray(moved, np.int32), o))
+        return o
+
+    def finalize(self, accept: bool):
+        _check(lib().plum_finalize(self.h, int(bool(accept))))
+
+    def run_moves(self, stream, n_moves, logs=True):
+        """Runs n_moves steps on the device consuming a recorded mt19937 stream."""
+        s = np.ascontiguousarray(stream, np.uint32)
+        mt = np.zeros(n_moves, np.int32) if logs else None
+        ac = np.zeros(n_moves, np.int32) if logs else None
+        et = np.zeros(n_moves, np.float64) if logs else None
+        used = C.c_long(0)
+        _check(lib().plum_run_moves(self.h, s, len(s), n_moves, _ptr(mt), _ptr(ac), _ptr(et),
+                                    C.byref(used)))
+        return used.value, mt, ac, et
+
+    def seed(self, seed: int):
+        _check(lib().plum_seed(self.h, seed))
+
+    def run(self, n_moves):
+        acc = C.c_int(0)
+        _check(lib().plum_run(self.h, n_moves, C.byref(acc)))
+        return acc.value
+
+    def positions(self):
+        o = np.zeros(3 * self.n_bead)
+        _check(lib().plum_get_positions(self.h, o))
+        return o.reshape(-1, 3)
+
+    def set_positions(self, xyz):
+        _check(lib().plum_set_positions(self.h, np.ascontiguousarray(xyz, np.float64).ravel()))
+
+    def observables(self):
+        o = np.zeros(5)
+        _check(lib().plum_observables(self.h, o))
+        return o
+
+    def set_recompute(self, every: int):
+        _check(lib().plum_set_recompute(self.h, every))
+
+    def drift(self):
+        o = np.zeros(5)
+        _check(lib().plum_drift(self.h, o))
+        return o
+
+    def last_timing(self):
+        ms = C.c_double(0)
+        k = C.c_long(0)
+        _check(lib().plum_last_timing(self.h, C.byref(ms), C.byref(k)))
+        return ms.value, k.value

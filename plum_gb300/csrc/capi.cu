@@ -1,0 +1,929 @@
+// C ABI of the engine (include/plum_gpu.h): context creation from the
+// reference's input files, device buffers, and the host-side orchestration of
+// the kernels in kern_energy.cu and kern_moves.cu.
+#include <cmath>
+#include <cstdio>
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/plum_gpu.h"
+#include "engine.h"
+#include "host/input.h"
+
+using namespace plum;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                 \
+  do {                                                                           \
+    cudaError_t e_ = (call);                                                     \
+    if (e_ != cudaSuccess)                                                       \
+      return fail(PLUM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+constexpr double kEwaldCut = 1e-7;   // utilities/constants.h:11
+constexpr double k216 = 1.12246204831;  // utilities/constants.h:62
+
+}  // namespace
+
+struct plum_ctx {
+  Input in;
+  DevParams P;
+  DevBuffers B;
+  int form = PLUM_FORM_FP64;
+  int device = 0;
+  cudaStream_t s = nullptr;
+  std::vector<double4_32a> h_pos;  // host mirror of the current positions
+  bool h_pos_valid = true;
+  // scratch
+  double* d_tot_part = nullptr;
+  int n_tot_part = 0;
+  double* d_out = nullptr;     // small result block
+  double* h_out = nullptr;     // pinned
+  uint32_t* d_stream = nullptr;
+  long long stream_cap = 0;
+  uint32_t* d_mt = nullptr;    // device mt19937 state (625 words)
+  long long gen_len = 0;       // valid words in d_stream for plum_run
+  int* d_log_type = nullptr;
+  int* d_log_acc = nullptr;
+  double* d_log_e = nullptr;
+  int log_cap = 0;
+  bool host_pending = false;
+  int max_len = 1;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+  long last_kernels = 0;
+  long recompute_every = 0;    // full FP64 recompute cadence of plum_run (0: never)
+  long since_recompute = 0;
+  double drift[4] = {0, 0, 0, 0};  // running minus recomputed at the last reset
+  double drift_max = 0.0;
+  // CUDA graph of one batch of moves (kernels read the pending move from
+  // device state, so one capture replays for every batch of the same size)
+  cudaGraphExec_t gexec = nullptr;
+  int g_moves = 0;
+  DevBuffers g_B;
+  bool g_warm = false;
+};
+
+namespace {
+
+// PotentialEwaldCoul::ReadParameters (potential_ewald_coul.cc:38-115):
+// padded z for the dipole correction, real-space cut-off and cells, k^2
+// cut-off and cells; then the half-space k-set {k : 0 < k^2 <= kc^2}.
+int setup_ewald(plum_ctx* c, std::vector<short4>* kn, std::vector<double>* kw) {
+  Input& in = c->in;
+  DevParams& P = c->P;
+  double ebox[3] = {in.box[0], in.box[1], in.box[2]};
+  if (in.dipole) {
+    double min_padding = 150;
+    if (ebox[2] * 3 > min_padding)
+      ebox[2] = ebox[2] * 3;
+    else
+      ebox[2] += min_padding;
+  }
+  const double vol = ebox[0] * ebox[1] * ebox[2];
+  double rc = 1;
+  while (0.5 * in.lB * 1 * 1 * std::erfc(std::sqrt(in.alpha) * rc) / rc > kEwaldCut) rc += 1;
+  if (in.x_real_cutoff > 0) rc = in.x_real_cutoff;
+  double kc2 = in.alpha;
+  const double min_box_vol = std::pow(ebox[0], 3);
+  while (in.lB * 1 * 1 / (2 * kPiRef * min_box_vol) * (4 * kPiRef * kPiRef) *
+             std::exp(-kc2 / (4 * in.alpha)) / kc2 >
+         kEwaldCut)
+    kc2 += in.alpha;
+  int kcell[3];
+  for (int a = 0; a < 3; a++) kcell[a] = (int)std::ceil(std::sqrt(kc2) * ebox[a] / (2 * kPiRef));
+  if (in.x_kmax > 0) {
+    for (int a = 0; a < 3; a++) kcell[a] = in.x_kmax;
+    if (!in.x_have_kcut2) kc2 = INFINITY;
+  }
+  if (in.x_have_kcut2) kc2 = in.x_kcut2 > 0 ? in.x_kcut2 : INFINITY;
+  for (int a = 0; a < 3; a++) {
+    if (kcell[a] > kMaxKmax)
+      return fail(PLUM_ERR_INPUT, "k-space range |n| = " + std::to_string(kcell[a]) +
+                                      " exceeds the supported " + std::to_string(kMaxKmax));
+    P.ebox[a] = ebox[a];
+    P.inv_ebox[a] = 1.0 / ebox[a];
+    P.real_cell[a] = (int)std::ceil(rc / ebox[a]);
+    P.kmax[a] = kcell[a];
+    P.kunit[a] = 2 * kPiRef / ebox[a];
+  }
+  P.kper = 0;
+  for (int a = 0; a < 3; a++) {
+    P.koff[a] = P.kper;
+    P.kper += kcell[a] + 1;
+  }
+  const int row = (int)(P.kper * sizeof(double2));
+  P.kchunk_delta = std::max(1, std::min(16, kKTableBytes / (2 * row)));
+  P.kchunk_sk = std::max(1, std::min(32, kKTableBytes / row));
+  P.real_cut = rc;
+  P.lB = in.lB;
+  P.sqrt_alpha = std::sqrt(in.alpha);
+  P.kpref = in.lB / (kPiRef * vol) * (4 * kPiRef * kPiRef);
+  P.self_coef = -in.lB * std::sqrt(in.alpha / kPiRef);
+  P.dip_coef = in.lB * 2 * kPiRef / (vol / 1.0);
+  P.dipole = in.dipole;
+  kn->clear();
+  kw->clear();
+  for (int lx = -kcell[0]; lx <= kcell[0]; lx++)
+    for (int ly = -kcell[1]; ly <= kcell[1]; ly++)
+      for (int lz = -kcell[2]; lz <= kcell[2]; lz++) {
+        bool half = lx > 0 || (lx == 0 && ly > 0) || (lx == 0 && ly == 0 && lz > 0);
+        if (!half) continue;
+        double kx = lx * 2 * kPiRef / ebox[0];
+        double ky = ly * 2 * kPiRef / ebox[1];
+        double kz = lz * 2 * kPiRef / ebox[2];
+        double k2 = kx * kx + ky * ky + kz * kz;
+        if (!(k2 > 0 && k2 <= kc2)) continue;
+        kn->push_back(make_short4((short)lx, (short)ly, (short)lz, 0));
+        kw->push_back(std::exp(-k2 / (4 * in.alpha)) / k2);
+      }
+  P.n_k = (int)kn->size();
+  c->in.x_kcut2 = kc2;  // effective k^2 cut-off, reported by plum_ctx_info
+  return PLUM_OK;
+}
+
+template <class T>
+int dalloc(T** p, size_t n) {
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e != cudaSuccess) return fail(PLUM_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  return PLUM_OK;
+}
+
+// Final fixed-order reductions of the from-scratch energy into out[8] and the
+// running state.
+__global__ void k_assemble_total(const DevParams P, const DevBuffers B, const double* tot_part,
+                                 int n_part, const double* misc, double* out) {
+  __shared__ double red[8];
+  double lj = 0.0, re = 0.0, ek = 0.0;
+  for (int i = threadIdx.x; i < n_part; i += blockDim.x) {
+    lj += tot_part[2 * i];
+    re += tot_part[2 * i + 1];
+  }
+  if (P.use_ewald)
+    for (int k = threadIdx.x; k < P.n_k; k += blockDim.x) {
+      double2 s = B.sk[k];
+      ek += B.kw[k] * (s.x * s.x + s.y * s.y);
+    }
+  double v[3] = {lj, re, ek};
+  double t[3];
+  for (int q = 0; q < 3; q++) {
+    double x = v[q];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    double s = 0.0;
+    for (int w = 0; w < (int)blockDim.x / 32; w++) s += red[w];
+    t[q] = s;
+  }
+  if (threadIdx.x == 0) {
+    DevState* st = B.state;
+    double e_pair = P.use_pair ? t[0] : 0.0;
+    double real = P.use_ewald ? t[1] + misc[3] : 0.0;
+    double recip = P.use_ewald ? P.kpref * t[2] : 0.0;
+    double self = P.use_ewald ? misc[2] : 0.0;
+    double dip = (P.use_ewald && P.dipole) ? P.dip_coef * misc[4] * misc[4] : 0.0;
+    st->e_pair = e_pair;
+    st->e_ewald = real + recip + self + dip;
+    st->e_bond = P.use_bond ? misc[0] : 0.0;
+    st->e_ext = P.use_ext ? misc[1] : 0.0;
+    st->mz = misc[4];
+    st->dipl_cur = dip;
+    out[0] = st->e_pair;
+    out[1] = st->e_ewald;
+    out[2] = st->e_bond;
+    out[3] = st->e_ext;
+    out[4] = real;
+    out[5] = recip;
+    out[6] = self;
+    out[7] = dip;
+  }
+}
+
+int total_energy(plum_ctx* c, double* out8) {
+  cudaSetDevice(c->device);
+  const DevParams& P = c->P;
+  if (P.use_pair || P.use_ewald) launch_total64(P, c->B, c->d_tot_part, c->n_tot_part, c->s);
+  else CK(cudaMemsetAsync(c->d_tot_part, 0, sizeof(double) * 2 * c->n_tot_part, c->s));
+  launch_sk_full64(P, c->B, c->s);
+  launch_misc_total64(P, c->B, c->d_out + 16, c->s);
+  k_assemble_total<<<1, 256, 0, c->s>>>(P, c->B, c->d_tot_part, c->n_tot_part, c->d_out + 16,
+                                        c->d_out);
+  if (c->form == PLUM_FORM_FP32) launch_fix_all(P, c->B, c->s);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(double) * 8, cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  if (out8) std::memcpy(out8, c->h_out, sizeof(double) * 8);
+  return PLUM_OK;
+}
+
+int read_state(plum_ctx* c, DevState* st) {
+  CK(cudaMemcpyAsync(st, c->B.state, sizeof(DevState), cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  return PLUM_OK;
+}
+
+int refresh_host_pos(plum_ctx* c) {
+  if (c->h_pos_valid) return PLUM_OK;
+  CK(cudaMemcpyAsync(c->h_pos.data(), c->B.pos, sizeof(double4_32a) * c->P.n_bead,
+                     cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  c->h_pos_valid = true;
+  return PLUM_OK;
+}
+
+int ensure_logs(plum_ctx* c, int n) {
+  if (n <= c->log_cap) return PLUM_OK;
+  cudaFree(c->d_log_type);
+  cudaFree(c->d_log_acc);
+  cudaFree(c->d_log_e);
+  if (dalloc(&c->d_log_type, n) || dalloc(&c->d_log_acc, n) || dalloc(&c->d_log_e, n))
+    return PLUM_ERR_CUDA;
+  c->log_cap = n;
+  return PLUM_OK;
+}
+
+int ensure_stream(plum_ctx* c, long long n) {
+  if (n <= c->stream_cap) return PLUM_OK;
+  cudaFree(c->d_stream);
+  c->d_stream = nullptr;
+  if (dalloc(&c->d_stream, (size_t)n)) return PLUM_ERR_CUDA;
+  c->stream_cap = n;
+  c->gen_len = 0;
+  return PLUM_OK;
+}
+
+// The energy-difference kernel of the context's form.
+void launch_delta(const plum_ctx* c, const DevBuffers& B) {
+  if (c->form == PLUM_FORM_FP32)
+    launch_delta_pairs32(c->P, B, c->s);
+  else
+    launch_delta_pairs64(c->P, B, c->s);
+}
+
+void enqueue_loop(plum_ctx* c, int n_moves, const DevBuffers& B) {
+  launch_serial64(c->P, B, kModeGen, c->s);
+  for (int i = 0; i < n_moves; i++) {
+    launch_delta(c, B);
+    int mode = kModeFinish | kModeDecide | (i + 1 < n_moves ? kModeGen : 0);
+    launch_serial64(c->P, B, mode, c->s);
+  }
+}
+
+// The device MC loop: gen, then (pairs, finish+decide+gen) per step. Batches
+// of a repeated size run as one CUDA graph, captured on the second use (the
+// first runs as plain launches so lazy kernel set-up happens outside a
+// capture); the kernels read the pending move from device state, so one
+// capture replays for every batch.
+int device_loop(plum_ctx* c, int n_moves, DevBuffers B) {
+  const long k = 1 + 2L * n_moves;
+  const bool same = c->gexec && c->g_moves == n_moves && !std::memcmp(&c->g_B, &B, sizeof(B));
+  if (same) {
+    CK(cudaGraphLaunch(c->gexec, c->s));
+    c->last_kernels += k;
+    return PLUM_OK;
+  }
+  if (c->g_warm && n_moves >= 8) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal));
+    enqueue_loop(c, n_moves, B);
+    CK(cudaStreamEndCapture(c->s, &g));
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&c->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(PLUM_ERR_CUDA, cudaGetErrorString(e));
+    c->g_moves = n_moves;
+    c->g_B = B;
+    CK(cudaGraphLaunch(c->gexec, c->s));
+    c->last_kernels += k;
+    return PLUM_OK;
+  }
+  c->g_warm = true;
+  enqueue_loop(c, n_moves, B);
+  CK(cudaGetLastError());
+  c->last_kernels += k;
+  return PLUM_OK;
+}
+
+}  // namespace
+
+// FMA throughput probe: every thread runs 8 independent FMA chains, so the
+// pipe, not latency, limits it.
+template <typename T>
+__global__ void k_fma_probe(T* out, int iters, T a, T b) {
+  T x[8];
+  for (int i = 0; i < 8; i++) x[i] = (T)(threadIdx.x + i) * (T)1e-3;
+  for (int it = 0; it < iters; it++)
+#pragma unroll
+    for (int i = 0; i < 8; i++) x[i] = x[i] * a + b;
+  T s = 0;
+  for (int i = 0; i < 8; i++) s += x[i];
+  if (s == (T)-1.2345) out[0] = s;  // keeps the chains live
+}
+
+extern "C" {
+
+const char* plum_last_error(void) { return g_err.c_str(); }
+
+int plum_ctx_create(const char* dir, const char* runin, int form, int device,
+                    plum_ctx** out) {
+  if (!out || !dir || !runin) return fail(PLUM_ERR_INPUT, "null argument");
+  *out = nullptr;
+  if (form != PLUM_FORM_FP64 && form != PLUM_FORM_FP32)
+    return fail(PLUM_ERR_INPUT, "unknown form");
+  plum_ctx* c = new plum_ctx();
+  c->form = form;
+  c->device = device;
+  std::string err;
+  if (!read_input(dir, runin, &c->in, &err)) {
+    delete c;
+    return fail(PLUM_ERR_INPUT, err);
+  }
+  Input& in = c->in;
+  // The reference's own input checks (simulation.cc:142-191, force_field.cc:205-209).
+  std::string bad;
+  double ptot = 0;
+  for (int i = 0; i < 5; i++) ptot += in.move_prob[i];
+  if (in.beta <= 0) bad = "beta must be positive";
+  else if (in.npbc < 2 || in.npbc > 3) bad = "PBC dimensions must be 2 or 3";
+  else if (std::fabs(ptot - 1.0) > 1e-4) bad = "MC move probabilities do not sum up to 1.0";
+  else if (in.move_prob[4] > 0 && !in.use_rigid)
+    bad = "the reptation move requires the rigid bond setting";
+  else if (in.calc_chem_pot && in.use_gc)
+    bad = "chemical potential cannot be calculated when GCMC is used";
+  else if (in.vp_bead_size < 0) bad = "virial bead size must not be negative";
+  else if ((int)in.type_names.size() > kMaxTypes)
+    bad = "more than " + std::to_string(kMaxTypes) + " bead types";
+  if (!bad.empty()) {
+    delete c;
+    return fail(PLUM_ERR_INPUT, bad);
+  }
+  DevParams& P = c->P;
+  std::memset(&P, 0, sizeof(P));
+  const int nb = (int)in.q.size();
+  P.n_bead = nb;
+  P.n_mol = in.n_mol;
+  P.n_type = (int)in.type_names.size();
+  P.npbc = in.npbc;
+  P.phantom = in.phantom;
+  P.grafted = in.grafted;
+  for (int a = 0; a < 3; a++) {
+    P.box[a] = in.box[a];
+    P.inv_box[a] = 1.0 / in.box[a];
+    P.ebox[a] = in.box[a];
+    P.inv_ebox[a] = 1.0 / in.box[a];
+  }
+  P.use_pair = in.use_pair;
+  P.use_ewald = in.use_ewald;
+  P.use_bond = in.use_bond;
+  P.use_rigid = in.use_rigid;
+  P.use_ext = in.use_ext;
+  P.beta = in.beta;
+  P.move_size = in.move_size;
+  for (int i = 0; i < 5; i++) P.move_prob[i] = in.move_prob[i];
+  // simulation.cc:286-296
+  P.bond_len = 0;
+  P.vary_bond = 0;
+  if (in.use_rigid) P.bond_len = in.rigid;
+  if (in.use_bond) {
+    P.bond_len = in.r0;
+    P.vary_bond = 1;
+  }
+  P.k_bond = in.k_bond;
+  P.r0 = in.r0;
+  // LJ mixing and shifts (potential_truncated_lj.cc:55-81).
+  for (int i = 0; i < P.n_type; i++)
+    for (int j = 0; j < P.n_type; j++) {
+      LJEntry a, b;
+      auto ia = in.lj.find(in.type_names[i]);
+      auto ib = in.lj.find(in.type_names[j]);
+      if (ia != in.lj.end()) a = ia->second;
+      if (ib != in.lj.end()) b = ib->second;
+      double sigma = (a.sigma + b.sigma) / 2;
+      double eps = std::sqrt((a.epsilon * b.epsilon));
+      int k = i * P.n_type + j;
+      P.lj_sig2[k] = sigma * sigma;
+      P.lj_eps4[k] = 4 * eps;
+      if (in.lj_cut < 0) {
+        double r6r = std::pow((1.0 / k216), 6);
+        P.lj_eref[k] = 4 * eps * (r6r * r6r - r6r);
+        P.lj_rc2[k] = (k216 * sigma) * (k216 * sigma);
+      } else {
+        double r6r = std::pow((sigma / in.lj_cut), 6);
+        P.lj_eref[k] = 4 * eps * (r6r * r6r - r6r);
+        P.lj_rc2[k] = in.lj_cut * in.lj_cut;
+      }
+    }
+  P.wall_cut = in.wall_cut;
+  for (int i = 0; i < P.n_type; i++) {
+    auto it = in.wall.find(in.type_names[i]);
+    P.wall_sig[i] = it != in.wall.end() ? it->second.sigma : 0.0;
+    P.wall_eps[i] = it != in.wall.end() ? it->second.epsilon : 0.0;
+    P.graft[i] = in.type_names[i] == "L" ? 1 : (in.type_names[i] == "R" ? 2 : 0);
+  }
+  std::vector<int> chains, ions;
+  for (int m = in.phantom; m < in.n_mol; m++) {
+    int sz = in.mol_start[m + 1] - in.mol_start[m];
+    (sz > 1 ? chains : ions).push_back(m);
+    c->max_len = std::max(c->max_len, sz);
+  }
+  P.n_chain_total = (int)chains.size();
+  P.n_ion_total = (int)ions.size();
+  std::vector<short4> kn;
+  std::vector<double> kw;
+  if (form == PLUM_FORM_FP32 && in.npbc == 3 && in.dipole) {
+    delete c;
+    return fail(PLUM_ERR_INPUT, "the precision form needs npbc = 2 when the dipole correction is on");
+  }
+  if (in.use_ewald) {
+    int rc = setup_ewald(c, &kn, &kw);
+    if (rc) {
+      delete c;
+      return rc;
+    }
+  }
+  // Precision-form constants: fixed point in units of the Ewald box.
+  P.form = form;
+  for (int a = 0; a < 3; a++) {
+    P.f_scale[a] = (float)(P.ebox[a] / 4294967296.0);
+    P.inv_fix[a] = 4294967296.0 / P.ebox[a];
+    P.f_box[a] = (float)P.ebox[a];
+  }
+  for (int k = 0; k < kMaxT2; k++) {
+    P.f_lj_sig2[k] = (float)P.lj_sig2[k];
+    P.f_lj_eps4[k] = (float)P.lj_eps4[k];
+    P.f_lj_rc2[k] = (float)P.lj_rc2[k];
+    P.f_lj_eref[k] = (float)P.lj_eref[k];
+  }
+  P.f_real_cut = (float)P.real_cut;
+  P.f_sqrt_alpha = (float)P.sqrt_alpha;
+  P.f_lB = (float)P.lB;
+  c->recompute_every = form == PLUM_FORM_FP32 ? 10000 : 0;
+  // Device state.
+  if (cudaSetDevice(device) != cudaSuccess) {
+    delete c;
+    return fail(PLUM_ERR_CUDA, "cannot select CUDA device " + std::to_string(device));
+  }
+  cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking);
+  cudaEventCreate(&c->ev0);
+  cudaEventCreate(&c->ev1);
+  DevBuffers& B = c->B;
+  std::memset(&B, 0, sizeof(B));
+  int rc = 0;
+  rc |= dalloc(&B.pos, nb);
+  rc |= dalloc(&B.trial, nb);
+  rc |= dalloc(&B.type, nb);
+  rc |= dalloc(&B.mol_start, in.n_mol + 1);
+  rc |= dalloc(&B.chain_ids, chains.size());
+  rc |= dalloc(&B.ion_ids, ions.size());
+  rc |= dalloc(&B.kn, kn.size());
+  rc |= dalloc(&B.kw, kw.size());
+  rc |= dalloc(&B.sk, kn.size());
+  rc |= dalloc(&B.dsk, kn.size());
+  rc |= dalloc(&B.partial, 4 * (size_t)std::max(pair_grid(), pair_grid32()));
+  rc |= dalloc(&B.fpos, nb);
+  rc |= dalloc(&B.fq, nb);
+  rc |= dalloc(&B.ftrial, c->max_len);
+  {
+    int groups = (c->max_len + std::max(1, P.kchunk_delta) - 1) / std::max(1, P.kchunk_delta);
+    rc |= dalloc(&B.dsk_part, (size_t)groups * std::max(1, P.n_k));
+    rc |= dalloc(&B.dsk_part32, (size_t)groups * std::max(1, P.n_k));
+    rc |= dalloc(&B.ktile_count, ktile_count(P));
+    rc |= dalloc(&B.kpartial, ktile_count(P));
+  }
+  rc |= dalloc(&B.bond_mol, in.n_mol);
+  rc |= dalloc(&B.state, 1);
+  c->n_tot_part = total_partials_count(P);
+  rc |= dalloc(&c->d_tot_part, 2 * (size_t)c->n_tot_part);
+  rc |= dalloc(&c->d_out, 64);
+  rc |= dalloc(&c->d_mt, 625);
+  if (rc) {
+    plum_ctx_destroy(c);
+    return PLUM_ERR_CUDA;
+  }
+  cudaMallocHost(&c->h_out, 64 * sizeof(double));
+  c->h_pos.resize(nb);
+  for (int i = 0; i < nb; i++)
+    c->h_pos[i] = make_double4_32a(in.xyz[3 * i], in.xyz[3 * i + 1], in.xyz[3 * i + 2], in.q[i]);
+  cudaMemcpy(B.pos, c->h_pos.data(), sizeof(double4_32a) * nb, cudaMemcpyHostToDevice);
+  cudaMemcpy(B.trial, c->h_pos.data(), sizeof(double4_32a) * nb, cudaMemcpyHostToDevice);
+  cudaMemcpy(B.type, in.type.data(), sizeof(int) * nb, cudaMemcpyHostToDevice);
+  cudaMemcpy(B.mol_start, in.mol_start.data(), sizeof(int) * (in.n_mol + 1),
+             cudaMemcpyHostToDevice);
+  if (!chains.empty())
+    cudaMemcpy(B.chain_ids, chains.data(), sizeof(int) * chains.size(), cudaMemcpyHostToDevice);
+  if (!ions.empty())
+    cudaMemcpy(B.ion_ids, ions.data(), sizeof(int) * ions.size(), cudaMemcpyHostToDevice);
+  if (!kn.empty()) {
+    cudaMemcpy(B.kn, kn.data(), sizeof(short4) * kn.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(B.kw, kw.data(), sizeof(double) * kw.size(), cudaMemcpyHostToDevice);
+  }
+  cudaMemset(B.state, 0, sizeof(DevState));
+  cudaMemset(B.ktile_count, 0, sizeof(int) * std::max(1, ktile_count(P)));
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    plum_ctx_destroy(c);
+    return fail(PLUM_ERR_CUDA, cudaGetErrorString(e));
+  }
+  rc = plum_seed(c, 5489u);
+  if (!rc) rc = total_energy(c, nullptr);
+  if (rc) {
+    plum_ctx_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return PLUM_OK;
+}
+
+int plum_ctx_destroy(plum_ctx* c) {
+  if (!c) return PLUM_OK;
+  cudaSetDevice(c->device);
+  if (c->s) cudaStreamSynchronize(c->s);
+  void* ptrs[] = {c->B.pos,      c->B.trial,   c->B.type,  c->B.mol_start, c->B.chain_ids,
+                  c->B.ion_ids,  c->B.kn,      c->B.kw,    c->B.sk,        c->B.dsk,
+                  c->B.partial,  c->B.bond_mol, c->B.state, c->d_tot_part,  c->d_out,
+                  c->B.dsk_part, c->B.ktile_count, c->B.kpartial, c->B.fpos,
+                  c->B.fq,       c->B.ftrial,  c->B.dsk_part32,
+                  c->d_stream,   c->d_mt,      c->d_log_type, c->d_log_acc, c->d_log_e};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (c->h_out) cudaFreeHost(c->h_out);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->s) cudaStreamDestroy(c->s);
+  delete c;
+  return PLUM_OK;
+}
+
+int plum_ctx_info(const plum_ctx* c, plum_info* o) {
+  if (!c || !o) return fail(PLUM_ERR_INPUT, "null argument");
+  std::memset(o, 0, sizeof(*o));
+  o->n_bead = c->P.n_bead;
+  o->n_mol = c->P.n_mol;
+  o->n_type = c->P.n_type;
+  o->n_kvec = c->P.n_k;
+  o->npbc = c->P.npbc;
+  o->form = c->form;
+  for (int a = 0; a < 3; a++) {
+    o->box[a] = c->P.box[a];
+    o->ewald_box[a] = c->P.ebox[a];
+    o->real_cell[a] = c->P.real_cell[a];
+    o->k_cell[a] = c->P.kmax[a];
+  }
+  o->real_cutoff = c->P.real_cut;
+  o->kcut2 = c->in.x_kcut2;
+  o->alpha = c->in.alpha;
+  o->lB = c->in.lB;
+  return PLUM_OK;
+}
+
+int plum_total_energy(plum_ctx* c, double* out) {
+  if (!c) return fail(PLUM_ERR_INPUT, "null context");
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
+  return total_energy(c, out);
+}
+
+int plum_energies(const plum_ctx* cc, double* out) {
+  plum_ctx* c = const_cast<plum_ctx*>(cc);
+  if (!c || !out) return fail(PLUM_ERR_INPUT, "null argument");
+  cudaSetDevice(c->device);
+  DevState st;
+  int rc = read_state(c, &st);
+  if (rc) return rc;
+  out[0] = st.e_pair, out[1] = st.e_ewald, out[2] = st.e_bond, out[3] = st.e_ext;
+  return PLUM_OK;
+}
+
+int plum_delta_energy(plum_ctx* c, int mol, const double* trial, const int* moved,
+                      double* out) {
+  if (!c || !trial || !moved || !out) return fail(PLUM_ERR_INPUT, "null argument");
+  if (mol < 0 || mol >= c->P.n_mol) return fail(PLUM_ERR_INPUT, "molecule index out of range");
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is already pending");
+  cudaSetDevice(c->device);
+  int rc = refresh_host_pos(c);
+  if (rc) return rc;
+  const int b0 = c->in.mol_start[mol], b1 = c->in.mol_start[mol + 1];
+  int lo = -1, hi = -1;
+  for (int i = b0; i < b1; i++)
+    if (moved[i - b0]) {
+      if (lo < 0) lo = i;
+      hi = i + 1;
+    }
+  if (lo < 0) lo = hi = b0;
+  // Beads inside [lo, hi) that are not flagged keep their current position,
+  // so their terms cancel exactly.
+  std::vector<double4_32a> span(hi - lo);
+  for (int i = lo; i < hi; i++) {
+    double4_32a p = c->h_pos[i];
+    if (moved[i - b0]) {
+      p.x = trial[3 * (i - b0)];
+      p.y = trial[3 * (i - b0) + 1];
+      p.z = trial[3 * (i - b0) + 2];
+    }
+    span[i - lo] = p;
+  }
+  if (hi > lo)
+    CK(cudaMemcpyAsync(c->B.trial + lo, span.data(), sizeof(double4_32a) * (hi - lo),
+                       cudaMemcpyHostToDevice, c->s));
+  launch_set_move(c->B, mol, lo, hi, c->s);
+  if (c->form == PLUM_FORM_FP32) launch_fix_trial(c->P, c->B, c->s);
+  launch_delta(c, c->B);
+  launch_serial64(c->P, c->B, kModeFinish, c->s);
+  CK(cudaGetLastError());
+  DevState st;
+  rc = read_state(c, &st);
+  if (rc) return rc;
+  if (st.error) return fail(st.error, "device reported an error in the energy difference");
+  out[0] = st.de, out[1] = st.de_pair, out[2] = st.de_ewald, out[3] = st.de_bond,
+  out[4] = st.de_ext;
+  c->host_pending = true;
+  return PLUM_OK;
+}
+
+int plum_finalize(plum_ctx* c, int accept) {
+  if (!c) return fail(PLUM_ERR_INPUT, "null context");
+  if (!c->host_pending) return fail(PLUM_ERR_STATE, "no pending trial move");
+  cudaSetDevice(c->device);
+  int acc = accept ? 1 : 0;
+  CK(cudaMemcpyAsync(&c->B.state->last_accept, &acc, sizeof(int), cudaMemcpyHostToDevice, c->s));
+  launch_serial64(c->P, c->B, kModeCommit, c->s);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->s));
+  c->host_pending = false;
+  if (accept) c->h_pos_valid = false;
+  return PLUM_OK;
+}
+
+int plum_run_moves(plum_ctx* c, const uint32_t* stream, long n_stream, int n_moves,
+                   int* move_type, int* accept, double* etot, long* draws_used) {
+  if (!c || (!stream && n_stream > 0) || n_moves < 0)
+    return fail(PLUM_ERR_INPUT, "bad argument");
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
+  if (c->in.use_gc) return fail(PLUM_ERR_INPUT, "grand-canonical steps are not run by this loop");
+  if (n_moves == 0) return PLUM_OK;
+  cudaSetDevice(c->device);
+  int rc = ensure_stream(c, n_stream);
+  if (!rc) rc = ensure_logs(c, n_moves);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(c->d_stream, stream, sizeof(uint32_t) * n_stream, cudaMemcpyHostToDevice,
+                     c->s));
+  c->gen_len = 0;  // the device generator's buffer is overwritten
+  DevState st;
+  rc = read_state(c, &st);
+  if (rc) return rc;
+  st.stream_pos = 0;
+  st.stream_len = n_stream;
+  st.step = 0;
+  st.step_open = 0;
+  st.error = 0;
+  st.pending = 0;
+  CK(cudaMemcpyAsync(c->B.state, &st, sizeof(DevState), cudaMemcpyHostToDevice, c->s));
+  DevBuffers B = c->B;
+  B.stream = c->d_stream;
+  B.log_type = c->d_log_type;
+  B.log_accept = c->d_log_acc;
+  B.log_etot = c->d_log_e;
+  c->last_kernels = 0;
+  CK(cudaEventRecord(c->ev0, c->s));
+  rc = device_loop(c, n_moves, B);
+  if (rc) return rc;
+  CK(cudaEventRecord(c->ev1, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->last_ms = ms;
+  rc = read_state(c, &st);
+  if (rc) return rc;
+  c->h_pos_valid = false;
+  if (move_type)
+    CK(cudaMemcpy(move_type, c->d_log_type, sizeof(int) * n_moves, cudaMemcpyDeviceToHost));
+  if (accept)
+    CK(cudaMemcpy(accept, c->d_log_acc, sizeof(int) * n_moves, cudaMemcpyDeviceToHost));
+  if (etot) CK(cudaMemcpy(etot, c->d_log_e, sizeof(double) * n_moves, cudaMemcpyDeviceToHost));
+  if (draws_used) *draws_used = (long)st.stream_pos;
+  if (st.error == PLUM_ERR_STREAM_DEV)
+    return fail(PLUM_ERR_STREAM, "the recorded random stream ran out");
+  if (st.error) return fail(st.error, "device reported an error during the moves");
+  return PLUM_OK;
+}
+
+int plum_seed(plum_ctx* c, uint32_t seed) {
+  if (!c) return fail(PLUM_ERR_INPUT, "null context");
+  // std::mt19937::seed: mt[0] = s, mt[i] = 1812433253 (mt[i-1] ^ (mt[i-1] >> 30)) + i.
+  uint32_t mt[625];
+  mt[0] = seed;
+  for (int i = 1; i < 624; i++) mt[i] = 1812433253u * (mt[i - 1] ^ (mt[i - 1] >> 30)) + (uint32_t)i;
+  mt[624] = 624;
+  cudaSetDevice(c->device);
+  CK(cudaMemcpyAsync(c->d_mt, mt, sizeof(mt), cudaMemcpyHostToDevice, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  c->gen_len = 0;
+  return PLUM_OK;
+}
+
+int plum_run(plum_ctx* c, int n_moves, int* accepted_out) {
+  if (!c || n_moves < 0) return fail(PLUM_ERR_INPUT, "bad argument");
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
+  if (c->in.use_gc) return fail(PLUM_ERR_INPUT, "grand-canonical steps are not run by this loop");
+  cudaSetDevice(c->device);
+  // Draw budget per step: 5 fixed draws + the move's own; a pivot consumes
+  // 2 + len (2 r + 1) with r rejected pairs per randSphere (mean 1.27).
+  const int batch = 256;
+  const long long per_move = 16 + 12LL * c->max_len;
+  const long long need = per_move * batch;
+  const long long cap = std::max<long long>(4 * need, 1 << 22);
+  int rc = ensure_stream(c, cap);
+  if (rc) return rc;
+  DevState st;
+  rc = read_state(c, &st);
+  if (rc) return rc;
+  if (c->gen_len == 0) st.stream_pos = 0;
+  st.step = 0;
+  st.step_open = 0;
+  st.error = 0;
+  st.pending = 0;
+  st.n_accept = 0;
+  long long pos = st.stream_pos, len = c->gen_len;
+  DevBuffers B = c->B;
+  B.stream = c->d_stream;
+  B.log_type = nullptr;
+  B.log_accept = nullptr;
+  B.log_etot = nullptr;
+  c->last_kernels = 0;
+  CK(cudaEventRecord(c->ev0, c->s));
+  int done = 0;
+  while (done < n_moves) {
+    // Keep at least `need` unread words: move the unread tail to the front
+    // and generate the rest on the device.
+    if (len - pos < need) {
+      long long tail = len - pos;
+      if (tail > 0)
+        CK(cudaMemcpyAsync(c->d_stream, c->d_stream + pos, sizeof(uint32_t) * tail,
+                           cudaMemcpyDeviceToDevice, c->s));
+      launch_mt_fill(c->d_mt, c->d_stream + tail, cap - tail, c->s);
+      c->last_kernels++;
+      len = cap;
+      pos = 0;
+      st.stream_pos = 0;
+    }
+    st.stream_len = len;
+    st.step = 0;
+    st.step_open = 0;
+    CK(cudaMemcpyAsync(c->B.state, &st, sizeof(DevState), cudaMemcpyHostToDevice, c->s));
+    int nb = std::min(batch, n_moves - done);
+    rc = device_loop(c, nb, B);
+    if (rc) return rc;
+    rc = read_state(c, &st);
+    if (rc) return rc;
+    if (st.error) break;
+    pos = st.stream_pos;
+    done += nb;
+    c->since_recompute += nb;
+    if (c->recompute_every > 0 && c->since_recompute >= c->recompute_every) {
+      // Full FP64 recompute: resets the running totals, S(k) and the fixed-
+      // point mirror; the difference is the drift accumulated since the last.
+      double fresh[8];
+      rc = total_energy(c, fresh);
+      if (rc) return rc;
+      double run[4] = {st.e_pair, st.e_ewald, st.e_bond, st.e_ext};
+      double tot = 0.0;
+      for (int q = 0; q < 4; q++) {
+        c->drift[q] = run[q] - fresh[q];
+        tot += c->drift[q];
+      }
+      c->drift_max = std::max(c->drift_max, std::fabs(tot));
+      c->since_recompute = 0;
+      rc = read_state(c, &st);
+      if (rc) return rc;
+      c->last_kernels += 5;
+    }
+  }
+  CK(cudaEventRecord(c->ev1, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->last_ms = ms;
+  c->gen_len = len;
+  c->h_pos_valid = false;
+  if (accepted_out) *accepted_out = st.n_accept;
+  if (st.error == PLUM_ERR_STREAM_DEV) return fail(PLUM_ERR_STREAM, "device stream ran out");
+  if (st.error) return fail(st.error, "device reported an error during the moves");
+  return PLUM_OK;
+}
+
+int plum_get_positions(const plum_ctx* cc, double* xyz) {
+  plum_ctx* c = const_cast<plum_ctx*>(cc);
+  if (!c || !xyz) return fail(PLUM_ERR_INPUT, "null argument");
+  cudaSetDevice(c->device);
+  int rc = refresh_host_pos(c);
+  if (rc) return rc;
+  for (int i = 0; i < c->P.n_bead; i++) {
+    xyz[3 * i] = c->h_pos[i].x;
+    xyz[3 * i + 1] = c->h_pos[i].y;
+    xyz[3 * i + 2] = c->h_pos[i].z;
+  }
+  return PLUM_OK;
+}
+
+int plum_set_positions(plum_ctx* c, const double* xyz) {
+  if (!c || !xyz) return fail(PLUM_ERR_INPUT, "null argument");
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
+  cudaSetDevice(c->device);
+  int rc = refresh_host_pos(c);
+  if (rc) return rc;
+  for (int i = 0; i < c->P.n_bead; i++) {
+    c->h_pos[i].x = xyz[3 * i];
+    c->h_pos[i].y = xyz[3 * i + 1];
+    c->h_pos[i].z = xyz[3 * i + 2];
+  }
+  CK(cudaMemcpyAsync(c->B.pos, c->h_pos.data(), sizeof(double4_32a) * c->P.n_bead,
+                     cudaMemcpyHostToDevice, c->s));
+  CK(cudaMemcpyAsync(c->B.trial, c->h_pos.data(), sizeof(double4_32a) * c->P.n_bead,
+                     cudaMemcpyHostToDevice, c->s));
+  return total_energy(c, nullptr);
+}
+
+int plum_observables(const plum_ctx* cc, double* out) {
+  plum_ctx* c = const_cast<plum_ctx*>(cc);
+  if (!c || !out) return fail(PLUM_ERR_INPUT, "null argument");
+  cudaSetDevice(c->device);
+  launch_observables64(c->P, c->B, c->d_out + 32, c->s);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(c->h_out, c->d_out + 32, sizeof(double) * 5, cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  std::memcpy(out, c->h_out, sizeof(double) * 5);
+  return PLUM_OK;
+}
+
+int plum_set_recompute(plum_ctx* c, long every) {
+  if (!c || every < 0) return fail(PLUM_ERR_INPUT, "bad argument");
+  c->recompute_every = every;
+  c->since_recompute = 0;
+  return PLUM_OK;
+}
+
+int plum_drift(const plum_ctx* c, double* out) {
+  if (!c || !out) return fail(PLUM_ERR_INPUT, "null argument");
+  for (int q = 0; q < 4; q++) out[q] = c->drift[q];
+  out[4] = c->drift_max;
+  return PLUM_OK;
+}
+
+int plum_probe_peaks(int device, double* fp32_tflops, double* fp64_tflops) {
+  if (cudaSetDevice(device) != cudaSuccess) return fail(PLUM_ERR_CUDA, "cannot select device");
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  float* o32 = nullptr;
+  double* o64 = nullptr;
+  CK(cudaMalloc(&o32, sizeof(float)));
+  CK(cudaMalloc(&o64, sizeof(double)));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int blocks = sms * 8, threads = 256;
+  float ms = 0;
+  // FP32: warm-up then timed
+  const int it32 = 4096;
+  k_fma_probe<float><<<blocks, threads>>>(o32, 64, 0.999f, 1e-4f);
+  cudaEventRecord(e0);
+  k_fma_probe<float><<<blocks, threads>>>(o32, it32, 0.999f, 1e-4f);
+  cudaEventRecord(e1);
+  CK(cudaEventSynchronize(e1));
+  cudaEventElapsedTime(&ms, e0, e1);
+  if (fp32_tflops) *fp32_tflops = 2.0 * 8 * it32 * (double)blocks * threads / (ms * 1e-3) / 1e12;
+  const int it64 = 256;
+  k_fma_probe<double><<<blocks, threads>>>(o64, 16, 0.999, 1e-4);
+  cudaEventRecord(e0);
+  k_fma_probe<double><<<blocks, threads>>>(o64, it64, 0.999, 1e-4);
+  cudaEventRecord(e1);
+  CK(cudaEventSynchronize(e1));
+  cudaEventElapsedTime(&ms, e0, e1);
+  if (fp64_tflops) *fp64_tflops = 2.0 * 8 * it64 * (double)blocks * threads / (ms * 1e-3) / 1e12;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(o32);
+  cudaFree(o64);
+  return PLUM_OK;
+}
+
+int plum_last_timing(const plum_ctx* c, double* ms, long* kernels) {
+  if (!c) return fail(PLUM_ERR_INPUT, "null context");
+  if (ms) *ms = c->last_ms;
+  if (kernels) *kernels = c->last_kernels;
+  return PLUM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,157 @@
+// Device-side layout of one Monte Carlo system and the kernel entry points.
+//
+// HBM layout (one system, FP64 form):
+//   pos    double4_32a[n_bead]  current (x, y, z, q), unwrapped coordinates
+//   trial  double4_32a[n_bead]  trial   (x, y, z, q); equals pos outside the
+//                           moved bead range of the pending move
+//   type   int[n_bead]      bead type (index into the per-type tables)
+//   mol_start int[n_mol+1]  beads of molecule m are [mol_start[m], mol_start[m+1])
+//   kn     short4[n_k]      integer k = (nx, ny, nz) of each half-space vector
+//   kw     double[n_k]      e^{-k^2/4a}/k^2 on the reference's k-set
+//   sk     double2[n_k]     running structure factor S(k) = sum q e^{i k.r}
+//   dsk    double2[n_k]     S(k) change of the pending move
+//   partial double[grid*4]  per-block partial sums of the pending move
+//   dsk_part double2[groups*n_k], kpartial double[k tiles]: k-space parts
+//   state  DevState         running energies, the pending move, stream cursor
+// Everything here is a few MB even at 20,000 beads and 15,624 k-vectors, so
+// it stays L2-resident across moves; the pair sweeps are FP64/FP32-pipe
+// bound, not HBM bound.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace plum {
+
+constexpr int kMaxTypes = 8;
+constexpr int kMaxT2 = kMaxTypes * kMaxTypes;
+constexpr double kVeryLarge = 1e8;   // utilities/constants.h:15
+constexpr double kPiRef = 3.14159265359;  // utilities/constants.h:20
+constexpr double kMtMax = 4294967295.0;   // std::mt19937::max()
+
+// Threads per block of the pair sweep.
+constexpr int kPairThreads = 256;
+constexpr int kMaxKmax = 1024;       // |n| per axis supported by the k tables
+constexpr int kKTableBytes = 96 * 1024;  // shared memory budget for phase tables
+constexpr int kSerialThreads = 256;
+constexpr int kDrawWindow = 4096;    // stream words staged per serial launch
+
+// Device-side error codes (same values as PLUM_ERR_* in include/plum_gpu.h).
+constexpr int PLUM_ERR_TIMEOUT_DEV = 3;
+constexpr int PLUM_ERR_NONFINITE_DEV = 4;
+constexpr int PLUM_ERR_STREAM_DEV = 6;
+
+struct DevParams {
+  int n_bead, n_mol, n_type, npbc;
+  int phantom, grafted, n_chain_total, n_ion_total;  // chain/ion pick lists
+  double box[3], inv_box[3];
+  double ebox[3], inv_ebox[3];
+  int use_pair, use_ewald, use_bond, use_rigid, use_ext, dipole;
+  double beta, move_size, move_prob[5];
+  double bond_len;   // r0 (bond potential) or the rigid length
+  int vary_bond;     // bond potential on: +-10% bond length draws
+  // LJ per ordered type pair k = ti*n_type+tj (potential_truncated_lj.cc:49-85)
+  double lj_sig2[kMaxT2], lj_eps4[kMaxT2], lj_rc2[kMaxT2], lj_eref[kMaxT2];
+  // Ewald (potential_ewald_coul.cc:29-115)
+  double lB, sqrt_alpha, real_cut;
+  int real_cell[3];
+  int n_k, kmax[3];
+  int koff[3], kper;  // per-bead table: axis a at koff[a], n = 0..kmax[a]; kper entries
+  int kchunk_delta, kchunk_sk;  // beads per table chunk (fits kKTableBytes)
+  double kunit[3];   // 2 kPi / ebox[a]
+  double kpref;      // lB/(kPi V) * 4 kPi^2
+  double self_coef;  // -lB sqrt(alpha/kPi)
+  double dip_coef;   // lB * 2 kPi / V
+  // bonds (potential_spring.cc:22-48)
+  double k_bond, r0;
+  // walls (potential_truncated_lj_wall.cc:46-134)
+  double wall_cut, wall_sig[kMaxTypes], wall_eps[kMaxTypes];
+  int graft[kMaxTypes];
+  // precision form (FP32 pair and k-space arithmetic)
+  int form;              // 0 FP64, 1 FP32
+  float f_scale[3];      // Ewald box length / 2^32: fixed-point unit per axis
+  float f_box[3];        // Ewald box lengths
+  float f_lj_sig2[kMaxT2], f_lj_eps4[kMaxT2], f_lj_rc2[kMaxT2], f_lj_eref[kMaxT2];
+  float f_real_cut, f_sqrt_alpha, f_lB;
+  double inv_fix[3];     // 2^32 / Ewald box length (FP64 -> fixed point)
+};
+
+// The pending move: beads [b_lo, b_hi) of molecule `mol` hold trial
+// positions in `trial`.
+struct DevState {
+  double e_pair, e_ewald, e_bond, e_ext;
+  double mz;         // sum q z over the current configuration
+  double dipl_cur;   // dipole energy as last committed (reference semantics)
+  // pending move
+  int pending, mol, b_lo, b_hi, move_type, step, step_open;
+  // results of the last energy difference
+  double de, de_pair, de_ewald, de_bond, de_ext, bond_trial, dipl_trial, dmz;
+  int last_accept;
+  // stream cursor
+  long long stream_pos, stream_len;
+  int error;         // PLUM_ERR_* raised on the device
+  int moves_left;
+  int n_accept;
+  int n_nonfinite;   // steps whose dE was NaN/Inf (rejected, as in the reference)
+};
+
+struct DevBuffers {
+  double4_32a* pos;
+  double4_32a* trial;
+  int* type;
+  int* mol_start;
+  int* chain_ids;
+  int* ion_ids;
+  short4* kn;
+  double* kw;
+  double2* sk;
+  double2* dsk;
+  double* partial;   // [grid][4]
+  // precision form mirrors: 32-bit fixed-point fractions of the Ewald box
+  int4* fpos;        // [n_bead] current (X, Y, Z, type)
+  float* fq;         // [n_bead] charges
+  int4* ftrial;      // [max molecule length] trial of the pending move's beads
+  float2* dsk_part32;  // [groups][n_k]
+  double2* dsk_part; // [groups][n_k] dS(k) parts of the pending move
+  int* ktile_count;  // [k tiles] arrival tickets (reset by the last arrival)
+  double* kpartial;  // [k tiles] energy change per k tile
+  double* bond_mol;  // [n_mol]
+  DevState* state;
+  const uint32_t* stream;
+  // per-step logs (may be null)
+  int* log_type;
+  int* log_accept;
+  double* log_etot;
+};
+
+// Launch helpers (kern_energy.cu / kern_moves.cu). All enqueue on `s`.
+int pair_grid();
+int ktile_count(const DevParams& P);
+void launch_delta_pairs64(const DevParams& P, const DevBuffers& B, cudaStream_t s);
+void launch_total64(const DevParams& P, const DevBuffers& B, double* out_partials,
+                    int n_part, cudaStream_t s);
+int total_partials_count(const DevParams& P);
+void launch_sk_full64(const DevParams& P, const DevBuffers& B, cudaStream_t s);
+void launch_misc_total64(const DevParams& P, const DevBuffers& B, double* out6,
+                         cudaStream_t s);
+
+// Serial step: mode bits
+constexpr int kModeFinish = 1;   // reduce partials, compose dE
+constexpr int kModeDecide = 2;   // Metropolis draw from the stream + commit
+constexpr int kModeGen = 4;      // generate the next move from the stream
+constexpr int kModeCommit = 8;   // commit/reject by state->last_accept (host decided)
+void launch_serial64(const DevParams& P, const DevBuffers& B, int mode, cudaStream_t s);
+void launch_set_move(const DevBuffers& B, int mol, int b_lo, int b_hi, cudaStream_t s);
+void launch_observables64(const DevParams& P, const DevBuffers& B, double* out5,
+                          cudaStream_t s);
+// precision form (kern_fp32.cu)
+int pair_grid32();
+void launch_delta_pairs32(const DevParams& P, const DevBuffers& B, cudaStream_t s);
+void launch_fix_all(const DevParams& P, const DevBuffers& B, cudaStream_t s);
+void launch_fix_trial(const DevParams& P, const DevBuffers& B, cudaStream_t s);
+__device__ int4 fix_point(const DevParams& P, double4_32a p, int type);
+
+// mt19937 on the device: state[625] (624 words + index), fills out[n].
+void launch_mt_fill(uint32_t* state, uint32_t* out, long long n, cudaStream_t s);
+
+}  // namespace plum

@@ -1,0 +1,278 @@
+// Precision form: the pending move's energy difference with FP32 pair and
+// k-space arithmetic (FP64 kept for S(k), the running totals and the
+// periodic full recompute, see kern_energy.cu / capi.cu).
+//
+// Coordinates are mirrored as 32-bit fixed-point fractions of the Ewald box
+// (fpos: X = round(w / L * 2^32), w wrapped into the primary cell on periodic
+// axes). Then
+//   * a minimum-image difference is one integer subtraction: int32 wraparound
+//     is the periodic wrap, and the difference converts to FP32 with a
+//     relative error of 2^-24 of |d| (close pairs stay accurate);
+//   * the phase of k = 2 pi n / L is n * X mod 2^32 exactly (integer
+//     multiply-add), so e^{i k.r} = sincospi(phase * 2^-31) has no FP32
+//     range-reduction error.
+// In the slab geometry z is not wrapped (|dz| < H < L_z,Ewald / 2), so the same
+// subtraction gives the raw dz the reference uses (GetDistVector, npbc = 2).
+//
+// Work decomposition is the FP64 kernel's: every (moved, other) pair dealt
+// across the grid, k tiles x moved-bead groups with a last-arrival reduction.
+// Per-thread and per-block sums are FP32; blocks are added in FP64 by the
+// serial kernel.
+#include "engine.h"
+
+namespace plum {
+
+constexpr int kKTile32 = 128;
+
+__device__ __forceinline__ int fix_axis(double x, double L, double inv_fix, bool periodic) {
+  double w = periodic ? x - L * floor(x / L) : x;
+  long long v = llrint(w * inv_fix);
+  return (int)(unsigned int)(unsigned long long)v;
+}
+
+__device__ int4 fix_point(const DevParams& P, double4_32a p, int type) {
+  return make_int4(fix_axis(p.x, P.ebox[0], P.inv_fix[0], true),
+                   fix_axis(p.y, P.ebox[1], P.inv_fix[1], true),
+                   fix_axis(p.z, P.ebox[2], P.inv_fix[2], P.npbc > 2), type);
+}
+
+__device__ __forceinline__ float fdiff(int a, int b, float scale) {
+  return (float)(int)((unsigned)b - (unsigned)a) * scale;
+}
+
+__device__ __forceinline__ float lj32(const DevParams& P, int k, float r2) {
+  if (r2 <= 0.0f) return (float)kVeryLarge;
+  if (r2 < P.f_lj_rc2[k]) {
+    float s2 = __fdividef(P.f_lj_sig2[k], r2);
+    float s6 = s2 * s2 * s2;
+    return P.f_lj_eps4[k] * (s6 * s6 - s6) - P.f_lj_eref[k];
+  }
+  return 0.0f;
+}
+
+__device__ __forceinline__ float real_images32(const DevParams& P, float dx, float dy,
+                                               float dz) {
+  float e = 0.0f;
+  const float rc = P.f_real_cut;
+  for (int a = -P.real_cell[0]; a <= P.real_cell[0]; a++) {
+    float x = dx + a * P.f_box[0];
+    if (fabsf(x) > rc) continue;
+    for (int b = -P.real_cell[1]; b <= P.real_cell[1]; b++) {
+      float y = dy + b * P.f_box[1];
+      if (fabsf(y) > rc) continue;
+      for (int c = -P.real_cell[2]; c <= P.real_cell[2]; c++) {
+        float z = dz + c * P.f_box[2];
+        if (fabsf(z) > rc) continue;
+        float r2 = x * x + y * y + z * z;
+        if (r2 > 0.0f) {
+          float ir = rsqrtf(r2);
+          float r = r2 * ir;
+          if (r <= rc) e += erfcf(P.f_sqrt_alpha * r) * ir;
+        }
+      }
+    }
+  }
+  return e;
+}
+
+__device__ __forceinline__ void pair32(const DevParams& P, int4 a, float qa, int4 b,
+                                       float qb, float& lj, float& re) {
+  const float dx = fdiff(a.x, b.x, P.f_scale[0]);
+  const float dy = fdiff(a.y, b.y, P.f_scale[1]);
+  const float dz = fdiff(a.z, b.z, P.f_scale[2]);
+  if (P.use_pair) lj += lj32(P, a.w * P.n_type + b.w, dx * dx + dy * dy + dz * dz);
+  if (P.use_ewald) {
+    const float qq = qa * qb;
+    if (qq != 0.0f) re += P.f_lB * qq * real_images32(P, dx, dy, dz);
+  }
+}
+
+template <int NT>
+__device__ __forceinline__ float block_sum32(float v, float* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  float t = 0.0f;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < NT / 32; i++) t += sh[i];
+  return t;
+}
+
+// Exact per-entry table: e^{i 2 pi n X / 2^32}, n = 0..kmax, q folded into x.
+__device__ __forceinline__ void table32(const DevParams& P, int4 f, float q, int axis,
+                                        float2* tab) {
+  const unsigned X = (unsigned)(axis == 0 ? f.x : (axis == 1 ? f.y : f.z));
+  float2* t = tab + P.koff[axis];
+  const float w = axis == 0 ? q : 1.0f;
+  for (int n = 0; n <= P.kmax[axis]; n++) {
+    unsigned ph = X * (unsigned)n;
+    float s, c;
+    sincospif((float)(int)ph * 4.6566128730773926e-10f, &s, &c);  // * 2^-31
+    t[n] = make_float2(w * c, w * s);
+  }
+}
+
+__device__ __forceinline__ float2 cmul32(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__device__ __forceinline__ float2 phase32(const DevParams& P, const float2* tab, short4 k) {
+  float2 ex = tab[P.koff[0] + k.x];
+  float2 ey = tab[P.koff[1] + (k.y >= 0 ? k.y : -k.y)];
+  if (k.y < 0) ey.y = -ey.y;
+  float2 ez = tab[P.koff[2] + (k.z >= 0 ? k.z : -k.z)];
+  if (k.z < 0) ez.y = -ez.y;
+  return cmul32(cmul32(ex, ey), ez);
+}
+
+__global__ void __launch_bounds__(kPairThreads)
+    k_delta32(const DevParams P, const DevBuffers B) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float red[kPairThreads / 32];
+  __shared__ int s_last;
+  const DevState* st = B.state;
+  const int b_lo = st->b_lo, b_hi = st->b_hi;
+  const int m = st->pending ? b_hi - b_lo : 0;
+  const int N = P.n_bead;
+
+  float acc_lj = 0.0f, acc_re = 0.0f;
+  if (P.use_pair || P.use_ewald) {
+    // pair p = ii * N + j, dealt with stride G; (ii, j) advanced without a
+    // division per pair
+    const long long total = (long long)m * N;
+    const long long G = (long long)gridDim.x * blockDim.x;
+    const long long p0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int gq = (int)(G / N), gr = (int)(G % N);
+    int ii = (int)(p0 / N), j = (int)(p0 % N);
+    for (long long p = p0; p < total; p += G, ii += gq, j += gr) {
+      if (j >= N) {
+        j -= N;
+        ii++;
+      }
+      const int i = b_lo + ii;
+      const bool jm = j >= b_lo && j < b_hi;
+      if (jm && j <= i) continue;
+      const int4 ti = B.ftrial[ii], ci = B.fpos[i];
+      const float qi = B.fq[i], qj = B.fq[j];
+      const int4 cj = B.fpos[j];
+      const int4 tj = jm ? B.ftrial[j - b_lo] : cj;
+      float l1 = 0, r1 = 0, l0 = 0, r0 = 0;
+      pair32(P, ti, qi, tj, qj, l1, r1);
+      pair32(P, ci, qi, cj, qj, l0, r0);
+      acc_lj += l1 - l0;
+      acc_re += r1 - r0;
+    }
+  }
+  float t0 = block_sum32<kPairThreads>(acc_lj, red);
+  float t1 = block_sum32<kPairThreads>(acc_re, red);
+  if (threadIdx.x == 0) {
+    B.partial[4 * blockIdx.x + 0] = (double)t0;
+    B.partial[4 * blockIdx.x + 1] = (double)t1;
+  }
+
+  if (!P.use_ewald || m == 0) return;
+  const int chunk = P.kchunk_delta;
+  const int n_groups = (m + chunk - 1) / chunk;
+  const int n_tiles = (P.n_k + kKTile32 - 1) / kKTile32;
+  const int n_items = n_tiles * n_groups;
+  float2* tabs = reinterpret_cast<float2*>(smem);  // [chunk][2][kper]
+  const int per = P.kper;
+  for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+    const int tile = item % n_tiles, grp = item / n_tiles;
+    const int c0 = b_lo + grp * chunk;
+    const int cnt = min(chunk, b_hi - c0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < cnt * 6; t += blockDim.x) {
+      int bead = t / 6, which = (t / 3) & 1, axis = t % 3;
+      int4 f = which ? B.fpos[c0 + bead] : B.ftrial[c0 - b_lo + bead];
+      table32(P, f, B.fq[c0 + bead], axis, tabs + (bead * 2 + which) * per);
+    }
+    __syncthreads();
+    const int k = tile * kKTile32 + threadIdx.x;
+    const bool mine = threadIdx.x < kKTile32 && k < P.n_k;
+    if (mine) {
+      const short4 kv = B.kn[k];
+      float2 ds = make_float2(0.0f, 0.0f);
+      for (int b = 0; b < cnt; b++) {
+        float2 e1 = phase32(P, tabs + (b * 2 + 0) * per, kv);
+        float2 e0 = phase32(P, tabs + (b * 2 + 1) * per, kv);
+        ds.x += e1.x - e0.x;
+        ds.y += e1.y - e0.y;
+      }
+      B.dsk_part32[(size_t)grp * P.n_k + k] = ds;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&B.ktile_count[tile], 1) == n_groups - 1;
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      float e = 0.0f;
+      if (mine) {
+        float2 ds = make_float2(0.0f, 0.0f);
+        for (int g = 0; g < n_groups; g++) {
+          float2 v = __ldcg(&B.dsk_part32[(size_t)g * P.n_k + k]);
+          ds.x += v.x;
+          ds.y += v.y;
+        }
+        B.dsk[k] = make_double2((double)ds.x, (double)ds.y);
+        double2 s = B.sk[k];
+        float sx = (float)s.x, sy = (float)s.y;
+        e = (float)B.kw[k] * (2.0f * (sx * ds.x + sy * ds.y) + (ds.x * ds.x + ds.y * ds.y));
+      }
+      e = block_sum32<kPairThreads>(e, red);
+      if (threadIdx.x == 0) {
+        B.kpartial[tile] = (double)e;
+        B.ktile_count[tile] = 0;
+      }
+    }
+  }
+}
+
+static int g_grid32 = 0;
+int pair_grid32() {
+  if (g_grid32 == 0) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    g_grid32 = 4 * (sms > 0 ? sms : 152);
+  }
+  return g_grid32;
+}
+
+void launch_delta_pairs32(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_delta32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kKTableBytes + 4096);
+    attr = true;
+  }
+  size_t smem = P.use_ewald ? (size_t)P.kchunk_delta * 2 * P.kper * sizeof(float2) : 0;
+  k_delta32<<<pair_grid32(), kPairThreads, smem, s>>>(P, B);
+}
+
+__global__ void k_fix_all(const DevParams P, const DevBuffers B) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n_bead; i += gridDim.x * blockDim.x) {
+    double4_32a p = B.pos[i];
+    B.fpos[i] = fix_point(P, p, B.type[i]);
+    B.fq[i] = (float)p.w;
+  }
+}
+
+__global__ void k_fix_trial(const DevParams P, const DevBuffers B) {
+  const DevState* st = B.state;
+  for (int i = st->b_lo + threadIdx.x; i < st->b_hi; i += blockDim.x)
+    B.ftrial[i - st->b_lo] = fix_point(P, B.trial[i], B.type[i]);
+}
+
+void launch_fix_all(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
+  k_fix_all<<<(P.n_bead + 255) / 256, 256, 0, s>>>(P, B);
+}
+
+void launch_fix_trial(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
+  k_fix_trial<<<1, 256, 0, s>>>(P, B);
+}
+
+}  // namespace plum

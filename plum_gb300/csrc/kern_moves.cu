@@ -1,0 +1,629 @@
+// Serial part of a Monte Carlo step (one CTA):
+//
+//   finish  adds the per-block partials of k_delta64 in a fixed order, adds
+//           the wall (potential_external.cc:100-117) and bond
+//           (potential_spring.cc:63-80) terms, and composes dE exactly as
+//           ForceField::EnergyDifference does (force_field.cc:407-434): pair,
+//           early return at >= 1e8, external, early return, Ewald (real +
+//           reciprocal + the dipole term from the *current* z, which is what
+//           the reference evaluates at potential_ewald.cc:527-531), bond.
+//   decide  one draw u; accept if dE < 1e8 and u < exp(-beta dE); no draw at
+//           dE >= 1e8 (simulation.cc:324-332)
+//   commit  trial -> current, S(k) += dS(k), running totals
+//           (force_field.cc:436-451, simulation.cc:336-351)
+//   gen     the next step's draws in the reference's order: one draw for the
+//           GC check (simulation.cc:221), chain and ion picks, move type
+//           (simulation.cc:247-276), then the move itself (molecule.cc:103-312)
+//
+// Build note: this file is compiled with -fmad=false. The draw-consuming
+// tests (randSphere's r1^2 + r2^2 > 1, the move-type and pick thresholds)
+// must round exactly like the reference or the draw sequence would diverge.
+#include "engine.h"
+
+namespace plum {
+
+__device__ double wall_energy64(const DevParams& P, double z, int ty);
+
+struct Draws {
+  const uint32_t* g;
+  const uint32_t* win;
+  long long pos, len, wbase;
+  int wlen;
+  int overrun;
+  __device__ uint32_t next() {
+    if (pos >= len) {
+      overrun = 1;
+      return 0u;
+    }
+    long long o = pos - wbase;
+    uint32_t v = (o >= 0 && o < wlen) ? win[o] : g[pos];
+    pos++;
+    return v;
+  }
+  __device__ double u() { return (double)next() / kMtMax; }
+  __device__ uint32_t at(long long o) const {
+    long long w = o - wbase;
+    return (w >= 0 && w < wlen) ? win[w] : g[o];
+  }
+};
+
+// randSphere (misc.cc:95-109) rejects the pair (u1, u2) while
+// r1^2 + r2^2 > 1 with r = 1 - 2 u / M, M = 2^32 - 1. In exact arithmetic
+// that is (M - 2 u1)^2 + (M - 2 u2)^2 > M^2, decided here in 64-bit integers.
+// The reference decides it in FP64, whose rounding can only matter within a
+// few ulps of the unit circle; there (|difference| < 2^26 of M^2 ~ 1.8e19)
+// the reference's own FP64 expression decides.
+__device__ __forceinline__ bool sphere_reject(uint32_t u1, uint32_t u2) {
+  const long long M = 4294967295LL;
+  long long a = M - 2LL * (long long)u1, b = M - 2LL * (long long)u2;
+  unsigned long long a2 = (unsigned long long)(a < 0 ? -a : a);
+  unsigned long long b2 = (unsigned long long)(b < 0 ? -b : b);
+  a2 *= a2;
+  b2 *= b2;
+  const unsigned long long M2 = 18446744065119617025ull;  // (2^32 - 1)^2
+  const unsigned long long rhs = M2 - b2;
+  const unsigned long long diff = a2 > rhs ? a2 - rhs : rhs - a2;
+  if (diff > (1ull << 26)) return a2 > rhs;
+  double r1 = 1.0 - 2.0 * ((double)u1 / kMtMax);
+  double r2 = 1.0 - 2.0 * ((double)u2 / kMtMax);
+  return r1 * r1 + r2 * r2 > 1.0;
+}
+
+// Consumes randSphere's draws; returns the stream index of the accepted pair.
+__device__ long long sphere_scan(Draws& d) {
+  for (int guard = 0; guard < (1 << 20); guard++) {
+    long long o = d.pos;
+    uint32_t u1 = d.next(), u2 = d.next();
+    if (d.overrun) return -1;
+    if (!sphere_reject(u1, u2)) return o;
+  }
+  d.overrun = 1;
+  return -1;
+}
+
+// The unit vector randSphere returns for an accepted pair.
+__device__ void sphere_vec(uint32_t u1, uint32_t u2, double* v) {
+  double r1 = 1.0 - 2.0 * ((double)u1 / kMtMax);
+  double r2 = 1.0 - 2.0 * ((double)u2 / kMtMax);
+  double rs = r1 * r1 + r2 * r2;
+  double ranh = 2.0 * sqrt(1.0 - rs);
+  v[0] = r1 * ranh;
+  v[1] = r2 * ranh;
+  v[2] = (1.0 - 2.0 * rs);
+}
+
+__device__ void rand_sphere(Draws& d, double* v) {
+  long long o = sphere_scan(d);
+  if (o < 0) {
+    v[0] = v[1] = 0.0;
+    v[2] = 1.0;
+    return;
+  }
+  sphere_vec(d.at(o), d.at(o + 1), v);
+}
+
+template <int NT>
+__device__ __forceinline__ double bsum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int i = 0; i < NT / 32; i++) t += sh[i];
+  __syncthreads();
+  return t;  // valid in every thread
+}
+
+struct GenPlan {
+  int type;      // move type, -1 none
+  int mol, b0, b1, b_lo, b_hi;
+  double vec[3];  // COM shift / reptation end step
+  double R[9];    // crankshaft rotation
+  int first;      // crankshaft first bead (molecule-relative)
+  int dir;        // reptation direction
+  int end;        // reptation end bead (molecule-relative)
+  double s;       // pivot displacement size
+  int pivot;      // pivot bead (molecule-relative); -1: generated sequentially
+};
+
+constexpr int kPivotMax = 512;  // chains up to this length pivot in parallel
+
+__global__ void __launch_bounds__(kSerialThreads)
+    k_serial64(const DevParams P, const DevBuffers B, int mode, int n_partial, int n_ktiles) {
+  __shared__ uint32_t win[kDrawWindow];
+  __shared__ double red[kSerialThreads / 32];
+  __shared__ GenPlan plan;
+  __shared__ int s_accept, s_ext_bad;
+  __shared__ int s_off[kPivotMax], s_boff[kPivotMax];  // draw offsets per bead
+  __shared__ double s_w[3][kPivotMax];                 // pivot bond steps
+  DevState* st = B.state;
+  if (st->error) return;
+
+  // Stage the next stream words.
+  const long long wbase = st->stream_pos;
+  int wlen = 0;
+  if (mode & (kModeDecide | kModeGen)) {
+    long long avail = st->stream_len - wbase;
+    wlen = (int)(avail < kDrawWindow ? (avail > 0 ? avail : 0) : kDrawWindow);
+    for (int i = threadIdx.x; i < wlen; i += blockDim.x) win[i] = B.stream[wbase + i];
+  }
+  __syncthreads();
+  Draws d{B.stream, win, wbase, st->stream_len, wbase, wlen, 0};
+
+  const int pending = st->pending;
+  const int b_lo = st->b_lo, b_hi = st->b_hi, mol = st->mol;
+
+  if ((mode & kModeFinish) && pending) {
+    // 1. fixed-order reduction of the block partials
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int i = threadIdx.x; i < n_partial; i += blockDim.x) {
+      a += B.partial[4 * i];
+      b += B.partial[4 * i + 1];
+    }
+    if (P.use_ewald && b_hi > b_lo)
+      for (int i = threadIdx.x; i < n_ktiles; i += blockDim.x) c += B.kpartial[i];
+    double de_lj = bsum<kSerialThreads>(a, red);
+    double de_re = bsum<kSerialThreads>(b, red);
+    double de_k = bsum<kSerialThreads>(c, red);
+    // 2. walls of the moved beads, sum q dz
+    if (threadIdx.x == 0) s_ext_bad = 0;
+    __syncthreads();
+    double ext = 0.0, dmz = 0.0;
+    for (int i = b_lo + threadIdx.x; i < b_hi; i += blockDim.x) {
+      double4_32a t = B.trial[i], p = B.pos[i];
+      if (P.use_ext) {
+        int ty = B.type[i];
+        double en = wall_energy64(P, t.z, ty);
+        if (en >= kVeryLarge) s_ext_bad = 1;
+        ext += en - wall_energy64(P, p.z, ty);
+      }
+      dmz += t.w * (t.z - p.z);
+    }
+    ext = bsum<kSerialThreads>(ext, red);
+    dmz = bsum<kSerialThreads>(dmz, red);
+    // 3. bonds of the moved molecule at trial positions
+    const int m0 = B.mol_start[mol], m1 = B.mol_start[mol + 1];
+    double bt = 0.0;
+    if (P.use_bond && m1 - m0 > 1)
+      for (int i = m0 + threadIdx.x; i < m1 - 1; i += blockDim.x) {
+        double4_32a p = B.trial[i], q = B.trial[i + 1];
+        double dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        double r = sqrt(dx * dx + dy * dy + dz * dz);
+        bt += 0.5 * P.k_bond * (r - P.r0) * (r - P.r0);
+      }
+    bt = bsum<kSerialThreads>(bt, red);
+    if (threadIdx.x == 0) {
+      double de = 0.0, dp = 0.0, dx = 0.0, dw = 0.0, db = 0.0;
+      double dip_t = st->dipl_cur;
+      bool done = false;
+      if (P.use_pair) {
+        dp = de_lj;
+        de += dp;
+        done = de >= kVeryLarge;
+      }
+      if (!done && P.use_ext) {
+        dx = s_ext_bad ? kVeryLarge : ext;
+        de += dx;
+        done = de >= kVeryLarge;
+      }
+      if (!done && P.use_ewald) {
+        dw = de_re + P.kpref * de_k;
+        if (P.dipole) {
+          dip_t = P.dip_coef * st->mz * st->mz;
+          dw += dip_t - st->dipl_cur;
+        }
+        de += dw;
+      }
+      if (!done && P.use_bond && m1 - m0 > 1) {
+        db = bt - B.bond_mol[mol];
+        de += db;
+      }
+      if (!isfinite(de)) st->n_nonfinite++;  // flagged, rejected as the reference does
+      st->de = de;
+      st->de_pair = dp;
+      st->de_ext = dx;
+      st->de_ewald = dw;
+      st->de_bond = db;
+      st->bond_trial = bt;
+      st->dipl_trial = dip_t;
+      st->dmz = dmz;
+    }
+    __syncthreads();
+  }
+
+  // Metropolis (simulation.cc:324-332) or the host's decision.
+  if ((mode & (kModeDecide | kModeCommit)) && pending) {
+    if (threadIdx.x == 0) {
+      int acc = 0;
+      if (mode & kModeDecide) {
+        if (!(st->de >= kVeryLarge)) acc = d.u() < exp(-P.beta * st->de);  // a NaN dE still draws
+        if (d.overrun) st->error = PLUM_ERR_STREAM_DEV;
+      } else {
+        acc = st->last_accept;
+      }
+      s_accept = acc;
+    }
+    __syncthreads();
+    const int acc = s_accept;
+    if (acc) {
+      for (int i = b_lo + threadIdx.x; i < b_hi; i += blockDim.x) {
+        B.pos[i] = B.trial[i];
+        if (P.form) B.fpos[i] = B.ftrial[i - b_lo];
+      }
+      if (P.use_ewald && b_hi > b_lo)
+        for (int k = threadIdx.x; k < P.n_k; k += blockDim.x) {
+          double2 s = B.sk[k], ds = B.dsk[k];
+          B.sk[k] = make_double2(s.x + ds.x, s.y + ds.y);
+        }
+    } else {
+      for (int i = b_lo + threadIdx.x; i < b_hi; i += blockDim.x) B.trial[i] = B.pos[i];
+    }
+    if (threadIdx.x == 0) {
+      if (acc) {
+        st->e_pair += st->de_pair;
+        st->e_ext += st->de_ext;
+        st->e_ewald += st->de_ewald;
+        st->e_bond += st->de_bond;
+        st->mz += st->dmz;
+        if (P.dipole) st->dipl_cur = st->dipl_trial;
+        if (P.use_bond && B.mol_start[mol + 1] - B.mol_start[mol] > 1)
+          B.bond_mol[mol] = st->bond_trial;
+        st->n_accept++;
+      }
+      st->last_accept = acc;
+      st->pending = 0;
+    }
+  }
+  // Per-step log (also for steps where nothing was attempted).
+  if ((mode & kModeDecide) && st->step_open && threadIdx.x == 0) {
+    int s = st->step;
+    if (B.log_type) B.log_type[s] = pending ? st->move_type : -1;
+    if (B.log_accept) B.log_accept[s] = pending ? st->last_accept : 0;
+    if (B.log_etot) B.log_etot[s] = st->e_pair + st->e_ewald + st->e_bond + st->e_ext;
+    st->step = s + 1;
+    st->step_open = 0;
+  }
+  __syncthreads();
+
+  if (!(mode & kModeGen) || st->error) {
+    if (threadIdx.x == 0) st->stream_pos = d.pos;
+    return;
+  }
+
+  // ----------------------------------------------------- generate next move
+  if (threadIdx.x == 0) {
+    plan.type = -1;
+    st->step_open = 1;
+    (void)d.next();  // simulation.cc:221 (the GC draw)
+    const int n_ch = P.n_chain_total, n_io = P.n_ion_total;
+    if (P.n_mol - P.phantom > 0) {
+      int wc = (int)floor((double)d.next() / kMtMax * n_ch);
+      int wi = (int)floor((double)d.next() / kMtMax * n_io);
+      if (wc == n_ch) wc--;
+      if (wi == n_io) wi--;
+      int chain_id = (wc >= 0 && wc < n_ch) ? B.chain_ids[wc] : -1;
+      int ion_id = (wi >= 0 && wi < n_io) ? B.ion_ids[wi] : -1;
+      int mt = 0;
+      double u = (double)d.next() / kMtMax;
+      double cur = P.move_prob[0];
+      while (cur < u && mt < 4) {
+        mt++;
+        cur += P.move_prob[mt];
+      }
+      if (cur < u) mt++;
+      if (mt > 4) mt = 4;
+      int molid = -1;
+      if (mt == 0 && n_io > 0)
+        molid = ion_id;
+      else if (n_ch > 0)
+        molid = chain_id;
+      const bool attempted = (mt == 0 && n_io > 0) || (mt > 0 && n_ch > 0);
+      if (attempted && molid >= 0) {
+        const int b0 = B.mol_start[molid], b1 = B.mol_start[molid + 1];
+        const int len = b1 - b0;
+        plan.mol = molid;
+        plan.b0 = b0;
+        plan.b1 = b1;
+        plan.b_lo = b0;
+        plan.b_hi = b1;
+        plan.type = mt;
+        if (mt == 0) {
+          // Molecule::BeadTranslate (molecule.cc:103-133)
+          double v[3];
+          rand_sphere(d, v);
+          double vl = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+          if (vl > 0) vl = 3 * P.move_size / vl;
+          for (int a = 0; a < 3; a++) plan.vec[a] = vl * v[a];
+          plan.b_hi = b0 + 1;
+        } else if (mt == 1) {
+          // Molecule::COMTranslate (molecule.cc:135-151)
+          for (int a = 0; a < 3; a++) plan.vec[a] = 0.5 * P.move_size * (double)d.next() / kMtMax;
+          for (int a = 0; a < 3; a++)
+            if (d.next() % 2u == 0u) plan.vec[a] = -plan.vec[a];
+        } else if (mt == 2) {
+          // Molecule::Pivot (molecule.cc:153-237). Bead i's new position is
+          // the previous one plus bl_i * unit(old_i - old_prev + s v_i): the
+          // reference's running translation of the chain tail cancels out of
+          // the bond direction. Thread 0 only locates each bead's draws; the
+          // geometry and the running sum are done by the block below.
+          int pivot = (int)floor(len * (double)d.next() / kMtMax);
+          if (pivot == len) pivot--;
+          double s = P.move_size * (double)d.next() / kMtMax;
+          plan.s = s;
+          plan.pivot = pivot;
+          if (len <= kPivotMax) {
+            for (int dirn = 0; dirn < 2; dirn++) {
+              int i = dirn == 0 ? pivot + 1 : pivot - 1;
+              for (; dirn == 0 ? i < len : i >= 0; i += dirn == 0 ? 1 : -1) {
+                long long o = sphere_scan(d);
+                s_off[i] = (int)(o - wbase);
+                if (P.vary_bond) {
+                  s_boff[i] = (int)(d.pos - wbase);
+                  (void)d.next();
+                }
+                if (d.overrun) break;
+              }
+            }
+          } else {
+            plan.pivot = -1;
+            const double eq = P.bond_len;
+            for (int dirn = 0; dirn < 2; dirn++) {
+              double T[3] = {0.0, 0.0, 0.0};
+              double4_32a pv = B.pos[b0 + pivot];
+              double prev[3] = {pv.x, pv.y, pv.z};
+              int i = dirn == 0 ? pivot + 1 : pivot - 1;
+              for (; dirn == 0 ? i < len : i >= 0; i += dirn == 0 ? 1 : -1) {
+                double v[3];
+                rand_sphere(d, v);
+                double4_32a o = B.pos[b0 + i];
+                double p[3] = {o.x + T[0], o.y + T[1], o.z + T[2]};
+                double dx = (p[0] + s * v[0]) - prev[0];
+                double dy = (p[1] + s * v[1]) - prev[1];
+                double dz = (p[2] + s * v[2]) - prev[2];
+                double bl = eq;
+                if (P.vary_bond) bl += (eq / 5.0) * ((double)d.next() / kMtMax - 0.5);
+                double norm = bl / sqrt(dx * dx + dy * dy + dz * dz);
+                double c[3] = {norm * dx + prev[0], norm * dy + prev[1], norm * dz + prev[2]};
+                for (int a = 0; a < 3; a++) {
+                  T[a] += c[a] - p[a];
+                  prev[a] = c[a];
+                }
+                B.trial[b0 + i] = make_double4_32a(c[0], c[1], c[2], o.w);
+                if (d.overrun) break;
+              }
+            }
+          }
+        } else if (mt == 3) {
+          // Molecule::Crankshaft (molecule.cc:239-265); Rodrigues rotation in
+          // the per-entry grouping of Eigen's AngleAxis::toRotationMatrix.
+          int first = (int)floor((len - 2) * (double)d.next() / kMtMax);
+          int last = (int)floor((len - first) * (double)d.next() / kMtMax) + first;
+          if (last > len - 1) last = len - 1;  // the reference reads past the chain here
+          double4_32a pf = B.pos[b0 + first], pl = B.pos[b0 + last];
+          double ax[3] = {pl.x - pf.x, pl.y - pf.y, pl.z - pf.z};
+          double z2 = ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2];
+          if (z2 > 0) {
+            double n = sqrt(z2);
+            for (int a = 0; a < 3; a++) ax[a] /= n;
+          }
+          const double pi_libm = 3.14159265358979323846;
+          double ang = P.move_size * ((double)d.next() / kMtMax * 2 * pi_libm - pi_libm);
+          double sn, cs;
+          sincos(ang, &sn, &cs);
+          double sa[3] = {sn * ax[0], sn * ax[1], sn * ax[2]};
+          double ca[3] = {(1.0 - cs) * ax[0], (1.0 - cs) * ax[1], (1.0 - cs) * ax[2]};
+          double t = ca[0] * ax[1];
+          plan.R[1] = t - sa[2];
+          plan.R[3] = t + sa[2];
+          t = ca[0] * ax[2];
+          plan.R[2] = t + sa[1];
+          plan.R[6] = t - sa[1];
+          t = ca[1] * ax[2];
+          plan.R[5] = t - sa[0];
+          plan.R[7] = t + sa[0];
+          for (int a = 0; a < 3; a++) plan.R[4 * a] = ca[a] * ax[a] + cs;
+          plan.first = first;
+          plan.b_lo = b0 + first + 1;
+          plan.b_hi = b0 + (last > first + 1 ? last : first + 1);
+        } else {
+          // Molecule::RandomReptation (molecule.cc:267-312)
+          double bl = P.bond_len;
+          if (P.vary_bond) bl += (P.bond_len / 5.0) * ((double)d.next() / kMtMax - 0.5);
+          int dir = 1, end = len - 1;
+          if (d.next() % 2u == 0u) {
+            dir = -1;
+            end = 0;
+          }
+          double v[3];
+          rand_sphere(d, v);
+          double vl = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+          for (int a = 0; a < 3; a++) plan.vec[a] = bl * v[a] / vl;
+          plan.dir = dir;
+          plan.end = end;
+        }
+      }
+    }
+    if (d.overrun) {
+      st->error = PLUM_ERR_STREAM_DEV;
+      plan.type = -1;
+    }
+    st->stream_pos = d.pos;
+  }
+  __syncthreads();
+  // Apply the plan in parallel (pivot already wrote its trial positions).
+  const GenPlan g = plan;
+  if (g.type == 0 || g.type == 1) {
+    for (int i = g.b_lo + threadIdx.x; i < g.b_hi; i += blockDim.x) {
+      double4_32a o = B.pos[i];
+      B.trial[i] = make_double4_32a(o.x + g.vec[0], o.y + g.vec[1], o.z + g.vec[2], o.w);
+    }
+  } else if (g.type == 3) {
+    const double4_32a pf = B.pos[g.b0 + g.first];
+    for (int i = g.b_lo + threadIdx.x; i < g.b_hi; i += blockDim.x) {
+      double4_32a o = B.pos[i];
+      double v[3] = {o.x - pf.x, o.y - pf.y, o.z - pf.z};
+      double r[3];
+      for (int a = 0; a < 3; a++)
+        r[a] = ((g.R[3 * a] * v[0] + g.R[3 * a + 1] * v[1]) + g.R[3 * a + 2] * v[2]);
+      B.trial[i] = make_double4_32a(r[0] + pf.x, r[1] + pf.y, r[2] + pf.z, o.w);
+    }
+  } else if (g.type == 2 && g.pivot >= 0) {
+    const int len = g.b1 - g.b0, pv = g.pivot;
+    const double eq = P.bond_len;
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+      if (i == pv) continue;
+      const int j = i > pv ? i - 1 : i + 1;
+      double v[3];
+      sphere_vec(d.at(wbase + s_off[i]), d.at(wbase + s_off[i] + 1), v);
+      double bl = eq;
+      if (P.vary_bond) bl += (eq / 5.0) * ((double)d.at(wbase + s_boff[i]) / kMtMax - 0.5);
+      const double4_32a oi = B.pos[g.b0 + i], oj = B.pos[g.b0 + j];
+      double dx = (oi.x - oj.x) + g.s * v[0];
+      double dy = (oi.y - oj.y) + g.s * v[1];
+      double dz = (oi.z - oj.z) + g.s * v[2];
+      double norm = bl / sqrt(dx * dx + dy * dy + dz * dz);
+      // scan slot: forward beads first (pivot+1 ..), then backward (pivot-1 ..)
+      const int k = i > pv ? i - pv - 1 : (len - 1 - pv) + (pv - 1 - i);
+      s_w[0][k] = norm * dx;
+      s_w[1][k] = norm * dy;
+      s_w[2][k] = norm * dz;
+    }
+    // Inclusive running sums within the two segments (Hillis-Steele).
+    const int nf = len - 1 - pv, n = len - 1;
+    for (int off = 1; off < n; off <<= 1) {
+      __syncthreads();
+      double add[3][2];
+      for (int r = 0; r < 2; r++) {
+        int k = threadIdx.x + r * blockDim.x;
+        bool ok = k < n && (k < nf ? k - off >= 0 : k - off >= nf);
+        for (int a = 0; a < 3; a++) add[a][r] = ok ? s_w[a][k - off] : 0.0;
+      }
+      __syncthreads();
+      for (int r = 0; r < 2; r++) {
+        int k = threadIdx.x + r * blockDim.x;
+        if (k < n)
+          for (int a = 0; a < 3; a++) s_w[a][k] += add[a][r];
+      }
+    }
+    __syncthreads();
+    const double4_32a pp = B.pos[g.b0 + pv];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      const int i = k < nf ? pv + 1 + k : pv - 1 - (k - nf);
+      const double q = B.pos[g.b0 + i].w;
+      B.trial[g.b0 + i] =
+          make_double4_32a(pp.x + s_w[0][k], pp.y + s_w[1][k], pp.z + s_w[2][k], q);
+    }
+  } else if (g.type == 4) {
+    const int len = g.b1 - g.b0;
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+      double4_32a nw;
+      if (i == g.end) {
+        double4_32a o = B.pos[g.b0 + i];
+        nw = make_double4_32a(o.x + g.vec[0], o.y + g.vec[1], o.z + g.vec[2], o.w);
+      } else {
+        double4_32a o = B.pos[g.b0 + i + g.dir];
+        nw = make_double4_32a(o.x, o.y, o.z, B.pos[g.b0 + i].w);
+      }
+      B.trial[g.b0 + i] = nw;
+    }
+  }
+  if (P.form && g.type >= 0) {
+    // fixed-point trial coordinates for the precision form's pair sweep
+    __syncthreads();
+    for (int i = g.b_lo + threadIdx.x; i < g.b_hi; i += blockDim.x)
+      B.ftrial[i - g.b_lo] = fix_point(P, B.trial[i], B.type[i]);
+  }
+  if (threadIdx.x == 0) {
+    if (g.type >= 0) {
+      st->pending = 1;
+      st->mol = g.mol;
+      st->b_lo = g.b_lo;
+      st->b_hi = g.b_hi;
+      st->move_type = g.type;
+    } else {
+      st->pending = 0;
+    }
+  }
+}
+
+void launch_serial64(const DevParams& P, const DevBuffers& B, int mode, cudaStream_t s) {
+  k_serial64<<<1, kSerialThreads, 0, s>>>(P, B, mode, P.form ? pair_grid32() : pair_grid(),
+                                           ktile_count(P));
+}
+
+__global__ void k_set_move(DevState* st, int mol, int b_lo, int b_hi) {
+  st->pending = 1;
+  st->mol = mol;
+  st->b_lo = b_lo;
+  st->b_hi = b_hi;
+  st->move_type = -1;
+}
+
+void launch_set_move(const DevBuffers& B, int mol, int b_lo, int b_hi, cudaStream_t s) {
+  k_set_move<<<1, 1, 0, s>>>(B.state, mol, b_lo, b_hi);
+}
+
+// ------------------------------------------------------------ mt19937 fill
+// One block regenerates the 624-word state in the three data-independent
+// phases of the MT19937 recurrence (i < 227 reads only old words; i < 454
+// reads new words of phase one; the rest reads phase-two words), then
+// tempers. state[624] holds the output index as in std::mt19937.
+__device__ __forceinline__ uint32_t mt_twist(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t y = (a & 0x80000000u) | (b & 0x7fffffffu);
+  uint32_t v = c ^ (y >> 1);
+  if (y & 1u) v ^= 0x9908b0dfu;
+  return v;
+}
+
+__global__ void __launch_bounds__(1024) k_mt_fill(uint32_t* state, uint32_t* out,
+                                                  long long n) {
+  __shared__ uint32_t mt[624], old[624];
+  for (int i = threadIdx.x; i < 624; i += blockDim.x) mt[i] = state[i];
+  __shared__ int idx;
+  if (threadIdx.x == 0) idx = (int)state[624];
+  __syncthreads();
+  long long w = 0;
+  while (w < n) {
+    if (idx >= 624) {
+      for (int i = threadIdx.x; i < 624; i += blockDim.x) old[i] = mt[i];
+      __syncthreads();
+      for (int i = threadIdx.x; i < 227; i += blockDim.x)
+        mt[i] = mt_twist(old[i], old[i + 1], old[i + 397]);
+      __syncthreads();
+      for (int i = 227 + threadIdx.x; i < 454; i += blockDim.x)
+        mt[i] = mt_twist(old[i], old[i + 1], mt[i - 227]);
+      __syncthreads();
+      for (int i = 454 + threadIdx.x; i < 623; i += blockDim.x)
+        mt[i] = mt_twist(old[i], old[i + 1], mt[i - 227]);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        mt[623] = mt_twist(old[623], mt[0], mt[396]);
+        idx = 0;
+      }
+      __syncthreads();
+    }
+    long long take = 624 - idx;
+    if (take > n - w) take = n - w;
+    for (int i = threadIdx.x; i < take; i += blockDim.x) {
+      uint32_t y = mt[idx + i];
+      y ^= y >> 11;
+      y ^= (y << 7) & 0x9d2c5680u;
+      y ^= (y << 15) & 0xefc60000u;
+      y ^= y >> 18;
+      out[w + i] = y;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) idx += (int)take;
+    w += take;
+    __syncthreads();
+  }
+  for (int i = threadIdx.x; i < 624; i += blockDim.x) state[i] = mt[i];
+  if (threadIdx.x == 0) state[624] = (uint32_t)idx;
+}
+
+void launch_mt_fill(uint32_t* state, uint32_t* out, long long n, cudaStream_t s) {
+  if (n > 0) k_mt_fill<<<1, 1024, 0, s>>>(state, out, n);
+}
+
+}  // namespace plum

@@ -292,3 +292,110 @@ def write_bulk(dirpath: str, spec: BulkSpec, seed: int, runin="run.in", **over) 
     with open(os.path.join(dirpath, runin), "w") as f:
         f.write(runin_text(**kw))
     return os.path.join(dirpath, runin)
+
+
+@dataclasses.dataclass
+class BrushSpec:
+    """One confined replica: end-grafted chains between walls at z=0 and z=H."""
+    n_graft: int = 16
+    chain_len: int = 20
+    lxy: float = 32.0
+    height: float = 40.0
+    charge_frac: float = 0.5     # probability that a chain bead carries -1
+    n_sites: int = 64            # LJ surface sites per wall (phantom molecules)
+    graft_z: float = 1.0
+    wall_cut: float = -1.0       # <0: purely repulsive 9-3 wall
+    lj_cutoff: float = 2.5
+    lB: float = 3.0
+    alpha_times_L: float = 5.0   # alpha = (alpha_times_L / lxy)^2
+    k_bond: float = 400.0
+    r0: float = 1.0
+    move_size: float = 1.0
+    move_prob: tuple = (0.3, 0.1, 0.2, 0.2, 0.2)
+    min_sep: float = 0.8
+    real_cutoff: Optional[float] = None
+    kmax: Optional[int] = None
+    kcut2: Optional[float] = None
+
+
+def brush_coordinates(spec: BrushSpec, seed: int):
+    """Phantom surface sites (symbol S, both walls), grafted chains (first bead
+    L at z = graft_z), then +1 counterions neutralising the chain charge."""
+    rng = np.random.default_rng(seed)
+    L, H = spec.lxy, spec.height
+    box = np.array([L, L, H])
+    per = (True, True, False)
+    grid = _Grid(box, max(spec.min_sep, 1.0))
+    mol, sym, xyz, q = [], [], [], []
+    m = 0
+    for w in (0.0, H):
+        for i in range(spec.n_sites):
+            p = np.array([rng.uniform(0, L), rng.uniform(0, L), w])
+            mol.append(m), sym.append("S"), xyz.append(p), q.append(0.0)
+            m += 1
+    zlo, zhi = spec.min_sep, H - spec.min_sep
+    nneg = 0
+    for c in range(spec.n_graft):
+        for attempt in range(1000):
+            p = np.array([rng.uniform(0, L), rng.uniform(0, L), spec.graft_z])
+            if not grid.ok(p, spec.min_sep, per):
+                continue
+            beads = [p]
+            local = _Grid(box, max(spec.min_sep, 1.0))
+            local.add(p)
+            okc = True
+            for b in range(1, spec.chain_len):
+                for t in range(400):
+                    cand = beads[-1] + spec.r0 * _unit(rng)
+                    if zlo < cand[2] < zhi and grid.ok(cand, spec.min_sep, per) and \
+                            local.ok(cand, spec.min_sep, per):
+                        break
+                else:
+                    okc = False
+                    break
+                beads.append(cand)
+                local.add(cand)
+            if okc:
+                break
+        else:
+            raise RuntimeError("could not graft chain %d" % c)
+        for b, p in enumerate(beads):
+            grid.add(p)
+            ch = -1.0 if rng.uniform() < spec.charge_frac else 0.0
+            nneg += ch < 0
+            mol.append(m), sym.append("L" if b == 0 else "P"), xyz.append(p), q.append(ch)
+        m += 1
+    for i in range(nneg):
+        for t in range(100000):
+            p = np.array([rng.uniform(0, L), rng.uniform(0, L), rng.uniform(zlo, zhi)])
+            if grid.ok(p, spec.min_sep, per):
+                break
+        else:
+            raise RuntimeError("could not place counterion %d" % i)
+        grid.add(p)
+        mol.append(m), sym.append("C"), xyz.append(p), q.append(1.0)
+        m += 1
+    return np.array(mol), sym, np.array(xyz), np.array(q, dtype=np.float64), nneg
+
+
+def write_brush(dirpath: str, spec: BrushSpec, seed: int, runin="run.in", **over) -> str:
+    """Writes run.in, input_crd.dat and input_top.dat for one brush replica."""
+    os.makedirs(dirpath, exist_ok=True)
+    mol, sym, xyz, q, nneg = brush_coordinates(spec, seed)
+    n_mol = int(mol.max()) + 1
+    write_crd(os.path.join(dirpath, "input_crd.dat"), mol, sym, xyz, q)
+    write_top(os.path.join(dirpath, "input_top.dat"), len(mol), n_mol,
+              (spec.lxy, spec.lxy, spec.height))
+    lj = (("P", 1.0, 1.0), ("L", 1.0, 1.0), ("C", 1.0, 1.0), ("S", 1.0, 1.0))
+    wall = (("P", 1.0, 1.0), ("L", 1.0, 1.0), ("C", 1.0, 1.0), ("S", 1.0, 0.0))
+    kw = dict(npbc=2, move_size=spec.move_size, move_prob=spec.move_prob,
+              phantom=2 * spec.n_sites, coion=0, grafted=spec.n_graft,
+              grafted_counterion=nneg, lj_cutoff=spec.lj_cutoff, lj_table=lj,
+              lB=spec.lB, alpha=(spec.alpha_times_L / spec.lxy) ** 2, dipole=True,
+              k_bond=spec.k_bond, r0=spec.r0, rigid=spec.r0, use_ext=True,
+              wall_cut=spec.wall_cut, wall_table=wall, real_cutoff=spec.real_cutoff,
+              kmax=spec.kmax, kcut2=spec.kcut2)
+    kw.update(over)
+    with open(os.path.join(dirpath, runin), "w") as f:
+        f.write(runin_text(**kw))
+    return os.path.join(dirpath, runin)

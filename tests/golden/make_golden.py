@@ -1,0 +1,115 @@
+"""Generates the golden fixtures under tests/golden/<case>/ by running the
+reference itself (oracle/_ref/libplumref.so: the unmodified reference sources
+linked with oracle/ref_harness.cc) on seeded inputs written by
+plum_gb300.systems.
+
+Each case directory holds the three reference-format inputs (run.in,
+input_crd.dat, input_top.dat) and ref.npz with, from the reference:
+  energies      running totals {pair, ewald, bond, ext} after initialisation
+  ewald         potential_ewald_coul.cc:38-115 derived values
+  de_mol/de_trial/de_moved/de_out
+                ForceField::EnergyDifference on seeded trial configurations
+  run_seed, run_type, run_accept, run_draws, run_etot
+                a seeded run of the reference's step loop
+  run_coords, run_obs, run_rhoz
+                final coordinates, observables, rho(z) after the run
+  rng_words     the reference generator's first outputs for run_seed
+
+Run from the repository root:  python tests/golden/make_golden.py
+(needs the reference checkout; the fixtures themselves are committed).
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from oracle import bindings as ob  # noqa: E402
+from plum_gb300 import systems  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+CASES = {
+    "bulk_small": dict(kind="bulk", seed=7, run_seed=123, steps=600,
+                       spec=systems.BulkSpec(n_chain=4, chain_len=20, n_ion=80, box=15.0)),
+    "bulk_wca": dict(kind="bulk", seed=8, run_seed=321, steps=600,
+                     spec=systems.BulkSpec(n_chain=3, chain_len=16, n_ion=48, box=13.0,
+                                           lj_cutoff=-1.0, use_bond=False,
+                                           move_prob=(0.4, 0.1, 0.2, 0.1, 0.2))),
+    "bulk_medium": dict(kind="bulk", seed=9, run_seed=77, steps=400,
+                        spec=systems.BulkSpec(n_chain=10, chain_len=20, n_ion=200, box=20.0)),
+    "slab_wca": dict(kind="brush", seed=3, run_seed=99, steps=600,
+                     spec=systems.BrushSpec(n_graft=4, chain_len=8, lxy=10.0, height=12.0,
+                                            n_sites=6, wall_cut=-1.0, charge_frac=0.7)),
+    "slab_lj": dict(kind="brush", seed=4, run_seed=98, steps=600,
+                    spec=systems.BrushSpec(n_graft=5, chain_len=10, lxy=12.0, height=16.0,
+                                           n_sites=8, wall_cut=2.5, charge_frac=0.5)),
+}
+
+
+def make_case(name, cfg, n_de=24):
+    d = os.path.join(HERE, name)
+    if os.path.isdir(d):
+        shutil.rmtree(d)
+    os.makedirs(d)
+    if cfg["kind"] == "bulk":
+        systems.write_bulk(d, cfg["spec"], seed=cfg["seed"])
+    else:
+        systems.write_brush(d, cfg["spec"], seed=cfg["seed"])
+    out = {}
+    R = ob.Ref(d, seed=cfg["run_seed"])
+    out["energies"] = R.energies()
+    out["ewald"] = R.ewald_info()
+    sizes = np.array([R.mol_size(m) for m in range(R.n_mol)])
+    start = np.concatenate([[0], np.cumsum(sizes)])
+    rng = np.random.default_rng(cfg["seed"] + 1000)
+    c = R.coords()
+    mols, trials, moveds, outs = [], [], [], []
+    movable = [m for m in range(R.n_mol) if sizes[m] > 1] + \
+              [m for m in range(R.n_mol) if sizes[m] == 1][-20:]
+    for k in range(n_de):
+        m = int(movable[rng.integers(len(movable))])
+        cur = c[start[m]:start[m + 1]]
+        n = sizes[m]
+        moved = np.zeros(n, np.int32)
+        if n == 1:
+            moved[:] = 1
+        else:
+            lo = int(rng.integers(0, n))
+            hi = int(rng.integers(lo + 1, n + 1))
+            moved[lo:hi] = 1
+        trial = cur + moved[:, None] * rng.normal(scale=0.25, size=cur.shape)
+        mols.append(m)
+        trials.append(trial)
+        moveds.append(moved)
+        outs.append(R.delta_energy(m, trial, moved))
+    out["de_mol"] = np.array(mols, np.int32)
+    out["de_start"] = start.astype(np.int32)
+    out["de_trial"] = np.concatenate(trials)
+    out["de_moved"] = np.concatenate(moveds)
+    out["de_out"] = np.array(outs)
+    out["rng_words"] = R.rng_words(4000)
+    out["run_seed"] = np.array(cfg["run_seed"])
+    mt, ac, dr, et = R.run(cfg["steps"])
+    out["run_type"], out["run_accept"], out["run_draws"], out["run_etot"] = mt, ac, dr, et
+    out["run_coords"] = R.coords()
+    out["run_obs"] = R.observables()
+    out["run_rhoz"] = R.rhoz()
+    out["run_recompute"] = R.recompute()
+    R.close()
+    for f in os.listdir(d):
+        if f not in ("run.in", "input_crd.dat", "input_top.dat"):
+            os.remove(os.path.join(d, f))
+    np.savez_compressed(os.path.join(d, "ref.npz"), **out)
+    print(name, "beads", int(start[-1]), "accept", ac.mean(), "types", np.bincount(mt + 1))
+
+
+if __name__ == "__main__":
+    ob.build()
+    for name, cfg in CASES.items():
+        make_case(name, cfg)

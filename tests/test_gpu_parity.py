@@ -1,0 +1,130 @@
+"""Plain FP64 form on the GPU against the reference's golden fixtures and the
+CPU oracle, through the C ABI (plum_gb300/_lib/libplumgpu.so).
+
+Bars: energies and dE within 1e-10 relative (dE relative to the size of its
+pair and Ewald parts); the recorded-stream replay must give the identical
+move-type, accept and draw-count sequence."""
+import numpy as np
+import pytest
+
+from _cases import CASES, de_moves, load, rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import plum_gb300
+    plum_gb300.lib()
+    return plum_gb300
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_total_energy(pg, case):
+    d, g = load(case)
+    s = pg.System(d)
+    e = s.total_energy()
+    for a, b in zip(e[:4], g["energies"]):
+        assert rel(a, b) < 1e-10, (e, g["energies"])
+    assert s.info.real_cutoff == g["ewald"][0]
+    assert list(s.info.real_cell) == list(g["ewald"][2:5])
+    assert list(s.info.k_cell) == list(g["ewald"][5:8])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_energy_difference(pg, case):
+    d, g = load(case)
+    s = pg.System(d)
+    for m, trial, moved, exp in de_moves(g):
+        got = s.energy_difference(m, trial, moved)
+        s.finalize(False)
+        scale = max(1.0, abs(exp[1]), abs(exp[2]))
+        assert rel(got[0], exp[0], scale) < 1e-10, (case, m, got, exp)
+        assert rel(got[1], exp[1], scale) < 1e-10
+        assert rel(got[2], exp[2], scale) < 1e-10
+    # rejected trials leave the running totals untouched
+    np.testing.assert_allclose(s.energies(), g["energies"], rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_replay_recorded_stream(pg, case, built):
+    d, g = load(case)
+    s = pg.System(d)
+    n = len(g["run_type"])
+    stream = built.mt19937(int(g["run_seed"]), 400000)
+    used, mt, ac, et = s.run_moves(stream, n)
+    np.testing.assert_array_equal(mt, g["run_type"])
+    np.testing.assert_array_equal(ac, g["run_accept"])
+    assert used == int(g["run_draws"].sum())
+    np.testing.assert_allclose(et, g["run_etot"], rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(s.positions(), g["run_coords"], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(s.observables()[[0, 4]], g["run_obs"][[0, 4]], rtol=1e-10)
+    fresh = s.total_energy()[:4]
+    np.testing.assert_allclose(fresh, g["run_recompute"], rtol=1e-10, atol=1e-9)
+
+
+def test_accept_commits_and_reject_restores(pg):
+    d, g = load("bulk_small")
+    s = pg.System(d)
+    e0 = s.energies().copy()
+    x0 = s.positions().copy()
+    m, trial, moved, exp = next(de_moves(g))
+    de = s.energy_difference(m, trial, moved)
+    s.finalize(True)
+    e1 = s.energies()
+    assert rel(e1.sum() - e0.sum(), de[0], max(1.0, abs(de[1]), abs(de[2]))) < 1e-10
+    x1 = s.positions()
+    start = g["de_start"]
+    np.testing.assert_array_equal(x1[start[m]:start[m + 1]][moved == 1], trial[moved == 1])
+    # a full recompute agrees with the incrementally updated totals
+    np.testing.assert_allclose(s.total_energy()[:4], e1, rtol=1e-10, atol=1e-9)
+    # and moving back gives -dE
+    back = s.energy_difference(m, x0[start[m]:start[m + 1]], moved)
+    s.finalize(False)
+    assert rel(back[0], -de[0], max(1.0, abs(de[1]), abs(de[2]))) < 1e-10
+
+
+def test_device_generator_matches_recorded_stream(pg, built):
+    d, g = load("bulk_small")
+    a = pg.System(d)
+    b = pg.System(d)
+    a.seed(99)
+    a.run(250)
+    b.run_moves(built.mt19937(99, 400000), 250, logs=False)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    np.testing.assert_array_equal(a.energies(), b.energies())
+
+
+def test_medium_system_long_replay_against_oracle(pg, built):
+    d, g = load("bulk_medium")
+    s = pg.System(d)
+    o = built.Oracle(d)
+    stream = built.mt19937(555, 2000000)
+    n = 1500
+    used, mt, ac, et = s.run_moves(stream, n)
+    used_o, mt_o, ac_o, et_o = o.run_stream(n, stream)
+    assert used == used_o
+    np.testing.assert_array_equal(mt, mt_o)
+    np.testing.assert_array_equal(ac, ac_o)
+    np.testing.assert_allclose(et, et_o, rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(s.positions(), o.coords(), rtol=0, atol=1e-8)
+
+
+def test_stream_exhaustion_reported(pg, built):
+    d, _ = load("bulk_small")
+    s = pg.System(d)
+    with pytest.raises(pg.PlumError) as ei:
+        s.run_moves(built.mt19937(3, 30), 50)
+    assert ei.value.code == 6
+
+
+def test_bad_input_is_an_error(pg, tmp_path):
+    import shutil, os
+    d, _ = load("bulk_small")
+    for f in ("input_crd.dat", "input_top.dat"):
+        shutil.copy(os.path.join(d, f), tmp_path / f)
+    text = open(os.path.join(d, "run.in")).read()
+    (tmp_path / "run.in").write_text(text[:text.index("s3_end_flag")])
+    with pytest.raises(pg.PlumError) as ei:
+        pg.System(str(tmp_path))
+    assert ei.value.code == 1
