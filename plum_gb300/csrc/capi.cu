@@ -126,6 +126,7 @@ int setup_ewald(plum_ctx* c, std::vector<short4>* kn, std::vector<double>* kw) {
   P.kchunk_delta = std::max(1, std::min(16, kKTableBytes / (2 * row)));
   P.kchunk_sk = std::max(1, std::min(32, kKTableBytes / row));
   P.real_cut = rc;
+  P.single_image = rc <= 0.5 * ebox[0] && rc <= 0.5 * ebox[1] && rc <= 0.5 * ebox[2];
   P.lB = in.lB;
   P.sqrt_alpha = std::sqrt(in.alpha);
   P.kpref = in.lB / (kPiRef * vol) * (4 * kPiRef * kPiRef);
@@ -200,6 +201,7 @@ __global__ void k_assemble_total(const DevParams P, const DevBuffers B, const do
     st->e_ext = P.use_ext ? misc[1] : 0.0;
     st->mz = misc[4];
     st->dipl_cur = dip;
+    st->sk_pending = 0;  // S(k) was rebuilt from the committed positions
     out[0] = st->e_pair;
     out[1] = st->e_ewald;
     out[2] = st->e_bond;
@@ -491,7 +493,8 @@ int plum_ctx_create(const char* dir, const char* runin, int form, int device,
   rc |= dalloc(&B.kn, kn.size());
   rc |= dalloc(&B.kw, kw.size());
   rc |= dalloc(&B.sk, kn.size());
-  rc |= dalloc(&B.dsk, kn.size());
+  rc |= dalloc(&B.dsk, 2 * kn.size());
+  rc |= dalloc(&B.done_count, 1);
   rc |= dalloc(&B.partial, 4 * (size_t)std::max(pair_grid(), pair_grid32()));
   rc |= dalloc(&B.fpos, nb);
   rc |= dalloc(&B.fq, nb);
@@ -532,6 +535,7 @@ int plum_ctx_create(const char* dir, const char* runin, int form, int device,
   }
   cudaMemset(B.state, 0, sizeof(DevState));
   cudaMemset(B.ktile_count, 0, sizeof(int) * std::max(1, ktile_count(P)));
+  cudaMemset(B.done_count, 0, sizeof(int));
   cudaError_t e = cudaDeviceSynchronize();
   if (e != cudaSuccess) {
     plum_ctx_destroy(c);
@@ -554,7 +558,7 @@ int plum_ctx_destroy(plum_ctx* c) {
   void* ptrs[] = {c->B.pos,      c->B.trial,   c->B.type,  c->B.mol_start, c->B.chain_ids,
                   c->B.ion_ids,  c->B.kn,      c->B.kw,    c->B.sk,        c->B.dsk,
                   c->B.partial,  c->B.bond_mol, c->B.state, c->d_tot_part,  c->d_out,
-                  c->B.dsk_part, c->B.ktile_count, c->B.kpartial, c->B.fpos,
+                  c->B.dsk_part, c->B.ktile_count, c->B.kpartial, c->B.fpos, c->B.done_count,
                   c->B.fq,       c->B.ftrial,  c->B.dsk_part32,
                   c->d_stream,   c->d_mt,      c->d_log_type, c->d_log_acc, c->d_log_e};
   for (void* p : ptrs)

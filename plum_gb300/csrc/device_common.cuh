@@ -1,0 +1,80 @@
+// Device helpers shared by the kernel translation units. They are inlined
+// where they are used: a DevParams kernel argument passed by reference into a
+// separately compiled function would be copied to local memory per thread.
+#pragma once
+
+#include "engine.h"
+
+namespace plum {
+
+// Wall energy of one bead at height z (potential_truncated_lj_wall.cc:46-134).
+__device__ __forceinline__ double wall64(const DevParams& P, double z, int ty) {
+  double energy = 0.0;
+  const double sigma = P.wall_sig[ty], eps = P.wall_eps[ty];
+  const double R0 = 3 * 1.25992104989 * sigma, K = 1.0;
+  const double lz = P.box[2];
+  const double k213 = 1.25992104989, c93 = 2.59807621135;
+  const int g = P.graft[ty];
+  if (eps == 0.0) return 0.0;
+  if (z <= 0.0 || z >= lz) return kVeryLarge;
+  if (P.wall_cut < 0 && g == 0) {
+    double r3r = pow(1.0 / k213, 3.0);
+    double eref = c93 * eps * (r3r * r3r - r3r);
+    if (z < k213 * sigma) {
+      double r3 = pow(sigma / z, 3.0);
+      energy += c93 * eps * (r3 * r3 - r3) - eref;
+    }
+    if (lz - z < k213 * sigma) {
+      double r3 = pow(sigma / (lz - z), 3.0);
+      energy += c93 * eps * (r3 * r3 - r3) - eref;
+    }
+  } else if (g == 1) {
+    double r3 = pow(sigma / z, 3.0);
+    energy += c93 * eps * (r3 * r3 - r3);
+    energy += -0.5 * K * R0 * R0 * log(1 - pow(z / R0, 2.0));
+    if (lz - z < k213 * sigma) {
+      r3 = pow(sigma / (lz - z), 3.0);
+      energy += c93 * eps * (r3 * r3 - r3);
+    } else {
+      r3 = pow(1.0 / k213, 3.0);
+      energy += c93 * eps * (r3 * r3 - r3);
+    }
+  } else if (g == 2) {
+    double r3 = pow(sigma / (lz - z), 3.0);
+    energy += c93 * eps * (r3 * r3 - r3);
+    energy += -0.5 * K * R0 * R0 * log(1 - pow((lz - z) / R0, 2.0));
+    if (z < k213 * sigma) {
+      r3 = pow(sigma / z, 3.0);
+      energy += c93 * eps * (r3 * r3 - r3);
+    } else {
+      r3 = pow(1.0 / k213, 3.0);
+      energy += c93 * eps * (r3 * r3 - r3);
+    }
+  } else {
+    double r3r = pow(1.0 / P.wall_cut, 3.0);
+    double eref = c93 * eps * (r3r * r3r - r3r);
+    if (z < P.wall_cut) {
+      double r3 = pow(sigma / z, 3.0);
+      energy += c93 * eps * (r3 * r3 - r3) - eref;
+    }
+    if (lz - z < P.wall_cut) {
+      double r3 = pow(sigma / (lz - z), 3.0);
+      energy += c93 * eps * (r3 * r3 - r3) - eref;
+    }
+  }
+  return energy;
+}
+
+__device__ __forceinline__ int fix_axis(double x, double L, double inv_fix, bool periodic) {
+  double w = periodic ? x - L * floor(x / L) : x;
+  long long v = llrint(w * inv_fix);
+  return (int)(unsigned int)(unsigned long long)v;
+}
+
+__device__ __forceinline__ int4 fix_point(const DevParams& P, double4_32a p, int type) {
+  return make_int4(fix_axis(p.x, P.ebox[0], P.inv_fix[0], true),
+                   fix_axis(p.y, P.ebox[1], P.inv_fix[1], true),
+                   fix_axis(p.z, P.ebox[2], P.inv_fix[2], P.npbc > 2), type);
+}
+
+}  // namespace plum

@@ -9,7 +9,9 @@
 //   kn     short4[n_k]      integer k = (nx, ny, nz) of each half-space vector
 //   kw     double[n_k]      e^{-k^2/4a}/k^2 on the reference's k-set
 //   sk     double2[n_k]     running structure factor S(k) = sum q e^{i k.r}
-//   dsk    double2[n_k]     S(k) change of the pending move
+//   dsk    double2[2*n_k]   S(k) change of the pending move (double-buffered:
+//                           an accepted change is added to sk by the next
+//                           delta kernel)
 //   partial double[grid*4]  per-block partial sums of the pending move
 //   dsk_part double2[groups*n_k], kpartial double[k tiles]: k-space parts
 //   state  DevState         running energies, the pending move, stream cursor
@@ -34,7 +36,7 @@ constexpr int kPairThreads = 256;
 constexpr int kMaxKmax = 1024;       // |n| per axis supported by the k tables
 constexpr int kKTableBytes = 96 * 1024;  // shared memory budget for phase tables
 constexpr int kSerialThreads = 256;
-constexpr int kDrawWindow = 4096;    // stream words staged per serial launch
+constexpr int kDrawWindow = 1024;    // stream words staged per serial launch
 
 // Device-side error codes (same values as PLUM_ERR_* in include/plum_gpu.h).
 constexpr int PLUM_ERR_TIMEOUT_DEV = 3;
@@ -55,6 +57,7 @@ struct DevParams {
   // Ewald (potential_ewald_coul.cc:29-115)
   double lB, sqrt_alpha, real_cut;
   int real_cell[3];
+  int single_image;  // real_cut <= half of every Ewald box length
   int n_k, kmax[3];
   int koff[3], kper;  // per-bead table: axis a at koff[a], n = 0..kmax[a]; kper entries
   int kchunk_delta, kchunk_sk;  // beads per table chunk (fits kKTableBytes)
@@ -93,6 +96,12 @@ struct DevState {
   int moves_left;
   int n_accept;
   int n_nonfinite;   // steps whose dE was NaN/Inf (rejected, as in the reference)
+  // pending move's sums, reduced by the last block of the delta kernel
+  double red_lj, red_re, red_k;
+  // S(k) commit of an accepted move is applied by the next delta kernel's
+  // k tiles: dsk[sk_buf] is pending while sk_pending; the delta kernel writes
+  // the new dS(k) into dsk[cur_buf]
+  int sk_pending, sk_buf, cur_buf;
 };
 
 struct DevBuffers {
@@ -105,7 +114,7 @@ struct DevBuffers {
   short4* kn;
   double* kw;
   double2* sk;
-  double2* dsk;
+  double2* dsk;      // [2][n_k] double-buffered dS(k)
   double* partial;   // [grid][4]
   // precision form mirrors: 32-bit fixed-point fractions of the Ewald box
   int4* fpos;        // [n_bead] current (X, Y, Z, type)
@@ -114,6 +123,7 @@ struct DevBuffers {
   float2* dsk_part32;  // [groups][n_k]
   double2* dsk_part; // [groups][n_k] dS(k) parts of the pending move
   int* ktile_count;  // [k tiles] arrival tickets (reset by the last arrival)
+  int* done_count;   // [1] block arrival ticket of the delta kernel
   double* kpartial;  // [k tiles] energy change per k tile
   double* bond_mol;  // [n_mol]
   DevState* state;
@@ -149,7 +159,6 @@ int pair_grid32();
 void launch_delta_pairs32(const DevParams& P, const DevBuffers& B, cudaStream_t s);
 void launch_fix_all(const DevParams& P, const DevBuffers& B, cudaStream_t s);
 void launch_fix_trial(const DevParams& P, const DevBuffers& B, cudaStream_t s);
-__device__ int4 fix_point(const DevParams& P, double4_32a p, int type);
 
 // mt19937 on the device: state[625] (624 words + index), fills out[n].
 void launch_mt_fill(uint32_t* state, uint32_t* out, long long n, cudaStream_t s);

@@ -23,6 +23,7 @@
 #include <cstdio>
 
 #include "engine.h"
+#include "device_common.cuh"
 
 namespace plum {
 
@@ -49,6 +50,13 @@ __device__ __forceinline__ double real_images64(const DevParams& P, double dx,
                                                 double dy, double dz) {
   double e = 0.0;
   const double rc = P.real_cut;
+  if (P.single_image) {
+    // r_c <= L/2 on every axis: any other image has a component >= L/2 >= r_c
+    // (ties at exactly L/2 are a set of measure zero)
+    double r = sqrt(dx * dx + dy * dy + dz * dz);
+    if (r > 0.0 && r <= rc) e = erfc(P.sqrt_alpha * r) / r;
+    return e;
+  }
   for (int a = -P.real_cell[0]; a <= P.real_cell[0]; a++) {
     double x = dx + a * P.ebox[0];
     if (fabs(x) > rc) continue;
@@ -153,6 +161,8 @@ __global__ void __launch_bounds__(kPairThreads)
   const DevState* st = B.state;
   const int b_lo = st->b_lo, b_hi = st->b_hi;
   const int m = st->pending ? b_hi - b_lo : 0;
+  const int sk_pend = st->sk_pending, sk_buf = st->sk_buf, cur_buf = st->cur_buf;
+  __shared__ int s_final;
   const int N = P.n_bead;
 
   double acc_lj = 0.0, acc_re = 0.0;
@@ -190,9 +200,9 @@ __global__ void __launch_bounds__(kPairThreads)
     B.partial[4 * blockIdx.x + 1] = t1;
   }
 
-  if (!P.use_ewald || m == 0) return;
+  const bool kwork = P.use_ewald && m > 0;
   const int chunk = P.kchunk_delta;
-  const int n_groups = (m + chunk - 1) / chunk;
+  const int n_groups = kwork ? (m + chunk - 1) / chunk : 0;
   const int n_tiles = (P.n_k + kKTile - 1) / kKTile;
   const int n_items = n_tiles * n_groups;
   double2* tabs = reinterpret_cast<double2*>(smem);  // [chunk][2][kper]
@@ -235,8 +245,13 @@ __global__ void __launch_bounds__(kPairThreads)
           ds.x += v.x;
           ds.y += v.y;
         }
-        B.dsk[k] = ds;
         double2 s = B.sk[k];
+        if (sk_pend) {
+          const double2 p = B.dsk[(size_t)sk_buf * P.n_k + k];
+          s = make_double2(s.x + p.x, s.y + p.y);
+          B.sk[k] = s;
+        }
+        B.dsk[(size_t)cur_buf * P.n_k + k] = ds;
         e = B.kw[k] * (2.0 * (s.x * ds.x + s.y * ds.y) + (ds.x * ds.x + ds.y * ds.y));
       }
       e = block_sum<kPairThreads>(e, red);
@@ -244,6 +259,32 @@ __global__ void __launch_bounds__(kPairThreads)
         B.kpartial[tile] = e;
         B.ktile_count[tile] = 0;
       }
+    }
+  }
+  // Last block to finish adds every block's and every k tile's sums in a
+  // fixed order (deterministic) for the serial kernel.
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_final = atomicAdd(B.done_count, 1) == (int)gridDim.x - 1;
+  __syncthreads();
+  if (s_final) {
+    __threadfence();
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+      a += __ldcg(&B.partial[4 * i]);
+      b += __ldcg(&B.partial[4 * i + 1]);
+    }
+    if (kwork)
+      for (int i = threadIdx.x; i < n_tiles; i += blockDim.x) c += __ldcg(&B.kpartial[i]);
+    a = block_sum<kPairThreads>(a, red);
+    b = block_sum<kPairThreads>(b, red);
+    c = block_sum<kPairThreads>(c, red);
+    if (threadIdx.x == 0) {
+      DevState* ws = B.state;
+      ws->red_lj = a;
+      ws->red_re = b;
+      ws->red_k = c;
+      *B.done_count = 0;
     }
   }
 }
@@ -399,64 +440,6 @@ void launch_sk_full64(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
   k_sk_sum<<<(P.n_k + 255) / 256, 256, 0, s>>>(P.n_k, part, B.sk);
 }
 
-// Wall energy of one bead at height z (potential_truncated_lj_wall.cc:46-134).
-__device__ double wall64(const DevParams& P, double z, int ty) {
-  double energy = 0.0;
-  const double sigma = P.wall_sig[ty], eps = P.wall_eps[ty];
-  const double R0 = 3 * 1.25992104989 * sigma, K = 1.0;
-  const double lz = P.box[2];
-  const double k213 = 1.25992104989, c93 = 2.59807621135;
-  const int g = P.graft[ty];
-  if (eps == 0.0) return 0.0;
-  if (z <= 0.0 || z >= lz) return kVeryLarge;
-  if (P.wall_cut < 0 && g == 0) {
-    double r3r = pow(1.0 / k213, 3.0);
-    double eref = c93 * eps * (r3r * r3r - r3r);
-    if (z < k213 * sigma) {
-      double r3 = pow(sigma / z, 3.0);
-      energy += c93 * eps * (r3 * r3 - r3) - eref;
-    }
-    if (lz - z < k213 * sigma) {
-      double r3 = pow(sigma / (lz - z), 3.0);
-      energy += c93 * eps * (r3 * r3 - r3) - eref;
-    }
-  } else if (g == 1) {
-    double r3 = pow(sigma / z, 3.0);
-    energy += c93 * eps * (r3 * r3 - r3);
-    energy += -0.5 * K * R0 * R0 * log(1 - pow(z / R0, 2.0));
-    if (lz - z < k213 * sigma) {
-      r3 = pow(sigma / (lz - z), 3.0);
-      energy += c93 * eps * (r3 * r3 - r3);
-    } else {
-      r3 = pow(1.0 / k213, 3.0);
-      energy += c93 * eps * (r3 * r3 - r3);
-    }
-  } else if (g == 2) {
-    double r3 = pow(sigma / (lz - z), 3.0);
-    energy += c93 * eps * (r3 * r3 - r3);
-    energy += -0.5 * K * R0 * R0 * log(1 - pow((lz - z) / R0, 2.0));
-    if (z < k213 * sigma) {
-      r3 = pow(sigma / z, 3.0);
-      energy += c93 * eps * (r3 * r3 - r3);
-    } else {
-      r3 = pow(1.0 / k213, 3.0);
-      energy += c93 * eps * (r3 * r3 - r3);
-    }
-  } else {
-    double r3r = pow(1.0 / P.wall_cut, 3.0);
-    double eref = c93 * eps * (r3r * r3r - r3r);
-    if (z < P.wall_cut) {
-      double r3 = pow(sigma / z, 3.0);
-      energy += c93 * eps * (r3 * r3 - r3) - eref;
-    }
-    if (lz - z < P.wall_cut) {
-      double r3 = pow(sigma / (lz - z), 3.0);
-      energy += c93 * eps * (r3 * r3 - r3) - eref;
-    }
-  }
-  return energy;
-}
-
 // Bond energy of molecule m on coordinates p (potential_spring.cc:22-48),
 // summed in bond order.
 __device__ double bond_mol64(const DevParams& P, const double4_32a* p, int b0, int b1) {
@@ -565,10 +548,5 @@ void launch_observables64(const DevParams& P, const DevBuffers& B, double* out5,
   k_obs_sum<<<1, 32, 0, s>>>(P.n_mol, P.n_chain_total, per, out5);
 }
 
-// Exposed to kern_moves.cu.
-__device__ double wall_energy64(const DevParams& P, double z, int ty) { return wall64(P, z, ty); }
-__device__ double bond_energy64(const DevParams& P, const double4_32a* p, int b0, int b1) {
-  return bond_mol64(P, p, b0, b1);
-}
 
 }  // namespace plum

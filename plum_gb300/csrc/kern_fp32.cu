@@ -19,22 +19,11 @@
 // Per-thread and per-block sums are FP32; blocks are added in FP64 by the
 // serial kernel.
 #include "engine.h"
+#include "device_common.cuh"
 
 namespace plum {
 
 constexpr int kKTile32 = 128;
-
-__device__ __forceinline__ int fix_axis(double x, double L, double inv_fix, bool periodic) {
-  double w = periodic ? x - L * floor(x / L) : x;
-  long long v = llrint(w * inv_fix);
-  return (int)(unsigned int)(unsigned long long)v;
-}
-
-__device__ int4 fix_point(const DevParams& P, double4_32a p, int type) {
-  return make_int4(fix_axis(p.x, P.ebox[0], P.inv_fix[0], true),
-                   fix_axis(p.y, P.ebox[1], P.inv_fix[1], true),
-                   fix_axis(p.z, P.ebox[2], P.inv_fix[2], P.npbc > 2), type);
-}
 
 __device__ __forceinline__ float fdiff(int a, int b, float scale) {
   return (float)(int)((unsigned)b - (unsigned)a) * scale;
@@ -54,6 +43,16 @@ __device__ __forceinline__ float real_images32(const DevParams& P, float dx, flo
                                                float dz) {
   float e = 0.0f;
   const float rc = P.f_real_cut;
+  if (P.single_image) {
+    // r_c <= L/2 on every axis: only the minimum image can be inside r_c
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 > 0.0f) {
+      const float ir = rsqrtf(r2);
+      const float r = r2 * ir;
+      if (r <= rc) e = erfcf(P.f_sqrt_alpha * r) * ir;
+    }
+    return e;
+  }
   for (int a = -P.real_cell[0]; a <= P.real_cell[0]; a++) {
     float x = dx + a * P.f_box[0];
     if (fabsf(x) > rc) continue;
@@ -100,6 +99,18 @@ __device__ __forceinline__ float block_sum32(float v, float* sh) {
   return t;
 }
 
+__device__ __forceinline__ double block_sum_d(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)blockDim.x / 32; i++) t += sh[i];
+  return t;
+}
+
 // Exact per-entry table: e^{i 2 pi n X / 2^32}, n = 0..kmax, q folded into x.
 __device__ __forceinline__ void table32(const DevParams& P, int4 f, float q, int axis,
                                         float2* tab) {
@@ -131,10 +142,13 @@ __global__ void __launch_bounds__(kPairThreads)
     k_delta32(const DevParams P, const DevBuffers B) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ float red[kPairThreads / 32];
+  __shared__ double redd[kPairThreads / 32];
   __shared__ int s_last;
   const DevState* st = B.state;
   const int b_lo = st->b_lo, b_hi = st->b_hi;
   const int m = st->pending ? b_hi - b_lo : 0;
+  const int sk_pend = st->sk_pending, sk_buf = st->sk_buf, cur_buf = st->cur_buf;
+  __shared__ int s_final;
   const int N = P.n_bead;
 
   float acc_lj = 0.0f, acc_re = 0.0f;
@@ -172,9 +186,9 @@ __global__ void __launch_bounds__(kPairThreads)
     B.partial[4 * blockIdx.x + 1] = (double)t1;
   }
 
-  if (!P.use_ewald || m == 0) return;
+  const bool kwork = P.use_ewald && m > 0;
   const int chunk = P.kchunk_delta;
-  const int n_groups = (m + chunk - 1) / chunk;
+  const int n_groups = kwork ? (m + chunk - 1) / chunk : 0;
   const int n_tiles = (P.n_k + kKTile32 - 1) / kKTile32;
   const int n_items = n_tiles * n_groups;
   float2* tabs = reinterpret_cast<float2*>(smem);  // [chunk][2][kper]
@@ -217,8 +231,13 @@ __global__ void __launch_bounds__(kPairThreads)
           ds.x += v.x;
           ds.y += v.y;
         }
-        B.dsk[k] = make_double2((double)ds.x, (double)ds.y);
         double2 s = B.sk[k];
+        if (sk_pend) {
+          const double2 p = B.dsk[(size_t)sk_buf * P.n_k + k];
+          s = make_double2(s.x + p.x, s.y + p.y);
+          B.sk[k] = s;
+        }
+        B.dsk[(size_t)cur_buf * P.n_k + k] = make_double2((double)ds.x, (double)ds.y);
         float sx = (float)s.x, sy = (float)s.y;
         e = (float)B.kw[k] * (2.0f * (sx * ds.x + sy * ds.y) + (ds.x * ds.x + ds.y * ds.y));
       }
@@ -227,6 +246,32 @@ __global__ void __launch_bounds__(kPairThreads)
         B.kpartial[tile] = (double)e;
         B.ktile_count[tile] = 0;
       }
+    }
+  }
+  // Last block to finish adds every block's and every k tile's sums in a
+  // fixed order (deterministic) for the serial kernel.
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_final = atomicAdd(B.done_count, 1) == (int)gridDim.x - 1;
+  __syncthreads();
+  if (s_final) {
+    __threadfence();
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+      a += __ldcg(&B.partial[4 * i]);
+      b += __ldcg(&B.partial[4 * i + 1]);
+    }
+    if (kwork)
+      for (int i = threadIdx.x; i < n_tiles; i += blockDim.x) c += __ldcg(&B.kpartial[i]);
+    a = block_sum_d(a, redd);
+    b = block_sum_d(b, redd);
+    c = block_sum_d(c, redd);
+    if (threadIdx.x == 0) {
+      DevState* ws = B.state;
+      ws->red_lj = a;
+      ws->red_re = b;
+      ws->red_k = c;
+      *B.done_count = 0;
     }
   }
 }

@@ -19,10 +19,10 @@
 // tests (randSphere's r1^2 + r2^2 > 1, the move-type and pick thresholds)
 // must round exactly like the reference or the draw sequence would diverge.
 #include "engine.h"
+#include "device_common.cuh"
 
 namespace plum {
 
-__device__ double wall_energy64(const DevParams& P, double z, int ty);
 
 struct Draws {
   const uint32_t* g;
@@ -129,168 +129,13 @@ struct GenPlan {
 
 constexpr int kPivotMax = 512;  // chains up to this length pivot in parallel
 
-__global__ void __launch_bounds__(kSerialThreads)
-    k_serial64(const DevParams P, const DevBuffers B, int mode, int n_partial, int n_ktiles) {
-  __shared__ uint32_t win[kDrawWindow];
-  __shared__ double red[kSerialThreads / 32];
-  __shared__ GenPlan plan;
-  __shared__ int s_accept, s_ext_bad;
-  __shared__ int s_off[kPivotMax], s_boff[kPivotMax];  // draw offsets per bead
-  __shared__ double s_w[3][kPivotMax];                 // pivot bond steps
-  DevState* st = B.state;
-  if (st->error) return;
-
-  // Stage the next stream words.
-  const long long wbase = st->stream_pos;
-  int wlen = 0;
-  if (mode & (kModeDecide | kModeGen)) {
-    long long avail = st->stream_len - wbase;
-    wlen = (int)(avail < kDrawWindow ? (avail > 0 ? avail : 0) : kDrawWindow);
-    for (int i = threadIdx.x; i < wlen; i += blockDim.x) win[i] = B.stream[wbase + i];
-  }
-  __syncthreads();
-  Draws d{B.stream, win, wbase, st->stream_len, wbase, wlen, 0};
-
-  const int pending = st->pending;
-  const int b_lo = st->b_lo, b_hi = st->b_hi, mol = st->mol;
-
-  if ((mode & kModeFinish) && pending) {
-    // 1. fixed-order reduction of the block partials
-    double a = 0.0, b = 0.0, c = 0.0;
-    for (int i = threadIdx.x; i < n_partial; i += blockDim.x) {
-      a += B.partial[4 * i];
-      b += B.partial[4 * i + 1];
-    }
-    if (P.use_ewald && b_hi > b_lo)
-      for (int i = threadIdx.x; i < n_ktiles; i += blockDim.x) c += B.kpartial[i];
-    double de_lj = bsum<kSerialThreads>(a, red);
-    double de_re = bsum<kSerialThreads>(b, red);
-    double de_k = bsum<kSerialThreads>(c, red);
-    // 2. walls of the moved beads, sum q dz
-    if (threadIdx.x == 0) s_ext_bad = 0;
-    __syncthreads();
-    double ext = 0.0, dmz = 0.0;
-    for (int i = b_lo + threadIdx.x; i < b_hi; i += blockDim.x) {
-      double4_32a t = B.trial[i], p = B.pos[i];
-      if (P.use_ext) {
-        int ty = B.type[i];
-        double en = wall_energy64(P, t.z, ty);
-        if (en >= kVeryLarge) s_ext_bad = 1;
-        ext += en - wall_energy64(P, p.z, ty);
-      }
-      dmz += t.w * (t.z - p.z);
-    }
-    ext = bsum<kSerialThreads>(ext, red);
-    dmz = bsum<kSerialThreads>(dmz, red);
-    // 3. bonds of the moved molecule at trial positions
-    const int m0 = B.mol_start[mol], m1 = B.mol_start[mol + 1];
-    double bt = 0.0;
-    if (P.use_bond && m1 - m0 > 1)
-      for (int i = m0 + threadIdx.x; i < m1 - 1; i += blockDim.x) {
-        double4_32a p = B.trial[i], q = B.trial[i + 1];
-        double dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-        double r = sqrt(dx * dx + dy * dy + dz * dz);
-        bt += 0.5 * P.k_bond * (r - P.r0) * (r - P.r0);
-      }
-    bt = bsum<kSerialThreads>(bt, red);
-    if (threadIdx.x == 0) {
-      double de = 0.0, dp = 0.0, dx = 0.0, dw = 0.0, db = 0.0;
-      double dip_t = st->dipl_cur;
-      bool done = false;
-      if (P.use_pair) {
-        dp = de_lj;
-        de += dp;
-        done = de >= kVeryLarge;
-      }
-      if (!done && P.use_ext) {
-        dx = s_ext_bad ? kVeryLarge : ext;
-        de += dx;
-        done = de >= kVeryLarge;
-      }
-      if (!done && P.use_ewald) {
-        dw = de_re + P.kpref * de_k;
-        if (P.dipole) {
-          dip_t = P.dip_coef * st->mz * st->mz;
-          dw += dip_t - st->dipl_cur;
-        }
-        de += dw;
-      }
-      if (!done && P.use_bond && m1 - m0 > 1) {
-        db = bt - B.bond_mol[mol];
-        de += db;
-      }
-      if (!isfinite(de)) st->n_nonfinite++;  // flagged, rejected as the reference does
-      st->de = de;
-      st->de_pair = dp;
-      st->de_ext = dx;
-      st->de_ewald = dw;
-      st->de_bond = db;
-      st->bond_trial = bt;
-      st->dipl_trial = dip_t;
-      st->dmz = dmz;
-    }
-    __syncthreads();
-  }
-
-  // Metropolis (simulation.cc:324-332) or the host's decision.
-  if ((mode & (kModeDecide | kModeCommit)) && pending) {
-    if (threadIdx.x == 0) {
-      int acc = 0;
-      if (mode & kModeDecide) {
-        if (!(st->de >= kVeryLarge)) acc = d.u() < exp(-P.beta * st->de);  // a NaN dE still draws
-        if (d.overrun) st->error = PLUM_ERR_STREAM_DEV;
-      } else {
-        acc = st->last_accept;
-      }
-      s_accept = acc;
-    }
-    __syncthreads();
-    const int acc = s_accept;
-    if (acc) {
-      for (int i = b_lo + threadIdx.x; i < b_hi; i += blockDim.x) {
-        B.pos[i] = B.trial[i];
-        if (P.form) B.fpos[i] = B.ftrial[i - b_lo];
-      }
-      if (P.use_ewald && b_hi > b_lo)
-        for (int k = threadIdx.x; k < P.n_k; k += blockDim.x) {
-          double2 s = B.sk[k], ds = B.dsk[k];
-          B.sk[k] = make_double2(s.x + ds.x, s.y + ds.y);
-        }
-    } else {
-      for (int i = b_lo + threadIdx.x; i < b_hi; i += blockDim.x) B.trial[i] = B.pos[i];
-    }
-    if (threadIdx.x == 0) {
-      if (acc) {
-        st->e_pair += st->de_pair;
-        st->e_ext += st->de_ext;
-        st->e_ewald += st->de_ewald;
-        st->e_bond += st->de_bond;
-        st->mz += st->dmz;
-        if (P.dipole) st->dipl_cur = st->dipl_trial;
-        if (P.use_bond && B.mol_start[mol + 1] - B.mol_start[mol] > 1)
-          B.bond_mol[mol] = st->bond_trial;
-        st->n_accept++;
-      }
-      st->last_accept = acc;
-      st->pending = 0;
-    }
-  }
-  // Per-step log (also for steps where nothing was attempted).
-  if ((mode & kModeDecide) && st->step_open && threadIdx.x == 0) {
-    int s = st->step;
-    if (B.log_type) B.log_type[s] = pending ? st->move_type : -1;
-    if (B.log_accept) B.log_accept[s] = pending ? st->last_accept : 0;
-    if (B.log_etot) B.log_etot[s] = st->e_pair + st->e_ewald + st->e_bond + st->e_ext;
-    st->step = s + 1;
-    st->step_open = 0;
-  }
-  __syncthreads();
-
-  if (!(mode & kModeGen) || st->error) {
-    if (threadIdx.x == 0) st->stream_pos = d.pos;
-    return;
-  }
-
+// Generates the next step's trial move into `trial` (and the fixed-point
+// mirror for the precision form); thread 0 consumes the draws, the block
+// applies the geometry.
+__device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B, DevState& S,
+                                      Draws& d, long long wbase, GenPlan& plan, int* s_off,
+                                      int* s_boff, double (*s_w)[kPivotMax]) {
+  DevState* const st = &S;
   // ----------------------------------------------------- generate next move
   if (threadIdx.x == 0) {
     plan.type = -1;
@@ -547,9 +392,180 @@ __global__ void __launch_bounds__(kSerialThreads)
   }
 }
 
+__global__ void __launch_bounds__(kSerialThreads)
+    k_serial64(const DevParams P, const DevBuffers B, int mode) {
+  __shared__ uint32_t win[kDrawWindow];
+  __shared__ double red[kSerialThreads / 32];
+  __shared__ GenPlan plan;
+  __shared__ int s_accept, s_ext_bad;
+  __shared__ int s_off[kPivotMax], s_boff[kPivotMax];  // draw offsets per bead
+  __shared__ double s_w[3][kPivotMax];                 // pivot bond steps
+  // The state lives in shared memory for the kernel's duration: thread 0's
+  // chain of decisions then never waits on global memory for it.
+  __shared__ DevState S;
+  {
+    const int nw = (int)(sizeof(DevState) / sizeof(int));
+    const int* src = reinterpret_cast<const int*>(B.state);
+    int* dst = reinterpret_cast<int*>(&S);
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  if (S.error) return;
+
+  // Stage the next stream words.
+  const long long wbase = S.stream_pos;
+  int wlen = 0;
+  if (mode & (kModeDecide | kModeGen)) {
+    long long avail = S.stream_len - wbase;
+    wlen = (int)(avail < kDrawWindow ? (avail > 0 ? avail : 0) : kDrawWindow);
+    for (int i = threadIdx.x; i < wlen; i += blockDim.x) win[i] = B.stream[wbase + i];
+  }
+  __syncthreads();
+  Draws d{B.stream, win, wbase, S.stream_len, wbase, wlen, 0};
+
+  const int pending = S.pending;
+  const int b_lo = S.b_lo, b_hi = S.b_hi, mol = S.mol;
+
+  if ((mode & kModeFinish) && pending) {
+    // walls of the moved beads, sum q dz
+    if (threadIdx.x == 0) s_ext_bad = 0;
+    __syncthreads();
+    double ext = 0.0, dmz = 0.0;
+    for (int i = b_lo + threadIdx.x; i < b_hi; i += blockDim.x) {
+      double4_32a t = B.trial[i], p = B.pos[i];
+      if (P.use_ext) {
+        int ty = B.type[i];
+        double en = wall64(P, t.z, ty);
+        if (en >= kVeryLarge) s_ext_bad = 1;
+        ext += en - wall64(P, p.z, ty);
+      }
+      dmz += t.w * (t.z - p.z);
+    }
+    ext = bsum<kSerialThreads>(ext, red);
+    dmz = bsum<kSerialThreads>(dmz, red);
+    // bonds of the moved molecule at trial positions
+    const int m0 = B.mol_start[mol], m1 = B.mol_start[mol + 1];
+    double bt = 0.0;
+    if (P.use_bond && m1 - m0 > 1)
+      for (int i = m0 + threadIdx.x; i < m1 - 1; i += blockDim.x) {
+        double4_32a p = B.trial[i], q = B.trial[i + 1];
+        double dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        double r = sqrt(dx * dx + dy * dy + dz * dz);
+        bt += 0.5 * P.k_bond * (r - P.r0) * (r - P.r0);
+      }
+    bt = bsum<kSerialThreads>(bt, red);
+    if (threadIdx.x == 0) {
+      // the delta kernel applied any pending S(k) commit if it ran k tiles
+      if (P.use_ewald && b_hi > b_lo) S.sk_pending = 0;
+      const double de_lj = S.red_lj, de_re = S.red_re, de_k = b_hi > b_lo ? S.red_k : 0.0;
+      double de = 0.0, dp = 0.0, dx = 0.0, dw = 0.0, db = 0.0;
+      double dip_t = S.dipl_cur;
+      bool done = false;
+      if (P.use_pair) {
+        dp = de_lj;
+        de += dp;
+        done = de >= kVeryLarge;
+      }
+      if (!done && P.use_ext) {
+        dx = s_ext_bad ? kVeryLarge : ext;
+        de += dx;
+        done = de >= kVeryLarge;
+      }
+      if (!done && P.use_ewald) {
+        dw = de_re + P.kpref * de_k;
+        if (P.dipole) {
+          dip_t = P.dip_coef * S.mz * S.mz;
+          dw += dip_t - S.dipl_cur;
+        }
+        de += dw;
+      }
+      if (!done && P.use_bond && m1 - m0 > 1) {
+        db = bt - B.bond_mol[mol];
+        de += db;
+      }
+      if (!isfinite(de)) S.n_nonfinite++;  // flagged, rejected as the reference does
+      S.de = de;
+      S.de_pair = dp;
+      S.de_ext = dx;
+      S.de_ewald = dw;
+      S.de_bond = db;
+      S.bond_trial = bt;
+      S.dipl_trial = dip_t;
+      S.dmz = dmz;
+    }
+    __syncthreads();
+  }
+
+  // Metropolis (simulation.cc:324-332) or the host's decision.
+  if ((mode & (kModeDecide | kModeCommit)) && pending) {
+    if (threadIdx.x == 0) {
+      int acc = 0;
+      if (mode & kModeDecide) {
+        if (!(S.de >= kVeryLarge)) acc = d.u() < exp(-P.beta * S.de);  // a NaN dE still draws
+        if (d.overrun) S.error = PLUM_ERR_STREAM_DEV;
+      } else {
+        acc = S.last_accept;
+      }
+      s_accept = acc;
+    }
+    __syncthreads();
+    const int acc = s_accept;
+    if (acc) {
+      for (int i = b_lo + threadIdx.x; i < b_hi; i += blockDim.x) {
+        B.pos[i] = B.trial[i];
+        if (P.form) B.fpos[i] = B.ftrial[i - b_lo];
+      }
+    } else {
+      for (int i = b_lo + threadIdx.x; i < b_hi; i += blockDim.x) B.trial[i] = B.pos[i];
+    }
+    if (threadIdx.x == 0) {
+      if (acc) {
+        S.e_pair += S.de_pair;
+        S.e_ext += S.de_ext;
+        S.e_ewald += S.de_ewald;
+        S.e_bond += S.de_bond;
+        S.mz += S.dmz;
+        if (P.dipole) S.dipl_cur = S.dipl_trial;
+        if (P.use_bond && B.mol_start[mol + 1] - B.mol_start[mol] > 1)
+          B.bond_mol[mol] = S.bond_trial;
+        if (P.use_ewald && b_hi > b_lo) {
+          // the next delta kernel adds dsk[cur_buf] into S(k)
+          S.sk_pending = 1;
+          S.sk_buf = S.cur_buf;
+          S.cur_buf ^= 1;
+        }
+        S.n_accept++;
+      }
+      S.last_accept = acc;
+      S.pending = 0;
+    }
+  }
+  // Per-step log (also for steps where nothing was attempted).
+  if ((mode & kModeDecide) && S.step_open && threadIdx.x == 0) {
+    int sidx = S.step;
+    if (B.log_type) B.log_type[sidx] = pending ? S.move_type : -1;
+    if (B.log_accept) B.log_accept[sidx] = pending ? S.last_accept : 0;
+    if (B.log_etot) B.log_etot[sidx] = S.e_pair + S.e_ewald + S.e_bond + S.e_ext;
+    S.step = sidx + 1;
+    S.step_open = 0;
+  }
+  __syncthreads();
+
+  if ((mode & kModeGen) && !S.error) gen_move(P, B, S, d, wbase, plan, s_off, s_boff, s_w);
+
+  // write the state back
+  if (threadIdx.x == 0) S.stream_pos = S.stream_pos > d.pos ? S.stream_pos : d.pos;
+  __syncthreads();
+  {
+    const int nw = (int)(sizeof(DevState) / sizeof(int));
+    int* dst = reinterpret_cast<int*>(B.state);
+    const int* src = reinterpret_cast<const int*>(&S);
+    for (int i = threadIdx.x; i < nw; i += blockDim.x) dst[i] = src[i];
+  }
+}
+
 void launch_serial64(const DevParams& P, const DevBuffers& B, int mode, cudaStream_t s) {
-  k_serial64<<<1, kSerialThreads, 0, s>>>(P, B, mode, P.form ? pair_grid32() : pair_grid(),
-                                           ktile_count(P));
+  k_serial64<<<1, kSerialThreads, 0, s>>>(P, B, mode);
 }
 
 __global__ void k_set_move(DevState* st, int mol, int b_lo, int b_hi) {
