@@ -54,6 +54,16 @@ typedef struct {
   int real_cell[3], k_cell[3];
 } plum_info;
 
+/* Run-control items of run.in (simulation.cc:30-50, force_field.cc:65-103). */
+typedef struct {
+  long steps, steps_eq, sample_freq, stat_out_freq, traj_out_freq;
+  double beta, move_size, move_prob[5];
+  int phantom, coion, grafted, grafted_counterion, calc_chem_pot;
+  int use_pair, use_ewald, use_bond, use_bond_rigid, use_ext, use_gc, gc_freq;
+  double rigid_bond, eq_bond;
+  char run_name[256];
+} plum_run_info;
+
 /* Message for the last failing call on this thread ("" if none). */
 const char* plum_last_error(void);
 
@@ -65,8 +75,19 @@ const char* plum_last_error(void);
  * The total energy is computed on the device before returning. */
 int plum_ctx_create(const char* dir, const char* runin, int form, int device,
                     plum_ctx** out);
+/* Same, with the run.in content passed as text (the reference reads it from
+ * stdin, simulation.cc:30-50); crd/top paths are relative to `dir`. */
+int plum_ctx_create_text(const char* dir, const char* runin_text, int form, int device,
+                         plum_ctx** out);
 int plum_ctx_destroy(plum_ctx* ctx);
 int plum_ctx_info(const plum_ctx* ctx, plum_info* out);
+int plum_run_params(const plum_ctx* ctx, plum_run_info* out);
+/* Molecule layout (n_mol+1 offsets), charges and type indices of the beads in
+ * molecule order, as read from the coordinate file (simulation.cc:582-608);
+ * any pointer may be NULL. */
+int plum_get_topology(const plum_ctx* ctx, int* mol_start, double* q, int* type);
+/* Bead symbol of a type index (first-appearance order in the crd file). */
+int plum_type_name(const plum_ctx* ctx, int type, char* buf, int cap);
 
 /* Recomputes every energy term of the current configuration from scratch on
  * the device in FP64 and resets the running totals and S(k) to it.

@@ -1,0 +1,155 @@
+// C++ host classes with the reference's public surface, backed by the GB300
+// engine (include/plum_gpu.h).
+//
+// A program written against the reference's Simulation / ForceField /
+// Molecule / Bead (src/simulation/simulation.h:20-201,
+// src/force_field/force_field.h:22-294, src/molecules/molecule.h:16-69,
+// src/molecules/bead.h:14-87) switches by including this header and using
+// namespace plum. Method names, argument meaning and draw order are the
+// reference's; energies live on the GPU:
+//
+//   ForceField::EnergyDifference / FinalizeEnergies / Tot*Energy / InitializeEnergy
+//       -> plum_delta_energy / plum_finalize / plum_energies / plum_total_energy
+//   Simulation::TranslationalMove   host control flow, device energies
+//   Simulation::Run                 the whole step loop on the device, with
+//                                   rand_gen kept in step with the draws used
+//
+// Differences: bad input throws plum::InputError instead of exit(1);
+// Simulation takes an explicit seed (the reference seeds from the clock,
+// simulation.cc:133-136); grand-canonical steps are not available here.
+#pragma once
+
+#include <istream>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "plum_gpu.h"
+
+namespace plum {
+
+struct InputError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+class Bead {  // bead.h:14-87
+ public:
+  Bead();
+  Bead(std::string symbol, int id, int c_id, double q, double x, double y, double z);
+  double Charge() const { return q_; }
+  void SetCharge(double q) { q_ = q; }
+  int ID() const { return id_; }
+  int ChainID() const { return c_id_; }
+  void SetID(int id) { id_ = id; }
+  void SetChainID(int c) { c_id_ = c; }
+  std::string Symbol() const { return symbol_; }
+  void SetSymbol(std::string s) { symbol_ = s; }
+  int Type() const { return type_; }
+  void SetType(int t) { type_ = t; }
+  bool GetMoved() const { return moved_; }
+  void SetMoved() { moved_ = true; }
+  void UnsetMoved() { moved_ = false; }
+  // flag 0: current position, 1: trial position; index 0..2 = x, y, z
+  double GetCrd(int flag, int index) const;
+  void SetCrd(int flag, int index, double value);
+  void SetAllCrd(double pos[3]);
+  void UpdateCurrentPos();
+  void UpdateTrialPos();
+  // minimum-image distance of the trial positions (bead.cc:162-176)
+  double BBDist(const Bead& other, const double box_l[], int npbc) const;
+
+ private:
+  double current_[3], trial_[3];
+  double q_ = 0;
+  int id_ = -1, c_id_ = -1, type_ = 0;
+  std::string symbol_ = "NONE";
+  bool moved_ = false;
+};
+
+class Molecule {  // molecule.h:16-69
+ public:
+  std::vector<Bead> bds;
+  std::vector<std::vector<int>> bonds;
+  void AddBead(Bead b) { bds.push_back(b); }
+  void AddBond(int i, int j) { bonds.push_back({i, j}); }
+  int Size() const { return (int)bds.size(); }
+  int NBond() const { return (int)bonds.size(); }
+  // Monte Carlo moves (molecule.cc:103-312): write trial positions and set
+  // the moved flags, consuming draws in the reference's order.
+  void BeadTranslate(double move_size, double box_l[3], std::mt19937& rand_gen);
+  void COMTranslate(double move_size, std::mt19937& rand_gen);
+  void Pivot(double move_size, std::mt19937& rand_gen, double eq_bond_len, bool vary_bond);
+  void Crankshaft(double move_size, std::mt19937& rand_gen);
+  void RandomReptation(std::mt19937& rand_gen, double eq_bond_len, bool vary_bond);
+};
+
+class ForceField {  // force_field.h:22-294 (energy surface)
+ public:
+  ForceField() = default;
+  ~ForceField();
+  ForceField(const ForceField&) = delete;
+  ForceField& operator=(const ForceField&) = delete;
+  // Builds the device context from run.in text (crd/top relative to dir) and
+  // fills mols with the system read from the coordinate file.
+  void Initialize(const std::string& dir, const std::string& runin_text,
+                  std::vector<Molecule>& mols, int form = PLUM_FORM_FP64, int device = 0);
+  void InitializeEnergy(std::vector<Molecule>& mols);
+  double EnergyDifference(std::vector<Molecule>& mols, int moved_mol);
+  void FinalizeEnergies(std::vector<Molecule>& mols, bool accept, int moved_mol);
+  double TotPairEnergy();
+  double TotEwaldEnergy();
+  double TotBondEnergy();
+  double TotExtEnergy();
+  bool UseGC() const { return run_.use_gc; }
+  bool UsePairPot() const { return run_.use_pair; }
+  bool UseEwaldPot() const { return run_.use_ewald; }
+  bool UseBondPot() const { return run_.use_bond; }
+  bool UseBondRigid() const { return run_.use_bond_rigid; }
+  bool UseExtPot() const { return run_.use_ext; }
+  int GCFrequency() const { return run_.gc_freq; }
+  double RigidBondLen() const { return run_.rigid_bond; }
+  double EqBondLen() const;
+  plum_ctx* Context() const { return ctx_; }
+  const plum_run_info& RunInfo() const { return run_; }
+  const plum_info& Info() const { return info_; }
+
+ private:
+  plum_ctx* ctx_ = nullptr;
+  plum_run_info run_{};
+  plum_info info_{};
+  std::vector<int> mol_start_;
+};
+
+class Simulation {  // simulation.h:20-201 (step loop and observables)
+ public:
+  // Reads run.in from `runin` (std::cin for the reference's usage
+  // `plum < run.in`); crd/top paths are relative to dir.
+  Simulation(std::istream& runin, const std::string& dir = ".", unsigned seed = 5489u,
+             int form = PLUM_FORM_FP64, int device = 0);
+  void Run();                 // steps from run.in, on the device
+  void RunSteps(long n);      // n steps on the device
+  void TranslationalMove();   // one step, host control flow (simulation.cc:241-355)
+  void Sample();              // simulation.cc:723-798 (energies, Rg; no pressure)
+  double RadiusOfGyration();  // simulation.cc:406-434
+  double EndToEndDistance();  // simulation.cc:483-501
+  void UpdateMolCounts();     // simulation.cc:1066-1094
+  void SyncFromDevice();      // refresh host bead positions after device steps
+
+  std::vector<Molecule> mols;
+  ForceField force_field;
+  std::mt19937 rand_gen;
+  long step = 0;
+  int accepted[5] = {0, 0, 0, 0, 0}, attempted[5] = {0, 0, 0, 0, 0};
+  double pair_e_cumu = 0, ewald_e_cumu = 0, bond_e_cumu = 0, ext_e_cumu = 0, rg_tot_cumu = 0;
+  long ff_avg_counter = 0, mol_avg_counter = 0;
+  int last_move_type = -1, last_accept = 0;
+
+ private:
+  plum_run_info run_{};
+  double box_l[3];
+  int npbc = 3;
+  int n_mol = 0, n_chain = 0, n_cion = 0, n_aion = 0, n_nion = 0;
+};
+
+}  // namespace plum

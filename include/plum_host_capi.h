@@ -1,0 +1,41 @@
+/* plum_host_capi.h -- C entry points that drive the C++ host classes of
+ * include/plum_host.hpp (the reference's Simulation surface) from C callers:
+ * tests, scripting languages, the command-line driver.
+ *
+ * Each replaces a reference call sequence:
+ *   plum_sim_create              Simulation::Simulation (simulation.cc:23-201)
+ *                                with an explicit seed (the reference seeds
+ *                                from the clock, simulation.cc:133-136)
+ *   plum_sim_translational_moves Simulation::TranslationalMove
+ *                                (simulation.cc:241-355), host control flow,
+ *                                energies on the GPU
+ *   plum_sim_run_steps           the step loop of Simulation::Run
+ *                                (simulation.cc:216-239) on the GPU
+ *   plum_sim_energies            ForceField::Tot*Energy (force_field.cc:1201-1219)
+ */
+#ifndef PLUM_HOST_CAPI_H_
+#define PLUM_HOST_CAPI_H_
+
+#include "plum_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct plum_sim plum_sim;
+
+int plum_sim_create(const char* dir, const char* runin_text, unsigned seed, int form,
+                    plum_sim** out);
+int plum_sim_destroy(plum_sim* sim);
+/* n steps of the host control flow; per step the move type (-1 none) and
+ * accept flag (host buffers of n, may be NULL). Each step also takes the
+ * draw simulation.cc:221 spends on the grand-canonical check. */
+int plum_sim_translational_moves(plum_sim* sim, int n, int* move_type, int* accept);
+int plum_sim_run_steps(plum_sim* sim, long n);
+int plum_sim_positions(plum_sim* sim, double* xyz);
+int plum_sim_energies(plum_sim* sim, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

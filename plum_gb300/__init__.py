@@ -72,6 +72,13 @@ def lib():
         L.plum_set_recompute.argtypes = [C.c_void_p, C.c_long]
         L.plum_drift.argtypes = [C.c_void_p, _dp]
         L.plum_probe_peaks.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.plum_sim_create.argtypes = [C.c_char_p, C.c_char_p, C.c_uint, C.c_int,
+                                      C.POINTER(C.c_void_p)]
+        L.plum_sim_destroy.argtypes = [C.c_void_p]
+        L.plum_sim_translational_moves.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        L.plum_sim_run_steps.argtypes = [C.c_void_p, C.c_long]
+        L.plum_sim_positions.argtypes = [C.c_void_p, _dp]
+        L.plum_sim_energies.argtypes = [C.c_void_p, _dp]
         _lib = L
     return _lib
 
@@ -184,3 +191,44 @@ class System:
         k = C.c_long(0)
         _check(lib().plum_last_timing(self.h, C.byref(ms), C.byref(k)))
         return ms.value, k.value
+
+
+class HostSimulation:
+    """The reference-named C++ host classes (include/plum_host.hpp) driven
+    through include/plum_host_capi.h: Simulation::TranslationalMove with host
+    control flow and device energies, or the device step loop."""
+
+    def __init__(self, dirpath: str, runin: str = "run.in", seed: int = 5489,
+                 form: int = FORM_FP64):
+        import os as _os
+        text = open(_os.path.join(dirpath, runin)).read()
+        h = C.c_void_p()
+        _check(lib().plum_sim_create(dirpath.encode(), text.encode(), seed, form, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().plum_sim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def translational_moves(self, n):
+        mt = np.zeros(n, np.int32)
+        ac = np.zeros(n, np.int32)
+        _check(lib().plum_sim_translational_moves(self.h, n, _ptr(mt), _ptr(ac)))
+        return mt, ac
+
+    def run_steps(self, n):
+        _check(lib().plum_sim_run_steps(self.h, n))
+
+    def positions(self, n_bead):
+        o = np.zeros(3 * n_bead)
+        _check(lib().plum_sim_positions(self.h, o))
+        return o.reshape(-1, 3)
+
+    def energies(self):
+        o = np.zeros(4)
+        _check(lib().plum_sim_energies(self.h, o))
+        return o

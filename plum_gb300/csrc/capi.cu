@@ -339,20 +339,41 @@ extern "C" {
 
 const char* plum_last_error(void) { return g_err.c_str(); }
 
+static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out);
+
 int plum_ctx_create(const char* dir, const char* runin, int form, int device,
                     plum_ctx** out) {
   if (!out || !dir || !runin) return fail(PLUM_ERR_INPUT, "null argument");
   *out = nullptr;
-  if (form != PLUM_FORM_FP64 && form != PLUM_FORM_FP32)
-    return fail(PLUM_ERR_INPUT, "unknown form");
   plum_ctx* c = new plum_ctx();
-  c->form = form;
-  c->device = device;
   std::string err;
   if (!read_input(dir, runin, &c->in, &err)) {
     delete c;
     return fail(PLUM_ERR_INPUT, err);
   }
+  return create_ctx(c, form, device, out);
+}
+
+int plum_ctx_create_text(const char* dir, const char* runin_text, int form, int device,
+                         plum_ctx** out) {
+  if (!out || !dir || !runin_text) return fail(PLUM_ERR_INPUT, "null argument");
+  *out = nullptr;
+  plum_ctx* c = new plum_ctx();
+  std::string err;
+  if (!read_input_text(dir, runin_text, &c->in, &err)) {
+    delete c;
+    return fail(PLUM_ERR_INPUT, err);
+  }
+  return create_ctx(c, form, device, out);
+}
+
+static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out) {
+  if (form != PLUM_FORM_FP64 && form != PLUM_FORM_FP32) {
+    delete c;
+    return fail(PLUM_ERR_INPUT, "unknown form");
+  }
+  c->form = form;
+  c->device = device;
   Input& in = c->in;
   // The reference's own input checks (simulation.cc:142-191, force_field.cc:205-209).
   std::string bad;
@@ -869,6 +890,52 @@ int plum_observables(const plum_ctx* cc, double* out) {
   CK(cudaMemcpyAsync(c->h_out, c->d_out + 32, sizeof(double) * 5, cudaMemcpyDeviceToHost, c->s));
   CK(cudaStreamSynchronize(c->s));
   std::memcpy(out, c->h_out, sizeof(double) * 5);
+  return PLUM_OK;
+}
+
+int plum_run_params(const plum_ctx* c, plum_run_info* o) {
+  if (!c || !o) return fail(PLUM_ERR_INPUT, "null argument");
+  const Input& in = c->in;
+  std::memset(o, 0, sizeof(*o));
+  o->steps = in.steps;
+  o->steps_eq = in.steps_eq;
+  o->sample_freq = in.sample_freq;
+  o->stat_out_freq = in.stat_out_freq;
+  o->traj_out_freq = in.traj_out_freq;
+  o->beta = in.beta;
+  o->move_size = in.move_size;
+  for (int i = 0; i < 5; i++) o->move_prob[i] = in.move_prob[i];
+  o->phantom = in.phantom;
+  o->coion = in.coion;
+  o->grafted = in.grafted;
+  o->grafted_counterion = in.grafted_counterion;
+  o->calc_chem_pot = in.calc_chem_pot;
+  o->use_pair = in.use_pair;
+  o->use_ewald = in.use_ewald;
+  o->use_bond = in.use_bond;
+  o->use_bond_rigid = in.use_rigid;
+  o->use_ext = in.use_ext;
+  o->use_gc = in.use_gc;
+  o->gc_freq = in.gc_freq;
+  o->rigid_bond = in.rigid;
+  o->eq_bond = in.r0;
+  std::snprintf(o->run_name, sizeof(o->run_name), "%s", in.run_name.c_str());
+  return PLUM_OK;
+}
+
+int plum_get_topology(const plum_ctx* c, int* mol_start, double* q, int* type) {
+  if (!c) return fail(PLUM_ERR_INPUT, "null context");
+  const Input& in = c->in;
+  if (mol_start) std::memcpy(mol_start, in.mol_start.data(), sizeof(int) * (in.n_mol + 1));
+  if (q) std::memcpy(q, in.q.data(), sizeof(double) * in.q.size());
+  if (type) std::memcpy(type, in.type.data(), sizeof(int) * in.type.size());
+  return PLUM_OK;
+}
+
+int plum_type_name(const plum_ctx* c, int type, char* buf, int cap) {
+  if (!c || !buf || cap <= 0) return fail(PLUM_ERR_INPUT, "bad argument");
+  if (type < 0 || type >= (int)c->in.type_names.size()) return fail(PLUM_ERR_INPUT, "bad type");
+  std::snprintf(buf, cap, "%s", c->in.type_names[type].c_str());
   return PLUM_OK;
 }
 

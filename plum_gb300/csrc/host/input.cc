@@ -50,14 +50,26 @@ std::string path_in(const std::string& dir, const std::string& name) {
 
 }  // namespace
 
+static bool read_stream(const std::string& dir, std::istream& f, Input* in, std::string* err);
+
 bool read_input(const std::string& dir, const std::string& runin, Input* in,
                 std::string* err) {
-  in->dir = dir;
   std::ifstream f(path_in(dir, runin));
   if (!f) {
     *err = "cannot open " + path_in(dir, runin);
     return false;
   }
+  return read_stream(dir, f, in, err);
+}
+
+bool read_input_text(const std::string& dir, const std::string& text, Input* in,
+                     std::string* err) {
+  std::istringstream f(text);
+  return read_stream(dir, f, in, err);
+}
+
+static bool read_stream(const std::string& dir, std::istream& f, Input* in, std::string* err) {
+  in->dir = dir;
   Reader r{f, err, false, "run.in"};
   int calc = 0;
   r.item(&in->crd_name, "coordinate file name");

@@ -76,5 +76,8 @@ struct Input {
 // malformed input.
 bool read_input(const std::string& dir, const std::string& runin, Input* in,
                 std::string* err);
+// Same, with the run.in content given as text (crd/top paths relative to dir).
+bool read_input_text(const std::string& dir, const std::string& runin_text, Input* in,
+                     std::string* err);
 
 }  // namespace plum

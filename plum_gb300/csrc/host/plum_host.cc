@@ -1,0 +1,502 @@
+// Host classes with the reference's public surface (include/plum_host.hpp).
+// Control flow and draw order follow the reference file by file; energies are
+// computed on the device through the C ABI.
+#include "../../../include/plum_host.hpp"
+#include "../../../include/plum_host_capi.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <iterator>
+#include <sstream>
+
+namespace plum {
+
+namespace {
+constexpr double kMax = 4294967295.0;  // std::mt19937::max()
+constexpr double kVeryLargeEnergy = 1e8;
+
+void check(int rc) {
+  if (rc != PLUM_OK) throw InputError(plum_last_error());
+}
+
+// randSphere (misc.cc:95-109)
+void rand_sphere(double* vec, std::mt19937& g) {
+  double rs = 2, r1 = 0, r2 = 0;
+  while (rs > 1) {
+    r1 = 1 - 2 * ((double)g() / kMax);
+    r2 = 1 - 2 * ((double)g() / kMax);
+    rs = r1 * r1 + r2 * r2;
+  }
+  double ranh = 2 * std::sqrt(1 - rs);
+  vec[0] = r1 * ranh;
+  vec[1] = r2 * ranh;
+  vec[2] = (1 - 2 * rs);
+}
+}  // namespace
+
+// ------------------------------------------------------------------ Bead
+Bead::Bead() {
+  for (int i = 0; i < 3; i++) current_[i] = trial_[i] = 0;
+}
+
+Bead::Bead(std::string symbol, int id, int c_id, double q, double x, double y, double z)
+    : q_(q), id_(id), c_id_(c_id), symbol_(symbol) {
+  trial_[0] = current_[0] = x;
+  trial_[1] = current_[1] = y;
+  trial_[2] = current_[2] = z;
+}
+
+double Bead::GetCrd(int flag, int index) const {
+  if (flag == 0) return current_[index];
+  if (flag == 1) return trial_[index];
+  throw InputError("Bead::GetCrd: invalid flag");
+}
+
+void Bead::SetCrd(int flag, int index, double value) {
+  if (flag == 0)
+    current_[index] = value;
+  else if (flag == 1)
+    trial_[index] = value;
+}
+
+void Bead::SetAllCrd(double pos[3]) {
+  for (int i = 0; i < 3; i++) current_[i] = trial_[i] = pos[i];
+}
+
+void Bead::UpdateCurrentPos() { std::memcpy(current_, trial_, sizeof(current_)); }
+void Bead::UpdateTrialPos() { std::memcpy(trial_, current_, sizeof(trial_)); }
+
+double Bead::BBDist(const Bead& o, const double box_l[], int npbc) const {
+  double dist = 0;
+  for (int i = 0; i < 3; i++) {
+    double d = trial_[i] - o.trial_[i];
+    if (i < npbc) {
+      d -= box_l[i] * std::round(d / box_l[i]);
+      if (std::fabs(d) > 0.5 * box_l[i]) d = box_l[i] - std::fabs(d);
+    }
+    dist += d * d;
+  }
+  return std::sqrt(dist);
+}
+
+// -------------------------------------------------------------- Molecule
+void Molecule::BeadTranslate(double move_size, double box_l[3], std::mt19937& g) {
+  (void)box_l;
+  double vec[3];
+  rand_sphere(vec, g);
+  double len = std::sqrt(vec[0] * vec[0] + vec[1] * vec[1] + vec[2] * vec[2]);
+  if (len > 0) len = 3 * move_size / len;  // ion step of 3 move sizes (molecule.cc:108-113)
+  bds[0].SetMoved();
+  for (int i = 0; i < 3; i++) bds[0].SetCrd(1, i, bds[0].GetCrd(0, i) + len * vec[i]);
+}
+
+void Molecule::COMTranslate(double move_size, std::mt19937& g) {
+  double vec[3];
+  for (int i = 0; i < 3; i++) vec[i] = 0.5 * move_size * (double)g() / kMax;
+  for (int i = 0; i < 3; i++)
+    if (g() % 2 == 0) vec[i] = -vec[i];
+  for (auto& b : bds) {
+    for (int j = 0; j < 3; j++) b.SetCrd(1, j, b.GetCrd(0, j) + vec[j]);
+    b.SetMoved();
+  }
+}
+
+void Molecule::Pivot(double move_size, std::mt19937& g, double eq, bool vary) {
+  const int len = Size();
+  int pivot = (int)std::floor(len * (double)g() / kMax);
+  if (pivot == len) pivot--;
+  const double s = move_size * (double)g() / kMax;
+  // Each bead is displaced by s * randSphere, put back at a bond length from
+  // its (already moved) neighbour toward the pivot, and the rest of that side
+  // follows by the same translation.
+  for (int dir = 0; dir < 2; dir++) {
+    const int step = dir == 0 ? 1 : -1;
+    for (int i = pivot + step; i >= 0 && i < len; i += step) {
+      double vec[3];
+      rand_sphere(vec, g);
+      const Bead& prev = bds[i - step];
+      double d[3];
+      for (int a = 0; a < 3; a++) d[a] = (bds[i].GetCrd(1, a) + s * vec[a]) - prev.GetCrd(1, a);
+      double bl = eq;
+      if (vary) bl += (eq / 5.0) * ((double)g() / kMax - 0.5);
+      const double norm = bl / std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      double m[3];
+      for (int a = 0; a < 3; a++) m[a] = (norm * d[a] + prev.GetCrd(1, a)) - bds[i].GetCrd(1, a);
+      for (int j = i; j >= 0 && j < len; j += step)
+        for (int a = 0; a < 3; a++) bds[j].SetCrd(1, a, bds[j].GetCrd(1, a) + m[a]);
+    }
+  }
+  for (auto& b : bds) b.SetMoved();
+}
+
+void Molecule::Crankshaft(double move_size, std::mt19937& g) {
+  const int len = Size();
+  int first = (int)std::floor((len - 2) * (double)g() / kMax);
+  int last = (int)std::floor((len - first) * (double)g() / kMax) + first;
+  if (last > len - 1) last = len - 1;  // the reference reads past the chain here
+  double ax[3];
+  for (int i = 0; i < 3; i++) ax[i] = bds[last].GetCrd(0, i) - bds[first].GetCrd(0, i);
+  double z = ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2];
+  if (z > 0)
+    for (int i = 0; i < 3; i++) ax[i] /= std::sqrt(z);
+  const double pi = 3.14159265358979323846;
+  const double angle = move_size * ((double)g() / kMax * 2 * pi - pi);
+  // Rodrigues rotation about the first->last axis.
+  const double sn = std::sin(angle), cs = std::cos(angle);
+  double R[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) R[i][j] = (1.0 - cs) * ax[i] * ax[j] + (i == j ? cs : 0.0);
+  R[0][1] -= sn * ax[2];
+  R[1][0] += sn * ax[2];
+  R[0][2] += sn * ax[1];
+  R[2][0] -= sn * ax[1];
+  R[1][2] -= sn * ax[0];
+  R[2][1] += sn * ax[0];
+  for (int i = first + 1; i < last; i++) {
+    bds[i].SetMoved();
+    double v[3];
+    for (int k = 0; k < 3; k++) v[k] = bds[i].GetCrd(0, k) - bds[first].GetCrd(0, k);
+    for (int k = 0; k < 3; k++)
+      bds[i].SetCrd(1, k, (R[k][0] * v[0] + R[k][1] * v[1]) + R[k][2] * v[2] +
+                              bds[first].GetCrd(0, k));
+  }
+}
+
+void Molecule::RandomReptation(std::mt19937& g, double eq, bool vary) {
+  if (eq < 0) throw InputError("reptation needs a rigid bond length");
+  double bl = eq;
+  if (vary) bl += (eq / 5.0) * ((double)g() / kMax - 0.5);
+  const int len = Size();
+  int dir = 1, begin = 0, end = len - 1;
+  if (g() % 2 == 0) {
+    dir = -1;
+    begin = len - 1;
+    end = 0;
+  }
+  for (int i = begin; i != end; i += dir)
+    for (int j = 0; j < 3; j++) bds[i].SetCrd(1, j, bds[i + dir].GetCrd(0, j));
+  double vec[3];
+  rand_sphere(vec, g);
+  const double vl = std::sqrt(vec[0] * vec[0] + vec[1] * vec[1] + vec[2] * vec[2]);
+  for (int i = 0; i < 3; i++) bds[end].SetCrd(1, i, bds[end].GetCrd(0, i) + bl * vec[i] / vl);
+  for (auto& b : bds) b.SetMoved();
+}
+
+// ------------------------------------------------------------ ForceField
+ForceField::~ForceField() {
+  if (ctx_) plum_ctx_destroy(ctx_);
+}
+
+void ForceField::Initialize(const std::string& dir, const std::string& runin_text,
+                            std::vector<Molecule>& mols, int form, int device) {
+  if (ctx_) plum_ctx_destroy(ctx_);
+  ctx_ = nullptr;
+  check(plum_ctx_create_text(dir.c_str(), runin_text.c_str(), form, device, &ctx_));
+  check(plum_ctx_info(ctx_, &info_));
+  check(plum_run_params(ctx_, &run_));
+  const int nb = info_.n_bead, nm = info_.n_mol;
+  mol_start_.assign(nm + 1, 0);
+  std::vector<double> q(nb), xyz(3 * (size_t)nb);
+  std::vector<int> type(nb);
+  check(plum_get_topology(ctx_, mol_start_.data(), q.data(), type.data()));
+  check(plum_get_positions(ctx_, xyz.data()));
+  std::vector<std::string> names(info_.n_type);
+  for (int t = 0; t < info_.n_type; t++) {
+    char buf[64];
+    check(plum_type_name(ctx_, t, buf, sizeof buf));
+    names[t] = buf;
+  }
+  mols.assign(nm, Molecule());
+  int id = 0;
+  for (int m = 0; m < nm; m++)
+    for (int i = mol_start_[m]; i < mol_start_[m + 1]; i++) {
+      Bead b(names[type[i]], id++, m, q[i], xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+      b.SetType(type[i]);
+      mols[m].AddBead(b);
+    }
+}
+
+void ForceField::InitializeEnergy(std::vector<Molecule>& mols) {
+  (void)mols;
+  double out[8];
+  check(plum_total_energy(ctx_, out));
+}
+
+double ForceField::EnergyDifference(std::vector<Molecule>& mols, int mol) {
+  const Molecule& M = mols[mol];
+  std::vector<double> trial(3 * (size_t)M.Size());
+  std::vector<int> moved(M.Size());
+  for (int i = 0; i < M.Size(); i++) {
+    for (int a = 0; a < 3; a++) trial[3 * i + a] = M.bds[i].GetCrd(1, a);
+    moved[i] = M.bds[i].GetMoved();
+  }
+  double out[5];
+  check(plum_delta_energy(ctx_, mol, trial.data(), moved.data(), out));
+  return out[0];
+}
+
+void ForceField::FinalizeEnergies(std::vector<Molecule>& mols, bool accept, int mol) {
+  (void)mols;
+  (void)mol;
+  check(plum_finalize(ctx_, accept ? 1 : 0));
+}
+
+static double term(plum_ctx* c, int k) {
+  double e[4];
+  check(plum_energies(c, e));
+  return e[k];
+}
+double ForceField::TotPairEnergy() { return term(ctx_, 0); }
+double ForceField::TotEwaldEnergy() { return term(ctx_, 1); }
+double ForceField::TotBondEnergy() { return term(ctx_, 2); }
+double ForceField::TotExtEnergy() { return term(ctx_, 3); }
+
+double ForceField::EqBondLen() const {
+  if (!run_.use_bond) throw InputError("Illegal request of bond length");
+  return run_.eq_bond;
+}
+
+// ------------------------------------------------------------ Simulation
+Simulation::Simulation(std::istream& runin, const std::string& dir, unsigned seed, int form,
+                       int device) {
+  std::string text((std::istreambuf_iterator<char>(runin)), std::istreambuf_iterator<char>());
+  force_field.Initialize(dir, text, mols, form, device);
+  run_ = force_field.RunInfo();
+  const plum_info& info = force_field.Info();
+  for (int a = 0; a < 3; a++) box_l[a] = info.box[a];
+  npbc = info.npbc;
+  rand_gen.seed(seed);
+  UpdateMolCounts();
+}
+
+void Simulation::UpdateMolCounts() {
+  n_mol = (int)mols.size();
+  n_chain = n_cion = n_aion = n_nion = 0;
+  for (int i = run_.phantom; i < n_mol; i++) {
+    if (mols[i].Size() > 1)
+      n_chain++;
+    else if (mols[i].bds[0].Charge() > 0)
+      n_cion++;
+    else if (mols[i].bds[0].Charge() < 0)
+      n_aion++;
+    else
+      n_nion++;
+  }
+  n_chain -= run_.grafted;
+}
+
+void Simulation::TranslationalMove() {
+  last_move_type = -1;
+  last_accept = 0;
+  if (n_mol - run_.phantom <= 0) return;
+  const int n_ch = run_.grafted + n_chain, n_io = n_cion + n_aion + n_nion;
+  int chain_id = -1, ion_id = -1, mol_id = -1;
+  int which_chain = (int)std::floor((double)rand_gen() / kMax * n_ch);
+  int which_ion = (int)std::floor((double)rand_gen() / kMax * n_io);
+  if (which_chain == n_ch) which_chain--;
+  if (which_ion == n_io) which_ion--;
+  int cc = -1, ic = -1;
+  for (int i = run_.phantom; i < n_mol; i++) {
+    if (mols[i].Size() > 1)
+      cc++;
+    else
+      ic++;
+    if (cc == which_chain) {
+      chain_id = i;
+      which_chain = -2;
+    }
+    if (ic == which_ion) {
+      ion_id = i;
+      which_ion = -2;
+    }
+  }
+  int move_type = 0;
+  const double u = (double)rand_gen() / kMax;
+  double cur = run_.move_prob[0];
+  while (cur < u && move_type < 4) cur += run_.move_prob[++move_type];
+  if (cur < u) move_type++;
+  if (move_type > 4) move_type = 4;
+  if (move_type == 0 && n_io > 0) {
+    mol_id = ion_id;
+    mols[mol_id].BeadTranslate(run_.move_size, box_l, rand_gen);
+  } else if (n_ch > 0) {
+    mol_id = chain_id;
+    double bond_len = 0;
+    bool vary = false;
+    if (force_field.UseBondRigid()) bond_len = force_field.RigidBondLen();
+    if (force_field.UseBondPot()) {
+      bond_len = force_field.EqBondLen();
+      vary = true;
+    }
+    switch (move_type) {
+      case 1: mols[mol_id].COMTranslate(run_.move_size, rand_gen); break;
+      case 2: mols[mol_id].Pivot(run_.move_size, rand_gen, bond_len, vary); break;
+      case 3: mols[mol_id].Crankshaft(run_.move_size, rand_gen); break;
+      case 4: mols[mol_id].RandomReptation(rand_gen, bond_len, vary); break;
+    }
+  }
+  if (!((move_type == 0 && n_io > 0) || (move_type > 0 && n_ch > 0))) return;
+  attempted[move_type]++;
+  const double dE = force_field.EnergyDifference(mols, mol_id);
+  bool accept = false;
+  if (!(dE >= kVeryLargeEnergy)) accept = (double)rand_gen() / kMax < std::exp(-run_.beta * dE);
+  force_field.FinalizeEnergies(mols, accept, mol_id);
+  for (auto& b : mols[mol_id].bds) {
+    if (accept)
+      b.UpdateCurrentPos();
+    else
+      b.UpdateTrialPos();
+    b.UnsetMoved();
+  }
+  if (accept) accepted[move_type]++;
+  last_move_type = move_type;
+  last_accept = accept;
+}
+
+void Simulation::RunSteps(long n) {
+  if (force_field.UseGC()) throw InputError("grand-canonical steps are not run by this loop");
+  int max_len = 1;
+  for (auto& m : mols) max_len = std::max(max_len, m.Size());
+  while (n > 0) {
+    const int chunk = (int)std::min<long>(n, 4096);
+    // The device consumes the same mt19937 words rand_gen would produce; the
+    // generator is then advanced by exactly the words used. Budget: a pivot
+    // takes 2 + len (2 r + 1) draws with r rejected pairs (mean 1.27).
+    std::mt19937 g0 = rand_gen;
+    const long words = (long)chunk * (16 + 6L * max_len) + 65536L;
+    std::vector<uint32_t> stream(words);
+    for (long i = 0; i < words; i++) stream[i] = rand_gen();
+    long used = 0;
+    check(plum_run_moves(force_field.Context(), stream.data(), words, chunk, nullptr, nullptr,
+                         nullptr, &used));
+    rand_gen = g0;
+    rand_gen.discard((unsigned long long)used);
+    step += chunk;
+    n -= chunk;
+  }
+  SyncFromDevice();
+}
+
+void Simulation::Run() {
+  for (long s = 0; s < run_.steps;) {
+    long to_sample = run_.sample_freq > 0 ? run_.sample_freq - (step % run_.sample_freq) : run_.steps;
+    long n = std::min(to_sample, run_.steps - s);
+    RunSteps(n);
+    s += n;
+    Sample();
+  }
+}
+
+void Simulation::SyncFromDevice() {
+  const int nb = force_field.Info().n_bead;
+  std::vector<double> xyz(3 * (size_t)nb);
+  check(plum_get_positions(force_field.Context(), xyz.data()));
+  int k = 0;
+  for (auto& m : mols)
+    for (auto& b : m.bds) {
+      double p[3] = {xyz[3 * k], xyz[3 * k + 1], xyz[3 * k + 2]};
+      b.SetAllCrd(p);
+      k++;
+    }
+}
+
+void Simulation::Sample() {
+  if (!(step > run_.steps_eq && run_.sample_freq > 0 && step % run_.sample_freq == 0)) return;
+  ff_avg_counter++;
+  double e[4];
+  check(plum_energies(force_field.Context(), e));
+  pair_e_cumu += e[0];
+  ewald_e_cumu += e[1];
+  bond_e_cumu += e[2];
+  ext_e_cumu += e[3];
+  mol_avg_counter++;
+  double o[5];
+  check(plum_observables(force_field.Context(), o));
+  rg_tot_cumu += o[0];
+}
+
+double Simulation::RadiusOfGyration() {
+  double o[5];
+  check(plum_observables(force_field.Context(), o));
+  return o[0];
+}
+
+double Simulation::EndToEndDistance() {
+  double o[5];
+  check(plum_observables(force_field.Context(), o));
+  return o[4];
+}
+
+}  // namespace plum
+
+// ---------------------------------------------------------------- C driver
+// Drives the host classes from a C caller (used by the tests and the CLI).
+extern "C" {
+
+struct plum_sim {
+  plum::Simulation* s;
+};
+
+int plum_sim_create(const char* dir, const char* runin_text, unsigned seed, int form,
+                    plum_sim** out) {
+  try {
+    std::istringstream is(runin_text);
+    *out = new plum_sim{new plum::Simulation(is, dir, seed, form, 0)};
+    return PLUM_OK;
+  } catch (const std::exception& e) {
+    *out = nullptr;
+    return PLUM_ERR_INPUT;
+  }
+}
+
+int plum_sim_destroy(plum_sim* s) {
+  if (s) {
+    delete s->s;
+    delete s;
+  }
+  return PLUM_OK;
+}
+
+int plum_sim_translational_moves(plum_sim* s, int n, int* move_type, int* accept) {
+  try {
+    for (int i = 0; i < n; i++) {
+      (void)s->s->rand_gen();  // simulation.cc:221, the grand-canonical check draw
+      s->s->TranslationalMove();
+      s->s->step++;
+      if (move_type) move_type[i] = s->s->last_move_type;
+      if (accept) accept[i] = s->s->last_accept;
+    }
+    return PLUM_OK;
+  } catch (const std::exception&) {
+    return PLUM_ERR_STATE;
+  }
+}
+
+int plum_sim_run_steps(plum_sim* s, long n) {
+  try {
+    s->s->RunSteps(n);
+    return PLUM_OK;
+  } catch (const std::exception&) {
+    return PLUM_ERR_STATE;
+  }
+}
+
+// host-side positions (current), n_bead*3
+int plum_sim_positions(plum_sim* s, double* xyz) {
+  int k = 0;
+  for (auto& m : s->s->mols)
+    for (auto& b : m.bds)
+      for (int a = 0; a < 3; a++) xyz[k++] = b.GetCrd(0, a);
+  return PLUM_OK;
+}
+
+int plum_sim_energies(plum_sim* s, double* out) {
+  out[0] = s->s->force_field.TotPairEnergy();
+  out[1] = s->s->force_field.TotEwaldEnergy();
+  out[2] = s->s->force_field.UseBondPot() ? s->s->force_field.TotBondEnergy() : 0.0;
+  out[3] = s->s->force_field.UseExtPot() ? s->s->force_field.TotExtEnergy() : 0.0;
+  return PLUM_OK;
+}
+
+}  // extern "C"

@@ -29,6 +29,25 @@ __device__ __forceinline__ float fdiff(int a, int b, float scale) {
   return (float)(int)((unsigned)b - (unsigned)a) * scale;
 }
 
+// erfc for x >= 0 by the Chebyshev fit of Press et al., Numerical Recipes
+// (2nd ed., section 6.2, "erfcc"): erfc(x) = t exp(-x^2 + P9(t)),
+// t = 1 / (1 + x/2), fractional error below 1.2e-7 for every x >= 0 -- at the
+// level of FP32 rounding, for about a third of erfcf's instructions.
+__device__ __forceinline__ float erfc_nr(float x) {
+  const float t = __fdividef(1.0f, fmaf(0.5f, x, 1.0f));
+  float p = 0.17087277f;
+  p = fmaf(p, t, -0.82215223f);
+  p = fmaf(p, t, 1.48851587f);
+  p = fmaf(p, t, -1.13520398f);
+  p = fmaf(p, t, 0.27886807f);
+  p = fmaf(p, t, -0.18628806f);
+  p = fmaf(p, t, 0.09678418f);
+  p = fmaf(p, t, 0.37409196f);
+  p = fmaf(p, t, 1.00002368f);
+  p = fmaf(p, t, -1.26551223f);
+  return t * __expf(fmaf(-x, x, p));
+}
+
 __device__ __forceinline__ float lj32(const DevParams& P, int k, float r2) {
   if (r2 <= 0.0f) return (float)kVeryLarge;
   if (r2 < P.f_lj_rc2[k]) {
@@ -49,7 +68,7 @@ __device__ __forceinline__ float real_images32(const DevParams& P, float dx, flo
     if (r2 > 0.0f) {
       const float ir = rsqrtf(r2);
       const float r = r2 * ir;
-      if (r <= rc) e = erfcf(P.f_sqrt_alpha * r) * ir;
+      if (r <= rc) e = erfc_nr(P.f_sqrt_alpha * r) * ir;
     }
     return e;
   }
@@ -66,7 +85,7 @@ __device__ __forceinline__ float real_images32(const DevParams& P, float dx, flo
         if (r2 > 0.0f) {
           float ir = rsqrtf(r2);
           float r = r2 * ir;
-          if (r <= rc) e += erfcf(P.f_sqrt_alpha * r) * ir;
+          if (r <= rc) e += erfc_nr(P.f_sqrt_alpha * r) * ir;
         }
       }
     }

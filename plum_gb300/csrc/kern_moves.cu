@@ -81,6 +81,31 @@ __device__ long long sphere_scan(Draws& d) {
   return -1;
 }
 
+// Same, using accept bits precomputed by the block for every window
+// position p: bit p set when the pair (p, p+1) is accepted. A pair starting at
+// `pos` is followed by the pair at pos+2, so thread 0 looks for the next set
+// bit of pos's parity; past the window it falls back to sphere_scan.
+__device__ long long sphere_scan_bits(Draws& d, const unsigned* accbits) {
+  const long long rel0 = d.pos - d.wbase;
+  if (rel0 < 0) return sphere_scan(d);
+  long long rel = rel0;
+  while (rel + 1 < d.wlen) {
+    const int w = (int)(rel >> 5), b = (int)(rel & 31);
+    const unsigned par = (rel & 1) ? 0xAAAAAAAAu : 0x55555555u;
+    const unsigned msk = accbits[w] & par & (0xFFFFFFFFu << b);
+    if (msk) {
+      const long long p = ((long long)w << 5) + (__ffs(msk) - 1);
+      d.pos = d.wbase + p + 2;
+      return d.wbase + p;
+    }
+    rel = ((long long)(w + 1) << 5) + (rel0 & 1);
+  }
+  // every pair of this parity inside the window was rejected: continue from
+  // the first pair not covered by the bits
+  if (rel0 + 1 < d.wlen) d.pos = d.wbase + rel0 + 2 * ((d.wlen - rel0) / 2);
+  return sphere_scan(d);
+}
+
 // The unit vector randSphere returns for an accepted pair.
 __device__ void sphere_vec(uint32_t u1, uint32_t u2, double* v) {
   double r1 = 1.0 - 2.0 * ((double)u1 / kMtMax);
@@ -92,8 +117,8 @@ __device__ void sphere_vec(uint32_t u1, uint32_t u2, double* v) {
   v[2] = (1.0 - 2.0 * rs);
 }
 
-__device__ void rand_sphere(Draws& d, double* v) {
-  long long o = sphere_scan(d);
+__device__ void rand_sphere(Draws& d, double* v, const unsigned* accbits) {
+  long long o = sphere_scan_bits(d, accbits);
   if (o < 0) {
     v[0] = v[1] = 0.0;
     v[2] = 1.0;
@@ -134,7 +159,8 @@ constexpr int kPivotMax = 512;  // chains up to this length pivot in parallel
 // applies the geometry.
 __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B, DevState& S,
                                       Draws& d, long long wbase, GenPlan& plan, int* s_off,
-                                      int* s_boff, double (*s_w)[kPivotMax]) {
+                                      int* s_boff, double (*s_w)[kPivotMax],
+                                      const unsigned* accbits) {
   DevState* const st = &S;
   // ----------------------------------------------------- generate next move
   if (threadIdx.x == 0) {
@@ -176,7 +202,7 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
         if (mt == 0) {
           // Molecule::BeadTranslate (molecule.cc:103-133)
           double v[3];
-          rand_sphere(d, v);
+          rand_sphere(d, v, accbits);
           double vl = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
           if (vl > 0) vl = 3 * P.move_size / vl;
           for (int a = 0; a < 3; a++) plan.vec[a] = vl * v[a];
@@ -201,7 +227,7 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
             for (int dirn = 0; dirn < 2; dirn++) {
               int i = dirn == 0 ? pivot + 1 : pivot - 1;
               for (; dirn == 0 ? i < len : i >= 0; i += dirn == 0 ? 1 : -1) {
-                long long o = sphere_scan(d);
+                long long o = sphere_scan_bits(d, accbits);
                 s_off[i] = (int)(o - wbase);
                 if (P.vary_bond) {
                   s_boff[i] = (int)(d.pos - wbase);
@@ -220,7 +246,7 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
               int i = dirn == 0 ? pivot + 1 : pivot - 1;
               for (; dirn == 0 ? i < len : i >= 0; i += dirn == 0 ? 1 : -1) {
                 double v[3];
-                rand_sphere(d, v);
+                rand_sphere(d, v, accbits);
                 double4_32a o = B.pos[b0 + i];
                 double p[3] = {o.x + T[0], o.y + T[1], o.z + T[2]};
                 double dx = (p[0] + s * v[0]) - prev[0];
@@ -281,7 +307,7 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
             end = 0;
           }
           double v[3];
-          rand_sphere(d, v);
+          rand_sphere(d, v, accbits);
           double vl = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
           for (int a = 0; a < 3; a++) plan.vec[a] = bl * v[a] / vl;
           plan.dir = dir;
@@ -395,6 +421,7 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
 __global__ void __launch_bounds__(kSerialThreads)
     k_serial64(const DevParams P, const DevBuffers B, int mode) {
   __shared__ uint32_t win[kDrawWindow];
+  __shared__ unsigned accbits[kDrawWindow / 32];  // randSphere acceptance per position
   __shared__ double red[kSerialThreads / 32];
   __shared__ GenPlan plan;
   __shared__ int s_accept, s_ext_bad;
@@ -421,6 +448,18 @@ __global__ void __launch_bounds__(kSerialThreads)
     for (int i = threadIdx.x; i < wlen; i += blockDim.x) win[i] = B.stream[wbase + i];
   }
   __syncthreads();
+  if (mode & kModeGen) {
+    // every window position's randSphere test, 32 positions per thread-word
+    for (int w = threadIdx.x; w < kDrawWindow / 32; w += blockDim.x) {
+      unsigned bits = 0u;
+      for (int k = 0; k < 32; k++) {
+        const int p = w * 32 + k;
+        if (p + 1 < wlen && !sphere_reject(win[p], win[p + 1])) bits |= 1u << k;
+      }
+      accbits[w] = bits;
+    }
+    __syncthreads();
+  }
   Draws d{B.stream, win, wbase, S.stream_len, wbase, wlen, 0};
 
   const int pending = S.pending;
@@ -551,7 +590,8 @@ __global__ void __launch_bounds__(kSerialThreads)
   }
   __syncthreads();
 
-  if ((mode & kModeGen) && !S.error) gen_move(P, B, S, d, wbase, plan, s_off, s_boff, s_w);
+  if ((mode & kModeGen) && !S.error)
+    gen_move(P, B, S, d, wbase, plan, s_off, s_boff, s_w, accbits);
 
   // write the state back
   if (threadIdx.x == 0) S.stream_pos = S.stream_pos > d.pos ? S.stream_pos : d.pos;
