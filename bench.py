@@ -181,11 +181,11 @@ def run_reference_arm(args, rank, world):
     return 0
 
 
-def make_workload(name):
+def make_workload(name, seed=20261203):
     from plum_gb300 import systems
-    d = os.path.join(tempfile.gettempdir(), "plum_bench_" + name)
+    d = os.path.join(tempfile.gettempdir(), "plum_bench_%s_%d" % (name, seed))
     if not os.path.exists(os.path.join(d, "run.in")):
-        systems.write_bulk(d, systems.CONFIGS[name], seed=20261203)
+        systems.write_bulk(d, systems.CONFIGS[name], seed=seed)
     return d
 
 
@@ -211,7 +211,10 @@ def main():
     ap.add_argument("--samples-seconds", type=float, default=0.0)
     ap.add_argument("--cpu-moves", type=int, default=20)
     ap.add_argument("--ref-moves", type=int, default=10)
-    ap.add_argument("--only", default=None, choices=[None, "fp32", "fp64"],
+    ap.add_argument("--replicas", type=int, default=16,
+                    help="replicas of the workload in the batched form (the chosen form)")
+    ap.add_argument("--batch-steps", type=int, default=256)
+    ap.add_argument("--only", default=None, choices=[None, "fp32", "fp64", "batch"],
                     help="profiling runs: time one form only, no baselines or e2e")
     args = ap.parse_args()
 
@@ -239,6 +242,18 @@ def main():
     s64.seed(1234 + rank)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
+    if args.only == "batch":
+        b = pg.Batch([make_workload(args.workload, seed=20261203 + r) for r in range(args.replicas)],
+                     device=local)
+        b.seed(77)
+        for _ in range(args.warmup + args.steps):
+            b.run(args.batch_steps)
+        ms, k = b.last_timing()
+        print(json.dumps({"profile_run": "batch", "replicas": args.replicas,
+                          "steps": args.batch_steps, "last_ms": ms,
+                          "moves_per_s": args.replicas * args.batch_steps / (ms / 1e3)}),
+              flush=True)
+        return 0
     if args.only:
         s = s32 if args.only == "fp32" else s64
         for _ in range(args.warmup + args.steps):
@@ -249,7 +264,13 @@ def main():
                           "moves_per_s": M / (ms / 1e3)}), flush=True)
         return 0
 
+    # the chosen form: replicas of the workload in one batch (precision form)
+    R, BS = args.replicas, args.batch_steps
+    batch = pg.Batch([make_workload(args.workload, seed=20261203 + r) for r in range(R)],
+                     device=local)
+    batch.seed(1000 * rank + 77)
     for _ in range(args.warmup):
+        batch.run(BS)
         s32.run(M)
         s64.run(args.plain_moves_per_step)
 
@@ -263,8 +284,8 @@ def main():
     for _ in range(args.steps):
         flush.zero_()          # L2 flush between steps (outside the step's events)
         torch.cuda.synchronize()
-        s32.run(M)
-        ms, k = s32.last_timing()
+        batch.run(BS)
+        ms, k = batch.last_timing()
         dev_ms.append(ms)
         kernels += k
     torch.cuda.synchronize()
@@ -275,7 +296,14 @@ def main():
         t = torch.tensor([step_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         step_ms = float(t.item())
-    value = world * M / (step_ms / 1e3)
+    value = world * R * BS / (step_ms / 1e3)
+
+    # one replica of the precision form alone
+    f_ms = []
+    for _ in range(3):
+        s32.run(M)
+        f_ms.append(s32.last_timing()[0])
+    single32 = M / (statistics.mean(f_ms) / 1e3)
 
     # plain FP64 on the same system
     p_ms = []
@@ -307,7 +335,7 @@ def main():
     frac_in = (4.0 / 3.0) * math.pi * info.real_cutoff ** 3 / (info.box[0] ** 3)
     W = alg_flops_per_move(info.n_bead, mean_moved, info.n_kvec, min(1.0, frac_in), mean_bonds)
     peak, peak64 = pg.probe_peaks(local)
-    achieved = W * (M / (step_ms / 1e3)) / 1e12
+    achieved = W * (R * BS / (step_ms / 1e3)) / 1e12
 
     samples = None
     if args.samples_seconds > 0:
@@ -340,14 +368,19 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": args.workload, "n_bead": info.n_bead, "n_kvec_half": info.n_kvec,
-                   "real_cutoff": info.real_cutoff, "moves_per_step": M,
-                   "form": "precision (FP32 pair/k, FP64 S(k) and totals)",
+                   "real_cutoff": info.real_cutoff, "replicas": R, "steps_per_batch": BS,
+                   "moves_per_step": R * BS,
+                   "form": "batched replicas, precision form (FP32 pair/k, FP64 S(k) and "
+                           "totals, FP64 recompute every 1e4 moves)",
                    "l2": "flushed between steps (256 MB write)", "parallelism": "replicas"},
+        "single_replica_fp32": {"value": single32, "unit": "moves/s", "moves_per_step": M},
         "plain_fp64": {"value": plain, "unit": "moves/s",
                        "moves_per_step": args.plain_moves_per_step},
         "speedup_vs_plain_fp64": value / plain,
         "e2e": {"value": e2e, "unit": "moves/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h),
+                "path": "plum_run_moves: one replica, precision form, recorded mt19937 stream "
+                        "copied in and per-move logs copied out in the timed region"},
         "gpu_launches": int(kernels),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,

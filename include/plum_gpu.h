@@ -166,6 +166,31 @@ int plum_last_timing(const plum_ctx* ctx, double* ms, long* kernels);
  * the tensor cores. No reference counterpart. */
 int plum_probe_peaks(int device, double* fp32_tflops, double* fp64_tflops);
 
+/* ---------------------------------------------------------------- replicas
+ * Many independent systems (replicas, of uneven size) advanced together on
+ * one GPU in the precision form: per step every replica attempts one move;
+ * one launch evaluates all replicas' energy differences from a shared item
+ * list (pair and k-space work items of every replica's pending move), one
+ * launch runs every replica's serial step (one block each). Replica r draws
+ * from its own device mt19937 seeded seed + r. Batches of steps are replayed
+ * as a CUDA graph. No reference counterpart: the reference runs one system
+ * per process (simulation.cc:216-239). */
+typedef struct plum_batch plum_batch;
+int plum_batch_create(int n, const char* const* dirs, const char* const* runins, int form,
+                      int device, plum_batch** out);
+int plum_batch_destroy(plum_batch* batch);
+int plum_batch_seed(plum_batch* batch, uint32_t seed);
+/* Seeds replica r's generator with seeds[r]. */
+int plum_batch_seed_each(plum_batch* batch, const uint32_t* seeds);
+/* n_steps moves per replica; *accepted_out = accepted moves summed over
+ * replicas. */
+int plum_batch_run(plum_batch* batch, int n_steps, long* accepted_out);
+int plum_batch_size(const plum_batch* batch);
+/* The context of replica r (owned by the batch): energies, positions and
+ * observables through the single-system calls above. */
+int plum_batch_replica(plum_batch* batch, int r, plum_ctx** ctx);
+int plum_batch_last_timing(const plum_batch* batch, double* ms, long* kernels);
+
 #ifdef __cplusplus
 }
 #endif

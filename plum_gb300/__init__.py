@@ -72,6 +72,16 @@ def lib():
         L.plum_set_recompute.argtypes = [C.c_void_p, C.c_long]
         L.plum_drift.argtypes = [C.c_void_p, _dp]
         L.plum_probe_peaks.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.plum_batch_create.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p),
+                                        C.c_int, C.c_int, C.POINTER(C.c_void_p)]
+        L.plum_batch_destroy.argtypes = [C.c_void_p]
+        L.plum_batch_seed.argtypes = [C.c_void_p, C.c_uint32]
+        L.plum_batch_seed_each.argtypes = [C.c_void_p, _up]
+        L.plum_batch_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_long)]
+        L.plum_batch_size.argtypes = [C.c_void_p]
+        L.plum_batch_replica.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
+        L.plum_batch_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_double),
+                                             C.POINTER(C.c_long)]
         L.plum_sim_create.argtypes = [C.c_char_p, C.c_char_p, C.c_uint, C.c_int,
                                       C.POINTER(C.c_void_p)]
         L.plum_sim_destroy.argtypes = [C.c_void_p]
@@ -190,6 +200,66 @@ class System:
         ms = C.c_double(0)
         k = C.c_long(0)
         _check(lib().plum_last_timing(self.h, C.byref(ms), C.byref(k)))
+        return ms.value, k.value
+
+
+class _Replica(System):
+    """A replica context owned by a Batch (not destroyed by this object)."""
+
+    def __init__(self, h):
+        self.h = h
+        info = Info()
+        _check(lib().plum_ctx_info(self.h, C.byref(info)))
+        self.info = info
+        self.n_bead = info.n_bead
+        self.n_mol = info.n_mol
+
+    def close(self):
+        self.h = None
+
+
+class Batch:
+    """Independent replicas (possibly of different systems) advanced together
+    in the precision form: one move per replica per step."""
+
+    def __init__(self, dirs, runins=None, form: int = FORM_FP32, device: int = 0):
+        n = len(dirs)
+        runins = runins or ["run.in"] * n
+        d = (C.c_char_p * n)(*[x.encode() for x in dirs])
+        r = (C.c_char_p * n)(*[x.encode() for x in runins])
+        h = C.c_void_p()
+        _check(lib().plum_batch_create(n, d, r, form, device, C.byref(h)))
+        self.h = h
+        self.n = n
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().plum_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def seed(self, seed):
+        if np.ndim(seed) == 0:
+            _check(lib().plum_batch_seed(self.h, int(seed)))
+        else:
+            _check(lib().plum_batch_seed_each(self.h, np.ascontiguousarray(seed, np.uint32)))
+
+    def run(self, n_steps):
+        acc = C.c_long(0)
+        _check(lib().plum_batch_run(self.h, n_steps, C.byref(acc)))
+        return acc.value
+
+    def replica(self, r) -> System:
+        h = C.c_void_p()
+        _check(lib().plum_batch_replica(self.h, r, C.byref(h)))
+        return _Replica(h)
+
+    def last_timing(self):
+        ms = C.c_double(0)
+        k = C.c_long(0)
+        _check(lib().plum_batch_last_timing(self.h, C.byref(ms), C.byref(k)))
         return ms.value, k.value
 
 

@@ -998,3 +998,286 @@ int plum_last_timing(const plum_ctx* c, double* ms, long* kernels) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------ batches
+struct plum_batch {
+  std::vector<plum_ctx*> reps;
+  int device = 0;
+  cudaStream_t s = nullptr;
+  DevParams* d_rp = nullptr;
+  DevBuffers* d_rb = nullptr;
+  int* d_item_off = nullptr;
+  double* d_slots = nullptr;
+  size_t kt_smem = 0;
+  // per-replica streams
+  std::vector<long long> cap, per_step;
+  uint32_t** d_states = nullptr;
+  uint32_t** d_outs = nullptr;
+  DevState** d_sts = nullptr;
+  long long *d_pos = nullptr, *d_len = nullptr, *d_cap = nullptr, *d_gather = nullptr;
+  int* d_need = nullptr;
+  long long* h_gather = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int g_steps = 0;
+  bool g_warm = false;
+  int batch_steps = 32;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0;
+  long last_kernels = 0;
+};
+
+namespace {
+
+void batch_enqueue(plum_batch* b, int steps) {
+  const int R = (int)b->reps.size();
+  launch_batch_serial(b->d_rp, b->d_rb, b->d_item_off, b->d_slots, R, kModeGen, b->s);
+  for (int i = 0; i < steps; i++) {
+    launch_batch_delta32(b->d_rp, b->d_rb, R, b->d_item_off, b->d_slots, b->kt_smem, b->s);
+    int mode = kModeFinish | kModeDecide | (i + 1 < steps ? kModeGen : 0);
+    launch_batch_serial(b->d_rp, b->d_rb, b->d_item_off, b->d_slots, R, mode, b->s);
+  }
+}
+
+int batch_steps_graph(plum_batch* b, int steps) {
+  if (b->gexec && b->g_steps == steps) {
+    CK(cudaGraphLaunch(b->gexec, b->s));
+    return PLUM_OK;
+  }
+  if (b->g_warm) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(b->s, cudaStreamCaptureModeThreadLocal));
+    batch_enqueue(b, steps);
+    CK(cudaStreamEndCapture(b->s, &g));
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    b->gexec = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&b->gexec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(PLUM_ERR_CUDA, cudaGetErrorString(e));
+    b->g_steps = steps;
+    CK(cudaGraphLaunch(b->gexec, b->s));
+    return PLUM_OK;
+  }
+  b->g_warm = true;
+  batch_enqueue(b, steps);
+  CK(cudaGetLastError());
+  return PLUM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int plum_batch_destroy(plum_batch* b) {
+  if (!b) return PLUM_OK;
+  cudaSetDevice(b->device);
+  if (b->s) cudaStreamSynchronize(b->s);
+  for (plum_ctx* c : b->reps) plum_ctx_destroy(c);
+  void* ptrs[] = {b->d_rp,    b->d_rb,  b->d_item_off, b->d_slots, b->d_states, b->d_outs,
+                  b->d_sts,   b->d_pos, b->d_len,      b->d_cap,   b->d_gather, b->d_need};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (b->h_gather) cudaFreeHost(b->h_gather);
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->s) cudaStreamDestroy(b->s);
+  delete b;
+  return PLUM_OK;
+}
+
+int plum_batch_create(int n, const char* const* dirs, const char* const* runins, int form,
+                      int device, plum_batch** out) {
+  if (!out || n <= 0 || !dirs || !runins) return fail(PLUM_ERR_INPUT, "bad argument");
+  if (n > kMaxReplicas) return fail(PLUM_ERR_INPUT, "too many replicas");
+  if (form != PLUM_FORM_FP32) return fail(PLUM_ERR_INPUT, "replica batches run the precision form");
+  *out = nullptr;
+  plum_batch* b = new plum_batch();
+  b->device = device;
+  for (int r = 0; r < n; r++) {
+    plum_ctx* c = nullptr;
+    int rc = plum_ctx_create(dirs[r], runins[r], form, device, &c);
+    if (rc) {
+      std::string msg = "replica " + std::to_string(r) + ": " + g_err;
+      plum_batch_destroy(b);
+      return fail(rc, msg);
+    }
+    if (c->in.use_gc) {
+      plum_ctx_destroy(c);
+      plum_batch_destroy(b);
+      return fail(PLUM_ERR_INPUT, "grand-canonical replicas are not batched");
+    }
+    b->reps.push_back(c);
+  }
+  cudaSetDevice(device);
+  cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking);
+  cudaEventCreate(&b->ev0);
+  cudaEventCreate(&b->ev1);
+  std::vector<DevParams> hp(n);
+  std::vector<DevBuffers> hb(n);
+  std::vector<uint32_t*> hst(n), hout(n);
+  std::vector<DevState*> hsts(n);
+  long long items = 0;
+  b->cap.resize(n);
+  b->per_step.resize(n);
+  for (int r = 0; r < n; r++) {
+    plum_ctx* c = b->reps[r];
+    const DevParams& P = c->P;
+    b->per_step[r] = 16 + 10LL * c->max_len;
+    b->cap[r] = std::max<long long>(4 * b->batch_steps * b->per_step[r], 1 << 16);
+    int rc = ensure_stream(c, b->cap[r]);
+    if (rc) {
+      plum_batch_destroy(b);
+      return rc;
+    }
+    hp[r] = P;
+    hb[r] = c->B;
+    hb[r].stream = c->d_stream;
+    hb[r].log_type = nullptr;
+    hb[r].log_accept = nullptr;
+    hb[r].log_etot = nullptr;
+    hst[r] = c->d_mt;
+    hout[r] = c->d_stream;
+    hsts[r] = c->B.state;
+    items += ((long long)c->max_len * P.n_bead + 4095) / 4096 + (P.n_k + 127) / 128;
+    size_t sm = P.use_ewald ? (size_t)P.kchunk_delta * 2 * P.kper * sizeof(float2) : 0;
+    b->kt_smem = std::max(b->kt_smem, sm);
+  }
+  int rc = 0;
+  rc |= dalloc(&b->d_rp, n);
+  rc |= dalloc(&b->d_rb, n);
+  rc |= dalloc(&b->d_item_off, 4 * (size_t)n);
+  rc |= dalloc(&b->d_slots, 2 * (size_t)items + 2);
+  rc |= dalloc(&b->d_states, n);
+  rc |= dalloc(&b->d_outs, n);
+  rc |= dalloc(&b->d_sts, n);
+  rc |= dalloc(&b->d_pos, n);
+  rc |= dalloc(&b->d_len, n);
+  rc |= dalloc(&b->d_cap, n);
+  rc |= dalloc(&b->d_gather, 6 * (size_t)n);
+  rc |= dalloc(&b->d_need, n);
+  if (rc) {
+    plum_batch_destroy(b);
+    return PLUM_ERR_CUDA;
+  }
+  cudaMallocHost(&b->h_gather, sizeof(long long) * 6 * n);
+  cudaMemcpy(b->d_rp, hp.data(), sizeof(DevParams) * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_rb, hb.data(), sizeof(DevBuffers) * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_states, hst.data(), sizeof(uint32_t*) * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_outs, hout.data(), sizeof(uint32_t*) * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_sts, hsts.data(), sizeof(DevState*) * n, cudaMemcpyHostToDevice);
+  cudaMemcpy(b->d_cap, b->cap.data(), sizeof(long long) * n, cudaMemcpyHostToDevice);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) {
+    plum_batch_destroy(b);
+    return fail(PLUM_ERR_CUDA, cudaGetErrorString(e));
+  }
+  rc = plum_batch_seed(b, 1u);
+  if (rc) {
+    plum_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return PLUM_OK;
+}
+
+int plum_batch_seed(plum_batch* b, uint32_t seed) {
+  if (!b) return fail(PLUM_ERR_INPUT, "null batch");
+  std::vector<uint32_t> seeds(b->reps.size());
+  for (size_t r = 0; r < seeds.size(); r++) seeds[r] = seed + (uint32_t)r;
+  return plum_batch_seed_each(b, seeds.data());
+}
+
+int plum_batch_seed_each(plum_batch* b, const uint32_t* seeds) {
+  if (!b || !seeds) return fail(PLUM_ERR_INPUT, "null argument");
+  for (size_t r = 0; r < b->reps.size(); r++) {
+    int rc = plum_seed(b->reps[r], seeds[r]);
+    if (rc) return rc;
+    // empty stream: the next run refills it
+    DevState st;
+    rc = read_state(b->reps[r], &st);
+    if (rc) return rc;
+    st.stream_pos = 0;
+    st.stream_len = 0;
+    st.pending = 0;
+    st.error = 0;
+    CK(cudaMemcpy(b->reps[r]->B.state, &st, sizeof(DevState), cudaMemcpyHostToDevice));
+  }
+  return PLUM_OK;
+}
+
+int plum_batch_run(plum_batch* b, int n_steps, long* accepted_out) {
+  if (!b || n_steps < 0) return fail(PLUM_ERR_INPUT, "bad argument");
+  cudaSetDevice(b->device);
+  const int R = (int)b->reps.size();
+  std::vector<int> need(R);
+  std::vector<long long> pos(R), len(R);
+  long long acc0 = 0, acc1 = 0;
+  b->last_kernels = 0;
+  CK(cudaEventRecord(b->ev0, b->s));
+  int done = 0;
+  bool first = true;
+  while (done < n_steps) {
+    const int steps = std::min(b->batch_steps, n_steps - done);
+    launch_gather_states(b->d_sts, R, b->d_gather, b->s);
+    CK(cudaMemcpyAsync(b->h_gather, b->d_gather, sizeof(long long) * 6 * R,
+                       cudaMemcpyDeviceToHost, b->s));
+    CK(cudaStreamSynchronize(b->s));
+    bool any = false;
+    for (int r = 0; r < R; r++) {
+      const long long* g = b->h_gather + 6 * r;
+      if (g[2]) return fail((int)g[2], "replica " + std::to_string(r) + " reported an error");
+      if (first) acc0 += g[3];
+      pos[r] = g[0];
+      len[r] = g[1];
+      need[r] = len[r] - pos[r] < (long long)steps * b->per_step[r];
+      any |= need[r] != 0;
+    }
+    first = false;
+    if (any) {
+      CK(cudaMemcpyAsync(b->d_need, need.data(), sizeof(int) * R, cudaMemcpyHostToDevice, b->s));
+      CK(cudaMemcpyAsync(b->d_pos, pos.data(), sizeof(long long) * R, cudaMemcpyHostToDevice, b->s));
+      CK(cudaMemcpyAsync(b->d_len, len.data(), sizeof(long long) * R, cudaMemcpyHostToDevice, b->s));
+      launch_mt_fill_batch(b->d_states, b->d_outs, b->d_pos, b->d_len, b->d_cap, b->d_need,
+                           b->d_sts, R, b->s);
+      b->last_kernels++;
+    }
+    int rc = batch_steps_graph(b, steps);
+    if (rc) return rc;
+    b->last_kernels += 1 + 2L * steps;
+    done += steps;
+  }
+  CK(cudaEventRecord(b->ev1, b->s));
+  launch_gather_states(b->d_sts, R, b->d_gather, b->s);
+  CK(cudaMemcpyAsync(b->h_gather, b->d_gather, sizeof(long long) * 6 * R, cudaMemcpyDeviceToHost,
+                     b->s));
+  CK(cudaStreamSynchronize(b->s));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+  b->last_ms = ms;
+  for (int r = 0; r < R; r++) {
+    const long long* g = b->h_gather + 6 * r;
+    if (g[2] == PLUM_ERR_STREAM_DEV) return fail(PLUM_ERR_STREAM, "replica stream ran out");
+    if (g[2]) return fail((int)g[2], "replica " + std::to_string(r) + " reported an error");
+    acc1 += g[3];
+    b->reps[r]->h_pos_valid = false;
+  }
+  if (accepted_out) *accepted_out = (long)(acc1 - acc0);
+  return PLUM_OK;
+}
+
+int plum_batch_size(const plum_batch* b) { return b ? (int)b->reps.size() : 0; }
+
+int plum_batch_replica(plum_batch* b, int r, plum_ctx** ctx) {
+  if (!b || !ctx || r < 0 || r >= (int)b->reps.size()) return fail(PLUM_ERR_INPUT, "bad replica");
+  *ctx = b->reps[r];
+  return PLUM_OK;
+}
+
+int plum_batch_last_timing(const plum_batch* b, double* ms, long* kernels) {
+  if (!b) return fail(PLUM_ERR_INPUT, "null batch");
+  if (ms) *ms = b->last_ms;
+  if (kernels) *kernels = b->last_kernels;
+  return PLUM_OK;
+}
+
+}  // extern "C"

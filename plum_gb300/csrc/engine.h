@@ -104,7 +104,7 @@ struct DevState {
   int sk_pending, sk_buf, cur_buf;
 };
 
-struct DevBuffers {
+struct DevBuffers {  // all pointers: copied word-wise into shared memory by the batch kernels
   double4_32a* pos;
   double4_32a* trial;
   int* type;
@@ -160,7 +160,24 @@ void launch_delta_pairs32(const DevParams& P, const DevBuffers& B, cudaStream_t 
 void launch_fix_all(const DevParams& P, const DevBuffers& B, cudaStream_t s);
 void launch_fix_trial(const DevParams& P, const DevBuffers& B, cudaStream_t s);
 
+// batched replicas (kern_fp32.cu / kern_moves.cu)
+constexpr int kMaxReplicas = 2048;
+void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, int* item_off,
+                          double* slots, size_t smem, cudaStream_t s);
+void launch_batch_serial(const DevParams* rp, const DevBuffers* rb, const int* item_off,
+                         const double* slots, int n_rep, int mode, cudaStream_t s);
+// per replica r: if need[r], shift the unread words [pos[r], len[r]) of out[r]
+// to the front and fill the rest up to cap[r] from state[r] (625 words)
+void launch_mt_fill_batch(uint32_t* const* states, uint32_t* const* outs, const long long* pos,
+                          const long long* len, const long long* cap, const int* need,
+                          DevState* const* sts, int n_rep, cudaStream_t s);
+void launch_gather_states(DevState* const* sts, int n_rep, long long* out, cudaStream_t s);
+
 // mt19937 on the device: state[625] (624 words + index), fills out[n].
 void launch_mt_fill(uint32_t* state, uint32_t* out, long long n, cudaStream_t s);
 
 }  // namespace plum
+
+static_assert(sizeof(plum::DevParams) % sizeof(int) == 0, "DevParams is copied as ints");
+static_assert(sizeof(plum::DevBuffers) % sizeof(long long) == 0, "DevBuffers is copied as 8-byte words");
+static_assert(sizeof(plum::DevState) % sizeof(int) == 0, "DevState is copied as ints");

@@ -317,6 +317,174 @@ void launch_delta_pairs32(const DevParams& P, const DevBuffers& B, cudaStream_t 
   k_delta32<<<pair_grid32(), kPairThreads, smem, s>>>(P, B);
 }
 
+// ------------------------------------------------------------ replicas
+// Batched replicas: every replica's pending move contributes pair items
+// (kItemPairs (moved, other) pairs each) and k items (one k tile of kKTile32
+// vectors over all moved beads). Every block derives the same item list from
+// the replicas' states, takes a contiguous share of it, and writes one slot
+// per item: pair items {lj, real}, k items {k-space energy change}. The serial
+// step of each replica adds its slots in item order.
+constexpr int kItemPairs = 4096;
+
+__global__ void __launch_bounds__(kPairThreads)
+    k_batch_delta32(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb,
+                    int n_rep, int* __restrict__ item_off, double* __restrict__ slots) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ float red[kPairThreads / 32];
+  __shared__ int s_pref[kMaxReplicas + 1];
+  __shared__ int s_np[kMaxReplicas];
+  __shared__ DevParams P;
+  __shared__ DevBuffers B;
+  __shared__ int s_bl[4];  // b_lo, b_hi, sk pending | sk_buf<<1 | cur_buf<<2, m
+  __shared__ int s_total;
+  // 1. item counts per replica and their prefix (same in every block)
+  for (int r = threadIdx.x; r < n_rep; r += blockDim.x) {
+    const DevState* st = rb[r].state;
+    const int m = st->pending ? st->b_hi - st->b_lo : 0;
+    const DevParams& pr = rp[r];
+    const long long pairs = (long long)m * pr.n_bead;
+    const int np = (pr.use_pair || pr.use_ewald) ? (int)((pairs + kItemPairs - 1) / kItemPairs) : 0;
+    const int nk = (pr.use_ewald && m > 0) ? (pr.n_k + kKTile32 - 1) / kKTile32 : 0;
+    s_np[r] = np;
+    s_pref[r + 1] = np + nk;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_pref[0] = 0;
+    for (int r = 0; r < n_rep; r++) s_pref[r + 1] += s_pref[r];
+    s_total = s_pref[n_rep];
+  }
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int r = threadIdx.x; r < n_rep; r += blockDim.x) {
+      item_off[4 * r] = s_pref[r];
+      item_off[4 * r + 1] = s_np[r];
+      item_off[4 * r + 2] = s_pref[r] + s_np[r];
+      item_off[4 * r + 3] = s_pref[r + 1] - s_pref[r] - s_np[r];
+    }
+  const int T = s_total;
+  const int it0 = (int)((long long)T * blockIdx.x / gridDim.x);
+  const int it1 = (int)((long long)T * (blockIdx.x + 1) / gridDim.x);
+  int cur = -1;
+  for (int item = it0; item < it1; item++) {
+    // replica of this item (s_pref is ascending)
+    int lo = 0, hi = n_rep - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (s_pref[mid] <= item) lo = mid; else hi = mid - 1;
+    }
+    const int r = lo;
+    if (r != cur) {
+      __syncthreads();
+      const int* src = reinterpret_cast<const int*>(rp + r);
+      int* dst = reinterpret_cast<int*>(&P);
+      for (int i = threadIdx.x; i < (int)(sizeof(DevParams) / sizeof(int)); i += blockDim.x)
+        dst[i] = src[i];
+      const long long* bs = reinterpret_cast<const long long*>(rb + r);
+      long long* bd = reinterpret_cast<long long*>(&B);
+      for (int i = threadIdx.x; i < (int)(sizeof(DevBuffers) / sizeof(long long)); i += blockDim.x)
+        bd[i] = bs[i];
+      if (threadIdx.x == 0) {
+        const DevState* st = rb[r].state;
+        s_bl[0] = st->b_lo;
+        s_bl[1] = st->b_hi;
+        s_bl[2] = st->sk_pending | (st->sk_buf << 1) | (st->cur_buf << 2);
+      }
+      __syncthreads();
+      cur = r;
+    }
+    const int b_lo = s_bl[0], b_hi = s_bl[1], m = b_hi - b_lo, N = P.n_bead;
+    const int local = item - s_pref[r];
+    if (local < s_np[r]) {
+      float acc_lj = 0.0f, acc_re = 0.0f;
+      const long long p0 = (long long)local * kItemPairs;
+      const long long p1 = min((long long)m * N, p0 + kItemPairs);
+      long long p = p0 + threadIdx.x;
+      int ii = (int)(p / N), j = (int)(p % N);
+      const int gq = kPairThreads / N, gr = kPairThreads % N;
+      for (; p < p1; p += kPairThreads, ii += gq, j += gr) {
+        if (j >= N) {
+          j -= N;
+          ii++;
+        }
+        const int i = b_lo + ii;
+        const bool jm = j >= b_lo && j < b_hi;
+        if (jm && j <= i) continue;
+        const int4 ti = B.ftrial[ii], ci = B.fpos[i];
+        const float qi = B.fq[i], qj = B.fq[j];
+        const int4 cj = B.fpos[j];
+        const int4 tj = jm ? B.ftrial[j - b_lo] : cj;
+        float l1 = 0, r1 = 0, l0 = 0, r0 = 0;
+        pair32(P, ti, qi, tj, qj, l1, r1);
+        pair32(P, ci, qi, cj, qj, l0, r0);
+        acc_lj += l1 - l0;
+        acc_re += r1 - r0;
+      }
+      float a = block_sum32<kPairThreads>(acc_lj, red);
+      float b = block_sum32<kPairThreads>(acc_re, red);
+      if (threadIdx.x == 0) {
+        slots[2 * item] = (double)a;
+        slots[2 * item + 1] = (double)b;
+      }
+    } else {
+      const int tile = local - s_np[r];
+      const int flags = s_bl[2];
+      const int sk_pend = flags & 1, sk_buf = (flags >> 1) & 1, cur_buf = (flags >> 2) & 1;
+      const int k = tile * kKTile32 + threadIdx.x;
+      const bool mine = threadIdx.x < kKTile32 && k < P.n_k;
+      const short4 kv = mine ? B.kn[k] : make_short4(0, 0, 0, 0);
+      float2* tabs = reinterpret_cast<float2*>(smem);
+      const int per = P.kper, chunk = P.kchunk_delta;
+      float2 ds = make_float2(0.0f, 0.0f);
+      for (int c0 = b_lo; c0 < b_hi; c0 += chunk) {
+        const int cnt = min(chunk, b_hi - c0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < cnt * 6; t += blockDim.x) {
+          int bead = t / 6, which = (t / 3) & 1, axis = t % 3;
+          int4 f = which ? B.fpos[c0 + bead] : B.ftrial[c0 - b_lo + bead];
+          table32(P, f, B.fq[c0 + bead], axis, tabs + (bead * 2 + which) * per);
+        }
+        __syncthreads();
+        if (mine)
+          for (int bb = 0; bb < cnt; bb++) {
+            float2 e1 = phase32(P, tabs + (bb * 2 + 0) * per, kv);
+            float2 e0 = phase32(P, tabs + (bb * 2 + 1) * per, kv);
+            ds.x += e1.x - e0.x;
+            ds.y += e1.y - e0.y;
+          }
+      }
+      float e = 0.0f;
+      if (mine) {
+        double2 sv = B.sk[k];
+        if (sk_pend) {
+          const double2 pd = B.dsk[(size_t)sk_buf * P.n_k + k];
+          sv = make_double2(sv.x + pd.x, sv.y + pd.y);
+          B.sk[k] = sv;
+        }
+        B.dsk[(size_t)cur_buf * P.n_k + k] = make_double2((double)ds.x, (double)ds.y);
+        const float sx = (float)sv.x, sy = (float)sv.y;
+        e = (float)B.kw[k] * (2.0f * (sx * ds.x + sy * ds.y) + (ds.x * ds.x + ds.y * ds.y));
+      }
+      e = block_sum32<kPairThreads>(e, red);
+      if (threadIdx.x == 0) {
+        slots[2 * item] = (double)e;
+        slots[2 * item + 1] = 0.0;
+      }
+    }
+  }
+}
+
+void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, int* item_off,
+                          double* slots, size_t smem, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_batch_delta32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kKTableBytes + 4096);
+    attr = true;
+  }
+  k_batch_delta32<<<pair_grid32(), kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots);
+}
+
 __global__ void k_fix_all(const DevParams P, const DevBuffers B) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n_bead; i += gridDim.x * blockDim.x) {
     double4_32a p = B.pos[i];

@@ -418,18 +418,39 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
   }
 }
 
-__global__ void __launch_bounds__(kSerialThreads)
-    k_serial64(const DevParams P, const DevBuffers B, int mode) {
-  __shared__ uint32_t win[kDrawWindow];
-  __shared__ unsigned accbits[kDrawWindow / 32];  // randSphere acceptance per position
-  __shared__ double red[kSerialThreads / 32];
-  __shared__ GenPlan plan;
-  __shared__ int s_accept, s_ext_bad;
-  __shared__ int s_off[kPivotMax], s_boff[kPivotMax];  // draw offsets per bead
-  __shared__ double s_w[3][kPivotMax];                 // pivot bond steps
-  // The state lives in shared memory for the kernel's duration: thread 0's
-  // chain of decisions then never waits on global memory for it.
-  __shared__ DevState S;
+// Shared memory of one serial step.
+struct SerialSmem {
+  uint32_t win[kDrawWindow];
+  unsigned accbits[kDrawWindow / 32];  // randSphere acceptance per position
+  double red[kSerialThreads / 32];
+  GenPlan plan;
+  int s_accept, s_ext_bad;
+  int s_off[kPivotMax], s_boff[kPivotMax];  // draw offsets per bead
+  double s_w[3][kPivotMax];                 // pivot bond steps
+  // The state lives in shared memory for the step: thread 0's chain of
+  // decisions then never waits on global memory for it.
+  DevState S;
+};
+
+// Batched replicas: the pending move's sums are per-item slots of the batch
+// delta kernel, added here in item order.
+struct SlotSums {
+  const double* slots;  // [items][2]
+  int pair_off, n_pair, k_off, n_k;
+};
+
+__device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers& B, int mode,
+                                            SerialSmem& sm, const SlotSums* slots) {
+  uint32_t* const win = sm.win;
+  unsigned* const accbits = sm.accbits;
+  double* const red = sm.red;
+  GenPlan& plan = sm.plan;
+  int& s_accept = sm.s_accept;
+  int& s_ext_bad = sm.s_ext_bad;
+  int* const s_off = sm.s_off;
+  int* const s_boff = sm.s_boff;
+  double(*const s_w)[kPivotMax] = sm.s_w;
+  DevState& S = sm.S;
   {
     const int nw = (int)(sizeof(DevState) / sizeof(int));
     const int* src = reinterpret_cast<const int*>(B.state);
@@ -438,6 +459,24 @@ __global__ void __launch_bounds__(kSerialThreads)
   }
   __syncthreads();
   if (S.error) return;
+  if (slots && (mode & kModeFinish) && S.pending) {
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int i = threadIdx.x; i < slots->n_pair; i += blockDim.x) {
+      a += slots->slots[2 * (slots->pair_off + i)];
+      b += slots->slots[2 * (slots->pair_off + i) + 1];
+    }
+    for (int i = threadIdx.x; i < slots->n_k; i += blockDim.x)
+      c += slots->slots[2 * (slots->k_off + i)];
+    a = bsum<kSerialThreads>(a, red);
+    b = bsum<kSerialThreads>(b, red);
+    c = bsum<kSerialThreads>(c, red);
+    if (threadIdx.x == 0) {
+      S.red_lj = a;
+      S.red_re = b;
+      S.red_k = c;
+    }
+    __syncthreads();
+  }
 
   // Stage the next stream words.
   const long long wbase = S.stream_pos;
@@ -604,6 +643,42 @@ __global__ void __launch_bounds__(kSerialThreads)
   }
 }
 
+__global__ void __launch_bounds__(kSerialThreads)
+    k_serial64(const DevParams P, const DevBuffers B, int mode) {
+  __shared__ SerialSmem sm;
+  serial_body(P, B, mode, sm, nullptr);
+}
+
+// One block per replica: the replica's parameters and buffers are staged in
+// shared memory, then the same serial step runs on them.
+__global__ void __launch_bounds__(kSerialThreads)
+    k_batch_serial(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb,
+                   const int* __restrict__ item_off, const double* __restrict__ slots, int mode) {
+  __shared__ SerialSmem sm;
+  __shared__ DevParams P;
+  __shared__ DevBuffers B;
+  const int r = blockIdx.x;
+  {
+    const int* src = reinterpret_cast<const int*>(rp + r);
+    int* dst = reinterpret_cast<int*>(&P);
+    for (int i = threadIdx.x; i < (int)(sizeof(DevParams) / sizeof(int)); i += blockDim.x)
+      dst[i] = src[i];
+    const long long* bs = reinterpret_cast<const long long*>(rb + r);
+    long long* bd = reinterpret_cast<long long*>(&B);
+    for (int i = threadIdx.x; i < (int)(sizeof(DevBuffers) / sizeof(long long)); i += blockDim.x)
+      bd[i] = bs[i];
+  }
+  __syncthreads();
+  SlotSums ss{slots, item_off[4 * r], item_off[4 * r + 1], item_off[4 * r + 2],
+              item_off[4 * r + 3]};
+  serial_body(P, B, mode, sm, &ss);
+}
+
+void launch_batch_serial(const DevParams* rp, const DevBuffers* rb, const int* item_off,
+                         const double* slots, int n_rep, int mode, cudaStream_t s) {
+  k_batch_serial<<<n_rep, kSerialThreads, 0, s>>>(rp, rb, item_off, slots, mode);
+}
+
 void launch_serial64(const DevParams& P, const DevBuffers& B, int mode, cudaStream_t s) {
   k_serial64<<<1, kSerialThreads, 0, s>>>(P, B, mode);
 }
@@ -632,8 +707,7 @@ __device__ __forceinline__ uint32_t mt_twist(uint32_t a, uint32_t b, uint32_t c)
   return v;
 }
 
-__global__ void __launch_bounds__(1024) k_mt_fill(uint32_t* state, uint32_t* out,
-                                                  long long n) {
+__device__ __forceinline__ void mt_fill_body(uint32_t* state, uint32_t* out, long long n) {
   __shared__ uint32_t mt[624], old[624];
   for (int i = threadIdx.x; i < 624; i += blockDim.x) mt[i] = state[i];
   __shared__ int idx;
@@ -676,6 +750,59 @@ __global__ void __launch_bounds__(1024) k_mt_fill(uint32_t* state, uint32_t* out
   }
   for (int i = threadIdx.x; i < 624; i += blockDim.x) state[i] = mt[i];
   if (threadIdx.x == 0) state[624] = (uint32_t)idx;
+}
+
+__global__ void __launch_bounds__(1024) k_mt_fill(uint32_t* state, uint32_t* out,
+                                                  long long n) {
+  mt_fill_body(state, out, n);
+}
+
+__global__ void __launch_bounds__(1024)
+    k_mt_fill_batch(uint32_t* const* states, uint32_t* const* outs, const long long* pos,
+                    const long long* len, const long long* cap, const int* need,
+                    DevState* const* sts) {
+  const int r = blockIdx.x;
+  if (!need[r]) return;
+  uint32_t* out = outs[r];
+  const long long p = pos[r], l = len[r];
+  const long long tail = l > p ? l - p : 0;
+  // move the unread words to the front (forward copy; source is ahead)
+  for (long long i0 = 0; i0 < tail; i0 += blockDim.x) {
+    long long i = i0 + threadIdx.x;
+    uint32_t v = i < tail ? out[p + i] : 0u;
+    __syncthreads();
+    if (i < tail) out[i] = v;
+    __syncthreads();
+  }
+  mt_fill_body(states[r], out + tail, cap[r] - tail);
+  if (threadIdx.x == 0) {
+    sts[r]->stream_pos = 0;
+    sts[r]->stream_len = cap[r];
+  }
+}
+
+// Compact copy of every replica's stream cursor, counters and error flag:
+// out[r] = {stream_pos, stream_len, error, n_accept, n_nonfinite, 0}.
+__global__ void k_gather_states(DevState* const* sts, int n_rep, long long* out) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rep; r += gridDim.x * blockDim.x) {
+    const DevState* st = sts[r];
+    out[6 * r] = st->stream_pos;
+    out[6 * r + 1] = st->stream_len;
+    out[6 * r + 2] = st->error;
+    out[6 * r + 3] = st->n_accept;
+    out[6 * r + 4] = st->n_nonfinite;
+    out[6 * r + 5] = 0;
+  }
+}
+
+void launch_gather_states(DevState* const* sts, int n_rep, long long* out, cudaStream_t s) {
+  k_gather_states<<<(n_rep + 255) / 256, 256, 0, s>>>(sts, n_rep, out);
+}
+
+void launch_mt_fill_batch(uint32_t* const* states, uint32_t* const* outs, const long long* pos,
+                          const long long* len, const long long* cap, const int* need,
+                          DevState* const* sts, int n_rep, cudaStream_t s) {
+  k_mt_fill_batch<<<n_rep, 1024, 0, s>>>(states, outs, pos, len, cap, need, sts);
 }
 
 void launch_mt_fill(uint32_t* state, uint32_t* out, long long n, cudaStream_t s) {

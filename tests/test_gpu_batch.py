@@ -1,0 +1,63 @@
+"""Replica batches (precision form): every replica of one launch must behave
+as the same system run alone -- on the reference's recorded stream each
+replica reproduces its golden trajectory until a near tie."""
+import numpy as np
+import pytest
+
+from _cases import CASES, load, rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import plum_gb300
+    plum_gb300.lib()
+    return plum_gb300
+
+
+def test_uneven_replicas_replay_their_references(pg):
+    dirs, gs = [], []
+    for c in CASES:
+        d, g = load(c)
+        dirs.append(d)
+        gs.append(g)
+    b = pg.Batch(dirs)
+    b.seed(np.array([int(g["run_seed"]) for g in gs], np.uint32))
+    n = 150
+    b.run(n)
+    for r, g in enumerate(gs):
+        rep = b.replica(r)
+        e = rep.energies().sum()
+        ref = g["run_etot"][n - 1]
+        assert rel(e, ref, max(1.0, abs(ref))) < 1e-4, (CASES[r], e, ref)
+        # the running totals stay consistent with an FP64 recompute (not for
+        # the slab cases: there the reference's running Ewald total carries
+        # the dipole term of the configuration before the last accepted move)
+        if not CASES[r].startswith("slab"):
+            fresh = rep.total_energy()[:4].sum()
+            assert rel(e, fresh, max(1.0, abs(fresh))) < 1e-4
+
+
+def test_replicas_match_single_system_runs(pg):
+    d, g = load("bulk_medium")
+    b = pg.Batch([d] * 4)
+    b.seed(np.array([11, 12, 13, 14], np.uint32))
+    b.run(300)
+    for r in range(4):
+        s = pg.System(d, form=pg.FORM_FP32)
+        s.seed(11 + r)
+        s.run(300)
+        np.testing.assert_allclose(b.replica(r).energies(), s.energies(), rtol=2e-4, atol=2e-3)
+
+
+def test_batch_runs_are_repeatable(pg):
+    d, _ = load("slab_lj")
+    a = pg.Batch([d] * 3)
+    c = pg.Batch([d] * 3)
+    a.seed(5)
+    c.seed(5)
+    a.run(200)
+    c.run(200)
+    for r in range(3):
+        np.testing.assert_array_equal(a.replica(r).positions(), c.replica(r).positions())
