@@ -146,6 +146,22 @@ int plum_set_positions(plum_ctx* ctx, const double* xyz);
  * RadiusOfGyrationXYZ and EndToEndDistance (simulation.cc:406-500). */
 int plum_observables(const plum_ctx* ctx, double* out);
 
+/* Configurational-bias trial-site energies of one growth step: for each of
+ * n_trials trial positions b1[t] of the grand-canonical species' next bead
+ * (and, for a charged species, its trial counterion b2[t]), the energy
+ * ForceField::BeadsEnergy (cbmc.cc:5-151) returns: LJ and Ewald with the
+ * system outside the molecules being deleted, with the chain_len beads grown
+ * so far (chain, and their counterions chain_ci), with each other, self and
+ * dipole terms and the walls; 1e8 on overlap. delete_mol is the molecule
+ * being deleted (cbmc.cc:340-346; its counterions follow it), -1 when
+ * inserting. Host buffers: b1, b2 [n_trials*3], chain, chain_ci
+ * [chain_len*3], u_out [n_trials]. Used by CBMCFGenTrialBeads
+ * (cbmc.cc:161-212), CBMCFChainInsertion and CBMCFChainDeletion
+ * (cbmc.cc:214-442). */
+int plum_cbmc_trials(plum_ctx* ctx, int n_trials, const double* b1, const double* b2,
+                     int chain_len, const double* chain, const double* chain_ci, int delete_mol,
+                     double* u_out);
+
 /* Full FP64 recompute cadence of plum_run, in moves (0 = never). The
  * precision form defaults to 10000: every 10^4 moves (at the next batch
  * boundary of 256) the totals, S(k) and the fixed-point mirror are rebuilt

@@ -72,6 +72,10 @@ def _load_ref():
         L.pr_rhoz.argtypes = [C.c_void_p, _dp, C.c_int]
         L.pr_rhoz.restype = C.c_int
         L.pr_rng_words.argtypes = [C.c_void_p, C.c_uint, _up]
+        L.pr_beads_energy.argtypes = [C.c_void_p, _dp, C.c_void_p, C.c_int, C.c_void_p,
+                                      C.c_void_p, C.c_int]
+        L.pr_beads_energy.restype = C.c_double
+        L.pr_gc_info.argtypes = [C.c_void_p, _dp]
         _ref_lib = L
     return _ref_lib
 
@@ -101,6 +105,9 @@ def _load_oracle():
         L.po_rhoz.restype = C.c_int
         L.po_mt19937.argtypes = [C.c_uint32, C.c_long, _up]
         L.po_set_fast_init.argtypes = [C.c_int]
+        L.po_beads_energy.argtypes = [C.c_void_p, _dp, C.c_void_p, C.c_int, C.c_void_p,
+                                      C.c_void_p, C.c_int]
+        L.po_beads_energy.restype = C.c_double
         _orc_lib = L
     return _orc_lib
 
@@ -187,6 +194,19 @@ class Ref(_Base):
         self.L.pr_rng_words(self.h, n, o)
         return o
 
+    def gc_info(self):
+        o = np.zeros(4)
+        self.L.pr_gc_info(self.h, o)
+        return o
+
+    def beads_energy(self, b1, b2, chain, chain_ci, delete_id=-1):
+        cl = 0 if chain is None else len(chain)
+        a = lambda x: None if x is None else np.ascontiguousarray(x, np.float64).ravel()
+        keep = [a(b2), a(chain), a(chain_ci)]
+        ptr = lambda x: None if x is None else x.ctypes.data_as(C.c_void_p)
+        return self.L.pr_beads_energy(self.h, a(b1), ptr(keep[0]), cl, ptr(keep[1]), ptr(keep[2]),
+                                      delete_id)
+
 
 class Oracle(_Base):
     """The FP64 CPU restatement (oracle/_ref/liboracle.so)."""
@@ -262,6 +282,14 @@ class Oracle(_Base):
         o = np.zeros(cap)
         nb = self.L.po_rhoz(self.h, o, cap)
         return o[:3 * nb].reshape(nb, 3)
+
+    def beads_energy(self, b1, b2, chain, chain_ci, delete_id=-1):
+        cl = 0 if chain is None else len(chain)
+        a = lambda x: None if x is None else np.ascontiguousarray(x, np.float64).ravel()
+        keep = [a(b2), a(chain), a(chain_ci)]
+        ptr = lambda x: None if x is None else x.ctypes.data_as(C.c_void_p)
+        return self.L.po_beads_energy(self.h, a(b1), ptr(keep[0]), cl, ptr(keep[1]),
+                                      ptr(keep[2]), delete_id)
 
 
 def mt19937(seed: int, n: int) -> np.ndarray:

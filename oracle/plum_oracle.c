@@ -130,6 +130,9 @@ struct po_ctx {
   double* bond_mol;
   /* counts (simulation.cc:1066-1094) */
   int n_chain, n_cion, n_aion, n_nion;
+  /* grand-canonical species (force_field.cc:96-103) */
+  double chem_pot, debroglie, gc_bead_charge;
+  int gc_freq, gc_chain_len, cbmc_trials, gc_type;
   mt_t g;
 };
 
@@ -544,8 +547,15 @@ po_ctx* po_create(const char* dir, const char* runin, uint32_t seed, char* err,
   c->use_dihed = rd_i(&r, "use_dihed");
   c->use_ext = rd_i(&r, "use_ext");
   c->use_gc = rd_i(&r, "use_gc");
+  char gc_sym[64] = "";
   if (c->use_gc) {
-    for (int i = 0; i < 7; i++) rd_item(&r, "gc parameter");
+    c->chem_pot = rd_d(&r, "chemical potential");
+    c->debroglie = rd_d(&r, "de Broglie prefactor");
+    c->gc_freq = rd_i(&r, "GC frequency");
+    c->gc_chain_len = rd_i(&r, "GC chain length");
+    c->gc_bead_charge = rd_d(&r, "GC bead charge");
+    snprintf(gc_sym, sizeof gc_sym, "%s", rd_item(&r, "GC bead symbol"));
+    c->cbmc_trials = rd_i(&r, "CBMC trials");
   }
   c->rigid = -1;
   if (c->use_pair) {
@@ -592,6 +602,7 @@ po_ctx* po_create(const char* dir, const char* runin, uint32_t seed, char* err,
     }
   }
   if (r.bad) goto fail;
+  c->gc_type = c->use_gc ? type_of(c, gc_sym) : -1;
   /* top file: simulation.cc:610-646 */
   p = join_path(dir, top);
   if (tok_open(&tt, p)) {
@@ -1209,4 +1220,101 @@ int po_rhoz(const po_ctx* c, double* out, int cap) {
     }
   }
   return nb;
+}
+
+/* ForceField::BeadsEnergy (cbmc.cc:5-151): energy of a trial chain bead b1
+ * (and, for a charged species, its trial counterion b2) against the system
+ * minus the molecules being deleted, the first current_len grown beads (and
+ * their counterions), each other, the walls, and in Ewald the self terms and
+ * the dipole change. LJ with the immediately preceding grown bead is left out
+ * (cbmc.cc:57-58). The reciprocal part is written with S(k) of the "other"
+ * charges: sum over the pairs + half the self pairs = (4 pi lB / V) sum_half
+ * e^{-k^2/4a}/k^2 (|S_o + q1 e1 + q2 e2|^2 - |S_o|^2). */
+double po_beads_energy(po_ctx* c, const double* b1, const double* b2, int cl,
+                       const double* chain, const double* chain_ci, int delete_id) {
+  const int charged = c->gc_bead_charge != 0;
+  const double q1 = c->gc_bead_charge, q2 = -c->gc_bead_charge;
+  const int t = c->gc_type;
+  const int L = c->gc_chain_len;
+  int d_lo = -1, d_hi = -1; /* excluded molecules [d_lo, d_hi] */
+  if (delete_id >= 0) {
+    d_lo = delete_id;
+    d_hi = delete_id + (charged ? L : 0);
+  }
+  double pair_e = 0, ew = 0;
+  for (int m = 0; m < c->n_mol; m++) {
+    if (m >= d_lo && m <= d_hi) continue;
+    for (int j = c->mol_start[m]; j < c->mol_start[m + 1]; j++) {
+      const double* pj = c->x + 3 * j;
+      if (c->use_pair) {
+        pair_e += lj_pair(c, b1, t, pj, c->type[j]);
+        if (charged) pair_e += lj_pair(c, b2, t, pj, c->type[j]);
+      }
+      if (c->use_ewald) {
+        ew += ew_real_pair(c, b1, q1, pj, c->q[j]);
+        if (charged) ew += ew_real_pair(c, b2, q2, pj, c->q[j]);
+      }
+    }
+  }
+  for (int i = 0; i < cl; i++) {
+    const double* ci = chain + 3 * i;
+    const double* cc = charged ? chain_ci + 3 * i : NULL;
+    if (c->use_pair) {
+      if (i < cl - 1) pair_e += lj_pair(c, b1, t, ci, t);
+      if (charged) {
+        pair_e += lj_pair(c, b1, t, cc, t);
+        pair_e += lj_pair(c, b2, t, ci, t);
+        pair_e += lj_pair(c, b2, t, cc, t);
+      }
+    }
+    if (c->use_ewald) {
+      ew += ew_real_pair(c, b1, q1, ci, q1);
+      if (charged) {
+        ew += ew_real_pair(c, b1, q1, cc, q2);
+        ew += ew_real_pair(c, b2, q2, ci, q1);
+        ew += ew_real_pair(c, b2, q2, cc, q2);
+      }
+    }
+  }
+  if (c->use_pair && charged) pair_e += lj_pair(c, b1, t, b2, t);
+  if (c->use_ewald && pair_e < K_VERY_LARGE) {
+    ew += ew_self(c, q1) + 0.5 * ew_real_pair(c, b1, q1, b1, q1);
+    if (charged) {
+      ew += ew_self(c, q2) + ew_real_pair(c, b1, q1, b2, q2) + 0.5 * ew_real_pair(c, b2, q2, b2, q2);
+    }
+    double* so = (double*)calloc((size_t)2 * (c->n_k > 0 ? c->n_k : 1), sizeof(double));
+    double* sn = (double*)calloc((size_t)2 * (c->n_k > 0 ? c->n_k : 1), sizeof(double));
+    double mz = 0;
+    for (int m = 0; m < c->n_mol; m++) {
+      if (m >= d_lo && m <= d_hi) continue;
+      for (int j = c->mol_start[m]; j < c->mol_start[m + 1]; j++) {
+        sk_add(c, c->x + 3 * j, c->q[j], 1.0, so);
+        mz += c->q[j] * c->x[3 * j + 2];
+      }
+    }
+    for (int i = 0; i < cl; i++) {
+      sk_add(c, chain + 3 * i, q1, 1.0, so);
+      mz += q1 * chain[3 * i + 2];
+      if (charged) {
+        sk_add(c, chain_ci + 3 * i, q2, 1.0, so);
+        mz += q2 * chain_ci[3 * i + 2];
+      }
+    }
+    memcpy(sn, so, sizeof(double) * 2 * (size_t)c->n_k);
+    sk_add(c, b1, q1, 1.0, sn);
+    if (charged) sk_add(c, b2, q2, 1.0, sn);
+    ew += sk_energy(c, sn) - sk_energy(c, so);
+    if (c->dipole) {
+      double mzn = mz + q1 * b1[2] + (charged ? q2 * b2[2] : 0.0);
+      ew += c->lB * 2 * K_PI / (c->evol / 1.0) * (mzn * mzn - mz * mz);
+    }
+    free(so);
+    free(sn);
+  }
+  if (c->use_ext) {
+    pair_e += wall_energy(c, b1[2], t);
+    if (charged) pair_e += wall_energy(c, b2[2], t);
+  }
+  if (pair_e >= K_VERY_LARGE) return K_VERY_LARGE;
+  return pair_e + ew;
 }

@@ -78,6 +78,11 @@ void po_set_coords(po_ctx* c, const double* xyz);
 void po_observables(const po_ctx* c, double* out);
 /* One CalcRhoZ pass into out[3*n_bin]; returns n_bin. */
 int po_rhoz(const po_ctx* c, double* out, int cap);
+/* ForceField::BeadsEnergy (cbmc.cc:5-151) for trial bead b1 and, for a
+ * charged species, trial counterion b2 (may be NULL), with cl grown beads
+ * chain[cl*3] (and counterions chain_ci); delete_id = -1 for insertion. */
+double po_beads_energy(po_ctx* c, const double* b1, const double* b2, int cl,
+                       const double* chain, const double* chain_ci, int delete_id);
 /* First n outputs of an mt19937 seeded with `seed`. */
 void po_mt19937(uint32_t seed, long n, uint32_t* out);
 

@@ -327,6 +327,42 @@ int pr_rhoz(void* hp, double* out, int cap) {
   return nb;
 }
 
+// ForceField::BeadsEnergy (cbmc.cc:5-151) for a trial chain bead at b1 and,
+// for a charged grand-canonical species, its trial counterion at b2, with the
+// first current_len grown beads (and counterions) taken from chain /
+// chain_ci (current_len x 3). delete_id = -1 for insertion. Bead symbols and
+// charges are the species' own (force_field.cc:383-401).
+double pr_beads_energy(void* hp, const double* b1, const double* b2, int current_len,
+                       const double* chain, const double* chain_ci, int delete_id) {
+  Simulation* s = ((Handle*)hp)->sim;
+  ForceField& f = s->force_field;
+  const int L = f.gc_chain_len;
+  for (int i = 0; i < current_len; i++) {
+    double p[3] = {chain[3 * i], chain[3 * i + 1], chain[3 * i + 2]};
+    f.cbmc_chain[i].SetAllCrd(p);
+    if (f.gc_bead_charge != 0) {
+      double c[3] = {chain_ci[3 * i], chain_ci[3 * i + 1], chain_ci[3 * i + 2]};
+      f.cbmc_chain[i + L].SetAllCrd(c);
+    }
+  }
+  Bead x1(f.gc_bead_symbol, -1, -1, f.gc_chain_chg[0], b1[0], b1[1], b1[2]);
+  Bead x2(f.gc_bead_symbol, -1, -1, -f.gc_chain_chg[0], 0, 0, 0);
+  if (b2) {
+    double c[3] = {b2[0], b2[1], b2[2]};
+    x2.SetAllCrd(c);
+  }
+  return f.BeadsEnergy(x1, x2, s->mols, current_len, delete_id);
+}
+
+// The grand-canonical species: {chain length, bead charge, trials, gc_freq}.
+void pr_gc_info(void* hp, double* out) {
+  ForceField& f = ((Handle*)hp)->sim->force_field;
+  out[0] = f.gc_chain_len;
+  out[1] = f.gc_bead_charge;
+  out[2] = f.cbmc_no_of_trials;
+  out[3] = f.gc_freq;
+}
+
 // The reference's generator state as 624 words + position.
 void pr_rng_words(void* hp, unsigned n, unsigned* out) {
   std::mt19937 g = ((Handle*)hp)->sim->rand_gen;

@@ -82,6 +82,8 @@ def lib():
         L.plum_batch_replica.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]
         L.plum_batch_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_double),
                                              C.POINTER(C.c_long)]
+        L.plum_cbmc_trials.argtypes = [C.c_void_p, C.c_int, _dp, C.c_void_p, C.c_int,
+                                       C.c_void_p, C.c_void_p, C.c_int, _dp]
         L.plum_sim_create.argtypes = [C.c_char_p, C.c_char_p, C.c_uint, C.c_int,
                                       C.POINTER(C.c_void_p)]
         L.plum_sim_destroy.argtypes = [C.c_void_p]
@@ -187,6 +189,19 @@ class System:
         o = np.zeros(5)
         _check(lib().plum_observables(self.h, o))
         return o
+
+    def cbmc_trials(self, b1, b2=None, chain=None, chain_ci=None, delete_mol=-1):
+        """BeadsEnergy of trial sites b1[T,3] (and trial counterions b2[T,3] for a
+        charged species) given the grown chain[cl,3] (and chain_ci[cl,3])."""
+        b1 = np.ascontiguousarray(b1, np.float64).reshape(-1, 3)
+        T = len(b1)
+        keep = [None if x is None else np.ascontiguousarray(x, np.float64).ravel()
+                for x in (b2, chain, chain_ci)]
+        cl = 0 if chain is None else len(np.asarray(chain).reshape(-1, 3))
+        u = np.zeros(T)
+        _check(lib().plum_cbmc_trials(self.h, T, b1.ravel(), _ptr(keep[0]), cl, _ptr(keep[1]),
+                                      _ptr(keep[2]), delete_mol, u))
+        return u
 
     def set_recompute(self, every: int):
         _check(lib().plum_set_recompute(self.h, every))

@@ -64,6 +64,13 @@ struct plum_ctx {
   long last_kernels = 0;
   long recompute_every = 0;    // full FP64 recompute cadence of plum_run (0: never)
   long since_recompute = 0;
+  // configurational-bias scratch
+  double4_32a* cb_b = nullptr;   // [2 * cap] trial beads and counterions
+  double4_32a* cb_c = nullptr;   // [2 * cap] grown chain and counterions
+  double2* cb_so = nullptr;
+  double* cb_part = nullptr;
+  double* cb_u = nullptr;
+  int cb_cap = 0;
   double drift[4] = {0, 0, 0, 0};  // running minus recomputed at the last reset
   double drift_max = 0.0;
   // CUDA graph of one batch of moves (kernels read the pending move from
@@ -374,6 +381,12 @@ static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out) {
   }
   c->form = form;
   c->device = device;
+  if (c->in.use_gc) {
+    // the grand-canonical species' symbol joins the type table (the
+    // reference creates its beads with that symbol, force_field.cc:383-401)
+    auto& tn = c->in.type_names;
+    if (std::find(tn.begin(), tn.end(), c->in.gc_symbol) == tn.end()) tn.push_back(c->in.gc_symbol);
+  }
   Input& in = c->in;
   // The reference's own input checks (simulation.cc:142-191, force_field.cc:205-209).
   std::string bad;
@@ -580,7 +593,8 @@ int plum_ctx_destroy(plum_ctx* c) {
                   c->B.ion_ids,  c->B.kn,      c->B.kw,    c->B.sk,        c->B.dsk,
                   c->B.partial,  c->B.bond_mol, c->B.state, c->d_tot_part,  c->d_out,
                   c->B.dsk_part, c->B.ktile_count, c->B.kpartial, c->B.fpos, c->B.done_count,
-                  c->B.fq,       c->B.ftrial,  c->B.dsk_part32,
+                  c->B.fq,       c->B.ftrial,  c->B.dsk_part32, c->cb_b, c->cb_c, c->cb_so,
+                  c->cb_part,    c->cb_u,
                   c->d_stream,   c->d_mt,      c->d_log_type, c->d_log_acc, c->d_log_e};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -936,6 +950,77 @@ int plum_type_name(const plum_ctx* c, int type, char* buf, int cap) {
   if (!c || !buf || cap <= 0) return fail(PLUM_ERR_INPUT, "bad argument");
   if (type < 0 || type >= (int)c->in.type_names.size()) return fail(PLUM_ERR_INPUT, "bad type");
   std::snprintf(buf, cap, "%s", c->in.type_names[type].c_str());
+  return PLUM_OK;
+}
+
+int plum_cbmc_trials(plum_ctx* c, int n_trials, const double* b1, const double* b2,
+                     int chain_len, const double* chain, const double* chain_ci, int delete_mol,
+                     double* u_out) {
+  if (!c || n_trials <= 0 || !b1 || !u_out || chain_len < 0) return fail(PLUM_ERR_INPUT, "bad argument");
+  const Input& in = c->in;
+  if (!in.use_gc) return fail(PLUM_ERR_INPUT, "run.in has no grand-canonical species");
+  const int charged = in.gc_bead_charge != 0;
+  if (charged && (!b2 || (chain_len > 0 && !chain_ci)))
+    return fail(PLUM_ERR_INPUT, "a charged species needs trial counterions");
+  if (chain_len > 0 && !chain) return fail(PLUM_ERR_INPUT, "missing grown chain");
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
+  cudaSetDevice(c->device);
+  const int cap = std::max(n_trials, std::max(chain_len, in.gc_chain_len));
+  const int groups = cbmc_groups(c->P);
+  if (cap > c->cb_cap) {
+    cudaFree(c->cb_b);
+    cudaFree(c->cb_c);
+    cudaFree(c->cb_part);
+    cudaFree(c->cb_u);
+    int rc = dalloc(&c->cb_b, 2 * (size_t)cap) | dalloc(&c->cb_c, 2 * (size_t)cap) |
+             dalloc(&c->cb_part, 2 * (size_t)cap * groups) | dalloc(&c->cb_u, cap);
+    if (rc) return PLUM_ERR_CUDA;
+    c->cb_cap = cap;
+  }
+  if (!c->cb_so && dalloc(&c->cb_so, std::max(1, c->P.n_k))) return PLUM_ERR_CUDA;
+  int type = (int)(std::find(in.type_names.begin(), in.type_names.end(), in.gc_symbol) -
+                   in.type_names.begin());
+  const double q1 = in.gc_bead_charge, q2 = -in.gc_bead_charge;
+  std::vector<double4_32a> hb(2 * n_trials), hc(2 * std::max(chain_len, 1));
+  for (int t = 0; t < n_trials; t++) {
+    hb[t] = make_double4_32a(b1[3 * t], b1[3 * t + 1], b1[3 * t + 2], q1);
+    hb[n_trials + t] = charged ? make_double4_32a(b2[3 * t], b2[3 * t + 1], b2[3 * t + 2], q2)
+                               : hb[t];
+  }
+  for (int i = 0; i < chain_len; i++) {
+    hc[i] = make_double4_32a(chain[3 * i], chain[3 * i + 1], chain[3 * i + 2], q1);
+    hc[chain_len + i] = charged ? make_double4_32a(chain_ci[3 * i], chain_ci[3 * i + 1],
+                                                   chain_ci[3 * i + 2], q2)
+                                : hc[i];
+  }
+  CK(cudaMemcpyAsync(c->cb_b, hb.data(), sizeof(double4_32a) * 2 * n_trials,
+                     cudaMemcpyHostToDevice, c->s));
+  if (chain_len > 0)
+    CK(cudaMemcpyAsync(c->cb_c, hc.data(), sizeof(double4_32a) * 2 * chain_len,
+                       cudaMemcpyHostToDevice, c->s));
+  CbmcJob J;
+  J.n_trials = n_trials;
+  J.charged = charged;
+  J.cl = chain_len;
+  J.type = type;
+  J.ex_lo = J.ex_hi = 0;
+  if (delete_mol >= 0) {
+    const int last = delete_mol + (charged ? in.gc_chain_len : 0);
+    if (last >= in.n_mol) return fail(PLUM_ERR_INPUT, "deleted molecule range out of bounds");
+    J.ex_lo = in.mol_start[delete_mol];
+    J.ex_hi = in.mol_start[last + 1];
+  }
+  J.b1 = c->cb_b;
+  J.b2 = c->cb_b + n_trials;
+  J.chain = c->cb_c;
+  J.chain_ci = c->cb_c + chain_len;
+  J.s_o = c->cb_so;
+  J.part = c->cb_part;
+  J.u = c->cb_u;
+  launch_cbmc(c->P, c->B, J, c->s);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(u_out, c->cb_u, sizeof(double) * n_trials, cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
   return PLUM_OK;
 }
 

@@ -160,6 +160,21 @@ void launch_delta_pairs32(const DevParams& P, const DevBuffers& B, cudaStream_t 
 void launch_fix_all(const DevParams& P, const DevBuffers& B, cudaStream_t s);
 void launch_fix_trial(const DevParams& P, const DevBuffers& B, cudaStream_t s);
 
+// configurational-bias trial sites (kern_cbmc.cu)
+struct CbmcJob {
+  int n_trials, charged, cl, type;  // trials, counterion present, grown beads, species type
+  int ex_lo, ex_hi;                 // system beads of the molecules being deleted
+  const double4_32a* b1;            // [n_trials] trial beads (x, y, z, q)
+  const double4_32a* b2;            // [n_trials] trial counterions
+  const double4_32a* chain;         // [cl] grown beads
+  const double4_32a* chain_ci;      // [cl] their counterions
+  double2* s_o;                     // [n_k] scratch: S(k) of the other charges
+  double* part;                     // [n_trials][groups][2] scratch
+  double* u;                        // [n_trials] result
+};
+int cbmc_groups(const DevParams& P);
+void launch_cbmc(const DevParams& P, const DevBuffers& B, const CbmcJob& J, cudaStream_t s);
+
 // batched replicas (kern_fp32.cu / kern_moves.cu)
 constexpr int kMaxReplicas = 2048;
 void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, int* item_off,

@@ -399,3 +399,99 @@ def write_brush(dirpath: str, spec: BrushSpec, seed: int, runin="run.in", **over
     with open(os.path.join(dirpath, runin), "w") as f:
         f.write(runin_text(**kw))
     return os.path.join(dirpath, runin)
+
+
+@dataclasses.dataclass
+class MuVTSpec:
+    """Grand-canonical bulk box: chains of the exchanged species (each
+    followed by its counterions when charged) plus fixed +-1 salt pairs."""
+    box: float = 50.0
+    n_chain: int = 40
+    chain_len: int = 30
+    bead_charge: float = 0.0     # charge of each chain bead (0: neutral species)
+    n_salt: int = 2000           # +1/-1 pairs
+    lj_cutoff: float = 2.5
+    lB: float = 3.0
+    alpha_times_L: float = 5.0
+    k_bond: float = 400.0
+    r0: float = 1.0
+    chem_pot: float = 0.0
+    trials: int = 32
+    gc_freq: int = 2             # the reference draws insert/delete when rand % gc_freq == 0
+    move_prob: tuple = (0.5, 0.1, 0.2, 0.0, 0.2)
+    min_sep: float = 0.8
+
+
+def muvt_coordinates(spec: MuVTSpec, seed: int):
+    rng = np.random.default_rng(seed)
+    L = spec.box
+    box = np.array([L, L, L])
+    grid = _Grid(box, max(spec.min_sep, 1.0))
+    per = (True, True, True)
+    mol, sym, xyz, q = [], [], [], []
+    m = 0
+
+    def place():
+        for t in range(100000):
+            p = rng.uniform(0, L, size=3)
+            if grid.ok(p, spec.min_sep, per):
+                grid.add(p)
+                return p
+        raise RuntimeError("could not place a bead")
+
+    for c in range(spec.n_chain):
+        for attempt in range(1000):
+            p = rng.uniform(0, L, size=3)
+            if not grid.ok(p, spec.min_sep, per):
+                continue
+            beads = [p]
+            local = _Grid(box, max(spec.min_sep, 1.0))
+            local.add(p)
+            ok = True
+            for b in range(1, spec.chain_len):
+                for t in range(200):
+                    cand = beads[-1] + spec.r0 * _unit(rng)
+                    if grid.ok(cand, spec.min_sep, per) and local.ok(cand, spec.min_sep, per):
+                        break
+                else:
+                    ok = False
+                    break
+                beads.append(cand)
+                local.add(cand)
+            if ok:
+                break
+        else:
+            raise RuntimeError("could not grow chain %d" % c)
+        for p in beads:
+            grid.add(p)
+            mol.append(m), sym.append("P"), xyz.append(p), q.append(spec.bead_charge)
+        m += 1
+        if spec.bead_charge != 0:
+            for b in range(spec.chain_len):
+                mol.append(m), sym.append("P"), xyz.append(place()), q.append(-spec.bead_charge)
+                m += 1
+    for i in range(spec.n_salt):
+        mol.append(m), sym.append("C"), xyz.append(place()), q.append(1.0)
+        m += 1
+        mol.append(m), sym.append("A"), xyz.append(place()), q.append(-1.0)
+        m += 1
+    return np.array(mol), sym, np.array(xyz), np.array(q, dtype=np.float64)
+
+
+def write_muvt(dirpath: str, spec: MuVTSpec, seed: int, runin="run.in", **over) -> str:
+    os.makedirs(dirpath, exist_ok=True)
+    mol, sym, xyz, q = muvt_coordinates(spec, seed)
+    write_crd(os.path.join(dirpath, "input_crd.dat"), mol, sym, xyz, q)
+    write_top(os.path.join(dirpath, "input_top.dat"), len(mol), int(mol.max()) + 1,
+              (spec.box,) * 3)
+    gc = {"chem_pot": spec.chem_pot, "deBroglie": 1, "gc_freq": spec.gc_freq,
+          "chain_len": spec.chain_len, "bead_charge": int(spec.bead_charge),
+          "bead_symbol": "P", "cbmc_trials": spec.trials}
+    kw = dict(move_prob=spec.move_prob, lj_cutoff=spec.lj_cutoff,
+              lj_table=(("P", 1.0, 1.0), ("C", 1.0, 1.0), ("A", 1.0, 1.0)), lB=spec.lB,
+              alpha=(spec.alpha_times_L / spec.box) ** 2, k_bond=spec.k_bond, r0=spec.r0,
+              rigid=spec.r0, use_gc=True, gc=gc)
+    kw.update(over)
+    with open(os.path.join(dirpath, runin), "w") as f:
+        f.write(runin_text(**kw))
+    return os.path.join(dirpath, runin)

@@ -52,6 +52,71 @@ CASES = {
 }
 
 
+CBMC_CASES = {
+    "muvt_neutral": dict(seed=21, spec=systems.MuVTSpec(box=14.0, n_chain=4, chain_len=10,
+                                                         n_salt=30, trials=8)),
+    "muvt_charged": dict(seed=22, spec=systems.MuVTSpec(box=14.0, n_chain=3, chain_len=6,
+                                                         bead_charge=-1.0, n_salt=12, trials=8)),
+}
+
+
+def make_cbmc_case(name, cfg, n_eval=24):
+    """BeadsEnergy (cbmc.cc:5-151) of seeded trial sites: inserting (growing
+    a chain from a random first bead) and deleting (regrowing an existing
+    chain), from the reference itself."""
+    d = os.path.join(HERE, name)
+    if os.path.isdir(d):
+        shutil.rmtree(d)
+    os.makedirs(d)
+    spec = cfg["spec"]
+    systems.write_muvt(d, spec, seed=cfg["seed"])
+    R = ob.Ref(d, seed=1)
+    L, qb, trials, _ = R.gc_info()
+    L = int(L)
+    charged = qb != 0
+    rng = np.random.default_rng(cfg["seed"] + 7)
+    sizes = np.array([R.mol_size(m) for m in range(R.n_mol)])
+    start = np.concatenate([[0], np.cumsum(sizes)])
+    coords = R.coords()
+    chain_mols = [m for m in range(R.n_mol) if sizes[m] > 1]
+    rows = []
+    for k in range(n_eval):
+        if k % 2 == 0:
+            delete_id = -1
+            cl = int(rng.integers(0, L))
+            first = rng.uniform(0, spec.box, size=3)
+            steps = rng.normal(size=(max(cl, 1), 3))
+            steps /= np.linalg.norm(steps, axis=1)[:, None]
+            chain = first + np.cumsum(np.vstack([[0, 0, 0], steps[:max(cl - 1, 0)]]), axis=0)[:cl]
+            chain_ci = rng.uniform(0, spec.box, size=(cl, 3))
+        else:
+            delete_id = int(chain_mols[rng.integers(len(chain_mols))])
+            cl = int(rng.integers(0, L))
+            chain = coords[start[delete_id]:start[delete_id] + cl]
+            chain_ci = np.array([coords[start[delete_id + 1 + i]] for i in range(cl)]) \
+                if charged else np.zeros((cl, 3))
+        base = chain[-1] if cl > 0 else rng.uniform(0, spec.box, size=3)
+        v = rng.normal(size=3)
+        b1 = base + 1.0 * v / np.linalg.norm(v)
+        b2 = rng.uniform(0, spec.box, size=3)
+        u = R.beads_energy(b1, b2 if charged else None, chain if cl else None,
+                           chain_ci if (charged and cl) else None, delete_id)
+        rows.append((delete_id, cl, b1, b2, chain, chain_ci, u))
+    R.close()
+    for f in os.listdir(d):
+        if f not in ("run.in", "input_crd.dat", "input_top.dat"):
+            os.remove(os.path.join(d, f))
+    out = {"delete_id": np.array([r[0] for r in rows], np.int32),
+           "cl": np.array([r[1] for r in rows], np.int32),
+           "b1": np.array([r[2] for r in rows]), "b2": np.array([r[3] for r in rows]),
+           "chain": np.concatenate([np.asarray(r[4]).reshape(-1, 3) for r in rows]),
+           "chain_ci": np.concatenate([np.asarray(r[5]).reshape(-1, 3) for r in rows]),
+           "u": np.array([r[6] for r in rows]), "charged": np.array(int(charged)),
+           "gc_len": np.array(L)}
+    np.savez_compressed(os.path.join(d, "cbmc.npz"), **out)
+    print(name, "beads", int(start[-1]), "u range", out["u"].min(), out["u"].max())
+
+
 def make_case(name, cfg, n_de=24):
     d = os.path.join(HERE, name)
     if os.path.isdir(d):
@@ -111,5 +176,10 @@ def make_case(name, cfg, n_de=24):
 
 if __name__ == "__main__":
     ob.build()
-    for name, cfg in CASES.items():
-        make_case(name, cfg)
+    which = sys.argv[1:] or ["moves", "cbmc"]
+    if "moves" in which:
+        for name, cfg in CASES.items():
+            make_case(name, cfg)
+    if "cbmc" in which:
+        for name, cfg in CBMC_CASES.items():
+            make_cbmc_case(name, cfg)
