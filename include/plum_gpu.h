@@ -162,6 +162,34 @@ int plum_cbmc_trials(plum_ctx* ctx, int n_trials, const double* b1, const double
                      int chain_len, const double* chain, const double* chain_ci, int delete_mol,
                      double* u_out);
 
+/* plum_cbmc_trials for callers that cannot allocate device memory: a host
+ * application whose device memory is owned by its own allocator or budget,
+ * or a grand-canonical driver that must not stall, since cudaMalloc and
+ * cudaFree (which plum_cbmc_trials uses when a larger request grows its
+ * buffers) synchronise the whole device. No counterpart in the reference.
+ *
+ * Same energies as plum_cbmc_trials, but every buffer is the caller's and is
+ * in DEVICE memory: d_b1, d_b2 [n_trials*3], d_chain, d_chain_ci
+ * [chain_len*3], d_u_out [n_trials]. The call allocates nothing (no
+ * cudaMalloc/cudaFree, no host heap): its working memory is one fixed array
+ * of 850 KiB inside the library, held on every GPU that loads the library
+ * until the process exits. Limits: n_trials <= 256, chain_len <= 1024, at
+ * most 32768 half-space k-vectors (the Ewald k-set of run.in); larger
+ * requests return PLUM_ERR_INPUT. Nothing has to be zeroed first: each call
+ * writes all the working memory it reads.
+ *
+ * The first call on each device does a one-time set-up (it looks up the
+ * array's device address, with that device current): make a first call on
+ * each device before starting any stream capture. All calls share the one
+ * array, so calls that overlap on the GPU (from several threads or contexts
+ * on the same device) race; serialise them. The call waits for its results
+ * on the context's stream. Errors are returned as codes, with the message
+ * written to err[err_cap] (may be NULL); plum_last_error is not updated. */
+int plum_cbmc_trials_noalloc(plum_ctx* ctx, int n_trials, const double* d_b1,
+                             const double* d_b2, int chain_len, const double* d_chain,
+                             const double* d_chain_ci, int delete_mol, double* d_u_out,
+                             char* err, int err_cap);
+
 /* Full FP64 recompute cadence of plum_run, in moves (0 = never). The
  * precision form defaults to 10000: every 10^4 moves (at the next batch
  * boundary of 256) the totals, S(k) and the fixed-point mirror are rebuilt

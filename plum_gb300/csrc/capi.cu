@@ -1024,6 +1024,52 @@ int plum_cbmc_trials(plum_ctx* c, int n_trials, const double* b1, const double* 
   return PLUM_OK;
 }
 
+int plum_cbmc_trials_noalloc(plum_ctx* c, int n_trials, const double* d_b1, const double* d_b2,
+                             int chain_len, const double* d_chain, const double* d_chain_ci,
+                             int delete_mol, double* d_u_out, char* err, int err_cap) {
+  auto say = [&](const char* m) {
+    if (err && err_cap > 0) std::snprintf(err, (size_t)err_cap, "%s", m);
+  };
+  if (!c || !d_b1 || !d_u_out || (chain_len > 0 && !d_chain)) {
+    say("plum_cbmc_trials_noalloc: null argument");
+    return PLUM_ERR_INPUT;
+  }
+  const Input& in = c->in;
+  if (!in.use_gc) {
+    say("plum_cbmc_trials_noalloc: run.in has no grand-canonical species");
+    return PLUM_ERR_INPUT;
+  }
+  const int charged = in.gc_bead_charge != 0;
+  if (charged && (!d_b2 || (chain_len > 0 && !d_chain_ci))) {
+    say("plum_cbmc_trials_noalloc: a charged species needs trial counterions");
+    return PLUM_ERR_INPUT;
+  }
+  if (c->host_pending) {
+    say("plum_cbmc_trials_noalloc: a trial move is pending");
+    return PLUM_ERR_STATE;
+  }
+  int ex_lo = 0, ex_hi = 0;
+  if (delete_mol >= 0) {
+    const int last = delete_mol + (charged ? in.gc_chain_len : 0);
+    if (last >= in.n_mol) {
+      say("plum_cbmc_trials_noalloc: deleted molecule range out of bounds");
+      return PLUM_ERR_INPUT;
+    }
+    ex_lo = in.mol_start[delete_mol];
+    ex_hi = in.mol_start[last + 1];
+  }
+  int type = 0;
+  while (type < (int)in.type_names.size() && in.type_names[type] != in.gc_symbol) type++;
+  if (cudaSetDevice(c->device) != cudaSuccess) {
+    say("plum_cbmc_trials_noalloc: cannot select the context's device");
+    return PLUM_ERR_CUDA;
+  }
+  int rc = cbmc_trials_noalloc(c->P, c->B, c->s, c->device, n_trials, d_b1, d_b2, chain_len,
+                               d_chain, d_chain_ci, type, charged, in.gc_bead_charge,
+                               -in.gc_bead_charge, ex_lo, ex_hi, d_u_out, err, err_cap);
+  return rc == 0 ? PLUM_OK : (rc == 1 ? PLUM_ERR_INPUT : PLUM_ERR_CUDA);
+}
+
 int plum_set_recompute(plum_ctx* c, long every) {
   if (!c || every < 0) return fail(PLUM_ERR_INPUT, "bad argument");
   c->recompute_every = every;

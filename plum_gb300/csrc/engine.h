@@ -174,6 +174,13 @@ struct CbmcJob {
 };
 int cbmc_groups(const DevParams& P);
 void launch_cbmc(const DevParams& P, const DevBuffers& B, const CbmcJob& J, cudaStream_t s);
+// The same on a fixed scratch array (no allocation); returns 0, 1 (sizes) or 2
+// (CUDA), with a message in err.
+int cbmc_trials_noalloc(const DevParams& P, const DevBuffers& B, cudaStream_t s, int device,
+                        int n_trials, const double* d_b1, const double* d_b2, int chain_len,
+                        const double* d_chain, const double* d_chain_ci, int type, int charged,
+                        double q1, double q2, int ex_lo, int ex_hi, double* d_u, char* err,
+                        int err_cap);
 
 // batched replicas (kern_fp32.cu / kern_moves.cu)
 constexpr int kMaxReplicas = 2048;

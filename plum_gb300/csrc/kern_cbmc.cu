@@ -14,6 +14,9 @@
 //                 change; 1e8 when the pair sum reaches 1e8 (cbmc.cc:146-148)
 // The arithmetic is the plain form's (FP64) with the same pair functions as
 // the move kernels.
+#include <cstdio>
+#include <mutex>
+
 #include "device_common.cuh"
 #include "engine.h"
 
@@ -231,6 +234,127 @@ void launch_cbmc(const DevParams& P, const DevBuffers& B, const CbmcJob& J, cuda
   const int g = cbmc_groups(P);
   k_cbmc_sys<<<dim3(g, J.n_trials), kCbThreads, 0, s>>>(P, B, J);
   k_cbmc_fin<<<J.n_trials, kCbThreads, 0, s>>>(P, B, J, g);
+}
+
+
+// ------------------------------------------------------------- no-alloc
+// Working memory of plum_cbmc_trials_noalloc, for callers that must not
+// allocate device memory (hosts whose device memory belongs to their own
+// allocator, or drivers that cannot take the device-wide synchronisation of
+// cudaMalloc/cudaFree). One fixed array on every GPU
+// that loads the library, held until the process exits:
+//   trial beads + counterions  2 * kMaxTrials double4          16 KiB
+//   grown chain + counterions  2 * kMaxChain  double4          64 KiB
+//   S_o(k)                     kMaxK          double2         512 KiB
+//   per-block sums             2 * kMaxTrials * kMaxGroups    256 KiB
+//   results                    kMaxTrials     double            2 KiB
+// Nothing in it has to start at zero: each call writes every element it
+// reads (k_na_pack the beads and chain, k_cbmc_so all n_k entries of S_o,
+// k_cbmc_sys one sum pair per (trial, block), k_cbmc_fin one result per
+// trial) before reading it. All calls on a device share the array, so calls
+// that overlap on the GPU race.
+namespace na {
+constexpr int kMaxTrials = 256, kMaxChain = 1024, kMaxK = 32768, kMaxGroups = 64;
+constexpr size_t kBeadsOff = 0;
+constexpr size_t kChainOff = kBeadsOff + sizeof(double4_32a) * 2 * kMaxTrials;
+constexpr size_t kSoOff = kChainOff + sizeof(double4_32a) * 2 * kMaxChain;
+constexpr size_t kPartOff = kSoOff + sizeof(double2) * kMaxK;
+constexpr size_t kUOff = kPartOff + sizeof(double) * 2 * kMaxTrials * kMaxGroups;
+constexpr size_t kBytes = kUOff + sizeof(double) * kMaxTrials;
+}  // namespace na
+
+static __device__ __align__(256) unsigned char g_cbmc_noalloc_scratch[na::kBytes];
+
+// Device address of the scratch array per device, resolved on the first call
+// made with that device current (a host-side name of a __device__ array is
+// not a device address).
+static std::mutex g_na_mu;
+static unsigned char* g_na_ptr[64];
+
+// Packs caller device arrays (xyz triples) into the scratch's double4 rows.
+__global__ void k_na_pack(const double* b1, const double* b2, int T, const double* chain,
+                          const double* chain_ci, int cl, double q1, double q2, int charged,
+                          double4_32a* beads, double4_32a* cbuf) {
+  for (int i = threadIdx.x; i < T; i += blockDim.x) {
+    beads[i] = make_double4_32a(b1[3 * i], b1[3 * i + 1], b1[3 * i + 2], q1);
+    beads[T + i] = charged ? make_double4_32a(b2[3 * i], b2[3 * i + 1], b2[3 * i + 2], q2)
+                           : beads[i];
+  }
+  for (int i = threadIdx.x; i < cl; i += blockDim.x) {
+    cbuf[i] = make_double4_32a(chain[3 * i], chain[3 * i + 1], chain[3 * i + 2], q1);
+    cbuf[cl + i] = charged ? make_double4_32a(chain_ci[3 * i], chain_ci[3 * i + 1],
+                                              chain_ci[3 * i + 2], q2)
+                           : cbuf[i];
+  }
+}
+
+int cbmc_trials_noalloc(const DevParams& P, const DevBuffers& B, cudaStream_t s, int device,
+                        int n_trials, const double* d_b1, const double* d_b2, int chain_len,
+                        const double* d_chain, const double* d_chain_ci, int type, int charged,
+                        double q1, double q2, int ex_lo, int ex_hi, double* d_u, char* err,
+                        int err_cap) {
+  auto say = [&](const char* m) {
+    if (err && err_cap > 0) snprintf(err, (size_t)err_cap, "%s", m);
+  };
+  if (n_trials < 1 || n_trials > na::kMaxTrials) {
+    say("plum_cbmc_trials_noalloc: n_trials must be 1..256");
+    return 1;
+  }
+  if (chain_len < 0 || chain_len > na::kMaxChain) {
+    say("plum_cbmc_trials_noalloc: chain_len must be 0..1024");
+    return 1;
+  }
+  if (P.n_k > na::kMaxK) {
+    say("plum_cbmc_trials_noalloc: more than 32768 half-space k-vectors");
+    return 1;
+  }
+  static_assert(na::kMaxGroups >= 64, "cbmc_groups() is at most 64");
+  if (device < 0 || device >= 64) {
+    say("plum_cbmc_trials_noalloc: device index out of range");
+    return 1;
+  }
+  unsigned char* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    if (!g_na_ptr[device]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_cbmc_noalloc_scratch);
+      if (e != cudaSuccess || !p) {
+        say("plum_cbmc_trials_noalloc: cudaGetSymbolAddress failed");
+        return 2;
+      }
+      g_na_ptr[device] = static_cast<unsigned char*>(p);
+    }
+    base = g_na_ptr[device];
+  }
+  double4_32a* beads = reinterpret_cast<double4_32a*>(base + na::kBeadsOff);
+  double4_32a* cbuf = reinterpret_cast<double4_32a*>(base + na::kChainOff);
+  k_na_pack<<<1, 256, 0, s>>>(d_b1, d_b2, n_trials, d_chain, d_chain_ci, chain_len, q1, q2,
+                              charged, beads, cbuf);
+  CbmcJob J;
+  J.n_trials = n_trials;
+  J.charged = charged;
+  J.cl = chain_len;
+  J.type = type;
+  J.ex_lo = ex_lo;
+  J.ex_hi = ex_hi;
+  J.b1 = beads;
+  J.b2 = beads + n_trials;
+  J.chain = cbuf;
+  J.chain_ci = cbuf + chain_len;
+  J.s_o = reinterpret_cast<double2*>(base + na::kSoOff);
+  J.part = reinterpret_cast<double*>(base + na::kPartOff);
+  J.u = reinterpret_cast<double*>(base + na::kUOff);
+  launch_cbmc(P, B, J, s);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_u, J.u, sizeof(double) * n_trials, cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    say(cudaGetErrorString(e));
+    return 2;
+  }
+  return 0;
 }
 
 }  // namespace plum
