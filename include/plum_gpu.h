@@ -146,6 +146,16 @@ int plum_set_positions(plum_ctx* ctx, const double* xyz);
  * RadiusOfGyrationXYZ and EndToEndDistance (simulation.cc:406-500). */
 int plum_observables(const plum_ctx* ctx, double* out);
 
+/* rho(z) of the current configuration, one sample of Simulation::CalcRhoZ
+ * (simulation.cc:1029-1045): bins of 0.02 along z (z wrapped into [0, Lz)),
+ * out[3*bin + id] with id 0 for chain beads, 1 for ions with q >= 0, 2 for
+ * q < 0, each bead adding 1/(Lx Ly 0.02); molecules before `phantom` are
+ * skipped. The reference accumulates samples into density_z_cumu; the
+ * caller sums the returned samples. *n_bins (may be NULL) receives
+ * ceil(Lz/0.02); at most cap values are written (cap = 0 only reports
+ * n_bins). */
+int plum_rhoz(const plum_ctx* ctx, double* out, int cap, int* n_bins);
+
 /* Configurational-bias trial-site energies of one growth step: for each of
  * n_trials trial positions b1[t] of the grand-canonical species' next bead
  * (and, for a charged species, its trial counterion b2[t]), the energy
@@ -234,6 +244,66 @@ int plum_batch_size(const plum_batch* batch);
  * observables through the single-system calls above. */
 int plum_batch_replica(plum_batch* batch, int r, plum_ctx** ctx);
 int plum_batch_last_timing(const plum_batch* batch, double* ms, long* kernels);
+
+/* ---------------------------------------------------------------------
+ * Learned surrogate and delayed acceptance. No counterpart in the
+ * reference: an addition that keeps the stationary distribution of its
+ * Metropolis step (simulation.cc:324-332).
+ *
+ * Descriptor of a move of beads [b_lo, b_hi) (96 values): 4 channels x 24
+ * Gaussian-smeared radial bins (width 0.25 sigma, centres 0.125..5.875
+ * sigma; pairs up to 7.5 sigma) of the pairs (moved bead, other bead; moved
+ * pairs once): channel 0 neighbours of the moved bead's type before the
+ * move, 1 other types before, 2 and 3 the same after the move. Values are
+ * sums in units of 2^-12.
+ *
+ * Network: 96 -> 128 -> 128 -> 1, SiLU, BF16 weights, FP32 accumulation,
+ * input standardised by (x - mu) * isd. Its surrogate energy change is
+ * s = y_scale (f(x) - f(swap x)), swap exchanging channels (0,1) with (2,3),
+ * so s of the reverse move is exactly -s. Parameters (fp32, in this order):
+ * W1 [128][96], b1 [128], W2 [128][128], b2 [128], w3 [128], b3. */
+typedef struct plum_surrogate plum_surrogate;
+int plum_surrogate_nparams(void);
+/* Glorot-uniform weights from seed, zero biases, mu = 0, isd = 1. */
+int plum_surrogate_create(int device, unsigned long long seed, plum_surrogate** out);
+int plum_surrogate_destroy(plum_surrogate* sg);
+int plum_surrogate_set_params(plum_surrogate* sg, const float* params);
+int plum_surrogate_get_params(const plum_surrogate* sg, float* params);
+int plum_surrogate_set_norm(plum_surrogate* sg, const float* mu, const float* isd,
+                            float y_scale);
+/* s for n descriptors x [n][96] (host buffers; _device: device buffers). */
+int plum_surrogate_predict(plum_surrogate* sg, const float* x, long n, float* s_out);
+int plum_surrogate_predict_device(plum_surrogate* sg, const float* d_x, long n, float* d_s);
+/* Gradient of mean_n (s - t)^2 over every parameter, then the loss:
+ * grad_out [nparams + 1] (host buffers). */
+int plum_surrogate_grad(plum_surrogate* sg, const float* x, const float* t, long n,
+                        float* grad_out);
+/* Adam (beta 0.9, 0.999, eps 1e-8) with the given gradient [nparams]. */
+int plum_surrogate_adam_step(plum_surrogate* sg, const float* grad, float lr);
+/* Adam training on DEVICE data d_x [n][96], d_t [n]: `epochs` shuffled
+ * passes (seeded) of n / batch steps; loss_out[epochs] (may be NULL) gets
+ * each pass's mean loss. */
+int plum_surrogate_train(plum_surrogate* sg, const float* d_x, const float* d_t, long n,
+                         int batch, int epochs, float lr, unsigned long long seed,
+                         double* loss_out);
+/* Descriptor [96] of the pending trial move of plum_delta_energy (before
+ * plum_finalize), in the units above. */
+int plum_move_descriptor(plum_ctx* ctx, double* out);
+/* Training data from the plain step loop (plum_run semantics, n_moves
+ * steps): for each pivot, crankshaft or reptation move, its descriptor and
+ * its exact energy change (1e8 on overlap) into DEVICE buffers d_desc
+ * [cap][96] and d_de [cap]; *n_logged = rows written (at most cap). */
+int plum_collect_surrogate_data(plum_ctx* ctx, int n_moves, long cap, float* d_desc,
+                                double* d_de, long* n_logged);
+/* Delayed acceptance in the replica batch (sg NULL turns it off; sg must
+ * outlive its use). A chain move draws u1 after its own draws and is
+ * rejected at stage one unless u1 < exp(-beta s); a move that passes draws
+ * u2 and is accepted if u2 < exp(-beta (dE - s)) (no draw when dE >= 1e8).
+ * Moves rejected at stage one skip the exact energy change. */
+int plum_batch_set_surrogate(plum_batch* batch, const plum_surrogate* sg);
+/* Totals since plum_batch_set_surrogate: out3 = {surrogate moves, stage-one
+ * passes, accepted}. */
+int plum_batch_da_stats(plum_batch* batch, long* out3);
 
 #ifdef __cplusplus
 }

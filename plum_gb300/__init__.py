@@ -67,6 +67,7 @@ def lib():
         L.plum_get_positions.argtypes = [C.c_void_p, _dp]
         L.plum_set_positions.argtypes = [C.c_void_p, _dp]
         L.plum_observables.argtypes = [C.c_void_p, _dp]
+        L.plum_rhoz.argtypes = [C.c_void_p, _dp, C.c_int, C.POINTER(C.c_int)]
         L.plum_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_double),
                                        C.POINTER(C.c_long)]
         L.plum_set_recompute.argtypes = [C.c_void_p, C.c_long]
@@ -91,6 +92,23 @@ def lib():
         L.plum_sim_run_steps.argtypes = [C.c_void_p, C.c_long]
         L.plum_sim_positions.argtypes = [C.c_void_p, _dp]
         L.plum_sim_energies.argtypes = [C.c_void_p, _dp]
+        _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
+        L.plum_surrogate_create.argtypes = [C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]
+        L.plum_surrogate_destroy.argtypes = [C.c_void_p]
+        L.plum_surrogate_set_params.argtypes = [C.c_void_p, _fp]
+        L.plum_surrogate_get_params.argtypes = [C.c_void_p, _fp]
+        L.plum_surrogate_set_norm.argtypes = [C.c_void_p, _fp, _fp, C.c_float]
+        L.plum_surrogate_predict.argtypes = [C.c_void_p, _fp, C.c_long, _fp]
+        L.plum_surrogate_predict_device.argtypes = [C.c_void_p, C.c_void_p, C.c_long, C.c_void_p]
+        L.plum_surrogate_grad.argtypes = [C.c_void_p, _fp, _fp, C.c_long, _fp]
+        L.plum_surrogate_adam_step.argtypes = [C.c_void_p, _fp, C.c_float]
+        L.plum_surrogate_train.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_long, C.c_int,
+                                           C.c_int, C.c_float, C.c_ulonglong, C.c_void_p]
+        L.plum_collect_surrogate_data.argtypes = [C.c_void_p, C.c_int, C.c_long, C.c_void_p,
+                                                  C.c_void_p, C.POINTER(C.c_long)]
+        L.plum_move_descriptor.argtypes = [C.c_void_p, _dp]
+        L.plum_batch_set_surrogate.argtypes = [C.c_void_p, C.c_void_p]
+        L.plum_batch_da_stats.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
         _lib = L
     return _lib
 
@@ -109,6 +127,13 @@ def _check(rc):
 
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _dev(t, dtype):
+    """Device pointer of a contiguous CUDA tensor of the given torch dtype."""
+    if not (t.is_cuda and t.is_contiguous() and t.dtype == dtype):
+        raise ValueError("expected a contiguous CUDA tensor of %s" % dtype)
+    return C.c_void_p(t.data_ptr())
 
 
 class System:
@@ -190,6 +215,14 @@ class System:
         _check(lib().plum_observables(self.h, o))
         return o
 
+    def rhoz(self):
+        """One rho(z) sample [n_bins, 3] (chain beads, q >= 0 ions, q < 0 ions)."""
+        nb = C.c_int(0)
+        _check(lib().plum_rhoz(self.h, None, 0, C.byref(nb)))
+        o = np.zeros(3 * nb.value)
+        _check(lib().plum_rhoz(self.h, o, len(o), C.byref(nb)))
+        return o.reshape(-1, 3)
+
     def cbmc_trials(self, b1, b2=None, chain=None, chain_ci=None, delete_mol=-1):
         """BeadsEnergy of trial sites b1[T,3] (and trial counterions b2[T,3] for a
         charged species) given the grown chain[cl,3] (and chain_ci[cl,3])."""
@@ -216,6 +249,101 @@ class System:
         k = C.c_long(0)
         _check(lib().plum_last_timing(self.h, C.byref(ms), C.byref(k)))
         return ms.value, k.value
+
+
+    def move_descriptor(self):
+        """Surrogate descriptor [96] of the pending trial move (after
+        energy_difference, before finalize)."""
+        o = np.zeros(96)
+        _check(lib().plum_move_descriptor(self.h, o))
+        return o
+
+    def collect_surrogate_data(self, n_moves: int, cap: int, out=None):
+        """Runs n_moves plain steps (as run) and returns (desc [k][96], dE [k])
+        of the chain moves among them as CUDA tensors (k <= cap). `out`: a
+        pair of preallocated tensors ([>= cap][96] float32, [>= cap] float64)
+        to write into instead (they must be idle on the GPU)."""
+        import torch
+        if out is None:
+            desc = torch.empty((cap, 96), dtype=torch.float32, device="cuda")
+            de = torch.empty(cap, dtype=torch.float64, device="cuda")
+            torch.cuda.current_stream().synchronize()
+        else:
+            desc, de = out
+            if desc.shape[0] < cap or de.shape[0] < cap:
+                raise ValueError("output tensors smaller than cap")
+        k = C.c_long(0)
+        _check(lib().plum_collect_surrogate_data(self.h, n_moves, cap, _dev(desc, torch.float32),
+                                                 _dev(de, torch.float64), C.byref(k)))
+        return desc[:k.value], de[:k.value]
+
+
+class Surrogate:
+    """The learned energy-change surrogate (include/plum_gpu.h,
+    plum_surrogate_*): BF16 tensor-core forward/backward and Adam on the GPU."""
+
+    N_IN = 96
+
+    def __init__(self, seed: int = 1, device: int = 0):
+        h = C.c_void_p()
+        _check(lib().plum_surrogate_create(device, seed, C.byref(h)))
+        self.h = h
+        self.n_params = lib().plum_surrogate_nparams()
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().plum_surrogate_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def params(self):
+        o = np.zeros(self.n_params, np.float32)
+        _check(lib().plum_surrogate_get_params(self.h, o))
+        return o
+
+    def set_params(self, p):
+        _check(lib().plum_surrogate_set_params(self.h, np.ascontiguousarray(p, np.float32)))
+
+    def set_norm(self, mu, isd, y_scale):
+        self.norm = (np.asarray(mu, np.float32), np.asarray(isd, np.float32), float(y_scale))
+        _check(lib().plum_surrogate_set_norm(self.h, np.ascontiguousarray(mu, np.float32),
+                                             np.ascontiguousarray(isd, np.float32), y_scale))
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 96)
+        o = np.zeros(len(x), np.float32)
+        _check(lib().plum_surrogate_predict(self.h, x, len(x), o))
+        return o
+
+    def predict_device(self, x):
+        import torch
+        out = torch.empty(x.shape[0], dtype=torch.float32, device=x.device)
+        torch.cuda.synchronize()
+        _check(lib().plum_surrogate_predict_device(self.h, _dev(x, torch.float32), x.shape[0],
+                                                   _dev(out, torch.float32)))
+        return out
+
+    def grad(self, x, t):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 96)
+        t = np.ascontiguousarray(t, np.float32)
+        o = np.zeros(self.n_params + 1, np.float32)
+        _check(lib().plum_surrogate_grad(self.h, x, t, len(x), o))
+        return o[:-1], float(o[-1])
+
+    def adam_step(self, g, lr):
+        _check(lib().plum_surrogate_adam_step(self.h, np.ascontiguousarray(g, np.float32), lr))
+
+    def train(self, x, t, batch=4096, epochs=1, lr=1e-3, seed=0):
+        """Adam on CUDA tensors x [n][96] (float32), t [n] (float32)."""
+        import torch
+        losses = np.zeros(max(epochs, 1))
+        torch.cuda.synchronize()
+        _check(lib().plum_surrogate_train(self.h, _dev(x, torch.float32), _dev(t, torch.float32),
+                                          x.shape[0], batch, epochs, lr, seed,
+                                          losses.ctypes.data_as(C.c_void_p)))
+        return losses[:epochs]
 
 
 class _Replica(System):
@@ -276,6 +404,17 @@ class Batch:
         k = C.c_long(0)
         _check(lib().plum_batch_last_timing(self.h, C.byref(ms), C.byref(k)))
         return ms.value, k.value
+
+    def set_surrogate(self, sg):
+        """Delayed acceptance with the surrogate sg (None: off)."""
+        self._sg = sg
+        _check(lib().plum_batch_set_surrogate(self.h, None if sg is None else sg.h))
+
+    def da_stats(self):
+        """(surrogate moves, stage-one passes, accepted) since set_surrogate."""
+        o = (C.c_long * 3)()
+        _check(lib().plum_batch_da_stats(self.h, o))
+        return tuple(o)
 
 
 class HostSimulation:

@@ -11,6 +11,8 @@
 #include "../../include/plum_gpu.h"
 #include "engine.h"
 #include "host/input.h"
+#include "mlp.h"
+#include "surrogate.h"
 
 using namespace plum;
 
@@ -22,6 +24,14 @@ int fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
+
+}  // namespace
+
+namespace plum {
+int fail_msg(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace plum
+
+namespace {
 
 #define CK(call)                                                                 \
   do {                                                                           \
@@ -48,6 +58,15 @@ struct plum_ctx {
   double* d_tot_part = nullptr;
   int n_tot_part = 0;
   double* d_out = nullptr;     // small result block
+  double* d_obs_per = nullptr;  // [n_mol * 5] per-molecule Rg / Ree sums
+  unsigned* d_rhoz = nullptr;   // [3 * rhoz_bins] rho(z) counts
+  int rhoz_bins = 0;
+  // surrogate training data: descriptor accumulator and device copies of
+  // P and B for the descriptor kernel
+  unsigned* desc_acc = nullptr;
+  unsigned* desc_fine = nullptr;
+  DevParams* d_rp1 = nullptr;
+  DevBuffers* d_rb1 = nullptr;
   double* h_out = nullptr;     // pinned
   uint32_t* d_stream = nullptr;
   long long stream_cap = 0;
@@ -282,11 +301,17 @@ void launch_delta(const plum_ctx* c, const DevBuffers& B) {
 }
 
 void enqueue_loop(plum_ctx* c, int n_moves, const DevBuffers& B) {
+  // with a training log, each generated chain move's descriptor is taken
+  // before its energy change
+  const bool desc = B.log_desc != nullptr;
   launch_serial64(c->P, B, kModeGen, c->s);
+  if (desc) launch_desc_batch(c->d_rp1, c->d_rb1, 1, B.desc_acc, c->P.form, c->s);
   for (int i = 0; i < n_moves; i++) {
     launch_delta(c, B);
     int mode = kModeFinish | kModeDecide | (i + 1 < n_moves ? kModeGen : 0);
     launch_serial64(c->P, B, mode, c->s);
+    if (desc && i + 1 < n_moves)
+      launch_desc_batch(c->d_rp1, c->d_rb1, 1, B.desc_acc, c->P.form, c->s);
   }
 }
 
@@ -296,7 +321,8 @@ void enqueue_loop(plum_ctx* c, int n_moves, const DevBuffers& B) {
 // capture); the kernels read the pending move from device state, so one
 // capture replays for every batch.
 int device_loop(plum_ctx* c, int n_moves, DevBuffers B) {
-  const long k = 1 + 2L * n_moves;
+  const long k = 1 + 2L * n_moves + (B.log_desc ? n_moves : 0);
+  if (B.log_desc) CK(cudaMemcpyAsync(c->d_rb1, &B, sizeof(B), cudaMemcpyHostToDevice, c->s));
   const bool same = c->gexec && c->g_moves == n_moves && !std::memcmp(&c->g_B, &B, sizeof(B));
   if (same) {
     CK(cudaGraphLaunch(c->gexec, c->s));
@@ -545,6 +571,9 @@ static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out) {
   c->n_tot_part = total_partials_count(P);
   rc |= dalloc(&c->d_tot_part, 2 * (size_t)c->n_tot_part);
   rc |= dalloc(&c->d_out, 64);
+  rc |= dalloc(&c->d_obs_per, 5 * (size_t)std::max(1, in.n_mol));
+  c->rhoz_bins = (int)std::ceil(in.box[2] / kRhoZRes);
+  rc |= dalloc(&c->d_rhoz, 3 * (size_t)std::max(1, c->rhoz_bins));
   rc |= dalloc(&c->d_mt, 625);
   if (rc) {
     plum_ctx_destroy(c);
@@ -594,7 +623,8 @@ int plum_ctx_destroy(plum_ctx* c) {
                   c->B.partial,  c->B.bond_mol, c->B.state, c->d_tot_part,  c->d_out,
                   c->B.dsk_part, c->B.ktile_count, c->B.kpartial, c->B.fpos, c->B.done_count,
                   c->B.fq,       c->B.ftrial,  c->B.dsk_part32, c->cb_b, c->cb_c, c->cb_so,
-                  c->cb_part,    c->cb_u,
+                  c->cb_part,    c->cb_u,      c->d_obs_per, c->d_rhoz, c->desc_acc,
+                  c->d_rp1,      c->d_rb1,     c->desc_fine,
                   c->d_stream,   c->d_mt,      c->d_log_type, c->d_log_acc, c->d_log_e};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -689,6 +719,40 @@ int plum_delta_energy(plum_ctx* c, int mol, const double* trial, const int* move
   out[0] = st.de, out[1] = st.de_pair, out[2] = st.de_ewald, out[3] = st.de_bond,
   out[4] = st.de_ext;
   c->host_pending = true;
+  return PLUM_OK;
+}
+
+namespace {
+int ensure_desc(plum_ctx* c) {
+  if (c->desc_acc) return PLUM_OK;
+  int rc = dalloc(&c->desc_acc, mlp::kIn) | dalloc(&c->desc_fine, mlp::kFineAll) |
+           dalloc(&c->d_rp1, 1) | dalloc(&c->d_rb1, 1);
+  if (rc) return PLUM_ERR_CUDA;
+  CK(cudaMemcpyAsync(c->d_rp1, &c->P, sizeof(DevParams), cudaMemcpyHostToDevice, c->s));
+  return PLUM_OK;
+}
+}  // namespace
+
+int plum_move_descriptor(plum_ctx* c, double* out) {
+  if (!c || !out) return fail(PLUM_ERR_INPUT, "null argument");
+  if (!c->host_pending) return fail(PLUM_ERR_STATE, "no pending trial move");
+  cudaSetDevice(c->device);
+  int rc = ensure_desc(c);
+  if (rc) return rc;
+  DevBuffers B = c->B;
+  B.desc_acc = c->desc_acc;
+  B.desc_fine = c->desc_fine;
+  const int one = 1, zero = 0;
+  CK(cudaMemcpyAsync(c->d_rb1, &B, sizeof(B), cudaMemcpyHostToDevice, c->s));
+  CK(cudaMemsetAsync(c->desc_fine, 0, sizeof(unsigned) * mlp::kFineAll, c->s));
+  CK(cudaMemcpyAsync(&c->B.state->da_active, &one, sizeof(int), cudaMemcpyHostToDevice, c->s));
+  launch_desc_batch(c->d_rp1, c->d_rb1, 1, c->desc_acc, c->P.form, c->s);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(&c->B.state->da_active, &zero, sizeof(int), cudaMemcpyHostToDevice, c->s));
+  unsigned h[mlp::kIn];
+  CK(cudaMemcpyAsync(h, c->desc_acc, sizeof(h), cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  for (int k = 0; k < mlp::kIn; k++) out[k] = h[k] * (double)mlp::kDescUnit;
   return PLUM_OK;
 }
 
@@ -899,11 +963,31 @@ int plum_observables(const plum_ctx* cc, double* out) {
   plum_ctx* c = const_cast<plum_ctx*>(cc);
   if (!c || !out) return fail(PLUM_ERR_INPUT, "null argument");
   cudaSetDevice(c->device);
-  launch_observables64(c->P, c->B, c->d_out + 32, c->s);
+  launch_observables64(c->P, c->B, c->d_obs_per, c->d_out + 32, c->s);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(c->h_out, c->d_out + 32, sizeof(double) * 5, cudaMemcpyDeviceToHost, c->s));
   CK(cudaStreamSynchronize(c->s));
   std::memcpy(out, c->h_out, sizeof(double) * 5);
+  return PLUM_OK;
+}
+
+int plum_rhoz(const plum_ctx* cc, double* out, int cap, int* n_bins) {
+  plum_ctx* c = const_cast<plum_ctx*>(cc);
+  if (!c || (!out && cap > 0) || cap < 0) return fail(PLUM_ERR_INPUT, "bad argument");
+  const int nb = c->rhoz_bins;
+  if (n_bins) *n_bins = nb;
+  if (cap == 0) return PLUM_OK;
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
+  cudaSetDevice(c->device);
+  launch_rhoz(c->P, c->B, kRhoZRes, nb, c->d_rhoz, c->s);
+  CK(cudaGetLastError());
+  std::vector<unsigned> cnt(3 * (size_t)nb);
+  CK(cudaMemcpyAsync(cnt.data(), c->d_rhoz, sizeof(unsigned) * cnt.size(),
+                     cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  const double w = 1.0 / (c->in.box[0] * c->in.box[1] * kRhoZRes);
+  const int n = std::min(cap, 3 * nb);
+  for (int i = 0; i < n; i++) out[i] = cnt[i] * w;
   return PLUM_OK;
 }
 
@@ -1020,6 +1104,39 @@ int plum_cbmc_trials(plum_ctx* c, int n_trials, const double* b1, const double* 
   launch_cbmc(c->P, c->B, J, c->s);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(u_out, c->cb_u, sizeof(double) * n_trials, cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  return PLUM_OK;
+}
+
+int plum_collect_surrogate_data(plum_ctx* c, int n_moves, long cap, float* d_desc,
+                                double* d_de, long* n_logged) {
+  if (!c || n_moves < 0 || cap <= 0 || cap > (1L << 31) - 1 || !d_desc || !d_de)
+    return fail(PLUM_ERR_INPUT, "bad argument");
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
+  cudaSetDevice(c->device);
+  int rc = ensure_desc(c);
+  if (rc) return rc;
+  DevState st;
+  rc = read_state(c, &st);
+  if (rc) return rc;
+  st.log_n = 0;
+  st.log_cap = (int)cap;
+  CK(cudaMemcpyAsync(c->B.state, &st, sizeof(DevState), cudaMemcpyHostToDevice, c->s));
+  c->B.desc_acc = c->desc_acc;
+  c->B.desc_fine = c->desc_fine;
+  c->B.log_desc = d_desc;
+  c->B.log_de = d_de;
+  rc = plum_run(c, n_moves, nullptr);
+  c->B.desc_acc = nullptr;
+  c->B.desc_fine = nullptr;
+  c->B.log_desc = nullptr;
+  c->B.log_de = nullptr;
+  int rc2 = read_state(c, &st);
+  if (rc) return rc;
+  if (rc2) return rc2;
+  if (n_logged) *n_logged = st.log_n;
+  st.log_cap = 0;
+  CK(cudaMemcpyAsync(c->B.state, &st, sizeof(DevState), cudaMemcpyHostToDevice, c->s));
   CK(cudaStreamSynchronize(c->s));
   return PLUM_OK;
 }
@@ -1155,17 +1272,34 @@ struct plum_batch {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double last_ms = 0;
   long last_kernels = 0;
+  // delayed acceptance: descriptors [replicas][96] and the surrogate in use
+  unsigned* d_desc = nullptr;
+  unsigned* d_fine = nullptr;
+  const plum_surrogate* sg = nullptr;
+  int* d_err = nullptr;
 };
 
 namespace {
 
+// One batch of steps: gen; then per step the exact energy change, finish +
+// decide + gen. With a surrogate, each gen is followed by the descriptors of
+// the generated chain moves and the surrogate's stage one, which marks the
+// moves it rejects so that the delta kernel skips them.
 void batch_enqueue(plum_batch* b, int steps) {
   const int R = (int)b->reps.size();
+  auto stage_one = [&]() {
+    if (!b->sg) return;
+    launch_desc_batch(b->d_rp, b->d_rb, R, b->d_desc, 1, b->s);
+    launch_mlp_infer_i(b->sg->net, b->d_desc, R, nullptr, DaArgs{b->d_sts, b->d_rp}, b->d_err,
+                       b->s);
+  };
   launch_batch_serial(b->d_rp, b->d_rb, b->d_item_off, b->d_slots, R, kModeGen, b->s);
+  stage_one();
   for (int i = 0; i < steps; i++) {
     launch_batch_delta32(b->d_rp, b->d_rb, R, b->d_item_off, b->d_slots, b->kt_smem, b->s);
     int mode = kModeFinish | kModeDecide | (i + 1 < steps ? kModeGen : 0);
     launch_batch_serial(b->d_rp, b->d_rb, b->d_item_off, b->d_slots, R, mode, b->s);
+    if (i + 1 < steps) stage_one();
   }
 }
 
@@ -1204,7 +1338,8 @@ int plum_batch_destroy(plum_batch* b) {
   if (b->s) cudaStreamSynchronize(b->s);
   for (plum_ctx* c : b->reps) plum_ctx_destroy(c);
   void* ptrs[] = {b->d_rp,    b->d_rb,  b->d_item_off, b->d_slots, b->d_states, b->d_outs,
-                  b->d_sts,   b->d_pos, b->d_len,      b->d_cap,   b->d_gather, b->d_need};
+                  b->d_sts,   b->d_pos, b->d_len,      b->d_cap,   b->d_gather, b->d_need,
+                  b->d_desc,  b->d_err, b->d_fine};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->h_gather) cudaFreeHost(b->h_gather);
@@ -1253,7 +1388,7 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
   for (int r = 0; r < n; r++) {
     plum_ctx* c = b->reps[r];
     const DevParams& P = c->P;
-    b->per_step[r] = 16 + 10LL * c->max_len;
+    b->per_step[r] = 17 + 10LL * c->max_len;  // + the stage-one draw
     b->cap[r] = std::max<long long>(4 * b->batch_steps * b->per_step[r], 1 << 16);
     int rc = ensure_stream(c, b->cap[r]);
     if (rc) {
@@ -1286,9 +1421,17 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
   rc |= dalloc(&b->d_cap, n);
   rc |= dalloc(&b->d_gather, 6 * (size_t)n);
   rc |= dalloc(&b->d_need, n);
+  rc |= dalloc(&b->d_desc, (size_t)mlp::kIn * n);
+  rc |= dalloc(&b->d_fine, (size_t)mlp::kFineAll * n);
+  rc |= dalloc(&b->d_err, 1);
   if (rc) {
     plum_batch_destroy(b);
     return PLUM_ERR_CUDA;
+  }
+  cudaMemset(b->d_err, 0, sizeof(int));
+  for (int r = 0; r < n; r++) {
+    hb[r].desc_acc = b->d_desc + (size_t)mlp::kIn * r;
+    hb[r].desc_fine = b->d_fine + (size_t)mlp::kFineAll * r;
   }
   cudaMallocHost(&b->h_gather, sizeof(long long) * 6 * n);
   cudaMemcpy(b->d_rp, hp.data(), sizeof(DevParams) * n, cudaMemcpyHostToDevice);
@@ -1374,7 +1517,7 @@ int plum_batch_run(plum_batch* b, int n_steps, long* accepted_out) {
     }
     int rc = batch_steps_graph(b, steps);
     if (rc) return rc;
-    b->last_kernels += 1 + 2L * steps;
+    b->last_kernels += 1 + 2L * steps + (b->sg ? 2L * steps : 0);
     done += steps;
   }
   CK(cudaEventRecord(b->ev1, b->s));
@@ -1392,7 +1535,54 @@ int plum_batch_run(plum_batch* b, int n_steps, long* accepted_out) {
     acc1 += g[3];
     b->reps[r]->h_pos_valid = false;
   }
+  if (b->sg) {
+    int e = 0;
+    CK(cudaMemcpy(&e, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) return fail(PLUM_ERR_TIMEOUT, "tensor-core wait timed out in the surrogate stage");
+  }
   if (accepted_out) *accepted_out = (long)(acc1 - acc0);
+  return PLUM_OK;
+}
+
+int plum_batch_set_surrogate(plum_batch* b, const plum_surrogate* sg) {
+  if (!b) return fail(PLUM_ERR_INPUT, "null batch");
+  if (sg && sg->device != b->device)
+    return fail(PLUM_ERR_INPUT, "the surrogate lives on another device");
+  cudaSetDevice(b->device);
+  if (sg) CK(cudaStreamSynchronize(sg->s));
+  for (plum_ctx* c : b->reps) {
+    DevState st;
+    int rc = read_state(c, &st);
+    if (rc) return rc;
+    st.da_on = sg ? 1 : 0;
+    st.da_active = 0;
+    st.da_skip = 0;
+    st.da_n_moves = st.da_n_pass = st.da_n_accept = 0;
+    CK(cudaMemcpy(c->B.state, &st, sizeof(DevState), cudaMemcpyHostToDevice));
+  }
+  b->sg = sg;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->g_steps = 0;
+  b->g_warm = false;
+  return PLUM_OK;
+}
+
+int plum_batch_da_stats(plum_batch* b, long* out3) {
+  if (!b || !out3) return fail(PLUM_ERR_INPUT, "null argument");
+  cudaSetDevice(b->device);
+  out3[0] = out3[1] = out3[2] = 0;
+  int e = 0;
+  CK(cudaMemcpy(&e, b->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) return fail(PLUM_ERR_TIMEOUT, "tensor-core wait timed out in the surrogate stage");
+  for (plum_ctx* c : b->reps) {
+    DevState st;
+    int rc = read_state(c, &st);
+    if (rc) return rc;
+    out3[0] += st.da_n_moves;
+    out3[1] += st.da_n_pass;
+    out3[2] += st.da_n_accept;
+  }
   return PLUM_OK;
 }
 

@@ -28,6 +28,7 @@ namespace plum {
 constexpr int kMaxTypes = 8;
 constexpr int kMaxT2 = kMaxTypes * kMaxTypes;
 constexpr double kVeryLarge = 1e8;   // utilities/constants.h:15
+constexpr double kRhoZRes = 0.02;    // density_z_res (simulation.cc:113)
 constexpr double kPiRef = 3.14159265359;  // utilities/constants.h:20
 constexpr double kMtMax = 4294967295.0;   // std::mt19937::max()
 
@@ -102,6 +103,15 @@ struct DevState {
   // k tiles: dsk[sk_buf] is pending while sk_pending; the delta kernel writes
   // the new dS(k) into dsk[cur_buf]
   int sk_pending, sk_buf, cur_buf;
+  // delayed acceptance (surrogate stage one before the exact energy change):
+  // da_on enables it for chain moves; da_active marks the pending move as a
+  // surrogate move, da_u1 is its stage-one draw, da_s the surrogate energy
+  // change, da_skip the stage-one rejection (the exact change is not
+  // computed). Counters: surrogate moves, stage-one passes, accepts.
+  int da_on, da_active, da_skip, da_n_moves, da_n_pass, da_n_accept;
+  double da_u1, da_s;
+  // training log of (descriptor, exact dE) for surrogate moves (log_desc set)
+  int log_n, log_cap;
 };
 
 struct DevBuffers {  // all pointers: copied word-wise into shared memory by the batch kernels
@@ -132,6 +142,12 @@ struct DevBuffers {  // all pointers: copied word-wise into shared memory by the
   int* log_type;
   int* log_accept;
   double* log_etot;
+  // surrogate: descriptor of the pending move [96] (integer units of
+  // 2^-12), its fine distance histogram, and the optional training log
+  unsigned* desc_acc;
+  unsigned* desc_fine;  // [4][240] pair counts per 1/32-sigma distance bin
+  float* log_desc;   // [log_cap][96]
+  double* log_de;    // [log_cap]
 };
 
 // Launch helpers (kern_energy.cu / kern_moves.cu). All enqueue on `s`.
@@ -152,8 +168,10 @@ constexpr int kModeGen = 4;      // generate the next move from the stream
 constexpr int kModeCommit = 8;   // commit/reject by state->last_accept (host decided)
 void launch_serial64(const DevParams& P, const DevBuffers& B, int mode, cudaStream_t s);
 void launch_set_move(const DevBuffers& B, int mol, int b_lo, int b_hi, cudaStream_t s);
-void launch_observables64(const DevParams& P, const DevBuffers& B, double* out5,
-                          cudaStream_t s);
+void launch_observables64(const DevParams& P, const DevBuffers& B, double* per_mol,
+                          double* out5, cudaStream_t s);
+void launch_rhoz(const DevParams& P, const DevBuffers& B, double res, int n_bins, unsigned* cnt,
+                 cudaStream_t s);
 // precision form (kern_fp32.cu)
 int pair_grid32();
 void launch_delta_pairs32(const DevParams& P, const DevBuffers& B, cudaStream_t s);

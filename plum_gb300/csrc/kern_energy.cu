@@ -20,6 +20,7 @@
 // built by complex recursion from one sincos per bead and axis, with theta_a
 // = 2 kPi w_a / L_a on coordinates wrapped into the primary cell (periodic
 // axes). This replaces the reference's cos(k.r) per pair and k.
+#include <algorithm>
 #include <cstdio>
 
 #include "engine.h"
@@ -535,17 +536,36 @@ __global__ void k_obs_sum(int n_mol, int n_chains, const double* per_mol, double
   for (int q = 0; q < 5; q++) out5[q] = n_chains > 0 ? s[q] / n_chains : s[q];
 }
 
-void launch_observables64(const DevParams& P, const DevBuffers& B, double* out5,
-                          cudaStream_t s) {
-  static double* per = nullptr;
-  static int cap = 0;
-  if (P.n_mol > cap) {
-    if (per) cudaFree(per);
-    cudaMalloc(&per, sizeof(double) * 5 * P.n_mol);
-    cap = P.n_mol;
+void launch_observables64(const DevParams& P, const DevBuffers& B, double* per_mol,
+                          double* out5, cudaStream_t s) {
+  k_obs_chain<<<P.n_mol, 256, 0, s>>>(P, B, per_mol);
+  k_obs_sum<<<1, 32, 0, s>>>(P.n_mol, P.n_chain_total, per_mol, out5);
+}
+
+// rho(z) counts of one configuration (Simulation::CalcRhoZ,
+// simulation.cc:1029-1045): molecules from `phantom` on, category 0 for
+// chains, 1 for ions with q >= 0, 2 for q < 0; z wrapped into [0, Lz) by
+// floor; bin floor(z / res) kept when inside [0, n_bins). Integer counts
+// (order-independent); the host scales them by 1 / (Lx Ly res).
+__global__ void k_rhoz(const DevParams P, const DevBuffers B, double res, int n_bins,
+                       unsigned* cnt) {
+  for (int m = P.phantom + blockIdx.x; m < P.n_mol; m += gridDim.x) {
+    const int b0 = B.mol_start[m], n = B.mol_start[m + 1] - b0;
+    const int id = n > 1 ? 0 : (B.pos[b0].w >= 0.0 ? 1 : 2);
+    for (int j = b0 + threadIdx.x; j < b0 + n; j += blockDim.x) {
+      double z = B.pos[j].z;
+      z -= P.box[2] * floor(z / P.box[2]);
+      const int bz = (int)floor(z / res);
+      if (bz >= 0 && bz < n_bins) atomicAdd(&cnt[3 * bz + id], 1u);
+    }
   }
-  k_obs_chain<<<P.n_mol, 256, 0, s>>>(P, B, per);
-  k_obs_sum<<<1, 32, 0, s>>>(P.n_mol, P.n_chain_total, per, out5);
+}
+
+void launch_rhoz(const DevParams& P, const DevBuffers& B, double res, int n_bins, unsigned* cnt,
+                 cudaStream_t s) {
+  cudaMemsetAsync(cnt, 0, sizeof(unsigned) * 3 * (size_t)n_bins, s);
+  const int m = P.n_mol - P.phantom;
+  if (m > 0) k_rhoz<<<std::min(m, 4 * 152), 128, 0, s>>>(P, B, res, n_bins, cnt);
 }
 
 

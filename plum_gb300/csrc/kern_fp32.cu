@@ -340,7 +340,8 @@ __global__ void __launch_bounds__(kPairThreads)
   // 1. item counts per replica and their prefix (same in every block)
   for (int r = threadIdx.x; r < n_rep; r += blockDim.x) {
     const DevState* st = rb[r].state;
-    const int m = st->pending ? st->b_hi - st->b_lo : 0;
+    // a move rejected by the surrogate's stage one has no exact change
+    const int m = (st->pending && !st->da_skip) ? st->b_hi - st->b_lo : 0;
     const DevParams& pr = rp[r];
     const long long pairs = (long long)m * pr.n_bead;
     const int np = (pr.use_pair || pr.use_ewald) ? (int)((pairs + kItemPairs - 1) / kItemPairs) : 0;

@@ -1,0 +1,765 @@
+// Surrogate network kernels on the 5th-generation tensor cores (tcgen05):
+// BF16 operands staged in shared memory, FP32 accumulators in tensor memory,
+// one elected thread issuing the MMAs, an mbarrier signalled by
+// tcgen05.commit, and tcgen05.ld for the epilogues. One CTA of 128 threads
+// owns a tile of 128 rows (64 samples as given, then the same 64 with the
+// before/after channels swapped), so the antisymmetric output
+// s = y_scale (f(x) - f(swap x)) and its gradient stay inside the CTA.
+//
+//   k_mlp<false>  forward: s per sample; with DaArgs, the delayed-acceptance
+//                 stage one of each replica's pending move
+//   k_mlp<true>   forward + backward of the mean squared error against the
+//                 targets; per-tile gradients of every parameter
+//   k_mlp_reduce  per-tile gradients summed in tile order (deterministic)
+//   k_mlp_adam    Adam on the fp32 master parameters, bf16 copies refreshed
+//   k_desc        descriptor of pending moves (integer Gaussian-bin sums)
+//
+// Shared-memory operands use the no-swizzle K-major layout: 8x8 core
+// matrices of 128 contiguous bytes, core (row/8, k/8) at
+// (row/8) * K*16 + (k/8) * 128 bytes, so a descriptor has leading-dimension
+// offset 128 B (next core along K) and stride offset K*16 B (next 8 rows),
+// and the k-th 16-wide slice starts 256*k bytes further.
+//
+// Tensor memory (512 columns while training, 256 for inference), lane = row:
+//   [0,128) z1 = W1 x'        later dW1 (96 columns)
+//   [128,256) z2 = W2 h1
+//   [256,384) dh1 = dz2 W2    [384,512) dW2 = dz2^T h1
+// Every wait on the mbarrier gives up after one second; the kernel then
+// records an error, issues no further MMA and still frees its tensor memory.
+#include <cstdio>
+#include <type_traits>
+
+#include "mlp.h"
+
+namespace plum {
+
+using namespace mlp;
+
+namespace {
+
+__host__ __device__ constexpr uint32_t op_off(int row, int k, int K) {
+  return (uint32_t)((row >> 3) * (K * 16) + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// tcgen05 instruction descriptor, kind::f16: D f32, A and B bf16, both
+// K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// shared-memory matrix descriptor (no swizzle, K-major, version 1)
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, int K) {
+  const uint32_t lbo = 128, sbo = (uint32_t)K * 16;
+  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+// D[128 x N] (+)= A[128 x K] B[N x K]^T, operands at shared addresses a, b
+__device__ __forceinline__ void mma_tile(uint32_t d, uint32_t a, uint32_t b, int K,
+                                         uint32_t idesc) {
+  for (int k = 0; k < K / 16; k++)
+    mma_bf16(d, sdesc(a + 256u * k, K), sdesc(b + 256u * k, K), idesc, k > 0 ? 1u : 0u);
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void proxy_fence() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ uint64_t gtime() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(mbar), "r"(phase)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait: false after one second
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+  const uint64_t t0 = gtime();
+  while (!mbar_try(mbar, phase))
+    if (gtime() - t0 > 1000000000ull) return false;
+  return true;
+}
+
+// 32 consecutive fp32 columns of this thread's lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, "
+      "[%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + expf(-z)); }
+
+__device__ __forceinline__ void st_bf16x8(unsigned char* p, const float* v) {
+  __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+  for (int e = 0; e < 8; e++) h[e] = __float2bfloat16_rn(v[e]);
+  *reinterpret_cast<uint4*>(p) = *reinterpret_cast<const uint4*>(h);
+}
+
+__device__ __forceinline__ void st_bf16(unsigned char* p, float v) {
+  *reinterpret_cast<__nv_bfloat16*>(p) = __float2bfloat16_rn(v);
+}
+
+// shared-memory map (bytes)
+constexpr uint32_t kW1 = 0;            // B [128][96]
+constexpr uint32_t kX = 24576;         // A [128][96]; W1+X later dZ2^T A [128][128]
+constexpr uint32_t kW2 = 49152;        // B [128][128]; later dZ1^T A [128][128]
+constexpr uint32_t kH1 = 81920;        // A [128][128]; later dZ2 A [128][128]
+// training only
+constexpr uint32_t kW2T = 114688;      // B [128 a][128 b]
+constexpr uint32_t kXT = 147456;       // B [96 c][128 i]
+constexpr uint32_t kH1T = 172032;      // B [128 a][128 i]
+constexpr uint32_t kRed = 204800;      // f32 [128][33]
+constexpr uint32_t kMiscT = 221696;
+constexpr uint32_t kMiscI = 114688;
+// misc block: y[128], dy[128], tmp[128], db1[128], db2[128], dw3[128] (f32),
+// mbarrier, tensor-memory address, flag
+constexpr uint32_t kMiscBytes = 6 * 512 + 16;
+constexpr uint32_t kSmemTrain = kMiscT + kMiscBytes;
+constexpr uint32_t kSmemInfer = kMiscI + kMiscBytes;
+static_assert(kSmemTrain <= 232448, "shared memory per CTA");
+static_assert(kW1 + 49152 >= 32768 && kX == kW1 + 24576, "dZ2^T fits over W1 and X");
+
+// column sums over the 128 rows of red[row][33] (first 32 columns), in a
+// fixed order; result in out[0..31]
+__device__ __forceinline__ void col_sum32(const float* red, float* tmp, float* out) {
+  const int t = threadIdx.x, c = t & 31, q = t >> 5;
+  __syncthreads();
+  float s = 0.0f;
+  for (int r = q * 32; r < q * 32 + 32; r++) s += red[r * 33 + c];
+  tmp[q * 32 + c] = s;
+  __syncthreads();
+  if (t < 32) out[t] = ((tmp[t] + tmp[32 + t]) + tmp[64 + t]) + tmp[96 + t];
+  __syncthreads();
+}
+
+template <bool kTrain, typename TIn>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_mlp(const MlpNet* __restrict__ net, const TIn* __restrict__ x, float xscale, int n,
+          const float* __restrict__ tgt, float* __restrict__ s_out, float* __restrict__ part,
+          float inv_n, DaArgs da, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int t = threadIdx.x, warp = t >> 5;
+  const uint32_t misc = kTrain ? kMiscT : kMiscI;
+  float* ys = reinterpret_cast<float*>(sm + misc);
+  float* dys = ys + 128;
+  float* tmp = ys + 256;
+  float* db1s = ys + 384;
+  float* db2s = ys + 512;
+  float* dw3s = ys + 640;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + misc + 3072);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + misc + 3080);
+  int* sflag = reinterpret_cast<int*>(sm + misc + 3084);
+  const uint32_t base = smem_u32(sm);
+  const uint32_t mb = smem_u32(mbar);
+  constexpr uint32_t kCols = kTrain ? 512u : 256u;
+
+  if (warp == 0) {
+    asm volatile(
+        "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n\t"
+        "tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::"r"(smem_u32(tslot)),
+        "r"(kCols)
+        : "memory");
+  }
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *sflag = 0;
+  }
+
+  // ---- operands: weights and the input tile
+  const __nv_bfloat16* w1 = net->w1;
+  const __nv_bfloat16* w2 = net->w2;
+#pragma unroll 4
+  for (int c = t; c < kHid * (kIn / 8); c += kThreads) {
+    const int row = c / (kIn / 8), k8 = c % (kIn / 8);
+    *reinterpret_cast<uint4*>(sm + kW1 + op_off(row, k8 * 8, kIn)) =
+        *reinterpret_cast<const uint4*>(w1 + row * kIn + k8 * 8);
+  }
+#pragma unroll 4
+  for (int c = t; c < kHid * (kHid / 8); c += kThreads) {
+    const int row = c / (kHid / 8), k8 = c % (kHid / 8);
+    *reinterpret_cast<uint4*>(sm + kW2 + op_off(row, k8 * 8, kHid)) =
+        *reinterpret_cast<const uint4*>(w2 + row * kHid + k8 * 8);
+  }
+  if (kTrain)
+    for (int e = t; e < kHid * kHid; e += kThreads) {
+      const int a = e % kHid, b = e / kHid;  // W2^T (a, b) = W2[b][a]
+      *reinterpret_cast<__nv_bfloat16*>(sm + kW2T + op_off(a, b, kHid)) = w2[b * kHid + a];
+    }
+  const int sample = blockIdx.x * kSamp + (t & (kSamp - 1));
+  const bool swapped = t >= kSamp;
+  const bool valid = sample < n;
+  // Launched as a dependent of the descriptor kernel, the weights above were
+  // staged while it ran; its results are visible after this wait (a no-op
+  // for an ordinary launch).
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  {
+    // the tile's input rows, staged with coalesced 16-byte loads (rows are
+    // 384 bytes, so every row starts 16-byte aligned) into the H1 region
+    float* xs = reinterpret_cast<float*>(sm + kH1);
+    const int s0 = blockIdx.x * kSamp;
+    constexpr int kVec = kSamp * kIn / 4;
+#pragma unroll 4
+    for (int e = t; e < kVec; e += kThreads) {
+      const int row = e / (kIn / 4);
+      float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (s0 + row < n) {
+        const uint4 raw = reinterpret_cast<const uint4*>(x + (size_t)s0 * kIn)[e];
+        if constexpr (std::is_same<TIn, float>::value) {
+          v = make_float4(__uint_as_float(raw.x), __uint_as_float(raw.y), __uint_as_float(raw.z),
+                          __uint_as_float(raw.w));
+        } else {  // unsigned integer descriptor sums
+          v = make_float4((float)raw.x, (float)raw.y, (float)raw.z, (float)raw.w);
+        }
+      }
+      reinterpret_cast<float4*>(xs)[e] = make_float4(v.x * xscale, v.y * xscale, v.z * xscale,
+                                                     v.w * xscale);
+    }
+  }
+  __syncthreads();
+  const float* xrow = reinterpret_cast<const float*>(sm + kH1) + (t & (kSamp - 1)) * kIn;
+  for (int k8 = 0; k8 < kIn / 8; k8++) {
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) {
+      const int f = k8 * 8 + e;
+      const int src = swapped ? (f + kIn / 2) % kIn : f;
+      v[e] = valid ? (xrow[src] - net->mu[f]) * net->isd[f] : 0.0f;
+    }
+    st_bf16x8(sm + kX + op_off(t, k8 * 8, kIn), v);
+    if (kTrain)
+#pragma unroll
+      for (int e = 0; e < 8; e++) st_bf16(sm + kXT + op_off(k8 * 8 + e, t, kHid), v[e]);
+  }
+  proxy_fence();
+  tc_before();
+  __syncthreads();
+  tc_after();
+  const uint32_t tmem = *tslot;
+  const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+  uint32_t phase = 0;
+  bool ok = true;
+  auto step = [&](bool issue) {
+    // wait for the MMAs committed by thread 0, then agree on the outcome
+    bool got = !issue || mbar_wait(mb, phase);
+    phase ^= 1u;
+    if (!got) atomicOr(sflag, 1);
+    tc_before();
+    __syncthreads();
+    tc_after();
+    ok = *sflag == 0;
+  };
+
+  // ---- layer 1: z1 = x' W1^T
+  if (t == 0) {
+    mma_tile(tmem, base + kX, base + kW1, kIn, idesc_bf16(128, 128));
+    mma_commit(mb);
+  }
+  step(true);
+  for (int q = 0; q < 4; q++) {
+    float v[32];
+    tmem_ld32(trow + 32 * q, v);
+#pragma unroll
+    for (int c = 0; c < 32; c++) {
+      const float z = v[c] + net->b1[32 * q + c];
+      v[c] = z * sigm(z);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; j++) st_bf16x8(sm + kH1 + op_off(t, 32 * q + 8 * j, kHid), v + 8 * j);
+    if (kTrain)
+#pragma unroll
+      for (int c = 0; c < 32; c++) st_bf16(sm + kH1T + op_off(32 * q + c, t, kHid), v[c]);
+  }
+  proxy_fence();
+  tc_before();
+  __syncthreads();
+  tc_after();
+
+  // ---- layer 2: z2 = h1 W2^T, then f = w3 . SiLU(z2) + b3
+  if (t == 0 && ok) {
+    mma_tile(tmem + 128, base + kH1, base + kW2, kHid, idesc_bf16(128, 128));
+    mma_commit(mb);
+  }
+  step(ok);
+  float y = net->b3;
+  for (int q = 0; q < 4; q++) {
+    float v[32];
+    tmem_ld32(trow + 128 + 32 * q, v);
+#pragma unroll
+    for (int c = 0; c < 32; c++) {
+      const float z = v[c] + net->b2[32 * q + c];
+      y += __bfloat162float(net->w3[32 * q + c]) * (z * sigm(z));
+    }
+  }
+  ys[t] = y;
+  __syncthreads();
+  float s = 0.0f;
+  if (t < kSamp) {
+    s = net->y_scale * (ys[t] - ys[t + kSamp]);
+    if (valid && s_out) s_out[sample] = s;
+    if (!kTrain && valid && da.sts) {
+      DevState* st = da.sts[sample];
+      if (st->pending && st->da_active) {
+        const double u1 = st->da_u1;
+        st->da_s = (double)s;
+        st->da_skip = !(u1 < exp(-da.rp[sample].beta * (double)s));
+      }
+    }
+  }
+
+  if (kTrain) {
+    float* red = reinterpret_cast<float*>(sm + kRed);
+    float* gp = part + (size_t)blockIdx.x * kGradStride;
+    float lossv = 0.0f;
+    if (t < kSamp) {
+      float g = 0.0f;
+      if (valid) {
+        const float d = s - tgt[sample];
+        g = 2.0f * d * net->y_scale * inv_n;
+        lossv = d * d * inv_n;
+      }
+      dys[t] = g;
+      dys[t + kSamp] = -g;
+    }
+    __syncthreads();
+    const float dyt = dys[t];
+    // loss and db3 (zero by construction: the two orientations cancel)
+    red[t * 33] = lossv;
+    red[t * 33 + 1] = dyt;
+    for (int c = 2; c < 32; c++) red[t * 33 + c] = 0.0f;
+    col_sum32(red, tmp, db1s);  // db1s is scratch here
+    if (t == 0) {
+      gp[kNParam] = db1s[0];
+      gp[kOffB3] = db1s[1];
+    }
+    __syncthreads();
+    // dz2 = dy w3 SiLU'(z2); dW3 and db2 column sums; dz2 in both layouts
+    for (int q = 0; q < 4; q++) {
+      float v[32], dz[32];
+      tmem_ld32(trow + 128 + 32 * q, v);
+#pragma unroll
+      for (int c = 0; c < 32; c++) {
+        const int b = 32 * q + c;
+        const float z = v[c] + net->b2[b];
+        const float sg = sigm(z);
+        red[t * 33 + c] = dyt * (z * sg);
+        dz[c] = dyt * __bfloat162float(net->w3[b]) * sg * (1.0f + z * (1.0f - sg));
+      }
+      col_sum32(red, tmp, dw3s + 32 * q);
+#pragma unroll
+      for (int c = 0; c < 32; c++) red[t * 33 + c] = dz[c];
+      col_sum32(red, tmp, db2s + 32 * q);
+#pragma unroll
+      for (int j = 0; j < 4; j++) st_bf16x8(sm + kH1 + op_off(t, 32 * q + 8 * j, kHid), dz + 8 * j);
+#pragma unroll
+      for (int c = 0; c < 32; c++) st_bf16(sm + kW1 + op_off(32 * q + c, t, kHid), dz[c]);
+    }
+    proxy_fence();
+    tc_before();
+    __syncthreads();
+    tc_after();
+    // dh1 = dz2 W2 (B = W2^T as [a][b]);  dW2 = dz2^T h1 (A = dz2^T, B = h1^T)
+    if (t == 0 && ok) {
+      mma_tile(tmem + 256, base + kH1, base + kW2T, kHid, idesc_bf16(128, 128));
+      mma_tile(tmem + 384, base + kW1, base + kH1T, kHid, idesc_bf16(128, 128));
+      mma_commit(mb);
+    }
+    step(ok);
+    for (int q = 0; q < 4; q++) {
+      float dh[32], z1[32];
+      tmem_ld32(trow + 256 + 32 * q, dh);
+      tmem_ld32(trow + 32 * q, z1);
+#pragma unroll
+      for (int c = 0; c < 32; c++) {
+        const float z = z1[c] + net->b1[32 * q + c];
+        const float sg = sigm(z);
+        dh[c] = dh[c] * sg * (1.0f + z * (1.0f - sg));
+        red[t * 33 + c] = dh[c];
+      }
+      col_sum32(red, tmp, db1s + 32 * q);
+#pragma unroll
+      for (int c = 0; c < 32; c++) st_bf16(sm + kW2 + op_off(32 * q + c, t, kHid), dh[c]);
+    }
+    for (int q = 0; q < 4; q++) {
+      float v[32];
+      tmem_ld32(trow + 384 + 32 * q, v);
+#pragma unroll
+      for (int c = 0; c < 32; c++) gp[kOffW2 + t * kHid + 32 * q + c] = v[c];
+    }
+    proxy_fence();
+    tc_before();
+    __syncthreads();
+    tc_after();
+    // dW1 = dz1^T x' (A = dz1^T [a][i], B = x'^T [c][i])
+    if (t == 0 && ok) {
+      mma_tile(tmem, base + kW2, base + kXT, kHid, idesc_bf16(128, 96));
+      mma_commit(mb);
+    }
+    step(ok);
+    for (int q = 0; q < 3; q++) {
+      float v[32];
+      tmem_ld32(trow + 32 * q, v);
+#pragma unroll
+      for (int c = 0; c < 32; c++) gp[kOffW1 + t * kIn + 32 * q + c] = v[c];
+    }
+    gp[kOffB1 + t] = db1s[t];
+    gp[kOffB2 + t] = db2s[t];
+    gp[kOffW3 + t] = dw3s[t];
+  }
+
+  tc_before();
+  __syncthreads();
+  if (t == 0 && !ok && err) atomicExch(err, 1);
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols)
+                 : "memory");
+}
+
+__global__ void k_mlp_reduce(const float* __restrict__ part, int tiles, float* __restrict__ grad) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > kNParam) return;
+  float s = 0.0f;
+  for (int i = 0; i < tiles; i++) s += part[(size_t)i * kGradStride + p];
+  grad[p] = s;
+}
+
+__device__ __forceinline__ void put_param(MlpNet* net, int p, float w) {
+  if (p < kOffB1) net->w1[p] = __float2bfloat16_rn(w);
+  else if (p < kOffW2) net->b1[p - kOffB1] = w;
+  else if (p < kOffB2) net->w2[p - kOffW2] = __float2bfloat16_rn(w);
+  else if (p < kOffW3) net->b2[p - kOffB2] = w;
+  else if (p < kOffB3) net->w3[p - kOffW3] = __float2bfloat16_rn(w);
+  else net->b3 = w;
+}
+
+__global__ void k_mlp_adam(float* __restrict__ param, float* __restrict__ m, float* __restrict__ v,
+                           const float* __restrict__ g, float lr, float c1, float c2,
+                           MlpNet* __restrict__ net) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= kNParam) return;
+  const float gi = g[p];
+  const float mi = 0.9f * m[p] + 0.1f * gi;
+  const float vi = 0.999f * v[p] + 0.001f * gi * gi;
+  m[p] = mi;
+  v[p] = vi;
+  const float w = param[p] - lr * (mi * c1) / (sqrtf(vi * c2) + 1e-8f);
+  param[p] = w;
+  put_param(net, p, w);
+}
+
+__global__ void k_mlp_pack(const float* __restrict__ param, MlpNet* __restrict__ net) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < kNParam) put_param(net, p, param[p]);
+}
+
+// ------------------------------------------------------------ descriptor
+// k_desc counts pairs in fine distance bins. Work items are (replica, tile of
+// up to 32 moved beads, chunk of 1024 other beads): the tile's current and
+// trial positions sit in shared memory and each thread holds 4 other beads,
+// so each load serves 32 pairs; a pair within the cut adds one to the
+// block's count of its (channel, fine bin) in shared memory, and the block's
+// counts go to the replica's desc_fine at the end of the item. k_desc_fin
+// then smears the counts into the 96 descriptor bins with integer weights.
+// Integer counts and sums make both independent of the order.
+constexpr int kDescThreads = 256;
+constexpr int kDescTile = 32;                   // moved beads per item
+constexpr int kDescPer = 4;                     // other beads per thread
+constexpr int kDescChunk = kDescThreads * kDescPer;
+
+// FP64 positions: one FP64 subtraction per axis, the periodic wrap in FP32
+// (the descriptor only uses pairs within 7.5 sigma, far from the half-box
+// distance where the two roundings could pick different images)
+__device__ __forceinline__ float wrap32(double d, float L, float invL, bool periodic) {
+  const float f = (float)d;
+  return periodic ? f - L * rintf(f * invL) : f;
+}
+
+// A bead position as the descriptor kernel keeps it: form 1 the fixed-point
+// mirror (x, y, z, type), form 0 FP64 (x, y, z) and the type.
+struct DPos {
+  int4 f;
+  double x, y, z;
+};
+
+template <int kForm>
+__device__ __forceinline__ DPos load_pos(const DevBuffers& B, int i, int ii, bool trial) {
+  DPos p;
+  if (kForm == 1) {
+    p.f = trial ? B.ftrial[ii] : B.fpos[i];
+    p.x = p.y = p.z = 0.0;
+  } else {
+    const double4_32a q = trial ? B.trial[i] : B.pos[i];
+    p.x = q.x;
+    p.y = q.y;
+    p.z = q.z;
+    p.f = make_int4(0, 0, 0, B.type[i]);
+  }
+  return p;
+}
+
+template <int kForm>
+__device__ __forceinline__ float dist2(const DevParams& P, const DPos& a, const DPos& b) {
+  float dx, dy, dz;
+  if (kForm == 1) {
+    dx = (float)(int)((unsigned)b.f.x - (unsigned)a.f.x) * P.f_scale[0];
+    dy = (float)(int)((unsigned)b.f.y - (unsigned)a.f.y) * P.f_scale[1];
+    dz = (float)(int)((unsigned)b.f.z - (unsigned)a.f.z) * P.f_scale[2];
+  } else {
+    dx = wrap32(b.x - a.x, (float)P.box[0], (float)P.inv_box[0], P.npbc > 0);
+    dy = wrap32(b.y - a.y, (float)P.box[1], (float)P.inv_box[1], P.npbc > 1);
+    dz = wrap32(b.z - a.z, (float)P.box[2], (float)P.inv_box[2], P.npbc > 2);
+  }
+  return dx * dx + dy * dy + dz * dz;
+}
+
+template <int kForm>
+__global__ void __launch_bounds__(kDescThreads)
+    k_desc(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb, int n_rep) {
+  __shared__ unsigned fh[kFineAll];
+  __shared__ DPos tile[2][kDescTile];  // [current | trial] of the moved beads
+  __shared__ int s_pref[kMaxReplicas + 1];
+  __shared__ int s_nc[kMaxReplicas];   // other-bead chunks per replica
+  __shared__ DevParams P;
+  __shared__ DevBuffers B;
+  __shared__ int s_bl[2];
+  for (int r = threadIdx.x; r < n_rep; r += blockDim.x) {
+    const DevState* st = rb[r].state;
+    const int m = (st->pending && st->da_active) ? st->b_hi - st->b_lo : 0;
+    const int nc = (rp[r].n_bead + kDescChunk - 1) / kDescChunk;
+    s_nc[r] = nc;
+    s_pref[r + 1] = ((m + kDescTile - 1) / kDescTile) * nc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    s_pref[0] = 0;
+    for (int r = 0; r < n_rep; r++) s_pref[r + 1] += s_pref[r];
+  }
+  __syncthreads();
+  const int T = s_pref[n_rep];
+  const int it0 = (int)((long long)T * blockIdx.x / gridDim.x);
+  const int it1 = (int)((long long)T * (blockIdx.x + 1) / gridDim.x);
+  int cur = -1;
+  for (int item = it0; item < it1; item++) {
+    int lo = 0, hi = n_rep - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (s_pref[mid] <= item) lo = mid; else hi = mid - 1;
+    }
+    const int r = lo;
+    __syncthreads();
+    if (r != cur) {
+      const int* src = reinterpret_cast<const int*>(rp + r);
+      int* dst = reinterpret_cast<int*>(&P);
+      for (int i = threadIdx.x; i < (int)(sizeof(DevParams) / sizeof(int)); i += blockDim.x)
+        dst[i] = src[i];
+      const long long* bs = reinterpret_cast<const long long*>(rb + r);
+      long long* bd = reinterpret_cast<long long*>(&B);
+      for (int i = threadIdx.x; i < (int)(sizeof(DevBuffers) / sizeof(long long)); i += blockDim.x)
+        bd[i] = bs[i];
+      if (threadIdx.x == 0) {
+        s_bl[0] = rb[r].state->b_lo;
+        s_bl[1] = rb[r].state->b_hi;
+      }
+    }
+    for (int k = threadIdx.x; k < kFineAll; k += blockDim.x) fh[k] = 0u;
+    __syncthreads();
+    cur = r;
+    const int b_lo = s_bl[0], b_hi = s_bl[1], N = P.n_bead;
+    const int local = item - s_pref[r], nc = s_nc[r];
+    const int t0 = b_lo + (local / nc) * kDescTile;
+    const int nt = min(kDescTile, b_hi - t0);
+    const int j0 = (local % nc) * kDescChunk;
+    for (int k = threadIdx.x; k < 2 * kDescTile; k += blockDim.x) {
+      const int w = k / kDescTile, q = k % kDescTile;
+      if (q < nt) tile[w][q] = load_pos<kForm>(B, t0 + q, t0 + q - b_lo, w == 1);
+    }
+    // this thread's other beads (current and, when moved, trial positions)
+    DPos jc[kDescPer], jt[kDescPer];
+    int jidx[kDescPer];
+#pragma unroll
+    for (int u = 0; u < kDescPer; u++) {
+      const int j = j0 + threadIdx.x + u * kDescThreads;
+      jidx[u] = j < N ? j : -1;
+      const int js = j < N ? j : 0;
+      const bool jm = js >= b_lo && js < b_hi;
+      jc[u] = load_pos<kForm>(B, js, 0, false);
+      jt[u] = jm ? load_pos<kForm>(B, js, js - b_lo, true) : jc[u];
+    }
+    __syncthreads();
+    for (int q = 0; q < nt; q++) {
+      const int i = t0 + q;
+      const DPos ic = tile[0][q], it = tile[1][q];
+#pragma unroll
+      for (int u = 0; u < kDescPer; u++) {
+        const int j = jidx[u];
+        const bool jm = j >= b_lo && j < b_hi;
+        if (j < 0 || j == i || (jm && j < i)) continue;
+        const int cls = ic.f.w == jc[u].f.w ? 0 : 1;
+        const float r0 = dist2<kForm>(P, ic, jc[u]);
+        const float r1 = dist2<kForm>(P, it, jt[u]);
+        if (r0 < kDescCut * kDescCut)
+          atomicAdd(&fh[cls * kFine + (int)(sqrtf(r0) * (float)kFinePerSigma + 0.5f)], 1u);
+        if (r1 < kDescCut * kDescCut)
+          atomicAdd(&fh[(2 + cls) * kFine + (int)(sqrtf(r1) * (float)kFinePerSigma + 0.5f)], 1u);
+      }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kFineAll; k += blockDim.x)
+      if (fh[k]) atomicAdd(&B.desc_fine[k], fh[k]);
+  }
+}
+
+// One block per replica: bin k of channel c = sum_f count[c][f] *
+// round(4096 exp(-(r_f - c_k)^2 / (2 w^2))) over the fine bins within
+// 1.2 sigma (where the weight rounds to zero beyond).
+__global__ void __launch_bounds__(128) k_desc_fin(const DevBuffers* __restrict__ rb) {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  const DevBuffers& B = rb[blockIdx.x];
+  const DevState* st = B.state;
+  if (!(st->pending && st->da_active)) return;
+  const int k = threadIdx.x;
+  if (k >= kIn) return;
+  const int ch = k / kBins, kb = k % kBins;
+  const float c = (kb + 0.5f) * kBinW;
+  const int f0 = max(0, (int)((c - 1.2f) * kFinePerSigma));
+  const int f1 = min(kFine - 1, (int)((c + 1.2f) * kFinePerSigma) + 1);
+  unsigned v = 0u;
+  for (int f = f0; f <= f1; f++) {
+    const unsigned n = B.desc_fine[ch * kFine + f];
+    if (!n) continue;
+    const float d = f * (1.0f / kFinePerSigma) - c;
+    v += n * __float2uint_rn(4096.0f * expf(-0.5f / (kBinW * kBinW) * d * d));
+  }
+  B.desc_acc[k] = v;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ launches
+static void smem_attr(const void* f, int bytes) {
+  cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+void launch_mlp_infer_f(const MlpNet* net, const float* x, int n, float* s_out, int* err,
+                        cudaStream_t st) {
+  if (n <= 0) return;
+  static bool attr = false;
+  if (!attr) {
+    smem_attr((const void*)k_mlp<false, float>, kSmemInfer);
+    attr = true;
+  }
+  k_mlp<false, float><<<(n + kSamp - 1) / kSamp, kThreads, kSmemInfer, st>>>(
+      net, x, 1.0f, n, nullptr, s_out, nullptr, 0.0f, DaArgs{nullptr, nullptr}, err);
+}
+
+void launch_mlp_infer_i(const MlpNet* net, const unsigned* x, int n, float* s_out, DaArgs da,
+                        int* err, cudaStream_t st) {
+  if (n <= 0) return;
+  static bool attr = false;
+  if (!attr) {
+    smem_attr((const void*)k_mlp<false, unsigned>, kSmemInfer);
+    attr = true;
+  }
+  // programmatic dependent launch: may start while the preceding kernel on
+  // the stream (the descriptor kernel) still runs
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((n + kSamp - 1) / kSamp);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = kSmemInfer;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_mlp<false, unsigned>, net, x, kDescUnit, n, (const float*)nullptr,
+                     s_out, (float*)nullptr, 0.0f, da, err);
+}
+
+void launch_mlp_grad(const MlpNet* net, const float* x, const float* t, int n, float* part,
+                     float* grad, int* err, cudaStream_t st) {
+  if (n <= 0) return;
+  static bool attr = false;
+  if (!attr) {
+    smem_attr((const void*)k_mlp<true, float>, kSmemTrain);
+    attr = true;
+  }
+  const int tiles = (n + kSamp - 1) / kSamp;
+  k_mlp<true, float><<<tiles, kThreads, kSmemTrain, st>>>(net, x, 1.0f, n, t, nullptr, part,
+                                                          1.0f / n, DaArgs{nullptr, nullptr}, err);
+  k_mlp_reduce<<<(kNParam + 1 + 255) / 256, 256, 0, st>>>(part, tiles, grad);
+}
+
+void launch_mlp_adam(float* param, float* m, float* v, const float* grad, int step, float lr,
+                     MlpNet* net, cudaStream_t st) {
+  const float c1 = 1.0f / (1.0f - powf(0.9f, (float)step));
+  const float c2 = 1.0f / (1.0f - powf(0.999f, (float)step));
+  k_mlp_adam<<<(kNParam + 255) / 256, 256, 0, st>>>(param, m, v, grad, lr, c1, c2, net);
+}
+
+void launch_mlp_pack(const float* param, MlpNet* net, cudaStream_t st) {
+  k_mlp_pack<<<(kNParam + 255) / 256, 256, 0, st>>>(param, net);
+}
+
+void launch_desc_batch(const DevParams* rp, const DevBuffers* rb, int n_rep, unsigned* acc,
+                       int form, cudaStream_t st) {
+  (void)acc;
+  if (form) k_desc<1><<<2 * 152, kDescThreads, 0, st>>>(rp, rb, n_rep);
+  else k_desc<0><<<2 * 152, kDescThreads, 0, st>>>(rp, rb, n_rep);
+  k_desc_fin<<<n_rep, 128, 0, st>>>(rb);
+}
+
+}  // namespace plum

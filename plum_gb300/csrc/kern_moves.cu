@@ -19,6 +19,7 @@
 // tests (randSphere's r1^2 + r2^2 > 1, the move-type and pick thresholds)
 // must round exactly like the reference or the draw sequence would diverge.
 #include "engine.h"
+#include "mlp.h"
 #include "device_common.cuh"
 
 namespace plum {
@@ -315,6 +316,9 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
         }
       }
     }
+    // Delayed acceptance: a chain move (pivot, crankshaft, reptation) takes
+    // its stage-one draw right after its own draws.
+    if (plan.type >= 2 && st->da_on && B.desc_acc && B.desc_fine) st->da_u1 = d.u();
     if (d.overrun) {
       st->error = PLUM_ERR_STREAM_DEV;
       plan.type = -1;
@@ -405,7 +409,13 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
     for (int i = g.b_lo + threadIdx.x; i < g.b_hi; i += blockDim.x)
       B.ftrial[i - g.b_lo] = fix_point(P, B.trial[i], B.type[i]);
   }
+  // surrogate move: its descriptor is accumulated from zero by the next launch
+  const bool surr = g.type >= 2 && B.desc_acc && B.desc_fine && (st->da_on || B.log_desc);
+  if (surr)
+    for (int k = threadIdx.x; k < mlp::kFineAll; k += blockDim.x) B.desc_fine[k] = 0u;
   if (threadIdx.x == 0) {
+    st->da_active = surr ? 1 : 0;
+    st->da_skip = 0;
     if (g.type >= 0) {
       st->pending = 1;
       st->mol = g.mol;
@@ -504,7 +514,26 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
   const int pending = S.pending;
   const int b_lo = S.b_lo, b_hi = S.b_hi, mol = S.mol;
 
-  if ((mode & kModeFinish) && pending) {
+  if ((mode & kModeFinish) && pending && S.da_skip) {
+    // Stage one rejected the move: no exact change was computed, and no
+    // delta kernel applied the S(k) change of the last accepted move.
+    if (P.use_ewald && S.sk_pending) {
+      const double2* add = B.dsk + (size_t)S.sk_buf * P.n_k;
+      for (int k = threadIdx.x; k < P.n_k; k += blockDim.x) {
+        const double2 a = add[k];
+        double2 v = B.sk[k];
+        v.x += a.x;
+        v.y += a.y;
+        B.sk[k] = v;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      S.sk_pending = 0;
+      S.de = 0.0;
+    }
+    __syncthreads();
+  } else if ((mode & kModeFinish) && pending) {
     // walls of the moved beads, sum q dz
     if (threadIdx.x == 0) s_ext_bad = 0;
     __syncthreads();
@@ -572,6 +601,17 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
       S.dmz = dmz;
     }
     __syncthreads();
+    // training log: (descriptor, exact dE) of a surrogate move
+    if (S.da_active && B.log_desc && S.log_n < S.log_cap) {
+      const long long row = S.log_n;  // rows of mlp::kIn values
+      for (int k = threadIdx.x; k < mlp::kIn; k += blockDim.x)
+        B.log_desc[row * mlp::kIn + k] = (float)B.desc_acc[k] * mlp::kDescUnit;
+      if (threadIdx.x == 0) {
+        B.log_de[row] = S.de;
+        S.log_n++;
+      }
+      __syncthreads();
+    }
   }
 
   // Metropolis (simulation.cc:324-332) or the host's decision.
@@ -579,7 +619,19 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
     if (threadIdx.x == 0) {
       int acc = 0;
       if (mode & kModeDecide) {
-        if (!(S.de >= kVeryLarge)) acc = d.u() < exp(-P.beta * S.de);  // a NaN dE still draws
+        if (S.da_active && S.da_on) {
+          // Delayed acceptance, stage two: with the stage-one probability
+          // min(1, exp(-beta s)) and s antisymmetric under reversing the
+          // move, min(1, exp(-beta (dE - s))) gives the same ratio
+          // exp(-beta dE) of forward to reverse acceptance as Metropolis.
+          if (!S.da_skip && !(S.de >= kVeryLarge))
+            acc = d.u() < exp(-P.beta * (S.de - S.da_s));
+          S.da_n_moves++;
+          S.da_n_pass += S.da_skip ? 0 : 1;
+          S.da_n_accept += acc;
+        } else if (!(S.de >= kVeryLarge)) {
+          acc = d.u() < exp(-P.beta * S.de);  // a NaN dE still draws
+        }
         if (d.overrun) S.error = PLUM_ERR_STREAM_DEV;
       } else {
         acc = S.last_accept;

@@ -16,7 +16,9 @@ input_crd.dat, input_top.dat) and ref.npz with, from the reference:
   rng_words     the reference generator's first outputs for run_seed
 
 Run from the repository root:  python tests/golden/make_golden.py
-(needs the reference checkout; the fixtures themselves are committed).
+[moves] [cbmc] [long | long:<case>] (needs the reference checkout; the
+fixtures themselves are committed). "long" adds long.npz, a 1e5-step run,
+to the cases in LONG_CASES (about 40 min each at the reference's speed).
 """
 from __future__ import annotations
 
@@ -117,6 +119,51 @@ def make_cbmc_case(name, cfg, n_eval=24):
     print(name, "beads", int(start[-1]), "u range", out["u"].min(), out["u"].max())
 
 
+def coarse_rhoz(rz, width=50):
+    """rho(z) [n_bins, 3] at 0.02 resolution averaged over groups of `width`
+    bins (1 sigma); a ragged last group is dropped."""
+    n = (len(rz) // width) * width
+    return rz[:n].reshape(-1, width, 3).mean(axis=1)
+
+
+LONG_CASES = {"bulk_small": 2024, "slab_wca": 2025}
+
+
+def make_long_case(name, seed, steps=100000, every=100):
+    """A 1e5-step seeded run of the reference's step loop on an existing
+    case's inputs: long.npz with the move-type, accept and draw-count
+    sequences, the running total after every `every` steps, samples of the
+    observables (Rg^2 averaged over chains, end-to-end^2) and of rho(z)
+    (averaged into 1-sigma bins, coarse_rhoz) at the same points, the final
+    full-resolution rho(z) and the final coordinates. Sampling between chunks of
+    the loop reads the state only, so the sequences are those of one run."""
+    import tempfile
+    src = os.path.join(HERE, name)
+    with tempfile.TemporaryDirectory() as d:
+        for f in ("run.in", "input_crd.dat", "input_top.dat"):
+            shutil.copy(os.path.join(src, f), os.path.join(d, f))
+        R = ob.Ref(d, seed=seed)
+        mts, acs, drs, ets, obs, rz = [], [], [], [], [], []
+        for _ in range(steps // every):
+            mt, ac, dr, et = R.run(every)
+            mts.append(mt)
+            acs.append(ac)
+            drs.append(dr)
+            ets.append(et[-1])
+            obs.append(R.observables())
+            rz.append(coarse_rhoz(R.rhoz()))
+        out = {"run_seed": np.array(seed), "every": np.array(every),
+               "run_type": np.concatenate(mts).astype(np.int8),
+               "run_accept": np.concatenate(acs).astype(np.int8),
+               "run_draws": np.concatenate(drs).astype(np.uint16),
+               "run_etot_sampled": np.array(ets), "run_obs_sampled": np.array(obs),
+               "run_rhoz_coarse": np.array(rz).astype(np.float32),
+               "run_rhoz": R.rhoz(), "run_coords": R.coords()}
+        R.close()
+    np.savez_compressed(os.path.join(src, "long.npz"), **out)
+    print(name, "long run accept", out["run_accept"].mean())
+
+
 def make_case(name, cfg, n_de=24):
     d = os.path.join(HERE, name)
     if os.path.isdir(d):
@@ -183,3 +230,6 @@ if __name__ == "__main__":
     if "cbmc" in which:
         for name, cfg in CBMC_CASES.items():
             make_cbmc_case(name, cfg)
+    for name, seed in LONG_CASES.items():
+        if "long" in which or "long:" + name in which:
+            make_long_case(name, seed)

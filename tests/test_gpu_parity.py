@@ -59,6 +59,7 @@ def test_replay_recorded_stream(pg, case, built):
     np.testing.assert_allclose(et, g["run_etot"], rtol=1e-9, atol=1e-9)
     np.testing.assert_allclose(s.positions(), g["run_coords"], rtol=0, atol=1e-9)
     np.testing.assert_allclose(s.observables()[[0, 4]], g["run_obs"][[0, 4]], rtol=1e-10)
+    np.testing.assert_allclose(s.rhoz(), g["run_rhoz"], rtol=1e-12, atol=1e-12)
     fresh = s.total_energy()[:4]
     np.testing.assert_allclose(fresh, g["run_recompute"], rtol=1e-10, atol=1e-9)
 
