@@ -214,6 +214,8 @@ def main():
     ap.add_argument("--replicas", type=int, default=16,
                     help="replicas of the workload in the batched form (the chosen form)")
     ap.add_argument("--batch-steps", type=int, default=256)
+    ap.add_argument("--no-surrogate", action="store_true",
+                    help="time the batched precision form without delayed acceptance")
     ap.add_argument("--only", default=None, choices=[None, "fp32", "fp64", "batch"],
                     help="profiling runs: time one form only, no baselines or e2e")
     args = ap.parse_args()
@@ -265,14 +267,25 @@ def main():
         return 0
 
     # the chosen form: replicas of the workload in one batch (precision form)
+    # with delayed acceptance by the learned surrogate when its weights exist
     R, BS = args.replicas, args.batch_steps
     batch = pg.Batch([make_workload(args.workload, seed=20261203 + r) for r in range(R)],
                      device=local)
     batch.seed(1000 * rank + 77)
+    sg, sg_meta = None, None
+    wpath = os.path.join(ROOT, "plum_gb300", "data", "surrogate_%s.npz" % args.workload)
+    if os.path.exists(wpath) and not args.no_surrogate:
+        from plum_gb300 import surrogate as S
+        sg = S.load(wpath, device=local)
+        z = np.load(wpath)
+        sg_meta = {k: (z[k].item() if z[k].ndim == 0 else None) for k in z.files
+                   if k not in ("params", "mu", "isd")}
+        batch.set_surrogate(sg)
     for _ in range(args.warmup):
         batch.run(BS)
         s32.run(M)
         s64.run(args.plain_moves_per_step)
+    da0 = np.array(batch.da_stats()) if sg is not None else None
 
     sampler = ClockSampler(local)
     sampler.start()
@@ -297,6 +310,32 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         step_ms = float(t.item())
     value = world * R * BS / (step_ms / 1e3)
+    da = None
+    if sg is not None:
+        mv, ps, ac = (np.array(batch.da_stats()) - da0).tolist()
+        da = {"surrogate_moves": mv, "stage1_pass": ps / max(mv, 1),
+              "surrogate_move_acceptance": ac / max(mv, 1),
+              "exact_evaluations_skipped": (mv - ps) / float(R * BS * args.steps),
+              "weights": os.path.relpath(wpath, ROOT), "training": sg_meta}
+    # per-kernel CUDA-event durations over a few more steps (plain launches)
+    kern_ms = batch.time_kernels(32)
+
+    # the same replicas without the surrogate (FP32 + batched)
+    batch.set_surrogate(None)
+    for _ in range(2):
+        batch.run(BS)
+    nb_ms = []
+    for _ in range(max(3, args.steps // 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        batch.run(BS)
+        nb_ms.append(batch.last_timing()[0])
+    batched32 = R * BS / (statistics.mean(nb_ms) / 1e3)
+    kern_ms_nb = batch.time_kernels(32)
+
+    # precision form against FP64 on identical trial moves
+    from plum_gb300 import precision
+    prec = precision.compare(s64, s32, s64.topology()[0], n=200, seed=5)
 
     # one replica of the precision form alone
     f_ms = []
@@ -335,7 +374,10 @@ def main():
     frac_in = (4.0 / 3.0) * math.pi * info.real_cutoff ** 3 / (info.box[0] ** 3)
     W = alg_flops_per_move(info.n_bead, mean_moved, info.n_kvec, min(1.0, frac_in), mean_bonds)
     peak, peak64 = pg.probe_peaks(local)
-    achieved = W * (R * BS / (step_ms / 1e3)) / 1e12
+    # dominant kernel: the batched energy change; per launch it evaluates the
+    # moves that reach the exact change (all of them without the surrogate)
+    evaluated = R * (1.0 - (da["exact_evaluations_skipped"] if da else 0.0))
+    achieved = W * evaluated / (kern_ms[0] / 1e3) / 1e12
 
     samples = None
     if args.samples_seconds > 0:
@@ -371,8 +413,18 @@ def main():
                    "real_cutoff": info.real_cutoff, "replicas": R, "steps_per_batch": BS,
                    "moves_per_step": R * BS,
                    "form": "batched replicas, precision form (FP32 pair/k, FP64 S(k) and "
-                           "totals, FP64 recompute every 1e4 moves)",
+                           "totals, FP64 recompute every 1e4 moves)" +
+                           (", delayed acceptance with the learned surrogate" if sg else ""),
                    "l2": "flushed between steps (256 MB write)", "parallelism": "replicas"},
+        "batched_fp32_no_surrogate": {"value": batched32, "unit": "moves/s",
+                                      "ms_per_step": statistics.mean(nb_ms)},
+        "delayed_acceptance": da,
+        "kernel_ms_per_launch": {
+            "chosen_form": dict(zip(("delta", "serial", "descriptor", "inference"),
+                                    [float(x) for x in kern_ms])),
+            "no_surrogate": dict(zip(("delta", "serial", "descriptor", "inference"),
+                                     [float(x) for x in kern_ms_nb]))},
+        "precision_vs_fp64": prec,
         "single_replica_fp32": {"value": single32, "unit": "moves/s", "moves_per_step": M},
         "plain_fp64": {"value": plain, "unit": "moves/s",
                        "moves_per_step": args.plain_moves_per_step},
@@ -382,8 +434,10 @@ def main():
                 "path": "plum_run_moves: one replica, precision form, recorded mt19937 stream "
                         "copied in and per-move logs copied out in the timed region"},
         "gpu_launches": int(kernels),
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+        "roofline": {"bound": "fp32", "kernel": "k_batch_delta32",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
+                     "launch_ms": float(kern_ms[0]), "moves_per_launch": evaluated,
                      "peak_source": "FP32 FMA probe kernel on this GPU (measured; the "
                                     "measured-peaks file has no FP32 entry)",
                      "fp64_peak_tflops": peak64,

@@ -200,6 +200,22 @@ int plum_cbmc_trials_noalloc(plum_ctx* ctx, int n_trials, const double* d_b1,
                              const double* d_chain_ci, int delete_mol, double* d_u_out,
                              char* err, int err_cap);
 
+/* Grand-canonical parameters of run.in (force_field.cc:96-103): out9 =
+ * {chem_pot, deBroglie prefactor, bead charge, chain length, CBMC trials,
+ * GC frequency, spring constant, r0, type index of the species' beads}. */
+int plum_gc_info(const plum_ctx* ctx, double* out9);
+/* Appends n_mols molecules after the last one (as the reference's
+ * mols.push_back on an accepted insertion, cbmc.cc:294-312): sizes[n_mols],
+ * and for the sum of sizes beads xyz[3*n], q[n], type[n] (type indices of
+ * plum_type_name). The running totals and S(k) are recomputed from scratch
+ * (ForceField::EnergyInitForAddedMolecule, force_field.cc:1088-1105, updates
+ * them incrementally; they agree to round-off). */
+int plum_append_molecules(plum_ctx* ctx, int n_mols, const int* sizes, const double* xyz,
+                          const double* q, const int* type);
+/* Removes molecules [first, first + count) (simulation.cc:383-391 with the
+ * potentials' AdjustEnergyUponMolDeletion); totals recomputed as above. */
+int plum_erase_molecules(plum_ctx* ctx, int first, int count);
+
 /* Full FP64 recompute cadence of plum_run, in moves (0 = never). The
  * precision form defaults to 10000: every 10^4 moves (at the next batch
  * boundary of 256) the totals, S(k) and the fixed-point mirror are rebuilt
@@ -244,6 +260,12 @@ int plum_batch_size(const plum_batch* batch);
  * observables through the single-system calls above. */
 int plum_batch_replica(plum_batch* batch, int r, plum_ctx** ctx);
 int plum_batch_last_timing(const plum_batch* batch, double* ms, long* kernels);
+/* n_steps more steps with plain launches and CUDA events around every
+ * kernel: out4 = mean milliseconds per launch of {energy change (delta),
+ * serial step, surrogate descriptor (with its smearing), surrogate
+ * inference} (0 for kernels that did not run). For measurement; the steps
+ * count as ordinary steps of the replicas. */
+int plum_batch_time_kernels(plum_batch* batch, int n_steps, double* out4);
 
 /* ---------------------------------------------------------------------
  * Learned surrogate and delayed acceptance. No counterpart in the

@@ -16,7 +16,8 @@
 //
 // Differences: bad input throws plum::InputError instead of exit(1);
 // Simulation takes an explicit seed (the reference seeds from the clock,
-// simulation.cc:133-136); grand-canonical steps are not available here.
+// simulation.cc:133-136); grand-canonical runs step on the host (Step), each
+// exchange growth step's trial energies in one device call.
 #pragma once
 
 #include <istream>
@@ -114,11 +115,39 @@ class ForceField {  // force_field.h:22-294 (energy surface)
   const plum_run_info& RunInfo() const { return run_; }
   const plum_info& Info() const { return info_; }
 
+  // Grand-canonical exchange with configurational bias (cbmc.cc:5-442):
+  // draws on the host in the reference's order, the trial-site energies of
+  // each growth step in one batched device call (plum_cbmc_trials).
+  // Insertion returns whether the grown chain was accepted (it is then
+  // appended to mols, with its counterions for a charged species); deletion
+  // returns the molecule to delete, or -1.
+  bool CBMCFChainInsertion(std::vector<Molecule>& mols, std::mt19937& rand_gen);
+  int CBMCFChainDeletion(std::vector<Molecule>& mols, std::mt19937& rand_gen);
+  // Commits the molecules appended to mols / removes molecules on the device
+  // (force_field.cc:1088-1105; the potentials' AdjustEnergyUponMolDeletion).
+  void EnergyInitForAddedMolecule(std::vector<Molecule>& mols, int n_added);
+  void AdjustEnergyUponMolDeletion(int first, int count);
+  double ChemPot() const { return gc_[0]; }
+  int GCChainLen() const { return (int)gc_[3]; }
+  double GCBeadCharge() const { return gc_[2]; }
+
  private:
+  double CBMCFGenTrialBeads(const double* end, int current_len, std::mt19937& rand_gen,
+                            int delete_id, const double* replace_first);
+  double RandomBondLen(std::mt19937& rand_gen);  // potential_spring.cc:50-61
+  double Gasdev(double mean, double sd, std::mt19937& rand_gen);  // misc.cc:111-134
+  void GCCounts(const std::vector<Molecule>& mols, int* spc1, int* spc2) const;
   plum_ctx* ctx_ = nullptr;
   plum_run_info run_{};
   plum_info info_{};
   std::vector<int> mol_start_;
+  double gc_[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // plum_gc_info
+  std::vector<std::string> type_names_;
+  // cbmc_chain (grown beads then their counterions), trial sites and weights
+  std::vector<double> chain_, tb1_, tb2_, w_, u_;
+  // gasdev's cached second deviate (the reference keeps it in statics)
+  int gd_iset_ = 0;
+  double gd_gset_ = 0;
 };
 
 class Simulation {  // simulation.h:20-201 (step loop and observables)
@@ -130,6 +159,11 @@ class Simulation {  // simulation.h:20-201 (step loop and observables)
   void Run();                 // steps from run.in, on the device
   void RunSteps(long n);      // n steps on the device
   void TranslationalMove();   // one step, host control flow (simulation.cc:241-355)
+  void GCMove();              // simulation.cc:357-404
+  // One step of Simulation::Run's loop (simulation.cc:219-226): the draw,
+  // then GCMove or TranslationalMove; last_move_type 5 / 6 for an insertion
+  // / deletion attempt, last_accept when the molecule count changed.
+  void Step();
   void Sample();              // simulation.cc:723-798 (energies, Rg; no pressure)
   double RadiusOfGyration();  // simulation.cc:406-434
   double EndToEndDistance();  // simulation.cc:483-501
@@ -144,6 +178,8 @@ class Simulation {  // simulation.h:20-201 (step loop and observables)
   double pair_e_cumu = 0, ewald_e_cumu = 0, bond_e_cumu = 0, ext_e_cumu = 0, rg_tot_cumu = 0;
   long ff_avg_counter = 0, mol_avg_counter = 0;
   int last_move_type = -1, last_accept = 0;
+  long insertion_attempted = 0, insertion_accepted = 0;
+  long deletion_attempted = 0, deletion_accepted = 0;
 
  private:
   plum_run_info run_{};

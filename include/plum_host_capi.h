@@ -11,6 +11,9 @@
  *                                energies on the GPU
  *   plum_sim_run_steps           the step loop of Simulation::Run
  *                                (simulation.cc:216-239) on the GPU
+ *   plum_sim_steps               the same loop with host control flow,
+ *                                Simulation::GCMove (simulation.cc:357-404)
+ *                                included
  *   plum_sim_energies            ForceField::Tot*Energy (force_field.cc:1201-1219)
  */
 #ifndef PLUM_HOST_CAPI_H_
@@ -32,6 +35,13 @@ int plum_sim_destroy(plum_sim* sim);
  * draw simulation.cc:221 spends on the grand-canonical check. */
 int plum_sim_translational_moves(plum_sim* sim, int n, int* move_type, int* accept);
 int plum_sim_run_steps(plum_sim* sim, long n);
+/* n steps of Simulation::Run's loop (simulation.cc:219-226) with host
+ * control flow, grand-canonical exchanges included: per step the move type
+ * (0-4 translational, 5 insertion, 6 deletion attempt, -1 none) and whether
+ * it was accepted. */
+int plum_sim_steps(plum_sim* sim, int n, int* move_type, int* accept);
+/* Beads currently in the host molecules (changes with exchanges). */
+int plum_sim_n_bead(plum_sim* sim);
 int plum_sim_positions(plum_sim* sim, double* xyz);
 int plum_sim_energies(plum_sim* sim, double* out);
 

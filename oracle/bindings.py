@@ -153,6 +153,7 @@ class Ref(_Base):
         return o
 
     def coords(self):
+        self.n_bead = self.L.pr_n_bead(self.h)  # grand-canonical moves change it
         o = np.zeros(3 * self.n_bead)
         self.L.pr_coords(self.h, o)
         return o.reshape(-1, 3)
@@ -266,6 +267,7 @@ class Oracle(_Base):
         return used, mt, ac, et
 
     def coords(self):
+        self.n_bead = self.L.po_n_bead(self.h)  # grand-canonical moves change it
         o = np.zeros(3 * self.n_bead)
         self.L.po_coords(self.h, o)
         return o.reshape(-1, 3)

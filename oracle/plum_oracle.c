@@ -133,6 +133,9 @@ struct po_ctx {
   /* grand-canonical species (force_field.cc:96-103) */
   double chem_pot, debroglie, gc_bead_charge;
   int gc_freq, gc_chain_len, cbmc_trials, gc_type;
+  /* gasdev's cached second deviate (misc.cc:112-113 keeps it in statics) */
+  int gd_iset;
+  double gd_gset;
   mt_t g;
 };
 
@@ -1131,17 +1134,31 @@ static int translational_move(po_ctx* c, rng_t* r, int* mv, de_t* d, int* acc) {
   return move_type;
 }
 
+static int gc_move(po_ctx* c, rng_t* r, int* acc);
+
 static long run_loop(po_ctx* c, rng_t* r, int n, int* move_type, int* accept,
                      int* draws, double* etot) {
-  int* mv = (int*)calloc((size_t)c->n_bead, sizeof(int));
+  int mv_cap = c->n_bead;
+  int* mv = (int*)calloc((size_t)mv_cap, sizeof(int));
   de_t d;
   memset(&d, 0, sizeof d);
   d.dsk = (double*)calloc((size_t)2 * (c->n_k > 0 ? c->n_k : 1), sizeof(double));
   for (int s = 0; s < n; s++) {
     long p0 = r->pos;
-    (void)rng_u32(r); /* simulation.cc:221 */
-    int acc = 0;
-    int mt = translational_move(c, r, mv, &d, &acc);
+    /* simulation.cc:221-226: int rand_num = rand_gen(); GC when
+     * rand_num % gc_freq == 0 (signed, as the reference's int) */
+    const int32_t rand_num = (int32_t)rng_u32(r);
+    int acc = 0, mt;
+    if (c->use_gc && c->gc_freq > 0 && rand_num % c->gc_freq == 0) {
+      mt = gc_move(c, r, &acc);
+      if (c->n_bead > mv_cap) {
+        mv_cap = c->n_bead;
+        free(mv);
+        mv = (int*)calloc((size_t)mv_cap, sizeof(int));
+      }
+    } else {
+      mt = translational_move(c, r, mv, &d, &acc);
+    }
     if (r->overrun) break;
     if (move_type) move_type[s] = mt;
     if (accept) accept[s] = acc;
@@ -1164,6 +1181,278 @@ long po_run_stream(po_ctx* c, int n, const uint32_t* stream, long n_stream,
                    int* move_type, int* accept, double* etot) {
   rng_t r = {NULL, stream, n_stream, 0, 0};
   return run_loop(c, &r, n, move_type, accept, NULL, etot);
+}
+
+/* ------------------------------------------------------ grand canonical */
+/* gasdev (misc.cc:111-134): polar Box-Muller; the second deviate is cached
+ * (the reference keeps it in function statics shared by the process; here
+ * per context, as in a fresh process). */
+static double gasdev(po_ctx* c, rng_t* r, double mean, double sd) {
+  if (c->gd_iset == 0) {
+    double v1, v2, rsq;
+    do {
+      v1 = 2.0 * ((double)rng_u32(r) / MT_MAX) - 1.0;
+      v2 = 2.0 * ((double)rng_u32(r) / MT_MAX) - 1.0;
+      rsq = v1 * v1 + v2 * v2;
+    } while ((rsq >= 1.0 || rsq == 0.0) && !r->overrun);
+    if (r->overrun) return mean;
+    double fac = sqrt(-2.0 * log(rsq) / rsq);
+    c->gd_gset = v1 * fac;
+    c->gd_iset = 1;
+    return v2 * fac * sd + mean;
+  }
+  c->gd_iset = 0;
+  return c->gd_gset * sd + mean;
+}
+
+/* PotentialSpring::RandomBondLen (potential_spring.cc:50-61): a Gaussian
+ * around r0 accepted with probability len^2 / (r0 + 3 sigma)^2. */
+static double random_bond_len(po_ctx* c, rng_t* r) {
+  const double sigma = sqrt(1 / (c->beta * c->k_bond));
+  const double a = (c->r0 + 3 * sigma) * (c->r0 + 3 * sigma);
+  double len = 0;
+  int ready = 0;
+  while (!ready && !r->overrun) {
+    len = gasdev(c, r, c->r0, sigma);
+    ready = ((double)rng_u32(r) / MT_MAX < (len * len / a));
+  }
+  return len;
+}
+
+/* ForceField::UpdateMolCounts (force_field.cc:1258-1277): its counts put
+ * neutral single beads with the cations. */
+static void ff_counts(const po_ctx* c, int* n_chain, int* n_cion, int* n_aion) {
+  *n_chain = *n_cion = *n_aion = 0;
+  for (int m = c->phantom; m < c->n_mol; m++) {
+    if (c->mol_start[m + 1] - c->mol_start[m] > 1)
+      (*n_chain)++;
+    else if (c->q[c->mol_start[m]] >= 0)
+      (*n_cion)++;
+    else
+      (*n_aion)++;
+  }
+  *n_chain -= c->grafted;
+}
+
+/* ForceField::CBMCFGenTrialBeads (cbmc.cc:161-212): each trial draws its
+ * bond length, its direction and (charged species) its counterion's
+ * position, then gets its Boltzmann weight; returns the weights' sum. */
+static double gen_trials(po_ctx* c, rng_t* r, const double* end, int cl, const double* chain,
+                         const double* chain_ci, int delete_id, double* tb1, double* tb2,
+                         double* w) {
+  const int charged = c->gc_bead_charge != 0;
+  double Wi = 0;
+  for (int i = 0; i < c->cbmc_trials; i++) {
+    double bl = 0;
+    if (c->use_bond)
+      bl = random_bond_len(c, r);
+    else if (c->use_rigid)
+      bl = c->rigid;
+    double v[3] = {0, 0, 0};
+    rand_sphere(r, v);
+    for (int j = 0; j < 3; j++) tb1[3 * i + j] = v[j] * bl + end[j];
+    if (charged)
+      for (int j = 0; j < 3; j++) tb2[3 * i + j] = (double)rng_u32(r) / MT_MAX * c->box[j];
+    if (r->overrun) return 0;
+    const double u = po_beads_energy(c, tb1 + 3 * i, charged ? tb2 + 3 * i : tb1 + 3 * i, cl,
+                                     chain, chain_ci, delete_id);
+    w[i] = exp(-c->beta * u);
+    Wi += w[i];
+  }
+  return Wi;
+}
+
+/* spc1: molecules of the exchanged species; spc2: its counter-species
+ * (cbmc.cc:265-275, 336-340, 407-411). */
+static void gc_species(const po_ctx* c, int* spc1, int* spc2) {
+  int nc, ncat, nan;
+  ff_counts(c, &nc, &ncat, &nan);
+  const double qb = c->gc_bead_charge;
+  if (c->gc_chain_len > 1)
+    *spc1 = nc;
+  else if (qb >= 0)
+    *spc1 = ncat - c->coion;
+  else
+    *spc1 = nan - c->coion;
+  *spc2 = qb == 0 ? 0 : (qb > 0 ? nan : ncat);
+}
+
+/* ForceField::CBMCFChainInsertion (cbmc.cc:214-328); chain [2L][3] gets the
+ * grown chain and (charged species) its counterions. */
+static int chain_insertion(po_ctx* c, rng_t* r, double* chain) {
+  const int L = c->gc_chain_len, T = c->cbmc_trials;
+  const int charged = c->gc_bead_charge != 0;
+  double weight = 1.0;
+  const int i_index = charged ? L : 0, initial = charged ? 2 : 1;
+  for (int i = 0; i < initial; i++)
+    for (int j = 0; j < 3; j++) chain[3 * (i * L) + j] = (double)rng_u32(r) / MT_MAX * c->box[j];
+  if (r->overrun) return 0;
+  weight *= exp(-c->beta * po_beads_energy(c, chain, chain + 3 * i_index, 0, chain,
+                                            chain + 3 * L, -1));
+  if (weight <= 0) return 0;
+  double* tb1 = (double*)malloc(sizeof(double) * 3 * (size_t)T);
+  double* tb2 = (double*)malloc(sizeof(double) * 3 * (size_t)T);
+  double* w = (double*)malloc(sizeof(double) * (size_t)T);
+  int ok = 1;
+  for (int i = 1; i < L && ok; i++) {
+    const double Wi = gen_trials(c, r, chain + 3 * (i - 1), i, chain, chain + 3 * L, -1, tb1,
+                                 tb2, w);
+    weight *= Wi / T;
+    if (r->overrun || weight <= 0) {
+      ok = 0;
+      break;
+    }
+    const double rn = (double)rng_u32(r) / MT_MAX * Wi;
+    int cb = 0;
+    double cum = w[0];
+    while (cum < rn && cb < T - 1) cum += w[++cb];
+    for (int j = 0; j < 3; j++) chain[3 * i + j] = tb1[3 * cb + j];
+    if (charged)
+      for (int j = 0; j < 3; j++) chain[3 * (i + L) + j] = tb2[3 * cb + j];
+  }
+  free(tb1);
+  free(tb2);
+  free(w);
+  if (!ok || r->overrun) return 0;
+  int spc1, spc2;
+  gc_species(c, &spc1, &spc2);
+  const int spc2_add = charged ? L : 0;
+  double factorial = 1;
+  for (int i = spc1 + 1; i <= spc1 + 1; i++) factorial *= i;
+  for (int i = spc2 + 1; i <= spc2 + spc2_add; i++) factorial *= i;
+  const double vol = c->box[0] * c->box[1] * c->box[2];
+  double vol_over_lam = 1;
+  vol_over_lam *= pow(vol / (c->debroglie / pow((double)L, 1.5)), 1);
+  vol_over_lam *= pow(vol / (c->debroglie / pow(1.0, 1.5)), spc2_add);
+  const double C = vol_over_lam * (1.0 / factorial);
+  const double rn = (double)rng_u32(r) / MT_MAX;
+  return rn < (exp(c->beta * c->chem_pot) * weight) * C;
+}
+
+/* ForceField::CBMCFChainDeletion (cbmc.cc:330-442): the molecule to delete
+ * or -1. */
+static int chain_deletion(po_ctx* c, rng_t* r) {
+  const int L = c->gc_chain_len, T = c->cbmc_trials;
+  const int charged = c->gc_bead_charge != 0;
+  int spc1, spc2;
+  gc_species(c, &spc1, &spc2);
+  int did = (int)floor((double)rng_u32(r) / MT_MAX * spc1);
+  if (did >= spc1) did = spc1 - 1;
+  if (r->overrun || did < 0) return -1;  /* nothing of the species to delete */
+  did = c->phantom + c->coion + c->grafted + c->grafted_counterion + (charged ? did * (1 + L) : did);
+  const int second = charged ? did + 1 : did;
+  double* chain = (double*)calloc((size_t)6 * L, sizeof(double));
+  double* tb1 = (double*)malloc(sizeof(double) * 3 * (size_t)T);
+  double* tb2 = (double*)malloc(sizeof(double) * 3 * (size_t)T);
+  double* w = (double*)malloc(sizeof(double) * (size_t)T);
+  const double* x0 = c->x + 3 * c->mol_start[did];
+  const double* s0 = c->x + 3 * c->mol_start[second];
+  double weight = exp(-c->beta * po_beads_energy(c, x0, s0, 0, chain, chain + 3 * L, did));
+  for (int j = 0; j < 3; j++) chain[j] = x0[j];
+  if (charged)
+    for (int j = 0; j < 3; j++) chain[3 * L + j] = s0[j];
+  for (int i = 1; i < L && !r->overrun; i++) {
+    for (int j = 0; j < 3; j++) chain[3 * i + j] = c->x[3 * (c->mol_start[did] + i) + j];
+    if (charged)
+      for (int j = 0; j < 3; j++)
+        chain[3 * (i + L) + j] = c->x[3 * c->mol_start[did + i + 1] + j];
+    gen_trials(c, r, chain + 3 * (i - 1), i, chain, chain + 3 * L, did, tb1, tb2, w);
+    w[0] = exp(-c->beta * po_beads_energy(c, chain + 3 * i, chain + 3 * (charged ? i + L : i), i,
+                                           chain, chain + 3 * L, did));
+    double Wi = 0;
+    for (int j = 0; j < T; j++) Wi += w[j];
+    weight *= Wi / T;
+  }
+  free(chain);
+  free(tb1);
+  free(tb2);
+  free(w);
+  if (r->overrun) return -1;
+  const int spc2_del = charged ? L : 0;
+  double factorial = 1;
+  for (int i = spc1; i > spc1 - 1; i--) factorial *= i;
+  for (int i = spc2; i > spc2 - spc2_del; i--) factorial *= i;
+  const double vol = c->box[0] * c->box[1] * c->box[2];
+  double lam_over_vol = 1;
+  lam_over_vol *= pow((c->debroglie / pow((double)L, 1.5)) / vol, 1);
+  lam_over_vol *= pow((c->debroglie / pow(1.0, 1.5)) / vol, spc2_del);
+  const double C = lam_over_vol * factorial;
+  const double rn = (double)rng_u32(r) / MT_MAX;
+  if (rn < C / (exp(c->beta * c->chem_pot) * weight)) return did;
+  return -1;
+}
+
+/* Appends the grown chain (one molecule of L beads) and, for a charged
+ * species, its L counterions (single-bead molecules), as the reference's
+ * mols.push_back does (cbmc.cc:294-312). */
+static void append_chain(po_ctx* c, const double* chain) {
+  const int L = c->gc_chain_len, charged = c->gc_bead_charge != 0;
+  const int add_b = charged ? 2 * L : L, add_m = charged ? 1 + L : 1;
+  const int nb = c->n_bead + add_b, nm = c->n_mol + add_m;
+  c->x = (double*)realloc(c->x, sizeof(double) * 3 * (size_t)nb);
+  c->t = (double*)realloc(c->t, sizeof(double) * 3 * (size_t)nb);
+  c->q = (double*)realloc(c->q, sizeof(double) * (size_t)nb);
+  c->type = (int*)realloc(c->type, sizeof(int) * (size_t)nb);
+  c->mol_start = (int*)realloc(c->mol_start, sizeof(int) * (size_t)(nm + 1));
+  c->bond_mol = (double*)realloc(c->bond_mol, sizeof(double) * (size_t)nm);
+  for (int i = 0; i < add_b; i++) {
+    const int b = c->n_bead + i;
+    for (int j = 0; j < 3; j++) c->x[3 * b + j] = c->t[3 * b + j] = chain[3 * i + j];
+    c->q[b] = i < L ? c->gc_bead_charge : -c->gc_bead_charge;
+    c->type[b] = c->gc_type;
+  }
+  int m = c->n_mol;
+  c->mol_start[m + 1] = c->n_bead + L;
+  for (int i = 1; i < add_m; i++) c->mol_start[m + 1 + i] = c->n_bead + L + i;
+  for (int i = 0; i < add_m; i++) c->bond_mol[m + i] = 0;
+  c->n_bead = nb;
+  c->n_mol = nm;
+}
+
+/* Erases molecules [m0, m0 + count) (simulation.cc:383-391). */
+static void erase_mols(po_ctx* c, int m0, int count) {
+  const int b0 = c->mol_start[m0], b1 = c->mol_start[m0 + count], nb = b1 - b0;
+  memmove(c->x + 3 * b0, c->x + 3 * b1, sizeof(double) * 3 * (size_t)(c->n_bead - b1));
+  memmove(c->t + 3 * b0, c->t + 3 * b1, sizeof(double) * 3 * (size_t)(c->n_bead - b1));
+  memmove(c->q + b0, c->q + b1, sizeof(double) * (size_t)(c->n_bead - b1));
+  memmove(c->type + b0, c->type + b1, sizeof(int) * (size_t)(c->n_bead - b1));
+  for (int m = m0; m + count <= c->n_mol; m++) c->mol_start[m] = c->mol_start[m + count] - nb;
+  memmove(c->bond_mol + m0, c->bond_mol + m0 + count,
+          sizeof(double) * (size_t)(c->n_mol - m0 - count));
+  c->n_bead -= nb;
+  c->n_mol -= count;
+}
+
+/* Simulation::GCMove (simulation.cc:357-404); move type 5 insertion, 6
+ * deletion. After an accepted exchange the running totals are recomputed
+ * (the reference updates them incrementally; the totals agree to
+ * round-off). */
+static int gc_move(po_ctx* c, rng_t* r, int* acc) {
+  *acc = 0;
+  const int insert = (int)(rng_u32(r) % 2u);
+  if (insert) {
+    double* chain = (double*)calloc((size_t)6 * c->gc_chain_len, sizeof(double));
+    const int ok = chain_insertion(c, r, chain);
+    if (ok && !r->overrun) {
+      append_chain(c, chain);
+      *acc = 1;
+    }
+    free(chain);
+  } else if (c->n_mol - c->phantom - c->coion > 0) {
+    const int did = chain_deletion(c, r);
+    if (did >= c->phantom + c->coion) {
+      int ions = 0;
+      for (int b = c->mol_start[did]; b < c->mol_start[did + 1]; b++)
+        ions += (int)round(fabs(c->q[b]));
+      erase_mols(c, did, 1 + ions);
+      *acc = 1;
+    }
+  }
+  if (*acc) {
+    update_counts(c);
+    po_total_energy(c, NULL);
+  }
+  return insert ? 5 : 6;
 }
 
 void po_coords(const po_ctx* c, double* out) {

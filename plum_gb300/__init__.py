@@ -68,6 +68,7 @@ def lib():
         L.plum_set_positions.argtypes = [C.c_void_p, _dp]
         L.plum_observables.argtypes = [C.c_void_p, _dp]
         L.plum_rhoz.argtypes = [C.c_void_p, _dp, C.c_int, C.POINTER(C.c_int)]
+        L.plum_get_topology.argtypes = [C.c_void_p, _ip, _dp, _ip]
         L.plum_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_double),
                                        C.POINTER(C.c_long)]
         L.plum_set_recompute.argtypes = [C.c_void_p, C.c_long]
@@ -90,6 +91,11 @@ def lib():
         L.plum_sim_destroy.argtypes = [C.c_void_p]
         L.plum_sim_translational_moves.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         L.plum_sim_run_steps.argtypes = [C.c_void_p, C.c_long]
+        L.plum_sim_steps.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+        L.plum_sim_n_bead.argtypes = [C.c_void_p]
+        L.plum_gc_info.argtypes = [C.c_void_p, _dp]
+        L.plum_append_molecules.argtypes = [C.c_void_p, C.c_int, _ip, _dp, _dp, _ip]
+        L.plum_erase_molecules.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.plum_sim_positions.argtypes = [C.c_void_p, _dp]
         L.plum_sim_energies.argtypes = [C.c_void_p, _dp]
         _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
@@ -108,6 +114,7 @@ def lib():
                                                   C.c_void_p, C.POINTER(C.c_long)]
         L.plum_move_descriptor.argtypes = [C.c_void_p, _dp]
         L.plum_batch_set_surrogate.argtypes = [C.c_void_p, C.c_void_p]
+        L.plum_batch_time_kernels.argtypes = [C.c_void_p, C.c_int, _dp]
         L.plum_batch_da_stats.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
         _lib = L
     return _lib
@@ -202,6 +209,24 @@ class System:
         _check(lib().plum_run(self.h, n_moves, C.byref(acc)))
         return acc.value
 
+    def _refresh_counts(self):
+        info = Info()
+        _check(lib().plum_ctx_info(self.h, C.byref(info)))
+        self.info, self.n_bead, self.n_mol = info, info.n_bead, info.n_mol
+
+    def append_molecules(self, sizes, xyz, q, types):
+        """Appends molecules (sizes[m] beads each) after the last one."""
+        sizes = np.ascontiguousarray(sizes, np.int32)
+        _check(lib().plum_append_molecules(self.h, len(sizes), sizes,
+                                           np.ascontiguousarray(xyz, np.float64).ravel(),
+                                           np.ascontiguousarray(q, np.float64),
+                                           np.ascontiguousarray(types, np.int32)))
+        self._refresh_counts()
+
+    def erase_molecules(self, first, count):
+        _check(lib().plum_erase_molecules(self.h, first, count))
+        self._refresh_counts()
+
     def positions(self):
         o = np.zeros(3 * self.n_bead)
         _check(lib().plum_get_positions(self.h, o))
@@ -209,6 +234,14 @@ class System:
 
     def set_positions(self, xyz):
         _check(lib().plum_set_positions(self.h, np.ascontiguousarray(xyz, np.float64).ravel()))
+
+    def topology(self):
+        """(mol_start [n_mol+1], charge [n_bead], type index [n_bead])."""
+        ms = np.zeros(self.n_mol + 1, np.int32)
+        q = np.zeros(self.n_bead)
+        ty = np.zeros(self.n_bead, np.int32)
+        _check(lib().plum_get_topology(self.h, ms, q, ty))
+        return ms, q, ty
 
     def observables(self):
         o = np.zeros(5)
@@ -218,7 +251,7 @@ class System:
     def rhoz(self):
         """One rho(z) sample [n_bins, 3] (chain beads, q >= 0 ions, q < 0 ions)."""
         nb = C.c_int(0)
-        _check(lib().plum_rhoz(self.h, None, 0, C.byref(nb)))
+        _check(lib().plum_rhoz(self.h, np.zeros(1), 0, C.byref(nb)))
         o = np.zeros(3 * nb.value)
         _check(lib().plum_rhoz(self.h, o, len(o), C.byref(nb)))
         return o.reshape(-1, 3)
@@ -405,6 +438,13 @@ class Batch:
         _check(lib().plum_batch_last_timing(self.h, C.byref(ms), C.byref(k)))
         return ms.value, k.value
 
+    def time_kernels(self, n_steps):
+        """n_steps steps with per-kernel CUDA events: mean ms per launch of
+        (delta, serial, descriptor, inference)."""
+        o = np.zeros(4)
+        _check(lib().plum_batch_time_kernels(self.h, n_steps, o))
+        return o
+
     def set_surrogate(self, sg):
         """Delayed acceptance with the surrogate sg (None: off)."""
         self._sg = sg
@@ -447,7 +487,19 @@ class HostSimulation:
     def run_steps(self, n):
         _check(lib().plum_sim_run_steps(self.h, n))
 
-    def positions(self, n_bead):
+    def steps(self, n):
+        """n steps of the reference's loop with host control flow, exchanges
+        included: (move type per step, accepted per step)."""
+        mt = np.zeros(n, np.int32)
+        ac = np.zeros(n, np.int32)
+        _check(lib().plum_sim_steps(self.h, n, _ptr(mt), _ptr(ac)))
+        return mt, ac
+
+    def n_bead(self):
+        return lib().plum_sim_n_bead(self.h)
+
+    def positions(self, n_bead=None):
+        n_bead = self.n_bead() if n_bead is None else n_bead
         o = np.zeros(3 * n_bead)
         _check(lib().plum_sim_positions(self.h, o))
         return o.reshape(-1, 3)

@@ -733,6 +733,153 @@ int ensure_desc(plum_ctx* c) {
 }
 }  // namespace
 
+namespace {
+// Re-creates the bead-count-dependent device buffers from the host copy of
+// the system (in.q, in.type, in.mol_start and h_pos) after molecules were
+// added or removed, then recomputes every energy term and S(k) from scratch.
+int rebuild_system(plum_ctx* c) {
+  Input& in = c->in;
+  DevParams& P = c->P;
+  DevBuffers& B = c->B;
+  const int nb = (int)in.q.size();
+  CK(cudaStreamSynchronize(c->s));
+  std::vector<int> chains, ions;
+  c->max_len = 1;
+  for (int m = in.phantom; m < in.n_mol; m++) {
+    const int sz = in.mol_start[m + 1] - in.mol_start[m];
+    (sz > 1 ? chains : ions).push_back(m);
+    c->max_len = std::max(c->max_len, sz);
+  }
+  P.n_bead = nb;
+  P.n_mol = in.n_mol;
+  P.n_chain_total = (int)chains.size();
+  P.n_ion_total = (int)ions.size();
+  void* old[] = {B.pos,      B.trial,      B.type,     B.mol_start, B.chain_ids, B.ion_ids,
+                 B.fpos,     B.fq,         B.ftrial,   B.dsk_part,  B.dsk_part32, B.bond_mol,
+                 c->d_tot_part, c->d_obs_per, c->cb_b, c->cb_c,    c->cb_part,  c->cb_u};
+  for (void* q : old)
+    if (q) cudaFree(q);
+  B.pos = B.trial = nullptr;
+  B.type = B.mol_start = B.chain_ids = B.ion_ids = nullptr;
+  B.fpos = B.ftrial = nullptr;
+  B.fq = nullptr;
+  B.dsk_part = nullptr;
+  B.dsk_part32 = nullptr;
+  B.bond_mol = nullptr;
+  c->d_tot_part = c->d_obs_per = nullptr;
+  c->cb_b = c->cb_c = nullptr;
+  c->cb_part = c->cb_u = nullptr;
+  c->cb_cap = 0;
+  int rc = dalloc(&B.pos, nb) | dalloc(&B.trial, nb) | dalloc(&B.type, nb) |
+           dalloc(&B.mol_start, in.n_mol + 1) | dalloc(&B.chain_ids, chains.size()) |
+           dalloc(&B.ion_ids, ions.size()) | dalloc(&B.fpos, nb) | dalloc(&B.fq, nb) |
+           dalloc(&B.ftrial, c->max_len) | dalloc(&B.bond_mol, in.n_mol);
+  const int groups = (c->max_len + std::max(1, P.kchunk_delta) - 1) / std::max(1, P.kchunk_delta);
+  rc |= dalloc(&B.dsk_part, (size_t)groups * std::max(1, P.n_k));
+  rc |= dalloc(&B.dsk_part32, (size_t)groups * std::max(1, P.n_k));
+  c->n_tot_part = total_partials_count(P);
+  rc |= dalloc(&c->d_tot_part, 2 * (size_t)c->n_tot_part);
+  rc |= dalloc(&c->d_obs_per, 5 * (size_t)std::max(1, in.n_mol));
+  if (rc) return PLUM_ERR_CUDA;
+  CK(cudaMemcpyAsync(B.pos, c->h_pos.data(), sizeof(double4_32a) * nb, cudaMemcpyHostToDevice,
+                     c->s));
+  CK(cudaMemcpyAsync(B.trial, c->h_pos.data(), sizeof(double4_32a) * nb, cudaMemcpyHostToDevice,
+                     c->s));
+  CK(cudaMemcpyAsync(B.type, in.type.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c->s));
+  CK(cudaMemcpyAsync(B.mol_start, in.mol_start.data(), sizeof(int) * (in.n_mol + 1),
+                     cudaMemcpyHostToDevice, c->s));
+  if (!chains.empty())
+    CK(cudaMemcpyAsync(B.chain_ids, chains.data(), sizeof(int) * chains.size(),
+                       cudaMemcpyHostToDevice, c->s));
+  if (!ions.empty())
+    CK(cudaMemcpyAsync(B.ion_ids, ions.data(), sizeof(int) * ions.size(), cudaMemcpyHostToDevice,
+                       c->s));
+  if (c->d_rp1) CK(cudaMemcpyAsync(c->d_rp1, &P, sizeof(P), cudaMemcpyHostToDevice, c->s));
+  DevState st;
+  rc = read_state(c, &st);
+  if (rc) return rc;
+  st.pending = 0;
+  st.sk_pending = 0;
+  CK(cudaMemcpyAsync(B.state, &st, sizeof(st), cudaMemcpyHostToDevice, c->s));
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  c->gexec = nullptr;
+  c->g_moves = 0;
+  c->g_warm = false;
+  c->host_pending = false;
+  c->h_pos_valid = true;
+  in.xyz.resize(3 * (size_t)nb);
+  for (int i = 0; i < nb; i++) {
+    in.xyz[3 * i] = c->h_pos[i].x;
+    in.xyz[3 * i + 1] = c->h_pos[i].y;
+    in.xyz[3 * i + 2] = c->h_pos[i].z;
+  }
+  return total_energy(c, nullptr);
+}
+}  // namespace
+
+int plum_gc_info(const plum_ctx* c, double* out) {
+  if (!c || !out) return fail(PLUM_ERR_INPUT, "null argument");
+  const Input& in = c->in;
+  if (!in.use_gc) return fail(PLUM_ERR_INPUT, "run.in has no grand-canonical species");
+  const auto& tn = in.type_names;
+  out[0] = in.chem_pot;
+  out[1] = in.deBroglie;
+  out[2] = in.gc_bead_charge;
+  out[3] = in.gc_chain_len;
+  out[4] = in.cbmc_trials;
+  out[5] = in.gc_freq;
+  out[6] = in.k_bond;
+  out[7] = in.r0;
+  out[8] = (double)(std::find(tn.begin(), tn.end(), in.gc_symbol) - tn.begin());
+  return PLUM_OK;
+}
+
+int plum_append_molecules(plum_ctx* c, int n_mols, const int* sizes, const double* xyz,
+                          const double* q, const int* type) {
+  if (!c || n_mols <= 0 || !sizes || !xyz || !q || !type)
+    return fail(PLUM_ERR_INPUT, "bad argument");
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
+  long total = 0;
+  for (int m = 0; m < n_mols; m++) {
+    if (sizes[m] <= 0) return fail(PLUM_ERR_INPUT, "empty molecule");
+    total += sizes[m];
+  }
+  for (long k = 0; k < total; k++)
+    if (type[k] < 0 || type[k] >= c->P.n_type || !std::isfinite(xyz[3 * k]) ||
+        !std::isfinite(xyz[3 * k + 1]) || !std::isfinite(xyz[3 * k + 2]))
+      return fail(PLUM_ERR_INPUT, "bad bead type or position");
+  cudaSetDevice(c->device);
+  int rc = refresh_host_pos(c);
+  if (rc) return rc;
+  Input& in = c->in;
+  for (long k = 0; k < total; k++) {
+    in.q.push_back(q[k]);
+    in.type.push_back(type[k]);
+    c->h_pos.push_back(make_double4_32a(xyz[3 * k], xyz[3 * k + 1], xyz[3 * k + 2], q[k]));
+  }
+  for (int m = 0; m < n_mols; m++) in.mol_start.push_back(in.mol_start.back() + sizes[m]);
+  in.n_mol += n_mols;
+  return rebuild_system(c);
+}
+
+int plum_erase_molecules(plum_ctx* c, int first, int count) {
+  if (!c || first < 0 || count <= 0 || first + count > c->in.n_mol)
+    return fail(PLUM_ERR_INPUT, "molecule range out of bounds");
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
+  cudaSetDevice(c->device);
+  int rc = refresh_host_pos(c);
+  if (rc) return rc;
+  Input& in = c->in;
+  const int b0 = in.mol_start[first], b1 = in.mol_start[first + count], nb = b1 - b0;
+  in.q.erase(in.q.begin() + b0, in.q.begin() + b1);
+  in.type.erase(in.type.begin() + b0, in.type.begin() + b1);
+  c->h_pos.erase(c->h_pos.begin() + b0, c->h_pos.begin() + b1);
+  in.mol_start.erase(in.mol_start.begin() + first + 1, in.mol_start.begin() + first + count + 1);
+  for (int m = first + 1; m <= in.n_mol - count; m++) in.mol_start[m] -= nb;
+  in.n_mol -= count;
+  return rebuild_system(c);
+}
+
 int plum_move_descriptor(plum_ctx* c, double* out) {
   if (!c || !out) return fail(PLUM_ERR_INPUT, "null argument");
   if (!c->host_pending) return fail(PLUM_ERR_STATE, "no pending trial move");
@@ -1541,6 +1688,90 @@ int plum_batch_run(plum_batch* b, int n_steps, long* accepted_out) {
     if (e) return fail(PLUM_ERR_TIMEOUT, "tensor-core wait timed out in the surrogate stage");
   }
   if (accepted_out) *accepted_out = (long)(acc1 - acc0);
+  return PLUM_OK;
+}
+
+int plum_batch_time_kernels(plum_batch* b, int n_steps, double* out4) {
+  if (!b || n_steps <= 0 || !out4) return fail(PLUM_ERR_INPUT, "bad argument");
+  cudaSetDevice(b->device);
+  const int R = (int)b->reps.size();
+  // the stream words these steps need (as plum_batch_run refills them)
+  launch_gather_states(b->d_sts, R, b->d_gather, b->s);
+  CK(cudaMemcpyAsync(b->h_gather, b->d_gather, sizeof(long long) * 6 * R, cudaMemcpyDeviceToHost,
+                     b->s));
+  CK(cudaStreamSynchronize(b->s));
+  std::vector<int> need(R);
+  std::vector<long long> pos(R), len(R);
+  bool any = false;
+  for (int r = 0; r < R; r++) {
+    const long long* g = b->h_gather + 6 * r;
+    if (g[2]) return fail((int)g[2], "replica " + std::to_string(r) + " reported an error");
+    pos[r] = g[0];
+    len[r] = g[1];
+    need[r] = len[r] - pos[r] < (long long)(n_steps + 1) * b->per_step[r];
+    any |= need[r] != 0;
+  }
+  if ((long long)(n_steps + 1) * *std::max_element(b->per_step.begin(), b->per_step.end()) >
+      *std::min_element(b->cap.begin(), b->cap.end()))
+    return fail(PLUM_ERR_INPUT, "too many steps for one timing run");
+  if (any) {
+    CK(cudaMemcpyAsync(b->d_need, need.data(), sizeof(int) * R, cudaMemcpyHostToDevice, b->s));
+    CK(cudaMemcpyAsync(b->d_pos, pos.data(), sizeof(long long) * R, cudaMemcpyHostToDevice, b->s));
+    CK(cudaMemcpyAsync(b->d_len, len.data(), sizeof(long long) * R, cudaMemcpyHostToDevice, b->s));
+    launch_mt_fill_batch(b->d_states, b->d_outs, b->d_pos, b->d_len, b->d_cap, b->d_need,
+                         b->d_sts, R, b->s);
+  }
+  // events around every kernel of the steps (plain launches, no graph)
+  std::vector<cudaEvent_t> ev(2 * (4 * n_steps + 4));
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  int k = 0;
+  std::vector<std::pair<int, int>> marks;  // (kind, event index of the start)
+  auto timed = [&](int kind, auto&& launch) {
+    CK(cudaEventRecord(ev[k], b->s));
+    launch();
+    CK(cudaEventRecord(ev[k + 1], b->s));
+    marks.push_back({kind, k});
+    k += 2;
+    return PLUM_OK;
+  };
+  auto stage_one = [&]() {
+    if (!b->sg) return PLUM_OK;
+    int rc = timed(2, [&] { launch_desc_batch(b->d_rp, b->d_rb, R, b->d_desc, 1, b->s); });
+    if (rc) return rc;
+    return timed(3, [&] {
+      launch_mlp_infer_i(b->sg->net, b->d_desc, R, nullptr, DaArgs{b->d_sts, b->d_rp}, b->d_err,
+                         b->s);
+    });
+  };
+  int rc = timed(1, [&] {
+    launch_batch_serial(b->d_rp, b->d_rb, b->d_item_off, b->d_slots, R, kModeGen, b->s);
+  });
+  if (!rc) rc = stage_one();
+  for (int i = 0; i < n_steps && !rc; i++) {
+    rc = timed(0, [&] {
+      launch_batch_delta32(b->d_rp, b->d_rb, R, b->d_item_off, b->d_slots, b->kt_smem, b->s);
+    });
+    const int mode = kModeFinish | kModeDecide | (i + 1 < n_steps ? kModeGen : 0);
+    if (!rc)
+      rc = timed(1, [&] {
+        launch_batch_serial(b->d_rp, b->d_rb, b->d_item_off, b->d_slots, R, mode, b->s);
+      });
+    if (!rc && i + 1 < n_steps) rc = stage_one();
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(b->s));
+  double sum[4] = {0, 0, 0, 0};
+  int cnt[4] = {0, 0, 0, 0};
+  for (auto& m : marks) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev[m.second], ev[m.second + 1]);
+    sum[m.first] += ms;
+    cnt[m.first]++;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (rc) return rc;
+  for (int q = 0; q < 4; q++) out4[q] = cnt[q] ? sum[q] / cnt[q] : 0.0;
+  for (plum_ctx* c : b->reps) c->h_pos_valid = false;
   return PLUM_OK;
 }
 

@@ -207,6 +207,8 @@ void ForceField::Initialize(const std::string& dir, const std::string& runin_tex
     check(plum_type_name(ctx_, t, buf, sizeof buf));
     names[t] = buf;
   }
+  type_names_ = names;
+  if (run_.use_gc) check(plum_gc_info(ctx_, gc_));
   mols.assign(nm, Molecule());
   int id = 0;
   for (int m = 0; m < nm; m++)
@@ -251,6 +253,236 @@ double ForceField::TotPairEnergy() { return term(ctx_, 0); }
 double ForceField::TotEwaldEnergy() { return term(ctx_, 1); }
 double ForceField::TotBondEnergy() { return term(ctx_, 2); }
 double ForceField::TotExtEnergy() { return term(ctx_, 3); }
+
+// ------------------------------------------------- grand-canonical exchange
+double ForceField::Gasdev(double mean, double sd, std::mt19937& g) {
+  if (gd_iset_ == 0) {
+    double v1, v2, rsq;
+    do {
+      v1 = 2.0 * ((double)g() / kMax) - 1.0;
+      v2 = 2.0 * ((double)g() / kMax) - 1.0;
+      rsq = v1 * v1 + v2 * v2;
+    } while (rsq >= 1.0 || rsq == 0.0);
+    const double fac = std::sqrt(-2.0 * std::log(rsq) / rsq);
+    gd_gset_ = v1 * fac;
+    gd_iset_ = 1;
+    return v2 * fac * sd + mean;
+  }
+  gd_iset_ = 0;
+  return gd_gset_ * sd + mean;
+}
+
+double ForceField::RandomBondLen(std::mt19937& g) {
+  const double k = gc_[6], r0 = gc_[7];
+  const double sigma = std::sqrt(1 / (run_.beta * k));
+  const double a = (r0 + 3 * sigma) * (r0 + 3 * sigma);
+  double len = 0;
+  bool ready = false;
+  while (!ready) {
+    len = Gasdev(r0, sigma, g);
+    ready = ((double)g() / kMax < (len * len / a));
+  }
+  return len;
+}
+
+void ForceField::GCCounts(const std::vector<Molecule>& mols, int* spc1, int* spc2) const {
+  // ForceField::UpdateMolCounts (force_field.cc:1258-1277): neutral single
+  // beads count with the cations
+  int nc = 0, ncat = 0, nan = 0;
+  for (int m = run_.phantom; m < (int)mols.size(); m++) {
+    if (mols[m].Size() > 1)
+      nc++;
+    else if (mols[m].bds[0].Charge() >= 0)
+      ncat++;
+    else
+      nan++;
+  }
+  nc -= run_.grafted;
+  const double qb = gc_[2];
+  if (GCChainLen() > 1)
+    *spc1 = nc;
+  else if (qb >= 0)
+    *spc1 = ncat - run_.coion;
+  else
+    *spc1 = nan - run_.coion;
+  *spc2 = qb == 0 ? 0 : (qb > 0 ? nan : ncat);
+}
+
+// CBMCFGenTrialBeads (cbmc.cc:161-212): every trial's draws (bond length,
+// direction, the counterion's position) in the reference's order, then all
+// trials' energies in one device call. replace_first (deletion) stands for
+// trial 0 in the energies, as cbmc.cc:386-388 overwrites its weight.
+double ForceField::CBMCFGenTrialBeads(const double* end, int cl, std::mt19937& g, int delete_id,
+                                      const double* replace_first) {
+  const int T = (int)gc_[4], L = GCChainLen();
+  const bool charged = gc_[2] != 0;
+  tb1_.assign(3 * (size_t)T, 0.0);
+  tb2_.assign(3 * (size_t)T, 0.0);
+  w_.assign(T, 0.0);
+  u_.assign(T, 0.0);
+  for (int i = 0; i < T; i++) {
+    double bl = 0;
+    if (run_.use_bond)
+      bl = RandomBondLen(g);
+    else if (run_.use_bond_rigid)
+      bl = run_.rigid_bond;
+    double v[3];
+    rand_sphere(v, g);
+    for (int a = 0; a < 3; a++) tb1_[3 * i + a] = v[a] * bl + end[a];
+    if (charged)
+      for (int a = 0; a < 3; a++) tb2_[3 * i + a] = (double)g() / kMax * info_.box[a];
+  }
+  if (replace_first)
+    for (int a = 0; a < 3; a++) {
+      tb1_[a] = replace_first[a];
+      tb2_[a] = replace_first[3 + a];
+    }
+  check(plum_cbmc_trials(ctx_, T, tb1_.data(), charged ? tb2_.data() : nullptr, cl,
+                         cl > 0 ? chain_.data() : nullptr,
+                         (charged && cl > 0) ? chain_.data() + 3 * L : nullptr, delete_id,
+                         u_.data()));
+  double Wi = 0;
+  for (int i = 0; i < T; i++) {
+    w_[i] = std::exp(-run_.beta * u_[i]);
+    Wi += w_[i];
+  }
+  return Wi;
+}
+
+bool ForceField::CBMCFChainInsertion(std::vector<Molecule>& mols, std::mt19937& g) {
+  const int L = GCChainLen(), T = (int)gc_[4];
+  const double qb = gc_[2];
+  const bool charged = qb != 0;
+  chain_.assign(6 * (size_t)L, 0.0);
+  double weight = 1.0;
+  const int i_index = charged ? L : 0, initial = charged ? 2 : 1;
+  for (int i = 0; i < initial; i++)
+    for (int a = 0; a < 3; a++) chain_[3 * (i * L) + a] = (double)g() / kMax * info_.box[a];
+  double u0 = 0;
+  check(plum_cbmc_trials(ctx_, 1, chain_.data(), charged ? chain_.data() + 3 * i_index : nullptr,
+                         0, nullptr, nullptr, -1, &u0));
+  weight *= std::exp(-run_.beta * u0);
+  if (weight <= 0) return false;
+  for (int i = 1; i < L; i++) {
+    const double Wi = CBMCFGenTrialBeads(&chain_[3 * (i - 1)], i, g, -1, nullptr);
+    weight *= Wi / T;
+    if (weight <= 0) return false;
+    const double rn = (double)g() / kMax * Wi;
+    int cb = 0;
+    double cum = w_[0];
+    while (cum < rn && cb < T - 1) cum += w_[++cb];
+    for (int a = 0; a < 3; a++) chain_[3 * i + a] = tb1_[3 * cb + a];
+    if (charged)
+      for (int a = 0; a < 3; a++) chain_[3 * (i + L) + a] = tb2_[3 * cb + a];
+  }
+  int spc1, spc2;
+  GCCounts(mols, &spc1, &spc2);
+  const int spc2_add = charged ? L : 0;
+  double factorial = 1;
+  for (int i = spc1 + 1; i <= spc1 + 1; i++) factorial *= i;
+  for (int i = spc2 + 1; i <= spc2 + spc2_add; i++) factorial *= i;
+  const double vol = info_.box[0] * info_.box[1] * info_.box[2], deb = gc_[1];
+  double vol_over_lam = 1;
+  vol_over_lam *= std::pow(vol / (deb / std::pow((double)L, 1.5)), 1);
+  vol_over_lam *= std::pow(vol / (deb / std::pow(1.0, 1.5)), spc2_add);
+  const double C = vol_over_lam * (1.0 / factorial);
+  const double rn = (double)g() / kMax;
+  if (!(rn < (std::exp(run_.beta * gc_[0]) * weight) * C)) return false;
+  const std::string& sym = type_names_[(int)gc_[8]];
+  Molecule chain;
+  for (int i = 0; i < L; i++) {
+    Bead b(sym, -1, (int)mols.size(), qb, chain_[3 * i], chain_[3 * i + 1], chain_[3 * i + 2]);
+    b.SetType((int)gc_[8]);
+    chain.AddBead(b);
+  }
+  for (int i = 0; i + 1 < L; i++) chain.AddBond(i, i + 1);
+  mols.push_back(chain);
+  if (charged)
+    for (int i = 0; i < L; i++) {
+      Molecule ion;
+      Bead b(sym, -1, (int)mols.size(), -qb, chain_[3 * (i + L)], chain_[3 * (i + L) + 1],
+             chain_[3 * (i + L) + 2]);
+      b.SetType((int)gc_[8]);
+      ion.AddBead(b);
+      mols.push_back(ion);
+    }
+  return true;
+}
+
+int ForceField::CBMCFChainDeletion(std::vector<Molecule>& mols, std::mt19937& g) {
+  const int L = GCChainLen();
+  const double qb = gc_[2];
+  const bool charged = qb != 0;
+  int spc1, spc2;
+  GCCounts(mols, &spc1, &spc2);
+  int did = (int)std::floor((double)g() / kMax * spc1);
+  if (did >= spc1) did = spc1 - 1;
+  // nothing of the species to delete (the reference would index outside it)
+  if (did < 0) return -1;
+  did = run_.phantom + run_.coion + run_.grafted + run_.grafted_counterion +
+        (charged ? did * (1 + L) : did);
+  const int second = charged ? did + 1 : did;
+  if (second >= (int)mols.size() || mols[did].Size() < L) return -1;
+  chain_.assign(6 * (size_t)L, 0.0);
+  for (int a = 0; a < 3; a++) {
+    chain_[a] = mols[did].bds[0].GetCrd(0, a);
+    if (charged) chain_[3 * L + a] = mols[second].bds[0].GetCrd(0, a);
+  }
+  double u0 = 0;
+  check(plum_cbmc_trials(ctx_, 1, chain_.data(), charged ? chain_.data() + 3 * L : nullptr, 0,
+                         nullptr, nullptr, did, &u0));
+  double weight = std::exp(-run_.beta * u0);
+  for (int i = 1; i < L; i++) {
+    for (int a = 0; a < 3; a++) {
+      chain_[3 * i + a] = mols[did].bds[i].GetCrd(0, a);
+      if (charged) chain_[3 * (i + L) + a] = mols[did + i + 1].bds[0].GetCrd(0, a);
+    }
+    double rep[6];
+    for (int a = 0; a < 3; a++) {
+      rep[a] = chain_[3 * i + a];
+      rep[3 + a] = charged ? chain_[3 * (i + L) + a] : chain_[3 * i + a];
+    }
+    const double Wi = CBMCFGenTrialBeads(&chain_[3 * (i - 1)], i, g, did, rep);
+    weight *= Wi / (int)gc_[4];
+  }
+  const int spc2_del = charged ? L : 0;
+  double factorial = 1;
+  for (int i = spc1; i > spc1 - 1; i--) factorial *= i;
+  for (int i = spc2; i > spc2 - spc2_del; i--) factorial *= i;
+  const double vol = info_.box[0] * info_.box[1] * info_.box[2], deb = gc_[1];
+  double lam_over_vol = 1;
+  lam_over_vol *= std::pow((deb / std::pow((double)L, 1.5)) / vol, 1);
+  lam_over_vol *= std::pow((deb / std::pow(1.0, 1.5)) / vol, spc2_del);
+  const double C = lam_over_vol * factorial;
+  const double rn = (double)g() / kMax;
+  if (rn < C / (std::exp(run_.beta * gc_[0]) * weight)) return did;
+  return -1;
+}
+
+void ForceField::EnergyInitForAddedMolecule(std::vector<Molecule>& mols, int n_added) {
+  std::vector<int> sizes;
+  std::vector<double> xyz, q;
+  std::vector<int> type;
+  for (int m = (int)mols.size() - n_added; m < (int)mols.size(); m++) {
+    sizes.push_back(mols[m].Size());
+    for (const Bead& b : mols[m].bds) {
+      for (int a = 0; a < 3; a++) xyz.push_back(b.GetCrd(0, a));
+      q.push_back(b.Charge());
+      type.push_back(b.Type());
+    }
+  }
+  check(plum_append_molecules(ctx_, n_added, sizes.data(), xyz.data(), q.data(), type.data()));
+  for (int sz : sizes) mol_start_.push_back(mol_start_.back() + sz);
+  check(plum_ctx_info(ctx_, &info_));
+}
+
+void ForceField::AdjustEnergyUponMolDeletion(int first, int count) {
+  check(plum_erase_molecules(ctx_, first, count));
+  const int nb = mol_start_[first + count] - mol_start_[first];
+  mol_start_.erase(mol_start_.begin() + first + 1, mol_start_.begin() + first + count + 1);
+  for (size_t m = first + 1; m < mol_start_.size(); m++) mol_start_[m] -= nb;
+  check(plum_ctx_info(ctx_, &info_));
+}
 
 double ForceField::EqBondLen() const {
   if (!run_.use_bond) throw InputError("Illegal request of bond length");
@@ -354,8 +586,52 @@ void Simulation::TranslationalMove() {
   last_accept = accept;
 }
 
+void Simulation::GCMove() {
+  const bool insert = rand_gen() % 2;
+  last_move_type = insert ? 5 : 6;
+  last_accept = 0;
+  if (insert) {
+    if (step > run_.steps_eq) insertion_attempted++;
+    const int before = (int)mols.size();
+    if (force_field.CBMCFChainInsertion(mols, rand_gen)) {
+      if (step > run_.steps_eq) insertion_accepted++;
+      force_field.EnergyInitForAddedMolecule(mols, (int)mols.size() - before);
+      last_accept = 1;
+    }
+  } else {
+    if (step > run_.steps_eq) deletion_attempted++;
+    int deleted = -1;
+    if (n_mol - run_.phantom - run_.coion > 0) deleted = force_field.CBMCFChainDeletion(mols, rand_gen);
+    if (deleted >= run_.phantom + run_.coion) {
+      if (step > run_.steps_eq) deletion_accepted++;
+      int ions = 0;
+      for (const Bead& b : mols[deleted].bds) ions += (int)std::round(std::fabs(b.Charge()));
+      force_field.AdjustEnergyUponMolDeletion(deleted, 1 + ions);
+      mols.erase(mols.begin() + deleted, mols.begin() + deleted + 1 + ions);
+      last_accept = 1;
+    }
+  }
+  UpdateMolCounts();
+}
+
+void Simulation::Step() {
+  step++;
+  // simulation.cc:221-226: int rand_num = rand_gen(); exchange when
+  // rand_num % gc_freq == 0, with the reference's signed remainder
+  const int32_t rand_num = (int32_t)rand_gen();
+  if (force_field.UseGC() && force_field.GCFrequency() > 0 &&
+      rand_num % force_field.GCFrequency() == 0)
+    GCMove();
+  else
+    TranslationalMove();
+}
+
 void Simulation::RunSteps(long n) {
-  if (force_field.UseGC()) throw InputError("grand-canonical steps are not run by this loop");
+  if (force_field.UseGC()) {
+    // exchanges need host control flow; every step runs here
+    for (long i = 0; i < n; i++) Step();
+    return;
+  }
   int max_len = 1;
   for (auto& m : mols) max_len = std::max(max_len, m.Size());
   while (n > 0) {
@@ -471,6 +747,25 @@ int plum_sim_translational_moves(plum_sim* s, int n, int* move_type, int* accept
   } catch (const std::exception&) {
     return PLUM_ERR_STATE;
   }
+}
+
+int plum_sim_steps(plum_sim* s, int n, int* move_type, int* accept) {
+  try {
+    for (int i = 0; i < n; i++) {
+      s->s->Step();
+      if (move_type) move_type[i] = s->s->last_move_type;
+      if (accept) accept[i] = s->s->last_accept;
+    }
+    return PLUM_OK;
+  } catch (const std::exception&) {
+    return PLUM_ERR_STATE;
+  }
+}
+
+int plum_sim_n_bead(plum_sim* s) {
+  int n = 0;
+  for (auto& m : s->s->mols) n += m.Size();
+  return n;
 }
 
 int plum_sim_run_steps(plum_sim* s, long n) {

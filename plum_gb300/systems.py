@@ -420,6 +420,13 @@ class MuVTSpec:
     gc_freq: int = 2             # the reference draws insert/delete when rand % gc_freq == 0
     move_prob: tuple = (0.5, 0.1, 0.2, 0.0, 0.2)
     min_sep: float = 0.8
+    # Salt before the exchanged chains, declared as the run's "surface
+    # counterions" (coion). The reference's deletion indexes the exchanged
+    # species as the molecules after phantom + coion + grafted +
+    # grafted_counterion (cbmc.cc:340-346) while insertion appends at the end
+    # (cbmc.cc:294-312), so any other molecule after the chains is read as a
+    # chain once one has been inserted; exchange runs need this layout.
+    salt_first: bool = False
 
 
 def muvt_coordinates(spec: MuVTSpec, seed: int):
@@ -439,6 +446,16 @@ def muvt_coordinates(spec: MuVTSpec, seed: int):
                 return p
         raise RuntimeError("could not place a bead")
 
+    def salt():
+        nonlocal m
+        for i in range(spec.n_salt):
+            mol.append(m), sym.append("C"), xyz.append(place()), q.append(1.0)
+            m += 1
+            mol.append(m), sym.append("A"), xyz.append(place()), q.append(-1.0)
+            m += 1
+
+    if spec.salt_first:
+        salt()
     for c in range(spec.n_chain):
         for attempt in range(1000):
             p = rng.uniform(0, L, size=3)
@@ -470,11 +487,8 @@ def muvt_coordinates(spec: MuVTSpec, seed: int):
             for b in range(spec.chain_len):
                 mol.append(m), sym.append("P"), xyz.append(place()), q.append(-spec.bead_charge)
                 m += 1
-    for i in range(spec.n_salt):
-        mol.append(m), sym.append("C"), xyz.append(place()), q.append(1.0)
-        m += 1
-        mol.append(m), sym.append("A"), xyz.append(place()), q.append(-1.0)
-        m += 1
+    if not spec.salt_first:
+        salt()
     return np.array(mol), sym, np.array(xyz), np.array(q, dtype=np.float64)
 
 
@@ -490,7 +504,8 @@ def write_muvt(dirpath: str, spec: MuVTSpec, seed: int, runin="run.in", **over) 
     kw = dict(move_prob=spec.move_prob, lj_cutoff=spec.lj_cutoff,
               lj_table=(("P", 1.0, 1.0), ("C", 1.0, 1.0), ("A", 1.0, 1.0)), lB=spec.lB,
               alpha=(spec.alpha_times_L / spec.box) ** 2, k_bond=spec.k_bond, r0=spec.r0,
-              rigid=spec.r0, use_gc=True, gc=gc)
+              rigid=spec.r0, use_gc=True, gc=gc,
+              coion=2 * spec.n_salt if spec.salt_first else 0)
     kw.update(over)
     with open(os.path.join(dirpath, runin), "w") as f:
         f.write(runin_text(**kw))

@@ -16,9 +16,11 @@ input_crd.dat, input_top.dat) and ref.npz with, from the reference:
   rng_words     the reference generator's first outputs for run_seed
 
 Run from the repository root:  python tests/golden/make_golden.py
-[moves] [cbmc] [long | long:<case>] (needs the reference checkout; the
-fixtures themselves are committed). "long" adds long.npz, a 1e5-step run,
-to the cases in LONG_CASES (about 40 min each at the reference's speed).
+[moves] [cbmc] [long | long:<case>] [stats] [gc] (needs the reference checkout;
+the fixtures themselves are committed). "long" adds long.npz, a 1e5-step
+run, to the cases in LONG_CASES (about 40 min each at the reference's
+speed); "stats" writes the STAT_CASES with stats.npz, 8 seeded 6e4-step
+reference runs each (about 15 min on 8 cores).
 """
 from __future__ import annotations
 
@@ -164,6 +166,119 @@ def make_long_case(name, seed, steps=100000, every=100):
     print(name, "long run accept", out["run_accept"].mean())
 
 
+GC_CASES = {
+    "gcx_neutral": dict(seed=31, run_seed=5, steps=400, over={},
+                        spec=systems.MuVTSpec(box=12.0, n_chain=4, chain_len=6, n_salt=15,
+                                              trials=8, chem_pot=2.0, salt_first=True)),
+    # rigid bonds: with the spring potential on, the reference's per-molecule
+    # bond energy arrays gain one entry per inserted chain while a charged
+    # species adds 1 + L molecules (potential_bond.cc:29-41), so its later
+    # bookkeeping reads past their end
+    "gcx_charged": dict(seed=32, run_seed=5, steps=400, over={"use_bond": False},
+                        spec=systems.MuVTSpec(box=12.0, n_chain=3, chain_len=4, bead_charge=-1.0,
+                                              n_salt=8, trials=8, chem_pot=2.0,
+                                              salt_first=True)),
+}
+
+
+def _gc_run(name):
+    """One reference run with grand-canonical exchanges (a fresh worker
+    process: the reference keeps gasdev's cached deviate in statics)."""
+    import tempfile
+    cfg = GC_CASES[name]
+    src = os.path.join(HERE, name)
+    with tempfile.TemporaryDirectory() as d:
+        for f in ("run.in", "input_crd.dat", "input_top.dat"):
+            shutil.copy(os.path.join(src, f), os.path.join(d, f))
+        R = ob.Ref(d, seed=cfg["run_seed"])
+        mt, ac, dr, et = R.run(cfg["steps"])
+        out = dict(run_seed=np.array(cfg["run_seed"]), run_type=mt.astype(np.int8),
+                   run_accept=ac.astype(np.int8), run_draws=dr.astype(np.int32), run_etot=et,
+                   run_coords=R.coords(), run_n_mol=np.array(R.L.pr_n_mol(R.h)))
+        R.close()
+    return out
+
+
+def make_gc_cases():
+    """Grand-canonical runs (Simulation::GCMove with configurational-bias
+    insertion and deletion) of the reference: gc.npz with the move-type,
+    accept and draw-count sequences, running totals and final coordinates."""
+    import multiprocessing as mp
+    for name, cfg in GC_CASES.items():
+        d = os.path.join(HERE, name)
+        if os.path.isdir(d):
+            shutil.rmtree(d)
+        os.makedirs(d)
+        systems.write_muvt(d, cfg["spec"], seed=cfg["seed"], **cfg["over"])
+    with mp.get_context("spawn").Pool(len(GC_CASES)) as pool:
+        res = pool.map(_gc_run, list(GC_CASES))
+    for name, out in zip(GC_CASES, res):
+        np.savez_compressed(os.path.join(HERE, name, "gc.npz"), **out)
+        mt, ac = out["run_type"], out["run_accept"]
+        print(name, "exchanges", int((mt >= 5).sum()), "accepted", int(ac[mt >= 5].sum()),
+              "molecules", int(out["run_n_mol"]))
+
+
+STAT_CASES = {
+    "stat_bulk": dict(kind="bulk", seed=11,
+                      spec=systems.BulkSpec(n_chain=2, chain_len=10, n_ion=20, box=9.0)),
+    "stat_slab": dict(kind="brush", seed=12,
+                      spec=systems.BrushSpec(n_graft=3, chain_len=6, lxy=8.0, height=10.0,
+                                             n_sites=4, wall_cut=-1.0, charge_frac=0.7)),
+}
+STAT_SEEDS = [101, 102, 103, 104, 105, 106, 107, 108]
+STAT_STEPS, STAT_EVERY, STAT_BURN = 60000, 100, 10000
+
+
+def _stat_run(args):
+    """One seeded reference run of a statistics case (a worker process)."""
+    name, seed = args
+    import tempfile
+    src = os.path.join(HERE, name)
+    with tempfile.TemporaryDirectory() as d:
+        for f in ("run.in", "input_crd.dat", "input_top.dat"):
+            shutil.copy(os.path.join(src, f), os.path.join(d, f))
+        R = ob.Ref(d, seed=seed)
+        E, G, Z = [], [], []
+        for k in range(STAT_STEPS // STAT_EVERY):
+            _, _, _, et = R.run(STAT_EVERY)
+            E.append(et[-1])
+            G.append(R.observables()[0])
+            if (k + 1) * STAT_EVERY > STAT_BURN:
+                Z.append(coarse_rhoz(R.rhoz()))
+        R.close()
+    return np.array(E), np.array(G), np.mean(Z, axis=0)
+
+
+def make_stat_cases(workers=8):
+    """Equilibrium statistics of the reference: 8 independently seeded runs
+    of STAT_STEPS steps per case, sampled every STAT_EVERY steps (total
+    energy, chain-averaged Rg^2) and, after STAT_BURN steps, rho(z) averaged
+    per run in 1-sigma bins. stats.npz holds the series and per-run means."""
+    import multiprocessing as mp
+    for name, cfg in STAT_CASES.items():
+        d = os.path.join(HERE, name)
+        if os.path.isdir(d):
+            shutil.rmtree(d)
+        os.makedirs(d)
+        if cfg["kind"] == "bulk":
+            systems.write_bulk(d, cfg["spec"], seed=cfg["seed"])
+        else:
+            systems.write_brush(d, cfg["spec"], seed=cfg["seed"])
+    tasks = [(name, s) for name in STAT_CASES for s in STAT_SEEDS]
+    with mp.get_context("spawn").Pool(workers) as pool:
+        res = pool.map(_stat_run, tasks)
+    for name in STAT_CASES:
+        rows = [r for (n, _), r in zip(tasks, res) if n == name]
+        np.savez_compressed(os.path.join(HERE, name, "stats.npz"),
+                            seeds=np.array(STAT_SEEDS), steps=np.array(STAT_STEPS),
+                            every=np.array(STAT_EVERY), burn=np.array(STAT_BURN),
+                            energy=np.array([r[0] for r in rows]),
+                            rg2=np.array([r[1] for r in rows]),
+                            rhoz=np.array([r[2] for r in rows]))
+        print(name, "runs", len(rows))
+
+
 def make_case(name, cfg, n_de=24):
     d = os.path.join(HERE, name)
     if os.path.isdir(d):
@@ -233,3 +348,7 @@ if __name__ == "__main__":
     for name, seed in LONG_CASES.items():
         if "long" in which or "long:" + name in which:
             make_long_case(name, seed)
+    if "stats" in which:
+        make_stat_cases()
+    if "gc" in which:
+        make_gc_cases()

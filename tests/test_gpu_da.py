@@ -1,0 +1,115 @@
+"""Delayed acceptance with the learned surrogate in the replica batch.
+
+* Exactness: replicas equilibrated with the plain rule and continued with
+  and without delayed acceptance sample the same mean energy and Rg^2
+  (paired per replica, within 2.5 standard errors).
+* The zero network (s = 0) passes every move at stage one, so stage two is
+  the plain Metropolis rule: its counters give the plain method's chain
+  acceptance on the same replicas.
+* Gain: the trained network rejects most chain moves that the exact energy
+  change would reject before that change is computed; the test states how
+  many exact evaluations one accepted chain move costs with and without it.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from _cases import load
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import plum_gb300
+    plum_gb300.lib()
+    return plum_gb300
+
+
+@pytest.fixture(scope="module")
+def trained(pg):
+    from plum_gb300 import surrogate as S
+    d, _ = load("bulk_small")
+    desc, de, _ = S.collect(d, 40000, n_ctx=4, seed=300, moves_per_call=20000)
+    sg, st = S.fit(desc, de, epochs=40, batch=1024, lr=1e-3, seed=3)
+    return sg, st
+
+
+def test_surrogate_learns_the_energy_change(trained):
+    _, st = trained
+    assert st["rmse_vs_fp64"] < 0.8 * st["exact_std"], st
+
+
+def _lj_fluid(tmp):
+    """100 beads (4 LJ chains of 10 + 60 free beads, cut at 2.5 sigma, no
+    charges) in a box of 8 sigma: equilibrates within a few thousand steps."""
+    from plum_gb300 import systems
+    d = str(tmp / "lj_fluid")
+    systems.write_bulk(d, systems.BulkSpec(n_chain=4, chain_len=10, n_ion=60, box=8.0,
+                                           bead_charge=0.0, use_ewald=False), seed=41)
+    return d
+
+
+def test_delayed_acceptance_keeps_the_stationary_distribution(pg, tmp_path):
+    """Replicas equilibrated with the plain rule continue from the same
+    configurations with and without delayed acceptance (independent seeds):
+    per replica the mean energy and Rg^2 over the continuation differ by no
+    more than 2.5 standard errors of the paired differences. A surrogate that
+    broke detailed balance would shift the sampled distribution away from
+    the equilibrium both runs start in."""
+    from plum_gb300 import surrogate as S
+    d = _lj_fluid(tmp_path)
+    desc, de, _ = S.collect(d, 30000, n_ctx=4, seed=900, moves_per_call=20000)
+    sg, st = S.fit(desc, de, epochs=40, batch=1024, lr=1e-3, seed=4)
+    R, every, n = 64, 100, 200
+    a = pg.Batch([d] * R)
+    a.seed(np.arange(100, 100 + R, dtype=np.uint32))
+    a.run(20000)
+    snap = [a.replica(r).positions() for r in range(R)]
+    b = pg.Batch([d] * R)
+    b.seed(np.arange(5000, 5000 + R, dtype=np.uint32))
+    for r in range(R):
+        b.replica(r).set_positions(snap[r])
+    b.set_surrogate(sg)
+    ra = [a.replica(r) for r in range(R)]
+    rb = [b.replica(r) for r in range(R)]
+    ea, eb, ga, gb = (np.zeros((n, R)) for _ in range(4))
+    for k in range(n):
+        a.run(every)
+        b.run(every)
+        for r in range(R):
+            ea[k, r] = ra[r].energies().sum()
+            eb[k, r] = rb[r].energies().sum()
+            ga[k, r] = ra[r].observables()[0]
+            gb[k, r] = rb[r].observables()[0]
+    moves, passed, acc = b.da_stats()
+    assert moves > 0 and 0 < passed < moves and acc > 0
+    for name, x, y in (("energy", ea, eb), ("Rg2", ga, gb)):
+        diff = y.mean(axis=0) - x.mean(axis=0)
+        se = diff.std(ddof=1) / np.sqrt(R)
+        assert abs(diff.mean()) <= 2.5 * se, (name, diff.mean(), se, x.mean(), y.mean())
+
+
+def test_gain_over_the_method_without_the_network(pg, trained):
+    sg, st = trained
+    d, _ = load("bulk_small")
+    zero = pg.Surrogate(seed=1)
+    zero.set_params(np.zeros(zero.n_params, np.float32))
+    out = {}
+    for name, net in (("plain", zero), ("surrogate", sg)):
+        b = pg.Batch([d] * 16)
+        b.seed(500)
+        b.set_surrogate(net)
+        b.run(2000)
+        moves, passed, acc = b.da_stats()
+        out[name] = dict(moves=moves, passed=passed, accepted=acc,
+                         exact_per_accept=passed / max(acc, 1), chain_acc=acc / moves)
+        b.close()
+    p, s = out["plain"], out["surrogate"]
+    assert p["passed"] == p["moves"]  # s = 0: stage one never rejects
+    gain = p["exact_per_accept"] / s["exact_per_accept"]
+    print("delayed acceptance", out, "exact evaluations saved per accepted move x%.2f" % gain,
+          "rmse", st["rmse_vs_fp64"])
+    assert gain > 1.5
+    assert s["chain_acc"] > 0.5 * p["chain_acc"]
