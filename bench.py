@@ -130,6 +130,66 @@ def tau_int(x, c=5.0):
     return float(tau)
 
 
+def chain_rg2(pos, mol_start):
+    """Rg^2 of every chain (simulation.cc:406-434: (1/n^2) sum_{j<k} r_jk^2 on
+    unwrapped coordinates = mean squared distance from the centre of mass)."""
+    import numpy as np
+    sizes = np.diff(mol_start)
+    out = []
+    for n in np.unique(sizes[sizes > 1]):
+        starts = mol_start[:-1][sizes == n]
+        idx = starts[:, None] + np.arange(n)[None, :]
+        x = pos[idx]
+        out.append(((x - x.mean(axis=1, keepdims=True)) ** 2).sum(axis=2).mean(axis=1))
+    return np.concatenate(out)
+
+
+def tau_pooled(X, c=5.0):
+    """Integrated autocorrelation time (in samples) of many series at once
+    (columns of X): the autocorrelation is averaged over the columns, then
+    Sokal's window; when the window would pass a third of the series, an
+    exponential fitted to the decay to 1/e stands in (method says which)."""
+    import numpy as np
+    X = np.asarray(X, np.float64)
+    T = X.shape[0]
+    if T < 16:
+        return float("nan"), "too short"
+    Y = X - X.mean(axis=0, keepdims=True)
+    f = np.fft.rfft(Y, 2 * T, axis=0)
+    acf = np.fft.irfft(f * np.conj(f), axis=0)[:T].mean(axis=1)
+    acf /= np.arange(T, 0, -1)  # unbiased per lag
+    if acf[0] <= 0:
+        return float("nan"), "flat"
+    rho = acf / acf[0]
+    tau = 0.5
+    for w in range(1, T):
+        tau += rho[w]
+        if w >= c * tau:
+            if w <= T // 3:
+                return float(tau), "sokal"
+            break
+    k = int(np.argmax(rho < math.exp(-1.0)))
+    if k < 2:
+        return float("nan"), "no decay"
+    lags = np.arange(k)
+    slope = np.polyfit(lags, np.log(np.maximum(rho[:k], 1e-12)), 1)[0]
+    return float(-1.0 / slope), "exponential fit"
+
+
+def measure_tau(batch, mol_start, seconds, every):
+    """tau_int of the chains' Rg^2 in moves per replica, from every replica's
+    chains sampled every `every` steps for about `seconds`."""
+    import numpy as np
+    reps = [batch.replica(r) for r in range(batch.n)]
+    X, t_end = [], time.perf_counter() + seconds
+    while time.perf_counter() < t_end:
+        batch.run(every)
+        X.append(np.concatenate([chain_rg2(r.positions(), mol_start) for r in reps]))
+    tau, how = tau_pooled(np.array(X))
+    return {"tau_moves_per_replica": tau * every, "tau_samples": tau, "method": how,
+            "samples": len(X), "chains": len(X[0]) if X else 0, "moves_per_sample": every}
+
+
 def alg_flops_per_move(n_bead, mean_moved, n_k, frac_in_rc, mean_bonds):
     """Algorithmic FP32 work per attempted move, with the weights fixed before
     measuring: 20 per (moved, other) pair for distance and wrap, 8 per image
@@ -208,12 +268,16 @@ def main():
     ap.add_argument("--workload", default="bulk_20000_pinned")
     ap.add_argument("--moves-per-step", type=int, default=2000)
     ap.add_argument("--plain-moves-per-step", type=int, default=200)
-    ap.add_argument("--samples-seconds", type=float, default=0.0)
+    ap.add_argument("--samples-seconds", type=float, default=75.0,
+                    help="seconds of Rg sampling per form for tau_int (0: skip)")
     ap.add_argument("--cpu-moves", type=int, default=20)
     ap.add_argument("--ref-moves", type=int, default=10)
     ap.add_argument("--replicas", type=int, default=16,
                     help="replicas of the workload in the batched form (the chosen form)")
     ap.add_argument("--batch-steps", type=int, default=256)
+    ap.add_argument("--da-margin", type=float, default=12.0,
+                    help="delayed-acceptance dead zone in k_BT (stage one rejects only moves "
+                         "the surrogate puts above it)")
     ap.add_argument("--no-surrogate", action="store_true",
                     help="time the batched precision form without delayed acceptance")
     ap.add_argument("--only", default=None, choices=[None, "fp32", "fp64", "batch"],
@@ -277,6 +341,7 @@ def main():
     if os.path.exists(wpath) and not args.no_surrogate:
         from plum_gb300 import surrogate as S
         sg = S.load(wpath, device=local)
+        sg.set_margin(args.da_margin)
         z = np.load(wpath)
         sg_meta = {k: (z[k].item() if z[k].ndim == 0 else None) for k in z.files
                    if k not in ("params", "mu", "isd")}
@@ -316,9 +381,16 @@ def main():
         da = {"surrogate_moves": mv, "stage1_pass": ps / max(mv, 1),
               "surrogate_move_acceptance": ac / max(mv, 1),
               "exact_evaluations_skipped": (mv - ps) / float(R * BS * args.steps),
+              "margin_kT": args.da_margin,
               "weights": os.path.relpath(wpath, ROOT), "training": sg_meta}
     # per-kernel CUDA-event durations over a few more steps (plain launches)
     kern_ms = batch.time_kernels(32)
+
+    # Rg decorrelation of the chosen form's dynamics (delayed acceptance
+    # changes the acceptance of chain moves, hence tau in moves)
+    mol_start = s64.topology()[0]
+    tau_da = measure_tau(batch, mol_start, args.samples_seconds, 1000) \
+        if args.samples_seconds > 0 and sg is not None else None
 
     # the same replicas without the surrogate (FP32 + batched)
     batch.set_surrogate(None)
@@ -332,6 +404,10 @@ def main():
         nb_ms.append(batch.last_timing()[0])
     batched32 = R * BS / (statistics.mean(nb_ms) / 1e3)
     kern_ms_nb = batch.time_kernels(32)
+    # the plain Metropolis dynamics (the FP64 and FP32 forms share it: their
+    # decisions differ with the flip fraction below)
+    tau_plain = measure_tau(batch, mol_start, args.samples_seconds, 1000) \
+        if args.samples_seconds > 0 else None
 
     # precision form against FP64 on identical trial moves
     from plum_gb300 import precision
@@ -380,17 +456,19 @@ def main():
     achieved = W * evaluated / (kern_ms[0] / 1e3) / 1e12
 
     samples = None
-    if args.samples_seconds > 0:
-        every = 1000
-        rg = []
-        t_end = time.perf_counter() + args.samples_seconds
-        while time.perf_counter() < t_end:
-            s32.run(every)
-            rg.append(s32.observables()[0])
-        tau = tau_int(rg)
-        samples = {"tau_int_samples": tau, "moves_per_sample": every, "n_samples": len(rg),
-                   "fp32_samples_per_s": value / (every * 2 * tau) if tau == tau else None,
-                   "fp64_samples_per_s": plain / (every * 2 * tau) if tau == tau else None}
+    if tau_plain is not None:
+        tp = tau_plain["tau_moves_per_replica"]
+        td = tau_da["tau_moves_per_replica"] if tau_da else tp
+        chosen = value / (2 * td)
+        plain_s = plain / (2 * tp)
+        samples = {"definition": "moves/s / (2 tau_int), tau_int of the chains' Rg^2 in moves per "
+                                 "system (Sokal window, c = 5, autocorrelation pooled over all "
+                                 "chains of all replicas)",
+                   "tau_plain": tau_plain, "tau_chosen_form": tau_da,
+                   "plain_fp64_samples_per_s": plain_s,
+                   "batched_fp32_samples_per_s": batched32 / (2 * tp),
+                   "chosen_form_samples_per_s": chosen,
+                   "chosen_vs_plain_fp64": chosen / plain_s}
 
     cpu = None
     if rank == 0:

@@ -293,6 +293,10 @@ int plum_surrogate_set_params(plum_surrogate* sg, const float* params);
 int plum_surrogate_get_params(const plum_surrogate* sg, float* params);
 int plum_surrogate_set_norm(plum_surrogate* sg, const float* mu, const float* isd,
                             float y_scale);
+/* Delayed acceptance uses s' = sign(s) max(|s| - margin, 0) (default 0):
+ * still antisymmetric, so still exact; stage one then only rejects moves
+ * predicted to cost more than `margin` k_BT. */
+int plum_surrogate_set_margin(plum_surrogate* sg, float margin);
 /* s for n descriptors x [n][96] (host buffers; _device: device buffers). */
 int plum_surrogate_predict(plum_surrogate* sg, const float* x, long n, float* s_out);
 int plum_surrogate_predict_device(plum_surrogate* sg, const float* d_x, long n, float* d_s);

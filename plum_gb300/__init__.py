@@ -104,6 +104,7 @@ def lib():
         L.plum_surrogate_set_params.argtypes = [C.c_void_p, _fp]
         L.plum_surrogate_get_params.argtypes = [C.c_void_p, _fp]
         L.plum_surrogate_set_norm.argtypes = [C.c_void_p, _fp, _fp, C.c_float]
+        L.plum_surrogate_set_margin.argtypes = [C.c_void_p, C.c_float]
         L.plum_surrogate_predict.argtypes = [C.c_void_p, _fp, C.c_long, _fp]
         L.plum_surrogate_predict_device.argtypes = [C.c_void_p, C.c_void_p, C.c_long, C.c_void_p]
         L.plum_surrogate_grad.argtypes = [C.c_void_p, _fp, _fp, C.c_long, _fp]
@@ -343,6 +344,11 @@ class Surrogate:
         self.norm = (np.asarray(mu, np.float32), np.asarray(isd, np.float32), float(y_scale))
         _check(lib().plum_surrogate_set_norm(self.h, np.ascontiguousarray(mu, np.float32),
                                              np.ascontiguousarray(isd, np.float32), y_scale))
+
+    def set_margin(self, margin):
+        """Dead zone of delayed acceptance: s' = sign(s) max(|s| - margin, 0)."""
+        self.margin = float(margin)
+        _check(lib().plum_surrogate_set_margin(self.h, margin))
 
     def predict(self, x):
         x = np.ascontiguousarray(x, np.float32).reshape(-1, 96)

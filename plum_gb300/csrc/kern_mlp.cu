@@ -354,8 +354,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       DevState* st = da.sts[sample];
       if (st->pending && st->da_active) {
         const double u1 = st->da_u1;
-        st->da_s = (double)s;
-        st->da_skip = !(u1 < exp(-da.rp[sample].beta * (double)s));
+        const float m = net->da_margin;
+        const float sd = s > m ? s - m : (s < -m ? s + m : 0.0f);
+        st->da_s = (double)sd;
+        st->da_skip = !(u1 < exp(-da.rp[sample].beta * (double)sd));
       }
     }
   }
@@ -506,18 +508,18 @@ __global__ void k_mlp_pack(const float* __restrict__ param, MlpNet* __restrict__
 }
 
 // ------------------------------------------------------------ descriptor
-// k_desc counts pairs in fine distance bins. Work items are (replica, tile of
-// up to 32 moved beads, chunk of 1024 other beads): the tile's current and
-// trial positions sit in shared memory and each thread holds 4 other beads,
-// so each load serves 32 pairs; a pair within the cut adds one to the
-// block's count of its (channel, fine bin) in shared memory, and the block's
-// counts go to the replica's desc_fine at the end of the item. k_desc_fin
-// then smears the counts into the 96 descriptor bins with integer weights.
+// k_desc counts pairs in fine distance bins. A work item is (replica, 256
+// other beads, up to 32 moved beads): one other bead per thread, run against
+// the item's moved beads, whose current and trial positions sit in shared
+// memory (all of a replica's, loaded once per replica a block visits), in a
+// loop with no barrier; items of equal size keep the blocks balanced. A pair within
+// the cut adds one to the block's count of its (channel, fine bin) in shared
+// memory; the counts go to the replica's desc_fine when the block moves on.
+// k_desc_fin smears them into the 96 descriptor bins with integer weights.
 // Integer counts and sums make both independent of the order.
 constexpr int kDescThreads = 256;
-constexpr int kDescTile = 32;                   // moved beads per item
-constexpr int kDescPer = 4;                     // other beads per thread
-constexpr int kDescChunk = kDescThreads * kDescPer;
+constexpr int kDescMaxMoved = 512;  // longest molecule (the pivot move's limit)
+constexpr int kDescSlab = 32;       // moved beads per work item
 
 // FP64 positions: one FP64 subtraction per axis, the periodic wrap in FP32
 // (the descriptor only uses pairs within 7.5 sigma, far from the half-box
@@ -528,32 +530,45 @@ __device__ __forceinline__ float wrap32(double d, float L, float invL, bool peri
 }
 
 // A bead position as the descriptor kernel keeps it: form 1 the fixed-point
-// mirror (x, y, z, type), form 0 FP64 (x, y, z) and the type.
-struct DPos {
+// mirror (x, y, z, type); form 0 FP64 (x, y, z) and the type.
+template <int kForm>
+struct DPos;
+template <>
+struct DPos<1> {
   int4 f;
+};
+template <>
+struct DPos<0> {
   double x, y, z;
+  int type;
 };
 
 template <int kForm>
-__device__ __forceinline__ DPos load_pos(const DevBuffers& B, int i, int ii, bool trial) {
-  DPos p;
-  if (kForm == 1) {
+__device__ __forceinline__ DPos<kForm> load_pos(const DevBuffers& B, int i, int ii, bool trial) {
+  DPos<kForm> p;
+  if constexpr (kForm == 1) {
     p.f = trial ? B.ftrial[ii] : B.fpos[i];
-    p.x = p.y = p.z = 0.0;
   } else {
     const double4_32a q = trial ? B.trial[i] : B.pos[i];
     p.x = q.x;
     p.y = q.y;
     p.z = q.z;
-    p.f = make_int4(0, 0, 0, B.type[i]);
+    p.type = B.type[i];
   }
   return p;
 }
 
 template <int kForm>
-__device__ __forceinline__ float dist2(const DevParams& P, const DPos& a, const DPos& b) {
+__device__ __forceinline__ int ptype(const DPos<kForm>& p) {
+  if constexpr (kForm == 1) return p.f.w;
+  else return p.type;
+}
+
+template <int kForm>
+__device__ __forceinline__ float dist2(const DevParams& P, const DPos<kForm>& a,
+                                       const DPos<kForm>& b) {
   float dx, dy, dz;
-  if (kForm == 1) {
+  if constexpr (kForm == 1) {
     dx = (float)(int)((unsigned)b.f.x - (unsigned)a.f.x) * P.f_scale[0];
     dy = (float)(int)((unsigned)b.f.y - (unsigned)a.f.y) * P.f_scale[1];
     dz = (float)(int)((unsigned)b.f.z - (unsigned)a.f.z) * P.f_scale[2];
@@ -565,22 +580,43 @@ __device__ __forceinline__ float dist2(const DevParams& P, const DPos& a, const 
   return dx * dx + dy * dy + dz * dz;
 }
 
+// Per-axis pre-test: a pair can only be within the cut when every axis
+// difference is; in fixed point that is one integer subtraction and compare
+// per axis (no conversion), and most pairs fail on the first axis. The
+// integer bound is one unit above the cut; boxes shorter than twice the cut
+// get no bound on that axis.
+template <int kForm>
+__device__ __forceinline__ bool near_axis(const DPos<kForm>& a, const DPos<kForm>& b, int axis,
+                                          const int* icut, const float* fcut,
+                                          const DevParams& P) {
+  if constexpr (kForm == 1) {
+    const unsigned ua = axis == 0 ? a.f.x : (axis == 1 ? a.f.y : a.f.z);
+    const unsigned ub = axis == 0 ? b.f.x : (axis == 1 ? b.f.y : b.f.z);
+    const int d = (int)(ub - ua);
+    return abs(d) <= icut[axis];
+  } else {
+    const double da = axis == 0 ? b.x - a.x : (axis == 1 ? b.y - a.y : b.z - a.z);
+    const float f = wrap32(da, (float)P.box[axis], (float)P.inv_box[axis], P.npbc > axis);
+    return fabsf(f) <= fcut[axis];
+  }
+}
+
 template <int kForm>
 __global__ void __launch_bounds__(kDescThreads)
     k_desc(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb, int n_rep) {
+  __shared__ int s_icut[3];
+  __shared__ float s_fcut[3];
   __shared__ unsigned fh[kFineAll];
-  __shared__ DPos tile[2][kDescTile];  // [current | trial] of the moved beads
+  __shared__ DPos<kForm> mcur[kDescMaxMoved], mtri[kDescMaxMoved];  // the moved beads
   __shared__ int s_pref[kMaxReplicas + 1];
-  __shared__ int s_nc[kMaxReplicas];   // other-bead chunks per replica
   __shared__ DevParams P;
   __shared__ DevBuffers B;
   __shared__ int s_bl[2];
   for (int r = threadIdx.x; r < n_rep; r += blockDim.x) {
     const DevState* st = rb[r].state;
-    const int m = (st->pending && st->da_active) ? st->b_hi - st->b_lo : 0;
-    const int nc = (rp[r].n_bead + kDescChunk - 1) / kDescChunk;
-    s_nc[r] = nc;
-    s_pref[r + 1] = ((m + kDescTile - 1) / kDescTile) * nc;
+    const int m = (st->pending && st->da_active) ? min(st->b_hi - st->b_lo, kDescMaxMoved) : 0;
+    s_pref[r + 1] = ((rp[r].n_bead + kDescThreads - 1) / kDescThreads) *
+                    ((m + kDescSlab - 1) / kDescSlab);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -592,6 +628,12 @@ __global__ void __launch_bounds__(kDescThreads)
   const int it0 = (int)((long long)T * blockIdx.x / gridDim.x);
   const int it1 = (int)((long long)T * (blockIdx.x + 1) / gridDim.x);
   int cur = -1;
+  // the block's counts go to a replica's desc_fine when the block moves on
+  // to the next replica and at the end
+  auto flush = [&]() {
+    for (int k = threadIdx.x; k < kFineAll; k += blockDim.x)
+      if (fh[k]) atomicAdd(&B.desc_fine[k], fh[k]);
+  };
   for (int item = it0; item < it1; item++) {
     int lo = 0, hi = n_rep - 1;
     while (lo < hi) {
@@ -599,8 +641,10 @@ __global__ void __launch_bounds__(kDescThreads)
       if (s_pref[mid] <= item) lo = mid; else hi = mid - 1;
     }
     const int r = lo;
-    __syncthreads();
     if (r != cur) {
+      __syncthreads();
+      if (cur >= 0) flush();
+      __syncthreads();
       const int* src = reinterpret_cast<const int*>(rp + r);
       int* dst = reinterpret_cast<int*>(&P);
       for (int i = threadIdx.x; i < (int)(sizeof(DevParams) / sizeof(int)); i += blockDim.x)
@@ -613,53 +657,61 @@ __global__ void __launch_bounds__(kDescThreads)
         s_bl[0] = rb[r].state->b_lo;
         s_bl[1] = rb[r].state->b_hi;
       }
+      if (threadIdx.x < 3) {
+        const int a = threadIdx.x;
+        const double unit = rp[r].ebox[a] / 4294967296.0;
+        const double lim = kDescCut / unit + 1.0;
+        s_icut[a] = lim < 2147483000.0 ? (int)lim : 2147483647;
+        s_fcut[a] = kDescCut * 1.0001f;
+      }
+      for (int k = threadIdx.x; k < kFineAll; k += blockDim.x) fh[k] = 0u;
+      __syncthreads();
+      const int m = min(s_bl[1] - s_bl[0], kDescMaxMoved);
+      for (int q = threadIdx.x; q < m; q += blockDim.x) {
+        mcur[q] = load_pos<kForm>(B, s_bl[0] + q, q, false);
+        mtri[q] = load_pos<kForm>(B, s_bl[0] + q, q, true);
+      }
+      __syncthreads();
+      cur = r;
     }
-    for (int k = threadIdx.x; k < kFineAll; k += blockDim.x) fh[k] = 0u;
-    __syncthreads();
-    cur = r;
-    const int b_lo = s_bl[0], b_hi = s_bl[1], N = P.n_bead;
-    const int local = item - s_pref[r], nc = s_nc[r];
-    const int t0 = b_lo + (local / nc) * kDescTile;
-    const int nt = min(kDescTile, b_hi - t0);
-    const int j0 = (local % nc) * kDescChunk;
-    for (int k = threadIdx.x; k < 2 * kDescTile; k += blockDim.x) {
-      const int w = k / kDescTile, q = k % kDescTile;
-      if (q < nt) tile[w][q] = load_pos<kForm>(B, t0 + q, t0 + q - b_lo, w == 1);
-    }
-    // this thread's other beads (current and, when moved, trial positions)
-    DPos jc[kDescPer], jt[kDescPer];
-    int jidx[kDescPer];
-#pragma unroll
-    for (int u = 0; u < kDescPer; u++) {
-      const int j = j0 + threadIdx.x + u * kDescThreads;
-      jidx[u] = j < N ? j : -1;
-      const int js = j < N ? j : 0;
-      const bool jm = js >= b_lo && js < b_hi;
-      jc[u] = load_pos<kForm>(B, js, 0, false);
-      jt[u] = jm ? load_pos<kForm>(B, js, js - b_lo, true) : jc[u];
-    }
-    __syncthreads();
-    for (int q = 0; q < nt; q++) {
-      const int i = t0 + q;
-      const DPos ic = tile[0][q], it = tile[1][q];
-#pragma unroll
-      for (int u = 0; u < kDescPer; u++) {
-        const int j = jidx[u];
-        const bool jm = j >= b_lo && j < b_hi;
-        if (j < 0 || j == i || (jm && j < i)) continue;
-        const int cls = ic.f.w == jc[u].f.w ? 0 : 1;
-        const float r0 = dist2<kForm>(P, ic, jc[u]);
-        const float r1 = dist2<kForm>(P, it, jt[u]);
-        if (r0 < kDescCut * kDescCut)
-          atomicAdd(&fh[cls * kFine + (int)(sqrtf(r0) * (float)kFinePerSigma + 0.5f)], 1u);
-        if (r1 < kDescCut * kDescCut)
-          atomicAdd(&fh[(2 + cls) * kFine + (int)(sqrtf(r1) * (float)kFinePerSigma + 0.5f)], 1u);
+    const int b_lo = s_bl[0], m = min(s_bl[1] - b_lo, kDescMaxMoved), N = P.n_bead;
+    const int n_chunks = (N + kDescThreads - 1) / kDescThreads;
+    const int local = item - s_pref[r];
+    const int q0 = (local / n_chunks) * kDescSlab, q1 = min(m, q0 + kDescSlab);
+    const int j = (local % n_chunks) * kDescThreads + threadIdx.x;
+    if (j < N) {
+      const bool jm = j >= b_lo && j < b_lo + m;
+      const DPos<kForm> jc = load_pos<kForm>(B, j, 0, false);
+      const DPos<kForm> jt = jm ? load_pos<kForm>(B, j, j - b_lo, true) : jc;
+      const int tj = ptype<kForm>(jc);
+      // moved pairs count once: j moved pairs only with moved i < j
+      const int q_end = jm ? min(q1, j - b_lo) : q1;
+      for (int q = q0; q < q_end; q++) {
+        const DPos<kForm> ic = mcur[q];
+        const DPos<kForm> it = mtri[q];
+        bool nb = near_axis<kForm>(ic, jc, 0, s_icut, s_fcut, P);
+        bool na = near_axis<kForm>(it, jt, 0, s_icut, s_fcut, P);
+        if (!(nb || na)) continue;
+        nb = nb && near_axis<kForm>(ic, jc, 1, s_icut, s_fcut, P);
+        na = na && near_axis<kForm>(it, jt, 1, s_icut, s_fcut, P);
+        if (!(nb || na)) continue;
+        const int cls = ptype<kForm>(ic) == tj ? 0 : 1;
+        if (nb) {
+          const float r0 = dist2<kForm>(P, ic, jc);
+          if (r0 < kDescCut * kDescCut)
+            atomicAdd(&fh[cls * kFine + (int)(sqrtf(r0) * (float)kFinePerSigma + 0.5f)], 1u);
+        }
+        if (na) {
+          const float r1 = dist2<kForm>(P, it, jt);
+          if (r1 < kDescCut * kDescCut)
+            atomicAdd(&fh[(2 + cls) * kFine + (int)(sqrtf(r1) * (float)kFinePerSigma + 0.5f)],
+                      1u);
+        }
       }
     }
-    __syncthreads();
-    for (int k = threadIdx.x; k < kFineAll; k += blockDim.x)
-      if (fh[k]) atomicAdd(&B.desc_fine[k], fh[k]);
   }
+  __syncthreads();
+  if (cur >= 0) flush();
 }
 
 // One block per replica: bin k of channel c = sum_f count[c][f] *
@@ -757,8 +809,8 @@ void launch_mlp_pack(const float* param, MlpNet* net, cudaStream_t st) {
 void launch_desc_batch(const DevParams* rp, const DevBuffers* rb, int n_rep, unsigned* acc,
                        int form, cudaStream_t st) {
   (void)acc;
-  if (form) k_desc<1><<<2 * 152, kDescThreads, 0, st>>>(rp, rb, n_rep);
-  else k_desc<0><<<2 * 152, kDescThreads, 0, st>>>(rp, rb, n_rep);
+  if (form) k_desc<1><<<4 * 152, kDescThreads, 0, st>>>(rp, rb, n_rep);
+  else k_desc<0><<<4 * 152, kDescThreads, 0, st>>>(rp, rb, n_rep);
   k_desc_fin<<<n_rep, 128, 0, st>>>(rb);
 }
 

@@ -59,6 +59,10 @@ struct MlpNet {
   float b1[mlp::kHid], b2[mlp::kHid];
   float mu[mlp::kIn], isd[mlp::kIn];
   float b3, y_scale;
+  // delayed acceptance uses s' = sign(s) max(|s| - da_margin, 0): odd in s,
+  // so still antisymmetric; stage one then rejects only moves predicted to
+  // cost more than da_margin k_BT
+  float da_margin;
 };
 
 // Delayed-acceptance hook of the inference kernel: when sts is set, sample r

@@ -112,9 +112,11 @@ int plum_surrogate_create(int device, unsigned long long seed, plum_surrogate** 
   fill(mlp::kOffW1, mlp::kNW1, mlp::kIn, mlp::kHid);
   fill(mlp::kOffW2, mlp::kNW2, mlp::kHid, mlp::kHid);
   fill(mlp::kOffW3, mlp::kHid, mlp::kHid, 1);
-  cudaMemset(g->m, 0, sizeof(float) * mlp::kNParam);
-  cudaMemset(g->v, 0, sizeof(float) * mlp::kNParam);
-  cudaMemset(g->d_err, 0, sizeof(int));
+  // on the surrogate's own (non-blocking) stream, ordered before the copies below
+  cudaMemsetAsync(g->m, 0, sizeof(float) * mlp::kNParam, g->s);
+  cudaMemsetAsync(g->v, 0, sizeof(float) * mlp::kNParam, g->s);
+  cudaMemsetAsync(g->d_err, 0, sizeof(int), g->s);
+  cudaMemsetAsync(g->net, 0, sizeof(MlpNet), g->s);
   std::vector<float> mu(mlp::kIn, 0.0f), isd(mlp::kIn, 1.0f);
   rc = plum_surrogate_set_norm(g, mu.data(), isd.data(), 1.0f);
   if (!rc) rc = plum_surrogate_set_params(g, p.data());
@@ -173,6 +175,15 @@ int plum_surrogate_set_norm(plum_surrogate* g, const float* mu, const float* isd
                       sizeof(float), cudaMemcpyHostToDevice, g->s));
   SCK(cudaStreamSynchronize(g->s));
   g->y_scale = y_scale;
+  return PLUM_OK;
+}
+
+int plum_surrogate_set_margin(plum_surrogate* g, float margin) {
+  if (!g || !(margin >= 0.0f)) return plum::fail_msg(PLUM_ERR_INPUT, "bad argument");
+  cudaSetDevice(g->device);
+  SCK(cudaMemcpyAsync(reinterpret_cast<char*>(g->net) + offsetof(MlpNet, da_margin), &margin,
+                      sizeof(float), cudaMemcpyHostToDevice, g->s));
+  SCK(cudaStreamSynchronize(g->s));
   return PLUM_OK;
 }
 
