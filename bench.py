@@ -249,6 +249,18 @@ def make_workload(name, seed=20261203):
     return d
 
 
+def make_brush_ensemble(n, seed=20261203):
+    """The confined-brush replicas of uneven size (systems.brush_ensemble)."""
+    from plum_gb300 import systems
+    dirs = []
+    for i, spec in enumerate(systems.brush_ensemble(n, seed)):
+        d = os.path.join(tempfile.gettempdir(), "plum_bench_brush_%d_%d" % (seed, i))
+        if not os.path.exists(os.path.join(d, "run.in")):
+            systems.write_brush(d, spec, seed=seed + i)
+        dirs.append(d)
+    return dirs
+
+
 def cpu_baseline_sample(d, moves):
     code = ("import sys,time; sys.path.insert(0,%r)\n"
             "from oracle import bindings as ob\n"
@@ -299,6 +311,33 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
+    if args.only == "batch":
+        if args.workload.startswith("brush_"):
+            dirs = make_brush_ensemble(int(args.workload.split("_")[1]))
+        else:
+            dirs = [make_workload(args.workload, seed=20261203 + r) for r in range(args.replicas)]
+        t0 = time.perf_counter()
+        b = pg.Batch(dirs, device=local)
+        setup_s = time.perf_counter() - t0
+        b.seed(77)
+        tune = b.autotune(8)
+        for _ in range(args.warmup):
+            b.run(args.batch_steps)
+        ms_all = []
+        for _ in range(args.steps):
+            b.run(args.batch_steps)
+            ms_all.append(b.last_timing()[0])
+        ms = statistics.mean(ms_all)
+        n_bead = sum(b.replica(r).n_bead for r in range(len(dirs)))
+        print(json.dumps({"profile_run": "batch", "workload": args.workload,
+                          "replicas": len(dirs), "beads_total": int(n_bead),
+                          "steps": args.batch_steps, "ms_per_batch": ms,
+                          "moves_per_s": len(dirs) * args.batch_steps / (ms / 1e3),
+                          "autotuned_items": tune, "setup_s": setup_s,
+                          "kernel_ms_per_launch": dict(zip(
+                              ("delta", "serial", "descriptor", "inference"),
+                              [float(x) for x in b.time_kernels(8)]))}), flush=True)
+        return 0
     d = make_workload(args.workload)
     M = args.moves_per_step
     s32 = pg.System(d, form=pg.FORM_FP32, device=local)
@@ -308,18 +347,7 @@ def main():
     s64.seed(1234 + rank)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
-    if args.only == "batch":
-        b = pg.Batch([make_workload(args.workload, seed=20261203 + r) for r in range(args.replicas)],
-                     device=local)
-        b.seed(77)
-        for _ in range(args.warmup + args.steps):
-            b.run(args.batch_steps)
-        ms, k = b.last_timing()
-        print(json.dumps({"profile_run": "batch", "replicas": args.replicas,
-                          "steps": args.batch_steps, "last_ms": ms,
-                          "moves_per_s": args.replicas * args.batch_steps / (ms / 1e3)}),
-              flush=True)
-        return 0
+
     if args.only:
         s = s32 if args.only == "fp32" else s64
         for _ in range(args.warmup + args.steps):
@@ -346,6 +374,8 @@ def main():
         sg_meta = {k: (z[k].item() if z[k].ndim == 0 else None) for k in z.files
                    if k not in ("params", "mu", "isd")}
         batch.set_surrogate(sg)
+    # work-item sizes of the batched energy change, timed on these replicas
+    tune = batch.autotune(16)
     for _ in range(args.warmup):
         batch.run(BS)
         s32.run(M)
@@ -493,7 +523,9 @@ def main():
                    "form": "batched replicas, precision form (FP32 pair/k, FP64 S(k) and "
                            "totals, FP64 recompute every 1e4 moves)" +
                            (", delayed acceptance with the learned surrogate" if sg else ""),
-                   "l2": "flushed between steps (256 MB write)", "parallelism": "replicas"},
+                   "l2": "flushed between steps (256 MB write)", "parallelism": "replicas",
+                   "autotuned_items": {"pairs_per_item": tune[0], "k_per_tile": tune[1],
+                                       "grid": tune[2]}},
         "batched_fp32_no_surrogate": {"value": batched32, "unit": "moves/s",
                                       "ms_per_step": statistics.mean(nb_ms)},
         "delayed_acceptance": da,

@@ -266,6 +266,15 @@ int plum_batch_last_timing(const plum_batch* batch, double* ms, long* kernels);
  * inference} (0 for kernels that did not run). For measurement; the steps
  * count as ordinary steps of the replicas. */
 int plum_batch_time_kernels(plum_batch* batch, int n_steps, double* out4);
+/* Work items of the batched energy change: (moved, other) pairs per pair
+ * item (>= 1024, a multiple of 256), k-vectors per k item (64..256) and
+ * the grid (0: 4 blocks per SM). */
+int plum_batch_set_tune(plum_batch* batch, int item_pairs, int k_tile, int grid);
+/* Times the energy-change kernel on these replicas (`steps` steps per
+ * candidate, see plum_batch_time_kernels) for item sizes {2048, 4096, 8192,
+ * 16384} x k tiles {128, 256} x grids {2, 4, 8} blocks per SM, keeps the
+ * fastest; out3 (may be NULL) = the chosen {item_pairs, k_tile, grid}. */
+int plum_batch_autotune(plum_batch* batch, int steps, int* out3);
 
 /* ---------------------------------------------------------------------
  * Learned surrogate and delayed acceptance. No counterpart in the

@@ -1404,6 +1404,7 @@ struct plum_batch {
   int* d_item_off = nullptr;
   double* d_slots = nullptr;
   size_t kt_smem = 0;
+  BatchTune tune{4096, 128, 0};
   // per-replica streams
   std::vector<long long> cap, per_step;
   uint32_t** d_states = nullptr;
@@ -1443,7 +1444,8 @@ void batch_enqueue(plum_batch* b, int steps) {
   launch_batch_serial(b->d_rp, b->d_rb, b->d_item_off, b->d_slots, R, kModeGen, b->s);
   stage_one();
   for (int i = 0; i < steps; i++) {
-    launch_batch_delta32(b->d_rp, b->d_rb, R, b->d_item_off, b->d_slots, b->kt_smem, b->s);
+    launch_batch_delta32(b->d_rp, b->d_rb, R, b->d_item_off, b->d_slots, b->kt_smem, b->tune,
+                           b->s);
     int mode = kModeFinish | kModeDecide | (i + 1 < steps ? kModeGen : 0);
     launch_batch_serial(b->d_rp, b->d_rb, b->d_item_off, b->d_slots, R, mode, b->s);
     if (i + 1 < steps) stage_one();
@@ -1551,7 +1553,8 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
     hst[r] = c->d_mt;
     hout[r] = c->d_stream;
     hsts[r] = c->B.state;
-    items += ((long long)c->max_len * P.n_bead + 4095) / 4096 + (P.n_k + 127) / 128;
+    items += ((long long)c->max_len * P.n_bead + kMinItemPairs - 1) / kMinItemPairs +
+             (P.n_k + kMinKTile - 1) / kMinKTile;
     size_t sm = P.use_ewald ? (size_t)P.kchunk_delta * 2 * P.kper * sizeof(float2) : 0;
     b->kt_smem = std::max(b->kt_smem, sm);
   }
@@ -1749,7 +1752,8 @@ int plum_batch_time_kernels(plum_batch* b, int n_steps, double* out4) {
   if (!rc) rc = stage_one();
   for (int i = 0; i < n_steps && !rc; i++) {
     rc = timed(0, [&] {
-      launch_batch_delta32(b->d_rp, b->d_rb, R, b->d_item_off, b->d_slots, b->kt_smem, b->s);
+      launch_batch_delta32(b->d_rp, b->d_rb, R, b->d_item_off, b->d_slots, b->kt_smem, b->tune,
+                           b->s);
     });
     const int mode = kModeFinish | kModeDecide | (i + 1 < n_steps ? kModeGen : 0);
     if (!rc)
@@ -1772,6 +1776,48 @@ int plum_batch_time_kernels(plum_batch* b, int n_steps, double* out4) {
   if (rc) return rc;
   for (int q = 0; q < 4; q++) out4[q] = cnt[q] ? sum[q] / cnt[q] : 0.0;
   for (plum_ctx* c : b->reps) c->h_pos_valid = false;
+  return PLUM_OK;
+}
+
+int plum_batch_set_tune(plum_batch* b, int item_pairs, int k_tile, int grid) {
+  if (!b || item_pairs < kMinItemPairs || item_pairs % 256 || k_tile < kMinKTile ||
+      k_tile > kPairThreads || grid < 0 || grid > 65535)
+    return fail(PLUM_ERR_INPUT, "bad work-item sizes");
+  b->tune = BatchTune{item_pairs, k_tile, grid};
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->g_steps = 0;
+  return PLUM_OK;
+}
+
+int plum_batch_autotune(plum_batch* b, int steps, int* out3) {
+  if (!b || steps <= 0) return fail(PLUM_ERR_INPUT, "bad argument");
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+  const int pairs[] = {2048, 4096, 8192, 16384};
+  const int ktiles[] = {128, 256};
+  const int grids[] = {2 * sms, 4 * sms, 8 * sms};
+  double best = 1e300;
+  BatchTune pick = b->tune;
+  for (int ip : pairs)
+    for (int kt : ktiles)
+      for (int g : grids) {
+        b->tune = BatchTune{ip, kt, g};
+        double ms[4];
+        int rc = plum_batch_time_kernels(b, steps, ms);
+        if (rc) return rc;
+        if (ms[0] < best) {
+          best = ms[0];
+          pick = b->tune;
+        }
+      }
+  int rc = plum_batch_set_tune(b, pick.item_pairs, pick.k_tile, pick.grid);
+  if (rc) return rc;
+  if (out3) {
+    out3[0] = pick.item_pairs;
+    out3[1] = pick.k_tile;
+    out3[2] = pick.grid;
+  }
   return PLUM_OK;
 }
 

@@ -202,8 +202,16 @@ int cbmc_trials_noalloc(const DevParams& P, const DevBuffers& B, cudaStream_t s,
 
 // batched replicas (kern_fp32.cu / kern_moves.cu)
 constexpr int kMaxReplicas = 2048;
+// Work-item sizes of the batched energy change (k_tile <= kPairThreads).
+struct BatchTune {
+  int item_pairs;  // (moved, other) pairs per pair item
+  int k_tile;      // k-vectors per k item
+  int grid;        // blocks (0: 4 per SM)
+};
+constexpr int kMinItemPairs = 1024;  // smallest item the slot buffers are sized for
+constexpr int kMinKTile = 64;
 void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, int* item_off,
-                          double* slots, size_t smem, cudaStream_t s);
+                          double* slots, size_t smem, BatchTune tune, cudaStream_t s);
 void launch_batch_serial(const DevParams* rp, const DevBuffers* rb, const int* item_off,
                          const double* slots, int n_rep, int mode, cudaStream_t s);
 // per replica r: if need[r], shift the unread words [pos[r], len[r]) of out[r]

@@ -324,11 +324,14 @@ void launch_delta_pairs32(const DevParams& P, const DevBuffers& B, cudaStream_t 
 // the replicas' states, takes a contiguous share of it, and writes one slot
 // per item: pair items {lj, real}, k items {k-space energy change}. The serial
 // step of each replica adds its slots in item order.
-constexpr int kItemPairs = 4096;
-
+// The item sizes and the grid are run-time choices (BatchTune, picked by
+// plum_batch_autotune); defaults: 4096 pairs per item, 128-vector k tiles,
+// 4 blocks per SM.
 __global__ void __launch_bounds__(kPairThreads)
     k_batch_delta32(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb,
-                    int n_rep, int* __restrict__ item_off, double* __restrict__ slots) {
+                    int n_rep, int* __restrict__ item_off, double* __restrict__ slots,
+                    BatchTune tune) {
+  const int kItemPairs = tune.item_pairs, kKTile32 = tune.k_tile;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ float red[kPairThreads / 32];
   __shared__ int s_pref[kMaxReplicas + 1];
@@ -476,14 +479,15 @@ __global__ void __launch_bounds__(kPairThreads)
 }
 
 void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, int* item_off,
-                          double* slots, size_t smem, cudaStream_t s) {
+                          double* slots, size_t smem, BatchTune tune, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_batch_delta32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          kKTableBytes + 4096);
     attr = true;
   }
-  k_batch_delta32<<<pair_grid32(), kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots);
+  const int grid = tune.grid > 0 ? tune.grid : pair_grid32();
+  k_batch_delta32<<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune);
 }
 
 __global__ void k_fix_all(const DevParams P, const DevBuffers B) {

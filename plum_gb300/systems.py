@@ -318,6 +318,23 @@ class BrushSpec:
     kcut2: Optional[float] = None
 
 
+def brush_ensemble(n: int, seed: int):
+    """n confined brush replicas of uneven size: wall gap H uniform in
+    [30, 60] sigma, Lx = Ly = 32 sigma, grafted chains uniform in {16..64} of
+    length uniform in {20..80}, bead charge -1 with probability f, f uniform
+    in [0.1, 1], +1 counterions, 64 LJ surface sites per wall and the 9-3
+    walls. The slab Ewald box follows the reference's rule (3H when 3H > 150,
+    else H + 150; potential_ewald_coul.cc:43-49)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        out.append(BrushSpec(n_graft=int(rng.integers(16, 65)),
+                             chain_len=int(rng.integers(20, 81)),
+                             lxy=32.0, height=float(rng.uniform(30.0, 60.0)),
+                             charge_frac=float(rng.uniform(0.1, 1.0)), n_sites=64))
+    return out
+
+
 def brush_coordinates(spec: BrushSpec, seed: int):
     """Phantom surface sites (symbol S, both walls), grafted chains (first bead
     L at z = graft_z), then +1 counterions neutralising the chain charge."""

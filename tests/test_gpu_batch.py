@@ -16,13 +16,18 @@ def pg():
     return plum_gb300
 
 
-def test_uneven_replicas_replay_their_references(pg):
+@pytest.mark.parametrize("tune", [None, (2048, 256, 304), (16384, 64, 1216)])
+def test_uneven_replicas_replay_their_references(pg, tune):
+    """Also with other work-item sizes than the defaults (what the autotuner
+    may pick): the items only change the order of FP32 partial sums."""
     dirs, gs = [], []
     for c in CASES:
         d, g = load(c)
         dirs.append(d)
         gs.append(g)
     b = pg.Batch(dirs)
+    if tune:
+        b.set_tune(*tune)
     b.seed(np.array([int(g["run_seed"]) for g in gs], np.uint32))
     n = 150
     b.run(n)
@@ -61,3 +66,12 @@ def test_batch_runs_are_repeatable(pg):
     c.run(200)
     for r in range(3):
         np.testing.assert_array_equal(a.replica(r).positions(), c.replica(r).positions())
+
+
+def test_autotune_picks_a_candidate_and_keeps_running(pg):
+    d, _ = load("bulk_medium")
+    b = pg.Batch([d] * 8)
+    b.seed(3)
+    ip, kt, grid = b.autotune(4)
+    assert ip in (2048, 4096, 8192, 16384) and kt in (128, 256) and grid > 0
+    assert b.run(100) > 0
