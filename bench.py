@@ -176,18 +176,31 @@ def tau_pooled(X, c=5.0):
     return float(-1.0 / slope), "exponential fit"
 
 
-def measure_tau(batch, mol_start, seconds, every):
-    """tau_int of the chains' Rg^2 in moves per replica, from every replica's
-    chains sampled every `every` steps for about `seconds`."""
+def measure_taus(batches, steps_done, mol_start, seconds, every, burn):
+    """tau_int of the chains' Rg^2 (moves per replica) for several batches
+    started from the same configurations: each is first brought to `burn`
+    steps per replica, then all are advanced in turn by `every` steps and
+    sampled, so every series covers the same stretch of its trajectory
+    (the chains still relax from their initial walks, which biases a tau
+    estimate; equal stretches bias them alike)."""
     import numpy as np
-    reps = [batch.replica(r) for r in range(batch.n)]
-    X, t_end = [], time.perf_counter() + seconds
+    for b, done in zip(batches, steps_done):
+        if burn > done:
+            b.run(burn - done)
+    reps = [[b.replica(r) for r in range(b.n)] for b in batches]
+    X = [[] for _ in batches]
+    t_end = time.perf_counter() + seconds
     while time.perf_counter() < t_end:
-        batch.run(every)
-        X.append(np.concatenate([chain_rg2(r.positions(), mol_start) for r in reps]))
-    tau, how = tau_pooled(np.array(X))
-    return {"tau_moves_per_replica": tau * every, "tau_samples": tau, "method": how,
-            "samples": len(X), "chains": len(X[0]) if X else 0, "moves_per_sample": every}
+        for i, b in enumerate(batches):
+            b.run(every)
+            X[i].append(np.concatenate([chain_rg2(r.positions(), mol_start) for r in reps[i]]))
+    out = []
+    for x in X:
+        tau, how = tau_pooled(np.array(x))
+        out.append({"tau_moves_per_replica": tau * every, "tau_samples": tau, "method": how,
+                    "samples": len(x), "chains": len(x[0]) if x else 0,
+                    "moves_per_sample": every, "burn_in_moves": burn})
+    return out
 
 
 def alg_flops_per_move(n_bead, mean_moved, n_k, frac_in_rc, mean_bonds):
@@ -280,8 +293,8 @@ def main():
     ap.add_argument("--workload", default="bulk_20000_pinned")
     ap.add_argument("--moves-per-step", type=int, default=2000)
     ap.add_argument("--plain-moves-per-step", type=int, default=200)
-    ap.add_argument("--samples-seconds", type=float, default=75.0,
-                    help="seconds of Rg sampling per form for tau_int (0: skip)")
+    ap.add_argument("--samples-seconds", type=float, default=150.0,
+                    help="seconds of Rg sampling (both forms together) for tau_int (0: skip)")
     ap.add_argument("--cpu-moves", type=int, default=20)
     ap.add_argument("--ref-moves", type=int, default=10)
     ap.add_argument("--replicas", type=int, default=16,
@@ -389,6 +402,7 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    torch.cuda.nvtx.range_push("timed")   # lets a profiler select the timed region
     for _ in range(args.steps):
         flush.zero_()          # L2 flush between steps (outside the step's events)
         torch.cuda.synchronize()
@@ -397,6 +411,7 @@ def main():
         dev_ms.append(ms)
         kernels += k
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
     step_ms = statistics.mean(dev_ms)
@@ -416,28 +431,38 @@ def main():
     # per-kernel CUDA-event durations over a few more steps (plain launches)
     kern_ms = batch.time_kernels(32)
 
-    # Rg decorrelation of the chosen form's dynamics (delayed acceptance
-    # changes the acceptance of chain moves, hence tau in moves)
-    mol_start = s64.topology()[0]
-    tau_da = measure_tau(batch, mol_start, args.samples_seconds, 1000) \
-        if args.samples_seconds > 0 and sg is not None else None
-
-    # the same replicas without the surrogate (FP32 + batched)
-    batch.set_surrogate(None)
+    # the same replicas (same starts and seeds) without the surrogate:
+    # FP32 + batched
+    nb = pg.Batch([make_workload(args.workload, seed=20261203 + r) for r in range(R)],
+                  device=local)
+    nb.seed(1000 * rank + 77)
+    tune_nb = nb.autotune(16)
     for _ in range(2):
-        batch.run(BS)
+        nb.run(BS)
     nb_ms = []
     for _ in range(max(3, args.steps // 2)):
         flush.zero_()
         torch.cuda.synchronize()
-        batch.run(BS)
-        nb_ms.append(batch.last_timing()[0])
+        nb.run(BS)
+        nb_ms.append(nb.last_timing()[0])
     batched32 = R * BS / (statistics.mean(nb_ms) / 1e3)
-    kern_ms_nb = batch.time_kernels(32)
-    # the plain Metropolis dynamics (the FP64 and FP32 forms share it: their
-    # decisions differ with the flip fraction below)
-    tau_plain = measure_tau(batch, mol_start, args.samples_seconds, 1000) \
-        if args.samples_seconds > 0 else None
+    kern_ms_nb = nb.time_kernels(32)
+    steps_nb = (2 + max(3, args.steps // 2)) * BS + 32
+
+    # Rg decorrelation of both dynamics: delayed acceptance changes the
+    # acceptance of chain moves, hence tau in moves; the plain Metropolis
+    # dynamics is shared by the FP64 and FP32 forms (their decisions differ
+    # with the flip fraction below)
+    mol_start = s64.topology()[0]
+    tau_da = tau_plain = None
+    if args.samples_seconds > 0:
+        steps_da = (args.warmup + args.steps) * BS + 32
+        if sg is not None:
+            tau_da, tau_plain = measure_taus([batch, nb], [steps_da, steps_nb], mol_start,
+                                             args.samples_seconds, 1000, 20000)
+        else:
+            tau_plain, = measure_taus([nb], [steps_nb], mol_start, args.samples_seconds,
+                                      1000, 20000)
 
     # precision form against FP64 on identical trial moves
     from plum_gb300 import precision
@@ -527,7 +552,8 @@ def main():
                    "autotuned_items": {"pairs_per_item": tune[0], "k_per_tile": tune[1],
                                        "grid": tune[2]}},
         "batched_fp32_no_surrogate": {"value": batched32, "unit": "moves/s",
-                                      "ms_per_step": statistics.mean(nb_ms)},
+                                      "ms_per_step": statistics.mean(nb_ms),
+                                      "autotuned_items": tune_nb},
         "delayed_acceptance": da,
         "kernel_ms_per_launch": {
             "chosen_form": dict(zip(("delta", "serial", "descriptor", "inference"),

@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int sample = blockIdx.x * kSamp + (t & (kSamp - 1));
   const bool swapped = t >= kSamp;
   const bool valid = sample < n;
-  // Launched as a dependent of the descriptor kernel, the weights above were
+  // Launched as a dependent of the previous kernel, the weights above were
   // staged while it ran; its results are visible after this wait (a no-op
   // for an ordinary launch).
   asm volatile("griddepcontrol.wait;" ::: "memory");
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if constexpr (std::is_same<TIn, float>::value) {
           v = make_float4(__uint_as_float(raw.x), __uint_as_float(raw.y), __uint_as_float(raw.z),
                           __uint_as_float(raw.w));
-        } else {  // unsigned integer descriptor sums
+        } else {  // integer descriptor sums
           v = make_float4((float)raw.x, (float)raw.y, (float)raw.z, (float)raw.w);
         }
       }
@@ -604,6 +604,8 @@ __device__ __forceinline__ bool near_axis(const DPos<kForm>& a, const DPos<kForm
 template <int kForm>
 __global__ void __launch_bounds__(kDescThreads)
     k_desc(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb, int n_rep) {
+  // the delayed-acceptance inference may start staging its weights now
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   __shared__ int s_icut[3];
   __shared__ float s_fcut[3];
   __shared__ unsigned fh[kFineAll];
@@ -718,7 +720,10 @@ __global__ void __launch_bounds__(kDescThreads)
 // round(4096 exp(-(r_f - c_k)^2 / (2 w^2))) over the fine bins within
 // 1.2 sigma (where the weight rounds to zero beyond).
 __global__ void __launch_bounds__(128) k_desc_fin(const DevBuffers* __restrict__ rb) {
+  // launched as a dependent of k_desc: let the inference start staging, then
+  // wait for the counts
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const DevBuffers& B = rb[blockIdx.x];
   const DevState* st = B.state;
   if (!(st->pending && st->da_active)) return;
@@ -806,12 +811,27 @@ void launch_mlp_pack(const float* param, MlpNet* net, cudaStream_t st) {
   k_mlp_pack<<<(kNParam + 255) / 256, 256, 0, st>>>(param, net);
 }
 
+void launch_desc_counts(const DevParams* rp, const DevBuffers* rb, int n_rep, int form,
+                        cudaStream_t st) {
+  if (form) k_desc<1><<<4 * 152, kDescThreads, 0, st>>>(rp, rb, n_rep);
+  else k_desc<0><<<4 * 152, kDescThreads, 0, st>>>(rp, rb, n_rep);
+}
+
 void launch_desc_batch(const DevParams* rp, const DevBuffers* rb, int n_rep, unsigned* acc,
                        int form, cudaStream_t st) {
   (void)acc;
-  if (form) k_desc<1><<<4 * 152, kDescThreads, 0, st>>>(rp, rb, n_rep);
-  else k_desc<0><<<4 * 152, kDescThreads, 0, st>>>(rp, rb, n_rep);
-  k_desc_fin<<<n_rep, 128, 0, st>>>(rb);
+  launch_desc_counts(rp, rb, n_rep, form, st);
+  // programmatic dependent of k_desc (it waits for the counts itself)
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(n_rep);
+  cfg.blockDim = dim3(128);
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_desc_fin, rb);
 }
 
 }  // namespace plum

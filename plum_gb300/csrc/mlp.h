@@ -97,5 +97,8 @@ void launch_mlp_pack(const float* param, MlpNet* net, cudaStream_t st);
 // positions. acc is the base of the batch's contiguous desc_acc rows.
 void launch_desc_batch(const DevParams* rp, const DevBuffers* rb, int n_rep, unsigned* acc,
                        int form, cudaStream_t st);
+// The fine counts only (k_desc).
+void launch_desc_counts(const DevParams* rp, const DevBuffers* rb, int n_rep, int form,
+                        cudaStream_t st);
 
 }  // namespace plum
