@@ -274,6 +274,55 @@ def make_brush_ensemble(n, seed=20261203):
     return dirs
 
 
+def cbmc_growth_steps(device, reps=200):
+    """Trial energies of configurational-bias growth steps on the
+    grand-canonical box (L = 50, 40 neutral chains of 30 beads, 2,000 salt
+    pairs, 32 trials per grown bead): the precision form's one launch against
+    the plain form's FP64 kernels, device time per growth step from CUDA
+    events, and the largest FP32 error over the steps."""
+    import numpy as np
+    import plum_gb300 as pg
+    from plum_gb300 import systems
+    d = os.path.join(tempfile.gettempdir(), "plum_bench_muvt_L50")
+    if not os.path.exists(os.path.join(d, "run.in")):
+        systems.write_muvt(d, systems.MuVTSpec(salt_first=True), seed=20261203)
+    s64 = pg.System(d, form=pg.FORM_FP64, device=device)
+    s32 = pg.System(d, form=pg.FORM_FP32, device=device)
+    rng = np.random.default_rng(11)
+    T, L = 32, 50.0
+    err, rel, t32, t64, n_l = 0.0, 0.0, [], [], None
+    for cl in (1, 8, 15, 22, 29):
+        start = rng.uniform(0, L, 3)
+        st = rng.normal(size=(cl, 3))
+        chain = start + np.cumsum(st / np.linalg.norm(st, axis=1)[:, None], axis=0)
+        dd = rng.normal(size=(T, 3))
+        b1 = chain[-1] + dd / np.linalg.norm(dd, axis=1)[:, None]
+        u64 = s64.cbmc_trials(b1, None, chain, None, -1)
+        u32 = s32.cbmc_trials(b1, None, chain, None, -1)
+        live = u64 < 1e8
+        if live.any():
+            rel = max(rel, float((np.abs(u32[live] - u64[live])
+                                  / np.maximum(1.0, np.abs(u64[live]))).max()))
+        small = np.abs(u64) < 50
+        if small.any():
+            err = max(err, float(np.abs(u32[small] - u64[small]).max()))
+        a, n_l = s32.cbmc_time(b1, None, chain, None, -1, reps=reps)
+        b, n64 = s64.cbmc_time(b1, None, chain, None, -1, reps=reps)
+        t32.append(a)
+        t64.append(b)
+    ms32, ms64 = statistics.mean(t32), statistics.mean(t64)
+    out = {"workload": "muvt_L50: 40 chains x 30 beads (neutral), 2,000 salt pairs, 5,200 beads",
+           "trials_per_growth_step": T, "grown_beads": [1, 8, 15, 22, 29],
+           "fp32_one_launch_ms": ms32, "fp32_launches": n_l,
+           "fp64_ms": ms64, "fp64_launches": n64,
+           "fp32_trial_sites_per_s": T / (ms32 / 1e3),
+           "fp32_vs_fp64": ms64 / ms32, "max_abs_err_vs_fp64_kT_where_u_below_50": err,
+           "max_rel_err_vs_fp64": rel}
+    s32.close()
+    s64.close()
+    return out
+
+
 def cpu_baseline_sample(d, moves):
     code = ("import sys,time; sys.path.insert(0,%r)\n"
             "from oracle import bindings as ob\n"
@@ -297,7 +346,9 @@ def main():
                     help="seconds of Rg sampling (both forms together) for tau_int (0: skip)")
     ap.add_argument("--cpu-moves", type=int, default=20)
     ap.add_argument("--ref-moves", type=int, default=10)
-    ap.add_argument("--replicas", type=int, default=16,
+    ap.add_argument("--tau-replicas", type=int, default=16,
+                    help="replicas whose chains' Rg^2 series give tau_int")
+    ap.add_argument("--replicas", type=int, default=64,
                     help="replicas of the workload in the batched form (the chosen form)")
     ap.add_argument("--batch-steps", type=int, default=256)
     ap.add_argument("--da-margin", type=float, default=12.0,
@@ -305,7 +356,7 @@ def main():
                          "the surrogate puts above it)")
     ap.add_argument("--no-surrogate", action="store_true",
                     help="time the batched precision form without delayed acceptance")
-    ap.add_argument("--only", default=None, choices=[None, "fp32", "fp64", "batch"],
+    ap.add_argument("--only", default=None, choices=[None, "fp32", "fp64", "batch", "cbmc"],
                     help="profiling runs: time one form only, no baselines or e2e")
     args = ap.parse_args()
 
@@ -350,6 +401,9 @@ def main():
                           "kernel_ms_per_launch": dict(zip(
                               ("delta", "serial", "descriptor", "inference"),
                               [float(x) for x in b.time_kernels(8)]))}), flush=True)
+        return 0
+    if args.only == "cbmc":
+        print(json.dumps({"profile_run": "cbmc", **cbmc_growth_steps(local)}), flush=True)
         return 0
     d = make_workload(args.workload)
     M = args.moves_per_step
@@ -447,26 +501,37 @@ def main():
         nb_ms.append(nb.last_timing()[0])
     batched32 = R * BS / (statistics.mean(nb_ms) / 1e3)
     kern_ms_nb = nb.time_kernels(32)
-    steps_nb = (2 + max(3, args.steps // 2)) * BS + 32
 
     # Rg decorrelation of both dynamics: delayed acceptance changes the
     # acceptance of chain moves, hence tau in moves; the plain Metropolis
     # dynamics is shared by the FP64 and FP32 forms (their decisions differ
     # with the flip fraction below)
+    # tau_int is a property of one replica's dynamics, not of the batch size:
+    # it is measured on the first TR replicas (same starts and seeds) so the
+    # sampling time yields series many tau long
     mol_start = s64.topology()[0]
     tau_da = tau_plain = None
+    TR = min(args.tau_replicas, R)
     if args.samples_seconds > 0:
-        steps_da = (args.warmup + args.steps) * BS + 32
+        def tau_batch(net):
+            b = pg.Batch([make_workload(args.workload, seed=20261203 + r) for r in range(TR)],
+                         device=local)
+            b.seed(1000 * rank + 77)
+            b.set_tune(*tune)
+            if net is not None:
+                b.set_surrogate(net)
+            return b
         if sg is not None:
-            tau_da, tau_plain = measure_taus([batch, nb], [steps_da, steps_nb], mol_start,
+            tau_da, tau_plain = measure_taus([tau_batch(sg), tau_batch(None)], [0, 0], mol_start,
                                              args.samples_seconds, 1000, 20000)
         else:
-            tau_plain, = measure_taus([nb], [steps_nb], mol_start, args.samples_seconds,
+            tau_plain, = measure_taus([tau_batch(None)], [0], mol_start, args.samples_seconds,
                                       1000, 20000)
 
     # precision form against FP64 on identical trial moves
     from plum_gb300 import precision
     prec = precision.compare(s64, s32, s64.topology()[0], n=200, seed=5)
+    cbmc = cbmc_growth_steps(local)
 
     # one replica of the precision form alone
     f_ms = []
@@ -518,7 +583,9 @@ def main():
         plain_s = plain / (2 * tp)
         samples = {"definition": "moves/s / (2 tau_int), tau_int of the chains' Rg^2 in moves per "
                                  "system (Sokal window, c = 5, autocorrelation pooled over all "
-                                 "chains of all replicas)",
+                                 "chains of %d replicas with the same starts and seeds as the "
+                                 "first %d of the throughput batch)" % (TR, TR),
+                   "tau_replicas": TR,
                    "tau_plain": tau_plain, "tau_chosen_form": tau_da,
                    "plain_fp64_samples_per_s": plain_s,
                    "batched_fp32_samples_per_s": batched32 / (2 * tp),
@@ -561,6 +628,7 @@ def main():
             "no_surrogate": dict(zip(("delta", "serial", "descriptor", "inference"),
                                      [float(x) for x in kern_ms_nb]))},
         "precision_vs_fp64": prec,
+        "cbmc_trials_grand_canonical": cbmc,
         "single_replica_fp32": {"value": single32, "unit": "moves/s", "moves_per_step": M},
         "plain_fp64": {"value": plain, "unit": "moves/s",
                        "moves_per_step": args.plain_moves_per_step},

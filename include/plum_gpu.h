@@ -167,10 +167,25 @@ int plum_rhoz(const plum_ctx* ctx, double* out, int cap, int* n_bins);
  * inserting. Host buffers: b1, b2 [n_trials*3], chain, chain_ci
  * [chain_len*3], u_out [n_trials]. Used by CBMCFGenTrialBeads
  * (cbmc.cc:161-212), CBMCFChainInsertion and CBMCFChainDeletion
- * (cbmc.cc:214-442). */
+ * (cbmc.cc:214-442).
+ *
+ * The context's form picks the arithmetic: PLUM_FORM_FP64 in FP64 (three
+ * launches); PLUM_FORM_FP32 in one launch with FP32 pair and k-space terms
+ * on the fixed-point coordinates and FP64 sums across blocks (limits: the
+ * trial sites and grown chain staged in at most 200 KiB of shared memory,
+ * about 2,000 trials with a chain of 1,000; larger requests return
+ * PLUM_ERR_INPUT). */
 int plum_cbmc_trials(plum_ctx* ctx, int n_trials, const double* b1, const double* b2,
                      int chain_len, const double* chain, const double* chain_ci, int delete_mol,
                      double* u_out);
+
+/* Device time of plum_cbmc_trials' kernels for these inputs: after three
+ * untimed launches, `reps` launches between CUDA events on the context's
+ * stream; ms_out = milliseconds per growth step, launches_out (may be NULL)
+ * = kernel launches per growth step. No reference counterpart. */
+int plum_cbmc_time(plum_ctx* ctx, int n_trials, const double* b1, const double* b2,
+                   int chain_len, const double* chain, const double* chain_ci, int delete_mol,
+                   int reps, double* ms_out, int* launches_out);
 
 /* plum_cbmc_trials for callers that cannot allocate device memory: a host
  * application whose device memory is owned by its own allocator or budget,
@@ -178,7 +193,8 @@ int plum_cbmc_trials(plum_ctx* ctx, int n_trials, const double* b1, const double
  * cudaFree (which plum_cbmc_trials uses when a larger request grows its
  * buffers) synchronise the whole device. No counterpart in the reference.
  *
- * Same energies as plum_cbmc_trials, but every buffer is the caller's and is
+ * Same energies as plum_cbmc_trials in the plain form (FP64, whatever the
+ * context's form), but every buffer is the caller's and is
  * in DEVICE memory: d_b1, d_b2 [n_trials*3], d_chain, d_chain_ci
  * [chain_len*3], d_u_out [n_trials]. The call allocates nothing (no
  * cudaMalloc/cudaFree, no host heap): its working memory is one fixed array

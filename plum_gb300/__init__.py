@@ -86,6 +86,9 @@ def lib():
                                              C.POINTER(C.c_long)]
         L.plum_cbmc_trials.argtypes = [C.c_void_p, C.c_int, _dp, C.c_void_p, C.c_int,
                                        C.c_void_p, C.c_void_p, C.c_int, _dp]
+        L.plum_cbmc_time.argtypes = [C.c_void_p, C.c_int, _dp, C.c_void_p, C.c_int,
+                                     C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                     C.POINTER(C.c_double), C.POINTER(C.c_int)]
         L.plum_sim_create.argtypes = [C.c_char_p, C.c_char_p, C.c_uint, C.c_int,
                                       C.POINTER(C.c_void_p)]
         L.plum_sim_destroy.argtypes = [C.c_void_p]
@@ -271,6 +274,19 @@ class System:
         _check(lib().plum_cbmc_trials(self.h, T, b1.ravel(), _ptr(keep[0]), cl, _ptr(keep[1]),
                                       _ptr(keep[2]), delete_mol, u))
         return u
+
+    def cbmc_time(self, b1, b2=None, chain=None, chain_ci=None, delete_mol=-1, reps=50):
+        """(ms per growth step, kernel launches per growth step) of
+        cbmc_trials' kernels on these inputs, CUDA events on the device."""
+        b1 = np.ascontiguousarray(b1, np.float64).reshape(-1, 3)
+        keep = [None if x is None else np.ascontiguousarray(x, np.float64).ravel()
+                for x in (b2, chain, chain_ci)]
+        cl = 0 if chain is None else len(np.asarray(chain).reshape(-1, 3))
+        ms, n = C.c_double(0), C.c_int(0)
+        _check(lib().plum_cbmc_time(self.h, len(b1), b1.ravel(), _ptr(keep[0]), cl,
+                                    _ptr(keep[1]), _ptr(keep[2]), delete_mol, reps,
+                                    C.byref(ms), C.byref(n)))
+        return ms.value, n.value
 
     def set_recompute(self, every: int):
         _check(lib().plum_set_recompute(self.h, every))

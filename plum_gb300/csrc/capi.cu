@@ -90,6 +90,9 @@ struct plum_ctx {
   double* cb_part = nullptr;
   double* cb_u = nullptr;
   int cb_cap = 0;
+  double* cb_part32 = nullptr;   // slots of the precision form's trial kernel
+  long long cb_part32_cap = 0;
+  int* cb_ticket = nullptr;      // its last-block counter (zero between launches)
   double drift[4] = {0, 0, 0, 0};  // running minus recomputed at the last reset
   double drift_max = 0.0;
   // CUDA graph of one batch of moves (kernels read the pending move from
@@ -624,7 +627,7 @@ int plum_ctx_destroy(plum_ctx* c) {
                   c->B.dsk_part, c->B.ktile_count, c->B.kpartial, c->B.fpos, c->B.done_count,
                   c->B.fq,       c->B.ftrial,  c->B.dsk_part32, c->cb_b, c->cb_c, c->cb_so,
                   c->cb_part,    c->cb_u,      c->d_obs_per, c->d_rhoz, c->desc_acc,
-                  c->d_rp1,      c->d_rb1,     c->desc_fine,
+                  c->d_rp1,      c->d_rb1,     c->desc_fine, c->cb_part32, c->cb_ticket,
                   c->d_stream,   c->d_mt,      c->d_log_type, c->d_log_acc, c->d_log_e};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -1184,10 +1187,12 @@ int plum_type_name(const plum_ctx* c, int type, char* buf, int cap) {
   return PLUM_OK;
 }
 
-int plum_cbmc_trials(plum_ctx* c, int n_trials, const double* b1, const double* b2,
-                     int chain_len, const double* chain, const double* chain_ci, int delete_mol,
-                     double* u_out) {
-  if (!c || n_trials <= 0 || !b1 || !u_out || chain_len < 0) return fail(PLUM_ERR_INPUT, "bad argument");
+// Uploads one growth step's trial sites and grown chain and fills the job
+// (and, in the precision form, the one-launch kernel's layout).
+static int cbmc_prepare(plum_ctx* c, int n_trials, const double* b1, const double* b2,
+                        int chain_len, const double* chain, const double* chain_ci,
+                        int delete_mol, CbmcJob* Jp, Cbmc32Layout* Gp) {
+  if (!c || n_trials <= 0 || !b1 || chain_len < 0) return fail(PLUM_ERR_INPUT, "bad argument");
   const Input& in = c->in;
   if (!in.use_gc) return fail(PLUM_ERR_INPUT, "run.in has no grand-canonical species");
   const int charged = in.gc_bead_charge != 0;
@@ -1196,6 +1201,14 @@ int plum_cbmc_trials(plum_ctx* c, int n_trials, const double* b1, const double* 
   if (chain_len > 0 && !chain) return fail(PLUM_ERR_INPUT, "missing grown chain");
   if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
   cudaSetDevice(c->device);
+  const bool fp32 = c->form == PLUM_FORM_FP32;
+  Cbmc32Layout G{};
+  if (fp32) {
+    G = cbmc32_layout(c->P, n_trials, chain_len);
+    if (G.smem > cbmc32_max_smem())
+      return fail(PLUM_ERR_INPUT, "too many trials or grown beads for the precision form's "
+                                  "trial kernel");
+  }
   const int cap = std::max(n_trials, std::max(chain_len, in.gc_chain_len));
   const int groups = cbmc_groups(c->P);
   if (cap > c->cb_cap) {
@@ -1209,6 +1222,18 @@ int plum_cbmc_trials(plum_ctx* c, int n_trials, const double* b1, const double* 
     c->cb_cap = cap;
   }
   if (!c->cb_so && dalloc(&c->cb_so, std::max(1, c->P.n_k))) return PLUM_ERR_CUDA;
+  if (fp32) {
+    if (G.slots > c->cb_part32_cap) {
+      cudaFree(c->cb_part32);
+      c->cb_part32 = nullptr;
+      if (dalloc(&c->cb_part32, (size_t)G.slots)) return PLUM_ERR_CUDA;
+      c->cb_part32_cap = G.slots;
+    }
+    if (!c->cb_ticket) {
+      if (dalloc(&c->cb_ticket, 1)) return PLUM_ERR_CUDA;
+      CK(cudaMemsetAsync(c->cb_ticket, 0, sizeof(int), c->s));
+    }
+  }
   int type = (int)(std::find(in.type_names.begin(), in.type_names.end(), in.gc_symbol) -
                    in.type_names.begin());
   const double q1 = in.gc_bead_charge, q2 = -in.gc_bead_charge;
@@ -1224,11 +1249,6 @@ int plum_cbmc_trials(plum_ctx* c, int n_trials, const double* b1, const double* 
                                                    chain_ci[3 * i + 2], q2)
                                 : hc[i];
   }
-  CK(cudaMemcpyAsync(c->cb_b, hb.data(), sizeof(double4_32a) * 2 * n_trials,
-                     cudaMemcpyHostToDevice, c->s));
-  if (chain_len > 0)
-    CK(cudaMemcpyAsync(c->cb_c, hc.data(), sizeof(double4_32a) * 2 * chain_len,
-                       cudaMemcpyHostToDevice, c->s));
   CbmcJob J;
   J.n_trials = n_trials;
   J.charged = charged;
@@ -1241,17 +1261,73 @@ int plum_cbmc_trials(plum_ctx* c, int n_trials, const double* b1, const double* 
     J.ex_lo = in.mol_start[delete_mol];
     J.ex_hi = in.mol_start[last + 1];
   }
+  // copies from pageable memory: the host vectors may go once these return
+  CK(cudaMemcpyAsync(c->cb_b, hb.data(), sizeof(double4_32a) * 2 * n_trials,
+                     cudaMemcpyHostToDevice, c->s));
+  if (chain_len > 0)
+    CK(cudaMemcpyAsync(c->cb_c, hc.data(), sizeof(double4_32a) * 2 * chain_len,
+                       cudaMemcpyHostToDevice, c->s));
   J.b1 = c->cb_b;
   J.b2 = c->cb_b + n_trials;
   J.chain = c->cb_c;
   J.chain_ci = c->cb_c + chain_len;
   J.s_o = c->cb_so;
-  J.part = c->cb_part;
+  J.part = fp32 ? c->cb_part32 : c->cb_part;
   J.u = c->cb_u;
-  launch_cbmc(c->P, c->B, J, c->s);
+  *Jp = J;
+  *Gp = G;
+  return PLUM_OK;
+}
+
+// One growth step's trial energies on the context's stream: one launch in the
+// precision form, the FP64 kernels (S_o, system sweep, per-trial sums) in the
+// plain form.
+static int cbmc_launch(plum_ctx* c, const CbmcJob& J, const Cbmc32Layout& G) {
+  if (c->form == PLUM_FORM_FP32) {
+    if (launch_cbmc32(c->P, c->B, J, G, c->cb_ticket, c->s))
+      return fail(PLUM_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+  } else {
+    launch_cbmc(c->P, c->B, J, c->s);
+  }
   CK(cudaGetLastError());
+  return PLUM_OK;
+}
+
+int plum_cbmc_trials(plum_ctx* c, int n_trials, const double* b1, const double* b2,
+                     int chain_len, const double* chain, const double* chain_ci, int delete_mol,
+                     double* u_out) {
+  if (!u_out) return fail(PLUM_ERR_INPUT, "bad argument");
+  CbmcJob J;
+  Cbmc32Layout G;
+  int rc = cbmc_prepare(c, n_trials, b1, b2, chain_len, chain, chain_ci, delete_mol, &J, &G);
+  if (rc) return rc;
+  rc = cbmc_launch(c, J, G);
+  if (rc) return rc;
   CK(cudaMemcpyAsync(u_out, c->cb_u, sizeof(double) * n_trials, cudaMemcpyDeviceToHost, c->s));
   CK(cudaStreamSynchronize(c->s));
+  return PLUM_OK;
+}
+
+int plum_cbmc_time(plum_ctx* c, int n_trials, const double* b1, const double* b2, int chain_len,
+                   const double* chain, const double* chain_ci, int delete_mol, int reps,
+                   double* ms_out, int* launches_out) {
+  if (!ms_out || reps <= 0) return fail(PLUM_ERR_INPUT, "bad argument");
+  CbmcJob J;
+  Cbmc32Layout G;
+  int rc = cbmc_prepare(c, n_trials, b1, b2, chain_len, chain, chain_ci, delete_mol, &J, &G);
+  if (rc) return rc;
+  for (int i = 0; i < 3; i++)
+    if ((rc = cbmc_launch(c, J, G))) return rc;
+  CK(cudaEventRecord(c->ev0, c->s));
+  for (int i = 0; i < reps; i++)
+    if ((rc = cbmc_launch(c, J, G))) return rc;
+  CK(cudaEventRecord(c->ev1, c->s));
+  CK(cudaEventSynchronize(c->ev1));
+  float ms = 0.0f;
+  CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  *ms_out = (double)ms / reps;
+  if (launches_out)
+    *launches_out = c->form == PLUM_FORM_FP32 ? 1 : ((c->P.use_ewald && c->P.n_k > 0) ? 3 : 2);
   return PLUM_OK;
 }
 

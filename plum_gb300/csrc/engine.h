@@ -192,6 +192,18 @@ struct CbmcJob {
 };
 int cbmc_groups(const DevParams& P);
 void launch_cbmc(const DevParams& P, const DevBuffers& B, const CbmcJob& J, cudaStream_t s);
+// The precision form's one-launch trial kernel (kern_cbmc32.cu): J.part holds
+// `slots` doubles laid out by cbmc32_layout; J.s_o is unused. ticket is one
+// int, zero before the first launch (each launch leaves it zero).
+struct Cbmc32Layout {
+  int n_grp, n_chunk, chunk, n_pair, n_kt, grid;
+  long long chain_off, k_off, slots;
+  size_t smem;
+};
+Cbmc32Layout cbmc32_layout(const DevParams& P, int n_trials, int chain_len);
+size_t cbmc32_max_smem();
+int launch_cbmc32(const DevParams& P, const DevBuffers& B, const CbmcJob& J,
+                  const Cbmc32Layout& G, int* ticket, cudaStream_t s);
 // The same on a fixed scratch array (no allocation); returns 0, 1 (sizes) or 2
 // (CUDA), with a message in err.
 int cbmc_trials_noalloc(const DevParams& P, const DevBuffers& B, cudaStream_t s, int device,

@@ -44,16 +44,24 @@ def test_oracle_exchange_replays_reference(built, case):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("form", [0, 1])
 @pytest.mark.parametrize("case", GC)
-def test_gpu_exchange_replays_reference(case):
+def test_gpu_exchange_replays_reference(case, form):
+    """form 0: plain FP64. form 1: the precision form, whose trial energies
+    come from the one-launch FP32 kernel (kern_cbmc32.cu) and whose moves use
+    the FP32 energy change; a near tie could turn one decision, but on these
+    fixtures' 400 steps (over 200 exchange attempts) none does, so the
+    sequence and coordinates are the reference's, and the running total
+    agrees to the FP32 bound."""
     import plum_gb300 as pg
     d, g = fixture(case)
-    sim = pg.HostSimulation(d, seed=int(g["run_seed"]))
+    sim = pg.HostSimulation(d, seed=int(g["run_seed"]), form=form)
     mt, ac = sim.steps(len(g["run_type"]))
     np.testing.assert_array_equal(mt, g["run_type"])
     np.testing.assert_array_equal(ac, g["run_accept"])
     np.testing.assert_allclose(sim.positions(), g["run_coords"], rtol=0, atol=1e-9)
-    assert abs(sim.energies().sum() - g["run_etot"][-1]) <= 1e-8 * max(1.0, abs(g["run_etot"][-1]))
+    tol = 1e-8 if form == 0 else 1e-6
+    assert abs(sim.energies().sum() - g["run_etot"][-1]) <= tol * max(1.0, abs(g["run_etot"][-1]))
 
 
 @pytest.mark.gpu
