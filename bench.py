@@ -346,6 +346,8 @@ def main():
                     help="seconds of Rg sampling (both forms together) for tau_int (0: skip)")
     ap.add_argument("--cpu-moves", type=int, default=20)
     ap.add_argument("--ref-moves", type=int, default=10)
+    ap.add_argument("--tune", default=None,
+                    help="with --only batch: item_pairs,k_tile,grid,min_blocks instead of autotuning")
     ap.add_argument("--tau-replicas", type=int, default=16,
                     help="replicas whose chains' Rg^2 series give tau_int")
     ap.add_argument("--replicas", type=int, default=64,
@@ -384,7 +386,11 @@ def main():
         b = pg.Batch(dirs, device=local)
         setup_s = time.perf_counter() - t0
         b.seed(77)
-        tune = b.autotune(8)
+        if args.tune:
+            tune = tuple(int(x) for x in args.tune.split(","))
+            b.set_tune(*tune)
+        else:
+            tune = b.autotune(8)
         for _ in range(args.warmup):
             b.run(args.batch_steps)
         ms_all = []
@@ -617,7 +623,7 @@ def main():
                            (", delayed acceptance with the learned surrogate" if sg else ""),
                    "l2": "flushed between steps (256 MB write)", "parallelism": "replicas",
                    "autotuned_items": {"pairs_per_item": tune[0], "k_per_tile": tune[1],
-                                       "grid": tune[2]}},
+                                       "grid": tune[2], "resident_blocks_per_sm": tune[3]}},
         "batched_fp32_no_surrogate": {"value": batched32, "unit": "moves/s",
                                       "ms_per_step": statistics.mean(nb_ms),
                                       "autotuned_items": tune_nb},

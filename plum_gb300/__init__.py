@@ -119,7 +119,7 @@ def lib():
         L.plum_move_descriptor.argtypes = [C.c_void_p, _dp]
         L.plum_batch_set_surrogate.argtypes = [C.c_void_p, C.c_void_p]
         L.plum_batch_time_kernels.argtypes = [C.c_void_p, C.c_int, _dp]
-        L.plum_batch_set_tune.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+        L.plum_batch_set_tune.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
         L.plum_batch_autotune.argtypes = [C.c_void_p, C.c_int, _ip]
         L.plum_batch_da_stats.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
         _lib = L
@@ -469,13 +469,13 @@ class Batch:
         _check(lib().plum_batch_time_kernels(self.h, n_steps, o))
         return o
 
-    def set_tune(self, item_pairs=4096, k_tile=128, grid=0):
-        _check(lib().plum_batch_set_tune(self.h, item_pairs, k_tile, grid))
+    def set_tune(self, item_pairs=4096, k_tile=128, grid=0, min_blocks=2):
+        _check(lib().plum_batch_set_tune(self.h, item_pairs, k_tile, grid, min_blocks))
 
     def autotune(self, steps=16):
         """Times the energy-change kernel's work-item sizes on these replicas
-        and keeps the fastest: (item_pairs, k_tile, grid)."""
-        o = np.zeros(3, np.int32)
+        and keeps the fastest: (item_pairs, k_tile, grid, min_blocks)."""
+        o = np.zeros(4, np.int32)
         _check(lib().plum_batch_autotune(self.h, steps, o))
         return tuple(int(x) for x in o)
 

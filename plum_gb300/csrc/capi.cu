@@ -1480,7 +1480,7 @@ struct plum_batch {
   int* d_item_off = nullptr;
   double* d_slots = nullptr;
   size_t kt_smem = 0;
-  BatchTune tune{4096, 128, 0};
+  BatchTune tune{4096, 128, 0, 2};
   // per-replica streams
   std::vector<long long> cap, per_step;
   uint32_t** d_states = nullptr;
@@ -1629,8 +1629,10 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
     hst[r] = c->d_mt;
     hout[r] = c->d_stream;
     hsts[r] = c->B.state;
-    items += ((long long)c->max_len * P.n_bead + kMinItemPairs - 1) / kMinItemPairs +
-             (P.n_k + kMinKTile - 1) / kMinKTile;
+    int most = 0;
+    for (int m = 1; m <= c->max_len; m++)
+      most = std::max(most, pair_item_count(m, P.n_bead, kMinItemPairs));
+    items += most + (P.n_k + kMinKTile - 1) / kMinKTile;
     size_t sm = P.use_ewald ? (size_t)P.kchunk_delta * 2 * P.kper * sizeof(float2) : 0;
     b->kt_smem = std::max(b->kt_smem, sm);
   }
@@ -1855,44 +1857,47 @@ int plum_batch_time_kernels(plum_batch* b, int n_steps, double* out4) {
   return PLUM_OK;
 }
 
-int plum_batch_set_tune(plum_batch* b, int item_pairs, int k_tile, int grid) {
+int plum_batch_set_tune(plum_batch* b, int item_pairs, int k_tile, int grid, int min_blocks) {
   if (!b || item_pairs < kMinItemPairs || item_pairs % 256 || k_tile < kMinKTile ||
-      k_tile > kPairThreads || grid < 0 || grid > 65535)
+      k_tile > kPairThreads || grid < 0 || grid > 65535 || min_blocks < 2 || min_blocks > 3)
     return fail(PLUM_ERR_INPUT, "bad work-item sizes");
-  b->tune = BatchTune{item_pairs, k_tile, grid};
+  b->tune = BatchTune{item_pairs, k_tile, grid, min_blocks};
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   b->gexec = nullptr;
   b->g_steps = 0;
   return PLUM_OK;
 }
 
-int plum_batch_autotune(plum_batch* b, int steps, int* out3) {
+int plum_batch_autotune(plum_batch* b, int steps, int* out4) {
   if (!b || steps <= 0) return fail(PLUM_ERR_INPUT, "bad argument");
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
   const int pairs[] = {2048, 4096, 8192, 16384};
   const int ktiles[] = {128, 256};
-  const int grids[] = {2 * sms, 4 * sms, 8 * sms};
+  const int per_sm[] = {2, 3, 4, 6, 8};
+  const int occ[] = {2, 3};
   double best = 1e300;
   BatchTune pick = b->tune;
-  for (int ip : pairs)
-    for (int kt : ktiles)
-      for (int g : grids) {
-        b->tune = BatchTune{ip, kt, g};
-        double ms[4];
-        int rc = plum_batch_time_kernels(b, steps, ms);
-        if (rc) return rc;
-        if (ms[0] < best) {
-          best = ms[0];
-          pick = b->tune;
+  for (int mb : occ)
+    for (int ip : pairs)
+      for (int kt : ktiles)
+        for (int ps : per_sm) {
+          b->tune = BatchTune{ip, kt, ps * sms, mb};
+          double ms[4];
+          int rc = plum_batch_time_kernels(b, steps, ms);
+          if (rc) return rc;
+          if (ms[0] < best) {
+            best = ms[0];
+            pick = b->tune;
+          }
         }
-      }
-  int rc = plum_batch_set_tune(b, pick.item_pairs, pick.k_tile, pick.grid);
+  int rc = plum_batch_set_tune(b, pick.item_pairs, pick.k_tile, pick.grid, pick.min_blocks);
   if (rc) return rc;
-  if (out3) {
-    out3[0] = pick.item_pairs;
-    out3[1] = pick.k_tile;
-    out3[2] = pick.grid;
+  if (out4) {
+    out4[0] = pick.item_pairs;
+    out4[1] = pick.k_tile;
+    out4[2] = pick.grid;
+    out4[3] = pick.min_blocks;
   }
   return PLUM_OK;
 }

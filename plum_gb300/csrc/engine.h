@@ -219,9 +219,23 @@ struct BatchTune {
   int item_pairs;  // (moved, other) pairs per pair item
   int k_tile;      // k-vectors per k item
   int grid;        // blocks (0: 4 per SM)
+  int min_blocks;  // register budget: 2 or 3 resident blocks per SM
 };
 constexpr int kMinItemPairs = 1024;  // smallest item the slot buffers are sized for
 constexpr int kMinKTile = 64;
+// Pair items of the batched energy change: kPairGroup moved beads (held in
+// registers) x a chunk of system beads (each loaded once for all of them);
+// one more item per move takes the pairs among the moved beads.
+constexpr int kPairGroup = 4;
+__host__ __device__ inline int pair_chunk(int m, int item_pairs) {
+  const int g = m < kPairGroup ? (m > 0 ? m : 1) : kPairGroup;
+  return item_pairs / g > 0 ? item_pairs / g : 1;
+}
+__host__ __device__ inline int pair_item_count(int m, int n_bead, int item_pairs) {
+  if (m <= 0) return 0;
+  const int c = pair_chunk(m, item_pairs);
+  return ((m + kPairGroup - 1) / kPairGroup) * ((n_bead + c - 1) / c) + (m > 1 ? 1 : 0);
+}
 void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, int* item_off,
                           double* slots, size_t smem, BatchTune tune, cudaStream_t s);
 void launch_batch_serial(const DevParams* rp, const DevBuffers* rb, const int* item_off,

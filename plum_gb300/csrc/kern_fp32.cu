@@ -240,15 +240,20 @@ void launch_delta_pairs32(const DevParams& P, const DevBuffers& B, cudaStream_t 
 
 // ------------------------------------------------------------ replicas
 // Batched replicas: every replica's pending move contributes pair items
-// (kItemPairs (moved, other) pairs each) and k items (one k tile of kKTile32
-// vectors over all moved beads). Every block derives the same item list from
-// the replicas' states, takes a contiguous share of it, and writes one slot
-// per item: pair items {lj, real}, k items {k-space energy change}. The serial
-// step of each replica adds its slots in item order.
-// The item sizes and the grid are run-time choices (BatchTune, picked by
+// (up to kPairGroup moved beads, held in registers at their trial and
+// current positions, x a chunk of kItemPairs / kPairGroup other beads, each
+// loaded once for all of them), one item for the pairs among the moved beads,
+// and k items (one k tile of kKTile32 vectors over all moved beads). Every
+// block derives the same item list from the replicas' states, takes a
+// contiguous share of it, and writes one slot per item: pair items
+// {lj, real}, k items {k-space energy change}. The serial step of each
+// replica adds its slots in item order.
+// The item sizes, the grid and the register budget (kMinBlocks resident
+// blocks per SM) are run-time choices (BatchTune, picked by
 // plum_batch_autotune); defaults: 4096 pairs per item, 128-vector k tiles,
-// 4 blocks per SM.
-__global__ void __launch_bounds__(kPairThreads)
+// 4 blocks per SM, 2 resident.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(kPairThreads, kMinBlocks)
     k_batch_delta32(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb,
                     int n_rep, int* __restrict__ item_off, double* __restrict__ slots,
                     BatchTune tune) {
@@ -267,8 +272,7 @@ __global__ void __launch_bounds__(kPairThreads)
     // a move rejected by the surrogate's stage one has no exact change
     const int m = (st->pending && !st->da_skip) ? st->b_hi - st->b_lo : 0;
     const DevParams& pr = rp[r];
-    const long long pairs = (long long)m * pr.n_bead;
-    const int np = (pr.use_pair || pr.use_ewald) ? (int)((pairs + kItemPairs - 1) / kItemPairs) : 0;
+    const int np = (pr.use_pair || pr.use_ewald) ? pair_item_count(m, pr.n_bead, kItemPairs) : 0;
     const int nk = (pr.use_ewald && m > 0) ? (pr.n_k + kKTile32 - 1) / kKTile32 : 0;
     s_np[r] = np;
     s_pref[r + 1] = np + nk;
@@ -322,28 +326,50 @@ __global__ void __launch_bounds__(kPairThreads)
     const int local = item - s_pref[r];
     if (local < s_np[r]) {
       float acc_lj = 0.0f, acc_re = 0.0f;
-      const long long p0 = (long long)local * kItemPairs;
-      const long long p1 = min((long long)m * N, p0 + kItemPairs);
-      long long p = p0 + threadIdx.x;
-      int ii = (int)(p / N), j = (int)(p % N);
-      const int gq = kPairThreads / N, gr = kPairThreads % N;
-      for (; p < p1; p += kPairThreads, ii += gq, j += gr) {
-        if (j >= N) {
-          j -= N;
-          ii++;
+      const int chunk = pair_chunk(m, kItemPairs);
+      const int n_chunk = (N + chunk - 1) / chunk;
+      const int n_grid = ((m + kPairGroup - 1) / kPairGroup) * n_chunk;
+      if (local < n_grid) {
+        // kPairGroup moved beads (trial and current) in registers x a chunk
+        // of the other beads: each loaded bead serves 2 kPairGroup pairs
+        const int g0 = (local / n_chunk) * kPairGroup, gn = min(kPairGroup, m - g0);
+        const int c0 = (local % n_chunk) * chunk, c1 = min(N, c0 + chunk);
+        int4 ti[kPairGroup], ci[kPairGroup];
+        float qi[kPairGroup];
+#pragma unroll
+        for (int u = 0; u < kPairGroup; u++) {
+          const int ii = g0 + (u < gn ? u : 0);
+          ti[u] = B.ftrial[ii];
+          ci[u] = B.fpos[b_lo + ii];
+          qi[u] = B.fq[b_lo + ii];
         }
-        const int i = b_lo + ii;
-        const bool jm = j >= b_lo && j < b_hi;
-        if (jm && j <= i) continue;
-        const int4 ti = B.ftrial[ii], ci = B.fpos[i];
-        const float qi = B.fq[i], qj = B.fq[j];
-        const int4 cj = B.fpos[j];
-        const int4 tj = jm ? B.ftrial[j - b_lo] : cj;
-        float l1 = 0, r1 = 0, l0 = 0, r0 = 0;
-        pair32(P, ti, qi, tj, qj, l1, r1);
-        pair32(P, ci, qi, cj, qj, l0, r0);
-        acc_lj += l1 - l0;
-        acc_re += r1 - r0;
+        for (int j = c0 + threadIdx.x; j < c1; j += kPairThreads) {
+          if (j >= b_lo && j < b_hi) continue;  // moved pairs: the last item
+          const int4 cj = B.fpos[j];
+          const float qj = B.fq[j];
+#pragma unroll
+          for (int u = 0; u < kPairGroup; u++) {
+            if (u < gn) {
+              float l1 = 0, r1 = 0, l0 = 0, r0 = 0;
+              pair32(P, ti[u], qi[u], cj, qj, l1, r1);
+              pair32(P, ci[u], qi[u], cj, qj, l0, r0);
+              acc_lj += l1 - l0;
+              acc_re += r1 - r0;
+            }
+          }
+        }
+      } else {
+        // pairs among the moved beads, each once (both trial / both current)
+        const int lane = threadIdx.x & 31;
+        for (int a = threadIdx.x >> 5; a < m; a += kPairThreads / 32)
+          for (int bb = a + 1 + lane; bb < m; bb += 32) {
+          float l1 = 0, r1 = 0, l0 = 0, r0 = 0;
+          pair32(P, B.ftrial[a], B.fq[b_lo + a], B.ftrial[bb], B.fq[b_lo + bb], l1, r1);
+          pair32(P, B.fpos[b_lo + a], B.fq[b_lo + a], B.fpos[b_lo + bb], B.fq[b_lo + bb], l0,
+                 r0);
+          acc_lj += l1 - l0;
+          acc_re += r1 - r0;
+        }
       }
       float a = block_sum32<kPairThreads>(acc_lj, red);
       float b = block_sum32<kPairThreads>(acc_re, red);
@@ -403,12 +429,17 @@ void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, 
                           double* slots, size_t smem, BatchTune tune, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_batch_delta32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_batch_delta32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kKTableBytes + 4096);
+    cudaFuncSetAttribute(k_batch_delta32<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          kKTableBytes + 4096);
     attr = true;
   }
   const int grid = tune.grid > 0 ? tune.grid : pair_grid32();
-  k_batch_delta32<<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune);
+  if (tune.min_blocks == 3)
+    k_batch_delta32<3><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune);
+  else
+    k_batch_delta32<2><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune);
 }
 
 __global__ void k_fix_all(const DevParams P, const DevBuffers B) {
