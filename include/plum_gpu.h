@@ -283,16 +283,17 @@ int plum_batch_last_timing(const plum_batch* batch, double* ms, long* kernels);
  * count as ordinary steps of the replicas. */
 int plum_batch_time_kernels(plum_batch* batch, int n_steps, double* out4);
 /* Work items of the batched energy change: (moved, other) pairs per pair
- * item (>= 1024, a multiple of 256; a pair item holds up to 4 moved beads
- * against item_pairs / 4 other beads), k-vectors per k item (64..256), the
- * grid (0: 4 blocks per SM) and the register budget as resident blocks per
- * SM (2 or 3). They change only the summation order inside FP32 partials. */
+ * item (>= 1024, a multiple of 256; a pair item holds up to 32 moved beads
+ * against item_pairs / 32 other beads, at least 256), k-vectors per k item
+ * (64..256), the grid (0: 4 blocks per SM) and the register budget as
+ * resident blocks per SM (2, 3 or 4). They change only the summation order
+ * inside FP32 partials. */
 int plum_batch_set_tune(plum_batch* batch, int item_pairs, int k_tile, int grid,
                         int min_blocks);
 /* Times the energy-change kernel on these replicas (`steps` steps per
  * candidate, see plum_batch_time_kernels) for item sizes {2048, 4096, 8192,
  * 16384} x k tiles {128, 256} x grids {2, 3, 4, 6, 8} blocks per SM x
- * register budgets {2, 3} blocks per SM, keeps the fastest; out4 (may be
+ * register budgets {2, 3, 4} blocks per SM, keeps the fastest; out4 (may be
  * NULL) = the chosen {item_pairs, k_tile, grid, min_blocks}. */
 int plum_batch_autotune(plum_batch* batch, int steps, int* out4);
 

@@ -1635,6 +1635,8 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
     items += most + (P.n_k + kMinKTile - 1) / kMinKTile;
     size_t sm = P.use_ewald ? (size_t)P.kchunk_delta * 2 * P.kper * sizeof(float2) : 0;
     b->kt_smem = std::max(b->kt_smem, sm);
+    // staged moved beads of a pair item (trial and current int4, charge)
+    b->kt_smem = std::max(b->kt_smem, (size_t)kPairGroup * (2 * sizeof(int4) + sizeof(float)));
   }
   int rc = 0;
   rc |= dalloc(&b->d_rp, n);
@@ -1859,7 +1861,7 @@ int plum_batch_time_kernels(plum_batch* b, int n_steps, double* out4) {
 
 int plum_batch_set_tune(plum_batch* b, int item_pairs, int k_tile, int grid, int min_blocks) {
   if (!b || item_pairs < kMinItemPairs || item_pairs % 256 || k_tile < kMinKTile ||
-      k_tile > kPairThreads || grid < 0 || grid > 65535 || min_blocks < 2 || min_blocks > 3)
+      k_tile > kPairThreads || grid < 0 || grid > 65535 || min_blocks < 2 || min_blocks > 4)
     return fail(PLUM_ERR_INPUT, "bad work-item sizes");
   b->tune = BatchTune{item_pairs, k_tile, grid, min_blocks};
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
@@ -1875,7 +1877,7 @@ int plum_batch_autotune(plum_batch* b, int steps, int* out4) {
   const int pairs[] = {2048, 4096, 8192, 16384};
   const int ktiles[] = {128, 256};
   const int per_sm[] = {2, 3, 4, 6, 8};
-  const int occ[] = {2, 3};
+  const int occ[] = {2, 3, 4};
   double best = 1e300;
   BatchTune pick = b->tune;
   for (int mb : occ)

@@ -223,13 +223,15 @@ struct BatchTune {
 };
 constexpr int kMinItemPairs = 1024;  // smallest item the slot buffers are sized for
 constexpr int kMinKTile = 64;
-// Pair items of the batched energy change: kPairGroup moved beads (held in
-// registers) x a chunk of system beads (each loaded once for all of them);
-// one more item per move takes the pairs among the moved beads.
-constexpr int kPairGroup = 4;
+// Pair items of the batched energy change: up to kPairGroup moved beads
+// (staged in shared memory) x a chunk of other beads (one per thread, a
+// multiple of the block size); one more item per move takes the pairs among
+// the moved beads.
+constexpr int kPairGroup = 32;
 __host__ __device__ inline int pair_chunk(int m, int item_pairs) {
   const int g = m < kPairGroup ? (m > 0 ? m : 1) : kPairGroup;
-  return item_pairs / g > 0 ? item_pairs / g : 1;
+  const int c = (item_pairs / g + kPairThreads - 1) / kPairThreads * kPairThreads;
+  return c > kPairThreads ? c : kPairThreads;
 }
 __host__ __device__ inline int pair_item_count(int m, int n_bead, int item_pairs) {
   if (m <= 0) return 0;

@@ -238,11 +238,86 @@ void launch_delta_pairs32(const DevParams& P, const DevBuffers& B, cudaStream_t 
   k_delta32<<<pair_grid32(), kPairThreads, smem, s>>>(P, B);
 }
 
+// Loop constants of a replica's pair sweep, in registers.
+struct PairConst {
+  float sx, sy, sz, rc, sa, lB, ljmax2;
+  int nt, use_pair, use_ewald;
+};
+
+__device__ __forceinline__ PairConst pair_const(const DevParams& P) {
+  PairConst K;
+  K.sx = P.f_scale[0];
+  K.sy = P.f_scale[1];
+  K.sz = P.f_scale[2];
+  K.rc = P.f_real_cut;
+  K.sa = P.f_sqrt_alpha;
+  K.lB = P.f_lB;
+  K.nt = P.n_type;
+  K.use_pair = P.use_pair;
+  K.use_ewald = P.use_ewald;
+  // r2 = 0 (coincident beads) must reach lj32, which returns the overlap value
+  float m2 = 1e-30f;
+  for (int k = 0; k < P.n_type * P.n_type; k++) m2 = fmaxf(m2, P.f_lj_rc2[k]);
+  K.ljmax2 = m2;
+  return K;
+}
+
+// pair32 with the LJ table read only inside the largest LJ cut-off and, for
+// kSingle (r_c <= L/2 on every axis), the minimum image inlined.
+template <bool kSingle>
+__device__ __forceinline__ void pair32k(const DevParams& P, const PairConst& K, int4 a, float qa,
+                                        int4 b, float qb, float& lj, float& re) {
+  const float dx = fdiff(a.x, b.x, K.sx);
+  const float dy = fdiff(a.y, b.y, K.sy);
+  const float dz = fdiff(a.z, b.z, K.sz);
+  const float r2 = dx * dx + dy * dy + dz * dz;
+  if (K.use_pair && r2 < K.ljmax2) lj += lj32(P, a.w * K.nt + b.w, r2);
+  if (K.use_ewald) {
+    const float qq = qa * qb;
+    if (qq != 0.0f) {
+      float e = 0.0f;
+      if (kSingle) {
+        if (r2 > 0.0f) {
+          const float ir = rsqrtf(r2);
+          const float r = r2 * ir;
+          if (r <= K.rc) e = erfc_nr(K.sa * r) * ir;
+        }
+      } else {
+        e = real_images32(P, dx, dy, dz);
+      }
+      re += K.lB * qq * e;
+    }
+  }
+}
+
+// One thread per other bead j in [c0, c1) (moved beads skipped), against the
+// gn staged moved beads at their trial (s_mt[u]) and current
+// (s_mt[kPairGroup + u]) positions.
+template <bool kSingle>
+__device__ __forceinline__ void pair_sweep(const DevParams& P, const PairConst& K,
+                                           const DevBuffers& B, const int4* s_mt,
+                                           const float* s_mq, int gn, int c0, int c1, int b_lo,
+                                           int b_hi, float& acc_lj, float& acc_re) {
+  for (int j = c0 + threadIdx.x; j < c1; j += kPairThreads) {
+    if (j >= b_lo && j < b_hi) continue;  // moved pairs: the last item
+    const int4 cj = B.fpos[j];
+    const float qj = B.fq[j];
+#pragma unroll 2
+    for (int u = 0; u < gn; u++) {
+      float l1 = 0, r1 = 0, l0 = 0, r0 = 0;
+      pair32k<kSingle>(P, K, s_mt[u], s_mq[u], cj, qj, l1, r1);
+      pair32k<kSingle>(P, K, s_mt[kPairGroup + u], s_mq[u], cj, qj, l0, r0);
+      acc_lj += l1 - l0;
+      acc_re += r1 - r0;
+    }
+  }
+}
+
 // ------------------------------------------------------------ replicas
 // Batched replicas: every replica's pending move contributes pair items
-// (up to kPairGroup moved beads, held in registers at their trial and
-// current positions, x a chunk of kItemPairs / kPairGroup other beads, each
-// loaded once for all of them), one item for the pairs among the moved beads,
+// (up to kPairGroup moved beads, staged in shared memory at their trial and
+// current positions, x a chunk of other beads, one per thread), one item for
+// the pairs among the moved beads,
 // and k items (one k tile of kKTile32 vectors over all moved beads). Every
 // block derives the same item list from the replicas' states, takes a
 // contiguous share of it, and writes one slot per item: pair items
@@ -330,34 +405,22 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
       const int n_chunk = (N + chunk - 1) / chunk;
       const int n_grid = ((m + kPairGroup - 1) / kPairGroup) * n_chunk;
       if (local < n_grid) {
-        // kPairGroup moved beads (trial and current) in registers x a chunk
-        // of the other beads: each loaded bead serves 2 kPairGroup pairs
         const int g0 = (local / n_chunk) * kPairGroup, gn = min(kPairGroup, m - g0);
         const int c0 = (local % n_chunk) * chunk, c1 = min(N, c0 + chunk);
-        int4 ti[kPairGroup], ci[kPairGroup];
-        float qi[kPairGroup];
-#pragma unroll
-        for (int u = 0; u < kPairGroup; u++) {
-          const int ii = g0 + (u < gn ? u : 0);
-          ti[u] = B.ftrial[ii];
-          ci[u] = B.fpos[b_lo + ii];
-          qi[u] = B.fq[b_lo + ii];
+        int4* s_mt = reinterpret_cast<int4*>(smem);  // trial, then current
+        float* s_mq = reinterpret_cast<float*>(s_mt + 2 * kPairGroup);
+        __syncthreads();  // the previous item may still read the staging area
+        for (int u = threadIdx.x; u < gn; u += kPairThreads) {
+          s_mt[u] = B.ftrial[g0 + u];
+          s_mt[kPairGroup + u] = B.fpos[b_lo + g0 + u];
+          s_mq[u] = B.fq[b_lo + g0 + u];
         }
-        for (int j = c0 + threadIdx.x; j < c1; j += kPairThreads) {
-          if (j >= b_lo && j < b_hi) continue;  // moved pairs: the last item
-          const int4 cj = B.fpos[j];
-          const float qj = B.fq[j];
-#pragma unroll
-          for (int u = 0; u < kPairGroup; u++) {
-            if (u < gn) {
-              float l1 = 0, r1 = 0, l0 = 0, r0 = 0;
-              pair32(P, ti[u], qi[u], cj, qj, l1, r1);
-              pair32(P, ci[u], qi[u], cj, qj, l0, r0);
-              acc_lj += l1 - l0;
-              acc_re += r1 - r0;
-            }
-          }
-        }
+        __syncthreads();
+        const PairConst K = pair_const(P);
+        if (P.single_image)
+          pair_sweep<true>(P, K, B, s_mt, s_mq, gn, c0, c1, b_lo, b_hi, acc_lj, acc_re);
+        else
+          pair_sweep<false>(P, K, B, s_mt, s_mq, gn, c0, c1, b_lo, b_hi, acc_lj, acc_re);
       } else {
         // pairs among the moved beads, each once (both trial / both current)
         const int lane = threadIdx.x & 31;
@@ -433,10 +496,14 @@ void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, 
                          kKTableBytes + 4096);
     cudaFuncSetAttribute(k_batch_delta32<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          kKTableBytes + 4096);
+    cudaFuncSetAttribute(k_batch_delta32<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kKTableBytes + 4096);
     attr = true;
   }
   const int grid = tune.grid > 0 ? tune.grid : pair_grid32();
-  if (tune.min_blocks == 3)
+  if (tune.min_blocks == 4)
+    k_batch_delta32<4><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune);
+  else if (tune.min_blocks == 3)
     k_batch_delta32<3><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune);
   else
     k_batch_delta32<2><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune);
