@@ -296,6 +296,14 @@ int plum_batch_set_tune(plum_batch* batch, int item_pairs, int k_tile, int grid,
  * register budgets {2, 3, 4} blocks per SM, keeps the fastest; out4 (may be
  * NULL) = the chosen {item_pairs, k_tile, grid, min_blocks}. */
 int plum_batch_autotune(plum_batch* batch, int steps, int* out4);
+/* The surrogate descriptor's cell lists (on by default for replicas of the
+ * precision form periodic on every axis with at least 3 cells of 7.5 sigma
+ * per axis). Off, every replica takes the all-pairs descriptor kernel; the
+ * descriptors are the same integers either way. */
+int plum_batch_set_cells(plum_batch* batch, int on);
+/* The descriptors of the replicas' last surrogate moves, out[R * 96] (the
+ * rows stay as they were for replicas whose last move was not one). */
+int plum_batch_descriptors(plum_batch* batch, float* out);
 
 /* ---------------------------------------------------------------------
  * Learned surrogate and delayed acceptance. No counterpart in the

@@ -120,6 +120,8 @@ def lib():
         L.plum_batch_set_surrogate.argtypes = [C.c_void_p, C.c_void_p]
         L.plum_batch_time_kernels.argtypes = [C.c_void_p, C.c_int, _dp]
         L.plum_batch_set_tune.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
+        L.plum_batch_set_cells.argtypes = [C.c_void_p, C.c_int]
+        L.plum_batch_descriptors.argtypes = [C.c_void_p, C.c_void_p]
         L.plum_batch_autotune.argtypes = [C.c_void_p, C.c_int, _ip]
         L.plum_batch_da_stats.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
         _lib = L
@@ -471,6 +473,17 @@ class Batch:
 
     def set_tune(self, item_pairs=4096, k_tile=128, grid=0, min_blocks=2):
         _check(lib().plum_batch_set_tune(self.h, item_pairs, k_tile, grid, min_blocks))
+
+    def set_cells(self, on=True):
+        """Surrogate descriptors through the cell lists (default) or the
+        all-pairs kernel; the same integers either way."""
+        _check(lib().plum_batch_set_cells(self.h, 1 if on else 0))
+
+    def descriptors(self):
+        """[replicas, 96] descriptors of the replicas' last surrogate moves."""
+        out = np.zeros((self.n, 96), np.float32)
+        _check(lib().plum_batch_descriptors(self.h, _ptr(out)))
+        return out
 
     def autotune(self, steps=16):
         """Times the energy-change kernel's work-item sizes on these replicas

@@ -308,13 +308,13 @@ void enqueue_loop(plum_ctx* c, int n_moves, const DevBuffers& B) {
   // before its energy change
   const bool desc = B.log_desc != nullptr;
   launch_serial64(c->P, B, kModeGen, c->s);
-  if (desc) launch_desc_batch(c->d_rp1, c->d_rb1, 1, B.desc_acc, c->P.form, c->s);
+  if (desc) launch_desc_batch(c->d_rp1, c->d_rb1, 1, B.desc_acc, c->P.form, 0, c->s);
   for (int i = 0; i < n_moves; i++) {
     launch_delta(c, B);
     int mode = kModeFinish | kModeDecide | (i + 1 < n_moves ? kModeGen : 0);
     launch_serial64(c->P, B, mode, c->s);
     if (desc && i + 1 < n_moves)
-      launch_desc_batch(c->d_rp1, c->d_rb1, 1, B.desc_acc, c->P.form, c->s);
+      launch_desc_batch(c->d_rp1, c->d_rb1, 1, B.desc_acc, c->P.form, 0, c->s);
   }
 }
 
@@ -896,7 +896,7 @@ int plum_move_descriptor(plum_ctx* c, double* out) {
   CK(cudaMemcpyAsync(c->d_rb1, &B, sizeof(B), cudaMemcpyHostToDevice, c->s));
   CK(cudaMemsetAsync(c->desc_fine, 0, sizeof(unsigned) * mlp::kFineAll, c->s));
   CK(cudaMemcpyAsync(&c->B.state->da_active, &one, sizeof(int), cudaMemcpyHostToDevice, c->s));
-  launch_desc_batch(c->d_rp1, c->d_rb1, 1, c->desc_acc, c->P.form, c->s);
+  launch_desc_batch(c->d_rp1, c->d_rb1, 1, c->desc_acc, c->P.form, 0, c->s);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(&c->B.state->da_active, &zero, sizeof(int), cudaMemcpyHostToDevice, c->s));
   unsigned h[mlp::kIn];
@@ -1501,6 +1501,11 @@ struct plum_batch {
   unsigned* d_fine = nullptr;
   const plum_surrogate* sg = nullptr;
   int* d_err = nullptr;
+  // descriptor cell lists (replicas that can have one)
+  int* d_cells = nullptr;
+  int cell_moved = 0;     // longest molecule among them (0: none)
+  bool cells_on = true;
+  int max_bead = 0;
 };
 
 namespace {
@@ -1509,11 +1514,19 @@ namespace {
 // decide + gen. With a surrogate, each gen is followed by the descriptors of
 // the generated chain moves and the surrogate's stage one, which marks the
 // moves it rejects so that the delta kernel skips them.
+// Cell lists are rebuilt from the positions at the start of every batch of
+// steps (or marked invalid when switched off).
+void cells_enqueue(plum_batch* b) {
+  if (b->sg && b->cell_moved)
+    launch_cell_rebuild(b->d_rp, b->d_rb, (int)b->reps.size(), b->max_bead, b->cells_on, b->s);
+}
+
 void batch_enqueue(plum_batch* b, int steps) {
   const int R = (int)b->reps.size();
+  cells_enqueue(b);
   auto stage_one = [&]() {
     if (!b->sg) return;
-    launch_desc_batch(b->d_rp, b->d_rb, R, b->d_desc, 1, b->s);
+    launch_desc_batch(b->d_rp, b->d_rb, R, b->d_desc, 1, b->cells_on ? b->cell_moved : 0, b->s);
     launch_mlp_infer_i(b->sg->net, b->d_desc, R, nullptr, DaArgs{b->d_sts, b->d_rp}, b->d_err,
                        b->s);
   };
@@ -1562,7 +1575,7 @@ int plum_batch_destroy(plum_batch* b) {
   cudaSetDevice(b->device);
   if (b->s) cudaStreamSynchronize(b->s);
   for (plum_ctx* c : b->reps) plum_ctx_destroy(c);
-  void* ptrs[] = {b->d_rp,    b->d_rb,  b->d_item_off, b->d_slots, b->d_states, b->d_outs,
+  void* ptrs[] = {b->d_cells, b->d_rp,    b->d_rb,  b->d_item_off, b->d_slots, b->d_states, b->d_outs,
                   b->d_sts,   b->d_pos, b->d_len,      b->d_cap,   b->d_gather, b->d_need,
                   b->d_desc,  b->d_err, b->d_fine};
   for (void* p : ptrs)
@@ -1662,6 +1675,49 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
   for (int r = 0; r < n; r++) {
     hb[r].desc_acc = b->d_desc + (size_t)mlp::kIn * r;
     hb[r].desc_fine = b->d_fine + (size_t)mlp::kFineAll * r;
+  }
+  // descriptor cell lists: periodic on every axis with at least 3 cells of
+  // the descriptor's cut per axis; cell_cap = 6 x the mean occupancy (at
+  // least 128) -- a cell that overflows sends its replica to the all-pairs
+  // kernel until the next rebuild
+  {
+    size_t words = 0;
+    std::vector<size_t> off(n, 0);
+    for (int r = 0; r < n; r++) {
+      DevParams& P = hp[r];
+      P.cell_cap = 0;
+      if (P.form != 1 || P.npbc != 3) continue;
+      int nc[3], cells = 1;
+      bool ok = true;
+      for (int a = 0; a < 3; a++) {
+        nc[a] = (int)std::floor(P.ebox[a] / ((double)mlp::kDescCut * 1.001));
+        nc[a] = std::min(nc[a], 64);
+        ok = ok && nc[a] >= 3;
+        cells *= std::max(nc[a], 1);
+      }
+      if (!ok) continue;
+      const int mean = (P.n_bead + cells - 1) / cells;
+      const int cap = std::max(128, 6 * mean);
+      for (int a = 0; a < 3; a++) P.cell_nc[a] = nc[a];
+      P.cell_cap = cap;
+      off[r] = words;
+      words += (size_t)P.n_bead + cells + (size_t)cells * cap;
+      b->cell_moved = std::max(b->cell_moved, std::min(b->reps[r]->max_len, 512));
+      b->max_bead = std::max(b->max_bead, P.n_bead);
+    }
+    if (words) {
+      if (dalloc(&b->d_cells, words)) {
+        plum_batch_destroy(b);
+        return PLUM_ERR_CUDA;
+      }
+      for (int r = 0; r < n; r++) {
+        if (!hp[r].cell_cap) continue;
+        const int cells = hp[r].cell_nc[0] * hp[r].cell_nc[1] * hp[r].cell_nc[2];
+        hb[r].cell_key = b->d_cells + off[r];
+        hb[r].cell_n = hb[r].cell_key + hp[r].n_bead;
+        hb[r].cell_beads = hb[r].cell_n + cells;
+      }
+    }
   }
   cudaMallocHost(&b->h_gather, sizeof(long long) * 6 * n);
   cudaMemcpy(b->d_rp, hp.data(), sizeof(DevParams) * n, cudaMemcpyHostToDevice);
@@ -1804,6 +1860,7 @@ int plum_batch_time_kernels(plum_batch* b, int n_steps, double* out4) {
     launch_mt_fill_batch(b->d_states, b->d_outs, b->d_pos, b->d_len, b->d_cap, b->d_need,
                          b->d_sts, R, b->s);
   }
+  cells_enqueue(b);
   // events around every kernel of the steps (plain launches, no graph)
   std::vector<cudaEvent_t> ev(2 * (4 * n_steps + 4));
   for (auto& e : ev) CK(cudaEventCreate(&e));
@@ -1819,7 +1876,9 @@ int plum_batch_time_kernels(plum_batch* b, int n_steps, double* out4) {
   };
   auto stage_one = [&]() {
     if (!b->sg) return PLUM_OK;
-    int rc = timed(2, [&] { launch_desc_batch(b->d_rp, b->d_rb, R, b->d_desc, 1, b->s); });
+    int rc = timed(2, [&] {
+      launch_desc_batch(b->d_rp, b->d_rb, R, b->d_desc, 1, b->cells_on ? b->cell_moved : 0, b->s);
+    });
     if (rc) return rc;
     return timed(3, [&] {
       launch_mlp_infer_i(b->sg->net, b->d_desc, R, nullptr, DaArgs{b->d_sts, b->d_rp}, b->d_err,
@@ -1864,6 +1923,26 @@ int plum_batch_set_tune(plum_batch* b, int item_pairs, int k_tile, int grid, int
       k_tile > kPairThreads || grid < 0 || grid > 65535 || min_blocks < 2 || min_blocks > 4)
     return fail(PLUM_ERR_INPUT, "bad work-item sizes");
   b->tune = BatchTune{item_pairs, k_tile, grid, min_blocks};
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->g_steps = 0;
+  return PLUM_OK;
+}
+
+int plum_batch_descriptors(plum_batch* b, float* out) {
+  if (!b || !out) return fail(PLUM_ERR_INPUT, "bad argument");
+  cudaSetDevice(b->device);
+  const size_t n = (size_t)mlp::kIn * b->reps.size();
+  std::vector<unsigned> h(n);
+  CK(cudaMemcpyAsync(h.data(), b->d_desc, sizeof(unsigned) * n, cudaMemcpyDeviceToHost, b->s));
+  CK(cudaStreamSynchronize(b->s));
+  for (size_t i = 0; i < n; i++) out[i] = (float)h[i] * mlp::kDescUnit;
+  return PLUM_OK;
+}
+
+int plum_batch_set_cells(plum_batch* b, int on) {
+  if (!b) return fail(PLUM_ERR_INPUT, "null batch");
+  b->cells_on = on != 0;
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   b->gexec = nullptr;
   b->g_steps = 0;

@@ -77,4 +77,15 @@ __device__ __forceinline__ int4 fix_point(const DevParams& P, double4_32a p, int
                    fix_axis(p.z, P.ebox[2], P.inv_fix[2], P.npbc > 2), type);
 }
 
+// Cell of a bead of the descriptor's cell list from its fixed-point
+// coordinates (fractions of the Ewald box in [0, 2^32)).
+__device__ __forceinline__ int cell_axis(unsigned x, int nc) {
+  return (int)(((unsigned long long)x * (unsigned)nc) >> 32);
+}
+__device__ __forceinline__ int cell_index(const DevParams& P, int4 f) {
+  return cell_axis((unsigned)f.x, P.cell_nc[0]) +
+         P.cell_nc[0] * (cell_axis((unsigned)f.y, P.cell_nc[1]) +
+                         P.cell_nc[1] * cell_axis((unsigned)f.z, P.cell_nc[2]));
+}
+
 }  // namespace plum

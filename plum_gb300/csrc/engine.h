@@ -78,6 +78,10 @@ struct DevParams {
   float f_lj_sig2[kMaxT2], f_lj_eps4[kMaxT2], f_lj_rc2[kMaxT2], f_lj_eref[kMaxT2];
   float f_real_cut, f_sqrt_alpha, f_lB;
   double inv_fix[3];     // 2^32 / Ewald box length (FP64 -> fixed point)
+  // cell list of the surrogate descriptor (replica batches, precision form,
+  // periodic on every axis): cell_nc cells per axis, each at least the
+  // descriptor's cut wide; cell_cap entries per cell (0: no cell list)
+  int cell_nc[3], cell_cap;
 };
 
 // The pending move: beads [b_lo, b_hi) of molecule `mol` hold trial
@@ -110,6 +114,10 @@ struct DevState {
   // computed). Counters: surrogate moves, stage-one passes, accepts.
   int da_on, da_active, da_skip, da_n_moves, da_n_pass, da_n_accept;
   double da_u1, da_s;
+  // the descriptor's cell list holds every bead (cleared when a cell
+  // overflowed: the all-pairs descriptor kernel then takes the replica
+  // until the next rebuild)
+  int cell_ok;
   // training log of (descriptor, exact dE) for surrogate moves (log_desc set)
   int log_n, log_cap;
 };
@@ -145,9 +153,17 @@ struct DevBuffers {  // all pointers: copied word-wise into shared memory by the
   // surrogate: descriptor of the pending move [96] (integer units of
   // 2^-12), its fine distance histogram, and the optional training log
   unsigned* desc_acc;
-  unsigned* desc_fine;  // [4][240] pair counts per 1/32-sigma distance bin
+  unsigned* desc_fine;  // [4][241] pair counts per 1/32-sigma distance bin
   float* log_desc;   // [log_cap][96]
   double* log_de;    // [log_cap]
+  // descriptor cell list (null when the replica has none): cell_beads
+  // [cells][cell_cap] holds bead indices appended per cell, cell_n the
+  // entries used; an entry e = c * cell_cap + k is live iff cell_key[bead]
+  // == e (a bead that changes cell is appended to its new cell and its old
+  // entry goes stale; each rebuild compacts)
+  int* cell_key;     // [n_bead]
+  int* cell_n;       // [cells]
+  int* cell_beads;   // [cells * cell_cap]
 };
 
 // Launch helpers (kern_energy.cu / kern_moves.cu). All enqueue on `s`.

@@ -29,6 +29,7 @@
 #include <cstdio>
 #include <type_traits>
 
+#include "device_common.cuh"
 #include "mlp.h"
 
 namespace plum {
@@ -529,6 +530,21 @@ __device__ __forceinline__ float wrap32(double d, float L, float invL, bool peri
   return periodic ? f - L * rintf(f * invL) : f;
 }
 
+// Squared distance of two fixed-point positions (b - a, minimum image by
+// integer wraparound) with every rounding pinned (no contraction), so the
+// all-pairs and the cell-list kernels give the same bins bit for bit.
+__device__ __forceinline__ float desc_r2_fix(const DevParams& P, int4 a, int4 b) {
+  const float dx = __fmul_rn((float)(int)((unsigned)b.x - (unsigned)a.x), P.f_scale[0]);
+  const float dy = __fmul_rn((float)(int)((unsigned)b.y - (unsigned)a.y), P.f_scale[1]);
+  const float dz = __fmul_rn((float)(int)((unsigned)b.z - (unsigned)a.z), P.f_scale[2]);
+  return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+}
+
+// Fine distance bin floor(32 r + 1/2) of a squared distance within the cut.
+__device__ __forceinline__ int fine_bin(float r2) {
+  return __float2int_rz(__fadd_rn(__fmul_rn(sqrtf(r2), (float)kFinePerSigma), 0.5f));
+}
+
 // A bead position as the descriptor kernel keeps it: form 1 the fixed-point
 // mirror (x, y, z, type); form 0 FP64 (x, y, z) and the type.
 template <int kForm>
@@ -567,17 +583,14 @@ __device__ __forceinline__ int ptype(const DPos<kForm>& p) {
 template <int kForm>
 __device__ __forceinline__ float dist2(const DevParams& P, const DPos<kForm>& a,
                                        const DPos<kForm>& b) {
-  float dx, dy, dz;
   if constexpr (kForm == 1) {
-    dx = (float)(int)((unsigned)b.f.x - (unsigned)a.f.x) * P.f_scale[0];
-    dy = (float)(int)((unsigned)b.f.y - (unsigned)a.f.y) * P.f_scale[1];
-    dz = (float)(int)((unsigned)b.f.z - (unsigned)a.f.z) * P.f_scale[2];
+    return desc_r2_fix(P, a.f, b.f);
   } else {
-    dx = wrap32(b.x - a.x, (float)P.box[0], (float)P.inv_box[0], P.npbc > 0);
-    dy = wrap32(b.y - a.y, (float)P.box[1], (float)P.inv_box[1], P.npbc > 1);
-    dz = wrap32(b.z - a.z, (float)P.box[2], (float)P.inv_box[2], P.npbc > 2);
+    const float dx = wrap32(b.x - a.x, (float)P.box[0], (float)P.inv_box[0], P.npbc > 0);
+    const float dy = wrap32(b.y - a.y, (float)P.box[1], (float)P.inv_box[1], P.npbc > 1);
+    const float dz = wrap32(b.z - a.z, (float)P.box[2], (float)P.inv_box[2], P.npbc > 2);
+    return dx * dx + dy * dy + dz * dz;
   }
-  return dx * dx + dy * dy + dz * dz;
 }
 
 // Per-axis pre-test: a pair can only be within the cut when every axis
@@ -616,7 +629,9 @@ __global__ void __launch_bounds__(kDescThreads)
   __shared__ int s_bl[2];
   for (int r = threadIdx.x; r < n_rep; r += blockDim.x) {
     const DevState* st = rb[r].state;
-    const int m = (st->pending && st->da_active) ? min(st->b_hi - st->b_lo, kDescMaxMoved) : 0;
+    const bool cells = rp[r].cell_cap && rb[r].cell_key && st->cell_ok;  // k_desc_cells
+    const int m = (st->pending && st->da_active && !cells)
+                      ? min(st->b_hi - st->b_lo, kDescMaxMoved) : 0;
     s_pref[r + 1] = ((rp[r].n_bead + kDescThreads - 1) / kDescThreads) *
                     ((m + kDescSlab - 1) / kDescSlab);
   }
@@ -700,20 +715,112 @@ __global__ void __launch_bounds__(kDescThreads)
         const int cls = ptype<kForm>(ic) == tj ? 0 : 1;
         if (nb) {
           const float r0 = dist2<kForm>(P, ic, jc);
-          if (r0 < kDescCut * kDescCut)
-            atomicAdd(&fh[cls * kFine + (int)(sqrtf(r0) * (float)kFinePerSigma + 0.5f)], 1u);
+          if (r0 < kDescCut * kDescCut) atomicAdd(&fh[cls * kFine + fine_bin(r0)], 1u);
         }
         if (na) {
           const float r1 = dist2<kForm>(P, it, jt);
-          if (r1 < kDescCut * kDescCut)
-            atomicAdd(&fh[(2 + cls) * kFine + (int)(sqrtf(r1) * (float)kFinePerSigma + 0.5f)],
-                      1u);
+          if (r1 < kDescCut * kDescCut) atomicAdd(&fh[(2 + cls) * kFine + fine_bin(r1)], 1u);
         }
       }
     }
   }
   __syncthreads();
   if (cur >= 0) flush();
+}
+
+// ------------------------------------------------- descriptor cell list
+// Replicas with a cell list (precision form, periodic on every axis, cells at
+// least the cut wide) take the descriptor from k_desc_cells: the pairs
+// within the cut of a moved bead lie in the 27 cells around it, about
+// 27 x N / cells candidates instead of N. The list is rebuilt (compacted) at
+// the start of every batch of steps and kept up to date by the serial step,
+// which appends each accepted bead that changed cell (kern_moves.cu).
+__global__ void k_cell_reset(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb) {
+  const DevParams& P = rp[blockIdx.x];
+  const DevBuffers& B = rb[blockIdx.x];
+  if (!P.cell_cap || !B.cell_key) return;
+  const int cells = P.cell_nc[0] * P.cell_nc[1] * P.cell_nc[2];
+  for (int c = threadIdx.x; c < cells; c += blockDim.x) B.cell_n[c] = 0;
+  if (threadIdx.x == 0) B.state->cell_ok = 1;
+}
+
+__global__ void k_cell_fill(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb) {
+  const DevParams& P = rp[blockIdx.y];
+  const DevBuffers& B = rb[blockIdx.y];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!P.cell_cap || !B.cell_key || j >= P.n_bead) return;
+  const int c = cell_index(P, B.fpos[j]);
+  const int k = atomicAdd(&B.cell_n[c], 1);
+  if (k < P.cell_cap) {
+    B.cell_beads[c * P.cell_cap + k] = j;
+    B.cell_key[j] = c * P.cell_cap + k;
+  } else {
+    B.cell_key[j] = -1;
+    B.state->cell_ok = 0;
+  }
+}
+
+constexpr int kCellWarps = 8;  // moved beads per block, a warp each
+
+// Block (x, r): moved beads [8x, 8x + 8) of replica r's pending surrogate
+// move, a warp per bead: before the move (channels 0, 1) the beads of the 27
+// cells around its current position, after the move (channels 2, 3) around
+// its trial position, skipping the moved beads (their pairs, each once, at
+// the end). The same pairs, distances and bins as k_desc.
+__global__ void __launch_bounds__(kCellWarps * 32)
+    k_desc_cells(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb) {
+  const DevParams& P = rp[blockIdx.y];
+  const DevBuffers& B = rb[blockIdx.y];
+  if (!P.cell_cap || !B.cell_key) return;
+  const DevState* st = B.state;
+  if (!(st->pending && st->da_active && st->cell_ok)) return;
+  const int b_lo = st->b_lo, m = min(st->b_hi - b_lo, kDescMaxMoved);
+  if ((int)blockIdx.x * kCellWarps >= m) return;
+  __shared__ unsigned fh[kFineAll];
+  for (int k = threadIdx.x; k < kFineAll; k += blockDim.x) fh[k] = 0u;
+  __syncthreads();
+  const int q = blockIdx.x * kCellWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (q < m) {
+    const int4 ic = B.fpos[b_lo + q], it = B.ftrial[q];
+    const int cap = P.cell_cap, nx = P.cell_nc[0], ny = P.cell_nc[1], nz = P.cell_nc[2];
+    const float cut2 = kDescCut * kDescCut;
+    for (int ch = 0; ch < 2; ch++) {
+      const int4 p = ch ? it : ic;
+      const int cx = cell_axis((unsigned)p.x, nx), cy = cell_axis((unsigned)p.y, ny),
+                cz = cell_axis((unsigned)p.z, nz);
+      for (int oz = -1; oz <= 1; oz++) {
+        const int z = cz + oz < 0 ? cz + oz + nz : (cz + oz >= nz ? cz + oz - nz : cz + oz);
+        for (int oy = -1; oy <= 1; oy++) {
+          const int y = cy + oy < 0 ? cy + oy + ny : (cy + oy >= ny ? cy + oy - ny : cy + oy);
+          for (int ox = -1; ox <= 1; ox++) {
+            const int x = cx + ox < 0 ? cx + ox + nx : (cx + ox >= nx ? cx + ox - nx : cx + ox);
+            const int base = (x + nx * (y + ny * z)) * cap;
+            const int n = min(B.cell_n[base / cap], cap);
+            for (int e = lane; e < n; e += 32) {
+              const int j = B.cell_beads[base + e];
+              if (B.cell_key[j] != base + e) continue;  // stale: moved to another cell
+              if (j >= b_lo && j < b_lo + m) continue;  // moved pairs below
+              const int4 jc = B.fpos[j];
+              const float r2 = desc_r2_fix(P, p, jc);
+              if (r2 < cut2)
+                atomicAdd(&fh[(2 * ch + (ic.w == jc.w ? 0 : 1)) * kFine + fine_bin(r2)], 1u);
+            }
+          }
+        }
+      }
+    }
+    for (int q2 = q + 1 + lane; q2 < m; q2 += 32) {
+      const int4 c2 = B.fpos[b_lo + q2], t2 = B.ftrial[q2];
+      const int cls = ic.w == c2.w ? 0 : 1;
+      float r2 = desc_r2_fix(P, ic, c2);
+      if (r2 < cut2) atomicAdd(&fh[cls * kFine + fine_bin(r2)], 1u);
+      r2 = desc_r2_fix(P, it, t2);
+      if (r2 < cut2) atomicAdd(&fh[(2 + cls) * kFine + fine_bin(r2)], 1u);
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < kFineAll; k += blockDim.x)
+    if (fh[k]) atomicAdd(&B.desc_fine[k], fh[k]);
 }
 
 // One block per replica: bin k of channel c = sum_f count[c][f] *
@@ -817,9 +924,26 @@ void launch_desc_counts(const DevParams* rp, const DevBuffers* rb, int n_rep, in
   else k_desc<0><<<4 * 152, kDescThreads, 0, st>>>(rp, rb, n_rep);
 }
 
+__global__ void k_cell_off(const DevBuffers* __restrict__ rb) {
+  if (threadIdx.x == 0) rb[blockIdx.x].state->cell_ok = 0;
+}
+
+void launch_cell_rebuild(const DevParams* rp, const DevBuffers* rb, int n_rep, int max_bead,
+                         int on, cudaStream_t st) {
+  if (!on) {
+    k_cell_off<<<n_rep, 32, 0, st>>>(rb);
+    return;
+  }
+  k_cell_reset<<<n_rep, 256, 0, st>>>(rp, rb);
+  k_cell_fill<<<dim3((max_bead + 255) / 256, n_rep), 256, 0, st>>>(rp, rb);
+}
+
 void launch_desc_batch(const DevParams* rp, const DevBuffers* rb, int n_rep, unsigned* acc,
-                       int form, cudaStream_t st) {
+                       int form, int cell_moved, cudaStream_t st) {
   (void)acc;
+  if (cell_moved > 0)
+    k_desc_cells<<<dim3((std::min(cell_moved, kDescMaxMoved) + kCellWarps - 1) / kCellWarps,
+                        n_rep), kCellWarps * 32, 0, st>>>(rp, rb);
   launch_desc_counts(rp, rb, n_rep, form, st);
   // programmatic dependent of k_desc (it waits for the counts itself)
   cudaLaunchConfig_t cfg = {};

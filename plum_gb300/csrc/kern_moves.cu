@@ -644,6 +644,20 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
       for (int i = b_lo + threadIdx.x; i < b_hi; i += blockDim.x) {
         B.pos[i] = B.trial[i];
         if (P.form) B.fpos[i] = B.ftrial[i - b_lo];
+        if (P.cell_cap && B.cell_key) {
+          // a bead that changes cell is appended to the new one; its old
+          // entry goes stale (cell_key no longer points at it)
+          const int c = cell_index(P, B.ftrial[i - b_lo]);
+          if (B.cell_key[i] / P.cell_cap != c) {
+            const int k = atomicAdd(&B.cell_n[c], 1);
+            if (k < P.cell_cap) {
+              B.cell_beads[c * P.cell_cap + k] = i;
+              B.cell_key[i] = c * P.cell_cap + k;
+            } else {
+              S.cell_ok = 0;  // every writer stores the same value
+            }
+          }
+        }
       }
     } else {
       for (int i = b_lo + threadIdx.x; i < b_hi; i += blockDim.x) B.trial[i] = B.pos[i];

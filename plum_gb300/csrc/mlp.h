@@ -95,8 +95,16 @@ void launch_mlp_pack(const float* param, MlpNet* net, cudaStream_t st);
 // desc_fine counts must be zero on entry; only replicas with da_active are
 // processed). form 1 reads the fixed-point mirrors, form 0 the FP64
 // positions. acc is the base of the batch's contiguous desc_acc rows.
+// cell_moved > 0 (the longest molecule of replicas that have a cell list)
+// first runs the cell-list kernel for the replicas whose list is valid; the
+// all-pairs kernel takes the others.
 void launch_desc_batch(const DevParams* rp, const DevBuffers* rb, int n_rep, unsigned* acc,
-                       int form, cudaStream_t st);
+                       int form, int cell_moved, cudaStream_t st);
+// Rebuilds the replicas' descriptor cell lists from their fixed-point
+// positions (replicas without one are skipped); max_bead = largest n_bead.
+// on = 0 marks every list invalid instead (the all-pairs kernel takes all).
+void launch_cell_rebuild(const DevParams* rp, const DevBuffers* rb, int n_rep, int max_bead,
+                         int on, cudaStream_t st);
 // The fine counts only (k_desc).
 void launch_desc_counts(const DevParams* rp, const DevBuffers* rb, int n_rep, int form,
                         cudaStream_t st);

@@ -113,3 +113,38 @@ def test_gain_over_the_method_without_the_network(pg, trained):
           "rmse", st["rmse_vs_fp64"])
     assert gain > 1.5
     assert s["chain_acc"] > 0.5 * p["chain_acc"]
+
+
+@pytest.mark.parametrize("workload,replicas,blocks", [("bulk_1000", 8, 20), ("bulk_20000_pinned", 2, 8)])
+def test_cell_list_descriptors_equal_all_pairs(pg, tmp_path, workload, replicas, blocks):
+    """The descriptor cell lists (rebuilt per batch of steps, appended to on
+    every accepted move) give the all-pairs kernel's integers: two batches
+    from the same starts and seeds, one with and one without the lists,
+    produce the same descriptors after every batch of steps and so the same
+    stage-one decisions and trajectories."""
+    from plum_gb300 import surrogate as S
+    from plum_gb300 import systems
+    d = str(tmp_path / workload)
+    systems.write_bulk(d, systems.CONFIGS[workload], seed=5)
+    here = os.path.dirname(os.path.abspath(__file__))
+    sg = S.load(os.path.join(here, "..", "plum_gb300", "data",
+                             "surrogate_bulk_20000_pinned.npz"))
+    out = []
+    for on in (True, False):
+        b = pg.Batch([d] * replicas)
+        b.seed(np.arange(42, 42 + replicas, dtype=np.uint32))
+        b.set_surrogate(sg)
+        b.set_cells(on)
+        desc = []
+        for _ in range(blocks):
+            b.run(25)
+            desc.append(b.descriptors())
+        out.append((np.array(desc), [b.replica(r).positions() for r in range(replicas)],
+                    b.da_stats()))
+        b.close()
+    (da, pa, sa), (db, pb, sb) = out
+    assert sa[0] > 0 and da.any()
+    np.testing.assert_array_equal(da, db)
+    for x, y in zip(pa, pb):
+        np.testing.assert_array_equal(x, y)
+    assert tuple(sa) == tuple(sb)
