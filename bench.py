@@ -488,6 +488,9 @@ def main():
               "exact_evaluations_skipped": (mv - ps) / float(R * BS * args.steps),
               "margin_kT": args.da_margin,
               "weights": os.path.relpath(wpath, ROOT), "training": sg_meta}
+        cs = batch.cell_stats()
+        da["descriptor_cell_lists"] = {"replicas": cs[0], "valid_after_timed_steps": cs[1],
+                                       "most_entries_in_a_cell": cs[2], "entries_per_cell": cs[3]}
     # per-kernel CUDA-event durations over a few more steps (plain launches)
     kern_ms = batch.time_kernels(32)
 

@@ -301,6 +301,14 @@ int plum_batch_autotune(plum_batch* batch, int steps, int* out4);
  * per axis). Off, every replica takes the all-pairs descriptor kernel; the
  * descriptors are the same integers either way. */
 int plum_batch_set_cells(plum_batch* batch, int on);
+/* Entries per cell of the descriptor cell lists (reallocates them). A cell
+ * that overflows sends its replica to the all-pairs descriptor kernel until
+ * the next batch of steps, and doubles the entries per cell. */
+int plum_batch_set_cell_cap(plum_batch* batch, int cap);
+/* out4 = {replicas with a descriptor cell list, of which valid (no cell
+ * overflowed since the last rebuild), most entries in one cell (live and
+ * stale), entries per cell}. For diagnostics. */
+int plum_batch_cell_stats(plum_batch* batch, int* out4);
 /* The descriptors of the replicas' last surrogate moves, out[R * 96] (the
  * rows stay as they were for replicas whose last move was not one). */
 int plum_batch_descriptors(plum_batch* batch, float* out);

@@ -1505,7 +1505,10 @@ struct plum_batch {
   int* d_cells = nullptr;
   int cell_moved = 0;     // longest molecule among them (0: none)
   bool cells_on = true;
+  bool cells_built = false;  // a batch of steps with the surrogate has rebuilt them
   int max_bead = 0;
+  std::vector<DevParams> h_rp;   // host copies of d_rp, d_rb
+  std::vector<DevBuffers> h_rb;
 };
 
 namespace {
@@ -1514,11 +1517,79 @@ namespace {
 // decide + gen. With a surrogate, each gen is followed by the descriptors of
 // the generated chain moves and the surrogate's stage one, which marks the
 // moves it rejects so that the delta kernel skips them.
+// (Re)allocates the descriptor cell lists of the replicas that have one
+// (h_rp[r].cell_cap > 0): per replica cell_key [n_bead], cell_n [cells] and,
+// on a 16-byte boundary, cell_ent [cells * cell_cap]; then uploads the
+// parameter and buffer tables.
+int cells_alloc(plum_batch* b) {
+  const int n = (int)b->reps.size();
+  if (b->d_cells) {
+    CK(cudaStreamSynchronize(b->s));
+    cudaFree(b->d_cells);
+    b->d_cells = nullptr;
+  }
+  size_t words = 0;
+  std::vector<size_t> off(n, 0);
+  for (int r = 0; r < n; r++) {
+    const DevParams& P = b->h_rp[r];
+    if (!P.cell_cap) continue;
+    const size_t cells = (size_t)P.cell_nc[0] * P.cell_nc[1] * P.cell_nc[2];
+    off[r] = words;
+    words += ((size_t)P.n_bead + cells + 3) / 4 * 4 + 4 * cells * P.cell_cap;
+  }
+  if (words && dalloc(&b->d_cells, words)) return PLUM_ERR_CUDA;
+  for (int r = 0; r < n; r++) {
+    const DevParams& P = b->h_rp[r];
+    DevBuffers& B = b->h_rb[r];
+    if (!P.cell_cap) continue;
+    const size_t cells = (size_t)P.cell_nc[0] * P.cell_nc[1] * P.cell_nc[2];
+    B.cell_key = b->d_cells + off[r];
+    B.cell_n = B.cell_key + P.n_bead;
+    B.cell_ent = reinterpret_cast<int4*>(B.cell_key + ((size_t)P.n_bead + cells + 3) / 4 * 4);
+  }
+  if (b->d_rp) {
+    CK(cudaMemcpyAsync(b->d_rp, b->h_rp.data(), sizeof(DevParams) * n, cudaMemcpyHostToDevice,
+                       b->s));
+    CK(cudaMemcpyAsync(b->d_rb, b->h_rb.data(), sizeof(DevBuffers) * n, cudaMemcpyHostToDevice,
+                       b->s));
+    CK(cudaStreamSynchronize(b->s));
+  }
+  b->cells_built = false;
+  return PLUM_OK;
+}
+
 // Cell lists are rebuilt from the positions at the start of every batch of
 // steps (or marked invalid when switched off).
 void cells_enqueue(plum_batch* b) {
   if (b->sg && b->cell_moved)
     launch_cell_rebuild(b->d_rp, b->d_rb, (int)b->reps.size(), b->max_bead, b->cells_on, b->s);
+}
+
+// Kernel launches of batch_enqueue(b, steps).
+long batch_kernels(const plum_batch* b, int steps) {
+  const bool cells = b->sg && b->cell_moved;
+  const long stage = b->sg ? (cells && b->cells_on ? 3 : 2) + 1 : 0;
+  return (cells ? (b->cells_on ? 2 : 1) : 0) + 1 + 2L * steps + steps * stage;
+}
+
+// After a batch of steps: a replica whose cell list overflowed doubles every
+// list's entries per cell (and the graph is captured again).
+int cells_check(plum_batch* b) {
+  if (!(b->sg && b->cell_moved && b->cells_on)) return PLUM_OK;
+  if (!b->cells_built) {
+    b->cells_built = true;
+    return PLUM_OK;
+  }
+  bool over = false;
+  for (size_t r = 0; r < b->reps.size(); r++)
+    over |= b->h_rp[r].cell_cap && !b->h_gather[6 * r + 5];
+  if (!over) return PLUM_OK;
+  for (auto& P : b->h_rp)
+    if (P.cell_cap) P.cell_cap *= 2;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->g_steps = 0;
+  return cells_alloc(b);
 }
 
 void batch_enqueue(plum_batch* b, int steps) {
@@ -1677,48 +1748,36 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
     hb[r].desc_fine = b->d_fine + (size_t)mlp::kFineAll * r;
   }
   // descriptor cell lists: periodic on every axis with at least 3 cells of
-  // the descriptor's cut per axis; cell_cap = 6 x the mean occupancy (at
-  // least 128) -- a cell that overflows sends its replica to the all-pairs
-  // kernel until the next rebuild
-  {
-    size_t words = 0;
-    std::vector<size_t> off(n, 0);
-    for (int r = 0; r < n; r++) {
-      DevParams& P = hp[r];
-      P.cell_cap = 0;
-      if (P.form != 1 || P.npbc != 3) continue;
-      int nc[3], cells = 1;
-      bool ok = true;
-      for (int a = 0; a < 3; a++) {
-        nc[a] = (int)std::floor(P.ebox[a] / ((double)mlp::kDescCut * 1.001));
-        nc[a] = std::min(nc[a], 64);
-        ok = ok && nc[a] >= 3;
-        cells *= std::max(nc[a], 1);
-      }
-      if (!ok) continue;
-      const int mean = (P.n_bead + cells - 1) / cells;
-      const int cap = std::max(128, 6 * mean);
-      for (int a = 0; a < 3; a++) P.cell_nc[a] = nc[a];
-      P.cell_cap = cap;
-      off[r] = words;
-      words += (size_t)P.n_bead + cells + (size_t)cells * cap;
-      b->cell_moved = std::max(b->cell_moved, std::min(b->reps[r]->max_len, 512));
-      b->max_bead = std::max(b->max_bead, P.n_bead);
+  // the descriptor's cut per axis; cell_cap = 8 x the mean occupancy + 64
+  // (at least 128), doubled whenever a cell overflowed during a batch of
+  // steps (the overflowing replica takes the all-pairs kernel until then)
+  for (int r = 0; r < n; r++) {
+    DevParams& P = hp[r];
+    P.cell_cap = 0;
+    if (P.form != 1 || P.npbc != 3) continue;
+    int nc[3], cells = 1;
+    bool ok = true;
+    for (int a = 0; a < 3; a++) {
+      nc[a] = (int)std::floor(P.ebox[a] / ((double)mlp::kDescCut * 1.001));
+      nc[a] = std::min(nc[a], 64);
+      ok = ok && nc[a] >= 3;
+      cells *= std::max(nc[a], 1);
     }
-    if (words) {
-      if (dalloc(&b->d_cells, words)) {
-        plum_batch_destroy(b);
-        return PLUM_ERR_CUDA;
-      }
-      for (int r = 0; r < n; r++) {
-        if (!hp[r].cell_cap) continue;
-        const int cells = hp[r].cell_nc[0] * hp[r].cell_nc[1] * hp[r].cell_nc[2];
-        hb[r].cell_key = b->d_cells + off[r];
-        hb[r].cell_n = hb[r].cell_key + hp[r].n_bead;
-        hb[r].cell_beads = hb[r].cell_n + cells;
-      }
-    }
+    if (!ok) continue;
+    const int mean = (P.n_bead + cells - 1) / cells;
+    for (int a = 0; a < 3; a++) P.cell_nc[a] = nc[a];
+    P.cell_cap = std::max(128, 8 * mean + 64);
+    b->cell_moved = std::max(b->cell_moved, std::min(b->reps[r]->max_len, 512));
+    b->max_bead = std::max(b->max_bead, P.n_bead);
   }
+  b->h_rp = hp;
+  b->h_rb = hb;
+  if (b->cell_moved && cells_alloc(b)) {
+    plum_batch_destroy(b);
+    return PLUM_ERR_CUDA;
+  }
+  hp = b->h_rp;
+  hb = b->h_rb;
   cudaMallocHost(&b->h_gather, sizeof(long long) * 6 * n);
   cudaMemcpy(b->d_rp, hp.data(), sizeof(DevParams) * n, cudaMemcpyHostToDevice);
   cudaMemcpy(b->d_rb, hb.data(), sizeof(DevBuffers) * n, cudaMemcpyHostToDevice);
@@ -1793,6 +1852,8 @@ int plum_batch_run(plum_batch* b, int n_steps, long* accepted_out) {
       any |= need[r] != 0;
     }
     first = false;
+    const int crc = cells_check(b);
+    if (crc) return crc;
     if (any) {
       CK(cudaMemcpyAsync(b->d_need, need.data(), sizeof(int) * R, cudaMemcpyHostToDevice, b->s));
       CK(cudaMemcpyAsync(b->d_pos, pos.data(), sizeof(long long) * R, cudaMemcpyHostToDevice, b->s));
@@ -1803,7 +1864,7 @@ int plum_batch_run(plum_batch* b, int n_steps, long* accepted_out) {
     }
     int rc = batch_steps_graph(b, steps);
     if (rc) return rc;
-    b->last_kernels += 1 + 2L * steps + (b->sg ? 2L * steps : 0);
+    b->last_kernels += batch_kernels(b, steps);
     done += steps;
   }
   CK(cudaEventRecord(b->ev1, b->s));
@@ -1940,9 +2001,54 @@ int plum_batch_descriptors(plum_batch* b, float* out) {
   return PLUM_OK;
 }
 
+int plum_batch_cell_stats(plum_batch* b, int* out4) {
+  if (!b || !out4) return fail(PLUM_ERR_INPUT, "bad argument");
+  cudaSetDevice(b->device);
+  int with = 0, ok = 0, most = 0, cap = 0;
+  std::vector<DevBuffers> hb(b->reps.size());
+  std::vector<DevParams> hp(b->reps.size());
+  CK(cudaMemcpyAsync(hb.data(), b->d_rb, sizeof(DevBuffers) * hb.size(), cudaMemcpyDeviceToHost,
+                     b->s));
+  CK(cudaMemcpyAsync(hp.data(), b->d_rp, sizeof(DevParams) * hp.size(), cudaMemcpyDeviceToHost,
+                     b->s));
+  CK(cudaStreamSynchronize(b->s));
+  for (size_t r = 0; r < b->reps.size(); r++) {
+    if (!hp[r].cell_cap || !hb[r].cell_n) continue;
+    with++;
+    cap = std::max(cap, hp[r].cell_cap);
+    DevState st;
+    int rc = read_state(b->reps[r], &st);
+    if (rc) return rc;
+    ok += st.cell_ok ? 1 : 0;
+    const int cells = hp[r].cell_nc[0] * hp[r].cell_nc[1] * hp[r].cell_nc[2];
+    std::vector<int> n(cells);
+    CK(cudaMemcpyAsync(n.data(), hb[r].cell_n, sizeof(int) * cells, cudaMemcpyDeviceToHost, b->s));
+    CK(cudaStreamSynchronize(b->s));
+    for (int v : n) most = std::max(most, v);
+  }
+  out4[0] = with;
+  out4[1] = ok;
+  out4[2] = most;
+  out4[3] = cap;
+  return PLUM_OK;
+}
+
+int plum_batch_set_cell_cap(plum_batch* b, int cap) {
+  if (!b || cap < 1 || cap > (1 << 20)) return fail(PLUM_ERR_INPUT, "bad argument");
+  cudaSetDevice(b->device);
+  if (!b->cell_moved) return PLUM_OK;
+  for (auto& P : b->h_rp)
+    if (P.cell_cap) P.cell_cap = cap;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->g_steps = 0;
+  return cells_alloc(b);
+}
+
 int plum_batch_set_cells(plum_batch* b, int on) {
   if (!b) return fail(PLUM_ERR_INPUT, "null batch");
   b->cells_on = on != 0;
+  b->cells_built = false;
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   b->gexec = nullptr;
   b->g_steps = 0;
@@ -2000,6 +2106,7 @@ int plum_batch_set_surrogate(plum_batch* b, const plum_surrogate* sg) {
     CK(cudaMemcpy(c->B.state, &st, sizeof(DevState), cudaMemcpyHostToDevice));
   }
   b->sg = sg;
+  b->cells_built = false;
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   b->gexec = nullptr;
   b->g_steps = 0;

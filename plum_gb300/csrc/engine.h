@@ -156,14 +156,15 @@ struct DevBuffers {  // all pointers: copied word-wise into shared memory by the
   unsigned* desc_fine;  // [4][241] pair counts per 1/32-sigma distance bin
   float* log_desc;   // [log_cap][96]
   double* log_de;    // [log_cap]
-  // descriptor cell list (null when the replica has none): cell_beads
-  // [cells][cell_cap] holds bead indices appended per cell, cell_n the
-  // entries used; an entry e = c * cell_cap + k is live iff cell_key[bead]
-  // == e (a bead that changes cell is appended to its new cell and its old
-  // entry goes stale; each rebuild compacts)
+  // descriptor cell list (null when the replica has none): cell_ent
+  // [cells][cell_cap] holds entries (X, Y, Z, bead << 3 | type) appended per
+  // cell, cell_n the entries used, cell_key the entry of each bead. An
+  // accepted bead rewrites its entry in place, or, when it changes cell,
+  // marks the old entry dead (w = -1) and appends a new one; each rebuild
+  // compacts.
   int* cell_key;     // [n_bead]
   int* cell_n;       // [cells]
-  int* cell_beads;   // [cells * cell_cap]
+  int4* cell_ent;    // [cells * cell_cap]
 };
 
 // Launch helpers (kern_energy.cu / kern_moves.cu). All enqueue on `s`.

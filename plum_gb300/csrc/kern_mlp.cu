@@ -749,10 +749,11 @@ __global__ void k_cell_fill(const DevParams* __restrict__ rp, const DevBuffers* 
   const DevBuffers& B = rb[blockIdx.y];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (!P.cell_cap || !B.cell_key || j >= P.n_bead) return;
-  const int c = cell_index(P, B.fpos[j]);
+  const int4 f = B.fpos[j];
+  const int c = cell_index(P, f);
   const int k = atomicAdd(&B.cell_n[c], 1);
   if (k < P.cell_cap) {
-    B.cell_beads[c * P.cell_cap + k] = j;
+    B.cell_ent[c * P.cell_cap + k] = make_int4(f.x, f.y, f.z, (j << 3) | f.w);
     B.cell_key[j] = c * P.cell_cap + k;
   } else {
     B.cell_key[j] = -1;
@@ -760,14 +761,16 @@ __global__ void k_cell_fill(const DevParams* __restrict__ rp, const DevBuffers* 
   }
 }
 
-constexpr int kCellWarps = 8;  // moved beads per block, a warp each
+constexpr int kCellBeads = 4;  // moved beads per block: a warp per (bead, before / after)
 
-// Block (x, r): moved beads [8x, 8x + 8) of replica r's pending surrogate
-// move, a warp per bead: before the move (channels 0, 1) the beads of the 27
-// cells around its current position, after the move (channels 2, 3) around
-// its trial position, skipping the moved beads (their pairs, each once, at
-// the end). The same pairs, distances and bins as k_desc.
-__global__ void __launch_bounds__(kCellWarps * 32)
+// Block (x, r): moved beads [4x, 4x + 4) of replica r's pending surrogate
+// move. Warp (bead, channel pair): before the move (channels 0, 1) the
+// entries of the 27 cells around the bead's current position, after it
+// (channels 2, 3) around its trial position, skipping the moved beads (their
+// pairs, each once, at the end). Entries carry the positions, so a candidate
+// costs one load, and the 27 cells' entries form one list spread over the
+// lanes (independent loads). The same pairs, distances and bins as k_desc.
+__global__ void __launch_bounds__(2 * kCellBeads * 32)
     k_desc_cells(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb) {
   const DevParams& P = rp[blockIdx.y];
   const DevBuffers& B = rb[blockIdx.y];
@@ -775,47 +778,64 @@ __global__ void __launch_bounds__(kCellWarps * 32)
   const DevState* st = B.state;
   if (!(st->pending && st->da_active && st->cell_ok)) return;
   const int b_lo = st->b_lo, m = min(st->b_hi - b_lo, kDescMaxMoved);
-  if ((int)blockIdx.x * kCellWarps >= m) return;
+  if ((int)blockIdx.x * kCellBeads >= m) return;
   __shared__ unsigned fh[kFineAll];
+  __shared__ int s_pre[2 * kCellBeads][32], s_base[2 * kCellBeads][32];
   for (int k = threadIdx.x; k < kFineAll; k += blockDim.x) fh[k] = 0u;
   __syncthreads();
-  const int q = blockIdx.x * kCellWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = blockIdx.x * kCellBeads + (w >> 1), ch = w & 1;
   if (q < m) {
-    const int4 ic = B.fpos[b_lo + q], it = B.ftrial[q];
+    const int tq = B.fpos[b_lo + q].w;
+    const int4 p = ch ? B.ftrial[q] : B.fpos[b_lo + q];
     const int cap = P.cell_cap, nx = P.cell_nc[0], ny = P.cell_nc[1], nz = P.cell_nc[2];
     const float cut2 = kDescCut * kDescCut;
-    for (int ch = 0; ch < 2; ch++) {
-      const int4 p = ch ? it : ic;
-      const int cx = cell_axis((unsigned)p.x, nx), cy = cell_axis((unsigned)p.y, ny),
-                cz = cell_axis((unsigned)p.z, nz);
-      for (int oz = -1; oz <= 1; oz++) {
-        const int z = cz + oz < 0 ? cz + oz + nz : (cz + oz >= nz ? cz + oz - nz : cz + oz);
-        for (int oy = -1; oy <= 1; oy++) {
-          const int y = cy + oy < 0 ? cy + oy + ny : (cy + oy >= ny ? cy + oy - ny : cy + oy);
-          for (int ox = -1; ox <= 1; ox++) {
-            const int x = cx + ox < 0 ? cx + ox + nx : (cx + ox >= nx ? cx + ox - nx : cx + ox);
-            const int base = (x + nx * (y + ny * z)) * cap;
-            const int n = min(B.cell_n[base / cap], cap);
-            for (int e = lane; e < n; e += 32) {
-              const int j = B.cell_beads[base + e];
-              if (B.cell_key[j] != base + e) continue;  // stale: moved to another cell
-              if (j >= b_lo && j < b_lo + m) continue;  // moved pairs below
-              const int4 jc = B.fpos[j];
-              const float r2 = desc_r2_fix(P, p, jc);
-              if (r2 < cut2)
-                atomicAdd(&fh[(2 * ch + (ic.w == jc.w ? 0 : 1)) * kFine + fine_bin(r2)], 1u);
-            }
-          }
-        }
+    unsigned* hist = fh + 2 * ch * kFine;
+    // lane l < 27: neighbour cell l (offsets -1..1 per axis) and its count
+    int cbase = 0, cn = 0;
+    if (lane < 27) {
+      const int ox = lane % 3 - 1, oy = (lane / 3) % 3 - 1, oz = lane / 9 - 1;
+      int x = cell_axis((unsigned)p.x, nx) + ox, y = cell_axis((unsigned)p.y, ny) + oy,
+          z = cell_axis((unsigned)p.z, nz) + oz;
+      x += x < 0 ? nx : (x >= nx ? -nx : 0);
+      y += y < 0 ? ny : (y >= ny ? -ny : 0);
+      z += z < 0 ? nz : (z >= nz ? -nz : 0);
+      const int c = x + nx * (y + ny * z);
+      cbase = c * cap;
+      cn = min(B.cell_n[c], cap);
+    }
+    auto visit = [&](int4 ent) {
+      if (ent.w < 0) return;  // dead: the bead moved to another cell
+      const int j = ent.w >> 3;
+      if (j >= b_lo && j < b_lo + m) return;  // moved pairs below
+      const float r2 = desc_r2_fix(P, p, ent);
+      if (r2 < cut2) atomicAdd(&hist[((ent.w & 7) == tq ? 0 : 1) * kFine + fine_bin(r2)], 1u);
+    };
+    // the 27 cells' entries as one list: lane e takes entries e, e + 32, ...,
+    // finding its cell by binary search in the inclusive prefix of the counts
+    int pre = cn;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, pre, o);
+      if (lane >= o) pre += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, pre, 26);
+    s_pre[w][lane] = pre;
+    s_base[w][lane] = cbase;
+    __syncwarp();
+#pragma unroll 4
+    for (int e = lane; e < total; e += 32) {
+      int lo = 0, hi = 26;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (s_pre[w][mid] > e) hi = mid; else lo = mid + 1;
       }
+      visit(B.cell_ent[s_base[w][lo] + e - (lo ? s_pre[w][lo - 1] : 0)]);
     }
     for (int q2 = q + 1 + lane; q2 < m; q2 += 32) {
-      const int4 c2 = B.fpos[b_lo + q2], t2 = B.ftrial[q2];
-      const int cls = ic.w == c2.w ? 0 : 1;
-      float r2 = desc_r2_fix(P, ic, c2);
-      if (r2 < cut2) atomicAdd(&fh[cls * kFine + fine_bin(r2)], 1u);
-      r2 = desc_r2_fix(P, it, t2);
-      if (r2 < cut2) atomicAdd(&fh[(2 + cls) * kFine + fine_bin(r2)], 1u);
+      const int4 o = ch ? B.ftrial[q2] : B.fpos[b_lo + q2];
+      const float r2 = desc_r2_fix(P, p, o);
+      if (r2 < cut2)
+        atomicAdd(&hist[(B.fpos[b_lo + q2].w == tq ? 0 : 1) * kFine + fine_bin(r2)], 1u);
     }
   }
   __syncthreads();
@@ -942,8 +962,8 @@ void launch_desc_batch(const DevParams* rp, const DevBuffers* rb, int n_rep, uns
                        int form, int cell_moved, cudaStream_t st) {
   (void)acc;
   if (cell_moved > 0)
-    k_desc_cells<<<dim3((std::min(cell_moved, kDescMaxMoved) + kCellWarps - 1) / kCellWarps,
-                        n_rep), kCellWarps * 32, 0, st>>>(rp, rb);
+    k_desc_cells<<<dim3((std::min(cell_moved, kDescMaxMoved) + kCellBeads - 1) / kCellBeads,
+                        n_rep), 2 * kCellBeads * 32, 0, st>>>(rp, rb);
   launch_desc_counts(rp, rb, n_rep, form, st);
   // programmatic dependent of k_desc (it waits for the counts itself)
   cudaLaunchConfig_t cfg = {};

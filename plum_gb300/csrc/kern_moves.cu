@@ -645,15 +645,21 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
         B.pos[i] = B.trial[i];
         if (P.form) B.fpos[i] = B.ftrial[i - b_lo];
         if (P.cell_cap && B.cell_key) {
-          // a bead that changes cell is appended to the new one; its old
-          // entry goes stale (cell_key no longer points at it)
-          const int c = cell_index(P, B.ftrial[i - b_lo]);
-          if (B.cell_key[i] / P.cell_cap != c) {
+          // the bead's entry follows it: rewritten in place within its cell,
+          // else marked dead and appended to the new cell
+          const int4 f = B.ftrial[i - b_lo];
+          const int4 ent = make_int4(f.x, f.y, f.z, (i << 3) | f.w);
+          const int c = cell_index(P, f), old = B.cell_key[i];
+          if (old >= 0 && old / P.cell_cap == c) {
+            B.cell_ent[old] = ent;
+          } else {
+            if (old >= 0) B.cell_ent[old] = make_int4(0, 0, 0, -1);
             const int k = atomicAdd(&B.cell_n[c], 1);
             if (k < P.cell_cap) {
-              B.cell_beads[c * P.cell_cap + k] = i;
+              B.cell_ent[c * P.cell_cap + k] = ent;
               B.cell_key[i] = c * P.cell_cap + k;
             } else {
+              B.cell_key[i] = -1;
               S.cell_ok = 0;  // every writer stores the same value
             }
           }
@@ -857,7 +863,7 @@ __global__ void k_gather_states(DevState* const* sts, int n_rep, long long* out)
     out[6 * r + 2] = st->error;
     out[6 * r + 3] = st->n_accept;
     out[6 * r + 4] = st->n_nonfinite;
-    out[6 * r + 5] = 0;
+    out[6 * r + 5] = st->cell_ok;
   }
 }
 

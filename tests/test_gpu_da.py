@@ -115,13 +115,17 @@ def test_gain_over_the_method_without_the_network(pg, trained):
     assert s["chain_acc"] > 0.5 * p["chain_acc"]
 
 
-@pytest.mark.parametrize("workload,replicas,blocks", [("bulk_1000", 8, 20), ("bulk_20000_pinned", 2, 8)])
-def test_cell_list_descriptors_equal_all_pairs(pg, tmp_path, workload, replicas, blocks):
-    """The descriptor cell lists (rebuilt per batch of steps, appended to on
+@pytest.mark.parametrize("workload,replicas,blocks,cap", [("bulk_1000", 8, 20, 0),
+                                                          ("bulk_1000", 4, 12, 6),
+                                                          ("bulk_20000_pinned", 2, 8, 0)])
+def test_cell_list_descriptors_equal_all_pairs(pg, tmp_path, workload, replicas, blocks, cap):
+    """The descriptor cell lists (rebuilt per batch of steps, entries moved on
     every accepted move) give the all-pairs kernel's integers: two batches
     from the same starts and seeds, one with and one without the lists,
     produce the same descriptors after every batch of steps and so the same
-    stage-one decisions and trajectories."""
+    stage-one decisions and trajectories. cap = 6 entries per cell makes
+    cells overflow: those replicas take the all-pairs kernel and the lists
+    grow until nothing overflows."""
     from plum_gb300 import surrogate as S
     from plum_gb300 import systems
     d = str(tmp_path / workload)
@@ -135,12 +139,18 @@ def test_cell_list_descriptors_equal_all_pairs(pg, tmp_path, workload, replicas,
         b.seed(np.arange(42, 42 + replicas, dtype=np.uint32))
         b.set_surrogate(sg)
         b.set_cells(on)
+        if cap:
+            b.set_cell_cap(cap)
         desc = []
         for _ in range(blocks):
             b.run(25)
             desc.append(b.descriptors())
         out.append((np.array(desc), [b.replica(r).positions() for r in range(replicas)],
                     b.da_stats()))
+        if on and cap:
+            # the lists grew past the cap
+            with_lists, valid, most, per_cell = b.cell_stats()
+            assert per_cell > cap and with_lists == replicas, (per_cell, with_lists)
         b.close()
     (da, pa, sa), (db, pb, sb) = out
     assert sa[0] > 0 and da.any()
