@@ -1503,6 +1503,7 @@ struct plum_batch {
   int* d_err = nullptr;
   // descriptor cell lists (replicas that can have one)
   int* d_cells = nullptr;
+  int* d_queue = nullptr;  // work queue of the batched energy change
   int cell_moved = 0;     // longest molecule among them (0: none)
   bool cells_on = true;
   bool cells_built = false;  // a batch of steps with the surrogate has rebuilt them
@@ -1605,7 +1606,7 @@ void batch_enqueue(plum_batch* b, int steps) {
   stage_one();
   for (int i = 0; i < steps; i++) {
     launch_batch_delta32(b->d_rp, b->d_rb, R, b->d_item_off, b->d_slots, b->kt_smem, b->tune,
-                           b->s);
+                         b->d_queue, b->s);
     int mode = kModeFinish | kModeDecide | (i + 1 < steps ? kModeGen : 0);
     launch_batch_serial(b->d_rp, b->d_rb, b->d_item_off, b->d_slots, R, mode, b->s);
     if (i + 1 < steps) stage_one();
@@ -1646,7 +1647,7 @@ int plum_batch_destroy(plum_batch* b) {
   cudaSetDevice(b->device);
   if (b->s) cudaStreamSynchronize(b->s);
   for (plum_ctx* c : b->reps) plum_ctx_destroy(c);
-  void* ptrs[] = {b->d_cells, b->d_rp,    b->d_rb,  b->d_item_off, b->d_slots, b->d_states, b->d_outs,
+  void* ptrs[] = {b->d_cells, b->d_queue, b->d_rp,    b->d_rb,  b->d_item_off, b->d_slots, b->d_states, b->d_outs,
                   b->d_sts,   b->d_pos, b->d_len,      b->d_cap,   b->d_gather, b->d_need,
                   b->d_desc,  b->d_err, b->d_fine};
   for (void* p : ptrs)
@@ -1738,11 +1739,13 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
   rc |= dalloc(&b->d_desc, (size_t)mlp::kIn * n);
   rc |= dalloc(&b->d_fine, (size_t)mlp::kFineAll * n);
   rc |= dalloc(&b->d_err, 1);
+  rc |= dalloc(&b->d_queue, 2);
   if (rc) {
     plum_batch_destroy(b);
     return PLUM_ERR_CUDA;
   }
   cudaMemset(b->d_err, 0, sizeof(int));
+  cudaMemset(b->d_queue, 0, 2 * sizeof(int));
   for (int r = 0; r < n; r++) {
     hb[r].desc_acc = b->d_desc + (size_t)mlp::kIn * r;
     hb[r].desc_fine = b->d_fine + (size_t)mlp::kFineAll * r;
@@ -1953,7 +1956,7 @@ int plum_batch_time_kernels(plum_batch* b, int n_steps, double* out4) {
   for (int i = 0; i < n_steps && !rc; i++) {
     rc = timed(0, [&] {
       launch_batch_delta32(b->d_rp, b->d_rb, R, b->d_item_off, b->d_slots, b->kt_smem, b->tune,
-                           b->s);
+                         b->d_queue, b->s);
     });
     const int mode = kModeFinish | kModeDecide | (i + 1 < n_steps ? kModeGen : 0);
     if (!rc)

@@ -255,8 +255,10 @@ __host__ __device__ inline int pair_item_count(int m, int n_bead, int item_pairs
   const int c = pair_chunk(m, item_pairs);
   return ((m + kPairGroup - 1) / kPairGroup) * ((n_bead + c - 1) / c) + (m > 1 ? 1 : 0);
 }
+// queue: two ints, zero before the first launch (each launch leaves them zero)
 void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, int* item_off,
-                          double* slots, size_t smem, BatchTune tune, cudaStream_t s);
+                          double* slots, size_t smem, BatchTune tune, int* queue,
+                          cudaStream_t s);
 void launch_batch_serial(const DevParams* rp, const DevBuffers* rb, const int* item_off,
                          const double* slots, int n_rep, int mode, cudaStream_t s);
 // per replica r: if need[r], shift the unread words [pos[r], len[r]) of out[r]

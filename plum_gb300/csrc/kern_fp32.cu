@@ -320,7 +320,7 @@ __device__ __forceinline__ void pair_sweep(const DevParams& P, const PairConst& 
 // the pairs among the moved beads,
 // and k items (one k tile of kKTile32 vectors over all moved beads). Every
 // block derives the same item list from the replicas' states, takes a
-// contiguous share of it, and writes one slot per item: pair items
+// share of it from a queue, and writes one slot per item: pair items
 // {lj, real}, k items {k-space energy change}. The serial step of each
 // replica adds its slots in item order.
 // The item sizes, the grid and the register budget (kMinBlocks resident
@@ -331,16 +331,13 @@ template <int kMinBlocks>
 __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
     k_batch_delta32(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb,
                     int n_rep, int* __restrict__ item_off, double* __restrict__ slots,
-                    BatchTune tune) {
+                    BatchTune tune, int* __restrict__ queue) {
   const int kItemPairs = tune.item_pairs, kKTile32 = tune.k_tile;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ float red[kPairThreads / 32];
   __shared__ int s_pref[kMaxReplicas + 1];
   __shared__ int s_np[kMaxReplicas];
-  __shared__ DevParams P;
-  __shared__ DevBuffers B;
-  __shared__ int s_bl[4];  // b_lo, b_hi, sk pending | sk_buf<<1 | cur_buf<<2, m
-  __shared__ int s_total;
+  __shared__ int s_total, s_item;
   // 1. item counts per replica and their prefix (same in every block)
   for (int r = threadIdx.x; r < n_rep; r += blockDim.x) {
     const DevState* st = rb[r].state;
@@ -366,11 +363,17 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
       item_off[4 * r + 2] = s_pref[r] + s_np[r];
       item_off[4 * r + 3] = s_pref[r + 1] - s_pref[r] - s_np[r];
     }
+  // 2. items are taken from a queue (queue[0]) one at a time: blocks that
+  // drew cheap items take more. Every item writes only its own slot, so
+  // the results do not depend on which block took it. The last block to
+  // run out resets the queue for the next launch.
   const int T = s_total;
-  const int it0 = (int)((long long)T * blockIdx.x / gridDim.x);
-  const int it1 = (int)((long long)T * (blockIdx.x + 1) / gridDim.x);
-  int cur = -1;
-  for (int item = it0; item < it1; item++) {
+  for (;;) {
+    __syncthreads();  // the previous item is done with s_item and the staging area
+    if (threadIdx.x == 0) s_item = atomicAdd(&queue[0], 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= T) break;
     // replica of this item (s_pref is ascending)
     int lo = 0, hi = n_rep - 1;
     while (lo < hi) {
@@ -378,26 +381,10 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
       if (s_pref[mid] <= item) lo = mid; else hi = mid - 1;
     }
     const int r = lo;
-    if (r != cur) {
-      __syncthreads();
-      const int* src = reinterpret_cast<const int*>(rp + r);
-      int* dst = reinterpret_cast<int*>(&P);
-      for (int i = threadIdx.x; i < (int)(sizeof(DevParams) / sizeof(int)); i += blockDim.x)
-        dst[i] = src[i];
-      const long long* bs = reinterpret_cast<const long long*>(rb + r);
-      long long* bd = reinterpret_cast<long long*>(&B);
-      for (int i = threadIdx.x; i < (int)(sizeof(DevBuffers) / sizeof(long long)); i += blockDim.x)
-        bd[i] = bs[i];
-      if (threadIdx.x == 0) {
-        const DevState* st = rb[r].state;
-        s_bl[0] = st->b_lo;
-        s_bl[1] = st->b_hi;
-        s_bl[2] = st->sk_pending | (st->sk_buf << 1) | (st->cur_buf << 2);
-      }
-      __syncthreads();
-      cur = r;
-    }
-    const int b_lo = s_bl[0], b_hi = s_bl[1], m = b_hi - b_lo, N = P.n_bead;
+    const DevParams& P = rp[r];
+    const DevBuffers& B = rb[r];
+    const DevState* st = B.state;
+    const int b_lo = st->b_lo, b_hi = st->b_hi, m = b_hi - b_lo, N = P.n_bead;
     const int local = item - s_pref[r];
     if (local < s_np[r]) {
       float acc_lj = 0.0f, acc_re = 0.0f;
@@ -442,8 +429,7 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
       }
     } else {
       const int tile = local - s_np[r];
-      const int flags = s_bl[2];
-      const int sk_pend = flags & 1, sk_buf = (flags >> 1) & 1, cur_buf = (flags >> 2) & 1;
+      const int sk_pend = st->sk_pending, sk_buf = st->sk_buf, cur_buf = st->cur_buf;
       const int k = tile * kKTile32 + threadIdx.x;
       const bool mine = threadIdx.x < kKTile32 && k < P.n_k;
       const short4 kv = mine ? B.kn[k] : make_short4(0, 0, 0, 0);
@@ -486,10 +472,17 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
       }
     }
   }
+  // every block takes its last (empty) item before it counts itself out, so
+  // the last one out knows that no block will read the queue again
+  if (threadIdx.x == 0 && atomicAdd(&queue[1], 1) == (int)gridDim.x - 1) {
+    queue[0] = 0;
+    queue[1] = 0;
+  }
 }
 
 void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, int* item_off,
-                          double* slots, size_t smem, BatchTune tune, cudaStream_t s) {
+                          double* slots, size_t smem, BatchTune tune, int* queue,
+                          cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_batch_delta32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -502,11 +495,11 @@ void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, 
   }
   const int grid = tune.grid > 0 ? tune.grid : pair_grid32();
   if (tune.min_blocks == 4)
-    k_batch_delta32<4><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune);
+    k_batch_delta32<4><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune, queue);
   else if (tune.min_blocks == 3)
-    k_batch_delta32<3><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune);
+    k_batch_delta32<3><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune, queue);
   else
-    k_batch_delta32<2><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune);
+    k_batch_delta32<2><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune, queue);
 }
 
 __global__ void k_fix_all(const DevParams P, const DevBuffers B) {
