@@ -348,6 +348,8 @@ def main():
     ap.add_argument("--ref-moves", type=int, default=10)
     ap.add_argument("--tune", default=None,
                     help="with --only batch: item_pairs,k_tile,grid,min_blocks instead of autotuning")
+    ap.add_argument("--groups", type=int, default=2, choices=[1, 2],
+                    help="step chains per batch (two: halves in two graph branches)")
     ap.add_argument("--tau-replicas", type=int, default=16,
                     help="replicas whose chains' Rg^2 series give tau_int")
     ap.add_argument("--replicas", type=int, default=64,
@@ -447,8 +449,10 @@ def main():
         sg_meta = {k: (z[k].item() if z[k].ndim == 0 else None) for k in z.files
                    if k not in ("params", "mu", "isd")}
         batch.set_surrogate(sg)
-    # work-item sizes of the batched energy change, timed on these replicas
+    # work-item sizes of the batched energy change, timed on these replicas;
+    # then the replicas' step chains in two graph branches (halves)
     tune = batch.autotune(16)
+    batch.set_groups(args.groups)
     for _ in range(args.warmup):
         batch.run(BS)
         s32.run(M)
@@ -490,7 +494,8 @@ def main():
               "weights": os.path.relpath(wpath, ROOT), "training": sg_meta}
         cs = batch.cell_stats()
         da["descriptor_cell_lists"] = {"replicas": cs[0], "valid_after_timed_steps": cs[1],
-                                       "most_entries_in_a_cell": cs[2], "entries_per_cell": cs[3]}
+                                       "most_beads_that_changed_cell": cs[2],
+                                       "capacity_for_them": cs[3]}
     # per-kernel CUDA-event durations over a few more steps (plain launches)
     kern_ms = batch.time_kernels(32)
 
@@ -500,6 +505,7 @@ def main():
                   device=local)
     nb.seed(1000 * rank + 77)
     tune_nb = nb.autotune(16)
+    nb.set_groups(args.groups)
     for _ in range(2):
         nb.run(BS)
     nb_ms = []
@@ -626,7 +632,8 @@ def main():
                            (", delayed acceptance with the learned surrogate" if sg else ""),
                    "l2": "flushed between steps (256 MB write)", "parallelism": "replicas",
                    "autotuned_items": {"pairs_per_item": tune[0], "k_per_tile": tune[1],
-                                       "grid": tune[2], "resident_blocks_per_sm": tune[3]}},
+                                       "grid": tune[2], "resident_blocks_per_sm": tune[3]},
+                   "step_chains": args.groups},
         "batched_fp32_no_surrogate": {"value": batched32, "unit": "moves/s",
                                       "ms_per_step": statistics.mean(nb_ms),
                                       "autotuned_items": tune_nb},

@@ -301,13 +301,19 @@ int plum_batch_autotune(plum_batch* batch, int steps, int* out4);
  * per axis). Off, every replica takes the all-pairs descriptor kernel; the
  * descriptors are the same integers either way. */
 int plum_batch_set_cells(plum_batch* batch, int on);
-/* Entries per cell of the descriptor cell lists (reallocates them). A cell
- * that overflows sends its replica to the all-pairs descriptor kernel until
- * the next batch of steps, and doubles the entries per cell. */
+/* Step chains per batch: 1 (default) or 2 -- the replicas split in halves
+ * whose chains run as two branches of the batch's graph on two streams, so
+ * one half's latency-bound kernels overlap the other half's energy change.
+ * Results are the same either way (each replica's arithmetic is unchanged). */
+int plum_batch_set_groups(plum_batch* batch, int groups);
+/* Capacity of the descriptor cell lists' list of beads that changed cell
+ * since the last rebuild (reallocates the lists). When it overflows, that
+ * replica takes the all-pairs descriptor kernel until the next batch of
+ * steps, and the capacity doubles. */
 int plum_batch_set_cell_cap(plum_batch* batch, int cap);
-/* out4 = {replicas with a descriptor cell list, of which valid (no cell
- * overflowed since the last rebuild), most entries in one cell (live and
- * stale), entries per cell}. For diagnostics. */
+/* out4 = {replicas with a descriptor cell list, of which valid (no overflow
+ * since the last rebuild), most beads in one replica's list of beads that
+ * changed cell, its capacity}. For diagnostics. */
 int plum_batch_cell_stats(plum_batch* batch, int* out4);
 /* The descriptors of the replicas' last surrogate moves, out[R * 96] (the
  * rows stay as they were for replicas whose last move was not one). */

@@ -124,6 +124,7 @@ def lib():
         L.plum_batch_descriptors.argtypes = [C.c_void_p, C.c_void_p]
         L.plum_batch_cell_stats.argtypes = [C.c_void_p, _ip]
         L.plum_batch_set_cell_cap.argtypes = [C.c_void_p, C.c_int]
+        L.plum_batch_set_groups.argtypes = [C.c_void_p, C.c_int]
         L.plum_batch_autotune.argtypes = [C.c_void_p, C.c_int, _ip]
         L.plum_batch_da_stats.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
         _lib = L
@@ -481,12 +482,16 @@ class Batch:
         all-pairs kernel; the same integers either way."""
         _check(lib().plum_batch_set_cells(self.h, 1 if on else 0))
 
+    def set_groups(self, groups):
+        """1 or 2 step chains (two graph branches on two streams)."""
+        _check(lib().plum_batch_set_groups(self.h, groups))
+
     def set_cell_cap(self, cap):
         _check(lib().plum_batch_set_cell_cap(self.h, cap))
 
     def cell_stats(self):
-        """(replicas with a cell list, of which valid, most entries in one
-        cell, entries per cell)."""
+        """(replicas with a cell list, of which valid, most beads in one
+        replica's list of beads that changed cell, its capacity)."""
         o = np.zeros(4, np.int32)
         _check(lib().plum_batch_cell_stats(self.h, o))
         return tuple(int(x) for x in o)

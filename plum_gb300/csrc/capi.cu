@@ -1503,7 +1503,11 @@ struct plum_batch {
   int* d_err = nullptr;
   // descriptor cell lists (replicas that can have one)
   int* d_cells = nullptr;
-  int* d_queue = nullptr;  // work queue of the batched energy change
+  int* d_queue = nullptr;  // work queues of the batched energy change [2 groups][2]
+  double* d_slots2 = nullptr;  // slots of the second group
+  int groups = 1;
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   int cell_moved = 0;     // longest molecule among them (0: none)
   bool cells_on = true;
   bool cells_built = false;  // a batch of steps with the surrogate has rebuilt them
@@ -1519,9 +1523,10 @@ namespace {
 // the generated chain moves and the surrogate's stage one, which marks the
 // moves it rejects so that the delta kernel skips them.
 // (Re)allocates the descriptor cell lists of the replicas that have one
-// (h_rp[r].cell_cap > 0): per replica cell_key [n_bead], cell_n [cells] and,
-// on a 16-byte boundary, cell_ent [cells * cell_cap]; then uploads the
-// parameter and buffer tables.
+// (h_rp[r].cell_cap > 0): per replica cell_key [n_bead], cell_n and
+// cell_start [cells + 1] (ints), then on a 16-byte boundary cell_ent
+// [n_bead] and cell_extra [cell_cap] (int4); then uploads the parameter and
+// buffer tables.
 int cells_alloc(plum_batch* b) {
   const int n = (int)b->reps.size();
   if (b->d_cells) {
@@ -1529,14 +1534,17 @@ int cells_alloc(plum_batch* b) {
     cudaFree(b->d_cells);
     b->d_cells = nullptr;
   }
+  auto head = [](const DevParams& P) {
+    const size_t cells = (size_t)P.cell_nc[0] * P.cell_nc[1] * P.cell_nc[2];
+    return ((size_t)P.n_bead + 2 * (cells + 1) + 3) / 4 * 4;
+  };
   size_t words = 0;
   std::vector<size_t> off(n, 0);
   for (int r = 0; r < n; r++) {
     const DevParams& P = b->h_rp[r];
     if (!P.cell_cap) continue;
-    const size_t cells = (size_t)P.cell_nc[0] * P.cell_nc[1] * P.cell_nc[2];
     off[r] = words;
-    words += ((size_t)P.n_bead + cells + 3) / 4 * 4 + 4 * cells * P.cell_cap;
+    words += head(P) + 4 * ((size_t)P.n_bead + P.cell_cap);
   }
   if (words && dalloc(&b->d_cells, words)) return PLUM_ERR_CUDA;
   for (int r = 0; r < n; r++) {
@@ -1546,7 +1554,9 @@ int cells_alloc(plum_batch* b) {
     const size_t cells = (size_t)P.cell_nc[0] * P.cell_nc[1] * P.cell_nc[2];
     B.cell_key = b->d_cells + off[r];
     B.cell_n = B.cell_key + P.n_bead;
-    B.cell_ent = reinterpret_cast<int4*>(B.cell_key + ((size_t)P.n_bead + cells + 3) / 4 * 4);
+    B.cell_start = B.cell_n + cells + 1;
+    B.cell_ent = reinterpret_cast<int4*>(B.cell_key + head(P));
+    B.cell_extra = B.cell_ent + P.n_bead;
   }
   if (b->d_rp) {
     CK(cudaMemcpyAsync(b->d_rp, b->h_rp.data(), sizeof(DevParams) * n, cudaMemcpyHostToDevice,
@@ -1570,7 +1580,8 @@ void cells_enqueue(plum_batch* b) {
 long batch_kernels(const plum_batch* b, int steps) {
   const bool cells = b->sg && b->cell_moved;
   const long stage = b->sg ? (cells && b->cells_on ? 3 : 2) + 1 : 0;
-  return (cells ? (b->cells_on ? 2 : 1) : 0) + 1 + 2L * steps + steps * stage;
+  const long chains = (b->groups > 1 && b->reps.size() > 1) ? 2 : 1;
+  return (cells ? (b->cells_on ? 2 : 1) : 0) + chains * (1 + 2L * steps + steps * stage);
 }
 
 // After a batch of steps: a replica whose cell list overflowed doubles every
@@ -1593,24 +1604,49 @@ int cells_check(plum_batch* b) {
   return cells_alloc(b);
 }
 
+// The step chain of replicas [r0, r0 + n) on stream st with its own slots
+// and work queue.
+void chain_enqueue(plum_batch* b, int steps, int r0, int n, double* slots, int* queue,
+                   cudaStream_t st) {
+  const DevParams* rp = b->d_rp + r0;
+  const DevBuffers* rb = b->d_rb + r0;
+  const int* item_off = b->d_item_off + 4 * r0;
+  int* item_off_w = b->d_item_off + 4 * r0;
+  auto stage_one = [&]() {
+    if (!b->sg) return;
+    launch_desc_batch(rp, rb, n, b->d_desc + (size_t)mlp::kIn * r0, 1,
+                      b->cells_on ? b->cell_moved : 0, st);
+    launch_mlp_infer_i(b->sg->net, b->d_desc + (size_t)mlp::kIn * r0, n, nullptr,
+                       DaArgs{b->d_sts + r0, b->d_rp + r0}, b->d_err, st);
+  };
+  launch_batch_serial(rp, rb, item_off, slots, n, kModeGen, st);
+  stage_one();
+  for (int i = 0; i < steps; i++) {
+    launch_batch_delta32(rp, rb, n, item_off_w, slots, b->kt_smem, b->tune, queue, st);
+    int mode = kModeFinish | kModeDecide | (i + 1 < steps ? kModeGen : 0);
+    launch_batch_serial(rp, rb, item_off, slots, n, mode, st);
+    if (i + 1 < steps) stage_one();
+  }
+}
+
+// One batch of steps. With two groups the replicas are split in halves whose
+// chains run on two streams (two branches of the graph): one half's
+// latency-bound kernels (serial step, descriptor, inference) overlap the
+// other half's energy change.
 void batch_enqueue(plum_batch* b, int steps) {
   const int R = (int)b->reps.size();
   cells_enqueue(b);
-  auto stage_one = [&]() {
-    if (!b->sg) return;
-    launch_desc_batch(b->d_rp, b->d_rb, R, b->d_desc, 1, b->cells_on ? b->cell_moved : 0, b->s);
-    launch_mlp_infer_i(b->sg->net, b->d_desc, R, nullptr, DaArgs{b->d_sts, b->d_rp}, b->d_err,
-                       b->s);
-  };
-  launch_batch_serial(b->d_rp, b->d_rb, b->d_item_off, b->d_slots, R, kModeGen, b->s);
-  stage_one();
-  for (int i = 0; i < steps; i++) {
-    launch_batch_delta32(b->d_rp, b->d_rb, R, b->d_item_off, b->d_slots, b->kt_smem, b->tune,
-                         b->d_queue, b->s);
-    int mode = kModeFinish | kModeDecide | (i + 1 < steps ? kModeGen : 0);
-    launch_batch_serial(b->d_rp, b->d_rb, b->d_item_off, b->d_slots, R, mode, b->s);
-    if (i + 1 < steps) stage_one();
+  if (b->groups < 2 || R < 2) {
+    chain_enqueue(b, steps, 0, R, b->d_slots, b->d_queue, b->s);
+    return;
   }
+  const int h = R / 2;
+  cudaEventRecord(b->fork_ev, b->s);
+  cudaStreamWaitEvent(b->s2, b->fork_ev, 0);
+  chain_enqueue(b, steps, 0, h, b->d_slots, b->d_queue, b->s);
+  chain_enqueue(b, steps, h, R - h, b->d_slots2, b->d_queue + 2, b->s2);
+  cudaEventRecord(b->join_ev, b->s2);
+  cudaStreamWaitEvent(b->s, b->join_ev, 0);
 }
 
 int batch_steps_graph(plum_batch* b, int steps) {
@@ -1647,7 +1683,7 @@ int plum_batch_destroy(plum_batch* b) {
   cudaSetDevice(b->device);
   if (b->s) cudaStreamSynchronize(b->s);
   for (plum_ctx* c : b->reps) plum_ctx_destroy(c);
-  void* ptrs[] = {b->d_cells, b->d_queue, b->d_rp,    b->d_rb,  b->d_item_off, b->d_slots, b->d_states, b->d_outs,
+  void* ptrs[] = {b->d_cells, b->d_queue, b->d_slots2, b->d_rp,    b->d_rb,  b->d_item_off, b->d_slots, b->d_states, b->d_outs,
                   b->d_sts,   b->d_pos, b->d_len,      b->d_cap,   b->d_gather, b->d_need,
                   b->d_desc,  b->d_err, b->d_fine};
   for (void* p : ptrs)
@@ -1656,6 +1692,9 @@ int plum_batch_destroy(plum_batch* b) {
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->fork_ev) cudaEventDestroy(b->fork_ev);
+  if (b->join_ev) cudaEventDestroy(b->join_ev);
+  if (b->s2) cudaStreamDestroy(b->s2);
   if (b->s) cudaStreamDestroy(b->s);
   delete b;
   return PLUM_OK;
@@ -1686,6 +1725,9 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
   }
   cudaSetDevice(device);
   cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking);
+  cudaStreamCreateWithFlags(&b->s2, cudaStreamNonBlocking);
+  cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
+  cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming);
   cudaEventCreate(&b->ev0);
   cudaEventCreate(&b->ev1);
   std::vector<DevParams> hp(n);
@@ -1739,21 +1781,23 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
   rc |= dalloc(&b->d_desc, (size_t)mlp::kIn * n);
   rc |= dalloc(&b->d_fine, (size_t)mlp::kFineAll * n);
   rc |= dalloc(&b->d_err, 1);
-  rc |= dalloc(&b->d_queue, 2);
+  rc |= dalloc(&b->d_queue, 4);
+  rc |= dalloc(&b->d_slots2, 2 * (size_t)items + 2);
   if (rc) {
     plum_batch_destroy(b);
     return PLUM_ERR_CUDA;
   }
   cudaMemset(b->d_err, 0, sizeof(int));
-  cudaMemset(b->d_queue, 0, 2 * sizeof(int));
+  cudaMemset(b->d_queue, 0, 4 * sizeof(int));
   for (int r = 0; r < n; r++) {
     hb[r].desc_acc = b->d_desc + (size_t)mlp::kIn * r;
     hb[r].desc_fine = b->d_fine + (size_t)mlp::kFineAll * r;
   }
   // descriptor cell lists: periodic on every axis with at least 3 cells of
-  // the descriptor's cut per axis; cell_cap = 8 x the mean occupancy + 64
-  // (at least 128), doubled whenever a cell overflowed during a batch of
-  // steps (the overflowing replica takes the all-pairs kernel until then)
+  // the descriptor's cut per axis; cell_cap (the list of beads that changed
+  // cell between rebuilds) = max(1024, n_bead / 16), doubled whenever it
+  // overflowed during a batch of steps (that replica takes the all-pairs
+  // kernel until the next rebuild)
   for (int r = 0; r < n; r++) {
     DevParams& P = hp[r];
     P.cell_cap = 0;
@@ -1767,9 +1811,8 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
       cells *= std::max(nc[a], 1);
     }
     if (!ok) continue;
-    const int mean = (P.n_bead + cells - 1) / cells;
     for (int a = 0; a < 3; a++) P.cell_nc[a] = nc[a];
-    P.cell_cap = std::max(128, 8 * mean + 64);
+    P.cell_cap = std::max(1024, P.n_bead / 16);  // beads that change cell per batch of steps
     b->cell_moved = std::max(b->cell_moved, std::min(b->reps[r]->max_len, 512));
     b->max_bead = std::max(b->max_bead, P.n_bead);
   }
@@ -2024,15 +2067,24 @@ int plum_batch_cell_stats(plum_batch* b, int* out4) {
     if (rc) return rc;
     ok += st.cell_ok ? 1 : 0;
     const int cells = hp[r].cell_nc[0] * hp[r].cell_nc[1] * hp[r].cell_nc[2];
-    std::vector<int> n(cells);
-    CK(cudaMemcpyAsync(n.data(), hb[r].cell_n, sizeof(int) * cells, cudaMemcpyDeviceToHost, b->s));
+    int used = 0;
+    CK(cudaMemcpyAsync(&used, hb[r].cell_n + cells, sizeof(int), cudaMemcpyDeviceToHost, b->s));
     CK(cudaStreamSynchronize(b->s));
-    for (int v : n) most = std::max(most, v);
+    most = std::max(most, used);
   }
   out4[0] = with;
   out4[1] = ok;
   out4[2] = most;
   out4[3] = cap;
+  return PLUM_OK;
+}
+
+int plum_batch_set_groups(plum_batch* b, int groups) {
+  if (!b || groups < 1 || groups > 2) return fail(PLUM_ERR_INPUT, "groups must be 1 or 2");
+  b->groups = groups;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->g_steps = 0;
   return PLUM_OK;
 }
 

@@ -80,7 +80,8 @@ struct DevParams {
   double inv_fix[3];     // 2^32 / Ewald box length (FP64 -> fixed point)
   // cell list of the surrogate descriptor (replica batches, precision form,
   // periodic on every axis): cell_nc cells per axis, each at least the
-  // descriptor's cut wide; cell_cap entries per cell (0: no cell list)
+  // descriptor's cut wide; cell_cap entries in the list of beads that left
+  // their cell since the last rebuild (0: no cell list)
   int cell_nc[3], cell_cap;
 };
 
@@ -156,15 +157,19 @@ struct DevBuffers {  // all pointers: copied word-wise into shared memory by the
   unsigned* desc_fine;  // [4][241] pair counts per 1/32-sigma distance bin
   float* log_desc;   // [log_cap][96]
   double* log_de;    // [log_cap]
-  // descriptor cell list (null when the replica has none): cell_ent
-  // [cells][cell_cap] holds entries (X, Y, Z, bead << 3 | type) appended per
-  // cell, cell_n the entries used, cell_key the entry of each bead. An
-  // accepted bead rewrites its entry in place, or, when it changes cell,
-  // marks the old entry dead (w = -1) and appends a new one; each rebuild
-  // compacts.
+  // descriptor cell list (null when the replica has none), rebuilt by a
+  // counting sort: cell_ent [n_bead] holds (X, Y, Z, bead << 3 | type) sorted
+  // by cell, cell c's entries at [cell_start[c], cell_start[c + 1]). An
+  // accepted bead rewrites its entry in place while it stays in its cell;
+  // when it leaves, the entry goes dead (w = -1) and the bead moves to
+  // cell_extra [cell_cap] (cell-less, counted in cell_n[cells]), where it
+  // stays until the next rebuild. cell_key: the bead's entry, k >= 0 in
+  // cell_ent or -2 - e in cell_extra.
   int* cell_key;     // [n_bead]
-  int* cell_n;       // [cells]
-  int4* cell_ent;    // [cells * cell_cap]
+  int* cell_n;       // [cells + 1] counts / cursors of the sort; [cells]: extra used
+  int* cell_start;   // [cells + 1]
+  int4* cell_ent;    // [n_bead]
+  int4* cell_extra;  // [cell_cap]
 };
 
 // Launch helpers (kern_energy.cu / kern_moves.cu). All enqueue on `s`.

@@ -732,33 +732,84 @@ __global__ void __launch_bounds__(kDescThreads)
 // Replicas with a cell list (precision form, periodic on every axis, cells at
 // least the cut wide) take the descriptor from k_desc_cells: the pairs
 // within the cut of a moved bead lie in the 27 cells around it, about
-// 27 x N / cells candidates instead of N. The list is rebuilt (compacted) at
-// the start of every batch of steps and kept up to date by the serial step,
-// which appends each accepted bead that changed cell (kern_moves.cu).
+// 27 x N / cells candidates instead of N. The list is rebuilt at the start of
+// every batch of steps by a counting sort (reset, count, scan, scatter) and
+// kept up to date by the serial step (kern_moves.cu): beads that leave their
+// cell go to a short cell-less list that every descriptor scans in full.
 __global__ void k_cell_reset(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb) {
   const DevParams& P = rp[blockIdx.x];
   const DevBuffers& B = rb[blockIdx.x];
   if (!P.cell_cap || !B.cell_key) return;
   const int cells = P.cell_nc[0] * P.cell_nc[1] * P.cell_nc[2];
-  for (int c = threadIdx.x; c < cells; c += blockDim.x) B.cell_n[c] = 0;
+  for (int c = threadIdx.x; c <= cells; c += blockDim.x) B.cell_n[c] = 0;
   if (threadIdx.x == 0) B.state->cell_ok = 1;
 }
 
-__global__ void k_cell_fill(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb) {
+__global__ void k_cell_count(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb) {
+  const DevParams& P = rp[blockIdx.y];
+  const DevBuffers& B = rb[blockIdx.y];
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (!P.cell_cap || !B.cell_key || j >= P.n_bead) return;
+  atomicAdd(&B.cell_n[cell_index(P, B.fpos[j])], 1);
+}
+
+// One block per replica: cell_start = exclusive prefix of the counts, and
+// the counts become the scatter cursors (cell_n[c] = cell_start[c]).
+__global__ void __launch_bounds__(1024)
+    k_cell_scan(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb) {
+  const DevParams& P = rp[blockIdx.x];
+  const DevBuffers& B = rb[blockIdx.x];
+  if (!P.cell_cap || !B.cell_key) return;
+  const int cells = P.cell_nc[0] * P.cell_nc[1] * P.cell_nc[2];
+  __shared__ int warp_sum[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int base = 0; base < cells; base += blockDim.x) {
+    const int c = base + threadIdx.x;
+    const int v = c < cells ? B.cell_n[c] : 0;
+    int x = v;  // inclusive scan within the warp
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += t;
+    }
+    if (lane == 31) warp_sum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      int y = lane < (int)(blockDim.x >> 5) ? warp_sum[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, y, o);
+        if (lane >= o) y += t;
+      }
+      warp_sum[lane] = y;  // inclusive prefix of the warp totals
+    }
+    __syncthreads();
+    const int ex = carry + (w ? warp_sum[w - 1] : 0) + x - v;
+    if (c < cells) {
+      B.cell_start[c] = ex;
+      B.cell_n[c] = ex;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carry += warp_sum[(blockDim.x >> 5) - 1];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    B.cell_start[cells] = carry;
+    B.cell_n[cells] = 0;  // extra list empty
+  }
+}
+
+__global__ void k_cell_scatter(const DevParams* __restrict__ rp,
+                               const DevBuffers* __restrict__ rb) {
   const DevParams& P = rp[blockIdx.y];
   const DevBuffers& B = rb[blockIdx.y];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (!P.cell_cap || !B.cell_key || j >= P.n_bead) return;
   const int4 f = B.fpos[j];
-  const int c = cell_index(P, f);
-  const int k = atomicAdd(&B.cell_n[c], 1);
-  if (k < P.cell_cap) {
-    B.cell_ent[c * P.cell_cap + k] = make_int4(f.x, f.y, f.z, (j << 3) | f.w);
-    B.cell_key[j] = c * P.cell_cap + k;
-  } else {
-    B.cell_key[j] = -1;
-    B.state->cell_ok = 0;
-  }
+  const int k = atomicAdd(&B.cell_n[cell_index(P, f)], 1);
+  B.cell_ent[k] = make_int4(f.x, f.y, f.z, (j << 3) | f.w);
+  B.cell_key[j] = k;
 }
 
 constexpr int kCellBeads = 4;  // moved beads per block: a warp per (bead, before / after)
@@ -766,10 +817,11 @@ constexpr int kCellBeads = 4;  // moved beads per block: a warp per (bead, befor
 // Block (x, r): moved beads [4x, 4x + 4) of replica r's pending surrogate
 // move. Warp (bead, channel pair): before the move (channels 0, 1) the
 // entries of the 27 cells around the bead's current position, after it
-// (channels 2, 3) around its trial position, skipping the moved beads (their
-// pairs, each once, at the end). Entries carry the positions, so a candidate
-// costs one load, and the 27 cells' entries form one list spread over the
-// lanes (independent loads). The same pairs, distances and bins as k_desc.
+// (channels 2, 3) around its trial position, then the cell-less list of
+// beads that changed cell, skipping the moved beads (their pairs, each
+// once, at the end). Entries carry the positions, so a candidate costs one
+// load, and the 27 cells' entries form one list spread over the lanes. The
+// same pairs, distances and bins as k_desc.
 __global__ void __launch_bounds__(2 * kCellBeads * 32)
     k_desc_cells(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb) {
   const DevParams& P = rp[blockIdx.y];
@@ -788,10 +840,11 @@ __global__ void __launch_bounds__(2 * kCellBeads * 32)
   if (q < m) {
     const int tq = B.fpos[b_lo + q].w;
     const int4 p = ch ? B.ftrial[q] : B.fpos[b_lo + q];
-    const int cap = P.cell_cap, nx = P.cell_nc[0], ny = P.cell_nc[1], nz = P.cell_nc[2];
+    const int nx = P.cell_nc[0], ny = P.cell_nc[1], nz = P.cell_nc[2];
     const float cut2 = kDescCut * kDescCut;
     unsigned* hist = fh + 2 * ch * kFine;
-    // lane l < 27: neighbour cell l (offsets -1..1 per axis) and its count
+    // lane l < 27: neighbour cell l (offsets -1..1 per axis): its first
+    // entry and count
     int cbase = 0, cn = 0;
     if (lane < 27) {
       const int ox = lane % 3 - 1, oy = (lane / 3) % 3 - 1, oz = lane / 9 - 1;
@@ -801,11 +854,11 @@ __global__ void __launch_bounds__(2 * kCellBeads * 32)
       y += y < 0 ? ny : (y >= ny ? -ny : 0);
       z += z < 0 ? nz : (z >= nz ? -nz : 0);
       const int c = x + nx * (y + ny * z);
-      cbase = c * cap;
-      cn = min(B.cell_n[c], cap);
+      cbase = B.cell_start[c];
+      cn = B.cell_start[c + 1] - cbase;
     }
     auto visit = [&](int4 ent) {
-      if (ent.w < 0) return;  // dead: the bead moved to another cell
+      if (ent.w < 0) return;  // dead: the bead left this cell
       const int j = ent.w >> 3;
       if (j >= b_lo && j < b_lo + m) return;  // moved pairs below
       const float r2 = desc_r2_fix(P, p, ent);
@@ -831,6 +884,8 @@ __global__ void __launch_bounds__(2 * kCellBeads * 32)
       }
       visit(B.cell_ent[s_base[w][lo] + e - (lo ? s_pre[w][lo - 1] : 0)]);
     }
+    const int n_extra = min(B.cell_n[nx * ny * nz], P.cell_cap);
+    for (int e = lane; e < n_extra; e += 32) visit(B.cell_extra[e]);
     for (int q2 = q + 1 + lane; q2 < m; q2 += 32) {
       const int4 o = ch ? B.ftrial[q2] : B.fpos[b_lo + q2];
       const float r2 = desc_r2_fix(P, p, o);
@@ -955,7 +1010,9 @@ void launch_cell_rebuild(const DevParams* rp, const DevBuffers* rb, int n_rep, i
     return;
   }
   k_cell_reset<<<n_rep, 256, 0, st>>>(rp, rb);
-  k_cell_fill<<<dim3((max_bead + 255) / 256, n_rep), 256, 0, st>>>(rp, rb);
+  k_cell_count<<<dim3((max_bead + 255) / 256, n_rep), 256, 0, st>>>(rp, rb);
+  k_cell_scan<<<n_rep, 1024, 0, st>>>(rp, rb);
+  k_cell_scatter<<<dim3((max_bead + 255) / 256, n_rep), 256, 0, st>>>(rp, rb);
 }
 
 void launch_desc_batch(const DevParams* rp, const DevBuffers* rb, int n_rep, unsigned* acc,

@@ -642,22 +642,27 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
     const int acc = s_accept;
     if (acc) {
       for (int i = b_lo + threadIdx.x; i < b_hi; i += blockDim.x) {
+        const int4 old_f = P.form ? B.fpos[i] : make_int4(0, 0, 0, 0);
         B.pos[i] = B.trial[i];
         if (P.form) B.fpos[i] = B.ftrial[i - b_lo];
         if (P.cell_cap && B.cell_key) {
-          // the bead's entry follows it: rewritten in place within its cell,
-          // else marked dead and appended to the new cell
+          // the bead's entry follows it: rewritten in place while it stays in
+          // its cell (or already is in the extra list), else marked dead and
+          // the bead appended to the extra list
           const int4 f = B.ftrial[i - b_lo];
           const int4 ent = make_int4(f.x, f.y, f.z, (i << 3) | f.w);
-          const int c = cell_index(P, f), old = B.cell_key[i];
-          if (old >= 0 && old / P.cell_cap == c) {
-            B.cell_ent[old] = ent;
+          const int key = B.cell_key[i];
+          if (key >= 0 && cell_index(P, old_f) == cell_index(P, f)) {
+            B.cell_ent[key] = ent;
+          } else if (key <= -2) {
+            B.cell_extra[-2 - key] = ent;
           } else {
-            if (old >= 0) B.cell_ent[old] = make_int4(0, 0, 0, -1);
-            const int k = atomicAdd(&B.cell_n[c], 1);
-            if (k < P.cell_cap) {
-              B.cell_ent[c * P.cell_cap + k] = ent;
-              B.cell_key[i] = c * P.cell_cap + k;
+            if (key >= 0) B.cell_ent[key] = make_int4(0, 0, 0, -1);
+            const int nc = P.cell_nc[0] * P.cell_nc[1] * P.cell_nc[2];
+            const int e = atomicAdd(&B.cell_n[nc], 1);
+            if (e < P.cell_cap) {
+              B.cell_extra[e] = ent;
+              B.cell_key[i] = -2 - e;
             } else {
               B.cell_key[i] = -1;
               S.cell_ok = 0;  // every writer stores the same value

@@ -76,3 +76,20 @@ def test_autotune_picks_a_candidate_and_keeps_running(pg):
     ip, kt, grid, mb = b.autotune(4)
     assert ip in (2048, 4096, 8192, 16384) and kt in (128, 256) and grid > 0 and mb in (2, 3, 4)
     assert b.run(100) > 0
+
+
+def test_two_step_chains_give_the_same_trajectories(pg):
+    """Replicas split in two graph branches (plum_batch_set_groups) do the
+    same arithmetic: bit-identical positions and energies."""
+    d, _ = load("bulk_medium")
+    out = []
+    for g in (1, 2):
+        b = pg.Batch([d] * 6)
+        b.seed(np.arange(30, 36, dtype=np.uint32))
+        b.set_groups(g)
+        b.run(300)
+        out.append([(b.replica(r).positions(), b.replica(r).energies()) for r in range(6)])
+        b.close()
+    for (pa, ea), (pb, eb) in zip(*out):
+        np.testing.assert_array_equal(pa, pb)
+        np.testing.assert_array_equal(ea, eb)

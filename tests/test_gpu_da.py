@@ -123,9 +123,9 @@ def test_cell_list_descriptors_equal_all_pairs(pg, tmp_path, workload, replicas,
     every accepted move) give the all-pairs kernel's integers: two batches
     from the same starts and seeds, one with and one without the lists,
     produce the same descriptors after every batch of steps and so the same
-    stage-one decisions and trajectories. cap = 6 entries per cell makes
-    cells overflow: those replicas take the all-pairs kernel and the lists
-    grow until nothing overflows."""
+    stage-one decisions and trajectories. cap = 6 makes the list of beads
+    that changed cell overflow: those replicas take the all-pairs kernel and
+    the list grows until nothing overflows."""
     from plum_gb300 import surrogate as S
     from plum_gb300 import systems
     d = str(tmp_path / workload)
