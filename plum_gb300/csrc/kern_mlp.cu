@@ -1021,7 +1021,13 @@ void launch_desc_batch(const DevParams* rp, const DevBuffers* rb, int n_rep, uns
   if (cell_moved > 0)
     k_desc_cells<<<dim3((std::min(cell_moved, kDescMaxMoved) + kCellBeads - 1) / kCellBeads,
                         n_rep), 2 * kCellBeads * 32, 0, st>>>(rp, rb);
-  launch_desc_counts(rp, rb, n_rep, form, st);
+  if (cell_moved > 0 && form) {
+    // the all-pairs kernel only takes replicas whose cell list overflowed:
+    // usually none, so a small grid (it still has to look at every replica)
+    k_desc<1><<<152, kDescThreads, 0, st>>>(rp, rb, n_rep);
+  } else {
+    launch_desc_counts(rp, rb, n_rep, form, st);
+  }
   // programmatic dependent of k_desc (it waits for the counts itself)
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(n_rep);
