@@ -1581,7 +1581,7 @@ long batch_kernels(const plum_batch* b, int steps) {
   const bool cells = b->sg && b->cell_moved;
   const long stage = b->sg ? (cells && b->cells_on ? 3 : 2) + 1 : 0;
   const long chains = (b->groups > 1 && b->reps.size() > 1) ? 2 : 1;
-  return (cells ? (b->cells_on ? 2 : 1) : 0) + chains * (1 + 2L * steps + steps * stage);
+  return (cells ? (b->cells_on ? 4 : 1) : 0) + chains * (1 + 2L * steps + steps * stage);
 }
 
 // After a batch of steps: a replica whose cell list overflowed doubles every

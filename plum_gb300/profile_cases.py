@@ -6,12 +6,17 @@
         with delayed acceptance; the third batch of 32 steps runs inside the
         NVTX range "da" (descriptor, smearing and tcgen05 inference launches),
         then the same without the surrogate inside "plain".
+    python -m plum_gb300.profile_cases chosen [replicas]
+        the measured form of the 20,000-particle workload: replicas
+        (default 64) with the shipped surrogate weights (dead zone 12 k_BT),
+        autotuned work items, two step chains; after 256 warm-up steps one
+        batch of 32 steps runs inside the NVTX range "chosen".
     python -m plum_gb300.profile_cases train
         one epoch of surrogate training on 65,536 random descriptors in
         batches of 4,096 inside the NVTX range "train" (k_mlp<true>, the
         gradient reduction and Adam), then one inference pass inside "infer".
 
-Both keep the device footprint under 1 GB so a full-set capture of one to
+All keep the device footprint under 1 GB so a full-set capture of one to
 three launches ends within a minute or two.
 """
 from __future__ import annotations
@@ -53,6 +58,28 @@ def delayed_acceptance(name="bulk_20000_pinned", replicas=16):
     b.close()
 
 
+def chosen(replicas=64):
+    import torch
+    import plum_gb300 as pg
+    from . import surrogate as S
+    here = os.path.dirname(os.path.abspath(__file__))
+    sg = S.load(os.path.join(here, "data", "surrogate_bulk_20000_pinned.npz"))
+    sg.set_margin(12.0)
+    b = pg.Batch([_workload("bulk_20000_pinned", 20261203 + r) for r in range(replicas)])
+    b.seed(77)
+    b.set_surrogate(sg)
+    tune = b.autotune(16)
+    b.set_groups(2)
+    b.run(256)
+    torch.cuda.nvtx.range_push("chosen")
+    b.run(32)
+    torch.cuda.nvtx.range_pop()
+    ms, k = b.last_timing()
+    print("chosen", replicas, "replicas, tune", tune, "ms per 32 steps", ms, "kernels", k,
+          flush=True)
+    b.close()
+
+
 def training(n=65536, batch=4096):
     import torch
     import plum_gb300 as pg
@@ -79,10 +106,13 @@ def main(argv=None):
     if what == "da":
         delayed_acceptance(argv[1] if len(argv) > 1 else "bulk_20000_pinned",
                            int(argv[2]) if len(argv) > 2 else 16)
+    elif what == "chosen":
+        chosen(int(argv[1]) if len(argv) > 1 else 64)
     elif what == "train":
         training()
     else:
-        raise SystemExit("usage: python -m plum_gb300.profile_cases {da [workload] [replicas] | train}")
+        raise SystemExit("usage: python -m plum_gb300.profile_cases "
+                         "{da [workload] [replicas] | chosen [replicas] | train}")
 
 
 if __name__ == "__main__":
