@@ -20,6 +20,7 @@
 // exchange growth step's trial energies in one device call.
 #pragma once
 
+#include <fstream>
 #include <istream>
 #include <random>
 #include <stdexcept>
@@ -156,6 +157,7 @@ class Simulation {  // simulation.h:20-201 (step loop and observables)
   // `plum < run.in`); crd/top paths are relative to dir.
   Simulation(std::istream& runin, const std::string& dir = ".", unsigned seed = 5489u,
              int form = PLUM_FORM_FP64, int device = 0);
+  ~Simulation() { Finish(); }  // the reference's destructor writes (simulation.cc:202-211)
   void Run();                 // steps from run.in, on the device
   void RunSteps(long n);      // n steps on the device
   void TranslationalMove();   // one step, host control flow (simulation.cc:241-355)
@@ -164,11 +166,30 @@ class Simulation {  // simulation.h:20-201 (step loop and observables)
   // then GCMove or TranslationalMove; last_move_type 5 / 6 for an insertion
   // / deletion attempt, last_accept when the molecule count changed.
   void Step();
-  void Sample();              // simulation.cc:723-798 (energies, Rg; no pressure)
+  // simulation.cc:723-798: energies, density, rho(z), Rg (x, y, z rounded to
+  // six significant digits as the reference's string round trip does), end
+  // to end distance; no pressure and no chemical potential
+  void Sample();
   double RadiusOfGyration();  // simulation.cc:406-434
   double EndToEndDistance();  // simulation.cc:483-501
   void UpdateMolCounts();     // simulation.cc:1066-1094
   void SyncFromDevice();      // refresh host bead positions after device steps
+
+  // The reference's output files (simulation.cc:120-131), written into dir:
+  // <run_name>_stat.dat (its header now), _traj_p/_c/_a/_n.xyz,
+  // _lastcrd.dat and .dat2, _lasttop.dat, _lastrhoZ.dat and .dat2, at the
+  // steps where the reference writes them. Off until this is called. Throws
+  // InputError for a run.in that asks for the chemical potential.
+  void EnableOutput(const std::string& dir = ".");
+  void PrintStatHeader();  // simulation.cc:685-721
+  void PrintStat();        // simulation.cc:800-867
+  void PrintTraj();        // simulation.cc:869-933
+  void PrintLastCrd();     // simulation.cc:935-979
+  void PrintLastTop();     // simulation.cc:981-1027
+  void PrintLastRhoZ();    // simulation.cc:1047-1064
+  // The writes of the reference's destructor (simulation.cc:202-211), which
+  // see step = steps + 1; closes the files.
+  void Finish();
 
   std::vector<Molecule> mols;
   ForceField force_field;
@@ -176,6 +197,8 @@ class Simulation {  // simulation.h:20-201 (step loop and observables)
   long step = 0;
   int accepted[5] = {0, 0, 0, 0, 0}, attempted[5] = {0, 0, 0, 0, 0};
   double pair_e_cumu = 0, ewald_e_cumu = 0, bond_e_cumu = 0, ext_e_cumu = 0, rg_tot_cumu = 0;
+  double rg_x_cumu = 0, rg_y_cumu = 0, rg_z_cumu = 0, e_to_e_cumu = 0, density_cumu = 0;
+  std::vector<double> density_z_cumu;  // [3 * bins] as CalcRhoZ accumulates it
   long ff_avg_counter = 0, mol_avg_counter = 0;
   int last_move_type = -1, last_accept = 0;
   long insertion_attempted = 0, insertion_accepted = 0;
@@ -185,7 +208,12 @@ class Simulation {  // simulation.h:20-201 (step loop and observables)
   plum_run_info run_{};
   double box_l[3];
   int npbc = 3;
-  int n_mol = 0, n_chain = 0, n_cion = 0, n_aion = 0, n_nion = 0;
+  int n_mol = 0, n_chain = 0, n_chain_b = 0, n_cion = 0, n_aion = 0, n_nion = 0;
+  int n_bead_ = 0;  // phantom + beads of the other molecules (UpdateMolCounts)
+  bool out_on_ = false;
+  std::string out_dir_, run_name_;
+  std::ofstream info_out, traj_p_out, traj_c_out, traj_a_out, traj_n_out;
+  std::ofstream crd_last_out[2], top_last_out, rho_last_out[2];
 };
 
 }  // namespace plum

@@ -44,6 +44,14 @@ int plum_sim_steps(plum_sim* sim, int n, int* move_type, int* accept);
 int plum_sim_n_bead(plum_sim* sim);
 int plum_sim_positions(plum_sim* sim, double* xyz);
 int plum_sim_energies(plum_sim* sim, double* out);
+/* Simulation::EnableOutput: the reference's output files go into dir
+ * (simulation.cc:120-131); then plum_sim_run runs the steps of run.in
+ * (Simulation::Run, sampling and writing where the reference does) and
+ * plum_sim_finish makes the writes of the reference's destructor and closes
+ * the files. */
+int plum_sim_enable_output(plum_sim* sim, const char* dir);
+int plum_sim_run(plum_sim* sim);
+int plum_sim_finish(plum_sim* sim);
 
 #ifdef __cplusplus
 }

@@ -76,6 +76,7 @@ def _load_ref():
                                       C.c_void_p, C.c_int]
         L.pr_beads_energy.restype = C.c_double
         L.pr_gc_info.argtypes = [C.c_void_p, _dp]
+        L.pr_run_full.argtypes = [C.c_void_p]
         _ref_lib = L
     return _ref_lib
 
@@ -179,6 +180,12 @@ class Ref(_Base):
 
     def run(self, n):
         return self._steps(self.L.pr_run, n)
+
+    def run_full(self):
+        """The reference's Simulation::Run with its sampling and output
+        files (into the case directory); close() runs its destructor, which
+        makes the last writes."""
+        self.L.pr_run_full(self.h)
 
     def observables(self):
         o = np.zeros(5)

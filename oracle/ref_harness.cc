@@ -252,6 +252,15 @@ void pr_delta_energy(void* hp, int mol, const double* trial, const int* moved,
   }
 }
 
+// The reference's own Simulation::Run (simulation.cc:216-239): every step
+// with its sampling and output files (written into the handle's directory).
+void pr_run_full(void* hp) {
+  Handle* h = (Handle*)hp;
+  CwdGuard cg(h->dir);
+  StreamSwap sw(std::cin.rdbuf(), h->log.rdbuf());
+  h->sim->Run();
+}
+
 // Runs `n` steps of the reference's Run loop body (simulation.cc:220-229)
 // without the sampling/printing calls. Per step records the move type
 // (0..4 translational, 5 insertion attempt, 6 deletion attempt), whether it

@@ -101,6 +101,9 @@ def lib():
         L.plum_erase_molecules.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.plum_sim_positions.argtypes = [C.c_void_p, _dp]
         L.plum_sim_energies.argtypes = [C.c_void_p, _dp]
+        L.plum_sim_enable_output.argtypes = [C.c_void_p, C.c_char_p]
+        L.plum_sim_run.argtypes = [C.c_void_p]
+        L.plum_sim_finish.argtypes = [C.c_void_p]
         _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
         L.plum_surrogate_create.argtypes = [C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]
         L.plum_surrogate_destroy.argtypes = [C.c_void_p]
@@ -572,3 +575,17 @@ class HostSimulation:
         o = np.zeros(4)
         _check(lib().plum_sim_energies(self.h, o))
         return o
+
+    def enable_output(self, dirpath="."):
+        """The reference's output files (stat, trajectories, last
+        coordinates / topology / rho(z)) into dirpath."""
+        _check(lib().plum_sim_enable_output(self.h, str(dirpath).encode()))
+
+    def run(self):
+        """The steps of run.in (Simulation::Run): samples and writes where
+        the reference does."""
+        _check(lib().plum_sim_run(self.h))
+
+    def finish(self):
+        """The writes of the reference's destructor; closes the files."""
+        _check(lib().plum_sim_finish(self.h))

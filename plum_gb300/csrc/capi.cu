@@ -1610,8 +1610,7 @@ void chain_enqueue(plum_batch* b, int steps, int r0, int n, double* slots, int* 
                    cudaStream_t st) {
   const DevParams* rp = b->d_rp + r0;
   const DevBuffers* rb = b->d_rb + r0;
-  const int* item_off = b->d_item_off + 4 * r0;
-  int* item_off_w = b->d_item_off + 4 * r0;
+  int* item_off = b->d_item_off + 4 * r0;
   auto stage_one = [&]() {
     if (!b->sg) return;
     launch_desc_batch(rp, rb, n, b->d_desc + (size_t)mlp::kIn * r0, 1,
@@ -1622,7 +1621,7 @@ void chain_enqueue(plum_batch* b, int steps, int r0, int n, double* slots, int* 
   launch_batch_serial(rp, rb, item_off, slots, n, kModeGen, st);
   stage_one();
   for (int i = 0; i < steps; i++) {
-    launch_batch_delta32(rp, rb, n, item_off_w, slots, b->kt_smem, b->tune, queue, st);
+    launch_batch_delta32(rp, rb, n, item_off, slots, b->kt_smem, b->tune, queue, st);
     int mode = kModeFinish | kModeDecide | (i + 1 < steps ? kModeGen : 0);
     launch_batch_serial(rp, rb, item_off, slots, n, mode, st);
     if (i + 1 < steps) stage_one();

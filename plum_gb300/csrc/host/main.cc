@@ -2,8 +2,9 @@
 //     plum_gpu [seed] [fp32] < run.in
 // Reads run.in from stdin (coordinate/topology files relative to the working
 // directory), runs the steps of run.in on the GPU through the reference-named
-// host classes, and prints the averaged energies, the mean Rg^2 and the
-// acceptance ratio. The reference seeds from the clock (simulation.cc:133-136);
+// host classes, writes the reference's output files (stat, trajectories,
+// last coordinates, topology and rho(z)) into the working directory, and
+// prints the averaged energies, the mean Rg^2 and the acceptance ratio. The reference seeds from the clock (simulation.cc:133-136);
 // this driver takes the seed as its first argument (default 5489).
 #include <cstdio>
 #include <cstdlib>
@@ -17,7 +18,9 @@ int main(int argc, char** argv) {
   int form = (argc > 2 && !std::strcmp(argv[2], "fp32")) ? PLUM_FORM_FP32 : PLUM_FORM_FP64;
   try {
     plum::Simulation sim(std::cin, ".", seed, form);
+    sim.EnableOutput(".");  // the reference's files in the working directory
     sim.Run();
+    sim.Finish();
     const double n = sim.ff_avg_counter > 0 ? (double)sim.ff_avg_counter : 1.0;
     std::printf("steps %ld\n", sim.step);
     std::printf("<PairEne> %.10g <EwaldEne> %.10g <BondEne> %.10g <ExtPotEne> %.10g\n",

@@ -1,0 +1,241 @@
+// The reference's output files, written by the host Simulation from the
+// device state at the steps where the reference writes them
+// (simulation.cc:120-131 opens them, 685-1064 writes them). The formatting
+// is the reference's: the same ostream insertions and precisions, including
+// the precision each stream keeps from its previous setprecision.
+//
+// Not built: the pressure (CalcPressure*, pressure.cc) and the chemical
+// potential (CalcChemicalPotentialF, cbmc.cc:444-531). The stat file's
+// pressure column is the reference's "nan" for systems without walls; with
+// walls it holds six "nan" where the reference prints its pressure tensor.
+#include <cmath>
+#include <fstream>
+#include <iomanip>
+
+#include "../../../include/plum_host.hpp"
+
+namespace plum {
+
+namespace {
+constexpr double kRhoZ = 0.02;  // density_z_res (simulation.cc:113)
+}
+
+void Simulation::EnableOutput(const std::string& dir) {
+  if (run_.calc_chem_pot)
+    throw InputError("the chemical potential (calc_chem_pot) is not built; outputs need it off");
+  out_dir_ = dir.empty() ? "." : dir;
+  run_name_ = run_.run_name;
+  const std::string base = out_dir_ + "/" + run_name_;
+  info_out.open(base + "_stat.dat");
+  traj_p_out.open(base + "_traj_p.xyz");
+  traj_c_out.open(base + "_traj_c.xyz");
+  traj_a_out.open(base + "_traj_a.xyz");
+  traj_n_out.open(base + "_traj_n.xyz");
+  if (!info_out || !traj_p_out || !traj_c_out || !traj_a_out || !traj_n_out)
+    throw InputError("cannot open the output files in " + out_dir_);
+  out_on_ = true;
+  PrintStatHeader();
+}
+
+void Simulation::PrintStatHeader() {
+  info_out << "#Step";
+  if (run_.use_pair) info_out << " " << "<PairEne>";
+  if (run_.use_ewald) info_out << " " << "<EwaldEne>";
+  if (run_.use_bond) info_out << " " << "<BondEne>";
+  if (run_.use_ext) info_out << " " << "<ExtPotEne>";
+  info_out << " " << "<TotalEnergy>";
+  if (run_.use_gc) {
+    info_out << " " << "NoOfMol";
+    info_out << " " << "<Density>";
+  }
+  if (run_.use_ext)
+    info_out << " " << "<Pzz_LJ_ion> <Pzz_LJ_pol> <Pzz_LJ_wal> <Pzz_EL_ion>"
+             << " " << "<Pzz_EL_pol> <Pzz_EL_wal>";
+  else
+    info_out << " " << "<P>";
+  info_out << " " << "<|Rg|> <|Rgx|> <|Rgy|> <|Rgz|> <ete>";
+  info_out << " " << "beadtrans comtrans pivot crankshaft reptate";
+  if (run_.use_gc) info_out << " " << "insert delete";
+  info_out << std::endl;
+}
+
+void Simulation::PrintStat() {
+  if (!out_on_ || run_.stat_out_freq <= 0 || step % run_.stat_out_freq != 0) return;
+  info_out << step;
+  const double n = (double)ff_avg_counter;
+  double tot_energy = 0;
+  if (run_.use_pair) {
+    info_out << " " << std::setprecision(7) << pair_e_cumu / n;
+    tot_energy += pair_e_cumu / n;
+  }
+  if (run_.use_ewald) {
+    info_out << " " << std::setprecision(7) << ewald_e_cumu / n;
+    tot_energy += ewald_e_cumu / n;
+  }
+  if (run_.use_bond) {
+    info_out << " " << std::setprecision(7) << bond_e_cumu / n;
+    tot_energy += bond_e_cumu / n;
+  }
+  if (run_.use_ext) {
+    info_out << " " << std::setprecision(7) << ext_e_cumu / n;
+    tot_energy += ext_e_cumu / n;
+  }
+  info_out << " " << tot_energy;
+  if (run_.use_gc)
+    info_out << " " << (int)mols.size() << " " << std::setprecision(4) << density_cumu / n;
+  // ForceField::GetPressure (pressure.cc:490-500)
+  if (run_.use_ext)
+    info_out << " " << "nan nan nan nan nan nan";
+  else
+    info_out << " " << "nan";
+  const double m = (double)mol_avg_counter;
+  info_out << " " << std::setprecision(4) << std::sqrt(rg_tot_cumu / m) << " "
+           << std::setprecision(4) << std::sqrt(rg_x_cumu / m) << " " << std::setprecision(4)
+           << std::sqrt(rg_y_cumu / m) << " " << std::setprecision(4) << std::sqrt(rg_z_cumu / m)
+           << " " << std::setprecision(4) << std::sqrt(e_to_e_cumu / m);
+  for (int k = 0; k < 5; k++) info_out << " " << accepted[k] / (double)attempted[k];
+  if (run_.use_gc) {
+    info_out << " " << insertion_accepted / (double)insertion_attempted;
+    info_out << " " << deletion_accepted / (double)deletion_attempted;
+  }
+  info_out << std::endl;
+}
+
+namespace {
+
+// Shift that brings a molecule's centre into the primary cell
+// (simulation.cc:895-906): floor(centre / L) * L per axis.
+void image_shift(const Molecule& m, const double* box, double* d) {
+  double c[3] = {0, 0, 0};
+  for (const Bead& b : m.bds)
+    for (int a = 0; a < 3; a++) c[a] += b.GetCrd(0, a);
+  for (int a = 0; a < 3; a++) {
+    c[a] /= (double)m.Size();
+    d[a] = std::floor(c[a] / box[a]) * box[a];
+  }
+}
+
+}  // namespace
+
+void Simulation::PrintTraj() {
+  if (!out_on_ || !(step > run_.steps_eq && run_.traj_out_freq > 0 &&
+                    step % run_.traj_out_freq == 0))
+    return;
+  if (run_.grafted + n_chain > 0) {
+    traj_p_out << n_chain_b << std::endl;
+    traj_p_out << "STEP: " << step << std::endl;
+  }
+  if (n_cion > 0) {
+    traj_c_out << n_cion << std::endl;
+    traj_c_out << "STEP: " << step << std::endl;
+  }
+  if (n_aion > 0) {
+    traj_a_out << n_aion << std::endl;
+    traj_a_out << "STEP: " << step << std::endl;
+  }
+  if (n_nion > 0) {
+    traj_n_out << n_nion << std::endl;
+    traj_n_out << "STEP: " << step << std::endl;
+  }
+  for (int i = run_.phantom; i < n_mol; i++) {
+    double d[3];
+    image_shift(mols[i], box_l, d);
+    std::ofstream* out;
+    if (mols[i].Size() > 1)
+      out = &traj_p_out;
+    else if (mols[i].bds[0].Charge() > 0)
+      out = &traj_c_out;
+    else if (mols[i].bds[0].Charge() < 0)
+      out = &traj_a_out;
+    else
+      out = &traj_n_out;
+    for (const Bead& b : mols[i].bds) {
+      *out << b.Symbol() << " ";
+      *out << b.GetCrd(0, 0) - d[0] << " ";
+      *out << b.GetCrd(0, 1) - d[1] << " ";
+      *out << b.GetCrd(0, 2) - d[2] << std::endl;
+    }
+  }
+}
+
+void Simulation::PrintLastCrd() {
+  if (!out_on_ || !(step > run_.steps_eq && run_.stat_out_freq > 0 &&
+                    step % run_.stat_out_freq == 0))
+    return;
+  const char* bck[2] = {"", "2"};
+  for (int f = 0; f < 2; f++) {
+    crd_last_out[f].open(out_dir_ + "/" + run_name_ + "_lastcrd.dat" + bck[f]);
+    crd_last_out[f] << n_bead_ << std::endl;
+    crd_last_out[f] << " " << std::endl;
+    for (int i = 0; i < n_mol; i++) {
+      double d[3];
+      image_shift(mols[i], box_l, d);
+      if (i < run_.phantom) d[0] = d[1] = d[2] = 0;
+      for (const Bead& b : mols[i].bds) {
+        crd_last_out[f] << i << " ";
+        crd_last_out[f] << b.Symbol() << " ";
+        crd_last_out[f] << std::setprecision(18) << b.GetCrd(0, 0) - d[0] << " ";
+        crd_last_out[f] << std::setprecision(18) << b.GetCrd(0, 1) - d[1] << " ";
+        crd_last_out[f] << std::setprecision(18) << b.GetCrd(0, 2) - d[2] << " ";
+        crd_last_out[f] << std::setprecision(4) << b.Charge() << std::endl;
+      }
+    }
+    crd_last_out[f].close();
+  }
+}
+
+void Simulation::PrintLastTop() {
+  if (!out_on_ || !(step > run_.steps_eq && run_.stat_out_freq > 0 &&
+                    step % run_.stat_out_freq == 0))
+    return;
+  top_last_out.open(out_dir_ + "/" + run_name_ + "_lasttop.dat");
+  top_last_out << "TotNoOfBeads: " << n_bead_ << std::endl;
+  top_last_out << "TotNoOfMolec: " << n_mol << std::endl;
+  top_last_out << "Box_Length_X: " << std::setprecision(18) << box_l[0] << std::endl;
+  top_last_out << "Box_Length_Y: " << std::setprecision(18) << box_l[1] << std::endl;
+  top_last_out << "Box_Length_Z: " << std::setprecision(18) << box_l[2] << std::endl;
+  top_last_out << "bonds:" << std::endl;
+  top_last_out << "-1" << std::endl;
+  top_last_out << "angles:" << std::endl;
+  top_last_out << "-1" << std::endl;
+  top_last_out << "diheds" << std::endl;
+  top_last_out << "-1" << std::endl;
+  top_last_out.close();
+}
+
+void Simulation::PrintLastRhoZ() {
+  if (!out_on_ || !(step > run_.steps_eq && run_.stat_out_freq > 0 &&
+                    step % run_.stat_out_freq == 0))
+    return;
+  const char* bck[2] = {"", "2"};
+  const int bins = (int)density_z_cumu.size() / 3;
+  for (int f = 0; f < 2; f++) {
+    rho_last_out[f].open(out_dir_ + "/" + run_name_ + "_lastrhoZ.dat" + bck[f]);
+    for (int bin = 0; bin < bins; bin++) {
+      const double pos = (bin + 0.5) * kRhoZ;
+      rho_last_out[f] << pos << '\t' << density_z_cumu[3 * bin + 0] / (double)ff_avg_counter
+                      << '\t' << density_z_cumu[3 * bin + 1] / (double)ff_avg_counter << '\t'
+                      << density_z_cumu[3 * bin + 2] / (double)ff_avg_counter << std::endl;
+    }
+    rho_last_out[f].close();
+  }
+}
+
+void Simulation::Finish() {
+  if (!out_on_) return;
+  // the reference's destructor runs after its step loop, with step one past
+  // the last step
+  const long keep = step;
+  step = keep + 1;
+  PrintLastCrd();
+  PrintLastTop();
+  step = keep;
+  info_out.close();
+  traj_p_out.close();
+  traj_c_out.close();
+  traj_a_out.close();
+  traj_n_out.close();
+  out_on_ = false;
+}
+
+}  // namespace plum

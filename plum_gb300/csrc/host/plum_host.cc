@@ -499,16 +499,22 @@ Simulation::Simulation(std::istream& runin, const std::string& dir, unsigned see
   for (int a = 0; a < 3; a++) box_l[a] = info.box[a];
   npbc = info.npbc;
   rand_gen.seed(seed);
+  // rho(z) accumulator: ceil(Lz / 0.02) bins x {chain, q >= 0 ion, q < 0 ion}
+  // (simulation.cc:112-117)
+  density_z_cumu.assign(3 * (size_t)std::ceil(box_l[2] / 0.02), 0.0);
   UpdateMolCounts();
 }
 
 void Simulation::UpdateMolCounts() {
   n_mol = (int)mols.size();
-  n_chain = n_cion = n_aion = n_nion = 0;
+  n_chain = n_chain_b = n_cion = n_aion = n_nion = 0;
+  n_bead_ = run_.phantom;  // each phantom molecule counted as one bead
   for (int i = run_.phantom; i < n_mol; i++) {
-    if (mols[i].Size() > 1)
+    n_bead_ += mols[i].Size();
+    if (mols[i].Size() > 1) {
       n_chain++;
-    else if (mols[i].bds[0].Charge() > 0)
+      n_chain_b += mols[i].Size();
+    } else if (mols[i].bds[0].Charge() > 0)
       n_cion++;
     else if (mols[i].bds[0].Charge() < 0)
       n_aion++;
@@ -644,10 +650,17 @@ void Simulation::RunSteps(long n) {
     std::vector<uint32_t> stream(words);
     for (long i = 0; i < words; i++) stream[i] = rand_gen();
     long used = 0;
-    check(plum_run_moves(force_field.Context(), stream.data(), words, chunk, nullptr, nullptr,
-                         nullptr, &used));
+    std::vector<int> mt(chunk), ac(chunk);
+    check(plum_run_moves(force_field.Context(), stream.data(), words, chunk, mt.data(),
+                         ac.data(), nullptr, &used));
     rand_gen = g0;
     rand_gen.discard((unsigned long long)used);
+    // attempted / accepted per move type (simulation.cc:319, 341)
+    for (int i = 0; i < chunk; i++)
+      if (mt[i] >= 0 && mt[i] < 5) {
+        attempted[mt[i]]++;
+        if (ac[i]) accepted[mt[i]]++;
+      }
     step += chunk;
     n -= chunk;
   }
@@ -655,12 +668,27 @@ void Simulation::RunSteps(long n) {
 }
 
 void Simulation::Run() {
+  UpdateMolCounts();
   for (long s = 0; s < run_.steps;) {
-    long to_sample = run_.sample_freq > 0 ? run_.sample_freq - (step % run_.sample_freq) : run_.steps;
-    long n = std::min(to_sample, run_.steps - s);
+    // run on the device up to the next step where the reference samples or
+    // writes (its loop checks every step, simulation.cc:219-237)
+    long n = run_.steps - s;
+    auto upto = [&](long f) {
+      if (f > 0) n = std::min(n, f - (step % f));
+    };
+    upto(run_.sample_freq);
+    if (out_on_) {
+      upto(run_.stat_out_freq);
+      upto(run_.traj_out_freq);
+    }
     RunSteps(n);
     s += n;
     Sample();
+    PrintStat();
+    PrintTraj();
+    PrintLastCrd();
+    PrintLastTop();
+    PrintLastRhoZ();
   }
 }
 
@@ -682,14 +710,34 @@ void Simulation::Sample() {
   ff_avg_counter++;
   double e[4];
   check(plum_energies(force_field.Context(), e));
-  pair_e_cumu += e[0];
-  ewald_e_cumu += e[1];
-  bond_e_cumu += e[2];
-  ext_e_cumu += e[3];
+  if (run_.use_pair) pair_e_cumu += e[0];
+  if (run_.use_ewald) ewald_e_cumu += e[1];
+  if (run_.use_bond) bond_e_cumu += e[2];
+  if (run_.use_ext) ext_e_cumu += e[3];
+  density_cumu += (double)mols.size() / (box_l[0] * box_l[1] * box_l[2]);
+  // CalcRhoZ (simulation.cc:1029-1045): one sample added to the accumulator
+  int bins = 0;
+  check(plum_rhoz(force_field.Context(), nullptr, 0, &bins));
+  std::vector<double> rz(3 * (size_t)bins);
+  check(plum_rhoz(force_field.Context(), rz.data(), (int)rz.size(), nullptr));
+  for (size_t k = 0; k < rz.size() && k < density_z_cumu.size(); k++) density_z_cumu[k] += rz[k];
+  if (mols.empty()) return;
   mol_avg_counter++;
   double o[5];
   check(plum_observables(force_field.Context(), o));
   rg_tot_cumu += o[0];
+  // RadiusOfGyrationXYZ returns its three values through an ostringstream
+  // with the default six significant digits (simulation.cc:476-478), and
+  // Sample reads them back from that string
+  std::ostringstream foo;
+  foo << o[1] << " " << o[2] << " " << o[3];
+  std::istringstream iss(foo.str());
+  double x = 0, y = 0, z = 0;
+  iss >> x >> y >> z;
+  rg_x_cumu += x;
+  rg_y_cumu += y;
+  rg_z_cumu += z;
+  e_to_e_cumu += o[4];
 }
 
 double Simulation::RadiusOfGyration() {
@@ -766,6 +814,33 @@ int plum_sim_n_bead(plum_sim* s) {
   int n = 0;
   for (auto& m : s->s->mols) n += m.Size();
   return n;
+}
+
+int plum_sim_enable_output(plum_sim* s, const char* dir) {
+  try {
+    s->s->EnableOutput(dir ? dir : ".");
+    return PLUM_OK;
+  } catch (const std::exception&) {
+    return PLUM_ERR_INPUT;
+  }
+}
+
+int plum_sim_run(plum_sim* s) {
+  try {
+    s->s->Run();
+    return PLUM_OK;
+  } catch (const std::exception&) {
+    return PLUM_ERR_STATE;
+  }
+}
+
+int plum_sim_finish(plum_sim* s) {
+  try {
+    s->s->Finish();
+    return PLUM_OK;
+  } catch (const std::exception&) {
+    return PLUM_ERR_STATE;
+  }
 }
 
 int plum_sim_run_steps(plum_sim* s, long n) {

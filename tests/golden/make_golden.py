@@ -16,11 +16,12 @@ input_crd.dat, input_top.dat) and ref.npz with, from the reference:
   rng_words     the reference generator's first outputs for run_seed
 
 Run from the repository root:  python tests/golden/make_golden.py
-[moves] [cbmc] [long | long:<case>] [stats] [gc] (needs the reference checkout;
+[moves] [cbmc] [long | long:<case>] [stats] [gc] [outputs] (needs the reference checkout;
 the fixtures themselves are committed). "long" adds long.npz, a 1e5-step
 run, to the cases in LONG_CASES (about 40 min each at the reference's
 speed); "stats" writes the STAT_CASES with stats.npz, 8 seeded 6e4-step
-reference runs each (about 15 min on 8 cores).
+reference runs each (about 15 min on 8 cores); "outputs" writes the
+OUTPUT_CASES: the reference's own output files of a sampled run.
 """
 from __future__ import annotations
 
@@ -336,6 +337,56 @@ def make_case(name, cfg, n_de=24):
     print(name, "beads", int(start[-1]), "accept", ac.mean(), "types", np.bincount(mt + 1))
 
 
+# Output files: the reference's Simulation::Run with sampling and writing on
+# an existing case's inputs, run.in items 4-8 replaced (steps, equilibration
+# steps, sampling / stat / trajectory frequencies).
+OUTPUT_CASES = {"outputs_bulk_small": dict(src="bulk_small", seed=77, steps=3000, steps_eq=1000,
+                                           sample_freq=10, stat_freq=500, traj_freq=1000)}
+OUTPUT_FILES = ("out_stat.dat", "out_traj_p.xyz", "out_traj_c.xyz", "out_traj_a.xyz",
+                "out_traj_n.xyz", "out_lastcrd.dat", "out_lastcrd.dat2", "out_lasttop.dat",
+                "out_lastrhoZ.dat", "out_lastrhoZ.dat2")
+
+
+def output_runin(src_runin, cfg):
+    """The case's run.in with the run name "out" and the run-control items
+    of the output case (lines 3-8 of the positional grammar)."""
+    lines = open(src_runin).read().splitlines()
+    keys = {2: "out", 3: cfg["steps"], 4: cfg["steps_eq"], 5: cfg["sample_freq"],
+            6: cfg["stat_freq"], 7: cfg["traj_freq"]}
+    for i, v in keys.items():
+        flag = lines[i].split()[0]
+        lines[i] = "%s %s" % (flag, v)
+    return "\n".join(lines) + "\n"
+
+
+def make_output_cases():
+    import tempfile
+    for name, cfg in OUTPUT_CASES.items():
+        src = os.path.join(HERE, cfg["src"])
+        dst = os.path.join(HERE, name)
+        os.makedirs(dst, exist_ok=True)
+        with open(os.path.join(dst, "run.in"), "w") as f:
+            f.write(output_runin(os.path.join(src, "run.in"), cfg))
+        with tempfile.TemporaryDirectory() as d:
+            for f in ("input_crd.dat", "input_top.dat"):
+                shutil.copy(os.path.join(src, f), os.path.join(d, f))
+            shutil.copy(os.path.join(dst, "run.in"), os.path.join(d, "run.in"))
+            R = ob.Ref(d, seed=cfg["seed"])
+            R.run_full()
+            coords = R.coords()
+            R.close()  # the destructor's last writes
+            for f in OUTPUT_FILES:
+                shutil.copy(os.path.join(d, f), os.path.join(dst, f))
+            # the sampling (and the pressure routine it calls every tenth
+            # sample) must leave the trajectory alone: the plain step loop
+            # from the same seed ends in the same coordinates
+            P = ob.Ref(d, seed=cfg["seed"])
+            P.run(cfg["steps"])
+            assert np.array_equal(P.coords(), coords), "sampling changed the trajectory"
+            P.close()
+        print(name, "written:", ", ".join(OUTPUT_FILES))
+
+
 if __name__ == "__main__":
     ob.build()
     which = sys.argv[1:] or ["moves", "cbmc"]
@@ -352,3 +403,5 @@ if __name__ == "__main__":
         make_stat_cases()
     if "gc" in which:
         make_gc_cases()
+    if "outputs" in which:
+        make_output_cases()
