@@ -141,6 +141,20 @@ int plum_get_positions(const plum_ctx* ctx, double* xyz);
 /* Replaces the current coordinates (n_bead*3) and recomputes the energy. */
 int plum_set_positions(plum_ctx* ctx, const double* xyz);
 
+/* Snapshot of a context's step state for an exact restart (no reference
+ * counterpart: the reference only writes its last coordinates): current
+ * positions, running energies, S(k) with any pending update of the last
+ * accepted move, per-molecule bond energies and the device counters.
+ * plum_ctx_save copies it into a host buffer of plum_ctx_snapshot_size
+ * bytes; plum_ctx_load restores it into a context created from the same
+ * inputs and form (else PLUM_ERR_INPUT), after which the same draws
+ * (plum_run_moves, or the host classes' generator) give bit-identical
+ * steps. The device generator of plum_run is not part of it. No move may be
+ * pending. */
+long plum_ctx_snapshot_size(const plum_ctx* ctx);
+int plum_ctx_save(const plum_ctx* ctx, void* buf, long size);
+int plum_ctx_load(plum_ctx* ctx, const void* buf, long size);
+
 /* out[5] = {Rg^2 averaged over chains, Rg_x^2, Rg_y^2, Rg_z^2, end-to-end^2}
  * of the current configuration. Replaces Simulation::RadiusOfGyration,
  * RadiusOfGyrationXYZ and EndToEndDistance (simulation.cc:406-500). */

@@ -190,6 +190,13 @@ class Simulation {  // simulation.h:20-201 (step loop and observables)
   // The writes of the reference's destructor (simulation.cc:202-211), which
   // see step = steps + 1; closes the files.
   void Finish();
+  // Exact restart (no reference counterpart): the step count, the
+  // generator's state, the counters and running averages, and the device
+  // context's snapshot (plum_ctx_save). ReadCheckpoint on a Simulation built
+  // from the same inputs continues bit-identically. Runs with
+  // grand-canonical exchange (whose molecule list changes) are refused.
+  void WriteCheckpoint(const std::string& path);
+  void ReadCheckpoint(const std::string& path);
 
   std::vector<Molecule> mols;
   ForceField force_field;

@@ -104,6 +104,8 @@ def lib():
         L.plum_sim_enable_output.argtypes = [C.c_void_p, C.c_char_p]
         L.plum_sim_run.argtypes = [C.c_void_p]
         L.plum_sim_finish.argtypes = [C.c_void_p]
+        L.plum_sim_write_checkpoint.argtypes = [C.c_void_p, C.c_char_p]
+        L.plum_sim_read_checkpoint.argtypes = [C.c_void_p, C.c_char_p]
         _fp = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
         L.plum_surrogate_create.argtypes = [C.c_int, C.c_ulonglong, C.POINTER(C.c_void_p)]
         L.plum_surrogate_destroy.argtypes = [C.c_void_p]
@@ -589,3 +591,11 @@ class HostSimulation:
     def finish(self):
         """The writes of the reference's destructor; closes the files."""
         _check(lib().plum_sim_finish(self.h))
+
+    def write_checkpoint(self, path):
+        """Step, generator state, counters, averages and the device state
+        for an exact restart."""
+        _check(lib().plum_sim_write_checkpoint(self.h, str(path).encode()))
+
+    def read_checkpoint(self, path):
+        _check(lib().plum_sim_read_checkpoint(self.h, str(path).encode()))

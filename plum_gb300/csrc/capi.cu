@@ -1109,6 +1109,98 @@ int plum_set_positions(plum_ctx* c, const double* xyz) {
   return total_energy(c, nullptr);
 }
 
+// Snapshot layout: a header of four ints {magic, n_bead, n_k, n_mol} and
+// the form, then DevState, pos [n_bead], sk [n_k], dsk [2 n_k], bond_mol
+// [n_mol], then the recompute bookkeeping {since_recompute, drift[4],
+// drift_max}.
+namespace {
+constexpr int kSnapMagic = 0x504c4d53;  // "SMLP"
+size_t snap_bytes(const plum_ctx* c) {
+  return 5 * sizeof(int) + sizeof(DevState) + sizeof(double4_32a) * c->P.n_bead +
+         sizeof(double2) * 3 * (size_t)c->P.n_k + sizeof(double) * c->P.n_mol +
+         sizeof(long) + 5 * sizeof(double);
+}
+}  // namespace
+
+long plum_ctx_snapshot_size(const plum_ctx* c) { return c ? (long)snap_bytes(c) : 0; }
+
+int plum_ctx_save(const plum_ctx* cc, void* buf, long size) {
+  plum_ctx* c = const_cast<plum_ctx*>(cc);
+  if (!c || !buf || size < (long)snap_bytes(c)) return fail(PLUM_ERR_INPUT, "bad argument");
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
+  cudaSetDevice(c->device);
+  unsigned char* p = static_cast<unsigned char*>(buf);
+  const int head[5] = {kSnapMagic, c->P.n_bead, c->P.n_k, c->P.n_mol, c->form};
+  std::memcpy(p, head, sizeof(head));
+  p += sizeof(head);
+  CK(cudaMemcpyAsync(p, c->B.state, sizeof(DevState), cudaMemcpyDeviceToHost, c->s));
+  p += sizeof(DevState);
+  CK(cudaMemcpyAsync(p, c->B.pos, sizeof(double4_32a) * c->P.n_bead, cudaMemcpyDeviceToHost,
+                     c->s));
+  p += sizeof(double4_32a) * c->P.n_bead;
+  if (c->P.n_k > 0) {
+    CK(cudaMemcpyAsync(p, c->B.sk, sizeof(double2) * c->P.n_k, cudaMemcpyDeviceToHost, c->s));
+    CK(cudaMemcpyAsync(p + sizeof(double2) * c->P.n_k, c->B.dsk, sizeof(double2) * 2 * c->P.n_k,
+                       cudaMemcpyDeviceToHost, c->s));
+  }
+  p += sizeof(double2) * 3 * (size_t)c->P.n_k;
+  CK(cudaMemcpyAsync(p, c->B.bond_mol, sizeof(double) * c->P.n_mol, cudaMemcpyDeviceToHost,
+                     c->s));
+  p += sizeof(double) * c->P.n_mol;
+  CK(cudaStreamSynchronize(c->s));
+  std::memcpy(p, &c->since_recompute, sizeof(long));
+  p += sizeof(long);
+  std::memcpy(p, c->drift, 4 * sizeof(double));
+  std::memcpy(p + 4 * sizeof(double), &c->drift_max, sizeof(double));
+  return PLUM_OK;
+}
+
+int plum_ctx_load(plum_ctx* c, const void* buf, long size) {
+  if (!c || !buf || size < (long)(5 * sizeof(int))) return fail(PLUM_ERR_INPUT, "bad argument");
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
+  const unsigned char* p = static_cast<const unsigned char*>(buf);
+  int head[5];
+  std::memcpy(head, p, sizeof(head));
+  if (head[0] != kSnapMagic || head[1] != c->P.n_bead || head[2] != c->P.n_k ||
+      head[3] != c->P.n_mol || head[4] != c->form || size < (long)snap_bytes(c))
+    return fail(PLUM_ERR_INPUT, "the snapshot belongs to another system or form");
+  cudaSetDevice(c->device);
+  p += sizeof(head);
+  CK(cudaStreamSynchronize(c->s));
+  // the snapshot replaces the device state, the generator's stream cursor
+  // included; it is then reset to an empty stream (plum_run refills it)
+  DevState st;
+  std::memcpy(&st, p, sizeof(DevState));
+  st.stream_pos = st.stream_len = 0;
+  p += sizeof(DevState);
+  CK(cudaMemcpyAsync(c->B.state, &st, sizeof(DevState), cudaMemcpyHostToDevice, c->s));
+  CK(cudaMemcpyAsync(c->B.pos, p, sizeof(double4_32a) * c->P.n_bead, cudaMemcpyHostToDevice,
+                     c->s));
+  CK(cudaMemcpyAsync(c->B.trial, p, sizeof(double4_32a) * c->P.n_bead, cudaMemcpyHostToDevice,
+                     c->s));
+  std::memcpy(c->h_pos.data(), p, sizeof(double4_32a) * c->P.n_bead);
+  p += sizeof(double4_32a) * c->P.n_bead;
+  if (c->P.n_k > 0) {
+    CK(cudaMemcpyAsync(c->B.sk, p, sizeof(double2) * c->P.n_k, cudaMemcpyHostToDevice, c->s));
+    CK(cudaMemcpyAsync(c->B.dsk, p + sizeof(double2) * c->P.n_k, sizeof(double2) * 2 * c->P.n_k,
+                       cudaMemcpyHostToDevice, c->s));
+  }
+  p += sizeof(double2) * 3 * (size_t)c->P.n_k;
+  CK(cudaMemcpyAsync(c->B.bond_mol, p, sizeof(double) * c->P.n_mol, cudaMemcpyHostToDevice,
+                     c->s));
+  p += sizeof(double) * c->P.n_mol;
+  std::memcpy(&c->since_recompute, p, sizeof(long));
+  p += sizeof(long);
+  std::memcpy(c->drift, p, 4 * sizeof(double));
+  std::memcpy(&c->drift_max, p + 4 * sizeof(double), sizeof(double));
+  if (c->form == PLUM_FORM_FP32) launch_fix_all(c->P, c->B, c->s);  // the fixed-point mirror
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->s));
+  c->h_pos_valid = true;
+  c->gen_len = 0;
+  return PLUM_OK;
+}
+
 int plum_observables(const plum_ctx* cc, double* out) {
   plum_ctx* c = const_cast<plum_ctx*>(cc);
   if (!c || !out) return fail(PLUM_ERR_INPUT, "null argument");

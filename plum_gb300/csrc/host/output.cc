@@ -9,8 +9,12 @@
 // pressure column is the reference's "nan" for systems without walls; with
 // walls it holds six "nan" where the reference prints its pressure tensor.
 #include <cmath>
+#include <cstdint>
 #include <fstream>
 #include <iomanip>
+#include <sstream>
+#include <stdexcept>
+#include <vector>
 
 #include "../../../include/plum_host.hpp"
 
@@ -236,6 +240,96 @@ void Simulation::Finish() {
   traj_a_out.close();
   traj_n_out.close();
   out_on_ = false;
+}
+
+namespace {
+
+template <typename T>
+void put(std::ostream& o, const T& v) {
+  o.write(reinterpret_cast<const char*>(&v), sizeof(T));
+}
+template <typename T>
+void get(std::istream& i, T& v) {
+  i.read(reinterpret_cast<char*>(&v), sizeof(T));
+}
+constexpr uint32_t kCkptMagic = 0x4b43504cu;  // "LPCK"
+
+}  // namespace
+
+void Simulation::WriteCheckpoint(const std::string& path) {
+  if (force_field.UseGC()) throw InputError("checkpoints of exchange runs are not built");
+  std::ofstream o(path, std::ios::binary);
+  if (!o) throw InputError("cannot write " + path);
+  std::ostringstream g;
+  g << rand_gen;
+  const std::string gs = g.str();
+  put(o, kCkptMagic);
+  put(o, step);
+  put(o, (uint64_t)gs.size());
+  o.write(gs.data(), (std::streamsize)gs.size());
+  for (int k = 0; k < 5; k++) {
+    put(o, accepted[k]);
+    put(o, attempted[k]);
+  }
+  const double sums[10] = {pair_e_cumu, ewald_e_cumu, bond_e_cumu, ext_e_cumu, rg_tot_cumu,
+                           rg_x_cumu,   rg_y_cumu,    rg_z_cumu,   e_to_e_cumu, density_cumu};
+  for (double v : sums) put(o, v);
+  put(o, ff_avg_counter);
+  put(o, mol_avg_counter);
+  put(o, (uint64_t)density_z_cumu.size());
+  o.write(reinterpret_cast<const char*>(density_z_cumu.data()),
+          (std::streamsize)(sizeof(double) * density_z_cumu.size()));
+  const long n = plum_ctx_snapshot_size(force_field.Context());
+  std::vector<char> snap((size_t)n);
+  if (plum_ctx_save(force_field.Context(), snap.data(), n))
+    throw std::runtime_error(std::string("plum_ctx_save: ") + plum_last_error());
+  put(o, (uint64_t)n);
+  o.write(snap.data(), n);
+  if (!o) throw InputError("cannot write " + path);
+}
+
+void Simulation::ReadCheckpoint(const std::string& path) {
+  if (force_field.UseGC()) throw InputError("checkpoints of exchange runs are not built");
+  std::ifstream i(path, std::ios::binary);
+  uint32_t magic = 0;
+  get(i, magic);
+  if (!i || magic != kCkptMagic) throw InputError(path + " is not a checkpoint");
+  get(i, step);
+  uint64_t len = 0;
+  get(i, len);
+  std::string gs(len, ' ');
+  i.read(&gs[0], (std::streamsize)len);
+  std::istringstream g(gs);
+  g >> rand_gen;
+  for (int k = 0; k < 5; k++) {
+    get(i, accepted[k]);
+    get(i, attempted[k]);
+  }
+  double sums[10];
+  for (double& v : sums) get(i, v);
+  pair_e_cumu = sums[0];
+  ewald_e_cumu = sums[1];
+  bond_e_cumu = sums[2];
+  ext_e_cumu = sums[3];
+  rg_tot_cumu = sums[4];
+  rg_x_cumu = sums[5];
+  rg_y_cumu = sums[6];
+  rg_z_cumu = sums[7];
+  e_to_e_cumu = sums[8];
+  density_cumu = sums[9];
+  get(i, ff_avg_counter);
+  get(i, mol_avg_counter);
+  get(i, len);
+  if (len != density_z_cumu.size()) throw InputError(path + " belongs to another box");
+  i.read(reinterpret_cast<char*>(density_z_cumu.data()), (std::streamsize)(sizeof(double) * len));
+  get(i, len);
+  std::vector<char> snap(len);
+  i.read(snap.data(), (std::streamsize)len);
+  if (!i) throw InputError(path + " is truncated");
+  if (plum_ctx_load(force_field.Context(), snap.data(), (long)len))
+    throw InputError(std::string("plum_ctx_load: ") + plum_last_error());
+  SyncFromDevice();
+  UpdateMolCounts();
 }
 
 }  // namespace plum

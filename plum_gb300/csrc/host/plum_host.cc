@@ -825,6 +825,24 @@ int plum_sim_enable_output(plum_sim* s, const char* dir) {
   }
 }
 
+int plum_sim_write_checkpoint(plum_sim* s, const char* path) {
+  try {
+    s->s->WriteCheckpoint(path ? path : "");
+    return PLUM_OK;
+  } catch (const std::exception&) {
+    return PLUM_ERR_INPUT;
+  }
+}
+
+int plum_sim_read_checkpoint(plum_sim* s, const char* path) {
+  try {
+    s->s->ReadCheckpoint(path ? path : "");
+    return PLUM_OK;
+  } catch (const std::exception&) {
+    return PLUM_ERR_INPUT;
+  }
+}
+
 int plum_sim_run(plum_sim* s) {
   try {
     s->s->Run();

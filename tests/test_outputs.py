@@ -88,3 +88,25 @@ def test_output_files_match_reference(tmp_path):
     for f in FILES:
         compare_files(tmp_path / f, os.path.join(CASE, f),
                       coord_tol=1e-7 if "lastcrd" in f else None)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", [0, 1])
+def test_checkpoint_restart_is_exact(tmp_path, form):
+    """300 steps, a checkpoint, 300 more steps; a second Simulation from the
+    same inputs (another seed) reads the checkpoint and runs the same 300
+    steps: bit-identical positions and energies."""
+    import numpy as np
+    import plum_gb300 as pg
+    a = pg.HostSimulation(SRC, seed=11, form=form)
+    a.run_steps(300)
+    ck = tmp_path / "state.ckpt"
+    a.write_checkpoint(ck)
+    a.run_steps(300)
+    b = pg.HostSimulation(SRC, seed=99, form=form)
+    b.read_checkpoint(ck)
+    b.run_steps(300)
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    np.testing.assert_array_equal(a.energies(), b.energies())
+    a.close()
+    b.close()
