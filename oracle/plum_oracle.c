@@ -124,6 +124,10 @@ struct po_ctx {
   double kpref;         /* lB/(kPi V) * 4 kPi^2 */
   double k_bond, r0;
   double wall_cut, wall_sig[MAXT], wall_eps[MAXT];
+  /* pair 0 TruncatedLJ, 1 HardSphere; external 0 TruncatedLJWall, 1
+   * HardWall, 2 WellWall: radii per type, the well's width and depth */
+  int pair_kind, ext_kind;
+  double hs_rad[MAXT], wall_rad[MAXT], well_width, well_depth;
   int graft[MAXT]; /* 0 none, 1 "L", 2 "R" */
   /* running totals (force_field.cc:1201-1219) */
   double e_pair, e_ewald, e_bond, e_ext, dipl_cur;
@@ -211,6 +215,7 @@ static int type_of(po_ctx* c, const char* s) {
   snprintf(c->sym[c->n_type], 16, "%s", s);
   c->lj_sig[c->n_type] = c->lj_eps[c->n_type] = 0.0;
   c->wall_sig[c->n_type] = c->wall_eps[c->n_type] = 0.0;
+  c->hs_rad[c->n_type] = c->wall_rad[c->n_type] = 0.0;
   c->graft[c->n_type] = !strcmp(s, "L") ? 1 : (!strcmp(s, "R") ? 2 : 0);
   return c->n_type++;
 }
@@ -233,6 +238,26 @@ static void rd_table(rd_t* r, po_ctx* c, double* sig, double* eps) {
     }
     sig[ti] = sg;
     eps[ti] = ep;
+  }
+}
+
+/* {symbol radius}... end (potential_hard_sphere.cc:20-36,
+ * potential_hard_wall.cc:15-33, potential_well_wall.cc:24-37); absent
+ * symbols keep radius 0 as std::map::operator[] gives the reference. */
+static void rd_radii(rd_t* r, po_ctx* c, double* rad) {
+  for (int guard = 0; guard < 100000 && !r->bad; guard++) {
+    const char* s = rd_item(r, "bead type symbol");
+    if (r->bad) return;
+    if (!strcmp(s, "end")) return;
+    char name[16];
+    snprintf(name, 16, "%s", s);
+    double v = rd_d(r, "radius");
+    int ti = type_of(c, name);
+    if (ti < 0) {
+      rd_fail(r, "too many bead types");
+      return;
+    }
+    rad[ti] = v;
   }
 }
 
@@ -267,6 +292,8 @@ static double lj_pair(const po_ctx* c, const double* a, int ta, const double* b,
                       int tb) {
   double energy = 0;
   double r = bbdist(a, b, c->box, c->npbc);
+  if (c->pair_kind == 1) /* PotentialHardSphere::PairEnergy (potential_hard_sphere.cc:38-49) */
+    return r <= c->hs_rad[ta] + c->hs_rad[tb] ? K_VERY_LARGE : 0;
   double sigma = (c->lj_sig[ta] + c->lj_sig[tb]) / 2;
   double epsilon = sqrt((c->lj_eps[ta] * c->lj_eps[tb]));
   if (r <= 0) return K_VERY_LARGE;
@@ -337,6 +364,16 @@ static double bond_mol_energy(const po_ctx* c, int m, const double* p) {
 /* PotentialTruncatedLJWall::BeadEnergy (potential_truncated_lj_wall.cc:46-134). */
 static double wall_energy(const po_ctx* c, double z, int ty) {
   double energy = 0;
+  if (c->ext_kind == 1) { /* PotentialHardWall::BeadEnergy (potential_hard_wall.cc:36-47) */
+    const double rad = c->wall_rad[ty];
+    return (z <= rad || z + rad >= c->box[2]) ? K_VERY_LARGE : 0;
+  }
+  if (c->ext_kind == 2) { /* PotentialWellWall::BeadEnergy (potential_well_wall.cc:41-55) */
+    const double rad = c->wall_rad[ty];
+    if (z <= rad || z >= c->box[2] - rad) return K_VERY_LARGE;
+    if (z < c->well_width || z > c->box[2] - c->well_width) return c->well_depth;
+    return 0;
+  }
   double sigma = c->wall_sig[ty], epsilon = c->wall_eps[ty];
   double R0 = 3 * K213 * sigma, K = 1;
   double lz = c->box[2];
@@ -563,9 +600,14 @@ po_ctx* po_create(const char* dir, const char* runin, uint32_t seed, char* err,
   c->rigid = -1;
   if (c->use_pair) {
     const char* nm = rd_item(&r, "pair potential");
-    if (strcmp(nm, "TruncatedLJ")) rd_fail(&r, "unsupported pair potential %s", nm);
-    c->lj_cut = rd_d(&r, "LJ cutoff");
-    rd_table(&r, c, c->lj_sig, c->lj_eps);
+    if (!strcmp(nm, "HardSphere")) {
+      c->pair_kind = 1;
+      rd_radii(&r, c, c->hs_rad);
+    } else {
+      if (strcmp(nm, "TruncatedLJ")) rd_fail(&r, "unsupported pair potential %s", nm);
+      c->lj_cut = rd_d(&r, "LJ cutoff");
+      rd_table(&r, c, c->lj_sig, c->lj_eps);
+    }
   }
   if (c->use_ewald) {
     const char* nm = rd_item(&r, "Ewald potential");
@@ -584,11 +626,21 @@ po_ctx* po_create(const char* dir, const char* runin, uint32_t seed, char* err,
   if (c->use_rigid) c->rigid = rd_d(&r, "rigid bond");
   if (c->use_ext) {
     const char* nm = rd_item(&r, "external potential");
-    if (strcmp(nm, "TruncatedLJWall")) rd_fail(&r, "unsupported external potential %s", nm);
-    c->wall_cut = rd_d(&r, "wall cutoff");
-    rd_item(&r, "wall sigma");
-    rd_item(&r, "wall epsilon");
-    rd_table(&r, c, c->wall_sig, c->wall_eps);
+    if (!strcmp(nm, "HardWall")) {
+      c->ext_kind = 1;
+      rd_radii(&r, c, c->wall_rad);
+    } else if (!strcmp(nm, "WellWall")) {
+      c->ext_kind = 2;
+      c->well_width = rd_d(&r, "well width");
+      c->well_depth = rd_d(&r, "well depth");
+      rd_radii(&r, c, c->wall_rad);
+    } else {
+      if (strcmp(nm, "TruncatedLJWall")) rd_fail(&r, "unsupported external potential %s", nm);
+      c->wall_cut = rd_d(&r, "wall cutoff");
+      rd_item(&r, "wall sigma");
+      rd_item(&r, "wall epsilon");
+      rd_table(&r, c, c->wall_sig, c->wall_eps);
+    }
   }
   /* Trailing extension block (never read by the reference). */
   double rc_over = -1, kc2_over = -1;
@@ -741,7 +793,8 @@ void po_total_energy(po_ctx* c, double* out) {
     for (int m = 0; m < c->n_mol; m++)
       for (int j = c->mol_start[m]; j < c->mol_start[m + 1] - 1; j++)
         for (int k = j + 1; k < c->mol_start[m + 1]; k++)
-          ep += lj_pair(c, c->x + 3 * j, c->type[j], c->x + 3 * k, c->type[k]);
+          if (!(c->pair_kind == 1 && k == j + 1))  /* hard spheres skip bonded neighbours */
+            ep += lj_pair(c, c->x + 3 * j, c->type[j], c->x + 3 * k, c->type[k]);
     for (int m = 0; m < c->n_mol - 1; m++)
       for (int i = c->mol_start[m]; i < c->mol_start[m + 1]; i++)
         for (int j = c->mol_start[m + 1]; j < c->n_bead; j++)
@@ -798,7 +851,7 @@ static void energy_difference(po_ctx* c, int m, const int* mv, de_t* d) {
     /* potential_pair.cc:152-201 */
     for (int i = b0; i < b1 - 1; i++)
       for (int j = i + 1; j < b1; j++)
-        if (mv[i] || mv[j])
+        if ((mv[i] || mv[j]) && !(c->pair_kind == 1 && j == i + 1))
           de += lj_pair(c, c->t + 3 * i, c->type[i], c->t + 3 * j, c->type[j]) -
                 lj_pair(c, c->x + 3 * i, c->type[i], c->x + 3 * j, c->type[j]);
     for (int o = 0; o < c->n_mol; o++) {

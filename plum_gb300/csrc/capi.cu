@@ -491,12 +491,33 @@ static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out) {
         P.lj_rc2[k] = in.lj_cut * in.lj_cut;
       }
     }
+  // hard spheres: radius sums; symbols absent from the table have radius 0
+  // (std::map::operator[] in potential_hard_sphere.cc:42)
+  P.pair_kind = in.pair_kind;
+  if (in.pair_kind == 1)
+    for (int i = 0; i < P.n_type; i++)
+      for (int j = 0; j < P.n_type; j++) {
+        auto ia = in.hs_radius.find(in.type_names[i]);
+        auto ib = in.hs_radius.find(in.type_names[j]);
+        const double s = (ia != in.hs_radius.end() ? ia->second : 0.0) +
+                         (ib != in.hs_radius.end() ? ib->second : 0.0);
+        const int k = i * P.n_type + j;
+        P.hs_sum[k] = s;
+        // pre-test bound: every r <= s passes r2 < lj_rc2
+        P.lj_rc2[k] = s * s * (1.0 + 1e-5) + 1e-30;
+        P.lj_sig2[k] = P.lj_eps4[k] = P.lj_eref[k] = 0.0;
+      }
   P.wall_cut = in.wall_cut;
+  P.ext_kind = in.ext_kind;
+  P.well_width = in.well_width;
+  P.well_depth = in.well_depth;
   for (int i = 0; i < P.n_type; i++) {
     auto it = in.wall.find(in.type_names[i]);
     P.wall_sig[i] = it != in.wall.end() ? it->second.sigma : 0.0;
     P.wall_eps[i] = it != in.wall.end() ? it->second.epsilon : 0.0;
     P.graft[i] = in.type_names[i] == "L" ? 1 : (in.type_names[i] == "R" ? 2 : 0);
+    auto ir = in.wall_radius.find(in.type_names[i]);
+    P.wall_rad[i] = ir != in.wall_radius.end() ? ir->second : 0.0;
   }
   std::vector<int> chains, ions;
   for (int m = in.phantom; m < in.n_mol; m++) {
@@ -531,6 +552,7 @@ static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out) {
     P.f_lj_eps4[k] = (float)P.lj_eps4[k];
     P.f_lj_rc2[k] = (float)P.lj_rc2[k];
     P.f_lj_eref[k] = (float)P.lj_eref[k];
+    P.f_hs_sum[k] = (float)P.hs_sum[k];
   }
   P.f_real_cut = (float)P.real_cut;
   P.f_sqrt_alpha = (float)P.sqrt_alpha;

@@ -9,6 +9,16 @@ namespace plum {
 
 // Wall energy of one bead at height z (potential_truncated_lj_wall.cc:46-134).
 __device__ __forceinline__ double wall64(const DevParams& P, double z, int ty) {
+  if (P.ext_kind == 1) {  // PotentialHardWall::BeadEnergy (potential_hard_wall.cc:36-47)
+    const double rad = P.wall_rad[ty];
+    return (z <= rad || z + rad >= P.box[2]) ? kVeryLarge : 0.0;
+  }
+  if (P.ext_kind == 2) {  // PotentialWellWall::BeadEnergy (potential_well_wall.cc:41-55)
+    const double rad = P.wall_rad[ty];
+    if (z <= rad || z >= P.box[2] - rad) return kVeryLarge;
+    if (z < P.well_width || z > P.box[2] - P.well_width) return P.well_depth;
+    return 0.0;
+  }
   double energy = 0.0;
   const double sigma = P.wall_sig[ty], eps = P.wall_eps[ty];
   const double R0 = 3 * 1.25992104989 * sigma, K = 1.0;
@@ -75,6 +85,22 @@ __device__ __forceinline__ int4 fix_point(const DevParams& P, double4_32a p, int
   return make_int4(fix_axis(p.x, P.ebox[0], P.inv_fix[0], true),
                    fix_axis(p.y, P.ebox[1], P.inv_fix[1], true),
                    fix_axis(p.z, P.ebox[2], P.inv_fix[2], P.npbc > 2), type);
+}
+
+// Hard spheres leave out the pair energy of a chain's bonded neighbours
+// (potential_pair.cc:64-67, 163-167): beads i and j = i +- 1 of the same
+// molecule (the higher index does not start a molecule; mol_start holds
+// n_mol + 1 ascending entries).
+__device__ __forceinline__ bool hs_bonded(const DevParams& P, const int* mol_start, int i,
+                                          int j) {
+  if (P.pair_kind != 1 || (j - i != 1 && i - j != 1)) return false;
+  const int hi = i > j ? i : j;
+  int lo = 0, up = P.n_mol;
+  while (lo < up) {
+    const int mid = (lo + up) >> 1;
+    if (mol_start[mid] < hi) lo = mid + 1; else up = mid;
+  }
+  return mol_start[lo] != hi;
 }
 
 // Cell of a bead of the descriptor's cell list from its fixed-point

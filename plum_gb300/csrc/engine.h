@@ -66,6 +66,17 @@ struct DevParams {
   double kpref;      // lB/(kPi V) * 4 kPi^2
   double self_coef;  // -lB sqrt(alpha/kPi)
   double dip_coef;   // lB * 2 kPi / V
+  // pair_kind 1: hard spheres (potential_hard_sphere.cc:38-49): overlap when
+  // r <= hs_sum[k] (radius sum of the type pair); bonded neighbours of a
+  // chain are skipped (potential_pair.cc:64-67, 163-167). The LJ tables then
+  // hold lj_rc2 = a bound just above hs_sum^2 for the pre-tests.
+  int pair_kind;
+  double hs_sum[kMaxT2];
+  float f_hs_sum[kMaxT2];
+  // ext_kind 1: hard wall, 2: square-well wall (potential_hard_wall.cc:36-47,
+  // potential_well_wall.cc:41-55), radius per type
+  int ext_kind;
+  double wall_rad[kMaxTypes], well_width, well_depth;
   // bonds (potential_spring.cc:22-48)
   double k_bond, r0;
   // walls (potential_truncated_lj_wall.cc:46-134)

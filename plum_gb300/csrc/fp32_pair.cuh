@@ -33,6 +33,7 @@ __device__ __forceinline__ float erfc_nr(float x) {
 }
 
 __device__ __forceinline__ float lj32(const DevParams& P, int k, float r2) {
+  if (P.pair_kind == 1) return sqrtf(r2) <= P.f_hs_sum[k] ? (float)kVeryLarge : 0.0f;
   if (r2 <= 0.0f) return (float)kVeryLarge;
   if (r2 < P.f_lj_rc2[k]) {
     float s2 = __fdividef(P.f_lj_sig2[k], r2);

@@ -31,6 +31,19 @@ struct Reader {
 };
 
 // {flag symbol; flag sigma; flag epsilon}... until the symbol "end".
+// {symbol radius}... end
+bool read_radii(Reader& r, std::map<std::string, double>* t) {
+  for (int guard = 0; guard < 1000000; guard++) {
+    std::string sym;
+    if (!r.item(&sym, "bead type symbol")) return false;
+    if (sym == "end") return true;
+    double v = 0;
+    if (!r.item(&v, "radius")) return false;
+    (*t)[sym] = v;
+  }
+  return r.fail("a radius table without an 'end' token");
+}
+
 bool read_table(Reader& r, std::map<std::string, LJEntry>* t) {
   for (int guard = 0; guard < 1000000; guard++) {
     std::string sym;
@@ -112,12 +125,17 @@ static bool read_stream(const std::string& dir, std::istream& f, Input* in, std:
   std::string name;
   if (in->use_pair && !r.bad) {
     r.item(&name, "pair potential name");
-    if (!r.bad && name != "TruncatedLJ") {
-      *err = "unsupported pair potential " + name;
-      return false;
+    if (!r.bad && name == "HardSphere") {
+      in->pair_kind = 1;
+      read_radii(r, &in->hs_radius);
+    } else {
+      if (!r.bad && name != "TruncatedLJ") {
+        *err = "unsupported pair potential " + name;
+        return false;
+      }
+      r.item(&in->lj_cut, "LJ cutoff");
+      read_table(r, &in->lj);
     }
-    r.item(&in->lj_cut, "LJ cutoff");
-    read_table(r, &in->lj);
   }
   if (in->use_ewald && !r.bad) {
     r.item(&name, "Ewald potential name");
@@ -142,14 +160,24 @@ static bool read_stream(const std::string& dir, std::istream& f, Input* in, std:
   if (in->use_rigid && !r.bad) r.item(&in->rigid, "rigid bond length");
   if (in->use_ext && !r.bad) {
     r.item(&name, "external potential name");
-    if (!r.bad && name != "TruncatedLJWall") {
-      *err = "unsupported external potential " + name;
-      return false;
+    if (!r.bad && name == "HardWall") {
+      in->ext_kind = 1;
+      read_radii(r, &in->wall_radius);
+    } else if (!r.bad && name == "WellWall") {
+      in->ext_kind = 2;
+      r.item(&in->well_width, "well width");
+      r.item(&in->well_depth, "well depth");
+      read_radii(r, &in->wall_radius);
+    } else {
+      if (!r.bad && name != "TruncatedLJWall") {
+        *err = "unsupported external potential " + name;
+        return false;
+      }
+      r.item(&in->wall_cut, "wall cutoff");
+      r.item(&in->wall_sigma, "wall sigma");
+      r.item(&in->wall_eps, "wall epsilon");
+      read_table(r, &in->wall);
     }
-    r.item(&in->wall_cut, "wall cutoff");
-    r.item(&in->wall_sigma, "wall sigma");
-    r.item(&in->wall_eps, "wall epsilon");
-    read_table(r, &in->wall);
   }
   if (r.bad) return false;
   for (;;) {

@@ -9,7 +9,10 @@
 //                                potential_truncated_lj.cc:20-47,
 //                                potential_ewald_coul.cc:29-37,
 //                                potential_spring.cc:11-20,
-//                                potential_truncated_lj_wall.cc:13-44
+//                                potential_truncated_lj_wall.cc:13-44,
+//                                potential_hard_sphere.cc:20-36,
+//                                potential_hard_wall.cc:15-33,
+//                                potential_well_wall.cc:15-40
 //   topology                     simulation.cc:610-646
 //   coordinates                  simulation.cc:582-608
 // Differences from the reference's readers, all on malformed input only: a
@@ -55,6 +58,13 @@ struct Input {
   double k_bond = 0, r0 = 0, rigid = -1;
   double wall_cut = 0, wall_sigma = 0, wall_eps = 0;
   std::map<std::string, LJEntry> wall;
+  // pair_kind 0 TruncatedLJ, 1 HardSphere (radius per symbol,
+  // potential_hard_sphere.cc:20-36); ext_kind 0 TruncatedLJWall, 1 HardWall,
+  // 2 WellWall (radius per symbol and the well, potential_hard_wall.cc:15-33,
+  // potential_well_wall.cc:15-40)
+  int pair_kind = 0, ext_kind = 0;
+  std::map<std::string, double> hs_radius, wall_radius;
+  double well_width = 0, well_depth = 0;
   // extension block
   double x_real_cutoff = -1;
   int x_kmax = -1;

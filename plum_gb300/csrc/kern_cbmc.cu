@@ -34,6 +34,7 @@ __device__ __forceinline__ double cb_lj(const DevParams& P, int ta, int tb, doub
   double z = P.npbc > 2 ? cb_wrap(b.z - a.z, P.box[2], P.inv_box[2]) : b.z - a.z;
   double r2 = x * x + y * y + z * z;
   int k = ta * P.n_type + tb;
+  if (P.pair_kind == 1) return sqrt(r2) <= P.hs_sum[k] ? kVeryLarge : 0.0;  // hard spheres
   if (r2 <= 0.0) return kVeryLarge;
   if (r2 < P.lj_rc2[k]) {
     double s2 = P.lj_sig2[k] / r2;

@@ -35,6 +35,7 @@ __device__ __forceinline__ double wrap_d(double d, double L, double invL) {
 // LJ of one pair at squared distance r2 (the reference's r <= 0 overlap gives
 // the 1e8 sentinel).
 __device__ __forceinline__ double lj64(const DevParams& P, int k, double r2) {
+  if (P.pair_kind == 1) return sqrt(r2) <= P.hs_sum[k] ? kVeryLarge : 0.0;  // hard spheres
   if (r2 <= 0.0) return kVeryLarge;
   if (r2 < P.lj_rc2[k]) {
     double s2 = P.lj_sig2[k] / r2;
@@ -190,7 +191,7 @@ __global__ void __launch_bounds__(kPairThreads)
       double l1 = 0, r1 = 0, l0 = 0, r0 = 0;
       pair64(P, ti, tyi, tj, tyj, l1, r1);
       pair64(P, ci, tyi, cj, tyj, l0, r0);
-      acc_lj += l1 - l0;
+      if (!hs_bonded(P, B.mol_start, i, j)) acc_lj += l1 - l0;
       acc_re += r1 - r0;
     }
   }
@@ -354,7 +355,9 @@ __global__ void __launch_bounds__(kTotTile)
     const int ti = B.type[i];
     for (int jj = 0; jj < jn; jj++) {
       if (ta == tb && jj <= (int)threadIdx.x) continue;
-      pair64(P, pi, ti, sp[jj], st[jj], lj, re);
+      double l = 0.0;
+      pair64(P, pi, ti, sp[jj], st[jj], l, re);
+      if (!hs_bonded(P, B.mol_start, i, j0 + jj)) lj += l;
     }
   }
   double a = block_sum<kTotTile>(lj, red);

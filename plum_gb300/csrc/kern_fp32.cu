@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(kPairThreads)
       float l1 = 0, r1 = 0, l0 = 0, r0 = 0;
       pair32(P, ti, qi, tj, qj, l1, r1);
       pair32(P, ci, qi, cj, qj, l0, r0);
-      acc_lj += l1 - l0;
+      if (!hs_bonded(P, B.mol_start, i, j)) acc_lj += l1 - l0;
       acc_re += r1 - r0;
     }
   }
@@ -296,8 +296,9 @@ __device__ __forceinline__ void pair32k(const DevParams& P, const PairConst& K, 
 template <bool kSingle>
 __device__ __forceinline__ void pair_sweep(const DevParams& P, const PairConst& K,
                                            const DevBuffers& B, const int4* s_mt,
-                                           const float* s_mq, int gn, int c0, int c1, int b_lo,
-                                           int b_hi, float& acc_lj, float& acc_re) {
+                                           const float* s_mq, int gn, int g_lo, int c0, int c1,
+                                           int b_lo, int b_hi, float& acc_lj, float& acc_re) {
+  const bool hs = P.pair_kind == 1;
   for (int j = c0 + threadIdx.x; j < c1; j += kPairThreads) {
     if (j >= b_lo && j < b_hi) continue;  // moved pairs: the last item
     const int4 cj = B.fpos[j];
@@ -307,7 +308,7 @@ __device__ __forceinline__ void pair_sweep(const DevParams& P, const PairConst& 
       float l1 = 0, r1 = 0, l0 = 0, r0 = 0;
       pair32k<kSingle>(P, K, s_mt[u], s_mq[u], cj, qj, l1, r1);
       pair32k<kSingle>(P, K, s_mt[kPairGroup + u], s_mq[u], cj, qj, l0, r0);
-      acc_lj += l1 - l0;
+      if (!(hs && hs_bonded(P, B.mol_start, g_lo + u, j))) acc_lj += l1 - l0;
       acc_re += r1 - r0;
     }
   }
@@ -405,9 +406,11 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
         __syncthreads();
         const PairConst K = pair_const(P);
         if (P.single_image)
-          pair_sweep<true>(P, K, B, s_mt, s_mq, gn, c0, c1, b_lo, b_hi, acc_lj, acc_re);
+          pair_sweep<true>(P, K, B, s_mt, s_mq, gn, b_lo + g0, c0, c1, b_lo, b_hi, acc_lj,
+                           acc_re);
         else
-          pair_sweep<false>(P, K, B, s_mt, s_mq, gn, c0, c1, b_lo, b_hi, acc_lj, acc_re);
+          pair_sweep<false>(P, K, B, s_mt, s_mq, gn, b_lo + g0, c0, c1, b_lo, b_hi, acc_lj,
+                            acc_re);
       } else {
         // pairs among the moved beads, each once (both trial / both current)
         const int lane = threadIdx.x & 31;
@@ -417,7 +420,8 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
           pair32(P, B.ftrial[a], B.fq[b_lo + a], B.ftrial[bb], B.fq[b_lo + bb], l1, r1);
           pair32(P, B.fpos[b_lo + a], B.fq[b_lo + a], B.fpos[b_lo + bb], B.fq[b_lo + bb], l0,
                  r0);
-          acc_lj += l1 - l0;
+          // the moved beads are one molecule's: neighbours are bonded
+          if (!(P.pair_kind == 1 && bb == a + 1)) acc_lj += l1 - l0;
           acc_re += r1 - r0;
         }
       }

@@ -195,8 +195,13 @@ def runin_text(*, crd="input_crd.dat", top="input_top.dat", run_name="output",
                alpha=0.015625, dipole=False, use_bond=True, k_bond=400.0, r0=1.0,
                use_rigid=True, rigid=1.0, use_ext=False, wall_cut=-1.0,
                wall_table=(), use_gc=False, gc=None, real_cutoff=None, kmax=None,
-               kcut2=None) -> str:
-    """A run.in in the reference's positional grammar."""
+               kcut2=None, pair_kind="TruncatedLJ", hs_radii=(), ext_kind="TruncatedLJWall",
+               wall_radii=(), well_width=1.0, well_depth=-1.0) -> str:
+    """A run.in in the reference's positional grammar. pair_kind
+    "HardSphere" reads hs_radii ((symbol, radius), ...) instead of the LJ
+    table (potential_hard_sphere.cc:20-36); ext_kind "HardWall" / "WellWall"
+    read wall_radii (and the well's width and depth) instead of the 9-3 wall
+    table (potential_hard_wall.cc:15-33, potential_well_wall.cc:15-40)."""
     L = []
     a = L.append
     a("s1_input_coordinate_file %s" % crd)
@@ -232,7 +237,13 @@ def runin_text(*, crd="input_crd.dat", top="input_top.dat", run_name="output",
         for k in ("chem_pot", "deBroglie", "gc_freq", "chain_len", "bead_charge",
                   "bead_symbol", "cbmc_trials"):
             a("s3_gc_%s %s" % (k, gc[k]))
-    if use_pair:
+    if use_pair and pair_kind == "HardSphere":
+        a("s3_short_range_potential_type HardSphere")
+        for i, (s, rad) in enumerate(hs_radii):
+            a("s3_bead_type_%d %s" % (i + 1, s))
+            a("s3_radius_for_bead_type_%d %.17g" % (i + 1, rad))
+        a("s3_end_flag end")
+    elif use_pair:
         a("s3_short_range_potential_type TruncatedLJ")
         a("s3_LJ_cutoff %.17g" % lj_cutoff)
         for i, (s, sg, ep) in enumerate(lj_table):
@@ -252,7 +263,16 @@ def runin_text(*, crd="input_crd.dat", top="input_top.dat", run_name="output",
         a("s3_equilibrium_length %.17g" % r0)
     if use_rigid:
         a("s3_rigid_bond_length %.17g" % rigid)
-    if use_ext:
+    if use_ext and ext_kind in ("HardWall", "WellWall"):
+        a("s3_external_potential_type %s" % ext_kind)
+        if ext_kind == "WellWall":
+            a("s3_well_width %.17g" % well_width)
+            a("s3_well_depth %.17g" % well_depth)
+        for i, (s, rad) in enumerate(wall_radii):
+            a("s3_bead_type_%d %s" % (i + 1, s))
+            a("s3_radius_for_bead_type_%d %.17g" % (i + 1, rad))
+        a("s3_end_flag end")
+    elif use_ext:
         a("s3_external_potential_type TruncatedLJWall")
         a("s3_LJ_cutoff %.17g" % wall_cut)
         a("s3_wall_sigma 1")

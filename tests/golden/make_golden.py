@@ -54,6 +54,23 @@ CASES = {
     "slab_lj": dict(kind="brush", seed=4, run_seed=98, steps=600,
                     spec=systems.BrushSpec(n_graft=5, chain_len=10, lxy=12.0, height=16.0,
                                            n_sites=8, wall_cut=2.5, charge_frac=0.5)),
+    # the other potentials of the reference's pair and external surface
+    # (potential_hard_sphere.cc, potential_hard_wall.cc, potential_well_wall.cc);
+    # radii below the generators' minimum separation of 0.8 and no surface
+    # sites (the external energy counts every bead, the sites included)
+    "hs_bulk": dict(kind="bulk", seed=10, run_seed=55, steps=600,
+                    spec=systems.BulkSpec(n_chain=4, chain_len=12, n_ion=48, box=13.0),
+                    over=dict(pair_kind="HardSphere", hs_radii=(("P", 0.35), ("C", 0.3)))),
+    "slab_hardwall": dict(kind="brush", seed=11, run_seed=56, steps=600,
+                          spec=systems.BrushSpec(n_graft=4, chain_len=8, lxy=10.0, height=12.0,
+                                                 n_sites=0, charge_frac=0.6),
+                          over=dict(ext_kind="HardWall",
+                                    wall_radii=(("P", 0.5), ("L", 0.0), ("C", 0.5)))),
+    "slab_wellwall": dict(kind="brush", seed=12, run_seed=57, steps=600,
+                          spec=systems.BrushSpec(n_graft=4, chain_len=8, lxy=10.0, height=12.0,
+                                                 n_sites=0, charge_frac=0.6),
+                          over=dict(ext_kind="WellWall", well_width=2.0, well_depth=-0.7,
+                                    wall_radii=(("P", 0.5), ("L", 0.0), ("C", 0.5)))),
 }
 
 
@@ -286,9 +303,9 @@ def make_case(name, cfg, n_de=24):
         shutil.rmtree(d)
     os.makedirs(d)
     if cfg["kind"] == "bulk":
-        systems.write_bulk(d, cfg["spec"], seed=cfg["seed"])
+        systems.write_bulk(d, cfg["spec"], seed=cfg["seed"], **cfg.get("over", {}))
     else:
-        systems.write_brush(d, cfg["spec"], seed=cfg["seed"])
+        systems.write_brush(d, cfg["spec"], seed=cfg["seed"], **cfg.get("over", {}))
     out = {}
     R = ob.Ref(d, seed=cfg["run_seed"])
     out["energies"] = R.energies()
@@ -392,6 +409,9 @@ if __name__ == "__main__":
     which = sys.argv[1:] or ["moves", "cbmc"]
     if "moves" in which:
         for name, cfg in CASES.items():
+            make_case(name, cfg)
+    for name, cfg in CASES.items():
+        if "case:" + name in which:
             make_case(name, cfg)
     if "cbmc" in which:
         for name, cfg in CBMC_CASES.items():
