@@ -77,6 +77,10 @@ def _load_ref():
         L.pr_beads_energy.restype = C.c_double
         L.pr_gc_info.argtypes = [C.c_void_p, _dp]
         L.pr_run_full.argtypes = [C.c_void_p]
+        L.pr_pressure_force_slit.argtypes = [C.c_void_p, _dp]
+        L.pr_wall_force.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        L.pr_wall_force.restype = C.c_double
+        L.pr_ewald_force_z.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _dp]
         _ref_lib = L
     return _ref_lib
 
@@ -109,6 +113,10 @@ def _load_oracle():
         L.po_beads_energy.argtypes = [C.c_void_p, _dp, C.c_void_p, C.c_int, C.c_void_p,
                                       C.c_void_p, C.c_int]
         L.po_beads_energy.restype = C.c_double
+        L.po_pressure_force_slit.argtypes = [C.c_void_p, _dp]
+        L.po_wall_force.argtypes = [C.c_void_p, C.c_int]
+        L.po_wall_force.restype = C.c_double
+        L.po_ewald_force_z.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp]
         _orc_lib = L
     return _orc_lib
 
@@ -180,6 +188,20 @@ class Ref(_Base):
 
     def run(self, n):
         return self._steps(self.L.pr_run, n)
+
+    def pressure_force_slit(self):
+        """p_tensor[0..11] after one CalcPressureForceLJELSlit."""
+        o = np.zeros(12)
+        self.L.pr_pressure_force_slit(self.h, o)
+        return o
+
+    def wall_force(self, mol, bead):
+        return self.L.pr_wall_force(self.h, mol, bead)
+
+    def ewald_force_z(self, ma, ia, mb, ib):
+        o = np.zeros(2)
+        self.L.pr_ewald_force_z(self.h, ma, ia, mb, ib, o)
+        return o
 
     def run_full(self):
         """The reference's Simulation::Run with its sampling and output
@@ -285,6 +307,21 @@ class Oracle(_Base):
     def observables(self):
         o = np.zeros(5)
         self.L.po_observables(self.h, o)
+        return o
+
+    def pressure_force_slit(self):
+        """p_tensor[0..11] after one wall-force pressure evaluation
+        (ForceField::CalcPressureForceLJELSlit, pressure.cc:400-488)."""
+        o = np.zeros(12)
+        self.L.po_pressure_force_slit(self.h, o)
+        return o
+
+    def wall_force(self, i):
+        return self.L.po_wall_force(self.h, i)
+
+    def ewald_force_z(self, a, b):
+        o = np.zeros(2)
+        self.L.po_ewald_force_z(self.h, a, b, o)
         return o
 
     def rhoz(self, cap=1 << 20):

@@ -129,6 +129,9 @@ struct po_ctx {
   int pair_kind, ext_kind;
   double hs_rad[MAXT], wall_rad[MAXT], well_width, well_depth;
   int graft[MAXT]; /* 0 none, 1 "L", 2 "R" */
+  /* wall-force pressure of slit systems (pressure.cc:400-488): the number of
+   * evaluations and the accumulators p_tensor[0..11] */
+  double vp_z, p_tensor[12];
   /* running totals (force_field.cc:1201-1219) */
   double e_pair, e_ewald, e_bond, e_ext, dipl_cur;
   double* bond_mol;
@@ -1520,6 +1523,205 @@ void po_set_coords(po_ctx* c, const double* xyz) {
 
 /* RadiusOfGyration / RadiusOfGyrationXYZ / EndToEndDistance
  * (simulation.cc:406-500). */
+/* ------------------------------------------------ wall-force pressure */
+/* PotentialTruncatedLJ::PairForce (potential_truncated_lj.cc:87-122): beyond
+ * a positive cut-off it returns the cut-off's r^-6 term at r, as the
+ * reference does; hard spheres have no force (potential_hard_sphere.cc:51-56). */
+static double lj_force(const po_ctx* c, const double* a, int ta, const double* b, int tb) {
+  if (c->pair_kind == 1) return 0;
+  double r = bbdist(a, b, c->box, c->npbc);
+  double sigma = (c->lj_sig[ta] + c->lj_sig[tb]) / 2;
+  double epsilon = sqrt((c->lj_eps[ta] * c->lj_eps[tb]));
+  double r6;
+  if (r <= 0) return K_VERY_LARGE;
+  if (c->lj_cut < 0) {
+    if (r < K216 * sigma) {
+      r6 = pow((sigma / r), 6);
+      return 4 * epsilon * (r6 * r6 * 12 / r - r6 * 6 / r);
+    }
+    return 0;
+  }
+  if (r < c->lj_cut)
+    r6 = pow((sigma / r), 6);
+  else
+    r6 = pow((sigma / c->lj_cut), 6);
+  return 4 * epsilon * (r6 * r6 * 12 / r - r6 * 6 / r);
+}
+
+/* GetDistVector (misc.cc:43-56): from b1 to b2, wrapped on periodic axes. */
+static void dist_vec(const double* b1, const double* b2, const double* box, int npbc,
+                     double* r) {
+  for (int i = 0; i < 3; i++) {
+    double di = b2[i] - b1[i];
+    if (i < npbc) di -= box[i] * round(di / box[i]);
+    r[i] = di;
+  }
+}
+
+/* PotentialEwaldCoul::PairForceZReal (potential_ewald_coul.cc:261-293): the
+ * z force on wall charge a from bead b, real space over the image cells. */
+static double ew_force_z_real(const po_ctx* c, const double* a, double qa, const double* b,
+                              double qb) {
+  double force_z = 0;
+  if (qa * qb == 0) return force_z;
+  double r[3];
+  dist_vec(b, a, c->ebox, c->npbc, r);
+  double prefactor = c->lB * qa * qb;
+  double prefactor2 = 2 * sqrt(c->alpha / K_PI);
+  for (int i = -c->real_cell[0]; i <= c->real_cell[0]; i++)
+    for (int j = -c->real_cell[1]; j <= c->real_cell[1]; j++)
+      for (int k = -c->real_cell[2]; k <= c->real_cell[2]; k++) {
+        double v[3] = {r[0] + i * c->ebox[0], r[1] + j * c->ebox[1], r[2] + k * c->ebox[2]};
+        double d = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        if (d > 0 && d <= c->real_cut)
+          force_z += prefactor * ((prefactor2 * exp(-c->alpha * d * d)) +
+                                  (erfc(sqrt(c->alpha) * d) / d)) * v[2] / (d * d);
+      }
+  return force_z;
+}
+
+/* PotentialEwaldCoul::PairForceZRepl (potential_ewald_coul.cc:297-324): the
+ * reference sums k_z e^{-k^2/4a}/k^2 sin(k.r) over the whole k cube; the
+ * summand is even under k -> -k, so here twice the half space. */
+static double ew_force_z_repl(const po_ctx* c, const double* a, double qa, const double* b,
+                              double qb) {
+  if (qa * qb == 0) return 0;
+  double r[3];
+  dist_vec(b, a, c->ebox, c->npbc, r);
+  double prefactor = c->lB * 4 * K_PI * qa * qb / c->evol;
+  double f = 0;
+  for (int k = 0; k < c->n_k; k++) {
+    const double* kv = c->kv + 3 * k;
+    f += kv[2] * c->kw[k] * sin(kv[0] * r[0] + kv[1] * r[1] + kv[2] * r[2]);
+  }
+  return prefactor * 2 * f;
+}
+
+/* PotentialTruncatedLJWall::BeadForceOnWall (potential_truncated_lj_wall.cc:
+ * 136-214); the hard and square-well walls have none. */
+static double wall_force(const po_ctx* c, double z, int ty) {
+  if (c->ext_kind != 0) return 0;
+  double force = 0;
+  double sigma = c->wall_sig[ty], epsilon = c->wall_eps[ty];
+  double R0 = 3 * K213 * sigma, K = 1, lz = c->box[2], mc = c->wall_cut;
+  const double k93 = 2.59807621135;
+  int g = c->graft[ty];
+  if (epsilon == 0) return 0;
+  if (z <= 0 || z >= lz) return K_VERY_LARGE;
+  if (mc < 0 && g == 0) {
+    if (z < K213 * sigma) {
+      double r3 = pow((sigma / z), 3);
+      force += k93 * epsilon * (r3 * r3 * 6 / z - r3 * 3 / z);
+    }
+    if (lz - z < K213 * sigma) {
+      double r3 = pow((sigma / (lz - z)), 3);
+      force += k93 * epsilon * (r3 * r3 * 6 / (lz - z) - r3 * 3 / (lz - z));
+    }
+  } else if (g == 1) {
+    double r3 = pow((sigma / z), 3);
+    force += k93 * epsilon * (r3 * r3 * 6 / z - r3 * 3 / z);
+    force += -K * R0 * z / (1 - pow(z / R0, 2));
+    if (lz - z < K213 * sigma) {
+      r3 = pow((sigma / (lz - z)), 3);
+      force += k93 * epsilon * (r3 * r3 * 6 / (lz - z) - r3 * 3 / (lz - z));
+    }
+  } else if (g == 2) {
+    double r3 = pow((sigma / (lz - z)), 3);
+    force += k93 * epsilon * (r3 * r3 * 6 / (lz - z) - r3 * 3 / (lz - z));
+    force += -K * R0 * (lz - z) / (1 - pow((lz - z) / R0, 2));
+    if (z < K213 * sigma) {
+      r3 = pow((sigma / z), 3);
+      force += k93 * epsilon * (r3 * r3 * 6 / z - r3 * 3 / z);
+    }
+  } else {
+    double r3 = pow((sigma / (z < mc ? z : mc)), 3);
+    force += k93 * epsilon * (r3 * r3 * 6 / z - r3 * 3 / z);
+    if (lz - z < mc) {
+      r3 = pow((sigma / (lz - z)), 3);
+      force += k93 * epsilon * (r3 * r3 * 6 / (lz - z) - r3 * 3 / (lz - z));
+    } else {
+      r3 = pow((sigma / mc), 3);
+      force += k93 * epsilon * (r3 * r3 * 6 / z - r3 * 3 / z);
+    }
+  }
+  return force;
+}
+
+/* The pieces, for the checks against the reference: the wall force of bead
+ * i, and the real / reciprocal z force on bead a from bead b. */
+double po_wall_force(const po_ctx* c, int i) { return wall_force(c, c->x[3 * i + 2], c->type[i]); }
+
+void po_ewald_force_z(const po_ctx* c, int a, int b, double* out2) {
+  out2[0] = ew_force_z_real(c, c->x + 3 * a, c->q[a], c->x + 3 * b, c->q[b]);
+  out2[1] = ew_force_z_repl(c, c->x + 3 * a, c->q[a], c->x + 3 * b, c->q[b]);
+}
+
+/* ForceField::CalcPressureForceLJELSlit (pressure.cc:400-488) on the current
+ * configuration: wall sites (the first phantom molecules, half on each wall)
+ * against the system, plus the 9-3 wall forces; out12 = p_tensor[0..11]
+ * (0-5 the averages the stat file prints, 6-11 the accumulators). */
+void po_pressure_force_slit(po_ctx* c, double* out12) {
+  double* p = c->p_tensor;
+  c->vp_z += 1;
+  const int ph = c->phantom, nm = c->n_mol;
+  for (int i = 0; i < ph; i++) {
+    const int wi = c->mol_start[i];
+    for (int j = ph / 2; j < nm; j++)
+      for (int k = c->mol_start[j]; k < c->mol_start[j + 1]; k++) {
+        double C;
+        if (i < ph / 2 && j >= ph)
+          C = -0.5;
+        else if (i < ph && j >= ph)
+          C = 0.5;
+        else
+          C = -1;
+        int k_id = 2;
+        if (j >= ph) k_id = (c->mol_start[j + 1] - c->mol_start[j] > 1) ? 1 : 0;
+        if (c->use_pair && (i < ph / 2 || j >= ph)) {
+          double r[3];
+          dist_vec(c->x + 3 * k, c->x + 3 * wi, c->box, c->npbc, r);
+          double zc = r[2] / sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+          double f = C * zc * lj_force(c, c->x + 3 * k, c->type[k], c->x + 3 * wi, c->type[wi]);
+          if (k_id == 0)
+            p[6] += f;
+          else if (k_id == 1)
+            p[7] += f;
+          else if (k_id == 2 && c->vp_z == 1)
+            p[8] += f;
+        }
+        if (c->use_ewald && (i < ph / 2 || j >= ph)) {
+          double f = C * ew_force_z_real(c, c->x + 3 * wi, c->q[wi], c->x + 3 * k, c->q[k]);
+          f += C * ew_force_z_repl(c, c->x + 3 * wi, c->q[wi], c->x + 3 * k, c->q[k]);
+          if (k_id == 0)
+            p[9] += f;
+          else if (k_id == 1)
+            p[10] += f;
+          else if (k_id == 2 && c->vp_z == 1)
+            p[11] += f;
+        }
+      }
+  }
+  if (c->use_ext)
+    for (int i = ph; i < nm; i++)
+      for (int j = c->mol_start[i]; j < c->mol_start[i + 1]; j++) {
+        double f = 0.5 * wall_force(c, c->x[3 * j + 2], c->type[j]);
+        if (c->mol_start[i + 1] - c->mol_start[i] > 1)
+          p[7] += f;
+        else
+          p[6] += f;
+      }
+  const double area = c->box[0] * c->box[1];
+  if (c->vp_z == 1) {
+    p[2] = p[8] / area;
+    p[5] = p[11] / area;
+  }
+  p[0] = p[6] / (c->vp_z * area);
+  p[1] = p[7] / (c->vp_z * area);
+  p[3] = p[9] / (c->vp_z * area);
+  p[4] = p[10] / (c->vp_z * area);
+  if (out12) memcpy(out12, p, 12 * sizeof(double));
+}
+
 void po_observables(const po_ctx* c, double* out) {
   double rg = 0, rx = 0, ry = 0, rz = 0, ete = 0;
   for (int m = 0; m < c->n_mol; m++) {

@@ -252,6 +252,33 @@ void pr_delta_energy(void* hp, int mol, const double* trial, const int* moved,
   }
 }
 
+// ForceField::CalcPressureForceLJELSlit (pressure.cc:400-488) on the current
+// configuration; out12 = p_tensor[0..11] after the call.
+void pr_pressure_force_slit(void* hp, double* out12) {
+  Handle* h = (Handle*)hp;
+  CwdGuard cg(h->dir);
+  StreamSwap sw(std::cin.rdbuf(), h->log.rdbuf());
+  h->sim->force_field.CalcPressureForceLJELSlit(h->sim->mols);
+  for (int i = 0; i < 12; i++) out12[i] = h->sim->force_field.p_tensor[i];
+}
+
+// The pieces of the wall-force pressure, on the current configuration:
+// PotentialExternal's BeadForceOnWall of one bead, and
+// PotentialEwaldCoul::PairForceZReal / PairForceZRepl of the z force on bead
+// (ma, ia) from bead (mb, ib): out2 = {real, reciprocal}.
+double pr_wall_force(void* hp, int mol, int bead) {
+  Simulation* s = ((Handle*)hp)->sim;
+  return s->force_field.ext_pot->BeadForceOnWall(s->mols[mol].bds[bead], s->box_l);
+}
+
+void pr_ewald_force_z(void* hp, int ma, int ia, int mb, int ib, double* out2) {
+  Simulation* s = ((Handle*)hp)->sim;
+  Bead& a = s->mols[ma].bds[ia];
+  Bead& b = s->mols[mb].bds[ib];
+  out2[0] = s->force_field.ewald_pot->PairForceZReal(a, b, s->npbc);
+  out2[1] = s->force_field.ewald_pot->PairForceZRepl(a, b, s->npbc);
+}
+
 // The reference's own Simulation::Run (simulation.cc:216-239): every step
 // with its sampling and output files (written into the handle's directory).
 void pr_run_full(void* hp) {
