@@ -81,6 +81,8 @@ def _load_ref():
         L.pr_wall_force.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.pr_wall_force.restype = C.c_double
         L.pr_ewald_force_z.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _dp]
+        L.pr_chem_pot.argtypes = [C.c_void_p]
+        L.pr_chem_pot.restype = C.c_double
         _ref_lib = L
     return _ref_lib
 
@@ -117,6 +119,8 @@ def _load_oracle():
         L.po_wall_force.argtypes = [C.c_void_p, C.c_int]
         L.po_wall_force.restype = C.c_double
         L.po_ewald_force_z.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp]
+        L.po_chem_pot.argtypes = [C.c_void_p]
+        L.po_chem_pot.restype = C.c_double
         _orc_lib = L
     return _orc_lib
 
@@ -202,6 +206,10 @@ class Ref(_Base):
         o = np.zeros(2)
         self.L.pr_ewald_force_z(self.h, ma, ia, mb, ib, o)
         return o
+
+    def chem_pot(self):
+        """CalcChemicalPotentialF's Widom average (consumes the generator)."""
+        return self.L.pr_chem_pot(self.h)
 
     def run_full(self):
         """The reference's Simulation::Run with its sampling and output
@@ -318,6 +326,10 @@ class Oracle(_Base):
 
     def wall_force(self, i):
         return self.L.po_wall_force(self.h, i)
+
+    def chem_pot(self):
+        """The Widom average of 50 test insertions (consumes the generator)."""
+        return self.L.po_chem_pot(self.h)
 
     def ewald_force_z(self, a, b):
         o = np.zeros(2)

@@ -1385,6 +1385,67 @@ static int chain_insertion(po_ctx* c, rng_t* r, double* chain) {
   return rn < (exp(c->beta * c->chem_pot) * weight) * C;
 }
 
+/* ForceField::CalcChemicalPotentialF (cbmc.cc:444-531): Widom's test
+ * insertion of the exchanged species grown by configurational bias,
+ * averaged over n_ins insertions (mu_tot_ins = 50, force_field.cc:236) with
+ * the reference's prefactor (its volume divided by 15.625, unlike the
+ * insertion move's) and an overlap test by equality with 1e8. */
+static double chem_pot_widom(po_ctx* c, rng_t* r, int n_ins) {
+  const int L = c->gc_chain_len, T = c->cbmc_trials;
+  const int charged = c->gc_bead_charge != 0;
+  int spc1, spc2;
+  gc_species(c, &spc1, &spc2);
+  const int spc2_add = charged ? L : 0;
+  double factorial = 1;
+  for (int i = spc1 + 1; i <= spc1 + 1; i++) factorial *= i;
+  for (int i = spc2 + 1; i <= spc2 + spc2_add; i++) factorial *= i;
+  const double vol = c->box[0] * c->box[1] * c->box[2];
+  double vol_over_lam = 1;
+  vol_over_lam *= pow(vol / 15.625 / (c->debroglie / pow((double)L, 1.5)), 1);
+  vol_over_lam *= pow(vol / 15.625 / (c->debroglie / pow(1.0, 1.5)), spc2_add);
+  const double C = vol_over_lam * (1.0 / factorial);
+  double* chain = (double*)calloc((size_t)6 * (L > 0 ? L : 1), sizeof(double));
+  double* tb1 = (double*)malloc(sizeof(double) * 3 * (size_t)T);
+  double* tb2 = (double*)malloc(sizeof(double) * 3 * (size_t)T);
+  double* w = (double*)malloc(sizeof(double) * (size_t)T);
+  double total = 0;
+  for (int n = 0; n < n_ins && !r->overrun; n++) {
+    double weight = 1.0;
+    const int i_index = charged ? L : 0, initial = charged ? 2 : 1;
+    for (int i = 0; i < initial; i++)
+      for (int j = 0; j < 3; j++) chain[3 * (i * L) + j] = (double)rng_u32(r) / MT_MAX * c->box[j];
+    const double dE = po_beads_energy(c, chain, chain + 3 * i_index, 0, chain, chain + 3 * L, -1);
+    if (dE == K_VERY_LARGE)
+      weight *= 0;
+    else
+      weight *= exp(-c->beta * dE);
+    for (int i = 1; i < L; i++) {
+      const double Wi = gen_trials(c, r, chain + 3 * (i - 1), i, chain, chain + 3 * L, -1, tb1,
+                                   tb2, w);
+      weight *= Wi / T;
+      if (weight <= 0 || r->overrun) break;
+      const double rn = (double)rng_u32(r) / MT_MAX * Wi;
+      int cb = 0;
+      double cum = w[0];
+      while (cum < rn && cb < T - 1) cum += w[++cb];
+      for (int j = 0; j < 3; j++) chain[3 * i + j] = tb1[3 * cb + j];
+      if (charged)
+        for (int j = 0; j < 3; j++) chain[3 * (i + L) + j] = tb2[3 * cb + j];
+    }
+    total += weight * C;
+  }
+  free(chain);
+  free(tb1);
+  free(tb2);
+  free(w);
+  return total / (double)n_ins;
+}
+
+double po_chem_pot(po_ctx* c) {
+  rng_t r = {&c->g, NULL, 0, 0, 0};
+  return chem_pot_widom(c, &r, 50);
+}
+
 /* ForceField::CBMCFChainDeletion (cbmc.cc:330-442): the molecule to delete
  * or -1. */
 static int chain_deletion(po_ctx* c, rng_t* r) {

@@ -279,6 +279,17 @@ void pr_ewald_force_z(void* hp, int ma, int ia, int mb, int ib, double* out2) {
   out2[1] = s->force_field.ewald_pot->PairForceZRepl(a, b, s->npbc);
 }
 
+// ForceField::CalcChemicalPotentialF (cbmc.cc:444-531) on the current
+// configuration with the run's generator (it consumes draws).
+double pr_chem_pot(void* hp) {
+  Handle* h = (Handle*)hp;
+  CwdGuard cg(h->dir);
+  StreamSwap sw(std::cin.rdbuf(), h->log.rdbuf());
+  Simulation* s = h->sim;
+  s->force_field.UpdateMolCounts(s->mols);
+  return s->force_field.CalcChemicalPotentialF(s->mols, s->rand_gen);
+}
+
 // The reference's own Simulation::Run (simulation.cc:216-239): every step
 // with its sampling and output files (written into the handle's directory).
 void pr_run_full(void* hp) {
