@@ -124,6 +124,9 @@ class ForceField {  // force_field.h:22-294 (energy surface)
   // returns the molecule to delete, or -1.
   bool CBMCFChainInsertion(std::vector<Molecule>& mols, std::mt19937& rand_gen);
   int CBMCFChainDeletion(std::vector<Molecule>& mols, std::mt19937& rand_gen);
+  // cbmc.cc:444-531: Widom's average over 50 configurational-bias test
+  // insertions of the exchanged species (consumes draws like the reference)
+  double CalcChemicalPotentialF(std::vector<Molecule>& mols, std::mt19937& rand_gen);
   // Commits the molecules appended to mols / removes molecules on the device
   // (force_field.cc:1088-1105; the potentials' AdjustEnergyUponMolDeletion).
   void EnergyInitForAddedMolecule(std::vector<Molecule>& mols, int n_added);
@@ -166,9 +169,10 @@ class Simulation {  // simulation.h:20-201 (step loop and observables)
   // then GCMove or TranslationalMove; last_move_type 5 / 6 for an insertion
   // / deletion attempt, last_accept when the molecule count changed.
   void Step();
-  // simulation.cc:723-798: energies, density, rho(z), Rg (x, y, z rounded to
-  // six significant digits as the reference's string round trip does), end
-  // to end distance; no pressure and no chemical potential
+  // simulation.cc:723-798: energies, density, rho(z), Widom's chemical
+  // potential when run.in asks for it, Rg (x, y, z rounded to six significant
+  // digits as the reference's string round trip does), end to end distance;
+  // no pressure
   void Sample();
   double RadiusOfGyration();  // simulation.cc:406-434
   double EndToEndDistance();  // simulation.cc:483-501
@@ -178,8 +182,7 @@ class Simulation {  // simulation.h:20-201 (step loop and observables)
   // The reference's output files (simulation.cc:120-131), written into dir:
   // <run_name>_stat.dat (its header now), _traj_p/_c/_a/_n.xyz,
   // _lastcrd.dat and .dat2, _lasttop.dat, _lastrhoZ.dat and .dat2, at the
-  // steps where the reference writes them. Off until this is called. Throws
-  // InputError for a run.in that asks for the chemical potential.
+  // steps where the reference writes them. Off until this is called.
   void EnableOutput(const std::string& dir = ".");
   void PrintStatHeader();  // simulation.cc:685-721
   void PrintStat();        // simulation.cc:800-867
@@ -205,6 +208,7 @@ class Simulation {  // simulation.h:20-201 (step loop and observables)
   int accepted[5] = {0, 0, 0, 0, 0}, attempted[5] = {0, 0, 0, 0, 0};
   double pair_e_cumu = 0, ewald_e_cumu = 0, bond_e_cumu = 0, ext_e_cumu = 0, rg_tot_cumu = 0;
   double rg_x_cumu = 0, rg_y_cumu = 0, rg_z_cumu = 0, e_to_e_cumu = 0, density_cumu = 0;
+  double chem_pot_cumu = 0;
   std::vector<double> density_z_cumu;  // [3 * bins] as CalcRhoZ accumulates it
   long ff_avg_counter = 0, mol_avg_counter = 0;
   int last_move_type = -1, last_accept = 0;

@@ -55,6 +55,9 @@ int plum_sim_enable_output(plum_sim* sim, const char* dir);
 int plum_sim_write_checkpoint(plum_sim* sim, const char* path);
 int plum_sim_read_checkpoint(plum_sim* sim, const char* path);
 int plum_sim_run(plum_sim* sim);
+/* ForceField::CalcChemicalPotentialF on the current configuration with the
+ * simulation's generator (Widom average of 50 test insertions). */
+int plum_sim_chem_pot(plum_sim* sim, double* out);
 int plum_sim_finish(plum_sim* sim);
 
 #ifdef __cplusplus

@@ -103,6 +103,7 @@ def lib():
         L.plum_sim_energies.argtypes = [C.c_void_p, _dp]
         L.plum_sim_enable_output.argtypes = [C.c_void_p, C.c_char_p]
         L.plum_sim_run.argtypes = [C.c_void_p]
+        L.plum_sim_chem_pot.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.plum_sim_finish.argtypes = [C.c_void_p]
         L.plum_sim_write_checkpoint.argtypes = [C.c_void_p, C.c_char_p]
         L.plum_sim_read_checkpoint.argtypes = [C.c_void_p, C.c_char_p]
@@ -582,6 +583,13 @@ class HostSimulation:
         """The reference's output files (stat, trajectories, last
         coordinates / topology / rho(z)) into dirpath."""
         _check(lib().plum_sim_enable_output(self.h, str(dirpath).encode()))
+
+    def chem_pot(self):
+        """Widom's average of 50 configurational-bias test insertions
+        (ForceField::CalcChemicalPotentialF; consumes the generator)."""
+        v = C.c_double(0)
+        _check(lib().plum_sim_chem_pot(self.h, C.byref(v)))
+        return v.value
 
     def run(self):
         """The steps of run.in (Simulation::Run): samples and writes where

@@ -4,8 +4,7 @@
 // is the reference's: the same ostream insertions and precisions, including
 // the precision each stream keeps from its previous setprecision.
 //
-// Not built: the pressure (CalcPressure*, pressure.cc) and the chemical
-// potential (CalcChemicalPotentialF, cbmc.cc:444-531). The stat file's
+// Not built: the pressure (CalcPressure*, pressure.cc). The stat file's
 // pressure column is the reference's "nan" for systems without walls; with
 // walls it holds six "nan" where the reference prints its pressure tensor.
 #include <cmath>
@@ -25,8 +24,6 @@ constexpr double kRhoZ = 0.02;  // density_z_res (simulation.cc:113)
 }
 
 void Simulation::EnableOutput(const std::string& dir) {
-  if (run_.calc_chem_pot)
-    throw InputError("the chemical potential (calc_chem_pot) is not built; outputs need it off");
   out_dir_ = dir.empty() ? "." : dir;
   run_name_ = run_.run_name;
   const std::string base = out_dir_ + "/" + run_name_;
@@ -57,6 +54,7 @@ void Simulation::PrintStatHeader() {
              << " " << "<Pzz_EL_pol> <Pzz_EL_wal>";
   else
     info_out << " " << "<P>";
+  if (run_.calc_chem_pot) info_out << " " << "mu";
   info_out << " " << "<|Rg|> <|Rgx|> <|Rgy|> <|Rgz|> <ete>";
   info_out << " " << "beadtrans comtrans pivot crankshaft reptate";
   if (run_.use_gc) info_out << " " << "insert delete";
@@ -92,6 +90,12 @@ void Simulation::PrintStat() {
     info_out << " " << "nan nan nan nan nan nan";
   else
     info_out << " " << "nan";
+  if (run_.calc_chem_pot) {
+    if (chem_pot_cumu / n > 0)
+      info_out << " " << -(1.0 / run_.beta) * std::log(chem_pot_cumu / n);
+    else
+      info_out << " INF";
+  }
   const double m = (double)mol_avg_counter;
   info_out << " " << std::setprecision(4) << std::sqrt(rg_tot_cumu / m) << " "
            << std::setprecision(4) << std::sqrt(rg_x_cumu / m) << " " << std::setprecision(4)

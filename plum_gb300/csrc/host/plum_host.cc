@@ -409,6 +409,55 @@ bool ForceField::CBMCFChainInsertion(std::vector<Molecule>& mols, std::mt19937& 
   return true;
 }
 
+double ForceField::CalcChemicalPotentialF(std::vector<Molecule>& mols, std::mt19937& g) {
+  if (!UseGC()) throw InputError("the chemical potential needs the grand-canonical block");
+  const int L = GCChainLen(), T = (int)gc_[4], n_ins = 50;  // mu_tot_ins (force_field.cc:236)
+  const double qb = gc_[2];
+  const bool charged = qb != 0;
+  int spc1, spc2;
+  GCCounts(mols, &spc1, &spc2);
+  const int spc2_add = charged ? L : 0;
+  double factorial = 1;
+  for (int i = spc1 + 1; i <= spc1 + 1; i++) factorial *= i;
+  for (int i = spc2 + 1; i <= spc2 + spc2_add; i++) factorial *= i;
+  // the reference's volume here is divided by 15.625 (cbmc.cc:465-466)
+  const double vol = info_.box[0] * info_.box[1] * info_.box[2], deb = gc_[1];
+  double vol_over_lam = 1;
+  vol_over_lam *= std::pow(vol / 15.625 / (deb / std::pow((double)L, 1.5)), 1);
+  vol_over_lam *= std::pow(vol / 15.625 / (deb / std::pow(1.0, 1.5)), spc2_add);
+  const double C = vol_over_lam * (1.0 / factorial);
+  chain_.assign(6 * (size_t)L, 0.0);
+  double total = 0;
+  for (int n = 0; n < n_ins; n++) {
+    double weight = 1.0;
+    const int i_index = charged ? L : 0, initial = charged ? 2 : 1;
+    for (int i = 0; i < initial; i++)
+      for (int a = 0; a < 3; a++) chain_[3 * (i * L) + a] = (double)g() / kMax * info_.box[a];
+    double u0 = 0;
+    check(plum_cbmc_trials(ctx_, 1, chain_.data(), charged ? chain_.data() + 3 * i_index : nullptr,
+                           0, nullptr, nullptr, -1, &u0));
+    if (u0 == kVeryLargeEnergy)
+      weight *= 0;
+    else
+      weight *= std::exp(-run_.beta * u0);
+    for (int i = 1; i < L; i++) {
+      // the trial beads are drawn before the weight is tested (cbmc.cc:495-497)
+      const double Wi = CBMCFGenTrialBeads(&chain_[3 * (i - 1)], i, g, -1, nullptr);
+      weight *= Wi / T;
+      if (weight <= 0) break;
+      const double rn = (double)g() / kMax * Wi;
+      int cb = 0;
+      double cum = w_[0];
+      while (cum < rn && cb < T - 1) cum += w_[++cb];
+      for (int a = 0; a < 3; a++) chain_[3 * i + a] = tb1_[3 * cb + a];
+      if (charged)
+        for (int a = 0; a < 3; a++) chain_[3 * (i + L) + a] = tb2_[3 * cb + a];
+    }
+    total += weight * C;
+  }
+  return total / (double)n_ins;
+}
+
 int ForceField::CBMCFChainDeletion(std::vector<Molecule>& mols, std::mt19937& g) {
   const int L = GCChainLen();
   const double qb = gc_[2];
@@ -721,6 +770,7 @@ void Simulation::Sample() {
   std::vector<double> rz(3 * (size_t)bins);
   check(plum_rhoz(force_field.Context(), rz.data(), (int)rz.size(), nullptr));
   for (size_t k = 0; k < rz.size() && k < density_z_cumu.size(); k++) density_z_cumu[k] += rz[k];
+  if (run_.calc_chem_pot) chem_pot_cumu += force_field.CalcChemicalPotentialF(mols, rand_gen);
   if (mols.empty()) return;
   mol_avg_counter++;
   double o[5];
@@ -837,6 +887,15 @@ int plum_sim_write_checkpoint(plum_sim* s, const char* path) {
 int plum_sim_read_checkpoint(plum_sim* s, const char* path) {
   try {
     s->s->ReadCheckpoint(path ? path : "");
+    return PLUM_OK;
+  } catch (const std::exception&) {
+    return PLUM_ERR_INPUT;
+  }
+}
+
+int plum_sim_chem_pot(plum_sim* s, double* out) {
+  try {
+    *out = s->s->force_field.CalcChemicalPotentialF(s->s->mols, s->s->rand_gen);
     return PLUM_OK;
   } catch (const std::exception&) {
     return PLUM_ERR_INPUT;

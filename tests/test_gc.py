@@ -83,3 +83,21 @@ def test_gpu_append_and_erase_keep_energies_exact():
     np.testing.assert_array_equal(s.positions(), pos)
     fresh = pg.System(d)
     np.testing.assert_allclose(s.energies(), fresh.energies(), rtol=1e-12, atol=1e-9)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", GC + ["muvt_neutral", "muvt_charged"])
+def test_gpu_widom_chemical_potential_matches_oracle(built, case):
+    """ForceField::CalcChemicalPotentialF of the host classes (trial energies
+    on the device) against the CPU restatement, which
+    tests/test_oracle_widom.py pins to the reference: three successive
+    averages from the same seed (so the same draws were consumed)."""
+    import plum_gb300 as pg
+    d = os.path.join(HERE, "golden", case)
+    sim = pg.HostSimulation(d, seed=9)
+    o = built.Oracle(d, seed=9)
+    for _ in range(3):
+        a, b = sim.chem_pot(), o.chem_pot()
+        assert abs(a - b) <= 1e-6 * abs(b), (case, a, b)
+    sim.close()
+    o.close()
