@@ -1698,8 +1698,8 @@ long batch_kernels(const plum_batch* b, int steps) {
   return (cells ? (b->cells_on ? 4 : 1) : 0) + chains * (1 + 2L * steps + steps * stage);
 }
 
-// After a batch of steps: a replica whose cell list overflowed doubles every
-// list's entries per cell (and the graph is captured again).
+// After a batch of steps: when a replica's list of beads that changed cell
+// overflowed, every list's capacity doubles (and the graph is captured again).
 int cells_check(plum_batch* b) {
   if (!(b->sg && b->cell_moved && b->cells_on)) return PLUM_OK;
   if (!b->cells_built) {

@@ -318,12 +318,12 @@ __device__ __forceinline__ void pair_sweep(const DevParams& P, const PairConst& 
 // Batched replicas: every replica's pending move contributes pair items
 // (up to kPairGroup moved beads, staged in shared memory at their trial and
 // current positions, x a chunk of other beads, one per thread), one item for
-// the pairs among the moved beads,
-// and k items (one k tile of kKTile32 vectors over all moved beads). Every
-// block derives the same item list from the replicas' states, takes a
-// share of it from a queue, and writes one slot per item: pair items
-// {lj, real}, k items {k-space energy change}. The serial step of each
-// replica adds its slots in item order.
+// the pairs among the moved beads, and k items (one k tile of kKTile32
+// vectors over all moved beads). Every block derives the same item list from
+// the replicas' states and takes items one at a time from a queue; each item
+// writes its own slot: pair items {lj, real}, k items {k-space energy
+// change}. The serial step of each replica adds its slots in item order, so
+// the result does not depend on which block took which item.
 // The item sizes, the grid and the register budget (kMinBlocks resident
 // blocks per SM) are run-time choices (BatchTune, picked by
 // plum_batch_autotune); defaults: 4096 pairs per item, 128-vector k tiles,
