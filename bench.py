@@ -370,6 +370,7 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference_arm(args, rank, world)
+    from plum_gb300 import replicas
 
     import numpy as np
     import torch
@@ -439,7 +440,7 @@ def main():
     R, BS = args.replicas, args.batch_steps
     batch = pg.Batch([make_workload(args.workload, seed=20261203 + r) for r in range(R)],
                      device=local)
-    batch.seed(1000 * rank + 77)
+    batch.seed(replicas.replica_seed(rank))
     sg, sg_meta = None, None
     wpath = os.path.join(ROOT, "plum_gb300", "data", "surrogate_%s.npz" % args.workload)
     if os.path.exists(wpath) and not args.no_surrogate:
@@ -479,12 +480,7 @@ def main():
     torch.cuda.nvtx.range_pop()
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
-    step_ms = statistics.mean(dev_ms)
-    if dist:
-        t = torch.tensor([step_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms = float(t.item())
-    value = world * R * BS / (step_ms / 1e3)
+    value, step_ms = replicas.job_rate(statistics.mean(dev_ms), R * BS, world, dist)
     da = None
     if sg is not None:
         mv, ps, ac = (np.array(batch.da_stats()) - da0).tolist()
@@ -504,7 +500,7 @@ def main():
     # FP32 + batched
     nb = pg.Batch([make_workload(args.workload, seed=20261203 + r) for r in range(R)],
                   device=local)
-    nb.seed(1000 * rank + 77)
+    nb.seed(replicas.replica_seed(rank))
     tune_nb = nb.autotune(16)
     nb.set_groups(args.groups)
     for _ in range(2):
@@ -532,7 +528,7 @@ def main():
         def tau_batch(net):
             b = pg.Batch([make_workload(args.workload, seed=20261203 + r) for r in range(TR)],
                          device=local)
-            b.seed(1000 * rank + 77)
+            b.seed(replicas.replica_seed(rank))
             b.set_tune(*tune)
             if net is not None:
                 b.set_surrogate(net)
