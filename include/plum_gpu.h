@@ -170,6 +170,21 @@ int plum_observables(const plum_ctx* ctx, double* out);
  * n_bins). */
 int plum_rhoz(const plum_ctx* ctx, double* out, int cap, int* n_bins);
 
+/* The wall-force pressure sums of slit systems on the current configuration,
+ * one evaluation of ForceField::CalcPressureForceLJELSlit (pressure.cc:404-488):
+ * the z forces between the wall sites (the first `phantom` molecules' first
+ * beads, half per wall) and the beads after them, LJ (PairForce) and Ewald
+ * (PairForceZReal + PairForceZRepl), weighted -1/2, +1/2 and -1 as the
+ * reference weights them, plus half of each system bead's external force
+ * (BeadForceOnWall). out6 = the increments of p_tensor[6..11]: {LJ ions, LJ
+ * polymers, LJ wall-wall, Ewald ions, Ewald polymers, Ewald wall-wall}. The
+ * reference adds the wall-wall terms only on its first evaluation (the walls
+ * do not move); the caller does the accumulating and averaging
+ * (pressure.cc:471-487). The LJ force follows the reference's evident intent:
+ * its PairForce reads an uninitialised local (potential_truncated_lj.cc:95-100).
+ * PLUM_ERR_STATE while a trial move is pending. */
+int plum_pressure_slit(plum_ctx* ctx, double* out6);
+
 /* Configurational-bias trial-site energies of one growth step: for each of
  * n_trials trial positions b1[t] of the grand-canonical species' next bead
  * (and, for a charged species, its trial counterion b2[t]), the energy

@@ -131,6 +131,17 @@ class ForceField {  // force_field.h:22-294 (energy surface)
   // (force_field.cc:1088-1105; the potentials' AdjustEnergyUponMolDeletion).
   void EnergyInitForAddedMolecule(std::vector<Molecule>& mols, int n_added);
   void AdjustEnergyUponMolDeletion(int first, int count);
+  // pressure.cc:404-488: one evaluation of the wall-force pressure of a slit
+  // system on the device (plum_pressure_slit), accumulated into p_tensor as
+  // the reference accumulates it (the wall-wall terms on the first
+  // evaluation only) and averaged over the evaluations.
+  void CalcPressureForceLJELSlit(std::vector<Molecule>& mols);
+  // pressure.cc:490-500: p_tensor[0..5] for systems with walls, else "nan"
+  std::string GetPressure() const;
+  // p_tensor[0..11]: 0-5 the averages GetPressure prints (LJ ions, polymers,
+  // wall-wall; Ewald ions, polymers, wall-wall), 6-11 the accumulators
+  double p_tensor[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  double vp_z = 0;  // evaluations so far
   double ChemPot() const { return gc_[0]; }
   int GCChainLen() const { return (int)gc_[3]; }
   double GCBeadCharge() const { return gc_[2]; }
@@ -169,10 +180,13 @@ class Simulation {  // simulation.h:20-201 (step loop and observables)
   // then GCMove or TranslationalMove; last_move_type 5 / 6 for an insertion
   // / deletion attempt, last_accept when the molecule count changed.
   void Step();
-  // simulation.cc:723-798: energies, density, rho(z), Widom's chemical
+  // simulation.cc:723-798: energies, density, rho(z), the wall-force
+  // pressure of systems with walls every 10 samples, Widom's chemical
   // potential when run.in asks for it, Rg (x, y, z rounded to six significant
-  // digits as the reference's string round trip does), end to end distance;
-  // no pressure
+  // digits as the reference's string round trip does), end to end distance.
+  // Without walls the reference evaluates CalcPressureVolScalingHSELSlit
+  // there, whose results are never printed (GetPressure prints "nan"); it is
+  // not evaluated here.
   void Sample();
   double RadiusOfGyration();  // simulation.cc:406-434
   double EndToEndDistance();  // simulation.cc:483-501

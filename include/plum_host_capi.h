@@ -58,6 +58,10 @@ int plum_sim_run(plum_sim* sim);
 /* ForceField::CalcChemicalPotentialF on the current configuration with the
  * simulation's generator (Widom average of 50 test insertions). */
 int plum_sim_chem_pot(plum_sim* sim, double* out);
+/* ForceField::p_tensor[0..11] and the number of pressure evaluations so far
+ * (out13[12]); with eval != 0 one more evaluation of
+ * CalcPressureForceLJELSlit on the current configuration first. */
+int plum_sim_pressure(plum_sim* sim, int eval, double* out13);
 int plum_sim_finish(plum_sim* sim);
 
 #ifdef __cplusplus

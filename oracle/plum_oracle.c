@@ -1717,6 +1717,33 @@ void po_ewald_force_z(const po_ctx* c, int a, int b, double* out2) {
   out2[1] = ew_force_z_repl(c, c->x + 3 * a, c->q[a], c->x + 3 * b, c->q[b]);
 }
 
+/* The oracle's configuration and parameters of the wall-force pressure, for
+ * harnesses that run another implementation of it on the same inputs. */
+void po_slit_inputs(const po_ctx* c, double* scal, double* per_type, int* type, double* q,
+                    int* mol_start, double* kv, double* kw) {
+  if (scal) {
+    double v[26] = {c->box[0], c->box[1], c->box[2], c->ebox[0], c->ebox[1], c->ebox[2],
+                    c->npbc, c->phantom, c->use_pair, c->use_ewald, c->use_ext,
+                    c->pair_kind, c->ext_kind, c->lj_cut, c->lB, c->alpha, c->real_cut,
+                    c->real_cell[0], c->real_cell[1], c->real_cell[2], c->evol,
+                    c->wall_cut, c->n_type, c->n_k, c->n_bead, c->n_mol};
+    memcpy(scal, v, sizeof v);
+  }
+  if (per_type)
+    for (int t = 0; t < c->n_type; t++) {
+      per_type[5 * t] = c->lj_sig[t];
+      per_type[5 * t + 1] = c->lj_eps[t];
+      per_type[5 * t + 2] = c->wall_sig[t];
+      per_type[5 * t + 3] = c->wall_eps[t];
+      per_type[5 * t + 4] = c->graft[t];
+    }
+  if (type) memcpy(type, c->type, sizeof(int) * (size_t)c->n_bead);
+  if (q) memcpy(q, c->q, sizeof(double) * (size_t)c->n_bead);
+  if (mol_start) memcpy(mol_start, c->mol_start, sizeof(int) * (size_t)(c->n_mol + 1));
+  if (kv) memcpy(kv, c->kv, sizeof(double) * 3 * (size_t)c->n_k);
+  if (kw) memcpy(kw, c->kw, sizeof(double) * (size_t)c->n_k);
+}
+
 /* ForceField::CalcPressureForceLJELSlit (pressure.cc:400-488) on the current
  * configuration: wall sites (the first phantom molecules, half on each wall)
  * against the system, plus the 9-3 wall forces; out12 = p_tensor[0..11]

@@ -83,6 +83,17 @@ int po_rhoz(const po_ctx* c, double* out, int cap);
  * chain[cl*3] (and counterions chain_ci); delete_id = -1 for insertion. */
 double po_beads_energy(po_ctx* c, const double* b1, const double* b2, int cl,
                        const double* chain, const double* chain_ci, int delete_id);
+/* ForceField::CalcPressureForceLJELSlit (pressure.cc:404-488) on the current
+ * configuration: out12 = p_tensor[0..11] after this evaluation (6-11 the
+ * accumulators: LJ ion, polymer, wall-wall; Ewald ion, polymer, wall-wall). */
+void po_pressure_force_slit(po_ctx* c, double* out12);
+/* Its inputs: scal = {box[3], ebox[3], npbc, phantom, use_pair, use_ewald,
+ * use_ext, pair_kind, ext_kind, lj_cut, lB, alpha, real_cut, real_cell[3],
+ * evol, wall_cut, n_type, n_k, n_bead, n_mol} (26 values); per_type[5 n_type] =
+ * {lj sigma, lj epsilon, wall sigma, wall epsilon, graft} per type; type,
+ * q [n_bead]; mol_start [n_mol + 1]; kv [3 n_k], kw [n_k]. NULL skips one. */
+void po_slit_inputs(const po_ctx* c, double* scal, double* per_type, int* type, double* q,
+                    int* mol_start, double* kv, double* kw);
 /* First n outputs of an mt19937 seeded with `seed`. */
 void po_mt19937(uint32_t seed, long n, uint32_t* out);
 

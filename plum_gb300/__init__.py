@@ -68,6 +68,7 @@ def lib():
         L.plum_set_positions.argtypes = [C.c_void_p, _dp]
         L.plum_observables.argtypes = [C.c_void_p, _dp]
         L.plum_rhoz.argtypes = [C.c_void_p, _dp, C.c_int, C.POINTER(C.c_int)]
+        L.plum_pressure_slit.argtypes = [C.c_void_p, _dp]
         L.plum_get_topology.argtypes = [C.c_void_p, _ip, _dp, _ip]
         L.plum_last_timing.argtypes = [C.c_void_p, C.POINTER(C.c_double),
                                        C.POINTER(C.c_long)]
@@ -104,6 +105,7 @@ def lib():
         L.plum_sim_enable_output.argtypes = [C.c_void_p, C.c_char_p]
         L.plum_sim_run.argtypes = [C.c_void_p]
         L.plum_sim_chem_pot.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.plum_sim_pressure.argtypes = [C.c_void_p, C.c_int, _dp]
         L.plum_sim_finish.argtypes = [C.c_void_p]
         L.plum_sim_write_checkpoint.argtypes = [C.c_void_p, C.c_char_p]
         L.plum_sim_read_checkpoint.argtypes = [C.c_void_p, C.c_char_p]
@@ -263,6 +265,14 @@ class System:
     def observables(self):
         o = np.zeros(5)
         _check(lib().plum_observables(self.h, o))
+        return o
+
+    def pressure_slit(self):
+        """One evaluation of the wall-force pressure sums of a slit system:
+        the increments of p_tensor[6..11] (LJ ions, polymers, wall-wall;
+        Ewald ions, polymers, wall-wall)."""
+        o = np.zeros(6)
+        _check(lib().plum_pressure_slit(self.h, o))
         return o
 
     def rhoz(self):
@@ -590,6 +600,13 @@ class HostSimulation:
         v = C.c_double(0)
         _check(lib().plum_sim_chem_pot(self.h, C.byref(v)))
         return v.value
+
+    def pressure(self, evaluate=False):
+        """(p_tensor[0..11], evaluations so far) of the host ForceField; with
+        evaluate one more CalcPressureForceLJELSlit first."""
+        o = np.zeros(13)
+        _check(lib().plum_sim_pressure(self.h, int(bool(evaluate)), o))
+        return o[:12], int(o[12])
 
     def run(self):
         """The steps of run.in (Simulation::Run): samples and writes where

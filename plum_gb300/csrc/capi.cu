@@ -10,6 +10,7 @@
 
 #include "../../include/plum_gpu.h"
 #include "engine.h"
+#include "slit_pressure.h"
 #include "host/input.h"
 #include "mlp.h"
 #include "surrogate.h"
@@ -59,6 +60,8 @@ struct plum_ctx {
   int n_tot_part = 0;
   double* d_out = nullptr;     // small result block
   double* d_obs_per = nullptr;  // [n_mol * 5] per-molecule Rg / Ree sums
+  double* d_press = nullptr;    // wall-force pressure partials and sums
+  int press_cap = 0;
   unsigned* d_rhoz = nullptr;   // [3 * rhoz_bins] rho(z) counts
   int rhoz_bins = 0;
   // surrogate training data: descriptor accumulator and device copies of
@@ -650,7 +653,8 @@ int plum_ctx_destroy(plum_ctx* c) {
                   c->B.fq,       c->B.ftrial,  c->B.dsk_part32, c->cb_b, c->cb_c, c->cb_so,
                   c->cb_part,    c->cb_u,      c->d_obs_per, c->d_rhoz, c->desc_acc,
                   c->d_rp1,      c->d_rb1,     c->desc_fine, c->cb_part32, c->cb_ticket,
-                  c->d_stream,   c->d_mt,      c->d_log_type, c->d_log_acc, c->d_log_e};
+                  c->d_stream,   c->d_mt,      c->d_log_type, c->d_log_acc, c->d_log_e,
+                  c->d_press};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_out) cudaFreeHost(c->h_out);
@@ -1252,6 +1256,66 @@ int plum_rhoz(const plum_ctx* cc, double* out, int cap, int* n_bins) {
   const double w = 1.0 / (c->in.box[0] * c->in.box[1] * kRhoZRes);
   const int n = std::min(cap, 3 * nb);
   for (int i = 0; i < n; i++) out[i] = cnt[i] * w;
+  return PLUM_OK;
+}
+
+int plum_pressure_slit(plum_ctx* c, double* out6) {
+  if (!c || !out6) return fail(PLUM_ERR_INPUT, "null argument");
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
+  cudaSetDevice(c->device);
+  const Input& in = c->in;
+  const DevParams& P = c->P;
+  SlitPressParams S{};
+  S.n_bead = P.n_bead;
+  S.n_mol = P.n_mol;
+  S.phantom = P.phantom;
+  S.npbc = P.npbc;
+  S.n_type = P.n_type;
+  S.use_pair = in.use_pair;
+  S.use_ewald = in.use_ewald;
+  S.use_ext = in.use_ext;
+  S.pair_kind = in.pair_kind;
+  S.ext_kind = in.ext_kind;
+  for (int a = 0; a < 3; a++) {
+    S.box[a] = in.box[a];
+    S.ebox[a] = P.ebox[a];
+    S.real_cell[a] = P.real_cell[a];
+  }
+  S.lj_cut = in.lj_cut;
+  S.lB = in.lB;
+  S.alpha = in.alpha;
+  S.real_cut = P.real_cut;
+  S.evol = P.ebox[0] * P.ebox[1] * P.ebox[2];
+  S.wall_cut = in.wall_cut;
+  for (int t = 0; t < P.n_type && t < kSlitMaxTypes; t++) {
+    auto il = in.lj.find(in.type_names[t]);
+    S.lj_sig[t] = il != in.lj.end() ? il->second.sigma : 0.0;
+    S.lj_eps[t] = il != in.lj.end() ? il->second.epsilon : 0.0;
+    S.wall_sig[t] = P.wall_sig[t];
+    S.wall_eps[t] = P.wall_eps[t];
+    S.graft[t] = P.graft[t];
+  }
+  if (S.phantom < 0 || S.phantom > S.n_mol) return fail(PLUM_ERR_INPUT, "bad number of wall sites");
+  const int* ms = in.mol_start.data();
+  const long long n_pair = slit_pair_items(S, ms);
+  const long long n_wall = slit_wall_items(S, ms);
+  const int n_k = (S.use_ewald && S.phantom > 0) ? P.n_k : 0;
+  int n1 = 0, n2 = 0;
+  const int need = slit_partials_count(n_pair + n_wall, n_k, &n1, &n2);
+  if (need > c->press_cap) {
+    if (c->d_press) cudaFree(c->d_press);
+    c->d_press = nullptr;
+    c->press_cap = 0;
+    if (dalloc(&c->d_press, need)) return PLUM_ERR_CUDA;
+    c->press_cap = need;
+  }
+  launch_slit_pressure(S, c->B, n_pair, n_wall, ms[S.phantom], n_k, P.kunit, c->d_press, n1, n2,
+                       c->s);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(c->h_out, c->d_press + 6 * (size_t)n1 + 3 * (size_t)n2, sizeof(double) * 6,
+                     cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  std::memcpy(out6, c->h_out, sizeof(double) * 6);
   return PLUM_OK;
 }
 

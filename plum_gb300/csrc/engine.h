@@ -183,6 +183,16 @@ struct DevBuffers {  // all pointers: copied word-wise into shared memory by the
   int4* cell_extra;  // [cell_cap]
 };
 
+// Wall-force pressure of slit systems (kern_pressure.cu, slit_pressure.h):
+// partial-sum block counts for n_items pair + wall items and n_k k vectors
+// (returns the scratch doubles needed), and the three launches; the six sums
+// land at scratch[6 n1 + 3 n2 ..].
+struct SlitPressParams;
+int slit_partials_count(long long n_items, int n_k, int* n1, int* n2);
+void launch_slit_pressure(const SlitPressParams& S, const DevBuffers& B, long long n_pair,
+                          long long n_wall, int wall_b0, int n_k, const double* kunit,
+                          double* scratch, int n1, int n2, cudaStream_t s);
+
 // Launch helpers (kern_energy.cu / kern_moves.cu). All enqueue on `s`.
 int pair_grid();
 int ktile_count(const DevParams& P);

@@ -4,9 +4,12 @@
 // is the reference's: the same ostream insertions and precisions, including
 // the precision each stream keeps from its previous setprecision.
 //
-// Not built: the pressure (CalcPressure*, pressure.cc). The stat file's
-// pressure column is the reference's "nan" for systems without walls; with
-// walls it holds six "nan" where the reference prints its pressure tensor.
+// The stat file's pressure columns are ForceField::GetPressure's: the
+// wall-force pressure tensor for systems with walls, "nan" without. The
+// reference's LJ columns there come from its PairForce, which reads an
+// uninitialised local (potential_truncated_lj.cc:95-100); these follow the
+// function's evident intent, so those three columns can differ from the
+// reference's own files.
 #include <cmath>
 #include <cstdint>
 #include <fstream>
@@ -85,11 +88,7 @@ void Simulation::PrintStat() {
   info_out << " " << tot_energy;
   if (run_.use_gc)
     info_out << " " << (int)mols.size() << " " << std::setprecision(4) << density_cumu / n;
-  // ForceField::GetPressure (pressure.cc:490-500)
-  if (run_.use_ext)
-    info_out << " " << "nan nan nan nan nan nan";
-  else
-    info_out << " " << "nan";
+  info_out << " " << force_field.GetPressure();
   if (run_.calc_chem_pot) {
     if (chem_pot_cumu / n > 0)
       info_out << " " << -(1.0 / run_.beta) * std::log(chem_pot_cumu / n);
@@ -256,7 +255,7 @@ template <typename T>
 void get(std::istream& i, T& v) {
   i.read(reinterpret_cast<char*>(&v), sizeof(T));
 }
-constexpr uint32_t kCkptMagic = 0x4b43504cu;  // "LPCK"
+constexpr uint32_t kCkptMagic = 0x3243504cu;  // "LPC2"
 
 }  // namespace
 
@@ -283,6 +282,9 @@ void Simulation::WriteCheckpoint(const std::string& path) {
   put(o, (uint64_t)density_z_cumu.size());
   o.write(reinterpret_cast<const char*>(density_z_cumu.data()),
           (std::streamsize)(sizeof(double) * density_z_cumu.size()));
+  put(o, chem_pot_cumu);
+  put(o, force_field.vp_z);
+  for (double v : force_field.p_tensor) put(o, v);
   const long n = plum_ctx_snapshot_size(force_field.Context());
   std::vector<char> snap((size_t)n);
   if (plum_ctx_save(force_field.Context(), snap.data(), n))
@@ -326,6 +328,9 @@ void Simulation::ReadCheckpoint(const std::string& path) {
   get(i, len);
   if (len != density_z_cumu.size()) throw InputError(path + " belongs to another box");
   i.read(reinterpret_cast<char*>(density_z_cumu.data()), (std::streamsize)(sizeof(double) * len));
+  get(i, chem_pot_cumu);
+  get(i, force_field.vp_z);
+  for (double& v : force_field.p_tensor) get(i, v);
   get(i, len);
   std::vector<char> snap(len);
   i.read(snap.data(), (std::streamsize)len);

@@ -458,6 +458,41 @@ double ForceField::CalcChemicalPotentialF(std::vector<Molecule>& mols, std::mt19
   return total / (double)n_ins;
 }
 
+void ForceField::CalcPressureForceLJELSlit(std::vector<Molecule>& /*mols*/) {
+  double d[6];
+  check(plum_pressure_slit(ctx_, d));
+  vp_z += 1;
+  double* p = p_tensor;
+  p[6] += d[0];
+  p[7] += d[1];
+  p[9] += d[3];
+  p[10] += d[4];
+  // the walls are fixed: their mutual force counts once (pressure.cc:438, 451)
+  if (vp_z == 1) {
+    p[8] += d[2];
+    p[11] += d[5];
+  }
+  const double area = info_.box[0] * info_.box[1];
+  if (vp_z == 1) {
+    p[2] = p[8] / area;
+    p[5] = p[11] / area;
+  }
+  p[0] = p[6] / (vp_z * area);
+  p[1] = p[7] / (vp_z * area);
+  p[3] = p[9] / (vp_z * area);
+  p[4] = p[10] / (vp_z * area);
+}
+
+std::string ForceField::GetPressure() const {
+  std::ostringstream foo;
+  if (run_.use_ext)
+    foo << p_tensor[0] << " " << p_tensor[1] << " " << p_tensor[2] << " " << p_tensor[3] << " "
+        << p_tensor[4] << " " << p_tensor[5];
+  else
+    foo << "nan";
+  return foo.str();
+}
+
 int ForceField::CBMCFChainDeletion(std::vector<Molecule>& mols, std::mt19937& g) {
   const int L = GCChainLen();
   const double qb = gc_[2];
@@ -770,6 +805,9 @@ void Simulation::Sample() {
   std::vector<double> rz(3 * (size_t)bins);
   check(plum_rhoz(force_field.Context(), rz.data(), (int)rz.size(), nullptr));
   for (size_t k = 0; k < rz.size() && k < density_z_cumu.size(); k++) density_z_cumu[k] += rz[k];
+  // pressure every 10 samples (simulation.cc:756-761)
+  if (run_.use_ext && step % (run_.sample_freq * 10) == 0)
+    force_field.CalcPressureForceLJELSlit(mols);
   if (run_.calc_chem_pot) chem_pot_cumu += force_field.CalcChemicalPotentialF(mols, rand_gen);
   if (mols.empty()) return;
   mol_avg_counter++;
@@ -896,6 +934,17 @@ int plum_sim_read_checkpoint(plum_sim* s, const char* path) {
 int plum_sim_chem_pot(plum_sim* s, double* out) {
   try {
     *out = s->s->force_field.CalcChemicalPotentialF(s->s->mols, s->s->rand_gen);
+    return PLUM_OK;
+  } catch (const std::exception&) {
+    return PLUM_ERR_INPUT;
+  }
+}
+
+int plum_sim_pressure(plum_sim* s, int eval, double* out13) {
+  try {
+    if (eval) s->s->force_field.CalcPressureForceLJELSlit(s->s->mols);
+    for (int k = 0; k < 12; k++) out13[k] = s->s->force_field.p_tensor[k];
+    out13[12] = s->s->force_field.vp_z;
     return PLUM_OK;
   } catch (const std::exception&) {
     return PLUM_ERR_INPUT;

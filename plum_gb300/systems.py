@@ -323,6 +323,7 @@ class BrushSpec:
     height: float = 40.0
     charge_frac: float = 0.5     # probability that a chain bead carries -1
     n_sites: int = 64            # LJ surface sites per wall (phantom molecules)
+    site_charge: float = 0.0     # sites carry +q, -q, +q, ... along each wall
     graft_z: float = 1.0
     wall_cut: float = -1.0       # <0: purely repulsive 9-3 wall
     lj_cutoff: float = 2.5
@@ -368,7 +369,8 @@ def brush_coordinates(spec: BrushSpec, seed: int):
     for w in (0.0, H):
         for i in range(spec.n_sites):
             p = np.array([rng.uniform(0, L), rng.uniform(0, L), w])
-            mol.append(m), sym.append("S"), xyz.append(p), q.append(0.0)
+            mol.append(m), sym.append("S"), xyz.append(p)
+            q.append(spec.site_charge * (1.0 if i % 2 == 0 else -1.0))
             m += 1
     zlo, zhi = spec.min_sep, H - spec.min_sep
     nneg = 0

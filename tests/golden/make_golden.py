@@ -146,6 +146,38 @@ def coarse_rhoz(rz, width=50):
     return rz[:n].reshape(-1, width, 3).mean(axis=1)
 
 
+# the wall-force pressure (pressure.cc:404-488) of a slit with charged wall
+# sites, so that its Ewald columns are not zero: the reference's p_tensor
+# after evaluations at three configurations (the start, then after `steps` and
+# 2 `steps` steps), with those configurations
+PRESSURE_CASE = dict(name="slab_charged_sites", seed=13, run_seed=61, steps=300,
+                     spec=systems.BrushSpec(n_graft=4, chain_len=8, lxy=10.0, height=12.0,
+                                            n_sites=8, wall_cut=2.5, charge_frac=0.6,
+                                            site_charge=0.5))
+
+
+def make_pressure_case(cfg=PRESSURE_CASE):
+    d = os.path.join(HERE, cfg["name"])
+    if os.path.isdir(d):
+        shutil.rmtree(d)
+    systems.write_brush(d, cfg["spec"], seed=cfg["seed"])
+    R = ob.Ref(d, seed=cfg["run_seed"])
+    coords, pt = [], []
+    for k in range(3):
+        if k:
+            R.run(cfg["steps"])
+        coords.append(R.coords())
+        pt.append(R.pressure_force_slit())
+    R.close()
+    for f in os.listdir(d):
+        if f not in ("run.in", "input_crd.dat", "input_top.dat"):
+            os.remove(os.path.join(d, f))
+    np.savez_compressed(os.path.join(d, "pressure.npz"), coords=np.array(coords),
+                        p_tensor=np.array(pt), steps=np.array(cfg["steps"]),
+                        run_seed=np.array(cfg["run_seed"]))
+    print(cfg["name"], "p_tensor[9:12]", np.array(pt)[:, 9:12])
+
+
 LONG_CASES = {"bulk_small": 2024, "slab_wca": 2025}
 
 
@@ -425,3 +457,5 @@ if __name__ == "__main__":
         make_gc_cases()
     if "outputs" in which:
         make_output_cases()
+    if "pressure" in which:
+        make_pressure_case()

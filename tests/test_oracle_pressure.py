@@ -20,7 +20,7 @@ import numpy as np
 import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SLAB = ["slab_wca", "slab_lj", "slab_hardwall", "slab_wellwall"]
+SLAB = ["slab_wca", "slab_lj", "slab_hardwall", "slab_wellwall", "slab_charged_sites"]
 
 
 def _pair(case, built):
@@ -63,7 +63,7 @@ def test_ewald_z_forces_match_reference(built, case):
     O.close()
 
 
-@pytest.mark.parametrize("case", ["slab_wca", "slab_lj"])
+@pytest.mark.parametrize("case", ["slab_wca", "slab_lj", "slab_charged_sites"])
 def test_electrostatic_pressure_columns_match_reference(built, case):
     R, O = _pair(case, built)
     for _ in range(2):
