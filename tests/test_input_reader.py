@@ -1,0 +1,76 @@
+"""The library's readers of run.in and the coordinate / topology files
+(plum_gb300/csrc/host/input.cc; the C ABI builds every device context from
+them) against the oracle's on every case directory: counts, box, switches,
+per-bead potential parameters, charges, coordinates and molecule boundaries
+must be identical (tests/input_reader_harness.cc). Malformed input is an
+error with a message, where the reference would exit or read forever
+(potential_truncated_lj.cc:31-35)."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+GOLDEN = os.path.join(HERE, "golden")
+DIRS = sorted(d for d in os.listdir(GOLDEN)
+              if os.path.isfile(os.path.join(GOLDEN, d, "input_crd.dat")))
+
+
+@pytest.fixture(scope="module")
+def harness(built, tmp_path_factory):
+    exe = str(tmp_path_factory.mktemp("reader") / "input_reader_harness")
+    lib = os.path.join(ROOT, "oracle", "_ref")
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-o", exe,
+                        os.path.join(HERE, "input_reader_harness.cc"),
+                        os.path.join(ROOT, "plum_gb300", "csrc", "host", "input.cc"),
+                        "-L" + lib, "-loracle", "-Wl,-rpath," + lib], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_every_case_directory_is_covered():
+    assert len(DIRS) >= 14
+    assert {"bulk_small", "slab_lj", "muvt_charged", "slab_charged_sites"} <= set(DIRS)
+
+
+@pytest.mark.parametrize("case", DIRS)
+def test_library_reader_matches_oracle(harness, case):
+    out = subprocess.run([harness, os.path.join(GOLDEN, case)], capture_output=True, text=True,
+                         timeout=120)
+    assert out.returncode == 0 and out.stdout.startswith("ok"), out.stdout + out.stderr
+
+
+def _copy_case(case, dst):
+    for f in ("run.in", "input_crd.dat", "input_top.dat"):
+        shutil.copy(os.path.join(GOLDEN, case, f), dst / f)
+    return (dst / "run.in").read_text().splitlines()
+
+
+def test_table_without_end_is_an_error(harness, tmp_path):
+    lines = _copy_case("bulk_small", tmp_path)
+    ends = [i for i, ln in enumerate(lines) if ln.split()[-1:] == ["end"]]
+    assert ends
+    (tmp_path / "run.in").write_text("\n".join(lines[:ends[0]]) + "\n")
+    out = subprocess.run([harness, str(tmp_path), "library"], capture_output=True, text=True,
+                         timeout=60)
+    assert out.returncode == 1 and "library reader:" in out.stdout, out.stdout
+
+
+def test_missing_coordinate_file_is_an_error(harness, tmp_path):
+    _copy_case("bulk_small", tmp_path)
+    os.remove(tmp_path / "input_crd.dat")
+    out = subprocess.run([harness, str(tmp_path), "library"], capture_output=True, text=True,
+                         timeout=60)
+    assert out.returncode == 1 and "input_crd.dat" in out.stdout, out.stdout
+
+
+def test_truncated_coordinates_are_an_error(harness, tmp_path):
+    _copy_case("bulk_small", tmp_path)
+    rows = (tmp_path / "input_crd.dat").read_text().splitlines()
+    (tmp_path / "input_crd.dat").write_text("\n".join(rows[:len(rows) // 2]) + "\n")
+    out = subprocess.run([harness, str(tmp_path), "library"], capture_output=True, text=True,
+                         timeout=60)
+    assert out.returncode == 1, out.stdout
