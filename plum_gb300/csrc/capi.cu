@@ -11,6 +11,7 @@
 #include "../../include/plum_gpu.h"
 #include "engine.h"
 #include "slit_pressure.h"
+#include "host/ewald_setup.h"
 #include "host/input.h"
 #include "mlp.h"
 #include "surrogate.h"
@@ -41,7 +42,6 @@ namespace {
       return fail(PLUM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
-constexpr double kEwaldCut = 1e-7;   // utilities/constants.h:11
 constexpr double k216 = 1.12246204831;  // utilities/constants.h:62
 
 }  // namespace
@@ -114,51 +114,28 @@ namespace {
 int setup_ewald(plum_ctx* c, std::vector<short4>* kn, std::vector<double>* kw) {
   Input& in = c->in;
   DevParams& P = c->P;
-  double ebox[3] = {in.box[0], in.box[1], in.box[2]};
-  if (in.dipole) {
-    double min_padding = 150;
-    if (ebox[2] * 3 > min_padding)
-      ebox[2] = ebox[2] * 3;
-    else
-      ebox[2] += min_padding;
-  }
-  const double vol = ebox[0] * ebox[1] * ebox[2];
-  double rc = 1;
-  while (0.5 * in.lB * 1 * 1 * std::erfc(std::sqrt(in.alpha) * rc) / rc > kEwaldCut) rc += 1;
-  if (in.x_real_cutoff > 0) rc = in.x_real_cutoff;
-  double kc2 = in.alpha;
-  const double min_box_vol = std::pow(ebox[0], 3);
-  while (in.lB * 1 * 1 / (2 * kPiRef * min_box_vol) * (4 * kPiRef * kPiRef) *
-             std::exp(-kc2 / (4 * in.alpha)) / kc2 >
-         kEwaldCut)
-    kc2 += in.alpha;
-  int kcell[3];
-  for (int a = 0; a < 3; a++) kcell[a] = (int)std::ceil(std::sqrt(kc2) * ebox[a] / (2 * kPiRef));
-  if (in.x_kmax > 0) {
-    for (int a = 0; a < 3; a++) kcell[a] = in.x_kmax;
-    if (!in.x_have_kcut2) kc2 = INFINITY;
-  }
-  if (in.x_have_kcut2) kc2 = in.x_kcut2 > 0 ? in.x_kcut2 : INFINITY;
+  EwaldSetup E;
+  std::string err;
+  if (!ewald_setup(in, kMaxKmax, &E, &err)) return fail(PLUM_ERR_INPUT, err);
+  const double vol = E.vol;
   for (int a = 0; a < 3; a++) {
-    if (kcell[a] > kMaxKmax)
-      return fail(PLUM_ERR_INPUT, "k-space range |n| = " + std::to_string(kcell[a]) +
-                                      " exceeds the supported " + std::to_string(kMaxKmax));
-    P.ebox[a] = ebox[a];
-    P.inv_ebox[a] = 1.0 / ebox[a];
-    P.real_cell[a] = (int)std::ceil(rc / ebox[a]);
-    P.kmax[a] = kcell[a];
-    P.kunit[a] = 2 * kPiRef / ebox[a];
+    P.ebox[a] = E.ebox[a];
+    P.inv_ebox[a] = 1.0 / E.ebox[a];
+    P.real_cell[a] = E.real_cell[a];
+    P.kmax[a] = E.kcell[a];
+    P.kunit[a] = 2 * kPiRef / E.ebox[a];
   }
   P.kper = 0;
   for (int a = 0; a < 3; a++) {
     P.koff[a] = P.kper;
-    P.kper += kcell[a] + 1;
+    P.kper += E.kcell[a] + 1;
   }
   const int row = (int)(P.kper * sizeof(double2));
   P.kchunk_delta = std::max(1, std::min(16, kKTableBytes / (2 * row)));
   P.kchunk_sk = std::max(1, std::min(32, kKTableBytes / row));
+  const double rc = E.real_cut;
   P.real_cut = rc;
-  P.single_image = rc <= 0.5 * ebox[0] && rc <= 0.5 * ebox[1] && rc <= 0.5 * ebox[2];
+  P.single_image = rc <= 0.5 * E.ebox[0] && rc <= 0.5 * E.ebox[1] && rc <= 0.5 * E.ebox[2];
   P.lB = in.lB;
   P.sqrt_alpha = std::sqrt(in.alpha);
   P.kpref = in.lB / (kPiRef * vol) * (4 * kPiRef * kPiRef);
@@ -167,21 +144,12 @@ int setup_ewald(plum_ctx* c, std::vector<short4>* kn, std::vector<double>* kw) {
   P.dipole = in.dipole;
   kn->clear();
   kw->clear();
-  for (int lx = -kcell[0]; lx <= kcell[0]; lx++)
-    for (int ly = -kcell[1]; ly <= kcell[1]; ly++)
-      for (int lz = -kcell[2]; lz <= kcell[2]; lz++) {
-        bool half = lx > 0 || (lx == 0 && ly > 0) || (lx == 0 && ly == 0 && lz > 0);
-        if (!half) continue;
-        double kx = lx * 2 * kPiRef / ebox[0];
-        double ky = ly * 2 * kPiRef / ebox[1];
-        double kz = lz * 2 * kPiRef / ebox[2];
-        double k2 = kx * kx + ky * ky + kz * kz;
-        if (!(k2 > 0 && k2 <= kc2)) continue;
-        kn->push_back(make_short4((short)lx, (short)ly, (short)lz, 0));
-        kw->push_back(std::exp(-k2 / (4 * in.alpha)) / k2);
-      }
+  for (size_t k = 0; k < E.kw.size(); k++) {
+    kn->push_back(make_short4((short)E.kn[3 * k], (short)E.kn[3 * k + 1], (short)E.kn[3 * k + 2], 0));
+    kw->push_back(E.kw[k]);
+  }
   P.n_k = (int)kn->size();
-  c->in.x_kcut2 = kc2;  // effective k^2 cut-off, reported by plum_ctx_info
+  c->in.x_kcut2 = E.kc2;  // effective k^2 cut-off, reported by plum_ctx_info
   return PLUM_OK;
 }
 

@@ -2,11 +2,13 @@
 // coordinate / topology readers (plum_gb300/csrc/host/input.cc, the host code
 // the C ABI builds its device context from) and with the oracle's, and
 // compares what both hold: counts, box, switches, potential parameters per
-// bead, charges, coordinates and molecule boundaries.
+// bead, charges, coordinates and molecule boundaries; then the library's
+// Ewald set-up (host/ewald_setup.cc) against the oracle's: Ewald box,
+// cut-offs, image and k cells, and the k-set with its weights, exactly.
 //
 //   input_reader_harness <case dir> [library]
 //
-// Prints "ok <n_bead> <n_mol>" and exits 0 when everything agrees, else
+// Prints "ok <n_bead> <n_mol> <k vectors checked>" and exits 0 when everything agrees, else
 // prints the first difference and exits 1. With "library" only the library's
 // reader runs (for malformed inputs, which the reference may read forever).
 #include <cmath>
@@ -15,6 +17,7 @@
 #include <vector>
 
 #include "../oracle/plum_oracle.h"
+#include "../plum_gb300/csrc/host/ewald_setup.h"
 #include "../plum_gb300/csrc/host/input.h"
 
 static int bad(const char* what, double a, double b) {
@@ -83,7 +86,37 @@ int main(int argc, char** argv) {
     if (in.use_ext && in.ext_kind == 0 && we != o[3]) return bad("wall epsilon", we, o[3]);
     if (g != o[4]) return bad("graft", g, o[4]);
   }
-  std::printf("ok %d %d\n", nb, in.n_mol);
+  int n_k_checked = 0;
+  if (in.use_ewald) {
+    plum::EwaldSetup E;
+    if (!plum::ewald_setup(in, 1 << 20, &E, &err)) {
+      std::printf("library Ewald set-up: %s\n", err.c_str());
+      return 1;
+    }
+    double ei[15];
+    po_ewald_info(c, ei);
+    if (E.real_cut != ei[0]) return bad("real_cut", E.real_cut, ei[0]);
+    if (E.kc2 != ei[1]) return bad("kc2", E.kc2, ei[1]);
+    for (int a = 0; a < 3; a++) {
+      if (E.real_cell[a] != ei[2 + a]) return bad("real_cell", E.real_cell[a], ei[2 + a]);
+      if (E.kcell[a] != ei[5 + a]) return bad("k cells", E.kcell[a], ei[5 + a]);
+      if (E.ebox[a] != ei[8 + a]) return bad("Ewald box", E.ebox[a], ei[8 + a]);
+    }
+    if (E.vol != ei[13]) return bad("Ewald volume", E.vol, ei[13]);
+    const int n_k = po_n_kvec(c);
+    if ((int)E.kw.size() != n_k) return bad("n_k", (double)E.kw.size(), n_k);
+    std::vector<double> kv(3 * (size_t)n_k + 3), kw(n_k + 1);
+    po_slit_inputs(c, nullptr, nullptr, nullptr, nullptr, nullptr, kv.data(), kw.data());
+    for (int k = 0; k < n_k; k++) {
+      for (int a = 0; a < 3; a++) {
+        const double kk = E.kn[3 * k + a] * 2 * 3.14159265359 / E.ebox[a];
+        if (kk != kv[3 * k + a]) return bad("k vector", kk, kv[3 * k + a]);
+      }
+      if (E.kw[k] != kw[k]) return bad("k weight", E.kw[k], kw[k]);
+    }
+    n_k_checked = n_k;
+  }
+  std::printf("ok %d %d %d\n", nb, in.n_mol, n_k_checked);
   po_destroy(c);
   return 0;
 }

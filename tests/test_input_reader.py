@@ -1,10 +1,10 @@
 """The library's readers of run.in and the coordinate / topology files
 (plum_gb300/csrc/host/input.cc; the C ABI builds every device context from
-them) against the oracle's on every case directory: counts, box, switches,
-per-bead potential parameters, charges, coordinates and molecule boundaries
-must be identical (tests/input_reader_harness.cc). Malformed input is an
-error with a message, where the reference would exit or read forever
-(potential_truncated_lj.cc:31-35)."""
+them) and its Ewald set-up (host/ewald_setup.cc: Ewald box, cut-offs, cells,
+the k-set and its weights) against the oracle's on every case directory:
+everything must be identical (tests/input_reader_harness.cc). Malformed
+input is an error with a message, where the reference would exit or read
+forever (potential_truncated_lj.cc:31-35)."""
 import os
 import shutil
 import subprocess
@@ -25,6 +25,7 @@ def harness(built, tmp_path_factory):
     r = subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-o", exe,
                         os.path.join(HERE, "input_reader_harness.cc"),
                         os.path.join(ROOT, "plum_gb300", "csrc", "host", "input.cc"),
+                        os.path.join(ROOT, "plum_gb300", "csrc", "host", "ewald_setup.cc"),
                         "-L" + lib, "-loracle", "-Wl,-rpath," + lib], capture_output=True,
                        text=True)
     assert r.returncode == 0, r.stderr
@@ -41,6 +42,7 @@ def test_library_reader_matches_oracle(harness, case):
     out = subprocess.run([harness, os.path.join(GOLDEN, case)], capture_output=True, text=True,
                          timeout=120)
     assert out.returncode == 0 and out.stdout.startswith("ok"), out.stdout + out.stderr
+    assert int(out.stdout.split()[3]) > 0  # every case has Ewald: its k-set was compared
 
 
 def _copy_case(case, dst):
