@@ -45,6 +45,22 @@ def test_library_reader_matches_oracle(harness, case):
     assert int(out.stdout.split()[3]) > 0  # every case has Ewald: its k-set was compared
 
 
+@pytest.mark.parametrize("workload", ["bulk_1000", "bulk_20000_pinned", "brush"])
+def test_library_reader_matches_oracle_on_generated_workloads(harness, tmp_path, workload):
+    """The generators' workloads at full size: the measured 20,000-bead
+    system (with the trailing plum_* Ewald items), the 1,000-bead one, and a
+    confined brush replica of the batched workload."""
+    from plum_gb300 import systems
+    d = str(tmp_path / workload)
+    if workload == "brush":
+        systems.write_brush(d, systems.brush_ensemble(1, seed=20261203)[0], seed=20261203)
+    else:
+        systems.write_bulk(d, systems.CONFIGS[workload], seed=20261203)
+    out = subprocess.run([harness, d], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0 and out.stdout.startswith("ok"), out.stdout + out.stderr
+    assert int(out.stdout.split()[3]) > 0
+
+
 def _copy_case(case, dst):
     for f in ("run.in", "input_crd.dat", "input_top.dat"):
         shutil.copy(os.path.join(GOLDEN, case, f), dst / f)
