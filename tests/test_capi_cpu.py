@@ -35,3 +35,19 @@ def test_product_does_not_reference_the_oracle():
             if f.endswith((".py", ".cu", ".cc", ".h", ".cuh")):
                 text = open(os.path.join(dp, f)).read()
                 assert "oracle" not in text.replace("the oracle", "").lower() or f == "systems.py", f
+
+
+def test_compute_without_a_gpu_fails_loudly():
+    """No CPU fallback: on a machine without a CUDA device, creating a
+    context is an error (PLUM_ERR_CUDA), not a silent host computation."""
+    import pytest
+    import plum_gb300 as pg
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    with pytest.raises(pg.PlumError) as ei:
+        pg.System(os.path.join(ROOT, "tests", "golden", "bulk_small"))
+    assert ei.value.code == 2
