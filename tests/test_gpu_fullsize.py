@@ -3,9 +3,10 @@
 periodic box of L = 80, r_c = L/2, |n| <= 12 per axis, 7,812 half-space k
 vectors), with tolerances that do not grow with the size:
 
-* the plain FP64 form's total energy and energy changes of trial moves of
-  every kind against the FP64 CPU restatement on the same configuration
-  (1e-9 of the larger energy component);
+* the plain FP64 form's total energy (1e-9) and energy changes of trial
+  moves of every kind (1e-8 of the larger energy component: a chain move
+  sums 2 x 10^6 pair differences, in another order than the restatement's)
+  against the FP64 CPU restatement on the same configuration;
 * the precision form's energy changes against the plain form's on the same
   trial moves (2e-4 of max(1, |dE|, |dE_pair|, |dE_ewald|); over 10^4 moves
   of this workload the largest error measured was 4e-5 of max(1, |dE|));
@@ -92,7 +93,7 @@ def test_energy_changes_match_restatement(oracle, system_dir):
             assert a[0] >= 1e8 and b[0] >= 1e8, (m, want, a, b)
             continue
         finite += 1
-        assert abs(a[0] - want[0]) <= 1e-9 * scale(want), (m, a, want)
+        assert abs(a[0] - want[0]) <= 1e-8 * scale(want), (m, a, want)
         assert abs(b[0] - a[0]) <= 2e-4 * max(scale(a), abs(a[0])), (m, b, a)
     assert finite >= 6
     s64.close()
