@@ -534,9 +534,11 @@ static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out) {
     delete c;
     return fail(PLUM_ERR_CUDA, "cannot select CUDA device " + std::to_string(device));
   }
-  cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking);
-  cudaEventCreate(&c->ev0);
-  cudaEventCreate(&c->ev1);
+  if (cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+    plum_ctx_destroy(c);
+    return fail(PLUM_ERR_CUDA, "cannot create the context's stream and events");
+  }
   DevBuffers& B = c->B;
   std::memset(&B, 0, sizeof(B));
   int rc = 0;
@@ -575,7 +577,11 @@ static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out) {
     plum_ctx_destroy(c);
     return PLUM_ERR_CUDA;
   }
-  cudaMallocHost(&c->h_out, 64 * sizeof(double));
+  if (cudaMallocHost(&c->h_out, 64 * sizeof(double)) != cudaSuccess) {
+    c->h_out = nullptr;
+    plum_ctx_destroy(c);
+    return fail(PLUM_ERR_CUDA, "cannot allocate pinned host memory");
+  }
   c->h_pos.resize(nb);
   for (int i = 0; i < nb; i++)
     c->h_pos[i] = make_double4_32a(in.xyz[3 * i], in.xyz[3 * i + 1], in.xyz[3 * i + 2], in.q[i]);
@@ -1869,12 +1875,14 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
     b->reps.push_back(c);
   }
   cudaSetDevice(device);
-  cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking);
-  cudaStreamCreateWithFlags(&b->s2, cudaStreamNonBlocking);
-  cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming);
-  cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming);
-  cudaEventCreate(&b->ev0);
-  cudaEventCreate(&b->ev1);
+  if (cudaStreamCreateWithFlags(&b->s, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->s2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->join_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess) {
+    plum_batch_destroy(b);
+    return fail(PLUM_ERR_CUDA, "cannot create the batch's streams and events");
+  }
   std::vector<DevParams> hp(n);
   std::vector<DevBuffers> hb(n);
   std::vector<uint32_t*> hst(n), hout(n);
@@ -1969,7 +1977,11 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
   }
   hp = b->h_rp;
   hb = b->h_rb;
-  cudaMallocHost(&b->h_gather, sizeof(long long) * 6 * n);
+  if (cudaMallocHost(&b->h_gather, sizeof(long long) * 6 * n) != cudaSuccess) {
+    b->h_gather = nullptr;
+    plum_batch_destroy(b);
+    return fail(PLUM_ERR_CUDA, "cannot allocate pinned host memory");
+  }
   cudaMemcpy(b->d_rp, hp.data(), sizeof(DevParams) * n, cudaMemcpyHostToDevice);
   cudaMemcpy(b->d_rb, hb.data(), sizeof(DevBuffers) * n, cudaMemcpyHostToDevice);
   cudaMemcpy(b->d_states, hst.data(), sizeof(uint32_t*) * n, cudaMemcpyHostToDevice);

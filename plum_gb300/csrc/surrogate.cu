@@ -94,7 +94,11 @@ int plum_surrogate_create(int device, unsigned long long seed, plum_surrogate** 
     return plum::fail_msg(PLUM_ERR_CUDA, "cannot select the device");
   plum_surrogate* g = new plum_surrogate();
   g->device = device;
-  cudaStreamCreateWithFlags(&g->s, cudaStreamNonBlocking);
+  if (cudaStreamCreateWithFlags(&g->s, cudaStreamNonBlocking) != cudaSuccess) {
+    g->s = nullptr;
+    plum_surrogate_destroy(g);
+    return plum::fail_msg(PLUM_ERR_CUDA, "cannot create the surrogate's stream");
+  }
   int rc = salloc(&g->net, 1) | salloc(&g->param, mlp::kNParam) | salloc(&g->m, mlp::kNParam) |
            salloc(&g->v, mlp::kNParam) | salloc(&g->grad, mlp::kNParam + 1) |
            salloc(&g->d_err, 1) | salloc(&g->d_loss, 1);
