@@ -142,6 +142,15 @@ class ForceField {  // force_field.h:22-294 (energy surface)
   // wall-wall; Ewald ions, polymers, wall-wall), 6-11 the accumulators
   double p_tensor[12] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   double vp_z = 0;  // evaluations so far
+  // gasdev's cached deviate (misc.cc:112-113), for checkpoints
+  void GasdevState(int* iset, double* gset) const {
+    *iset = gd_iset_;
+    *gset = gd_gset_;
+  }
+  void SetGasdevState(int iset, double gset) {
+    gd_iset_ = iset;
+    gd_gset_ = gset;
+  }
   double ChemPot() const { return gc_[0]; }
   int GCChainLen() const { return (int)gc_[3]; }
   double GCBeadCharge() const { return gc_[2]; }
@@ -209,9 +218,12 @@ class Simulation {  // simulation.h:20-201 (step loop and observables)
   void Finish();
   // Exact restart (no reference counterpart): the step count, the
   // generator's state, the counters and running averages, and the device
-  // context's snapshot (plum_ctx_save). ReadCheckpoint on a Simulation built
-  // from the same inputs continues bit-identically. Runs with
-  // grand-canonical exchange (whose molecule list changes) are refused.
+  // context's snapshot (plum_ctx_save); for runs with grand-canonical
+  // exchange also the molecule list, the exchange counters and gasdev's
+  // cached deviate. ReadCheckpoint on a Simulation built from the same
+  // inputs continues bit-identically: it first gives the context the
+  // checkpoint's molecules (the molecules after the longest common prefix
+  // are replaced, as an exchange appends and erases them).
   void WriteCheckpoint(const std::string& path);
   void ReadCheckpoint(const std::string& path);
 

@@ -50,8 +50,8 @@ int plum_sim_energies(plum_sim* sim, double* out);
  * plum_sim_finish makes the writes of the reference's destructor and closes
  * the files. */
 int plum_sim_enable_output(plum_sim* sim, const char* dir);
-/* Simulation::WriteCheckpoint / ReadCheckpoint (exact restart; not for runs
- * with grand-canonical exchange). */
+/* Simulation::WriteCheckpoint / ReadCheckpoint (exact restart, runs with
+ * grand-canonical exchange included). */
 int plum_sim_write_checkpoint(plum_sim* sim, const char* path);
 int plum_sim_read_checkpoint(plum_sim* sim, const char* path);
 int plum_sim_run(plum_sim* sim);

@@ -257,10 +257,86 @@ void get(std::istream& i, T& v) {
 }
 constexpr uint32_t kCkptMagic = 0x3243504cu;  // "LPC2"
 
+void put_str(std::ostream& o, const std::string& v) {
+  put(o, (uint32_t)v.size());
+  o.write(v.data(), (std::streamsize)v.size());
+}
+bool get_str(std::istream& i, std::string* v) {
+  uint32_t n = 0;
+  get(i, n);
+  if (!i || n > 4096) return false;
+  v->assign(n, ' ');
+  i.read(&(*v)[0], (std::streamsize)n);
+  return (bool)i;
+}
+
+// The molecule list of an exchange run: per molecule its beads (symbol, id,
+// chain id, type, charge, position) and bonds.
+void put_mols(std::ostream& o, const std::vector<Molecule>& mols) {
+  put(o, (uint64_t)mols.size());
+  for (const Molecule& m : mols) {
+    put(o, (uint32_t)m.bds.size());
+    for (const Bead& b : m.bds) {
+      put_str(o, b.Symbol());
+      const int iv[3] = {b.ID(), b.ChainID(), b.Type()};
+      const double dv[4] = {b.Charge(), b.GetCrd(0, 0), b.GetCrd(0, 1), b.GetCrd(0, 2)};
+      for (int v : iv) put(o, v);
+      for (double v : dv) put(o, v);
+    }
+    put(o, (uint32_t)m.bonds.size());
+    for (const auto& bd : m.bonds) {
+      put(o, (int32_t)bd[0]);
+      put(o, (int32_t)bd[1]);
+    }
+  }
+}
+
+bool get_mols(std::istream& i, std::vector<Molecule>* mols) {
+  uint64_t n = 0;
+  get(i, n);
+  if (!i || n > (1u << 26)) return false;
+  mols->assign(n, Molecule());
+  for (Molecule& m : *mols) {
+    uint32_t nb = 0;
+    get(i, nb);
+    if (!i || nb > (1u << 26)) return false;
+    for (uint32_t k = 0; k < nb; k++) {
+      std::string sym;
+      if (!get_str(i, &sym)) return false;
+      int iv[3];
+      double dv[4];
+      for (int& v : iv) get(i, v);
+      for (double& v : dv) get(i, v);
+      Bead b(sym, iv[0], iv[1], dv[0], dv[1], dv[2], dv[3]);
+      b.SetType(iv[2]);
+      m.AddBead(b);
+    }
+    uint32_t nbond = 0;
+    get(i, nbond);
+    if (!i || nbond > (1u << 26)) return false;
+    for (uint32_t k = 0; k < nbond; k++) {
+      int32_t a = 0, c = 0;
+      get(i, a);
+      get(i, c);
+      m.AddBond(a, c);
+    }
+  }
+  return (bool)i;
+}
+
+// Same beads (type and charge) in the same order: the structure a context
+// holds for a molecule; positions are the snapshot's.
+bool same_structure(const Molecule& a, const Molecule& b) {
+  if (a.Size() != b.Size()) return false;
+  for (int k = 0; k < a.Size(); k++)
+    if (a.bds[k].Type() != b.bds[k].Type() || a.bds[k].Charge() != b.bds[k].Charge())
+      return false;
+  return true;
+}
+
 }  // namespace
 
 void Simulation::WriteCheckpoint(const std::string& path) {
-  if (force_field.UseGC()) throw InputError("checkpoints of exchange runs are not built");
   std::ofstream o(path, std::ios::binary);
   if (!o) throw InputError("cannot write " + path);
   std::ostringstream g;
@@ -285,6 +361,19 @@ void Simulation::WriteCheckpoint(const std::string& path) {
   put(o, chem_pot_cumu);
   put(o, force_field.vp_z);
   for (double v : force_field.p_tensor) put(o, v);
+  put(o, (int32_t)force_field.UseGC());
+  if (force_field.UseGC()) {
+    const long gc[4] = {insertion_attempted, insertion_accepted, deletion_attempted,
+                        deletion_accepted};
+    for (long v : gc) put(o, v);
+    int iset = 0;
+    double gset = 0;
+    force_field.GasdevState(&iset, &gset);
+    put(o, iset);
+    put(o, gset);
+    SyncFromDevice();
+    put_mols(o, mols);
+  }
   const long n = plum_ctx_snapshot_size(force_field.Context());
   std::vector<char> snap((size_t)n);
   if (plum_ctx_save(force_field.Context(), snap.data(), n))
@@ -295,7 +384,6 @@ void Simulation::WriteCheckpoint(const std::string& path) {
 }
 
 void Simulation::ReadCheckpoint(const std::string& path) {
-  if (force_field.UseGC()) throw InputError("checkpoints of exchange runs are not built");
   std::ifstream i(path, std::ios::binary);
   uint32_t magic = 0;
   get(i, magic);
@@ -331,6 +419,40 @@ void Simulation::ReadCheckpoint(const std::string& path) {
   get(i, chem_pot_cumu);
   get(i, force_field.vp_z);
   for (double& v : force_field.p_tensor) get(i, v);
+  int32_t gc_run = 0;
+  get(i, gc_run);
+  if (!i || gc_run != (int32_t)force_field.UseGC())
+    throw InputError(path + " belongs to another kind of run");
+  if (gc_run) {
+    long gc[4];
+    for (long& v : gc) get(i, v);
+    insertion_attempted = gc[0];
+    insertion_accepted = gc[1];
+    deletion_attempted = gc[2];
+    deletion_accepted = gc[3];
+    int iset = 0;
+    double gset = 0;
+    get(i, iset);
+    get(i, gset);
+    force_field.SetGasdevState(iset, gset);
+    std::vector<Molecule> saved;
+    if (!get_mols(i, &saved)) throw InputError(path + " is truncated");
+    // give the context the checkpoint's molecules: keep the common prefix,
+    // append the checkpoint's tail, then erase the old tail (as GCMove
+    // appends and erases), so the context never holds zero molecules
+    size_t keep = 0;
+    while (keep < mols.size() && keep < saved.size() && same_structure(mols[keep], saved[keep]))
+      keep++;
+    const int old_n = (int)mols.size();
+    const int n_add = (int)(saved.size() - keep);
+    for (size_t m = keep; m < saved.size(); m++) mols.push_back(saved[m]);
+    if (n_add > 0) force_field.EnergyInitForAddedMolecule(mols, n_add);
+    if (old_n > (int)keep) {
+      force_field.AdjustEnergyUponMolDeletion((int)keep, old_n - (int)keep);
+      mols.erase(mols.begin() + keep, mols.begin() + old_n);
+    }
+    for (size_t m = 0; m < keep; m++) mols[m] = saved[m];
+  }
   get(i, len);
   std::vector<char> snap(len);
   i.read(snap.data(), (std::streamsize)len);

@@ -110,3 +110,34 @@ def test_checkpoint_restart_is_exact(tmp_path, form):
     np.testing.assert_array_equal(a.energies(), b.energies())
     a.close()
     b.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["gcx_neutral", "gcx_charged"])
+def test_checkpoint_restart_is_exact_with_exchange(tmp_path, case):
+    """Runs with grand-canonical exchange: 300 steps (insertions and
+    deletions change the molecule list), a checkpoint, 300 more steps. A
+    second Simulation from the same inputs (another seed) reads the
+    checkpoint, which first gives its context the checkpoint's molecules, and
+    runs the same 300 steps: the same molecules, bit-identical positions and
+    energies."""
+    import numpy as np
+    import plum_gb300 as pg
+    d = os.path.join(HERE, "golden", case)
+    a = pg.HostSimulation(d, seed=11)
+    n0 = a.n_bead()
+    a.steps(300)
+    ck = tmp_path / "gc.ckpt"
+    a.write_checkpoint(ck)
+    n_ck = a.n_bead()
+    a.steps(300)
+    b = pg.HostSimulation(d, seed=99)
+    b.read_checkpoint(ck)
+    assert b.n_bead() == n_ck
+    b.steps(300)
+    assert a.n_bead() == b.n_bead()
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    np.testing.assert_array_equal(a.energies(), b.energies())
+    assert n0 > 0
+    a.close()
+    b.close()
