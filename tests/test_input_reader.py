@@ -92,3 +92,38 @@ def test_truncated_coordinates_are_an_error(harness, tmp_path):
     out = subprocess.run([harness, str(tmp_path), "library"], capture_output=True, text=True,
                          timeout=60)
     assert out.returncode == 1, out.stdout
+
+
+def test_readers_are_clean_under_sanitizers(built, tmp_path):
+    """The readers and the Ewald set-up built with AddressSanitizer and
+    UndefinedBehaviorSanitizer: well-formed cases and cut-off or corrupted
+    files end without a sanitizer report (malformed input is an error)."""
+    exe = str(tmp_path / "reader_asan")
+    lib = os.path.join(ROOT, "oracle", "_ref")
+    r = subprocess.run(["g++", "-std=c++17", "-O1", "-g", "-fsanitize=address,undefined",
+                        "-fno-omit-frame-pointer", "-o", exe,
+                        os.path.join(HERE, "input_reader_harness.cc"),
+                        os.path.join(ROOT, "plum_gb300", "csrc", "host", "input.cc"),
+                        os.path.join(ROOT, "plum_gb300", "csrc", "host", "ewald_setup.cc"),
+                        "-L" + lib, "-loracle", "-Wl,-rpath," + lib], capture_output=True,
+                       text=True)
+    if r.returncode != 0:
+        pytest.skip("no sanitizer runtime: " + r.stderr[-200:])
+    env = dict(os.environ, ASAN_OPTIONS="detect_leaks=1", UBSAN_OPTIONS="print_stacktrace=1")
+
+    def run(d, *extra):
+        out = subprocess.run([exe, d, *extra], capture_output=True, text=True, timeout=300,
+                             env=env)
+        assert "Sanitizer" not in out.stderr and "runtime error" not in out.stderr, out.stderr
+        return out
+
+    for case in ("bulk_small", "slab_lj", "muvt_charged"):
+        assert run(os.path.join(GOLDEN, case)).returncode == 0
+    lines = _copy_case("bulk_small", tmp_path)
+    for cut in (3, 20, len(lines) - 3):
+        (tmp_path / "run.in").write_text("\n".join(lines[:cut]) + "\n")
+        assert run(str(tmp_path), "library").returncode == 1
+    (tmp_path / "run.in").write_text("\n".join(lines) + "\n")
+    rows = (tmp_path / "input_crd.dat").read_text().splitlines()
+    (tmp_path / "input_crd.dat").write_text("\n".join(rows[:2] + ["x y z"] + rows[3:]) + "\n")
+    assert run(str(tmp_path), "library").returncode == 1
