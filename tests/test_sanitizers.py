@@ -1,6 +1,6 @@
 """The CPU restatement (oracle/plum_oracle.c) built with AddressSanitizer and
 UndefinedBehaviorSanitizer and driven through tests/slit_pressure_harness.cc:
-reading each case, 500 steps of its Monte Carlo loop (exchange moves in the
+reading each case, 120 steps of its Monte Carlo loop (exchange moves in the
 grand-canonical cases) and two wall-force pressure evaluations end without a
 sanitizer report, so the checker's own memory and arithmetic are sound where
 it is used."""
@@ -35,7 +35,7 @@ def harness(tmp_path_factory):
 
 @pytest.mark.parametrize("case", CASES)
 def test_oracle_is_clean_under_sanitizers(harness, case):
-    out = subprocess.run([harness, os.path.join(HERE, "golden", case), "7", "200", "300"],
+    out = subprocess.run([harness, os.path.join(HERE, "golden", case), "7", "60", "60"],
                          capture_output=True, text=True, timeout=600,
                          env=dict(os.environ, ASAN_OPTIONS="detect_leaks=1"))
     assert out.returncode == 0, out.stderr[-2000:]
