@@ -16,6 +16,13 @@
         batches of 4,096 inside the NVTX range "train" (k_mlp<true>, the
         gradient reduction and Adam), then one inference pass inside "infer".
 
+    python -m plum_gb300.profile_cases pressure [evaluations]
+        the wall-force pressure of one confined brush replica of the batched
+        workload with charged surface sites (64 per wall, +-0.5): after two
+        warm-up evaluations, the given number (default 3) run inside the
+        NVTX range "pressure" (k_slit_pairs, k_slit_recip, k_slit_sum), with
+        their mean wall time printed.
+
 All keep the device footprint under 1 GB so a full-set capture of one to
 three launches ends within a minute or two.
 """
@@ -100,6 +107,31 @@ def training(n=65536, batch=4096):
     print("train ok, mean |s| %.4f" % float(out.abs().mean()), flush=True)
 
 
+def pressure(evaluations=3):
+    import time
+    import torch
+    import plum_gb300 as pg
+    from . import systems
+    spec = systems.brush_ensemble(1, seed=20261203)[0]
+    spec.site_charge = 0.5
+    d = os.path.join(tempfile.gettempdir(), "plum_prof_pressure")
+    if not os.path.exists(os.path.join(d, "run.in")):
+        systems.write_brush(d, spec, seed=20261203)
+    s = pg.System(d)
+    for _ in range(2):
+        s.pressure_slit()
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("pressure")
+    t0 = time.perf_counter()
+    for _ in range(evaluations):
+        out = s.pressure_slit()
+    dt = (time.perf_counter() - t0) / max(1, evaluations)
+    torch.cuda.nvtx.range_pop()
+    print("pressure ok: beads %d, k vectors %d, %.3f ms per evaluation, sums %s"
+          % (s.n_bead, s.info.n_kvec, 1e3 * dt, out), flush=True)
+    s.close()
+
+
 def main(argv=None):
     argv = list(sys.argv[1:] if argv is None else argv)
     what = argv[0] if argv else "da"
@@ -110,9 +142,12 @@ def main(argv=None):
         chosen(int(argv[1]) if len(argv) > 1 else 64)
     elif what == "train":
         training()
+    elif what == "pressure":
+        pressure(int(argv[1]) if len(argv) > 1 else 3)
     else:
         raise SystemExit("usage: python -m plum_gb300.profile_cases "
-                         "{da [workload] [replicas] | chosen [replicas] | train}")
+                         "{da [workload] [replicas] | chosen [replicas] | train | "
+                         "pressure [evaluations]}")
 
 
 if __name__ == "__main__":
