@@ -173,6 +173,17 @@ PLUM_HD double slit_wall_force(const SlitPressParams& S, double z, int ty) {
   return f;
 }
 
+// acc[base + kid] += v with constant indices only, so that a caller's
+// accumulator array can stay in registers.
+PLUM_HD void slit_add(double* acc, int base, int kid, double v) {
+  if (kid == 0)
+    acc[base] += v;
+  else if (kid == 1)
+    acc[base + 1] += v;
+  else
+    acc[base + 2] += v;
+}
+
 // First bead of the pair items and their count: sites x beads from the
 // second wall's first bead on.
 PLUM_HD long long slit_pair_items(const SlitPressParams& S, const int* mol_start) {
@@ -211,7 +222,7 @@ PLUM_HD void slit_pair_item(const SlitPressParams& S, const double* xyzq, const 
       r[a] = a < S.npbc ? slit_wrap(d, S.box[a]) : d;
     }
     const double rr = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-    acc[kid] += C * (r[2] / rr) * slit_lj_force(S, type[b], type[w], rr);
+    slit_add(acc, 0, kid, C * (r[2] / rr) * slit_lj_force(S, type[b], type[w], rr));
   }
   if (S.use_ewald) {
     double r[3];
@@ -219,7 +230,7 @@ PLUM_HD void slit_pair_item(const SlitPressParams& S, const double* xyzq, const 
       const double d = pw[a] - pb[a];
       r[a] = a < S.npbc ? slit_wrap(d, S.ebox[a]) : d;
     }
-    acc[3 + kid] += C * slit_ew_real_z(S, r[0], r[1], r[2], pw[3] * pb[3]);
+    slit_add(acc, 3, kid, C * slit_ew_real_z(S, r[0], r[1], r[2], pw[3] * pb[3]));
   }
 }
 
@@ -229,7 +240,7 @@ PLUM_HD void slit_wall_item(const SlitPressParams& S, const double* xyzq, const 
                             const int* mol_start, int b, double* acc) {
   const int j = slit_mol_of(mol_start, S.n_mol, b);
   const int jid = mol_start[j + 1] - mol_start[j] > 1 ? 1 : 0;
-  acc[jid] += 0.5 * slit_wall_force(S, xyzq[4 * (long long)b + 2], type[b]);
+  slit_add(acc, 0, jid, 0.5 * slit_wall_force(S, xyzq[4 * (long long)b + 2], type[b]));
 }
 
 // Group membership of bead b for the k items, a bit per group:
