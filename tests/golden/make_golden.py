@@ -390,7 +390,18 @@ def make_case(name, cfg, n_de=24):
 # an existing case's inputs, run.in items 4-8 replaced (steps, equilibration
 # steps, sampling / stat / trajectory frequencies).
 OUTPUT_CASES = {"outputs_bulk_small": dict(src="bulk_small", seed=77, steps=3000, steps_eq=1000,
-                                           sample_freq=10, stat_freq=500, traj_freq=1000)}
+                                           sample_freq=10, stat_freq=500, traj_freq=1000),
+                # walls, dipole, grafted chains and charged surface sites: the stat
+                # file carries the wall-force pressure (its LJ columns are
+                # undefined in the reference: PairForce reads an uninitialised
+                # local, potential_truncated_lj.cc:95-100)
+                "outputs_slab_charged_sites": dict(src="slab_charged_sites", seed=61, steps=2000,
+                                                   steps_eq=500, sample_freq=10, stat_freq=500,
+                                                   traj_freq=1000),
+                # grand-canonical exchange of a charged species: the stat file's
+                # molecule count, density and exchange acceptance columns
+                "outputs_gcx_charged": dict(src="gcx_charged", seed=5, steps=1200, steps_eq=200,
+                                            sample_freq=10, stat_freq=400, traj_freq=600)}
 OUTPUT_FILES = ("out_stat.dat", "out_traj_p.xyz", "out_traj_c.xyz", "out_traj_a.xyz",
                 "out_traj_n.xyz", "out_lastcrd.dat", "out_lastcrd.dat2", "out_lasttop.dat",
                 "out_lastrhoZ.dat", "out_lastrhoZ.dat2")
@@ -408,9 +419,11 @@ def output_runin(src_runin, cfg):
     return "\n".join(lines) + "\n"
 
 
-def make_output_cases():
+def make_output_cases(only=None):
     import tempfile
     for name, cfg in OUTPUT_CASES.items():
+        if only and name not in only:
+            continue
         src = os.path.join(HERE, cfg["src"])
         dst = os.path.join(HERE, name)
         os.makedirs(dst, exist_ok=True)
@@ -457,5 +470,8 @@ if __name__ == "__main__":
         make_gc_cases()
     if "outputs" in which:
         make_output_cases()
+    picked = [w.split(":", 1)[1] for w in which if w.startswith("outputs:")]
+    if picked:
+        make_output_cases(picked)
     if "pressure" in which:
         make_pressure_case()
