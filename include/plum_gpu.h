@@ -129,6 +129,17 @@ int plum_finalize(plum_ctx* ctx, int accept);
 int plum_run_moves(plum_ctx* ctx, const uint32_t* stream, long n_stream,
                    int n_moves, int* move_type, int* accept, double* etot,
                    long* draws_used);
+/* plum_run_moves with one more per-step log (host buffer of n_moves, may be
+ * NULL): de[i] = the energy change ForceField::EnergyDifference
+ * (force_field.cc:407-434) gives step i's proposal in the context's form (the
+ * value the Metropolis test of simulation.cc:324-332 uses; >= 1e8 on
+ * overlap), NaN for a step without a move. Two contexts of the same system in
+ * the two forms fed the same stream propose the same moves until their first
+ * differing decision, so their logs compare FP32 with FP64 energy changes
+ * proposal by proposal on the chain's own moves. */
+int plum_run_moves_de(plum_ctx* ctx, const uint32_t* stream, long n_stream,
+                      int n_moves, int* move_type, int* accept, double* etot,
+                      double* de, long* draws_used);
 
 /* Same loop with the mt19937 stream generated on the device from `seed`
  * (std::mt19937 semantics) instead of a host buffer: the throughput path.
@@ -154,6 +165,16 @@ int plum_set_positions(plum_ctx* ctx, const double* xyz);
 long plum_ctx_snapshot_size(const plum_ctx* ctx);
 int plum_ctx_save(const plum_ctx* ctx, void* buf, long size);
 int plum_ctx_load(plum_ctx* ctx, const void* buf, long size);
+
+/* The running Ewald structure factor S(k) = sum_i q_i e^{i k.r_i} over the
+ * half-space k-set (plum_info.n_kvec vectors), with the change of the last
+ * accepted move applied: sk_out[2 k + {0, 1}] = {Re, Im}, kn_out[3 k + a] =
+ * the integer k components (k_a = 2 pi n_a / ewald_box[a]); either may be
+ * NULL, nothing is written without Ewald. The reference keeps no S(k): its
+ * reciprocal energy is a pairwise sum over the same k-set
+ * (potential_ewald_coul.cc:198-225); plum_total_energy rebuilds S(k) from
+ * scratch, so comparing the two checks the incremental updates. */
+int plum_structure_factor(const plum_ctx* ctx, double* sk_out, int* kn_out);
 
 /* out[5] = {Rg^2 averaged over chains, Rg_x^2, Rg_y^2, Rg_z^2, end-to-end^2}
  * of the current configuration. Replaces Simulation::RadiusOfGyration,
@@ -222,8 +243,11 @@ int plum_cbmc_time(plum_ctx* ctx, int n_trials, const double* b1, const double* 
  * cudaFree (which plum_cbmc_trials uses when a larger request grows its
  * buffers) synchronise the whole device. No counterpart in the reference.
  *
- * Same energies as plum_cbmc_trials in the plain form (FP64, whatever the
- * context's form), but every buffer is the caller's and is
+ * The energies are those of plum_cbmc_trials in the plain form: the FP64
+ * kernels run whatever the context's form. They start from the context's
+ * running S(k), which in a precision-form context carries the FP32 drift of
+ * the moves since its last full recompute (none right after plum_ctx_create
+ * or plum_total_energy). Every buffer is the caller's and is
  * in DEVICE memory: d_b1, d_b2 [n_trials*3], d_chain, d_chain_ci
  * [chain_len*3], d_u_out [n_trials]. The call allocates nothing (no
  * cudaMalloc/cudaFree, no host heap): its working memory is one fixed array
@@ -234,11 +258,11 @@ int plum_cbmc_time(plum_ctx* ctx, int n_trials, const double* b1, const double* 
  * writes all the working memory it reads.
  *
  * The first call on each device does a one-time set-up (it looks up the
- * array's device address, with that device current): make a first call on
- * each device before starting any stream capture. All calls share the one
+ * array's device address, with that device current): make that first call
+ * on each device before any stream capture begins. All calls share the one
  * array, so calls that overlap on the GPU (from several threads or contexts
- * on the same device) race; serialise them. The call waits for its results
- * on the context's stream. Errors are returned as codes, with the message
+ * on the same device) race; serialise them. Every call ends by
+ * synchronising the context's stream. Errors are returned as codes, with the message
  * written to err[err_cap] (may be NULL); plum_last_error is not updated. */
 int plum_cbmc_trials_noalloc(plum_ctx* ctx, int n_trials, const double* d_b1,
                              const double* d_b2, int chain_len, const double* d_chain,
@@ -298,8 +322,30 @@ int plum_batch_seed(plum_batch* batch, uint32_t seed);
 /* Seeds replica r's generator with seeds[r]. */
 int plum_batch_seed_each(plum_batch* batch, const uint32_t* seeds);
 /* n_steps moves per replica; *accepted_out = accepted moves summed over
- * replicas. */
+ * replicas. Includes the replicas' full FP64 recomputes that fall due
+ * (plum_batch_set_recompute): their device time is part of
+ * plum_batch_last_timing. */
 int plum_batch_run(plum_batch* batch, int n_steps, long* accepted_out);
+/* Full FP64 recompute cadence of the replicas, in moves per replica (0 =
+ * never; default 10000, as plum_set_recompute for one system): after every
+ * `every` of its moves (at the next boundary of the batch's 32-step graphs)
+ * a replica's totals, S(k) and fixed-point mirror are rebuilt from its FP64
+ * positions, which resets its FP32 drift. The replicas' cadences start at
+ * staggered phases (replica r after r * every / R moves), so each batch of
+ * steps recomputes its share of them. No reference counterpart (the
+ * reference sums exact FP64 changes and never recomputes,
+ * force_field.cc:436-451, 1201-1219). */
+int plum_batch_set_recompute(plum_batch* batch, long every);
+/* Drift found by the recomputes: out[6 * r + q] for replica r = {pair,
+ * ewald, bond, ext running-minus-recomputed at its last recompute, the
+ * largest |total drift| over its recomputes, the number of its recomputes}.
+ * *count (may be NULL) = recomputes in the last plum_batch_run, *ms (may be
+ * NULL) = their device time in milliseconds. */
+int plum_batch_drift(plum_batch* batch, double* out, long* count, double* ms);
+/* Running totals of every replica in one device gather and one copy:
+ * out[4 * r + q] = {pair, ewald, bond, ext} of replica r (plum_energies of
+ * each replica, ForceField::Tot*Energy, force_field.cc:1201-1219). */
+int plum_batch_energies(plum_batch* batch, double* out);
 int plum_batch_size(const plum_batch* batch);
 /* The context of replica r (owned by the batch): energies, positions and
  * observables through the single-system calls above. */

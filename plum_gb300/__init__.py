@@ -62,6 +62,9 @@ def lib():
         L.plum_finalize.argtypes = [C.c_void_p, C.c_int]
         L.plum_run_moves.argtypes = [C.c_void_p, _up, C.c_long, C.c_int, C.c_void_p,
                                      C.c_void_p, C.c_void_p, C.POINTER(C.c_long)]
+        L.plum_run_moves_de.argtypes = [C.c_void_p, _up, C.c_long, C.c_int, C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.POINTER(C.c_long)]
         L.plum_seed.argtypes = [C.c_void_p, C.c_uint32]
         L.plum_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int)]
         L.plum_get_positions.argtypes = [C.c_void_p, _dp]
@@ -135,6 +138,11 @@ def lib():
         L.plum_batch_set_groups.argtypes = [C.c_void_p, C.c_int]
         L.plum_batch_autotune.argtypes = [C.c_void_p, C.c_int, _ip]
         L.plum_batch_da_stats.argtypes = [C.c_void_p, C.POINTER(C.c_long)]
+        L.plum_batch_set_recompute.argtypes = [C.c_void_p, C.c_long]
+        L.plum_structure_factor.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.plum_batch_energies.argtypes = [C.c_void_p, _dp]
+        L.plum_batch_drift.argtypes = [C.c_void_p, _dp, C.POINTER(C.c_long),
+                                       C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -220,6 +228,19 @@ class System:
                                     C.byref(used)))
         return used.value, mt, ac, et
 
+    def run_moves_de(self, stream, n_moves):
+        """run_moves that also logs each step's proposal energy change:
+        (draws used, move types, accept flags, totals, dE [NaN: no move])."""
+        s = np.ascontiguousarray(stream, np.uint32)
+        mt = np.zeros(n_moves, np.int32)
+        ac = np.zeros(n_moves, np.int32)
+        et = np.zeros(n_moves, np.float64)
+        de = np.zeros(n_moves, np.float64)
+        used = C.c_long(0)
+        _check(lib().plum_run_moves_de(self.h, s, len(s), n_moves, _ptr(mt), _ptr(ac), _ptr(et),
+                                       _ptr(de), C.byref(used)))
+        return used.value, mt, ac, et, de
+
     def seed(self, seed: int):
         _check(lib().plum_seed(self.h, seed))
 
@@ -266,6 +287,15 @@ class System:
         o = np.zeros(5)
         _check(lib().plum_observables(self.h, o))
         return o
+
+    def structure_factor(self):
+        """(S(k) [n_kvec] complex, k [n_kvec, 3] integer components): the
+        running structure factor with the last accepted change applied."""
+        nk = self.info.n_kvec
+        sk = np.zeros(2 * max(nk, 1))
+        kn = np.zeros(3 * max(nk, 1), np.int32)
+        _check(lib().plum_structure_factor(self.h, _ptr(sk), _ptr(kn)))
+        return sk[:2 * nk].view(np.complex128), kn[:3 * nk].reshape(-1, 3)
 
     def pressure_slit(self):
         """One evaluation of the wall-force pressure sums of a slit system:
@@ -535,6 +565,29 @@ class Batch:
         o = (C.c_long * 3)()
         _check(lib().plum_batch_da_stats(self.h, o))
         return tuple(o)
+
+    def energies(self):
+        """[replicas, 4] running totals (pair, ewald, bond, ext), gathered on
+        the device and copied in one transfer."""
+        o = np.zeros((self.n, 4))
+        _check(lib().plum_batch_energies(self.h, o))
+        return o
+
+    def set_recompute(self, every):
+        """Full FP64 recompute of each replica every `every` of its moves
+        (0: never; default 10,000), staggered over the replicas."""
+        _check(lib().plum_batch_set_recompute(self.h, int(every)))
+
+    def drift(self):
+        """([replicas, 6] per replica: running-minus-recomputed pair, ewald,
+        bond, ext at its last recompute, the largest |total drift| so far,
+        its number of recomputes), recomputes in the last run, their device
+        milliseconds)."""
+        o = np.zeros((self.n, 6))
+        n = C.c_long(0)
+        ms = C.c_double(0)
+        _check(lib().plum_batch_drift(self.h, o, C.byref(n), C.byref(ms)))
+        return o, n.value, ms.value
 
 
 class HostSimulation:

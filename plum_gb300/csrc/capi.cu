@@ -58,6 +58,7 @@ struct plum_ctx {
   // scratch
   double* d_tot_part = nullptr;
   int n_tot_part = 0;
+  double2* d_sk_part = nullptr;  // [kSkGroupsTotal][n_k] partial S(k) of a recompute
   double* d_out = nullptr;     // small result block
   double* d_obs_per = nullptr;  // [n_mol * 5] per-molecule Rg / Ree sums
   double* d_press = nullptr;    // wall-force pressure partials and sums
@@ -78,6 +79,7 @@ struct plum_ctx {
   int* d_log_type = nullptr;
   int* d_log_acc = nullptr;
   double* d_log_e = nullptr;
+  double* d_log_de = nullptr;
   int log_cap = 0;
   bool host_pending = false;
   int max_len = 1;
@@ -162,9 +164,11 @@ int dalloc(T** p, size_t n) {
 }
 
 // Final fixed-order reductions of the from-scratch energy into out[8] and the
-// running state.
+// running state. With drift != null the running totals it replaces are
+// compared first: drift[0..3] = running - recomputed per term, drift[4] =
+// the largest |total drift| seen (kept across calls), drift[5] += 1.
 __global__ void k_assemble_total(const DevParams P, const DevBuffers B, const double* tot_part,
-                                 int n_part, const double* misc, double* out) {
+                                 int n_part, const double* misc, double* out, double* drift) {
   __shared__ double red[8];
   double lj = 0.0, re = 0.0, ek = 0.0;
   for (int i = threadIdx.x; i < n_part; i += blockDim.x) {
@@ -195,6 +199,18 @@ __global__ void k_assemble_total(const DevParams P, const DevBuffers B, const do
     double recip = P.use_ewald ? P.kpref * t[2] : 0.0;
     double self = P.use_ewald ? misc[2] : 0.0;
     double dip = (P.use_ewald && P.dipole) ? P.dip_coef * misc[4] * misc[4] : 0.0;
+    if (drift) {
+      const double fresh[4] = {e_pair, real + recip + self + dip, P.use_bond ? misc[0] : 0.0,
+                               P.use_ext ? misc[1] : 0.0};
+      const double run[4] = {st->e_pair, st->e_ewald, st->e_bond, st->e_ext};
+      double tot = 0.0;
+      for (int q = 0; q < 4; q++) {
+        drift[q] = run[q] - fresh[q];
+        tot += drift[q];
+      }
+      drift[4] = fmax(drift[4], fabs(tot));
+      drift[5] += 1.0;
+    }
     st->e_pair = e_pair;
     st->e_ewald = real + recip + self + dip;
     st->e_bond = P.use_bond ? misc[0] : 0.0;
@@ -213,16 +229,37 @@ __global__ void k_assemble_total(const DevParams P, const DevBuffers B, const do
   }
 }
 
+// The from-scratch FP64 energy of context c enqueued on stream s (no host
+// synchronisation): pair and real-space sums, S(k), bonds/walls/self terms,
+// then the assembly into the running state (and drift, when given) and, in
+// the precision form, the fixed-point mirror. Returns the kernels launched.
+int enqueue_total(plum_ctx* c, cudaStream_t s, double* drift) {
+  const DevParams& P = c->P;
+  int k = 0;
+  if (P.use_pair || P.use_ewald) {
+    launch_total64(P, c->B, c->d_tot_part, c->n_tot_part, s);
+    k++;
+  } else {
+    cudaMemsetAsync(c->d_tot_part, 0, sizeof(double) * 2 * c->n_tot_part, s);
+  }
+  if (P.use_ewald && P.n_k > 0) {
+    launch_sk_full64(P, c->B, c->d_sk_part, s);
+    k += 2;
+  }
+  launch_misc_total64(P, c->B, c->d_out + 16, s);
+  k_assemble_total<<<1, 256, 0, s>>>(P, c->B, c->d_tot_part, c->n_tot_part, c->d_out + 16,
+                                     c->d_out, drift);
+  k += 2;
+  if (c->form == PLUM_FORM_FP32) {
+    launch_fix_all(P, c->B, s);
+    k++;
+  }
+  return k;
+}
+
 int total_energy(plum_ctx* c, double* out8) {
   cudaSetDevice(c->device);
-  const DevParams& P = c->P;
-  if (P.use_pair || P.use_ewald) launch_total64(P, c->B, c->d_tot_part, c->n_tot_part, c->s);
-  else CK(cudaMemsetAsync(c->d_tot_part, 0, sizeof(double) * 2 * c->n_tot_part, c->s));
-  launch_sk_full64(P, c->B, c->s);
-  launch_misc_total64(P, c->B, c->d_out + 16, c->s);
-  k_assemble_total<<<1, 256, 0, c->s>>>(P, c->B, c->d_tot_part, c->n_tot_part, c->d_out + 16,
-                                        c->d_out);
-  if (c->form == PLUM_FORM_FP32) launch_fix_all(P, c->B, c->s);
+  enqueue_total(c, c->s, nullptr);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(c->h_out, c->d_out, sizeof(double) * 8, cudaMemcpyDeviceToHost, c->s));
   CK(cudaStreamSynchronize(c->s));
@@ -250,7 +287,9 @@ int ensure_logs(plum_ctx* c, int n) {
   cudaFree(c->d_log_type);
   cudaFree(c->d_log_acc);
   cudaFree(c->d_log_e);
-  if (dalloc(&c->d_log_type, n) || dalloc(&c->d_log_acc, n) || dalloc(&c->d_log_e, n))
+  cudaFree(c->d_log_de);
+  if (dalloc(&c->d_log_type, n) || dalloc(&c->d_log_acc, n) || dalloc(&c->d_log_e, n) ||
+      dalloc(&c->d_log_de, n))
     return PLUM_ERR_CUDA;
   c->log_cap = n;
   return PLUM_OK;
@@ -568,6 +607,7 @@ static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out) {
   rc |= dalloc(&B.state, 1);
   c->n_tot_part = total_partials_count(P);
   rc |= dalloc(&c->d_tot_part, 2 * (size_t)c->n_tot_part);
+  rc |= dalloc(&c->d_sk_part, (size_t)sk_full_groups() * std::max(1, P.n_k));
   rc |= dalloc(&c->d_out, 64);
   rc |= dalloc(&c->d_obs_per, 5 * (size_t)std::max(1, in.n_mol));
   c->rhoz_bins = (int)std::ceil(in.box[2] / kRhoZRes);
@@ -628,7 +668,7 @@ int plum_ctx_destroy(plum_ctx* c) {
                   c->cb_part,    c->cb_u,      c->d_obs_per, c->d_rhoz, c->desc_acc,
                   c->d_rp1,      c->d_rb1,     c->desc_fine, c->cb_part32, c->cb_ticket,
                   c->d_stream,   c->d_mt,      c->d_log_type, c->d_log_acc, c->d_log_e,
-                  c->d_press};
+                  c->d_press,    c->d_sk_part, c->d_log_de};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_out) cudaFreeHost(c->h_out);
@@ -922,6 +962,13 @@ int plum_finalize(plum_ctx* c, int accept) {
 
 int plum_run_moves(plum_ctx* c, const uint32_t* stream, long n_stream, int n_moves,
                    int* move_type, int* accept, double* etot, long* draws_used) {
+  return plum_run_moves_de(c, stream, n_stream, n_moves, move_type, accept, etot, nullptr,
+                           draws_used);
+}
+
+int plum_run_moves_de(plum_ctx* c, const uint32_t* stream, long n_stream, int n_moves,
+                      int* move_type, int* accept, double* etot, double* de,
+                      long* draws_used) {
   if (!c || (!stream && n_stream > 0) || n_moves < 0)
     return fail(PLUM_ERR_INPUT, "bad argument");
   if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
@@ -949,6 +996,7 @@ int plum_run_moves(plum_ctx* c, const uint32_t* stream, long n_stream, int n_mov
   B.log_type = c->d_log_type;
   B.log_accept = c->d_log_acc;
   B.log_etot = c->d_log_e;
+  B.log_step_de = de ? c->d_log_de : nullptr;
   c->last_kernels = 0;
   CK(cudaEventRecord(c->ev0, c->s));
   rc = device_loop(c, n_moves, B);
@@ -966,6 +1014,7 @@ int plum_run_moves(plum_ctx* c, const uint32_t* stream, long n_stream, int n_mov
   if (accept)
     CK(cudaMemcpy(accept, c->d_log_acc, sizeof(int) * n_moves, cudaMemcpyDeviceToHost));
   if (etot) CK(cudaMemcpy(etot, c->d_log_e, sizeof(double) * n_moves, cudaMemcpyDeviceToHost));
+  if (de) CK(cudaMemcpy(de, c->d_log_de, sizeof(double) * n_moves, cudaMemcpyDeviceToHost));
   if (draws_used) *draws_used = (long)st.stream_pos;
   if (st.error == PLUM_ERR_STREAM_DEV)
     return fail(PLUM_ERR_STREAM, "the recorded random stream ran out");
@@ -1015,6 +1064,7 @@ int plum_run(plum_ctx* c, int n_moves, int* accepted_out) {
   B.log_type = nullptr;
   B.log_accept = nullptr;
   B.log_etot = nullptr;
+  B.log_step_de = nullptr;
   c->last_kernels = 0;
   CK(cudaEventRecord(c->ev0, c->s));
   int done = 0;
@@ -1198,6 +1248,41 @@ int plum_ctx_load(plum_ctx* c, const void* buf, long size) {
   CK(cudaStreamSynchronize(c->s));
   c->h_pos_valid = true;
   c->gen_len = 0;
+  return PLUM_OK;
+}
+
+int plum_structure_factor(const plum_ctx* cc, double* sk_out, int* kn_out) {
+  plum_ctx* c = const_cast<plum_ctx*>(cc);
+  if (!c) return fail(PLUM_ERR_INPUT, "null context");
+  if (c->host_pending) return fail(PLUM_ERR_STATE, "a trial move is pending");
+  cudaSetDevice(c->device);
+  const int nk = c->P.use_ewald ? c->P.n_k : 0;
+  if (nk == 0) return PLUM_OK;
+  if (kn_out) {
+    std::vector<short4> kn(nk);
+    CK(cudaMemcpyAsync(kn.data(), c->B.kn, sizeof(short4) * nk, cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    for (int k = 0; k < nk; k++) {
+      kn_out[3 * k] = kn[k].x;
+      kn_out[3 * k + 1] = kn[k].y;
+      kn_out[3 * k + 2] = kn[k].z;
+    }
+  }
+  if (sk_out) {
+    DevState st;
+    int rc = read_state(c, &st);
+    if (rc) return rc;
+    std::vector<double2> sk(nk), add(nk);
+    CK(cudaMemcpyAsync(sk.data(), c->B.sk, sizeof(double2) * nk, cudaMemcpyDeviceToHost, c->s));
+    if (st.sk_pending)
+      CK(cudaMemcpyAsync(add.data(), c->B.dsk + (size_t)st.sk_buf * nk, sizeof(double2) * nk,
+                         cudaMemcpyDeviceToHost, c->s));
+    CK(cudaStreamSynchronize(c->s));
+    for (int k = 0; k < nk; k++) {
+      sk_out[2 * k] = sk[k].x + (st.sk_pending ? add[k].x : 0.0);
+      sk_out[2 * k + 1] = sk[k].y + (st.sk_pending ? add[k].y : 0.0);
+    }
+  }
   return PLUM_OK;
 }
 
@@ -1666,6 +1751,18 @@ struct plum_batch {
   int max_bead = 0;
   std::vector<DevParams> h_rp;   // host copies of d_rp, d_rb
   std::vector<DevBuffers> h_rb;
+  // full FP64 recompute of each replica every rc_every of its moves (0:
+  // never); rc_since[r] counts replica r's moves since its last one. The
+  // replicas start at staggered phases (r * rc_every / R), so every batch of
+  // steps recomputes its share of them and any run of whole batches carries
+  // the cost in proportion. d_drift [R][6] as k_assemble_total writes it.
+  long rc_every = 10000;
+  std::vector<long> rc_since;
+  double* d_drift = nullptr;
+  double* d_energies = nullptr;    // [R][4] gathered running totals
+  std::vector<cudaEvent_t> rc_ev;  // start/end pairs around the recomputes of one run
+  double rc_ms = 0.0;              // device time of the last run's recomputes
+  long rc_count = 0;               // recomputes in the last run
 };
 
 namespace {
@@ -1825,9 +1922,73 @@ int batch_steps_graph(plum_batch* b, int steps) {
   return PLUM_OK;
 }
 
+// After a batch of `steps` steps: the full FP64 recompute (enqueue_total with
+// drift) of every replica whose count reached rc_every, on the batch stream
+// between CUDA events, so it is part of the run's device time. No move is
+// pending between batches of steps (the last step of a batch only finishes
+// and decides).
+int batch_recompute_due(plum_batch* b, int steps, int* n_pairs) {
+  if (b->rc_every <= 0) return PLUM_OK;
+  const int R = (int)b->reps.size();
+  bool any = false;
+  for (int r = 0; r < R; r++) {
+    b->rc_since[r] += steps;
+    any |= b->rc_since[r] >= b->rc_every;
+  }
+  if (!any) return PLUM_OK;
+  const int i = *n_pairs;
+  while ((int)b->rc_ev.size() < 2 * (i + 1)) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    b->rc_ev.push_back(e);
+  }
+  CK(cudaEventRecord(b->rc_ev[2 * i], b->s));
+  for (int r = 0; r < R; r++) {
+    if (b->rc_since[r] < b->rc_every) continue;
+    b->last_kernels += enqueue_total(b->reps[r], b->s, b->d_drift + 6 * r);
+    b->rc_since[r] -= b->rc_every;
+    b->rc_count++;
+  }
+  CK(cudaEventRecord(b->rc_ev[2 * i + 1], b->s));
+  CK(cudaGetLastError());
+  *n_pairs = i + 1;
+  return PLUM_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int plum_batch_energies(plum_batch* b, double* out) {
+  if (!b || !out) return fail(PLUM_ERR_INPUT, "null argument");
+  cudaSetDevice(b->device);
+  const int R = (int)b->reps.size();
+  // one gather launch and one copy for all replicas
+  launch_gather_energies(b->d_sts, R, b->d_energies, b->s);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, b->d_energies, sizeof(double) * 4 * R, cudaMemcpyDeviceToHost, b->s));
+  CK(cudaStreamSynchronize(b->s));
+  return PLUM_OK;
+}
+
+int plum_batch_set_recompute(plum_batch* b, long every) {
+  if (!b || every < 0) return fail(PLUM_ERR_INPUT, "bad argument");
+  b->rc_every = every;
+  const int R = (int)b->reps.size();
+  for (int r = 0; r < R; r++) b->rc_since[r] = every ? (long)((long long)r * every / R) : 0;
+  return PLUM_OK;
+}
+
+int plum_batch_drift(plum_batch* b, double* out, long* count, double* ms) {
+  if (!b || !out) return fail(PLUM_ERR_INPUT, "null argument");
+  cudaSetDevice(b->device);
+  const int R = (int)b->reps.size();
+  CK(cudaMemcpyAsync(out, b->d_drift, sizeof(double) * 6 * R, cudaMemcpyDeviceToHost, b->s));
+  CK(cudaStreamSynchronize(b->s));
+  if (count) *count = b->rc_count;
+  if (ms) *ms = b->rc_ms;
+  return PLUM_OK;
+}
 
 int plum_batch_destroy(plum_batch* b) {
   if (!b) return PLUM_OK;
@@ -1836,9 +1997,10 @@ int plum_batch_destroy(plum_batch* b) {
   for (plum_ctx* c : b->reps) plum_ctx_destroy(c);
   void* ptrs[] = {b->d_cells, b->d_queue, b->d_slots2, b->d_rp,    b->d_rb,  b->d_item_off, b->d_slots, b->d_states, b->d_outs,
                   b->d_sts,   b->d_pos, b->d_len,      b->d_cap,   b->d_gather, b->d_need,
-                  b->d_desc,  b->d_err, b->d_fine};
+                  b->d_desc,  b->d_err, b->d_fine,     b->d_drift,  b->d_energies};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (cudaEvent_t e : b->rc_ev) cudaEventDestroy(e);
   if (b->h_gather) cudaFreeHost(b->h_gather);
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   if (b->ev0) cudaEventDestroy(b->ev0);
@@ -1906,6 +2068,7 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
     hb[r].log_type = nullptr;
     hb[r].log_accept = nullptr;
     hb[r].log_etot = nullptr;
+    hb[r].log_step_de = nullptr;
     hst[r] = c->d_mt;
     hout[r] = c->d_stream;
     hsts[r] = c->B.state;
@@ -1936,10 +2099,15 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
   rc |= dalloc(&b->d_err, 1);
   rc |= dalloc(&b->d_queue, 4);
   rc |= dalloc(&b->d_slots2, 2 * (size_t)items + 2);
+  rc |= dalloc(&b->d_drift, 6 * (size_t)n);
+  rc |= dalloc(&b->d_energies, 4 * (size_t)n);
   if (rc) {
     plum_batch_destroy(b);
     return PLUM_ERR_CUDA;
   }
+  cudaMemset(b->d_drift, 0, sizeof(double) * 6 * n);
+  b->rc_since.resize(n);
+  for (int r = 0; r < n; r++) b->rc_since[r] = (long)((long long)r * b->rc_every / n);
   cudaMemset(b->d_err, 0, sizeof(int));
   cudaMemset(b->d_queue, 0, 4 * sizeof(int));
   for (int r = 0; r < n; r++) {
@@ -2035,6 +2203,9 @@ int plum_batch_run(plum_batch* b, int n_steps, long* accepted_out) {
   std::vector<long long> pos(R), len(R);
   long long acc0 = 0, acc1 = 0;
   b->last_kernels = 0;
+  b->rc_count = 0;
+  b->rc_ms = 0.0;
+  int n_pairs = 0;  // event pairs recorded around recomputes in this run
   CK(cudaEventRecord(b->ev0, b->s));
   int done = 0;
   bool first = true;
@@ -2069,6 +2240,8 @@ int plum_batch_run(plum_batch* b, int n_steps, long* accepted_out) {
     if (rc) return rc;
     b->last_kernels += batch_kernels(b, steps);
     done += steps;
+    rc = batch_recompute_due(b, steps, &n_pairs);
+    if (rc) return rc;
   }
   CK(cudaEventRecord(b->ev1, b->s));
   launch_gather_states(b->d_sts, R, b->d_gather, b->s);
@@ -2078,6 +2251,11 @@ int plum_batch_run(plum_batch* b, int n_steps, long* accepted_out) {
   float ms = 0;
   cudaEventElapsedTime(&ms, b->ev0, b->ev1);
   b->last_ms = ms;
+  for (int i = 0; i < n_pairs; i++) {
+    float t = 0;
+    cudaEventElapsedTime(&t, b->rc_ev[2 * i], b->rc_ev[2 * i + 1]);
+    b->rc_ms += t;
+  }
   for (int r = 0; r < R; r++) {
     const long long* g = b->h_gather + 6 * r;
     if (g[2] == PLUM_ERR_STREAM_DEV) return fail(PLUM_ERR_STREAM, "replica stream ran out");

@@ -162,6 +162,7 @@ struct DevBuffers {  // all pointers: copied word-wise into shared memory by the
   int* log_type;
   int* log_accept;
   double* log_etot;
+  double* log_step_de;  // energy change of each step's proposal (NaN: none)
   // surrogate: descriptor of the pending move [96] (integer units of
   // 2^-12), its fine distance histogram, and the optional training log
   unsigned* desc_acc;
@@ -200,7 +201,10 @@ void launch_delta_pairs64(const DevParams& P, const DevBuffers& B, cudaStream_t 
 void launch_total64(const DevParams& P, const DevBuffers& B, double* out_partials,
                     int n_part, cudaStream_t s);
 int total_partials_count(const DevParams& P);
-void launch_sk_full64(const DevParams& P, const DevBuffers& B, cudaStream_t s);
+// S(k) from scratch; part: sk_full_groups() * n_k double2 of scratch owned by
+// the caller (one per context, so contexts on different streams never share it)
+int sk_full_groups();
+void launch_sk_full64(const DevParams& P, const DevBuffers& B, double2* part, cudaStream_t s);
 void launch_misc_total64(const DevParams& P, const DevBuffers& B, double* out6,
                          cudaStream_t s);
 
@@ -293,6 +297,7 @@ void launch_mt_fill_batch(uint32_t* const* states, uint32_t* const* outs, const 
                           const long long* len, const long long* cap, const int* need,
                           DevState* const* sts, int n_rep, cudaStream_t s);
 void launch_gather_states(DevState* const* sts, int n_rep, long long* out, cudaStream_t s);
+void launch_gather_energies(DevState* const* sts, int n_rep, double* out, cudaStream_t s);
 
 // mt19937 on the device: state[625] (624 words + index), fills out[n].
 void launch_mt_fill(uint32_t* state, uint32_t* out, long long n, cudaStream_t s);

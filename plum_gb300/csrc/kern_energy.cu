@@ -423,16 +423,10 @@ __global__ void k_sk_sum(int n_k, const double2* part, double2* sk) {
   sk[k] = s;
 }
 
-void launch_sk_full64(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
+int sk_full_groups() { return kSkGroups; }
+
+void launch_sk_full64(const DevParams& P, const DevBuffers& B, double2* part, cudaStream_t s) {
   if (!P.use_ewald || P.n_k == 0) return;
-  static double2* part = nullptr;
-  static size_t cap = 0;
-  size_t need = (size_t)kSkGroups * P.n_k * sizeof(double2);
-  if (need > cap) {
-    if (part) cudaFree(part);
-    cudaMalloc(&part, need);
-    cap = need;
-  }
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_sk64, cudaFuncAttributeMaxDynamicSharedMemorySize, kKTableBytes + 4096);

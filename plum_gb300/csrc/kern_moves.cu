@@ -701,6 +701,7 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
     if (B.log_type) B.log_type[sidx] = pending ? S.move_type : -1;
     if (B.log_accept) B.log_accept[sidx] = pending ? S.last_accept : 0;
     if (B.log_etot) B.log_etot[sidx] = S.e_pair + S.e_ewald + S.e_bond + S.e_ext;
+    if (B.log_step_de) B.log_step_de[sidx] = pending ? S.de : __longlong_as_double(0x7ff8000000000000LL);
     S.step = sidx + 1;
     S.step_open = 0;
   }
@@ -874,6 +875,21 @@ __global__ void k_gather_states(DevState* const* sts, int n_rep, long long* out)
 
 void launch_gather_states(DevState* const* sts, int n_rep, long long* out, cudaStream_t s) {
   k_gather_states<<<(n_rep + 255) / 256, 256, 0, s>>>(sts, n_rep, out);
+}
+
+// Running totals {pair, ewald, bond, ext} of every replica into out[4 r + q].
+__global__ void k_gather_energies(DevState* const* sts, int n_rep, double* out) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n_rep; r += gridDim.x * blockDim.x) {
+    const DevState* st = sts[r];
+    out[4 * r] = st->e_pair;
+    out[4 * r + 1] = st->e_ewald;
+    out[4 * r + 2] = st->e_bond;
+    out[4 * r + 3] = st->e_ext;
+  }
+}
+
+void launch_gather_energies(DevState* const* sts, int n_rep, double* out, cudaStream_t s) {
+  k_gather_energies<<<(n_rep + 255) / 256, 256, 0, s>>>(sts, n_rep, out);
 }
 
 void launch_mt_fill_batch(uint32_t* const* states, uint32_t* const* outs, const long long* pos,

@@ -71,7 +71,96 @@ CASES = {
                                                  n_sites=0, charge_frac=0.6),
                           over=dict(ext_kind="WellWall", well_width=2.0, well_depth=-0.7,
                                     wall_radii=(("P", 0.5), ("L", 0.0), ("C", 0.5)))),
+    # the 1,000-particle bulk polyelectrolyte at its own size (10 x 50 chains,
+    # 500 counterions, L = 40, alpha = (5/L)^2) with the reference's own Ewald
+    # rule: real cut-off 28 > L/2 (several image cells per pair) and 460
+    # k-vectors; the generator seed is the one the benchmark workload uses
+    "bulk_1000": dict(kind="bulk", seed=20261203, run_seed=12345, steps=400, kinds=True,
+                      spec=systems.CONFIGS["bulk_1000"]),
+    # the smallest replica of the 256-replica confined-brush ensemble
+    # (systems.brush_ensemble(256, 20261203); its index is stored as
+    # ref.npz["ensemble"][2]) at full size: 16 grafted chains of 26 beads,
+    # 64 LJ surface sites per wall, 9-3 walls, slab Ewald with the dipole
+    # correction
+    "brush_ens_smallest": dict(kind="brush", seed=None, run_seed=4321, steps=300, kinds=True,
+                               spec=None, ensemble=(256, 20261203)),
 }
+
+
+def ensemble_member(n, seed, pick="smallest"):
+    """(index, spec, generator seed) of one replica of the confined-brush
+    ensemble, the seed as the benchmark writes it (seed + index)."""
+    specs = systems.brush_ensemble(n, seed)
+    size = [s.n_graft * s.chain_len * (1.0 + s.charge_frac) for s in specs]
+    i = int(np.argmin(size)) if pick == "smallest" else int(pick)
+    return i, specs[i], seed + i
+
+
+def _unit(rng):
+    v = rng.normal(size=3)
+    return v / np.linalg.norm(v)
+
+
+def kind_trials(coords, start, sizes, rng, move_size=1.0, bond=1.0, per_kind=5, first_mol=0):
+    """Trial configurations of each of the reference's move kinds
+    (molecule.cc:103-312), built from the current coordinates with numpy
+    draws: ion translation by exactly 3 move_size, chain COM translation
+    (per axis up to 0.5 move_size), pivot (each bead outward of the pivot
+    perturbed by up to move_size and re-projected to a bond of r0 +- 10%,
+    the rest of that side carried along), crankshaft (beads strictly between
+    first and last rotated about the first-last axis) and reptation (shift by
+    one bead, new end one bond from the old end). Yields (kind, mol, trial,
+    moved) with kind 0..4 in the reference's order [bead, COM, pivot, crank,
+    rept]."""
+    chains = [m for m in range(first_mol, len(sizes)) if sizes[m] > 1]
+    ions = [m for m in range(first_mol, len(sizes)) if sizes[m] == 1]
+    for kind in range(5):
+        for _ in range(per_kind):
+            if kind == 0:
+                m = int(ions[rng.integers(len(ions))])
+            else:
+                m = int(chains[rng.integers(len(chains))])
+            cur = coords[start[m]:start[m + 1]].copy()
+            n = len(cur)
+            moved = np.ones(n, np.int32)
+            t = cur.copy()
+            if kind == 0:
+                t[0] = cur[0] + 3.0 * move_size * _unit(rng)
+            elif kind == 1:
+                t = cur + 0.5 * move_size * rng.uniform(-1.0, 1.0, size=3)
+            elif kind == 2:
+                p = int(rng.integers(n))
+                size = move_size * rng.uniform()
+                for rng_dir in (range(p + 1, n), range(p - 1, -1, -1)):
+                    for i in rng_dir:
+                        j = i - 1 if rng_dir.step == 1 else i + 1
+                        x = t[i] + size * _unit(rng)
+                        d = x - t[j]
+                        b = bond + (bond / 5.0) * (rng.uniform() - 0.5)
+                        c = t[j] + d * (b / np.linalg.norm(d))
+                        sl = slice(i, n) if rng_dir.step == 1 else slice(0, i + 1)
+                        t[sl] += c - t[i]
+            elif kind == 3:
+                first = int(rng.integers(0, n - 2))
+                last = min(n - 1, first + 2 + int(rng.integers(0, n - first - 2)))
+                axis = cur[last] - cur[first]
+                axis /= np.linalg.norm(axis)
+                ang = move_size * (rng.uniform() * 2 * np.pi - np.pi)
+                K = np.array([[0, -axis[2], axis[1]], [axis[2], 0, -axis[0]],
+                              [-axis[1], axis[0], 0]])
+                Rm = np.eye(3) + np.sin(ang) * K + (1 - np.cos(ang)) * (K @ K)
+                moved[:] = 0
+                moved[first + 1:last] = 1
+                t[first + 1:last] = (cur[first + 1:last] - cur[first]) @ Rm.T + cur[first]
+            else:
+                b = bond + (bond / 5.0) * (rng.uniform() - 0.5)
+                if rng.integers(2):
+                    t[:-1] = cur[1:]
+                    t[-1] = cur[-1] + b * _unit(rng)
+                else:
+                    t[1:] = cur[:-1]
+                    t[0] = cur[0] + b * _unit(rng)
+            yield kind, m, t, moved
 
 
 CBMC_CASES = {
@@ -330,21 +419,27 @@ def make_stat_cases(workers=8):
 
 
 def make_case(name, cfg, n_de=24):
+    import time
+    t0 = time.time()
     d = os.path.join(HERE, name)
     if os.path.isdir(d):
         shutil.rmtree(d)
     os.makedirs(d)
-    if cfg["kind"] == "bulk":
-        systems.write_bulk(d, cfg["spec"], seed=cfg["seed"], **cfg.get("over", {}))
-    else:
-        systems.write_brush(d, cfg["spec"], seed=cfg["seed"], **cfg.get("over", {}))
+    spec, seed = cfg["spec"], cfg["seed"]
     out = {}
+    if cfg.get("ensemble"):
+        idx, spec, seed = ensemble_member(*cfg["ensemble"])
+        out["ensemble"] = np.array([cfg["ensemble"][0], cfg["ensemble"][1], idx])
+    if cfg["kind"] == "bulk":
+        systems.write_bulk(d, spec, seed=seed, **cfg.get("over", {}))
+    else:
+        systems.write_brush(d, spec, seed=seed, **cfg.get("over", {}))
     R = ob.Ref(d, seed=cfg["run_seed"])
     out["energies"] = R.energies()
     out["ewald"] = R.ewald_info()
     sizes = np.array([R.mol_size(m) for m in range(R.n_mol)])
     start = np.concatenate([[0], np.cumsum(sizes)])
-    rng = np.random.default_rng(cfg["seed"] + 1000)
+    rng = np.random.default_rng(seed + 1000)
     c = R.coords()
     mols, trials, moveds, outs = [], [], [], []
     movable = [m for m in range(R.n_mol) if sizes[m] > 1] + \
@@ -365,6 +460,23 @@ def make_case(name, cfg, n_de=24):
         trials.append(trial)
         moveds.append(moved)
         outs.append(R.delta_energy(m, trial, moved))
+    kinds = [-1] * len(mols)
+    if cfg.get("kinds"):
+        first = spec.n_sites * 2 if cfg["kind"] == "brush" else 0
+        for kind, m, trial, moved in kind_trials(c, start, sizes, rng, move_size=spec.move_size,
+                                                 bond=spec.r0, first_mol=first):
+            kinds.append(kind)
+            mols.append(m)
+            trials.append(trial)
+            moveds.append(moved)
+            outs.append(R.delta_energy(m, trial, moved))
+    # When the pair (or pair + external) change reaches 1e8 the reference
+    # returns before the Ewald part (force_field.cc:411-422), so the Ewald
+    # potential's dE member still holds the previous call's value: the
+    # component is recorded as 0, the change the early return adds. (The
+    # bond and Ewald terms cannot lift a total below 1e8 to it.)
+    outs = [np.array([o[0], o[1], 0.0 if o[0] >= 1e8 else o[2]]) for o in outs]
+    out["de_kind"] = np.array(kinds, np.int32)
     out["de_mol"] = np.array(mols, np.int32)
     out["de_start"] = start.astype(np.int32)
     out["de_trial"] = np.concatenate(trials)
@@ -383,7 +495,8 @@ def make_case(name, cfg, n_de=24):
         if f not in ("run.in", "input_crd.dat", "input_top.dat"):
             os.remove(os.path.join(d, f))
     np.savez_compressed(os.path.join(d, "ref.npz"), **out)
-    print(name, "beads", int(start[-1]), "accept", ac.mean(), "types", np.bincount(mt + 1))
+    print(name, "beads", int(start[-1]), "accept", ac.mean(), "types", np.bincount(mt + 1),
+          "%.0f s" % (time.time() - t0))
 
 
 # Output files: the reference's Simulation::Run with sampling and writing on

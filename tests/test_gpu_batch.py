@@ -37,10 +37,11 @@ def test_uneven_replicas_replay_their_references(pg, tune):
         e = rep.energies().sum()
         ref = g["run_etot"][n - 1]
         assert rel(e, ref, max(1.0, abs(ref))) < 1e-4, (CASES[r], e, ref)
-        # the running totals stay consistent with an FP64 recompute (not for
-        # the slab cases: there the reference's running Ewald total carries
-        # the dipole term of the configuration before the last accepted move)
-        if not CASES[r].startswith("slab"):
+        # the running totals stay consistent with an FP64 recompute (not with
+        # the dipole correction on: there the reference's running Ewald total
+        # carries the dipole term of the configuration before the last
+        # accepted move)
+        if not g["ewald"][14]:
             fresh = rep.total_energy()[:4].sum()
             assert rel(e, fresh, max(1.0, abs(fresh))) < 1e-4
 
@@ -93,3 +94,49 @@ def test_two_step_chains_give_the_same_trajectories(pg):
     for (pa, ea), (pb, eb) in zip(*out):
         np.testing.assert_array_equal(pa, pb)
         np.testing.assert_array_equal(ea, eb)
+
+
+def test_batch_recompute_resets_drift_past_1e4_steps(pg):
+    """The batch's full FP64 recompute (every 10^4 moves per replica, phases
+    staggered over the replicas) on a charged case: after 12,000 steps every
+    replica has been recomputed at least once, the drift it found is finite,
+    non-zero (FP32 energy changes) and small against the total, the
+    recomputes ran inside the timed batch runs, and the running totals still
+    equal a from-scratch recompute to the precision form's 1e-4."""
+    d, _ = load("bulk_medium")
+    R = 4
+    b = pg.Batch([d] * R)
+    b.seed(np.arange(31, 31 + R, dtype=np.uint32))
+    n_rc, ms = 0, 0.0
+    for _ in range(12):
+        b.run(1000)
+        dr, n, t = b.drift()
+        n_rc += n
+        ms += t
+    assert n_rc >= R and ms > 0.0, (n_rc, ms)
+    assert (dr[:, 5] >= 1).all(), dr[:, 5]
+    for r in range(R):
+        rep = b.replica(r)
+        e = rep.energies().copy()
+        assert np.isfinite(dr[r]).all()
+        assert 0.0 < dr[r, 4] < 1e-3 * max(1.0, abs(e.sum())), (dr[r], e)
+        fresh = rep.total_energy()[:4]
+        assert rel(e.sum(), fresh.sum(), max(1.0, abs(fresh.sum()))) < 1e-4
+    b.close()
+
+
+def test_batch_recompute_off_and_cadence(pg):
+    """set_recompute(0) switches the recompute off; a cadence of 64 moves
+    recomputes every replica about once per 64 steps."""
+    d, _ = load("bulk_small")
+    b = pg.Batch([d] * 3)
+    b.seed(9)
+    b.set_recompute(0)
+    b.run(640)
+    dr, n, _ = b.drift()
+    assert n == 0 and (dr[:, 5] == 0).all()
+    b.set_recompute(64)
+    b.run(640)
+    dr, n, _ = b.drift()
+    assert 27 <= n <= 33, n
+    b.close()

@@ -51,21 +51,16 @@ def _lj_fluid(tmp):
     return d
 
 
-def test_delayed_acceptance_keeps_the_stationary_distribution(pg, tmp_path):
+def _paired_stationarity(pg, d, sg, R=64, burn=20000, every=100, n=200):
     """Replicas equilibrated with the plain rule continue from the same
     configurations with and without delayed acceptance (independent seeds):
     per replica the mean energy and Rg^2 over the continuation differ by no
     more than 2.5 standard errors of the paired differences. A surrogate that
     broke detailed balance would shift the sampled distribution away from
-    the equilibrium both runs start in."""
-    from plum_gb300 import surrogate as S
-    d = _lj_fluid(tmp_path)
-    desc, de, _ = S.collect(d, 30000, n_ctx=4, seed=900, moves_per_call=20000)
-    sg, st = S.fit(desc, de, epochs=40, batch=1024, lr=1e-3, seed=4)
-    R, every, n = 64, 100, 200
+    the equilibrium both runs start in. Returns the surrogate's counters."""
     a = pg.Batch([d] * R)
     a.seed(np.arange(100, 100 + R, dtype=np.uint32))
-    a.run(20000)
+    a.run(burn)
     snap = [a.replica(r).positions() for r in range(R)]
     b = pg.Batch([d] * R)
     b.seed(np.arange(5000, 5000 + R, dtype=np.uint32))
@@ -89,6 +84,67 @@ def test_delayed_acceptance_keeps_the_stationary_distribution(pg, tmp_path):
         diff = y.mean(axis=0) - x.mean(axis=0)
         se = diff.std(ddof=1) / np.sqrt(R)
         assert abs(diff.mean()) <= 2.5 * se, (name, diff.mean(), se, x.mean(), y.mean())
+    a.close()
+    b.close()
+    return moves, passed, acc
+
+
+def test_delayed_acceptance_keeps_the_stationary_distribution(pg, tmp_path):
+    """The paired test on an uncharged LJ fluid with a surrogate trained on it."""
+    from plum_gb300 import surrogate as S
+    d = _lj_fluid(tmp_path)
+    desc, de, _ = S.collect(d, 30000, n_ctx=4, seed=900, moves_per_call=20000)
+    sg, st = S.fit(desc, de, epochs=40, batch=1024, lr=1e-3, seed=4)
+    _paired_stationarity(pg, d, sg)
+
+
+def test_delayed_acceptance_keeps_the_stationary_distribution_charged(pg, trained):
+    """The paired test on the charged bulk case (Ewald on: every stage-one
+    rejection takes the serial step's own S(k) commit path), with the
+    surrogate trained on it and no dead zone, so that stage one rejects
+    often."""
+    sg, _ = trained
+    d, _ = load("bulk_small")
+    moves, passed, acc = _paired_stationarity(pg, d, sg)
+    assert moves - passed > 0.2 * moves, (moves, passed)
+
+
+def test_delayed_acceptance_bookkeeping_matches_recompute_charged(pg, trained):
+    """After 2,500 delayed-acceptance steps of 8 charged replicas, with the
+    periodic recompute off so that every running sum spans the whole run,
+    each replica's running totals and S(k) equal a from-scratch FP64
+    recompute of its final configuration. Moves that stage one rejects skip
+    the exact energy change, and the serial step then applies the S(k) change
+    of the last accepted move itself (the delta kernel would otherwise do
+    it); a missed or doubled commit would move S(k) by a whole bead's
+    q e^{ik.r} (order 1) at most k. Tolerances: the totals within 1e-4 of
+    their size (FP32 energy changes summed in FP64, as the precision form's
+    other recompute checks), S(k) within 1e-3 per vector (FP32 phase
+    changes summed in FP64: about 1e-5 after this run)."""
+    sg, _ = trained
+    d, _ = load("bulk_small")
+    R = 8
+    b = pg.Batch([d] * R)
+    b.seed(np.arange(70, 70 + R, dtype=np.uint32))
+    b.set_recompute(0)
+    b.set_surrogate(sg)
+    b.run(2500)
+    moves, passed, acc = b.da_stats()
+    assert moves - passed > 0.2 * moves and acc > 0, (moves, passed, acc)
+    worst_e, worst_s = 0.0, 0.0
+    for r in range(R):
+        rep = b.replica(r)
+        run = rep.energies().copy()
+        sk_run, kn = rep.structure_factor()
+        assert len(kn) > 0
+        fresh = rep.total_energy()[:4]
+        sk_fresh, _ = rep.structure_factor()
+        worst_e = max(worst_e, abs(run.sum() - fresh.sum()) / max(1.0, abs(fresh.sum())))
+        worst_s = max(worst_s, float(np.abs(sk_run - sk_fresh).max()))
+        np.testing.assert_allclose(run, fresh, rtol=1e-4, atol=1e-3)
+    assert worst_e < 1e-4, worst_e
+    assert worst_s < 1e-3, worst_s
+    b.close()
 
 
 def test_gain_over_the_method_without_the_network(pg, trained):
