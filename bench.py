@@ -6,26 +6,40 @@ plus 10,000 +1 counterions, periodic cube L = 80, LJ eps = sigma = 1 cut at
 2.5, harmonic bonds k = 400 r0 = 1, lB = 3, Ewald alpha = (5.6/L)^2 with the
 real-space cut-off at L/2 and |n| <= 12 per axis (7,812 half-space k-vectors),
 move mix ion 0.3 / COM 0.1 / pivot 0.2 / crankshaft 0.2 / reptation 0.2.
-Seeded synthetic initial configuration (self-avoiding chains, uniform ions,
+Seeded synthetic initial configurations (self-avoiding chains, uniform ions,
 no pair closer than 0.8 sigma), written in the reference's input formats.
 
 A "step" is a batch of Monte Carlo moves run on the device. Reported:
-  value        moves/s of the precision form (FP32 pair/k arithmetic, FP64
-               accumulators, FP64 recompute every 1e4 moves), device time
-  plain_fp64   moves/s of the plain FP64 form on the same system
-  e2e          moves/s through the C ABI with host buffers: the recorded
-               mt19937 stream copied in and the per-move logs copied out
-               inside the timed region
-  samples      Rg-decorrelated samples/s (tau_int of the chain-averaged Rg^2
-               series, Sokal window c = 5) when --samples-seconds > 0
-  roofline     FP32 pipe: algorithmic FLOPs per move x moves/s over the FP32
+  value        moves/s of the chosen form: 64 replicas in one batch, precision
+               form (FP32 pair/k arithmetic, FP64 S(k) and totals), delayed
+               acceptance with the learned surrogate, and each replica's full
+               FP64 recompute every 1e4 of its moves (staggered over the
+               replicas, inside the timed region); device time
+  e2e          the same through the public batch call with every replica's
+               running energies copied to the host after every step
+  plain_fp64   moves/s of the plain FP64 form on one system, with its own
+               FP64-pipe roofline and an e2e through plum_run_moves (the
+               recorded mt19937 stream copied in, per-move logs copied out)
+  precision_on_chain
+               FP32 against FP64 energy changes of the chain's own proposals
+               (both forms fed one recorded stream) on the 1,000-particle
+               bulk system, this workload and a confined-brush replica: error
+               and the fraction of Metropolis decisions that flip
+  equilibrium  burn-in of 16 replicas with the chosen form, tau_int of the
+               chains' Rg^2 (Sokal window, c = 5) for the chosen form and the
+               plain Metropolis dynamics, and the chosen form's mean energy
+               and Rg^2 against plain FP64 runs from the same equilibrated
+               starts (2 standard errors of the paired differences)
+  samples      Rg-decorrelated samples/s = moves/s / (2 tau_int)
+  roofline     FP32 pipe of the batched energy-change kernel: algorithmic
+               FLOPs per move x moves per launch / launch time, over the FP32
                FMA peak measured on this GPU by a probe kernel
   cpu_baseline the FP64 CPU restatement of the reference (the reference
                itself cannot hold 20,000 particles: O(N^2) std::map storage)
                on a bounded sample of moves, one core
 
-``--impl reference`` times the reference's CPU path (oracle/_ref where the
-reference compiled, else the CPU restatement) with one process per host core.
+``--impl reference`` times the reference's CPU path (the CPU restatement, one
+process per host core). ``--only MODE`` runs one profiling case instead.
 """
 from __future__ import annotations
 
@@ -44,6 +58,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "MC moves/s and Rg-decorrelated samples/s: plain FP64 vs chosen form, 1 GB300"
+
+# DRAM bytes per evaluated move of the batched energy-change kernel on this
+# workload: dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture
+# (64 replicas, every move evaluated: 44 MB per launch of 64 moves)
+TRAFFIC_PER_EXACT_MOVE = 44.0e6 / 64
 
 
 def mt19937_stream(seed: int, n: int):
@@ -109,41 +128,6 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(mhz)}
 
 
-def tau_int(x, c=5.0):
-    """Integrated autocorrelation time with Sokal's automatic window."""
-    import numpy as np
-    x = np.asarray(x, dtype=np.float64)
-    n = len(x)
-    if n < 8:
-        return float("nan")
-    x = x - x.mean()
-    f = np.fft.rfft(x, 2 * n)
-    acf = np.fft.irfft(f * np.conj(f))[:n]
-    if acf[0] <= 0:
-        return float("nan")
-    rho = acf / acf[0]
-    tau = 0.5
-    for w in range(1, n):
-        tau += rho[w]
-        if w >= c * tau:
-            break
-    return float(tau)
-
-
-def chain_rg2(pos, mol_start):
-    """Rg^2 of every chain (simulation.cc:406-434: (1/n^2) sum_{j<k} r_jk^2 on
-    unwrapped coordinates = mean squared distance from the centre of mass)."""
-    import numpy as np
-    sizes = np.diff(mol_start)
-    out = []
-    for n in np.unique(sizes[sizes > 1]):
-        starts = mol_start[:-1][sizes == n]
-        idx = starts[:, None] + np.arange(n)[None, :]
-        x = pos[idx]
-        out.append(((x - x.mean(axis=1, keepdims=True)) ** 2).sum(axis=2).mean(axis=1))
-    return np.concatenate(out)
-
-
 def tau_pooled(X, c=5.0):
     """Integrated autocorrelation time (in samples) of many series at once
     (columns of X): the autocorrelation is averaged over the columns, then
@@ -176,31 +160,16 @@ def tau_pooled(X, c=5.0):
     return float(-1.0 / slope), "exponential fit"
 
 
-def measure_taus(batches, steps_done, mol_start, seconds, every, burn):
-    """tau_int of the chains' Rg^2 (moves per replica) for several batches
-    started from the same configurations: each is first brought to `burn`
-    steps per replica, then all are advanced in turn by `every` steps and
-    sampled, so every series covers the same stretch of its trajectory
-    (the chains still relax from their initial walks, which biases a tau
-    estimate; equal stretches bias them alike)."""
+def paired_check(x, y, k=2.0):
+    """Per-replica means x (chosen form) and y (plain FP64) paired by their
+    starting configuration: the mean difference against k standard errors
+    of the paired differences."""
     import numpy as np
-    for b, done in zip(batches, steps_done):
-        if burn > done:
-            b.run(burn - done)
-    reps = [[b.replica(r) for r in range(b.n)] for b in batches]
-    X = [[] for _ in batches]
-    t_end = time.perf_counter() + seconds
-    while time.perf_counter() < t_end:
-        for i, b in enumerate(batches):
-            b.run(every)
-            X[i].append(np.concatenate([chain_rg2(r.positions(), mol_start) for r in reps[i]]))
-    out = []
-    for x in X:
-        tau, how = tau_pooled(np.array(x))
-        out.append({"tau_moves_per_replica": tau * every, "tau_samples": tau, "method": how,
-                    "samples": len(x), "chains": len(x[0]) if x else 0,
-                    "moves_per_sample": every, "burn_in_moves": burn})
-    return out
+    diff = np.asarray(x, np.float64) - np.asarray(y, np.float64)
+    se = float(diff.std(ddof=1) / math.sqrt(len(diff)))
+    return {"chosen_mean": float(np.mean(x)), "plain_fp64_mean": float(np.mean(y)),
+            "paired_difference": float(diff.mean()), "standard_error": se,
+            "within_2_se": bool(abs(diff.mean()) <= k * se)}
 
 
 def alg_flops_per_move(n_bead, mean_moved, n_k, frac_in_rc, mean_bonds):
@@ -214,6 +183,8 @@ def alg_flops_per_move(n_bead, mean_moved, n_k, frac_in_rc, mean_bonds):
     pairs = mean_moved * (n_bead - 1)
     return (pairs * (20 + 8) + pairs * frac_in_rc * 25 + mean_moved * n_k * 16
             + n_k * 10 + 15 * mean_bonds)
+
+
 
 
 def run_reference_arm(args, rank, world):
@@ -263,16 +234,34 @@ def make_workload(name, seed=20261203):
     return d
 
 
-def make_brush_ensemble(n, seed=20261203):
-    """The confined-brush replicas of uneven size (systems.brush_ensemble)."""
+def make_brush_ensemble(n, seed=20261203, only=None):
+    """The confined-brush replicas of uneven size (systems.brush_ensemble);
+    `only` picks one replica index."""
     from plum_gb300 import systems
     dirs = []
     for i, spec in enumerate(systems.brush_ensemble(n, seed)):
+        if only is not None and i != only:
+            continue
         d = os.path.join(tempfile.gettempdir(), "plum_bench_brush_%d_%d" % (seed, i))
         if not os.path.exists(os.path.join(d, "run.in")):
             systems.write_brush(d, spec, seed=seed + i)
         dirs.append(d)
     return dirs
+
+
+def shipped_surrogate(workload, device, margin):
+    """The surrogate trained for this workload (plum_gb300/data), or None."""
+    import numpy as np
+    wpath = os.path.join(ROOT, "plum_gb300", "data", "surrogate_%s.npz" % workload)
+    if not os.path.exists(wpath):
+        return None, None, wpath
+    from plum_gb300 import surrogate as S
+    sg = S.load(wpath, device=device)
+    sg.set_margin(margin)
+    z = np.load(wpath)
+    meta = {k: (z[k].item() if z[k].ndim == 0 else None) for k in z.files
+            if k not in ("params", "mu", "isd")}
+    return sg, meta, wpath
 
 
 def cbmc_growth_steps(device, reps=200):
@@ -334,53 +323,221 @@ def cpu_baseline_sample(d, moves):
     return moves / t
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="bulk_20000_pinned")
-    ap.add_argument("--moves-per-step", type=int, default=2000)
-    ap.add_argument("--plain-moves-per-step", type=int, default=200)
-    ap.add_argument("--samples-seconds", type=float, default=150.0,
-                    help="seconds of Rg sampling (both forms together) for tau_int (0: skip)")
-    ap.add_argument("--cpu-moves", type=int, default=20)
-    ap.add_argument("--ref-moves", type=int, default=10)
-    ap.add_argument("--tune", default=None,
-                    help="with --only batch: item_pairs,k_tile,grid,min_blocks instead of autotuning")
-    ap.add_argument("--groups", type=int, default=2, choices=[1, 2],
-                    help="step chains per batch (two: halves in two graph branches)")
-    ap.add_argument("--tau-replicas", type=int, default=16,
-                    help="replicas whose chains' Rg^2 series give tau_int")
-    ap.add_argument("--replicas", type=int, default=64,
-                    help="replicas of the workload in the batched form (the chosen form)")
-    ap.add_argument("--batch-steps", type=int, default=256)
-    ap.add_argument("--da-margin", type=float, default=12.0,
-                    help="delayed-acceptance dead zone in k_BT (stage one rejects only moves "
-                         "the surrogate puts above it)")
-    ap.add_argument("--no-surrogate", action="store_true",
-                    help="time the batched precision form without delayed acceptance")
-    ap.add_argument("--only", default=None, choices=[None, "fp32", "fp64", "batch", "cbmc"],
-                    help="profiling runs: time one form only, no baselines or e2e")
-    args = ap.parse_args()
+def precision_on_chain(d, device, n, seed, label):
+    """FP32 against FP64 energy changes on the chain's own proposals: a plain
+    (FP64) and a precision (FP32) context of the same system run the same
+    recorded mt19937 stream with per-step energy-change logs, so they propose
+    the same moves until their first differing decision (a flip; after it the
+    chains diverge and the comparison stops, the flipping proposal included).
+    For uniform u the decisions u < exp(-beta dE32) and u < exp(-beta dE64)
+    differ with probability |min(1, e^{-beta dE32}) - min(1, e^{-beta dE64})|;
+    its mean over the proposals is the expected flip fraction."""
+    import numpy as np
+    import plum_gb300 as pg
+    s64 = pg.System(d, form=pg.FORM_FP64, device=device)
+    s32 = pg.System(d, form=pg.FORM_FP32, device=device)
+    beta = s64.run_params().beta
+    ms = s64.topology()[0]
+    max_len = int(np.diff(ms).max())
+    stream = mt19937_stream(seed, n * (24 + 4 * max_len) + 65536)
+    t0 = time.perf_counter()
+    _, mt64, ac64, _, de64 = s64.run_moves_de(stream, n)
+    _, mt32, ac32, _, de32 = s32.run_moves_de(stream, n)
+    wall = time.perf_counter() - t0
+    same = (mt64 == mt32) & (ac64 == ac32)
+    first = n if same.all() else int(np.argmin(same))
+    k = min(n, first + 1)
+    mt, a, b = mt64[:k], de64[:k], de32[:k]
+    live = (mt >= 0) & np.isfinite(a) & np.isfinite(b)
 
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if args.impl == "reference":
-        return run_reference_arm(args, rank, world)
-    from plum_gb300 import replicas
+    def prob(x):
+        return np.where(x >= 1e8, 0.0, np.exp(-beta * np.maximum(x, 0.0)))
 
+    fin = live & (a < 1e8) & (b < 1e8)
+    err = np.abs(b - a)
+    rel = err / np.maximum(1.0, np.abs(a))
+    flips = np.abs(prob(b) - prob(a))
+    by_kind = {}
+    for kind, name in enumerate(("ion", "com", "pivot", "crankshaft", "reptation")):
+        sel = fin & (mt == kind)
+        if sel.any():
+            by_kind[name] = {"proposals": int(sel.sum()),
+                             "de_abs_err_rms": float(np.sqrt((err[sel] ** 2).mean())),
+                             "de_abs_err_max": float(err[sel].max()),
+                             "de_rel_err_max": float(rel[sel].max()),
+                             "expected_flip_fraction": float(flips[sel].mean())}
+    out = {"system": label, "n_bead": int(s64.n_bead), "proposals": int(live.sum()),
+           "steps_compared": int(k), "first_differing_decision": None if first == n else first,
+           "overlap_agreement": float(((a[live] >= 1e8) == (b[live] >= 1e8)).mean()),
+           "de_abs_err_rms": float(np.sqrt((err[fin] ** 2).mean())) if fin.any() else None,
+           "de_abs_err_max": float(err[fin].max()) if fin.any() else None,
+           "de_rel_err_max": float(rel[fin].max()) if fin.any() else None,
+           "expected_flip_fraction": float(flips[live].mean()) if live.any() else None,
+           "observed_flips": int(first < n), "by_kind": by_kind, "wall_s": wall,
+           "definition": "dE of the FP32 form against the plain FP64 form on the same "
+                         "proposals of one chain (recorded stream); relative error over "
+                         "max(1, |dE64|); flip fraction = mean |p32 - p64| with "
+                         "p = min(1, exp(-beta dE)), 0 at overlap"}
+    s64.close()
+    s32.close()
+    return out
+
+
+def equilibrium(args, device, sg, tune):
+    """Equilibrium statistics of the chosen form on the workload.
+
+    R replicas (the first R of the throughput batch: same starts) are burnt
+    in with the chosen form. From the equilibrated configurations: (a) the
+    chosen form and (b) the plain Metropolis dynamics in the precision form
+    (the plain FP64 form's dynamics: the two decide alike but for the flip
+    fraction measured by precision_on_chain) run side by side, sampled every
+    `every` moves; tau_int of the chains' Rg^2 (pooled over all chains, Sokal
+    window c = 5) and of the total energy for each; (c) R plain FP64 systems
+    run from the same configurations. The chosen form's per-replica means of
+    the total energy and the chain-averaged Rg^2 are compared with the plain
+    FP64 runs' (paired by starting configuration): the mean difference must
+    lie within 2 standard errors of the paired differences."""
+    import numpy as np
+    import plum_gb300 as pg
+    R = args.stat_replicas
+    dirs = [make_workload(args.workload, seed=20261203 + r) for r in range(R)]
+    out = {"replicas": R, "burn_in_moves_per_replica": args.burn}
+    t0 = time.perf_counter()
+    eq = pg.Batch(dirs, device=device)
+    eq.seed(np.arange(9000, 9000 + R, dtype=np.uint32))
+    eq.set_tune(*tune)
+    if sg is not None:
+        eq.set_surrogate(sg)
+    done = 0
+    trace = []
+    while done < args.burn:
+        step = min(args.burn - done, max(args.burn // 20, 1000))
+        eq.run(step)
+        done += step
+        trace.append((done, float(eq.energies().sum(axis=1).mean()),
+                      float(np.mean([eq.replica(r).observables()[0] for r in range(R)]))))
+    snap = [eq.replica(r).positions() for r in range(R)]
+    eq.close()
+    out["burn_in_s"] = time.perf_counter() - t0
+    out["burn_in_trace"] = {"moves": [t[0] for t in trace],
+                            "mean_energy": [t[1] for t in trace],
+                            "mean_rg2": [t[2] for t in trace]}
+
+    def series(net, seed0, moves, every):
+        b = pg.Batch(dirs, device=device)
+        b.seed(np.arange(seed0, seed0 + R, dtype=np.uint32))
+        b.set_tune(*tune)
+        for r in range(R):
+            b.replica(r).set_positions(snap[r])
+        if net is not None:
+            b.set_surrogate(net)
+        reps = [b.replica(r) for r in range(R)]
+        E, G, Gm = [], [], []
+        t1 = time.perf_counter()
+        for _ in range(moves // every):
+            b.run(every)
+            E.append(b.energies().sum(axis=1))
+            rg = [rep.chain_observables()[:, 0] for rep in reps]
+            G.append(np.concatenate(rg))
+            Gm.append([x.mean() for x in rg])
+        wall = time.perf_counter() - t1
+        b.close()
+        return np.array(E), np.array(G), np.array(Gm), wall
+
+    res = {}
+    for name, net, seed0 in (("chosen_form", sg, 11000), ("plain_dynamics_fp32", None, 13000)):
+        E, G, Gm, wall = series(net, seed0, args.tau_moves, args.tau_every)
+        tg, mg = tau_pooled(G)
+        te, me = tau_pooled(E)
+        res[name] = {"tau_rg2_moves": tg * args.tau_every, "tau_rg2_method": mg,
+                     "tau_energy_moves": te * args.tau_every, "tau_energy_method": me,
+                     "samples": int(len(E)), "moves_per_sample": args.tau_every,
+                     "moves_per_replica": int(len(E) * args.tau_every), "chains": int(G.shape[1]),
+                     "wall_s": wall, "mean_energy_per_replica": E.mean(axis=0).tolist(),
+                     "mean_rg2_per_replica": Gm.mean(axis=0).tolist()}
+    out["series"] = res
+
+    # plain FP64 systems from the same starting configurations
+    t1 = time.perf_counter()
+    Ep, Gp = [], []
+    for r in range(R):
+        s = pg.System(dirs[r], form=pg.FORM_FP64, device=device)
+        s.set_positions(snap[r])
+        s.seed(15000 + r)
+        e, g = [], []
+        for _ in range(args.plain_stat_moves // args.plain_stat_every):
+            s.run(args.plain_stat_every)
+            e.append(s.energies().sum())
+            g.append(s.observables()[0])
+        Ep.append(np.mean(e))
+        Gp.append(np.mean(g))
+        s.close()
+    out["plain_fp64"] = {"moves_per_replica": args.plain_stat_moves,
+                         "moves_per_sample": args.plain_stat_every,
+                         "wall_s": time.perf_counter() - t1,
+                         "mean_energy_per_replica": Ep, "mean_rg2_per_replica": Gp}
+    ch = res["chosen_form"]
+    out["stat_check"] = {
+        "energy": paired_check(ch["mean_energy_per_replica"], Ep),
+        "rg2": paired_check(ch["mean_rg2_per_replica"], Gp),
+        "definition": "per-replica means of the chosen form (over its tau series) and of the "
+                      "plain FP64 form, each started from the same equilibrated "
+                      "configuration; the mean paired difference against 2 standard "
+                      "errors of the paired differences"}
+    return out
+
+
+def precision_cases(args, local):
+    """precision_on_chain for the three bulk/confined configurations: the
+    1,000-particle bulk system (reference Ewald rule: multi-image real
+    space), the benchmark workload and the first confined-brush replica."""
+    return [precision_on_chain(make_workload("bulk_1000"), local, args.precision_moves, 21,
+                               "bulk_1000 (10 x 50 chains + 500 ions, L = 40, r_c = 28, 460 k)"),
+            precision_on_chain(make_workload(args.workload), local, args.precision_moves, 22,
+                               args.workload),
+            precision_on_chain(make_brush_ensemble(256, only=0)[0], local,
+                               args.precision_moves, 23,
+                               "brush replica 0 of the 256-replica ensemble")]
+
+
+def profile_case(args, local):
+    """--only MODE: one profiling case, no baselines. Every mode prints one
+    JSON line; the cases with an NVTX range let a profiler select the
+    launches of interest (ncu --nvtx --nvtx-include "<range>/")."""
     import numpy as np
     import torch
     import plum_gb300 as pg
-
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    if args.only in ("fp32", "fp64"):
+        d = make_workload(args.workload)
+        s = pg.System(d, form=pg.FORM_FP32 if args.only == "fp32" else pg.FORM_FP64,
+                      device=local)
+        s.seed(1234)
+        M = args.moves_per_step
+        for _ in range(args.warmup + args.steps):
+            s.run(M)
+        torch.cuda.synchronize()
+        ms, k = s.last_timing()
+        kern = s.time_kernels(min(M, 64))
+        print(json.dumps({"profile_run": args.only, "moves_per_step": M, "last_ms": ms,
+                          "moves_per_s": M / (ms / 1e3),
+                          "kernel_ms_per_launch": {"delta": float(kern[0]),
+                                                   "serial": float(kern[1])}}), flush=True)
+        return 0
+    if args.only == "total":
+        # the full FP64 recompute of one replica of the workload
+        d = make_workload(args.workload)
+        s = pg.System(d, form=pg.FORM_FP32, device=local)
+        for _ in range(3):
+            s.total_energy()
+        torch.cuda.synchronize()
+        t = []
+        for _ in range(max(1, args.steps)):
+            t0 = time.perf_counter()
+            s.total_energy()
+            t.append(time.perf_counter() - t0)
+        print(json.dumps({"profile_run": "total", "workload": args.workload,
+                          "ms_per_recompute": 1e3 * statistics.median(t)}), flush=True)
+        return 0
     if args.only == "batch":
         if args.workload.startswith("brush_"):
             dirs = make_brush_ensemble(int(args.workload.split("_")[1]))
@@ -412,44 +569,183 @@ def main():
                               ("delta", "serial", "descriptor", "inference"),
                               [float(x) for x in b.time_kernels(8)]))}), flush=True)
         return 0
+    if args.only == "chosen":
+        # the measured form: replicas with the shipped surrogate, autotuned
+        # items, two step chains; one batch of 32 steps in the range "chosen"
+        sg, _, _ = shipped_surrogate(args.workload, local, args.da_margin)
+        b = pg.Batch([make_workload(args.workload, seed=20261203 + r)
+                      for r in range(args.replicas)], device=local)
+        b.seed(77)
+        if sg is not None:
+            b.set_surrogate(sg)
+        tune = b.autotune(16)
+        b.set_groups(args.groups)
+        b.run(256)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("chosen")
+        b.run(32)
+        torch.cuda.nvtx.range_pop()
+        ms, k = b.last_timing()
+        print(json.dumps({"profile_run": "chosen", "replicas": args.replicas, "tune": tune,
+                          "ms_per_32_steps": ms, "kernels": k}), flush=True)
+        return 0
+    if args.only == "da":
+        # a small surrogate trained on 6,000 collected moves, then 16
+        # replicas with delayed acceptance: the third batch of 32 steps runs
+        # in the range "da", the same without the surrogate in "plain"
+        from plum_gb300 import surrogate as S
+        d = make_workload(args.workload)
+        desc, de, _ = S.collect(d, 6000, n_ctx=1, moves_per_call=10000)
+        sg, _ = S.fit(desc, de, epochs=5, batch=1024)
+        b = pg.Batch([make_workload(args.workload, seed=20261203 + i) for i in range(16)],
+                     device=local)
+        b.seed(77)
+        res = {}
+        for label, net in (("da", sg), ("plain", None)):
+            b.set_surrogate(net)
+            for i in range(3):
+                if i == 2:
+                    torch.cuda.nvtx.range_push(label)
+                b.run(32)
+                if i == 2:
+                    torch.cuda.nvtx.range_pop()
+            res[label] = b.last_timing()[0]
+        print(json.dumps({"profile_run": "da", "ms_per_32_steps": res}), flush=True)
+        return 0
+    if args.only == "train":
+        # one epoch of surrogate training on 65,536 random descriptors in
+        # batches of 4,096 (range "train"), then one inference pass ("infer")
+        rng = np.random.default_rng(0)
+        x = rng.gamma(2.0, 3.0, size=(65536, 96)).astype(np.float32)
+        t = rng.normal(0.0, 3.0, 65536).astype(np.float32)
+        sg = pg.Surrogate(seed=1)
+        sg.set_norm(x.mean(0), 1.0 / (x.std(0) + 1e-3), 3.0)
+        xd = torch.tensor(x, device="cuda")
+        td = torch.tensor(t, device="cuda")
+        torch.cuda.nvtx.range_push("train")
+        sg.train(xd, td, batch=4096, epochs=1, lr=1e-3)
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.nvtx.range_push("infer")
+        out = sg.predict_device(xd)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        print(json.dumps({"profile_run": "train", "mean_abs_s": float(out.abs().mean())}),
+              flush=True)
+        return 0
+    if args.only == "pressure":
+        # the wall-force pressure of the first brush replica with charged
+        # surface sites (+-0.5): two warm-up evaluations, then `steps` in
+        # the range "pressure"
+        from plum_gb300 import systems
+        spec = systems.brush_ensemble(1, seed=20261203)[0]
+        spec.site_charge = 0.5
+        d = os.path.join(tempfile.gettempdir(), "plum_bench_pressure")
+        if not os.path.exists(os.path.join(d, "run.in")):
+            systems.write_brush(d, spec, seed=20261203)
+        s = pg.System(d, device=local)
+        for _ in range(2):
+            s.pressure_slit()
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("pressure")
+        t0 = time.perf_counter()
+        for _ in range(max(1, args.steps)):
+            s.pressure_slit()
+        dt = (time.perf_counter() - t0) / max(1, args.steps)
+        torch.cuda.nvtx.range_pop()
+        print(json.dumps({"profile_run": "pressure", "n_bead": int(s.n_bead),
+                          "n_kvec": int(s.info.n_kvec), "ms_per_evaluation": 1e3 * dt}),
+              flush=True)
+        return 0
     if args.only == "cbmc":
         print(json.dumps({"profile_run": "cbmc", **cbmc_growth_steps(local)}), flush=True)
         return 0
+    if args.only == "precision":
+        print(json.dumps({"profile_run": "precision",
+                          "cases": precision_cases(args, local)}), flush=True)
+        return 0
+    if args.only == "stats":
+        sg, _, _ = shipped_surrogate(args.workload, local, args.da_margin)
+        tune = tuple(int(x) for x in args.tune.split(",")) if args.tune else (4096, 256, 608, 4)
+        print(json.dumps({"profile_run": "stats", **equilibrium(args, local, sg, tune)}),
+              flush=True)
+        return 0
+    raise SystemExit("unknown profiling mode %r" % args.only)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="bulk_20000_pinned")
+    ap.add_argument("--moves-per-step", type=int, default=2000)
+    ap.add_argument("--plain-moves-per-step", type=int, default=200)
+    ap.add_argument("--cpu-moves", type=int, default=20)
+    ap.add_argument("--ref-moves", type=int, default=10)
+    ap.add_argument("--tune", default=None,
+                    help="item_pairs,k_tile,grid,min_blocks instead of autotuning")
+    ap.add_argument("--groups", type=int, default=2, choices=[1, 2],
+                    help="step chains per batch (two: halves in two graph branches)")
+    ap.add_argument("--replicas", type=int, default=64,
+                    help="replicas of the workload in the batched form (the chosen form)")
+    ap.add_argument("--batch-steps", type=int, default=256)
+    ap.add_argument("--da-margin", type=float, default=12.0,
+                    help="delayed-acceptance dead zone in k_BT (stage one rejects only moves "
+                         "the surrogate puts above it)")
+    ap.add_argument("--no-surrogate", action="store_true",
+                    help="time the batched precision form without delayed acceptance")
+    ap.add_argument("--precision-moves", type=int, default=10000,
+                    help="proposals per configuration for the FP32-vs-FP64 comparison")
+    ap.add_argument("--stats", type=int, default=1, help="0: skip the equilibrium block")
+    ap.add_argument("--stat-replicas", type=int, default=16)
+    ap.add_argument("--burn", type=int, default=500000,
+                    help="burn-in moves per replica (chosen form) before the statistics")
+    ap.add_argument("--tau-moves", type=int, default=750000,
+                    help="moves per replica of each tau series")
+    ap.add_argument("--tau-every", type=int, default=2500)
+    ap.add_argument("--plain-stat-moves", type=int, default=20000,
+                    help="moves per replica of the plain FP64 statistics runs")
+    ap.add_argument("--plain-stat-every", type=int, default=1000)
+    ap.add_argument("--only", default=None,
+                    choices=[None, "fp32", "fp64", "total", "batch", "chosen", "da", "train",
+                             "pressure", "cbmc", "precision", "stats"],
+                    help="profiling runs: one case only, no baselines or e2e")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference_arm(args, rank, world)
+    from plum_gb300 import replicas
+
+    import numpy as np
+    import torch
+    import plum_gb300 as pg
+
+    torch.cuda.set_device(local)
+    if args.only:
+        return profile_case(args, local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     d = make_workload(args.workload)
     M = args.moves_per_step
-    s32 = pg.System(d, form=pg.FORM_FP32, device=local)
-    s64 = pg.System(d, form=pg.FORM_FP64, device=local)
-    info = s32.info
-    s32.seed(1234 + rank)
-    s64.seed(1234 + rank)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
 
-
-    if args.only:
-        s = s32 if args.only == "fp32" else s64
-        for _ in range(args.warmup + args.steps):
-            s.run(M)
-        torch.cuda.synchronize()
-        ms, k = s.last_timing()
-        print(json.dumps({"profile_run": args.only, "moves_per_step": M, "last_ms": ms,
-                          "moves_per_s": M / (ms / 1e3)}), flush=True)
-        return 0
-
-    # the chosen form: replicas of the workload in one batch (precision form)
-    # with delayed acceptance by the learned surrogate when its weights exist
+    # the chosen form: replicas of the workload in one batch (precision form,
+    # FP64 recompute every 1e4 moves per replica) with delayed acceptance by
+    # the learned surrogate when its weights exist
     R, BS = args.replicas, args.batch_steps
-    batch = pg.Batch([make_workload(args.workload, seed=20261203 + r) for r in range(R)],
-                     device=local)
+    dirs = [make_workload(args.workload, seed=20261203 + r) for r in range(R)]
+    batch = pg.Batch(dirs, device=local)
     batch.seed(replicas.replica_seed(rank))
-    sg, sg_meta = None, None
-    wpath = os.path.join(ROOT, "plum_gb300", "data", "surrogate_%s.npz" % args.workload)
-    if os.path.exists(wpath) and not args.no_surrogate:
-        from plum_gb300 import surrogate as S
-        sg = S.load(wpath, device=local)
-        sg.set_margin(args.da_margin)
-        z = np.load(wpath)
-        sg_meta = {k: (z[k].item() if z[k].ndim == 0 else None) for k in z.files
-                   if k not in ("params", "mu", "isd")}
+    sg, sg_meta, wpath = (None, None, None)
+    if not args.no_surrogate:
+        sg, sg_meta, wpath = shipped_surrogate(args.workload, local, args.da_margin)
+    if sg is not None:
         batch.set_surrogate(sg)
     # work-item sizes of the batched energy change, timed on these replicas;
     # then the replicas' step chains in two graph branches (halves)
@@ -457,13 +753,11 @@ def main():
     batch.set_groups(args.groups)
     for _ in range(args.warmup):
         batch.run(BS)
-        s32.run(M)
-        s64.run(args.plain_moves_per_step)
     da0 = np.array(batch.da_stats()) if sg is not None else None
 
     sampler = ClockSampler(local)
     sampler.start()
-    dev_ms, kernels = [], 0
+    dev_ms, kernels, n_rc, rc_ms = [], 0, 0, 0.0
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
@@ -476,11 +770,16 @@ def main():
         ms, k = batch.last_timing()
         dev_ms.append(ms)
         kernels += k
+        _, n, t = batch.drift()
+        n_rc += n
+        rc_ms += t
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     wall = time.perf_counter() - t0
     clocks = sampler.stop()
     value, step_ms = replicas.job_rate(statistics.mean(dev_ms), R * BS, world, dist)
+    drift_tab, _, _ = batch.drift()
+    etot = batch.energies().sum(axis=1)
     da = None
     if sg is not None:
         mv, ps, ac = (np.array(batch.da_stats()) - da0).tolist()
@@ -493,13 +792,34 @@ def main():
         da["descriptor_cell_lists"] = {"replicas": cs[0], "valid_after_timed_steps": cs[1],
                                        "most_beads_that_changed_cell": cs[2],
                                        "capacity_for_them": cs[3]}
+    recompute = {"every_moves_per_replica": 10000, "recomputes_in_timed_steps": n_rc,
+                 "device_ms_in_timed_steps": rc_ms,
+                 "share_of_timed_device_time": rc_ms / max(sum(dev_ms), 1e-9),
+                 "ms_per_recompute": rc_ms / max(n_rc, 1),
+                 "drift_last_max_abs_total": float(np.abs(drift_tab[:, :4].sum(axis=1)).max()),
+                 "drift_max_abs_total": float(drift_tab[:, 4].max()),
+                 "drift_max_rel_total": float((drift_tab[:, 4]
+                                               / np.maximum(1.0, np.abs(etot))).max()),
+                 "recomputes_per_replica_so_far": [int(x) for x in drift_tab[:, 5]]}
+
+    # e2e through the public batch call: every step, every replica's running
+    # energies come back to the host (the result a user samples)
+    e2e_t = []
+    for _ in range(max(3, args.steps // 2)):
+        t1 = time.perf_counter()
+        batch.run(BS)
+        e = batch.energies()
+        e2e_t.append(time.perf_counter() - t1)
+    e2e = R * BS / statistics.mean(e2e_t)
+    e2e_d2h = int(e.nbytes)
+
     # per-kernel CUDA-event durations over a few more steps (plain launches)
     kern_ms = batch.time_kernels(32)
+    batch.close()
 
     # the same replicas (same starts and seeds) without the surrogate:
     # FP32 + batched
-    nb = pg.Batch([make_workload(args.workload, seed=20261203 + r) for r in range(R)],
-                  device=local)
+    nb = pg.Batch(dirs, device=local)
     nb.seed(replicas.replica_seed(rank))
     tune_nb = nb.autotune(16)
     nb.set_groups(args.groups)
@@ -513,64 +833,53 @@ def main():
         nb_ms.append(nb.last_timing()[0])
     batched32 = R * BS / (statistics.mean(nb_ms) / 1e3)
     kern_ms_nb = nb.time_kernels(32)
+    nb.close()
 
-    # Rg decorrelation of both dynamics: delayed acceptance changes the
-    # acceptance of chain moves, hence tau in moves; the plain Metropolis
-    # dynamics is shared by the FP64 and FP32 forms (their decisions differ
-    # with the flip fraction below)
-    # tau_int is a property of one replica's dynamics, not of the batch size:
-    # it is measured on the first TR replicas (same starts and seeds) so the
-    # sampling time yields series many tau long
-    mol_start = s64.topology()[0]
-    tau_da = tau_plain = None
-    TR = min(args.tau_replicas, R)
-    if args.samples_seconds > 0:
-        def tau_batch(net):
-            b = pg.Batch([make_workload(args.workload, seed=20261203 + r) for r in range(TR)],
-                         device=local)
-            b.seed(replicas.replica_seed(rank))
-            b.set_tune(*tune)
-            if net is not None:
-                b.set_surrogate(net)
-            return b
-        if sg is not None:
-            tau_da, tau_plain = measure_taus([tau_batch(sg), tau_batch(None)], [0, 0], mol_start,
-                                             args.samples_seconds, 1000, 20000)
-        else:
-            tau_plain, = measure_taus([tau_batch(None)], [0], mol_start, args.samples_seconds,
-                                      1000, 20000)
-
-    # precision form against FP64 on identical trial moves
-    from plum_gb300 import precision
-    prec = precision.compare(s64, s32, s64.topology()[0], n=200, seed=5)
-    cbmc = cbmc_growth_steps(local)
-
-    # one replica of the precision form alone
-    f_ms = []
-    for _ in range(3):
-        s32.run(M)
-        f_ms.append(s32.last_timing()[0])
-    single32 = M / (statistics.mean(f_ms) / 1e3)
-
-    # plain FP64 on the same system
+    # plain FP64 on one system of the workload: moves/s, per-kernel times and
+    # an e2e through plum_run_moves (recorded stream in, logs out)
+    s64 = pg.System(d, form=pg.FORM_FP64, device=local)
+    s64.seed(1234 + rank)
+    info = s64.info
+    for _ in range(2):
+        s64.run(args.plain_moves_per_step)
     p_ms = []
     for _ in range(max(3, args.steps // 2)):
         s64.run(args.plain_moves_per_step)
         p_ms.append(s64.last_timing()[0])
     plain = args.plain_moves_per_step / (statistics.mean(p_ms) / 1e3)
-
-    # e2e through the C ABI with host buffers (stream in, logs out)
-    n_e2e = M
-    words = n_e2e * (24 + 4 * 100)
-    stream = mt19937_stream(99 + rank, words)
-    e2e_t = []
+    kern64 = s64.time_kernels(64)
+    n64 = args.plain_moves_per_step
+    stream64 = mt19937_stream(99 + rank, n64 * (24 + 4 * 100))
+    s64.run_moves(stream64, n64)
+    t64 = []
     for _ in range(3):
         t1 = time.perf_counter()
-        used, mt, ac, et = s32.run_moves(stream, n_e2e)
-        e2e_t.append(time.perf_counter() - t1)
-    e2e = n_e2e / statistics.median(e2e_t)
-    h2d = stream.nbytes
-    d2h = n_e2e * (4 + 4 + 8)
+        s64.run_moves(stream64, n64)
+        t64.append(time.perf_counter() - t1)
+    e2e64 = n64 / statistics.median(t64)
+    s64.close()
+
+    # one replica of the precision form alone, and its e2e (recorded stream)
+    s32 = pg.System(d, form=pg.FORM_FP32, device=local)
+    s32.seed(1234 + rank)
+    s32.run(M)
+    f_ms = []
+    for _ in range(3):
+        s32.run(M)
+        f_ms.append(s32.last_timing()[0])
+    single32 = M / (statistics.mean(f_ms) / 1e3)
+    stream32 = mt19937_stream(98 + rank, M * (24 + 4 * 100))
+    t32 = []
+    for _ in range(3):
+        t1 = time.perf_counter()
+        s32.run_moves(stream32, M)
+        t32.append(time.perf_counter() - t1)
+    e2e32 = M / statistics.median(t32)
+    s32.close()
+
+    # FP32 against FP64 on the chain's own proposals (configs 0, 1, 2)
+    prec = precision_cases(args, local)
+    cbmc = cbmc_growth_steps(local)
 
     # algorithmic work per move (mean moved beads from the move mix)
     prob = (0.3, 0.1, 0.2, 0.2, 0.2)
@@ -586,19 +895,25 @@ def main():
     # moves that reach the exact change (all of them without the surrogate)
     evaluated = R * (1.0 - (da["exact_evaluations_skipped"] if da else 0.0))
     achieved = W * evaluated / (kern_ms[0] / 1e3) / 1e12
+    achieved64 = W / (kern64[0] / 1e3) / 1e12
 
+    eqm = None
+    if args.stats:
+        eqm = equilibrium(args, local, sg, tune)
     samples = None
-    if tau_plain is not None:
-        tp = tau_plain["tau_moves_per_replica"]
-        td = tau_da["tau_moves_per_replica"] if tau_da else tp
-        chosen = value / (2 * td)
+    if eqm is not None:
+        tc = eqm["series"]["chosen_form"]["tau_rg2_moves"]
+        tp = eqm["series"]["plain_dynamics_fp32"]["tau_rg2_moves"]
+        chosen = value / (2 * tc)
         plain_s = plain / (2 * tp)
-        samples = {"definition": "moves/s / (2 tau_int), tau_int of the chains' Rg^2 in moves per "
-                                 "system (Sokal window, c = 5, autocorrelation pooled over all "
-                                 "chains of %d replicas with the same starts and seeds as the "
-                                 "first %d of the throughput batch)" % (TR, TR),
-                   "tau_replicas": TR,
-                   "tau_plain": tau_plain, "tau_chosen_form": tau_da,
+        samples = {"definition": "moves/s / (2 tau_int), tau_int of the chains' Rg^2 in moves "
+                                 "per system (Sokal window, c = 5, autocorrelation pooled over "
+                                 "all chains of the equilibrium block's replicas, after its "
+                                 "burn-in)",
+                   "tau_chosen_form": {"moves": tc,
+                                       "method": eqm["series"]["chosen_form"]["tau_rg2_method"]},
+                   "tau_plain_dynamics": {"moves": tp, "method": eqm["series"][
+                       "plain_dynamics_fp32"]["tau_rg2_method"]},
                    "plain_fp64_samples_per_s": plain_s,
                    "batched_fp32_samples_per_s": batched32 / (2 * tp),
                    "chosen_form_samples_per_s": chosen,
@@ -615,7 +930,6 @@ def main():
             cpu = {"value": None, "unit": "moves/s", "cores": 1, "kind": "port",
                    "sample": "failed: %s" % e}
 
-    drift = s32.drift()
     line = {
         "metric": METRIC, "value": value, "unit": "moves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
@@ -625,12 +939,14 @@ def main():
                    "real_cutoff": info.real_cutoff, "replicas": R, "steps_per_batch": BS,
                    "moves_per_step": R * BS,
                    "form": "batched replicas, precision form (FP32 pair/k, FP64 S(k) and "
-                           "totals, FP64 recompute every 1e4 moves)" +
+                           "totals), each replica's full FP64 recompute every 1e4 of its "
+                           "moves inside the timed steps" +
                            (", delayed acceptance with the learned surrogate" if sg else ""),
                    "l2": "flushed between steps (256 MB write)", "parallelism": "replicas",
                    "autotuned_items": {"pairs_per_item": tune[0], "k_per_tile": tune[1],
                                        "grid": tune[2], "resident_blocks_per_sm": tune[3]},
                    "step_chains": args.groups},
+        "fp64_recompute": recompute,
         "batched_fp32_no_surrogate": {"value": batched32, "unit": "moves/s",
                                       "ms_per_step": statistics.mean(nb_ms),
                                       "autotuned_items": tune_nb},
@@ -639,28 +955,51 @@ def main():
             "chosen_form": dict(zip(("delta", "serial", "descriptor", "inference"),
                                     [float(x) for x in kern_ms])),
             "no_surrogate": dict(zip(("delta", "serial", "descriptor", "inference"),
-                                     [float(x) for x in kern_ms_nb]))},
-        "precision_vs_fp64": prec,
+                                     [float(x) for x in kern_ms_nb])),
+            "plain_fp64": {"delta": float(kern64[0]), "serial": float(kern64[1])}},
+        "precision_on_chain": prec,
         "cbmc_trials_grand_canonical": cbmc,
-        "single_replica_fp32": {"value": single32, "unit": "moves/s", "moves_per_step": M},
-        "plain_fp64": {"value": plain, "unit": "moves/s",
-                       "moves_per_step": args.plain_moves_per_step},
+        "single_replica_fp32": {"value": single32, "unit": "moves/s", "moves_per_step": M,
+                                "e2e": {"value": e2e32, "unit": "moves/s",
+                                        "h2d_bytes_per_step": int(stream32.nbytes),
+                                        "d2h_bytes_per_step": M * (4 + 4 + 8)}},
+        "plain_fp64": {"value": plain, "unit": "moves/s", "dtype": "f64",
+                       "moves_per_step": args.plain_moves_per_step,
+                       "e2e": {"value": e2e64, "unit": "moves/s",
+                               "h2d_bytes_per_step": int(stream64.nbytes),
+                               "d2h_bytes_per_step": n64 * (4 + 4 + 8),
+                               "path": "plum_run_moves: the recorded mt19937 stream copied in "
+                                       "and per-move logs (type, accept, total energy) copied "
+                                       "out in the timed region"},
+                       "roofline": {"bound": "fp64", "kernel": "k_delta64",
+                                    "achieved": achieved64, "peak": peak64, "unit": "TFLOP/s",
+                                    "frac": achieved64 / peak64,
+                                    "launch_ms": float(kern64[0]),
+                                    "peak_source": "FP64 FMA probe kernel on this GPU"}},
         "speedup_vs_plain_fp64": value / plain,
-        "e2e": {"value": e2e, "unit": "moves/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h),
-                "path": "plum_run_moves: one replica, precision form, recorded mt19937 stream "
-                        "copied in and per-move logs copied out in the timed region"},
+        "e2e": {"value": e2e, "unit": "moves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": e2e_d2h,
+                "path": "plum_batch_run of the chosen form (FP64 recomputes included) and "
+                        "plum_batch_energies every step: all replicas' running energies "
+                        "copied to the host; a Monte Carlo step takes no host input (the "
+                        "replicas' generators and configurations stay on the device; the "
+                        "configurations were uploaded when the batch was created)"},
         "gpu_launches": int(kernels),
         "roofline": {"bound": "fp32", "kernel": "k_batch_delta32",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
+                     "frac": achieved / peak,
+                     "traffic": TRAFFIC_PER_EXACT_MOVE * evaluated,
+                     "traffic_source": "DRAM bytes (dram__bytes_read.sum + dram__bytes_write"
+                                       ".sum) of one ncu capture of this kernel on this "
+                                       "workload, per evaluated move, times the moves one "
+                                       "launch evaluates",
                      "launch_ms": float(kern_ms[0]), "moves_per_launch": evaluated,
                      "peak_source": "FP32 FMA probe kernel on this GPU (measured; the "
                                     "measured-peaks file has no FP32 entry)",
                      "fp64_peak_tflops": peak64,
                      "alg_flops_per_move": W},
+        "equilibrium": eqm,
         "samples": samples,
-        "drift_fp32": {"last": list(drift[:4]), "max_abs_total": drift[4]},
         "cpu_baseline": cpu,
         "clocks": clocks,
         "wall_s": wall,

@@ -181,6 +181,13 @@ int plum_structure_factor(const plum_ctx* ctx, double* sk_out, int* kn_out);
  * RadiusOfGyrationXYZ and EndToEndDistance (simulation.cc:406-500). */
 int plum_observables(const plum_ctx* ctx, double* out);
 
+/* The same per chain (molecules of more than one bead, in molecule order):
+ * out[5 i + q] = {Rg^2, Rg_x^2, Rg_y^2, Rg_z^2, end-to-end^2} of chain i,
+ * the terms plum_observables averages (simulation.cc:406-500). *n_chains
+ * (may be NULL) receives the number of chains; at most cap chains are
+ * written (cap = 0 only reports it). */
+int plum_chain_observables(const plum_ctx* ctx, double* out, int cap, int* n_chains);
+
 /* rho(z) of the current configuration, one sample of Simulation::CalcRhoZ
  * (simulation.cc:1029-1045): bins of 0.02 along z (z wrapped into [0, Lz)),
  * out[3*bin + id] with id 0 for chain beads, 1 for ions with q >= 0, 2 for
@@ -298,6 +305,11 @@ int plum_drift(const plum_ctx* ctx, double* out);
 /* Measured duration (ms) of the last plum_run/plum_run_moves call's device
  * work, and the number of kernels it launched. */
 int plum_last_timing(const plum_ctx* ctx, double* ms, long* kernels);
+/* n_moves more steps of plum_run as plain launches with CUDA events around
+ * each kernel: out2 = mean milliseconds per launch of {energy change,
+ * serial step}. For measurement; the steps count as ordinary steps. No
+ * reference counterpart. */
+int plum_time_kernels(plum_ctx* ctx, int n_moves, double* out2);
 
 /* Measures the FP32 and FP64 FMA throughput of `device` (TFLOP/s, an FMA
  * counted as 2 FLOPs) with a short probe kernel: the roofline denominator of

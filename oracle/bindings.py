@@ -24,7 +24,13 @@ _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _up = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
 
 
-def build(ref_dir: str = "/root/reference", quiet: bool = True) -> None:
+# Where the reference checkout is read from (only to build the checker
+# libplumref.so); PLUM_REF_DIR overrides it. Absent on machines that only run
+# the prebuilt checkers.
+REF_DIR = os.environ.get("PLUM_REF_DIR", "/root/reference")
+
+
+def build(ref_dir: str = REF_DIR, quiet: bool = True) -> None:
     """Runs oracle/Makefile (the reference part only if its sources exist)."""
     out = subprocess.run(["make", "-C", HERE, "-j4", "REF=%s" % ref_dir],
                          capture_output=quiet, text=True)

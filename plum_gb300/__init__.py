@@ -38,6 +38,19 @@ class Info(C.Structure):
                 ("real_cell", C.c_int * 3), ("k_cell", C.c_int * 3)]
 
 
+class RunInfo(C.Structure):
+    """plum_run_info: the run-control items of run.in."""
+    _fields_ = [("steps", C.c_long), ("steps_eq", C.c_long), ("sample_freq", C.c_long),
+                ("stat_out_freq", C.c_long), ("traj_out_freq", C.c_long),
+                ("beta", C.c_double), ("move_size", C.c_double), ("move_prob", C.c_double * 5),
+                ("phantom", C.c_int), ("coion", C.c_int), ("grafted", C.c_int),
+                ("grafted_counterion", C.c_int), ("calc_chem_pot", C.c_int),
+                ("use_pair", C.c_int), ("use_ewald", C.c_int), ("use_bond", C.c_int),
+                ("use_bond_rigid", C.c_int), ("use_ext", C.c_int), ("use_gc", C.c_int),
+                ("gc_freq", C.c_int), ("rigid_bond", C.c_double), ("eq_bond", C.c_double),
+                ("run_name", C.c_char * 256)]
+
+
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _up = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
@@ -141,6 +154,10 @@ def lib():
         L.plum_batch_set_recompute.argtypes = [C.c_void_p, C.c_long]
         L.plum_structure_factor.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.plum_batch_energies.argtypes = [C.c_void_p, _dp]
+        L.plum_time_kernels.argtypes = [C.c_void_p, C.c_int, _dp]
+        L.plum_run_params.argtypes = [C.c_void_p, C.POINTER(RunInfo)]
+        L.plum_chain_observables.argtypes = [C.c_void_p, C.c_void_p, C.c_int,
+                                             C.POINTER(C.c_int)]
         L.plum_batch_drift.argtypes = [C.c_void_p, _dp, C.POINTER(C.c_long),
                                        C.POINTER(C.c_double)]
         _lib = L
@@ -244,6 +261,13 @@ class System:
     def seed(self, seed: int):
         _check(lib().plum_seed(self.h, seed))
 
+    def time_kernels(self, n_moves):
+        """n_moves device steps with CUDA events around each kernel: mean ms
+        per launch of (energy change, serial step)."""
+        o = np.zeros(2)
+        _check(lib().plum_time_kernels(self.h, n_moves, o))
+        return o
+
     def run(self, n_moves):
         acc = C.c_int(0)
         _check(lib().plum_run(self.h, n_moves, C.byref(acc)))
@@ -287,6 +311,20 @@ class System:
         o = np.zeros(5)
         _check(lib().plum_observables(self.h, o))
         return o
+
+    def run_params(self) -> RunInfo:
+        """The run-control items of run.in (beta, move_size, move_prob, ...)."""
+        o = RunInfo()
+        _check(lib().plum_run_params(self.h, C.byref(o)))
+        return o
+
+    def chain_observables(self):
+        """[chains, 5] per chain: Rg^2, Rg_x^2, Rg_y^2, Rg_z^2, end-to-end^2."""
+        n = C.c_int(0)
+        _check(lib().plum_chain_observables(self.h, None, 0, C.byref(n)))
+        o = np.zeros((max(n.value, 1), 5))
+        _check(lib().plum_chain_observables(self.h, _ptr(o), n.value, C.byref(n)))
+        return o[:n.value]
 
     def structure_factor(self):
         """(S(k) [n_kvec] complex, k [n_kvec, 3] integer components): the

@@ -106,6 +106,12 @@ struct plum_ctx {
   int g_moves = 0;
   DevBuffers g_B;
   bool g_warm = false;
+  // per-kernel timing (plum_time_kernels): while set, the step loop runs as
+  // plain launches with events around each energy-change (kind 0) and
+  // serial (kind 1) launch
+  bool kt_on = false;
+  std::vector<cudaEvent_t> kt_ev;
+  std::vector<int> kt_kind;
 };
 
 namespace {
@@ -313,6 +319,15 @@ void launch_delta(const plum_ctx* c, const DevBuffers& B) {
     launch_delta_pairs64(c->P, B, c->s);
 }
 
+// Records an event on the context's stream for per-kernel timing.
+void kt_mark(plum_ctx* c, int kind) {
+  cudaEvent_t e;
+  if (cudaEventCreate(&e) != cudaSuccess) return;
+  cudaEventRecord(e, c->s);
+  c->kt_ev.push_back(e);
+  c->kt_kind.push_back(kind);
+}
+
 void enqueue_loop(plum_ctx* c, int n_moves, const DevBuffers& B) {
   // with a training log, each generated chain move's descriptor is taken
   // before its energy change
@@ -320,9 +335,12 @@ void enqueue_loop(plum_ctx* c, int n_moves, const DevBuffers& B) {
   launch_serial64(c->P, B, kModeGen, c->s);
   if (desc) launch_desc_batch(c->d_rp1, c->d_rb1, 1, B.desc_acc, c->P.form, 0, c->s);
   for (int i = 0; i < n_moves; i++) {
+    if (c->kt_on) kt_mark(c, 0);
     launch_delta(c, B);
+    if (c->kt_on) kt_mark(c, 1);
     int mode = kModeFinish | kModeDecide | (i + 1 < n_moves ? kModeGen : 0);
     launch_serial64(c->P, B, mode, c->s);
+    if (c->kt_on) kt_mark(c, 2);
     if (desc && i + 1 < n_moves)
       launch_desc_batch(c->d_rp1, c->d_rb1, 1, B.desc_acc, c->P.form, 0, c->s);
   }
@@ -336,6 +354,12 @@ void enqueue_loop(plum_ctx* c, int n_moves, const DevBuffers& B) {
 int device_loop(plum_ctx* c, int n_moves, DevBuffers B) {
   const long k = 1 + 2L * n_moves + (B.log_desc ? n_moves : 0);
   if (B.log_desc) CK(cudaMemcpyAsync(c->d_rb1, &B, sizeof(B), cudaMemcpyHostToDevice, c->s));
+  if (c->kt_on) {
+    enqueue_loop(c, n_moves, B);
+    CK(cudaGetLastError());
+    c->last_kernels += k;
+    return PLUM_OK;
+  }
   const bool same = c->gexec && c->g_moves == n_moves && !std::memcmp(&c->g_B, &B, sizeof(B));
   if (same) {
     CK(cudaGraphLaunch(c->gexec, c->s));
@@ -674,6 +698,7 @@ int plum_ctx_destroy(plum_ctx* c) {
   if (c->h_out) cudaFreeHost(c->h_out);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  for (cudaEvent_t e : c->kt_ev) cudaEventDestroy(e);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->s) cudaStreamDestroy(c->s);
   delete c;
@@ -1127,6 +1152,32 @@ int plum_run(plum_ctx* c, int n_moves, int* accepted_out) {
   return PLUM_OK;
 }
 
+int plum_time_kernels(plum_ctx* c, int n_moves, double* out2) {
+  if (!c || n_moves <= 0 || !out2) return fail(PLUM_ERR_INPUT, "bad argument");
+  c->kt_on = true;
+  for (cudaEvent_t e : c->kt_ev) cudaEventDestroy(e);
+  c->kt_ev.clear();
+  c->kt_kind.clear();
+  int rc = plum_run(c, n_moves, nullptr);
+  c->kt_on = false;
+  double sum[2] = {0, 0};
+  int cnt[2] = {0, 0};
+  for (size_t i = 0; i + 1 < c->kt_ev.size(); i++) {
+    const int kind = c->kt_kind[i];
+    if (kind > 1 || c->kt_kind[i + 1] != kind + 1) continue;
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, c->kt_ev[i], c->kt_ev[i + 1]) != cudaSuccess) continue;
+    sum[kind] += ms;
+    cnt[kind]++;
+  }
+  for (cudaEvent_t e : c->kt_ev) cudaEventDestroy(e);
+  c->kt_ev.clear();
+  c->kt_kind.clear();
+  if (rc) return rc;
+  for (int q = 0; q < 2; q++) out2[q] = cnt[q] ? sum[q] / cnt[q] : 0.0;
+  return PLUM_OK;
+}
+
 int plum_get_positions(const plum_ctx* cc, double* xyz) {
   plum_ctx* c = const_cast<plum_ctx*>(cc);
   if (!c || !xyz) return fail(PLUM_ERR_INPUT, "null argument");
@@ -1295,6 +1346,30 @@ int plum_observables(const plum_ctx* cc, double* out) {
   CK(cudaMemcpyAsync(c->h_out, c->d_out + 32, sizeof(double) * 5, cudaMemcpyDeviceToHost, c->s));
   CK(cudaStreamSynchronize(c->s));
   std::memcpy(out, c->h_out, sizeof(double) * 5);
+  return PLUM_OK;
+}
+
+int plum_chain_observables(const plum_ctx* cc, double* out, int cap, int* n_chains) {
+  plum_ctx* c = const_cast<plum_ctx*>(cc);
+  if (!c || (!out && cap > 0) || cap < 0) return fail(PLUM_ERR_INPUT, "bad argument");
+  const Input& in = c->in;
+  int n = 0;
+  for (int m = 0; m < in.n_mol; m++) n += in.mol_start[m + 1] - in.mol_start[m] > 1;
+  if (n_chains) *n_chains = n;
+  if (cap == 0) return PLUM_OK;
+  cudaSetDevice(c->device);
+  launch_observables64(c->P, c->B, c->d_obs_per, c->d_out + 32, c->s);
+  CK(cudaGetLastError());
+  std::vector<double> per(5 * (size_t)in.n_mol);
+  CK(cudaMemcpyAsync(per.data(), c->d_obs_per, sizeof(double) * per.size(),
+                     cudaMemcpyDeviceToHost, c->s));
+  CK(cudaStreamSynchronize(c->s));
+  int i = 0;
+  for (int m = 0; m < in.n_mol && i < cap; m++) {
+    if (in.mol_start[m + 1] - in.mol_start[m] <= 1) continue;
+    for (int q = 0; q < 5; q++) out[5 * i + q] = per[5 * (size_t)m + q];
+    i++;
+  }
   return PLUM_OK;
 }
 

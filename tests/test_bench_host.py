@@ -1,5 +1,5 @@
 """Host-side measurement helpers of bench.py: the pooled integrated
-autocorrelation time and the per-chain Rg^2 (CPU only)."""
+autocorrelation time and the paired 2-SE check (CPU only)."""
 import os
 import sys
 
@@ -22,15 +22,15 @@ def test_pooled_tau_of_ar1_series():
     assert how == "sokal" and abs(tau - want) < 0.1 * want, (tau, want)
 
 
-def test_chain_rg2_matches_the_reference_definition():
+def test_paired_check():
+    """Same mean: the difference of paired means lies within 2 SE; a shift of
+    10 SE is flagged."""
     rng = np.random.default_rng(1)
-    pos = rng.normal(size=(35, 3)) * 3
-    mol_start = np.array([0, 10, 20, 21, 22, 35])  # chains of 10, 10, 13 and two ions
-    got = bench.chain_rg2(pos, mol_start)
-    want = []
-    for a, b in ((0, 10), (10, 20), (22, 35)):
-        x = pos[a:b]
-        n = len(x)
-        d = ((x[:, None, :] - x[None, :, :]) ** 2).sum(axis=2)
-        want.append(d[np.triu_indices(n, 1)].sum() / n ** 2)
-    np.testing.assert_allclose(np.sort(got), np.sort(want), rtol=1e-12)
+    start = rng.normal(size=64) * 5.0        # what each pair shares
+    x = start + rng.normal(size=64)
+    y = start + rng.normal(size=64)
+    ok = bench.paired_check(x, y)
+    assert ok["within_2_se"] and abs(ok["paired_difference"]) < 2 * ok["standard_error"]
+    assert ok["standard_error"] < 0.3  # pairing removes the shared spread
+    bad = bench.paired_check(x + 10 * ok["standard_error"], y)
+    assert not bad["within_2_se"]

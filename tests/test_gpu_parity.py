@@ -129,3 +129,29 @@ def test_bad_input_is_an_error(pg, tmp_path):
     with pytest.raises(pg.PlumError) as ei:
         pg.System(str(tmp_path))
     assert ei.value.code == 1
+
+
+@pytest.mark.parametrize("case", ["bulk_small", "slab_wca", "bulk_1000"])
+def test_chain_observables_match_the_definition(pg, case):
+    """Per-chain Rg^2 (simulation.cc:406-434: (1/n^2) sum_{j<k} r_jk^2 on the
+    unwrapped coordinates) and end-to-end^2 from the device against numpy on
+    the same positions, and their chain average against plum_observables."""
+    d, _ = load(case)
+    s = pg.System(d)
+    s.seed(3)
+    s.run(300)
+    pos = s.positions()
+    ms = s.topology()[0]
+    got = s.chain_observables()
+    want = []
+    for m in range(len(ms) - 1):
+        x = pos[ms[m]:ms[m + 1]]
+        n = len(x)
+        if n < 2:
+            continue
+        dd = ((x[:, None, :] - x[None, :, :]) ** 2).sum(axis=2)
+        want.append((dd[np.triu_indices(n, 1)].sum() / n ** 2, ((x[0] - x[-1]) ** 2).sum()))
+    want = np.array(want)
+    np.testing.assert_allclose(got[:, 0], want[:, 0], rtol=1e-12)
+    np.testing.assert_allclose(got[:, 4], want[:, 1], rtol=1e-12)
+    np.testing.assert_allclose(got[:, 0].mean(), s.observables()[0], rtol=1e-12)

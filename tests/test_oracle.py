@@ -92,7 +92,12 @@ def test_malformed_runin_is_an_error_not_a_hang(built, tmp_path):
         built.Oracle(str(tmp_path))
 
 
-REF_EXAMPLES = "/root/reference/examples"
+def _ref_dir():
+    from oracle import bindings as ob
+    return ob.REF_DIR
+
+
+REF_EXAMPLES = os.path.join(_ref_dir(), "examples")
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_EXAMPLES), reason="reference checkout absent")
@@ -116,7 +121,8 @@ def test_reference_examples_live(built, example, tmp_path):
     np.testing.assert_allclose(et2, et1, rtol=1e-10, atol=1e-9)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/src"), reason="reference checkout absent")
+@pytest.mark.skipif(not os.path.isdir(os.path.join(_ref_dir(), "src")),
+                    reason="reference checkout absent")
 def test_fresh_seeded_system_live(built, tmp_path):
     """A freshly generated system (not a committed fixture), reference vs oracle."""
     if not built.have_ref():
