@@ -357,6 +357,7 @@ def precision_on_chain(d, device, n, seed, label):
     err = np.abs(b - a)
     rel = err / np.maximum(1.0, np.abs(a))
     flips = np.abs(prob(b) - prob(a))
+    rel_sel = fin & (np.abs(a) <= 30.0 / beta)
     by_kind = {}
     for kind, name in enumerate(("ion", "com", "pivot", "crankshaft", "reptation")):
         sel = fin & (mt == kind)
@@ -373,6 +374,15 @@ def precision_on_chain(d, device, n, seed, label):
            "de_abs_err_max": float(err[fin].max()) if fin.any() else None,
            "de_rel_err_max": float(rel[fin].max()) if fin.any() else None,
            "expected_flip_fraction": float(flips[live].mean()) if live.any() else None,
+           # the proposals whose decision can go either way (|dE64| <= 30 kT:
+           # acceptance probability above 1e-13); the errors above include
+           # overlapping chain moves with dE near 1e7, where 1e-6 relative is
+           # tens of kT but the acceptance probability is nil
+           "relevant": {"proposals": int(rel_sel.sum()),
+                        "de_abs_err_rms": float(np.sqrt((err[rel_sel] ** 2).mean()))
+                        if rel_sel.any() else None,
+                        "de_abs_err_max": float(err[rel_sel].max()) if rel_sel.any() else None,
+                        "definition": "proposals with |dE64| <= 30 / beta"},
            "observed_flips": int(first < n), "by_kind": by_kind, "wall_s": wall,
            "definition": "dE of the FP32 form against the plain FP64 form on the same "
                          "proposals of one chain (recorded stream); relative error over "
@@ -552,6 +562,8 @@ def profile_case(args, local):
             b.set_tune(*tune)
         else:
             tune = b.autotune(8)
+        if args.real_term != "auto":
+            b.set_real_term(args.real_term == "table")
         for _ in range(args.warmup):
             b.run(args.batch_steps)
         ms_all = []
@@ -565,6 +577,7 @@ def profile_case(args, local):
                           "steps": args.batch_steps, "ms_per_batch": ms,
                           "moves_per_s": len(dirs) * args.batch_steps / (ms / 1e3),
                           "autotuned_items": tune, "setup_s": setup_s,
+                          "real_term": "table" if b.real_term() else "erfc fit",
                           "kernel_ms_per_launch": dict(zip(
                               ("delta", "serial", "descriptor", "inference"),
                               [float(x) for x in b.time_kernels(8)]))}), flush=True)
@@ -707,6 +720,9 @@ def main():
     ap.add_argument("--plain-stat-moves", type=int, default=20000,
                     help="moves per replica of the plain FP64 statistics runs")
     ap.add_argument("--plain-stat-every", type=int, default=1000)
+    ap.add_argument("--real-term", default="auto", choices=["auto", "table", "fit"],
+                    help="real-space term of the batched kernel: the autotuner's pick, the "
+                         "h(u) table or the erfc fit")
     ap.add_argument("--only", default=None,
                     choices=[None, "fp32", "fp64", "total", "batch", "chosen", "da", "train",
                              "pressure", "cbmc", "precision", "stats"],
@@ -750,6 +766,9 @@ def main():
     # work-item sizes of the batched energy change, timed on these replicas;
     # then the replicas' step chains in two graph branches (halves)
     tune = batch.autotune(16)
+    if args.real_term != "auto":
+        batch.set_real_term(args.real_term == "table")
+    real_term = "table" if batch.real_term() else "erfc fit"
     batch.set_groups(args.groups)
     for _ in range(args.warmup):
         batch.run(BS)
@@ -944,7 +963,8 @@ def main():
                            (", delayed acceptance with the learned surrogate" if sg else ""),
                    "l2": "flushed between steps (256 MB write)", "parallelism": "replicas",
                    "autotuned_items": {"pairs_per_item": tune[0], "k_per_tile": tune[1],
-                                       "grid": tune[2], "resident_blocks_per_sm": tune[3]},
+                                       "grid": tune[2], "resident_blocks_per_sm": tune[3],
+                                       "real_space_term": real_term},
                    "step_chains": args.groups},
         "fp64_recompute": recompute,
         "batched_fp32_no_surrogate": {"value": batched32, "unit": "moves/s",

@@ -383,6 +383,28 @@ int plum_batch_set_tune(plum_batch* batch, int item_pairs, int k_tile, int grid,
  * register budgets {2, 3, 4} blocks per SM, keeps the fastest; out4 (may be
  * NULL) = the chosen {item_pairs, k_tile, grid, min_blocks}. */
 int plum_batch_autotune(plum_batch* batch, int steps, int* out4);
+/* The real-space Ewald term of the batched energy change: table = 1 (the
+ * default where it applies) evaluates erfc(sqrt(alpha) r)/r as
+ * sqrt(alpha) h(alpha r^2) from a table of h(u) = erfc(sqrt u)/sqrt u (cubic
+ * pieces, 32 per octave of u, about 1e-7 relative below u = 4), for LJ +
+ * Ewald replicas whose real cut-off is at most half the box; table = 0 uses
+ * the FP32 erfc fit everywhere. PLUM_ERR_INPUT if a replica's alpha r_c^2 is
+ * past the table (2^5). plum_batch_autotune keeps whichever is faster at the
+ * sizes it picks; plum_batch_real_term reports the current choice. */
+int plum_batch_set_real_term(plum_batch* batch, int table);
+int plum_batch_real_term(const plum_batch* batch);
+/* The h(u) table itself (host copy, built like the batch's): out[4 b + q] =
+ * coefficient q of bin b, at most cap bins; returns the number of bins. For
+ * checks of its accuracy. */
+int plum_h32_table(float* out, int cap);
+/* The FP64 table every form's FP64 real-space term uses (erfc(sqrt(alpha)
+ * r)/r = sqrt(alpha) h(alpha r^2), h(u) = erfc(sqrt u)/sqrt u): 32 bins per
+ * octave of u from 2^-12 to 2^5, a degree-8 polynomial in the bin-local
+ * y in [-1/2, 1/2) per bin, out[10 b + q] = coefficient q of bin b (q = 9
+ * is 0), at most cap bins; returns the number of bins. About 2e-16
+ * relative below u = 8. For checks of its accuracy; no reference
+ * counterpart (the reference calls erfc, potential_ewald_coul.cc:134-164). */
+int plum_h64_table(double* out, int cap);
 /* The surrogate descriptor's cell lists (on by default for replicas of the
  * precision form periodic on every axis with at least 3 cells of 7.5 sigma
  * per axis). Off, every replica takes the all-pairs descriptor kernel; the

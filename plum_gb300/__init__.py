@@ -155,6 +155,10 @@ def lib():
         L.plum_structure_factor.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.plum_batch_energies.argtypes = [C.c_void_p, _dp]
         L.plum_time_kernels.argtypes = [C.c_void_p, C.c_int, _dp]
+        L.plum_batch_set_real_term.argtypes = [C.c_void_p, C.c_int]
+        L.plum_batch_real_term.argtypes = [C.c_void_p]
+        L.plum_h32_table.argtypes = [C.c_void_p, C.c_int]
+        L.plum_h64_table.argtypes = [C.c_void_p, C.c_int]
         L.plum_run_params.argtypes = [C.c_void_p, C.POINTER(RunInfo)]
         L.plum_chain_observables.argtypes = [C.c_void_p, C.c_void_p, C.c_int,
                                              C.POINTER(C.c_int)]
@@ -162,6 +166,24 @@ def lib():
                                        C.POINTER(C.c_double)]
         _lib = L
     return _lib
+
+
+def h32_table():
+    """[bins, 4] cubic coefficients of the FP32 h(u) = erfc(sqrt u)/sqrt u
+    table (bins of 1/32 octave from u = 2^-14 to 2^5)."""
+    n = lib().plum_h32_table(None, 0)
+    out = np.zeros(4 * n, np.float32)
+    lib().plum_h32_table(_ptr(out), n)
+    return out.reshape(n, 4)
+
+
+def h64_table():
+    """[bins, 10] degree-8 coefficients (and a zero) of the FP64 h(u) table
+    (bins of 1/32 octave from u = 2^-12 to 2^5)."""
+    n = lib().plum_h64_table(None, 0)
+    out = np.zeros(10 * n, np.float64)
+    lib().plum_h64_table(_ptr(out), n)
+    return out.reshape(n, 10)
 
 
 def probe_peaks(device: int = 0):
@@ -610,6 +632,14 @@ class Batch:
         o = np.zeros((self.n, 4))
         _check(lib().plum_batch_energies(self.h, o))
         return o
+
+    def set_real_term(self, table=True):
+        """Real-space Ewald term from the h(u) table (True) or the erfc fit."""
+        _check(lib().plum_batch_set_real_term(self.h, 1 if table else 0))
+
+    def real_term(self):
+        """1: the h(u) table, 0: the erfc fit."""
+        return int(lib().plum_batch_real_term(self.h))
 
     def set_recompute(self, every):
         """Full FP64 recompute of each replica every `every` of its moves

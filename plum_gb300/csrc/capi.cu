@@ -58,7 +58,9 @@ struct plum_ctx {
   // scratch
   double* d_tot_part = nullptr;
   int n_tot_part = 0;
-  double2* d_sk_part = nullptr;  // [kSkGroupsTotal][n_k] partial S(k) of a recompute
+  double2* d_sk_part = nullptr;
+  float4* d_htab = nullptr;      // FP32 h(u) table (precision form)
+  double* d_htab64 = nullptr;    // FP64 h(u) table  // [kSkGroupsTotal][n_k] partial S(k) of a recompute
   double* d_out = nullptr;     // small result block
   double* d_obs_per = nullptr;  // [n_mol * 5] per-molecule Rg / Ree sums
   double* d_press = nullptr;    // wall-force pressure partials and sums
@@ -146,6 +148,7 @@ int setup_ewald(plum_ctx* c, std::vector<short4>* kn, std::vector<double>* kw) {
   P.single_image = rc <= 0.5 * E.ebox[0] && rc <= 0.5 * E.ebox[1] && rc <= 0.5 * E.ebox[2];
   P.lB = in.lB;
   P.sqrt_alpha = std::sqrt(in.alpha);
+  P.alpha = in.alpha;
   P.kpref = in.lB / (kPiRef * vol) * (4 * kPiRef * kPiRef);
   P.self_coef = -in.lB * std::sqrt(in.alpha / kPiRef);
   P.dip_coef = in.lB * 2 * kPiRef / (vol / 1.0);
@@ -578,6 +581,8 @@ static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out) {
   P.form = form;
   for (int a = 0; a < 3; a++) {
     P.f_scale[a] = (float)(P.ebox[a] / 4294967296.0);
+    P.same_wrap = (a == 0 ? 1 : P.same_wrap) &&
+                  (a >= P.npbc || (P.box[a] == P.ebox[a] && P.inv_box[a] == P.inv_ebox[a]));
     P.inv_fix[a] = 4294967296.0 / P.ebox[a];
     P.f_box[a] = (float)P.ebox[a];
   }
@@ -637,6 +642,31 @@ static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out) {
   c->rhoz_bins = (int)std::ceil(in.box[2] / kRhoZRes);
   rc |= dalloc(&c->d_rhoz, 3 * (size_t)std::max(1, c->rhoz_bins));
   rc |= dalloc(&c->d_mt, 625);
+  // the FP64 real-space term from the h(u) table (every form: the plain
+  // form's moves, the from-scratch energies, the FP64 trial energies)
+  P.htab64 = nullptr;
+  if (P.use_ewald) {
+    rc |= dalloc(&c->d_htab64, (size_t)kH64Bins * kH64Stride);
+    if (!rc) {
+      std::vector<double> h((size_t)kH64Bins * kH64Stride);
+      build_h64_table(h.data());
+      cudaMemcpy(c->d_htab64, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice);
+      P.htab64 = c->d_htab64;
+    }
+  }
+  // the precision form's real-space term from the h(u) table where the
+  // cut-off lies inside it (alpha r_c^2 < 2^kH32EHi)
+  P.htab = nullptr;
+  if (form == PLUM_FORM_FP32 && P.use_ewald &&
+      P.sqrt_alpha * P.sqrt_alpha * P.real_cut * P.real_cut < std::ldexp(1.0, kH32EHi)) {
+    rc |= dalloc(&c->d_htab, kH32Bins);
+    if (!rc) {
+      std::vector<float4> h(kH32Bins);
+      build_h32_table(h.data());
+      cudaMemcpy(c->d_htab, h.data(), sizeof(float4) * kH32Bins, cudaMemcpyHostToDevice);
+      P.htab = c->d_htab;
+    }
+  }
   if (rc) {
     plum_ctx_destroy(c);
     return PLUM_ERR_CUDA;
@@ -692,7 +722,7 @@ int plum_ctx_destroy(plum_ctx* c) {
                   c->cb_part,    c->cb_u,      c->d_obs_per, c->d_rhoz, c->desc_acc,
                   c->d_rp1,      c->d_rb1,     c->desc_fine, c->cb_part32, c->cb_ticket,
                   c->d_stream,   c->d_mt,      c->d_log_type, c->d_log_acc, c->d_log_e,
-                  c->d_press,    c->d_sk_part, c->d_log_de};
+                  c->d_press,    c->d_sk_part, c->d_log_de, c->d_htab, c->d_htab64};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_out) cudaFreeHost(c->h_out);
@@ -1792,7 +1822,9 @@ struct plum_batch {
   int* d_item_off = nullptr;
   double* d_slots = nullptr;
   size_t kt_smem = 0;
-  BatchTune tune{4096, 128, 0, 2};
+  BatchTune tune{4096, 128, 0, 2, 1};
+  float4* d_htab = nullptr;  // h(u) table of the real-space term (kH32Bins)
+  bool htab_ok = false;      // every replica's alpha r_c^2 lies inside the table
   // per-replica streams
   std::vector<long long> cap, per_step;
   uint32_t** d_states = nullptr;
@@ -1945,7 +1977,7 @@ void chain_enqueue(plum_batch* b, int steps, int r0, int n, double* slots, int* 
   launch_batch_serial(rp, rb, item_off, slots, n, kModeGen, st);
   stage_one();
   for (int i = 0; i < steps; i++) {
-    launch_batch_delta32(rp, rb, n, item_off, slots, b->kt_smem, b->tune, queue, st);
+    launch_batch_delta32(rp, rb, n, item_off, slots, b->kt_smem, b->tune, queue, b->d_htab, st);
     int mode = kModeFinish | kModeDecide | (i + 1 < steps ? kModeGen : 0);
     launch_batch_serial(rp, rb, item_off, slots, n, mode, st);
     if (i + 1 < steps) stage_one();
@@ -2072,7 +2104,8 @@ int plum_batch_destroy(plum_batch* b) {
   for (plum_ctx* c : b->reps) plum_ctx_destroy(c);
   void* ptrs[] = {b->d_cells, b->d_queue, b->d_slots2, b->d_rp,    b->d_rb,  b->d_item_off, b->d_slots, b->d_states, b->d_outs,
                   b->d_sts,   b->d_pos, b->d_len,      b->d_cap,   b->d_gather, b->d_need,
-                  b->d_desc,  b->d_err, b->d_fine,     b->d_drift,  b->d_energies};
+                  b->d_desc,  b->d_err, b->d_fine,     b->d_drift,  b->d_energies,
+                  b->d_htab};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t e : b->rc_ev) cudaEventDestroy(e);
@@ -2176,11 +2209,27 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
   rc |= dalloc(&b->d_slots2, 2 * (size_t)items + 2);
   rc |= dalloc(&b->d_drift, 6 * (size_t)n);
   rc |= dalloc(&b->d_energies, 4 * (size_t)n);
+  rc |= dalloc(&b->d_htab, kH32Bins);
   if (rc) {
     plum_batch_destroy(b);
     return PLUM_ERR_CUDA;
   }
   cudaMemset(b->d_drift, 0, sizeof(double) * 6 * n);
+  {
+    // the h(u) table covers u = alpha r^2 < 2^kH32EHi; a replica whose
+    // cut-off reaches past it keeps the erfc fit for the whole batch
+    std::vector<float4> h(kH32Bins);
+    build_h32_table(h.data());
+    cudaMemcpy(b->d_htab, h.data(), sizeof(float4) * kH32Bins, cudaMemcpyHostToDevice);
+    b->htab_ok = true;
+    for (int r = 0; r < n; r++) {
+      const DevParams& P = hp[r];
+      if (P.use_ewald && P.sqrt_alpha * P.sqrt_alpha * P.real_cut * P.real_cut >=
+                             std::ldexp(1.0, kH32EHi))
+        b->htab_ok = false;
+    }
+    b->tune.htab = b->htab_ok ? 1 : 0;
+  }
   b->rc_since.resize(n);
   for (int r = 0; r < n; r++) b->rc_since[r] = (long)((long long)r * b->rc_every / n);
   cudaMemset(b->d_err, 0, sizeof(int));
@@ -2409,7 +2458,7 @@ int plum_batch_time_kernels(plum_batch* b, int n_steps, double* out4) {
   for (int i = 0; i < n_steps && !rc; i++) {
     rc = timed(0, [&] {
       launch_batch_delta32(b->d_rp, b->d_rb, R, b->d_item_off, b->d_slots, b->kt_smem, b->tune,
-                         b->d_queue, b->s);
+                         b->d_queue, b->d_htab, b->s);
     });
     const int mode = kModeFinish | kModeDecide | (i + 1 < n_steps ? kModeGen : 0);
     if (!rc)
@@ -2439,7 +2488,7 @@ int plum_batch_set_tune(plum_batch* b, int item_pairs, int k_tile, int grid, int
   if (!b || item_pairs < kMinItemPairs || item_pairs % 256 || k_tile < kMinKTile ||
       k_tile > kPairThreads || grid < 0 || grid > 65535 || min_blocks < 2 || min_blocks > 4)
     return fail(PLUM_ERR_INPUT, "bad work-item sizes");
-  b->tune = BatchTune{item_pairs, k_tile, grid, min_blocks};
+  b->tune = BatchTune{item_pairs, k_tile, grid, min_blocks, b->tune.htab};
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   b->gexec = nullptr;
   b->g_steps = 0;
@@ -2534,7 +2583,7 @@ int plum_batch_autotune(plum_batch* b, int steps, int* out4) {
     for (int ip : pairs)
       for (int kt : ktiles)
         for (int ps : per_sm) {
-          b->tune = BatchTune{ip, kt, ps * sms, mb};
+          b->tune = BatchTune{ip, kt, ps * sms, mb, b->htab_ok ? 1 : 0};
           double ms[4];
           int rc = plum_batch_time_kernels(b, steps, ms);
           if (rc) return rc;
@@ -2543,6 +2592,16 @@ int plum_batch_autotune(plum_batch* b, int steps, int* out4) {
             pick = b->tune;
           }
         }
+  if (pick.htab) {
+    // the erfc fit at the chosen sizes, kept if it is faster
+    b->tune = pick;
+    b->tune.htab = 0;
+    double ms[4];
+    int rc = plum_batch_time_kernels(b, steps, ms);
+    if (rc) return rc;
+    if (ms[0] < best) pick = b->tune;
+  }
+  b->tune.htab = pick.htab;
   int rc = plum_batch_set_tune(b, pick.item_pairs, pick.k_tile, pick.grid, pick.min_blocks);
   if (rc) return rc;
   if (out4) {
@@ -2552,6 +2611,39 @@ int plum_batch_autotune(plum_batch* b, int steps, int* out4) {
     out4[3] = pick.min_blocks;
   }
   return PLUM_OK;
+}
+
+int plum_batch_set_real_term(plum_batch* b, int table) {
+  if (!b) return fail(PLUM_ERR_INPUT, "null batch");
+  if (table && !b->htab_ok)
+    return fail(PLUM_ERR_INPUT, "a replica's real-space cut-off lies outside the h(u) table");
+  b->tune.htab = table ? 1 : 0;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->g_steps = 0;
+  return PLUM_OK;
+}
+
+int plum_batch_real_term(const plum_batch* b) { return b ? b->tune.htab : -1; }
+
+int plum_h64_table(double* out, int cap) {
+  std::vector<double> h((size_t)kH64Bins * kH64Stride);
+  build_h64_table(h.data());
+  for (int i = 0; i < std::min(cap, kH64Bins); i++)
+    for (int q = 0; q < kH64Stride; q++) out[(size_t)i * kH64Stride + q] = h[(size_t)i * kH64Stride + q];
+  return kH64Bins;
+}
+
+int plum_h32_table(float* out, int cap) {
+  std::vector<float4> h(kH32Bins);
+  build_h32_table(h.data());
+  for (int i = 0; i < std::min(cap, kH32Bins); i++) {
+    out[4 * i] = h[i].x;
+    out[4 * i + 1] = h[i].y;
+    out[4 * i + 2] = h[i].z;
+    out[4 * i + 3] = h[i].w;
+  }
+  return kH32Bins;
 }
 
 int plum_batch_set_surrogate(plum_batch* b, const plum_surrogate* sg) {

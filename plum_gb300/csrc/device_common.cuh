@@ -114,4 +114,41 @@ __device__ __forceinline__ int cell_index(const DevParams& P, int4 f) {
                          P.cell_nc[1] * cell_axis((unsigned)f.z, P.cell_nc[2]));
 }
 
+// ------------------------------------------------------- FP64 real space
+static_assert(kH64Per == 32, "bin index below assumes 5 mantissa bits per octave");
+constexpr long long kH64LoBits = (long long)(1023 + kH64ELo) << 52;
+
+// h(u) = erfc(sqrt u) / sqrt u from the FP64 table at the bits of u >= 2^kH64ELo:
+// the exponent and top five mantissa bits pick the bin, the remaining 47 bits
+// shifted into a double of [1, 2) give 1 + f exactly, y = f - 1/2.
+__device__ __forceinline__ double h64_tab(const double* __restrict__ tab, long long bits) {
+  int idx = (int)(bits >> 47) - ((1023 + kH64ELo) << 5);
+  idx = min(max(idx, 0), kH64Bins - 1);
+  const double2* c = reinterpret_cast<const double2*>(tab + (size_t)idx * kH64Stride);
+  const double2 c01 = __ldg(c), c23 = __ldg(c + 1), c45 = __ldg(c + 2), c67 = __ldg(c + 3),
+                c89 = __ldg(c + 4);
+  const double y = __longlong_as_double(((bits << 5) & 0xFFFFFFFFFFFFFLL) |
+                                        0x3FF0000000000000LL) - 1.5;
+  double h = fma(c89.x, y, c67.y);
+  h = fma(h, y, c67.x);
+  h = fma(h, y, c45.y);
+  h = fma(h, y, c45.x);
+  h = fma(h, y, c23.y);
+  h = fma(h, y, c23.x);
+  h = fma(h, y, c01.y);
+  return fma(h, y, c01.x);
+}
+
+// erfc(sqrt(alpha) r) / r at squared distance r2 > 0 (the caller excludes
+// r2 = 0, as the reference's r > 0 test does): sqrt(alpha) h(alpha r2) from
+// the table, or directly where there is none or u is below it.
+__device__ __forceinline__ double real_term64(const DevParams& P, double r2) {
+  if (P.htab64) {
+    const long long bits = __double_as_longlong(P.alpha * r2);
+    if (bits >= kH64LoBits) return P.sqrt_alpha * h64_tab(P.htab64, bits);
+  }
+  const double r = sqrt(r2);
+  return erfc(P.sqrt_alpha * r) / r;
+}
+
 }  // namespace plum

@@ -94,6 +94,15 @@ struct DevParams {
   // descriptor's cut wide; cell_cap entries in the list of beads that left
   // their cell since the last rebuild (0: no cell list)
   int cell_nc[3], cell_cap;
+  // FP32 h(u) table of the real-space term (kH32Bins entries, device memory;
+  // null when alpha r_c^2 lies past it: the FP32 erfc fit is used then)
+  const float4* htab;
+  // FP64 h(u) table (kH64Bins x kH64Stride doubles; null: erfc / r), alpha
+  // itself, and whether the pair box and the Ewald box wrap every periodic
+  // axis alike (then one minimum-image vector serves LJ and Ewald)
+  const double* htab64;
+  double alpha;
+  int same_wrap;
 };
 
 // The pending move: beads [b_lo, b_hi) of molecule `mol` hold trial
@@ -267,7 +276,27 @@ struct BatchTune {
   int k_tile;      // k-vectors per k item
   int grid;        // blocks (0: 4 per SM)
   int min_blocks;  // register budget: 2 or 3 resident blocks per SM
+  int htab;        // real-space term from the h(u) table (1) or the erfc fit (0)
 };
+// FP32 table of h(u) = erfc(sqrt u) / sqrt u, the real-space Ewald term
+// erfc(sqrt(alpha) r) / r = sqrt(alpha) h(alpha r^2) as a function of the
+// dimensionless u = alpha r^2 alone, so one table serves every system. Bins:
+// kH32Per per octave of u for octaves 2^kH32ELo .. 2^(kH32EHi - 1); bin b
+// holds a cubic in y = f - 1/2, f in [0, 1) the bin-local fraction of u
+// (its float mantissa bits below the top five). Built on the host by
+// Chebyshev interpolation of std::erfc in double precision (build_h32_table).
+constexpr int kH32ELo = -14, kH32EHi = 5, kH32Per = 32;
+constexpr int kH32Bins = (kH32EHi - kH32ELo) * kH32Per;
+void build_h32_table(float4* out);  // kH32Bins entries
+// The FP64 table of h(u): kH64Per bins per octave of u for octaves
+// 2^kH64ELo .. 2^(kH64EHi - 1), a degree-8 polynomial in y = f - 1/2 per bin
+// (kH64Stride doubles per bin, the last zero, for 16-byte loads): Chebyshev
+// interpolation of erfcl at 9 nodes in long double, converted to powers of y.
+// About 2e-16 relative below u = 8; above it h < 3e-5 and the absolute error
+// stays below 1e-17. u below the table takes erfc / r directly.
+constexpr int kH64ELo = -12, kH64EHi = 5, kH64Per = 32, kH64Stride = 10;
+constexpr int kH64Bins = (kH64EHi - kH64ELo) * kH64Per;
+void build_h64_table(double* out);  // kH64Bins * kH64Stride entries
 constexpr int kMinItemPairs = 1024;  // smallest item the slot buffers are sized for
 constexpr int kMinKTile = 64;
 // Pair items of the batched energy change: up to kPairGroup moved beads
@@ -288,7 +317,7 @@ __host__ __device__ inline int pair_item_count(int m, int n_bead, int item_pairs
 // queue: two ints, zero before the first launch (each launch leaves them zero)
 void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, int* item_off,
                           double* slots, size_t smem, BatchTune tune, int* queue,
-                          cudaStream_t s);
+                          const float4* htab, cudaStream_t s);
 void launch_batch_serial(const DevParams* rp, const DevBuffers* rb, const int* item_off,
                          const double* slots, int n_rep, int mode, cudaStream_t s);
 // per replica r: if need[r], shift the unread words [pos[r], len[r]) of out[r]

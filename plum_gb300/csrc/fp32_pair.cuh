@@ -32,6 +32,47 @@ __device__ __forceinline__ float erfc_nr(float x) {
   return t * __expf(fmaf(-x, x, p));
 }
 
+static_assert(kH32Per == 32, "bin index below assumes 5 mantissa bits per octave");
+constexpr int kH32LoBits = (127 + kH32ELo) << 23;  // float bits of 2^kH32ELo
+
+// h(u) = erfc(sqrt u) / sqrt u from the table (in shared memory) at the
+// float bits of u: the exponent and top five mantissa bits pick the bin, the
+// remaining 18 bits are the bin-local fraction f (shifted up into a float of
+// [1, 2), 1 + f exactly), y = f - 1/2. Bins outside
+// the table are clamped (their values are replaced or cut off by the caller).
+__device__ __forceinline__ float h32_tab(const float4* tab, int bits) {
+  int idx = (bits >> 18) - ((127 + kH32ELo) << 5);
+  idx = min(max(idx, 0), kH32Bins - 1);
+  const float4 c = tab[idx];
+  // the 18 bits below the bin index moved to the top of a float in [1, 2)
+  const float y = __int_as_float(((bits << 5) & 0x7FFFFF) | 0x3F800000) - 1.5f;
+  return fmaf(fmaf(fmaf(c.w, y, c.z), y, c.y), y, c.x);
+}
+
+// Below the table (u < 2^kH32ELo: r under 1/128 of 1/sqrt(alpha)): the erfc
+// fit; 0 at r = 0 (the reference's r > 0 test).
+static __device__ __noinline__ float h32_small(float u) {
+  return u > 0.0f ? erfc_nr(sqrtf(u)) * rsqrtf(u) : 0.0f;
+}
+
+// h(u) for any u >= 0 from a table in shared or global memory.
+__device__ __forceinline__ float h32(const float4* tab, float u) {
+  const int bits = __float_as_int(u);
+  float h = h32_tab(tab, bits);
+  if (bits < kH32LoBits) h = h32_small(u);
+  return h;
+}
+
+// erfc(sqrt(alpha) r) / r at squared distance r2 > 0 (0 at r2 = 0): from the
+// context's h(u) table when it has one (alpha r_c^2 inside the table), else
+// the erfc fit.
+__device__ __forceinline__ float real_term32(const DevParams& P, float r2) {
+  if (P.htab) return P.f_sqrt_alpha * h32(P.htab, P.f_sqrt_alpha * P.f_sqrt_alpha * r2);
+  if (!(r2 > 0.0f)) return 0.0f;
+  const float ir = rsqrtf(r2);
+  return erfc_nr(P.f_sqrt_alpha * r2 * ir) * ir;
+}
+
 __device__ __forceinline__ float lj32(const DevParams& P, int k, float r2) {
   if (P.pair_kind == 1) return sqrtf(r2) <= P.f_hs_sum[k] ? (float)kVeryLarge : 0.0f;
   if (r2 <= 0.0f) return (float)kVeryLarge;
@@ -50,11 +91,7 @@ __device__ __forceinline__ float real_images32(const DevParams& P, float dx, flo
   if (P.single_image) {
     // r_c <= L/2 on every axis: only the minimum image can be inside r_c
     const float r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 > 0.0f) {
-      const float ir = rsqrtf(r2);
-      const float r = r2 * ir;
-      if (r <= rc) e = erfc_nr(P.f_sqrt_alpha * r) * ir;
-    }
+    if (r2 <= rc * rc) e = real_term32(P, r2);
     return e;
   }
   for (int a = -P.real_cell[0]; a <= P.real_cell[0]; a++) {
@@ -67,11 +104,7 @@ __device__ __forceinline__ float real_images32(const DevParams& P, float dx, flo
         float z = dz + c * P.f_box[2];
         if (fabsf(z) > rc) continue;
         float r2 = x * x + y * y + z * z;
-        if (r2 > 0.0f) {
-          float ir = rsqrtf(r2);
-          float r = r2 * ir;
-          if (r <= rc) e += erfc_nr(P.f_sqrt_alpha * r) * ir;
-        }
+        if (r2 <= rc * rc) e += real_term32(P, r2);
       }
     }
   }

@@ -61,8 +61,8 @@ __device__ __forceinline__ double cb_real(const DevParams& P, double4_32a a, dou
       for (int k = -P.real_cell[2]; k <= P.real_cell[2]; k++) {
         double z = dz + k * P.ebox[2];
         if (fabs(z) > rc) continue;
-        double r = sqrt(x * x + y * y + z * z);
-        if (r > 0.0 && r <= rc) e += erfc(P.sqrt_alpha * r) / r;
+        const double r2 = x * x + y * y + z * z;
+        if (r2 > 0.0 && r2 <= rc * rc) e += real_term64(P, r2);
       }
     }
   }

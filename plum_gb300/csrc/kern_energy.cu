@@ -21,6 +21,7 @@
 // = 2 kPi w_a / L_a on coordinates wrapped into the primary cell (periodic
 // axes). This replaces the reference's cos(k.r) per pair and k.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 
 #include "engine.h"
@@ -52,11 +53,12 @@ __device__ __forceinline__ double real_images64(const DevParams& P, double dx,
                                                 double dy, double dz) {
   double e = 0.0;
   const double rc = P.real_cut;
+  const double rc2 = rc * rc;
   if (P.single_image) {
     // r_c <= L/2 on every axis: any other image has a component >= L/2 >= r_c
     // (ties at exactly L/2 are a set of measure zero)
-    double r = sqrt(dx * dx + dy * dy + dz * dz);
-    if (r > 0.0 && r <= rc) e = erfc(P.sqrt_alpha * r) / r;
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    if (r2 > 0.0 && r2 <= rc2) e = real_term64(P, r2);
     return e;
   }
   for (int a = -P.real_cell[0]; a <= P.real_cell[0]; a++) {
@@ -68,8 +70,8 @@ __device__ __forceinline__ double real_images64(const DevParams& P, double dx,
       for (int c = -P.real_cell[2]; c <= P.real_cell[2]; c++) {
         double z = dz + c * P.ebox[2];
         if (fabs(z) > rc) continue;
-        double r = sqrt(x * x + y * y + z * z);
-        if (r > 0.0 && r <= rc) e += erfc(P.sqrt_alpha * r) / r;
+        const double r2 = x * x + y * y + z * z;
+        if (r2 > 0.0 && r2 <= rc2) e += real_term64(P, r2);
       }
     }
   }
@@ -80,6 +82,19 @@ __device__ __forceinline__ double real_images64(const DevParams& P, double dx,
 __device__ __forceinline__ void pair64(const DevParams& P, double4_32a a, int ta,
                                        double4_32a b, int tb, double& lj, double& re) {
   double dx = b.x - a.x, dy = b.y - a.y, dz = b.z - a.z;
+  if (P.same_wrap) {
+    // the pair box wraps every periodic axis as the Ewald box does: one
+    // minimum-image vector for both terms
+    const double x = wrap_d(dx, P.box[0], P.inv_box[0]);
+    const double y = wrap_d(dy, P.box[1], P.inv_box[1]);
+    const double z = P.npbc > 2 ? wrap_d(dz, P.box[2], P.inv_box[2]) : dz;
+    if (P.use_pair) lj += lj64(P, ta * P.n_type + tb, x * x + y * y + z * z);
+    if (P.use_ewald) {
+      const double qq = a.w * b.w;
+      if (qq != 0.0) re += P.lB * qq * real_images64(P, x, y, z);
+    }
+    return;
+  }
   if (P.use_pair) {
     double x = wrap_d(dx, P.box[0], P.inv_box[0]);
     double y = wrap_d(dy, P.box[1], P.inv_box[1]);
@@ -565,5 +580,40 @@ void launch_rhoz(const DevParams& P, const DevBuffers& B, double res, int n_bins
   if (m > 0) k_rhoz<<<std::min(m, 4 * 152), 128, 0, s>>>(P, B, res, n_bins, cnt);
 }
 
+
+// The FP64 h(u) table: per bin the degree-8 Chebyshev interpolant of
+// h(u) = erfc(sqrt u) / sqrt u at the 9 Chebyshev nodes of y in [-1/2, 1/2]
+// (u = lo + (y + 1/2) w), in long double, then rewritten in powers of y.
+void build_h64_table(double* out) {
+  constexpr int n = 9;
+  const long double pi = 3.141592653589793238462643383279503L;
+  long double T[n][n] = {};  // T_j(t) coefficients in powers of t
+  T[0][0] = 1.0L;
+  T[1][1] = 1.0L;
+  for (int j = 2; j < n; j++)
+    for (int q = 0; q < n; q++)
+      T[j][q] = (q ? 2.0L * T[j - 1][q - 1] : 0.0L) - T[j - 2][q];
+  int b = 0;
+  for (int e = kH64ELo; e < kH64EHi; e++)
+    for (int j = 0; j < kH64Per; j++, b++) {
+      const long double lo = std::ldexp(1.0L + (long double)j / kH64Per, e);
+      const long double w = std::ldexp(1.0L / kH64Per, e);
+      long double f[n], tk[n];
+      for (int k = 0; k < n; k++) {
+        tk[k] = std::cos(pi * (k + 0.5L) / n);  // t = 2 y in [-1, 1]
+        const long double u = lo + (0.5L * tk[k] + 0.5L) * w;
+        const long double r = std::sqrt(u);
+        f[k] = std::erfc(r) / r;
+      }
+      long double mono[n] = {};  // powers of y
+      for (int jj = 0; jj < n; jj++) {
+        long double a = 0.0L;
+        for (int k = 0; k < n; k++) a += f[k] * std::cos(pi * jj * (k + 0.5L) / n);
+        a *= (jj ? 2.0L : 1.0L) / n;
+        for (int q = 0; q < n; q++) mono[q] += a * T[jj][q] * std::ldexp(1.0L, q);
+      }
+      for (int q = 0; q < kH64Stride; q++) out[(size_t)b * kH64Stride + q] = q < n ? (double)mono[q] : 0.0;
+    }
+}
 
 }  // namespace plum

@@ -18,6 +18,9 @@
 // across the grid, k tiles x moved-bead groups with a last-arrival reduction.
 // Per-thread and per-block sums are FP32; blocks are added in FP64 by the
 // serial kernel.
+#include <algorithm>
+#include <cmath>
+
 #include "engine.h"
 #include "device_common.cuh"
 #include "fp32_pair.cuh"
@@ -277,11 +280,7 @@ __device__ __forceinline__ void pair32k(const DevParams& P, const PairConst& K, 
     if (qq != 0.0f) {
       float e = 0.0f;
       if (kSingle) {
-        if (r2 > 0.0f) {
-          const float ir = rsqrtf(r2);
-          const float r = r2 * ir;
-          if (r <= K.rc) e = erfc_nr(K.sa * r) * ir;
-        }
+        if (r2 <= K.rc * K.rc) e = real_term32(P, r2);
       } else {
         e = real_images32(P, dx, dy, dz);
       }
@@ -314,6 +313,101 @@ __device__ __forceinline__ void pair_sweep(const DevParams& P, const PairConst& 
   }
 }
 
+// ------------------------------------------------ table-driven real space
+// pair_sweep for LJ + Ewald with r_c <= L/2 on every axis, the real-space term
+// from the h(u) table: per (moved u, other j) the trial and current distances
+// share the other bead's load, one LJ pre-test and one charge product, and the
+// cut-off is a select, so a warp runs no divergent erfc. kCubic (equal
+// fixed-point scales on the three axes): r^2 stays in fixed-point units and
+// the box scale is folded into the constants. gn4 staged beads, a multiple of
+// 4 (the padding beads have q = 0 and equal trial and current positions, so
+// they add exactly zero).
+template <bool kCubic>
+__device__ __forceinline__ void pair_sweep_tab(const DevParams& P, const DevBuffers& B,
+                                               const int4* s_mt, const float* s_mq,
+                                               const float4* s_h, int gn4, int c0, int c1,
+                                               int b_lo, int b_hi, float& acc_lj,
+                                               float& acc_re) {
+  const float sx = P.f_scale[0], sy = P.f_scale[1], sz = P.f_scale[2];
+  const float cs = kCubic ? sx * sx : 1.0f;  // real r^2 per unit of r2 below
+  const float ics = 1.0f / cs;
+  const float rc2 = P.f_real_cut * P.f_real_cut * ics;
+  const float ua = P.f_sqrt_alpha * P.f_sqrt_alpha * cs;
+  float ljm = 1e-30f;  // r2 = 0 (coincident beads) must reach lj32
+  for (int k = 0; k < P.n_type * P.n_type; k++) ljm = fmaxf(ljm, P.f_lj_rc2[k]);
+  const float ljlim = ljm * ics;
+  const float pref = P.f_lB * P.f_sqrt_alpha;
+  const int nt = P.n_type;
+  const bool use_pair = P.use_pair;
+  for (int j = c0 + threadIdx.x; j < c1; j += kPairThreads) {
+    if (j >= b_lo && j < b_hi) continue;  // moved pairs: the last item
+    const int4 cj = B.fpos[j];
+    const float qj = B.fq[j] * pref;
+#pragma unroll 4
+    for (int u = 0; u < gn4; u++) {
+      const int4 t = s_mt[u], c = s_mt[kPairGroup + u];
+      float x1 = (float)(int)((unsigned)cj.x - (unsigned)t.x);
+      float y1 = (float)(int)((unsigned)cj.y - (unsigned)t.y);
+      float z1 = (float)(int)((unsigned)cj.z - (unsigned)t.z);
+      float x0 = (float)(int)((unsigned)cj.x - (unsigned)c.x);
+      float y0 = (float)(int)((unsigned)cj.y - (unsigned)c.y);
+      float z0 = (float)(int)((unsigned)cj.z - (unsigned)c.z);
+      if (!kCubic) {
+        x1 *= sx, y1 *= sy, z1 *= sz;
+        x0 *= sx, y0 *= sy, z0 *= sz;
+      }
+      const float r1 = fmaf(x1, x1, fmaf(y1, y1, z1 * z1));
+      const float r0 = fmaf(x0, x0, fmaf(y0, y0, z0 * z0));
+      if (use_pair && fminf(r1, r0) < ljlim)
+        acc_lj += lj32(P, t.w * nt + cj.w, r1 * cs) - lj32(P, c.w * nt + cj.w, r0 * cs);
+      const int b1 = __float_as_int(r1 * ua), b0 = __float_as_int(r0 * ua);
+      float h1 = h32_tab(s_h, b1), h0 = h32_tab(s_h, b0);
+      if (min(b1, b0) < kH32LoBits) {
+        if (b1 < kH32LoBits) h1 = h32_small(__int_as_float(b1));
+        if (b0 < kH32LoBits) h0 = h32_small(__int_as_float(b0));
+      }
+      h1 = r1 <= rc2 ? h1 : 0.0f;
+      h0 = r0 <= rc2 ? h0 : 0.0f;
+      acc_re = fmaf(s_mq[u] * qj, h1 - h0, acc_re);
+    }
+  }
+}
+
+// The table (kH32Bins float4): per bin the cubic through h at the four
+// Chebyshev nodes of y in [-1/2, 1/2], h in double precision from std::erfc,
+// the 4 x 4 Vandermonde system solved by Gaussian elimination.
+void build_h32_table(float4* out) {
+  const double kPi = 3.14159265358979323846;
+  int i = 0;
+  for (int e = kH32ELo; e < kH32EHi; e++)
+    for (int j = 0; j < kH32Per; j++, i++) {
+      const double lo = std::ldexp(1.0 + (double)j / kH32Per, e);
+      const double w = std::ldexp(1.0 / kH32Per, e);
+      double A[4][5];
+      for (int k = 0; k < 4; k++) {
+        const double y = 0.5 * std::cos(kPi * (k + 0.5) / 4.0);
+        const double u = lo + (y + 0.5) * w;
+        const double r = std::sqrt(u);
+        double p = 1.0;
+        for (int q = 0; q < 4; q++, p *= y) A[k][q] = p;
+        A[k][4] = std::erfc(r) / r;
+      }
+      for (int col = 0; col < 4; col++) {
+        int piv = col;
+        for (int rr = col + 1; rr < 4; rr++)
+          if (std::fabs(A[rr][col]) > std::fabs(A[piv][col])) piv = rr;
+        for (int q = 0; q < 5; q++) std::swap(A[col][q], A[piv][q]);
+        for (int rr = 0; rr < 4; rr++) {
+          if (rr == col) continue;
+          const double f = A[rr][col] / A[col][col];
+          for (int q = col; q < 5; q++) A[rr][q] -= f * A[col][q];
+        }
+      }
+      out[i] = make_float4((float)(A[0][4] / A[0][0]), (float)(A[1][4] / A[1][1]),
+                           (float)(A[2][4] / A[2][2]), (float)(A[3][4] / A[3][3]));
+    }
+}
+
 // ------------------------------------------------------------ replicas
 // Batched replicas: every replica's pending move contributes pair items
 // (up to kPairGroup moved beads, staged in shared memory at their trial and
@@ -332,9 +426,14 @@ template <int kMinBlocks>
 __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
     k_batch_delta32(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb,
                     int n_rep, int* __restrict__ item_off, double* __restrict__ slots,
-                    BatchTune tune, int* __restrict__ queue) {
+                    BatchTune tune, int* __restrict__ queue, const float4* __restrict__ htab) {
   const int kItemPairs = tune.item_pairs, kKTile32 = tune.k_tile;
-  extern __shared__ __align__(16) unsigned char smem[];
+  extern __shared__ __align__(16) unsigned char smem_all[];
+  // with the h(u) table: the table first, then the staging / k-table area
+  float4* s_h = reinterpret_cast<float4*>(smem_all);
+  unsigned char* smem = smem_all + (htab ? kH32Bins * sizeof(float4) : 0);
+  if (htab)
+    for (int i = threadIdx.x; i < kH32Bins; i += blockDim.x) s_h[i] = htab[i];
   __shared__ float red[kPairThreads / 32];
   __shared__ int s_pref[kMaxReplicas + 1];
   __shared__ int s_np[kMaxReplicas];
@@ -397,15 +496,33 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
         const int c0 = (local % n_chunk) * chunk, c1 = min(N, c0 + chunk);
         int4* s_mt = reinterpret_cast<int4*>(smem);  // trial, then current
         float* s_mq = reinterpret_cast<float*>(s_mt + 2 * kPairGroup);
+        const bool tab = htab && P.single_image && P.pair_kind == 0 && P.use_ewald;
+        // the table path pads the staged beads to a multiple of 4 with the
+        // last bead's current position at both places and q = 0
+        const int gn4 = tab ? (gn + 3) & ~3 : gn;
         __syncthreads();  // the previous item may still read the staging area
-        for (int u = threadIdx.x; u < gn; u += kPairThreads) {
-          s_mt[u] = B.ftrial[g0 + u];
-          s_mt[kPairGroup + u] = B.fpos[b_lo + g0 + u];
-          s_mq[u] = B.fq[b_lo + g0 + u];
+        for (int u = threadIdx.x; u < gn4; u += kPairThreads) {
+          if (u < gn) {
+            s_mt[u] = B.ftrial[g0 + u];
+            s_mt[kPairGroup + u] = B.fpos[b_lo + g0 + u];
+            s_mq[u] = B.fq[b_lo + g0 + u];
+          } else {
+            const int4 p = B.fpos[b_lo + g0 + gn - 1];
+            s_mt[u] = p;
+            s_mt[kPairGroup + u] = p;
+            s_mq[u] = 0.0f;
+          }
         }
         __syncthreads();
         const PairConst K = pair_const(P);
-        if (P.single_image)
+        if (tab) {
+          if (P.npbc == 3 && P.f_scale[0] == P.f_scale[1] && P.f_scale[1] == P.f_scale[2])
+            pair_sweep_tab<true>(P, B, s_mt, s_mq, s_h, gn4, c0, c1, b_lo, b_hi, acc_lj,
+                                 acc_re);
+          else
+            pair_sweep_tab<false>(P, B, s_mt, s_mq, s_h, gn4, c0, c1, b_lo, b_hi, acc_lj,
+                                  acc_re);
+        } else if (P.single_image)
           pair_sweep<true>(P, K, B, s_mt, s_mq, gn, b_lo + g0, c0, c1, b_lo, b_hi, acc_lj,
                            acc_re);
         else
@@ -486,24 +603,27 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
 
 void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, int* item_off,
                           double* slots, size_t smem, BatchTune tune, int* queue,
-                          cudaStream_t s) {
+                          const float4* htab, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_batch_delta32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kKTableBytes + 4096);
-    cudaFuncSetAttribute(k_batch_delta32<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kKTableBytes + 4096);
-    cudaFuncSetAttribute(k_batch_delta32<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kKTableBytes + 4096);
+    const int most = kKTableBytes + 4096 + kH32Bins * (int)sizeof(float4);
+    cudaFuncSetAttribute(k_batch_delta32<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+    cudaFuncSetAttribute(k_batch_delta32<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+    cudaFuncSetAttribute(k_batch_delta32<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
     attr = true;
   }
   const int grid = tune.grid > 0 ? tune.grid : pair_grid32();
+  if (!tune.htab) htab = nullptr;
+  if (htab) smem += kH32Bins * sizeof(float4);
   if (tune.min_blocks == 4)
-    k_batch_delta32<4><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune, queue);
+    k_batch_delta32<4><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune,
+                                                        queue, htab);
   else if (tune.min_blocks == 3)
-    k_batch_delta32<3><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune, queue);
+    k_batch_delta32<3><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune,
+                                                        queue, htab);
   else
-    k_batch_delta32<2><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune, queue);
+    k_batch_delta32<2><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune,
+                                                        queue, htab);
 }
 
 __global__ void k_fix_all(const DevParams P, const DevBuffers B) {

@@ -6,8 +6,9 @@
 // before/after channels swapped), so the antisymmetric output
 // s = y_scale (f(x) - f(swap x)) and its gradient stay inside the CTA.
 //
-//   k_mlp<false>  forward: s per sample; with DaArgs, the delayed-acceptance
-//                 stage one of each replica's pending move
+//   k_mlp_infer   forward on 512 threads (four per tile row, one 32-column
+//                 slice each): s per sample; with DaArgs, the
+//                 delayed-acceptance stage one of each replica's pending move
 //   k_mlp<true>   forward + backward of the mean squared error against the
 //                 targets; per-tile gradients of every parameter
 //   k_mlp_reduce  per-tile gradients summed in tile order (deterministic)
@@ -471,6 +472,174 @@ __global__ void __launch_bounds__(kThreads, 1)
                  : "memory");
 }
 
+// Inference on 512 threads: thread t takes tile row (TMEM lane) t % 128 and
+// the 32-column slice t / 128 of every 128-column epilogue, so each lane
+// quarter's rows are shared by four warps (a warp reads only its own lane
+// quarter, 32 (warp % 4) .. +31). The per-slice partial outputs are added in
+// slice order. Same operands, layout and MMAs as k_mlp; SiLU with the fast
+// exponential and divide (relative error ~1e-6, far below the bf16 rounding
+// of the operands).
+constexpr int kInferThreads = 512;
+
+__device__ __forceinline__ float silu_fast(float z) {
+  return __fdividef(z, 1.0f + __expf(-z));  // 0 once exp(-z) passes 2^126
+}
+
+template <typename TIn>
+__global__ void __launch_bounds__(kInferThreads, 1)
+    k_mlp_infer(const MlpNet* __restrict__ net, const TIn* __restrict__ x, float xscale, int n,
+                float* __restrict__ s_out, DaArgs da, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int t = threadIdx.x, warp = t >> 5;
+  const int row = t & 127, cq = t >> 7;
+  float* ypart = reinterpret_cast<float*>(sm + kMiscI);  // [4 slices][128 rows]
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kMiscI + 3072);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + kMiscI + 3080);
+  int* sflag = reinterpret_cast<int*>(sm + kMiscI + 3084);
+  const uint32_t base = smem_u32(sm);
+  const uint32_t mb = smem_u32(mbar);
+  constexpr uint32_t kCols = 256u;
+
+  if (warp == 0) {
+    asm volatile(
+        "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n\t"
+        "tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::"r"(smem_u32(tslot)),
+        "r"(kCols)
+        : "memory");
+  }
+  if (t == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *sflag = 0;
+  }
+  const __nv_bfloat16* w1 = net->w1;
+  const __nv_bfloat16* w2 = net->w2;
+  for (int c = t; c < kHid * (kIn / 8); c += kInferThreads) {
+    const int r = c / (kIn / 8), k8 = c % (kIn / 8);
+    *reinterpret_cast<uint4*>(sm + kW1 + op_off(r, k8 * 8, kIn)) =
+        *reinterpret_cast<const uint4*>(w1 + r * kIn + k8 * 8);
+  }
+  for (int c = t; c < kHid * (kHid / 8); c += kInferThreads) {
+    const int r = c / (kHid / 8), k8 = c % (kHid / 8);
+    *reinterpret_cast<uint4*>(sm + kW2 + op_off(r, k8 * 8, kHid)) =
+        *reinterpret_cast<const uint4*>(w2 + r * kHid + k8 * 8);
+  }
+  const int sample = blockIdx.x * kSamp + (row & (kSamp - 1));
+  const bool swapped = row >= kSamp;
+  const bool valid = sample < n;
+  // launched as a dependent of the previous kernel: the weights above were
+  // staged while it ran; its results are visible after this wait
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  {
+    float* xs = reinterpret_cast<float*>(sm + kH1);
+    const int s0 = blockIdx.x * kSamp;
+    constexpr int kVec = kSamp * kIn / 4;
+    for (int e = t; e < kVec; e += kInferThreads) {
+      const int r = e / (kIn / 4);
+      float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (s0 + r < n) {
+        const uint4 raw = reinterpret_cast<const uint4*>(x + (size_t)s0 * kIn)[e];
+        if constexpr (std::is_same<TIn, float>::value) {
+          v = make_float4(__uint_as_float(raw.x), __uint_as_float(raw.y), __uint_as_float(raw.z),
+                          __uint_as_float(raw.w));
+        } else {  // integer descriptor sums
+          v = make_float4((float)raw.x, (float)raw.y, (float)raw.z, (float)raw.w);
+        }
+      }
+      reinterpret_cast<float4*>(xs)[e] = make_float4(v.x * xscale, v.y * xscale, v.z * xscale,
+                                                     v.w * xscale);
+    }
+  }
+  __syncthreads();
+  const float* xrow = reinterpret_cast<const float*>(sm + kH1) + (row & (kSamp - 1)) * kIn;
+  for (int k8 = cq; k8 < kIn / 8; k8 += 4) {
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; e++) {
+      const int f = k8 * 8 + e;
+      const int src = swapped ? (f + kIn / 2) % kIn : f;
+      v[e] = valid ? (xrow[src] - net->mu[f]) * net->isd[f] : 0.0f;
+    }
+    st_bf16x8(sm + kX + op_off(row, k8 * 8, kIn), v);
+  }
+  proxy_fence();
+  tc_before();
+  __syncthreads();
+  tc_after();
+  const uint32_t tmem = *tslot;
+  const uint32_t trow = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  uint32_t phase = 0;
+  bool ok = true;
+  auto step = [&](bool issue) {
+    bool got = !issue || mbar_wait(mb, phase);
+    phase ^= 1u;
+    if (!got) atomicOr(sflag, 1);
+    tc_before();
+    __syncthreads();
+    tc_after();
+    ok = *sflag == 0;
+  };
+
+  // layer 1: z1 = x' W1^T; this thread's 32 columns through SiLU into H1
+  if (t == 0) {
+    mma_tile(tmem, base + kX, base + kW1, kIn, idesc_bf16(128, 128));
+    mma_commit(mb);
+  }
+  step(true);
+  {
+    float v[32];
+    tmem_ld32(trow + 32 * cq, v);
+#pragma unroll
+    for (int c = 0; c < 32; c++) v[c] = silu_fast(v[c] + net->b1[32 * cq + c]);
+#pragma unroll
+    for (int j = 0; j < 4; j++) st_bf16x8(sm + kH1 + op_off(row, 32 * cq + 8 * j, kHid), v + 8 * j);
+  }
+  proxy_fence();
+  tc_before();
+  __syncthreads();
+  tc_after();
+
+  // layer 2: z2 = h1 W2^T; partial w3 . SiLU(z2) over this thread's columns
+  if (t == 0 && ok) {
+    mma_tile(tmem + 128, base + kH1, base + kW2, kHid, idesc_bf16(128, 128));
+    mma_commit(mb);
+  }
+  step(ok);
+  {
+    float v[32];
+    tmem_ld32(trow + 128 + 32 * cq, v);
+    float y = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 32; c++)
+      y = fmaf(__bfloat162float(net->w3[32 * cq + c]), silu_fast(v[c] + net->b2[32 * cq + c]), y);
+    ypart[cq * 128 + row] = y;
+  }
+  __syncthreads();
+  if (t < kSamp) {
+    auto yrow = [&](int r) {
+      return net->b3 + (((ypart[r] + ypart[128 + r]) + ypart[256 + r]) + ypart[384 + r]);
+    };
+    const float s = net->y_scale * (yrow(t) - yrow(t + kSamp));
+    if (valid && s_out) s_out[sample] = s;
+    if (valid && da.sts) {
+      DevState* st = da.sts[sample];
+      if (st->pending && st->da_active) {
+        const double u1 = st->da_u1;
+        const float m = net->da_margin;
+        const float sd = s > m ? s - m : (s < -m ? s + m : 0.0f);
+        st->da_s = (double)sd;
+        st->da_skip = !(u1 < exp(-da.rp[sample].beta * (double)sd));
+      }
+    }
+  }
+  tc_before();
+  __syncthreads();
+  if (t == 0 && !ok && err) atomicExch(err, 1);
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols)
+                 : "memory");
+}
+
 __global__ void k_mlp_reduce(const float* __restrict__ part, int tiles, float* __restrict__ grad) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p > kNParam) return;
@@ -812,7 +981,9 @@ __global__ void k_cell_scatter(const DevParams* __restrict__ rp,
   B.cell_key[j] = k;
 }
 
-constexpr int kCellBeads = 4;  // moved beads per block: a warp per (bead, before / after)
+constexpr int kCellBeads = 2;  // moved beads per block
+constexpr int kCellSplit = 4;  // warps per (bead, before / after), each a quarter of its entries
+constexpr int kCellWarps = 2 * kCellBeads * kCellSplit;
 
 // Block (x, r): moved beads [4x, 4x + 4) of replica r's pending surrogate
 // move. Warp (bead, channel pair): before the move (channels 0, 1) the
@@ -822,7 +993,7 @@ constexpr int kCellBeads = 4;  // moved beads per block: a warp per (bead, befor
 // once, at the end). Entries carry the positions, so a candidate costs one
 // load, and the 27 cells' entries form one list spread over the lanes. The
 // same pairs, distances and bins as k_desc.
-__global__ void __launch_bounds__(2 * kCellBeads * 32)
+__global__ void __launch_bounds__(kCellWarps * 32)
     k_desc_cells(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb) {
   const DevParams& P = rp[blockIdx.y];
   const DevBuffers& B = rb[blockIdx.y];
@@ -832,11 +1003,12 @@ __global__ void __launch_bounds__(2 * kCellBeads * 32)
   const int b_lo = st->b_lo, m = min(st->b_hi - b_lo, kDescMaxMoved);
   if ((int)blockIdx.x * kCellBeads >= m) return;
   __shared__ unsigned fh[kFineAll];
-  __shared__ int s_pre[2 * kCellBeads][32], s_base[2 * kCellBeads][32];
+  __shared__ int s_pre[kCellWarps][32], s_base[kCellWarps][32];
   for (int k = threadIdx.x; k < kFineAll; k += blockDim.x) fh[k] = 0u;
   __syncthreads();
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int q = blockIdx.x * kCellBeads + (w >> 1), ch = w & 1;
+  const int part = w % kCellSplit, pc = w / kCellSplit;
+  const int q = blockIdx.x * kCellBeads + (pc >> 1), ch = pc & 1;
   if (q < m) {
     const int tq = B.fpos[b_lo + q].w;
     const int4 p = ch ? B.ftrial[q] : B.fpos[b_lo + q];
@@ -864,8 +1036,10 @@ __global__ void __launch_bounds__(2 * kCellBeads * 32)
       const float r2 = desc_r2_fix(P, p, ent);
       if (r2 < cut2) atomicAdd(&hist[((ent.w & 7) == tq ? 0 : 1) * kFine + fine_bin(r2)], 1u);
     };
-    // the 27 cells' entries as one list: lane e takes entries e, e + 32, ...,
-    // finding its cell by binary search in the inclusive prefix of the counts
+    // the 27 cells' entries as one list, split in kCellSplit contiguous
+    // parts (one per warp of this bead and channel): lane e of a part takes
+    // its entries e, e + 32, ..., finding the cell by binary search in the
+    // inclusive prefix of the counts
     int pre = cn;
     for (int o = 1; o < 32; o <<= 1) {
       const int t = __shfl_up_sync(0xffffffffu, pre, o);
@@ -875,8 +1049,9 @@ __global__ void __launch_bounds__(2 * kCellBeads * 32)
     s_pre[w][lane] = pre;
     s_base[w][lane] = cbase;
     __syncwarp();
+    const int e_lo = part * total / kCellSplit, e_hi = (part + 1) * total / kCellSplit;
 #pragma unroll 4
-    for (int e = lane; e < total; e += 32) {
+    for (int e = e_lo + lane; e < e_hi; e += 32) {
       int lo = 0, hi = 26;
       while (lo < hi) {
         const int mid = (lo + hi) >> 1;
@@ -885,8 +1060,8 @@ __global__ void __launch_bounds__(2 * kCellBeads * 32)
       visit(B.cell_ent[s_base[w][lo] + e - (lo ? s_pre[w][lo - 1] : 0)]);
     }
     const int n_extra = min(B.cell_n[nx * ny * nz], P.cell_cap);
-    for (int e = lane; e < n_extra; e += 32) visit(B.cell_extra[e]);
-    for (int q2 = q + 1 + lane; q2 < m; q2 += 32) {
+    for (int e = part * 32 + lane; e < n_extra; e += 32 * kCellSplit) visit(B.cell_extra[e]);
+    for (int q2 = q + 1 + part * 32 + lane; q2 < m; q2 += 32 * kCellSplit) {
       const int4 o = ch ? B.ftrial[q2] : B.fpos[b_lo + q2];
       const float r2 = desc_r2_fix(P, p, o);
       if (r2 < cut2)
@@ -937,11 +1112,11 @@ void launch_mlp_infer_f(const MlpNet* net, const float* x, int n, float* s_out, 
   if (n <= 0) return;
   static bool attr = false;
   if (!attr) {
-    smem_attr((const void*)k_mlp<false, float>, kSmemInfer);
+    smem_attr((const void*)k_mlp_infer<float>, kSmemInfer);
     attr = true;
   }
-  k_mlp<false, float><<<(n + kSamp - 1) / kSamp, kThreads, kSmemInfer, st>>>(
-      net, x, 1.0f, n, nullptr, s_out, nullptr, 0.0f, DaArgs{nullptr, nullptr}, err);
+  k_mlp_infer<float><<<(n + kSamp - 1) / kSamp, kInferThreads, kSmemInfer, st>>>(
+      net, x, 1.0f, n, s_out, DaArgs{nullptr, nullptr}, err);
 }
 
 void launch_mlp_infer_i(const MlpNet* net, const unsigned* x, int n, float* s_out, DaArgs da,
@@ -949,14 +1124,14 @@ void launch_mlp_infer_i(const MlpNet* net, const unsigned* x, int n, float* s_ou
   if (n <= 0) return;
   static bool attr = false;
   if (!attr) {
-    smem_attr((const void*)k_mlp<false, unsigned>, kSmemInfer);
+    smem_attr((const void*)k_mlp_infer<unsigned>, kSmemInfer);
     attr = true;
   }
   // programmatic dependent launch: may start while the preceding kernel on
   // the stream (the descriptor kernel) still runs
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((n + kSamp - 1) / kSamp);
-  cfg.blockDim = dim3(kThreads);
+  cfg.blockDim = dim3(kInferThreads);
   cfg.dynamicSmemBytes = kSmemInfer;
   cfg.stream = st;
   cudaLaunchAttribute at[1];
@@ -964,8 +1139,7 @@ void launch_mlp_infer_i(const MlpNet* net, const unsigned* x, int n, float* s_ou
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, k_mlp<false, unsigned>, net, x, kDescUnit, n, (const float*)nullptr,
-                     s_out, (float*)nullptr, 0.0f, da, err);
+  cudaLaunchKernelEx(&cfg, k_mlp_infer<unsigned>, net, x, kDescUnit, n, s_out, da, err);
 }
 
 void launch_mlp_grad(const MlpNet* net, const float* x, const float* t, int n, float* part,
@@ -1020,7 +1194,7 @@ void launch_desc_batch(const DevParams* rp, const DevBuffers* rb, int n_rep, uns
   (void)acc;
   if (cell_moved > 0)
     k_desc_cells<<<dim3((std::min(cell_moved, kDescMaxMoved) + kCellBeads - 1) / kCellBeads,
-                        n_rep), 2 * kCellBeads * 32, 0, st>>>(rp, rb);
+                        n_rep), kCellWarps * 32, 0, st>>>(rp, rb);
   if (cell_moved > 0 && form) {
     // the all-pairs kernel only takes replicas whose cell list overflowed:
     // usually none, so a small grid (it still has to look at every replica)

@@ -141,6 +141,37 @@ __device__ __forceinline__ double bsum(double v, double* sh) {
   return t;  // valid in every thread
 }
 
+// Three block sums at once (two barriers for all three, plus one before sh
+// is reused); each value is added in bsum's order, so the results are the
+// same bits as three bsum calls. sh: 3 NT / 32 doubles.
+template <int NT>
+__device__ __forceinline__ void bsum3(double& a, double& b, double& c, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  constexpr int W = NT / 32;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) {
+    sh[w] = a;
+    sh[W + w] = b;
+    sh[2 * W + w] = c;
+  }
+  __syncthreads();
+  double ta = 0.0, tb = 0.0, tc = 0.0;
+  for (int i = 0; i < W; i++) {
+    ta += sh[i];
+    tb += sh[W + i];
+    tc += sh[2 * W + i];
+  }
+  __syncthreads();
+  a = ta;
+  b = tb;
+  c = tc;
+}
+
 struct GenPlan {
   int type;      // move type, -1 none
   int mol, b0, b1, b_lo, b_hi;
@@ -432,7 +463,7 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
 struct SerialSmem {
   uint32_t win[kDrawWindow];
   unsigned accbits[kDrawWindow / 32];  // randSphere acceptance per position
-  double red[kSerialThreads / 32];
+  double red[3 * (kSerialThreads / 32)];
   GenPlan plan;
   int s_accept, s_ext_bad;
   int s_off[kPivotMax], s_boff[kPivotMax];  // draw offsets per bead
@@ -477,9 +508,7 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
     }
     for (int i = threadIdx.x; i < slots->n_k; i += blockDim.x)
       c += slots->slots[2 * (slots->k_off + i)];
-    a = bsum<kSerialThreads>(a, red);
-    b = bsum<kSerialThreads>(b, red);
-    c = bsum<kSerialThreads>(c, red);
+    bsum3<kSerialThreads>(a, b, c, red);
     if (threadIdx.x == 0) {
       S.red_lj = a;
       S.red_re = b;
@@ -548,8 +577,6 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
       }
       dmz += t.w * (t.z - p.z);
     }
-    ext = bsum<kSerialThreads>(ext, red);
-    dmz = bsum<kSerialThreads>(dmz, red);
     // bonds of the moved molecule at trial positions
     const int m0 = B.mol_start[mol], m1 = B.mol_start[mol + 1];
     double bt = 0.0;
@@ -560,7 +587,7 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
         double r = sqrt(dx * dx + dy * dy + dz * dz);
         bt += 0.5 * P.k_bond * (r - P.r0) * (r - P.r0);
       }
-    bt = bsum<kSerialThreads>(bt, red);
+    bsum3<kSerialThreads>(ext, dmz, bt, red);
     if (threadIdx.x == 0) {
       // the delta kernel applied any pending S(k) commit if it ran k tiles
       if (P.use_ewald && b_hi > b_lo) S.sk_pending = 0;
