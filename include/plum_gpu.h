@@ -372,16 +372,19 @@ int plum_batch_time_kernels(plum_batch* batch, int n_steps, double* out4);
 /* Work items of the batched energy change: (moved, other) pairs per pair
  * item (>= 1024, a multiple of 256; a pair item holds up to 32 moved beads
  * against item_pairs / 32 other beads, at least 256), k-vectors per k item
- * (64..256), the grid (0: 4 blocks per SM) and the register budget as
+ * (64..256, or 512 / 1024: up to four per thread, the moved beads' phase
+ * tables built once per item), the grid (0: 4 blocks per SM) and the register budget as
  * resident blocks per SM (2, 3 or 4). They change only the summation order
  * inside FP32 partials. */
 int plum_batch_set_tune(plum_batch* batch, int item_pairs, int k_tile, int grid,
                         int min_blocks);
 /* Times the energy-change kernel on these replicas (`steps` steps per
  * candidate, see plum_batch_time_kernels) for item sizes {2048, 4096, 8192,
- * 16384} x k tiles {128, 256} x grids {2, 3, 4, 6, 8} blocks per SM x
- * register budgets {2, 3, 4} blocks per SM, keeps the fastest; out4 (may be
- * NULL) = the chosen {item_pairs, k_tile, grid, min_blocks}. */
+ * 16384} x k tiles {128, 256, 512, 1024} x grids {2, 3, 4, 6, 8} blocks per
+ * SM x register budgets {2, 3, 4} blocks per SM, keeps the fastest (then the
+ * real-space term's FP32 erfc fit against the table at those sizes, see
+ * plum_batch_set_real_term); out4 (may be NULL) = the chosen {item_pairs,
+ * k_tile, grid, min_blocks}. */
 int plum_batch_autotune(plum_batch* batch, int steps, int* out4);
 /* The real-space Ewald term of the batched energy change: table = 1 (the
  * default where it applies) evaluates erfc(sqrt(alpha) r)/r as

@@ -586,6 +586,11 @@ static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out) {
     P.inv_fix[a] = 4294967296.0 / P.ebox[a];
     P.f_box[a] = (float)P.ebox[a];
   }
+  // the largest LJ (or hard-sphere bound) cut-off over the type pairs in
+  // use: a uniform pre-test before the per-pair table lookup; > 0, so a
+  // coincident pair (r2 = 0, the overlap value) always reaches lj64
+  P.lj_max2 = 1e-300;
+  for (int k = 0; k < P.n_type * P.n_type; k++) P.lj_max2 = std::max(P.lj_max2, P.lj_rc2[k]);
   for (int k = 0; k < kMaxT2; k++) {
     P.f_lj_sig2[k] = (float)P.lj_sig2[k];
     P.f_lj_eps4[k] = (float)P.lj_eps4[k];
@@ -2486,7 +2491,8 @@ int plum_batch_time_kernels(plum_batch* b, int n_steps, double* out4) {
 
 int plum_batch_set_tune(plum_batch* b, int item_pairs, int k_tile, int grid, int min_blocks) {
   if (!b || item_pairs < kMinItemPairs || item_pairs % 256 || k_tile < kMinKTile ||
-      k_tile > kPairThreads || grid < 0 || grid > 65535 || min_blocks < 2 || min_blocks > 4)
+      k_tile > 4 * kPairThreads || (k_tile > kPairThreads && k_tile % kPairThreads) ||
+      grid < 0 || grid > 65535 || min_blocks < 2 || min_blocks > 4)
     return fail(PLUM_ERR_INPUT, "bad work-item sizes");
   b->tune = BatchTune{item_pairs, k_tile, grid, min_blocks, b->tune.htab};
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
@@ -2574,7 +2580,7 @@ int plum_batch_autotune(plum_batch* b, int steps, int* out4) {
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
   const int pairs[] = {2048, 4096, 8192, 16384};
-  const int ktiles[] = {128, 256};
+  const int ktiles[] = {128, 256, 512, 1024};
   const int per_sm[] = {2, 3, 4, 6, 8};
   const int occ[] = {2, 3, 4};
   double best = 1e300;

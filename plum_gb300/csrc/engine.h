@@ -103,6 +103,7 @@ struct DevParams {
   const double* htab64;
   double alpha;
   int same_wrap;
+  double lj_max2;  // largest lj_rc2 over the type pairs in use
 };
 
 // The pending move: beads [b_lo, b_hi) of molecule `mol` hold trial

@@ -88,7 +88,8 @@ __device__ __forceinline__ void pair64(const DevParams& P, double4_32a a, int ta
     const double x = wrap_d(dx, P.box[0], P.inv_box[0]);
     const double y = wrap_d(dy, P.box[1], P.inv_box[1]);
     const double z = P.npbc > 2 ? wrap_d(dz, P.box[2], P.inv_box[2]) : dz;
-    if (P.use_pair) lj += lj64(P, ta * P.n_type + tb, x * x + y * y + z * z);
+    const double r2 = x * x + y * y + z * z;
+    if (P.use_pair && r2 < P.lj_max2) lj += lj64(P, ta * P.n_type + tb, r2);
     if (P.use_ewald) {
       const double qq = a.w * b.w;
       if (qq != 0.0) re += P.lB * qq * real_images64(P, x, y, z);

@@ -409,6 +409,8 @@ void build_h32_table(float4* out) {
 }
 
 // ------------------------------------------------------------ replicas
+constexpr int kMaxKPerThread = 4;  // k vectors per thread of a k item (k_tile <= 1024)
+static_assert(kMaxKPerThread * kPairThreads >= 1024, "k items of up to 1024 vectors");
 // Batched replicas: every replica's pending move contributes pair items
 // (up to kPairGroup moved beads, staged in shared memory at their trial and
 // current positions, x a chunk of other beads, one per thread), one item for
@@ -549,14 +551,25 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
         slots[2 * item + 1] = (double)b;
       }
     } else {
+      // a k item of up to kMaxKPerThread * kPairThreads vectors: thread t
+      // takes k = tile * k_tile + t + q kPairThreads, so the moved beads'
+      // phase tables, built once per item, serve up to four vectors per thread
       const int tile = local - s_np[r];
       const int sk_pend = st->sk_pending, sk_buf = st->sk_buf, cur_buf = st->cur_buf;
-      const int k = tile * kKTile32 + threadIdx.x;
-      const bool mine = threadIdx.x < kKTile32 && k < P.n_k;
-      const short4 kv = mine ? B.kn[k] : make_short4(0, 0, 0, 0);
+      int kk[kMaxKPerThread];
+      bool mine[kMaxKPerThread];
+      short4 kv[kMaxKPerThread];
+      float2 ds[kMaxKPerThread];
+#pragma unroll
+      for (int q = 0; q < kMaxKPerThread; q++) {
+        const int t = threadIdx.x + q * kPairThreads;
+        kk[q] = tile * kKTile32 + t;
+        mine[q] = t < kKTile32 && kk[q] < P.n_k;
+        kv[q] = mine[q] ? B.kn[kk[q]] : make_short4(0, 0, 0, 0);
+        ds[q] = make_float2(0.0f, 0.0f);
+      }
       float2* tabs = reinterpret_cast<float2*>(smem);
       const int per = P.kper, chunk = P.kchunk_delta;
-      float2 ds = make_float2(0.0f, 0.0f);
       for (int c0 = b_lo; c0 < b_hi; c0 += chunk) {
         const int cnt = min(chunk, b_hi - c0);
         __syncthreads();
@@ -566,26 +579,32 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
           table32(P, f, B.fq[c0 + bead], axis, tabs + (bead * 2 + which) * per);
         }
         __syncthreads();
-        if (mine)
-          for (int bb = 0; bb < cnt; bb++) {
-            float2 e1 = phase32(P, tabs + (bb * 2 + 0) * per, kv);
-            float2 e0 = phase32(P, tabs + (bb * 2 + 1) * per, kv);
-            ds.x += e1.x - e0.x;
-            ds.y += e1.y - e0.y;
-          }
+#pragma unroll
+        for (int q = 0; q < kMaxKPerThread; q++)
+          if (mine[q])
+            for (int bb = 0; bb < cnt; bb++) {
+              float2 e1 = phase32(P, tabs + (bb * 2 + 0) * per, kv[q]);
+              float2 e0 = phase32(P, tabs + (bb * 2 + 1) * per, kv[q]);
+              ds[q].x += e1.x - e0.x;
+              ds[q].y += e1.y - e0.y;
+            }
       }
       float e = 0.0f;
-      if (mine) {
-        double2 sv = B.sk[k];
-        if (sk_pend) {
-          const double2 pd = B.dsk[(size_t)sk_buf * P.n_k + k];
-          sv = make_double2(sv.x + pd.x, sv.y + pd.y);
-          B.sk[k] = sv;
+#pragma unroll
+      for (int q = 0; q < kMaxKPerThread; q++)
+        if (mine[q]) {
+          const int k = kk[q];
+          double2 sv = B.sk[k];
+          if (sk_pend) {
+            const double2 pd = B.dsk[(size_t)sk_buf * P.n_k + k];
+            sv = make_double2(sv.x + pd.x, sv.y + pd.y);
+            B.sk[k] = sv;
+          }
+          const float2 d = ds[q];
+          B.dsk[(size_t)cur_buf * P.n_k + k] = make_double2((double)d.x, (double)d.y);
+          const float sx = (float)sv.x, sy = (float)sv.y;
+          e += (float)B.kw[k] * (2.0f * (sx * d.x + sy * d.y) + (d.x * d.x + d.y * d.y));
         }
-        B.dsk[(size_t)cur_buf * P.n_k + k] = make_double2((double)ds.x, (double)ds.y);
-        const float sx = (float)sv.x, sy = (float)sv.y;
-        e = (float)B.kw[k] * (2.0f * (sx * ds.x + sy * ds.y) + (ds.x * ds.x + ds.y * ds.y));
-      }
       e = block_sum32<kPairThreads>(e, red);
       if (threadIdx.x == 0) {
         slots[2 * item] = (double)e;

@@ -981,8 +981,10 @@ __global__ void k_cell_scatter(const DevParams* __restrict__ rp,
   B.cell_key[j] = k;
 }
 
-constexpr int kCellBeads = 2;  // moved beads per block
-constexpr int kCellSplit = 4;  // warps per (bead, before / after), each a quarter of its entries
+// moved beads per block: a warp per (bead, before / after); many beads per
+// block keep the per-block histogram flush (global atomics) few
+constexpr int kCellBeads = 16;
+constexpr int kCellSplit = 1;  // warps per (bead, before / after), each a part of its entries
 constexpr int kCellWarps = 2 * kCellBeads * kCellSplit;
 
 // Block (x, r): moved beads [4x, 4x + 4) of replica r's pending surrogate
@@ -993,7 +995,7 @@ constexpr int kCellWarps = 2 * kCellBeads * kCellSplit;
 // once, at the end). Entries carry the positions, so a candidate costs one
 // load, and the 27 cells' entries form one list spread over the lanes. The
 // same pairs, distances and bins as k_desc.
-__global__ void __launch_bounds__(kCellWarps * 32)
+__global__ void __launch_bounds__(kCellWarps * 32, 1)
     k_desc_cells(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb) {
   const DevParams& P = rp[blockIdx.y];
   const DevBuffers& B = rb[blockIdx.y];
