@@ -394,19 +394,30 @@ def precision_on_chain(d, device, n, seed, label):
 
 
 def equilibrium(args, device, sg, tune):
-    """Equilibrium statistics of the chosen form on the workload.
+    """Statistics of the chosen form on the workload, against plain
+    Metropolis and plain FP64, from common starting configurations.
 
     R replicas (the first R of the throughput batch: same starts) are burnt
-    in with the chosen form. From the equilibrated configurations: (a) the
-    chosen form and (b) the plain Metropolis dynamics in the precision form
-    (the plain FP64 form's dynamics: the two decide alike but for the flip
-    fraction measured by precision_on_chain) run side by side, sampled every
-    `every` moves; tau_int of the chains' Rg^2 (pooled over all chains, Sokal
-    window c = 5) and of the total energy for each; (c) R plain FP64 systems
-    run from the same configurations. The chosen form's per-replica means of
-    the total energy and the chain-averaged Rg^2 are compared with the plain
-    FP64 runs' (paired by starting configuration): the mean difference must
-    lie within 2 standard errors of the paired differences."""
+    in with the chosen form; the trace of the mean energy and Rg^2 and the
+    energy drift over the last fifth of the burn-in say how close to
+    equilibrium the starts are. From them:
+      (a) the chosen form and the plain Metropolis dynamics in the precision
+          form run side by side for the same number of moves (different
+          seeds), sampled every `tau_every` moves: tau_int of the chains'
+          Rg^2 (pooled over all chains, Sokal window c = 5, an exponential
+          fit when the window does not close) and of the total energy, and
+          the paired check of their per-replica means (same protocol: with
+          the 12 k_BT dead zone stage one only rejects moves Metropolis
+          rejects but for the surrogate's errors, and delayed acceptance
+          keeps the stationary distribution);
+      (b) plain Metropolis in FP32 and in FP64 from the same starts with the
+          same seeds: the two make the same decisions until a flipped one,
+          so their trajectories (and Rg^2, exactly) agree until then; the
+          replicas whose trajectories stayed identical and the largest
+          energy difference are reported;
+      (c) the chosen form's per-replica means against the FP64 runs' of (b):
+          the direct check, valid when the starts are equilibrated (the
+          burn-in drift says whether they are)."""
     import numpy as np
     import plum_gb300 as pg
     R = args.stat_replicas
@@ -433,6 +444,12 @@ def equilibrium(args, device, sg, tune):
     out["burn_in_trace"] = {"moves": [t[0] for t in trace],
                             "mean_energy": [t[1] for t in trace],
                             "mean_rg2": [t[2] for t in trace]}
+    k = max(1, len(trace) // 5)
+    if len(trace) > k:
+        de = trace[-1][1] - trace[-1 - k][1]
+        dm = trace[-1][0] - trace[-1 - k][0]
+        out["burn_in_energy_drift_per_1e5_moves"] = de / dm * 1e5
+        out["burn_in_rg2_drift_per_1e5_moves"] = (trace[-1][2] - trace[-1 - k][2]) / dm * 1e5
 
     def series(net, seed0, moves, every):
         b = pg.Batch(dirs, device=device)
@@ -468,34 +485,55 @@ def equilibrium(args, device, sg, tune):
                      "wall_s": wall, "mean_energy_per_replica": E.mean(axis=0).tolist(),
                      "mean_rg2_per_replica": Gm.mean(axis=0).tolist()}
     out["series"] = res
+    ch, pl = res["chosen_form"], res["plain_dynamics_fp32"]
+    out["chosen_vs_plain_dynamics"] = {
+        "energy": paired_check(ch["mean_energy_per_replica"], pl["mean_energy_per_replica"]),
+        "rg2": paired_check(ch["mean_rg2_per_replica"], pl["mean_rg2_per_replica"]),
+        "definition": "(a): same starts, same number of moves, different seeds; per-replica "
+                      "means, mean paired difference against 2 standard errors"}
 
-    # plain FP64 systems from the same starting configurations
+    # (b) FP32 and FP64 plain Metropolis, same starts and seeds
     t1 = time.perf_counter()
-    Ep, Gp = [], []
+    Ep, Gp, same, worst = [], [], 0, 0.0
     for r in range(R):
-        s = pg.System(dirs[r], form=pg.FORM_FP64, device=device)
-        s.set_positions(snap[r])
-        s.seed(15000 + r)
-        e, g = [], []
+        s64 = pg.System(dirs[r], form=pg.FORM_FP64, device=device)
+        s32 = pg.System(dirs[r], form=pg.FORM_FP32, device=device)
+        s64.set_positions(snap[r])
+        s32.set_positions(snap[r])
+        s64.seed(15000 + r)
+        s32.seed(15000 + r)
+        e, g, ident = [], [], True
         for _ in range(args.plain_stat_moves // args.plain_stat_every):
-            s.run(args.plain_stat_every)
-            e.append(s.energies().sum())
-            g.append(s.observables()[0])
+            s64.run(args.plain_stat_every)
+            s32.run(args.plain_stat_every)
+            e64, e32 = s64.energies().sum(), s32.energies().sum()
+            g64, g32 = s64.observables()[0], s32.observables()[0]
+            e.append(e64)
+            g.append(g64)
+            if ident:
+                ident = g64 == g32
+                worst = max(worst, abs(e64 - e32) / max(1.0, abs(e64)))
+        same += int(ident)
         Ep.append(np.mean(e))
         Gp.append(np.mean(g))
-        s.close()
+        s64.close()
+        s32.close()
     out["plain_fp64"] = {"moves_per_replica": args.plain_stat_moves,
                          "moves_per_sample": args.plain_stat_every,
                          "wall_s": time.perf_counter() - t1,
                          "mean_energy_per_replica": Ep, "mean_rg2_per_replica": Gp}
-    ch = res["chosen_form"]
+    out["fp32_vs_fp64_same_seeds"] = {
+        "replicas_identical_trajectories": same, "replicas": R,
+        "max_rel_energy_difference_while_identical": worst,
+        "definition": "(b): a replica counts as identical when Rg^2 of the FP32 and FP64 "
+                      "chains agreed exactly at every sample (no flipped decision)"}
+    # (c) the direct check
     out["stat_check"] = {
         "energy": paired_check(ch["mean_energy_per_replica"], Ep),
         "rg2": paired_check(ch["mean_rg2_per_replica"], Gp),
-        "definition": "per-replica means of the chosen form (over its tau series) and of the "
-                      "plain FP64 form, each started from the same equilibrated "
-                      "configuration; the mean paired difference against 2 standard "
-                      "errors of the paired differences"}
+        "definition": "(c): the chosen form's per-replica means over its series against the "
+                      "plain FP64 runs' over theirs, each from the same starting configuration; "
+                      "valid when the starts are equilibrated (see the burn-in drift)"}
     return out
 
 
@@ -579,7 +617,8 @@ def profile_case(args, local):
                           "steps": args.batch_steps, "ms_per_batch": ms,
                           "moves_per_s": len(dirs) * args.batch_steps / (ms / 1e3),
                           "autotuned_items": tune, "setup_s": setup_s,
-                          "real_term": "table" if b.real_term() else "erfc fit",
+                          "pair_loop": "shared h(u) table, paired evaluations" if b.real_term()
+                          else "one evaluation at a time",
                           "kernel_ms_per_launch": dict(zip(
                               ("delta", "serial", "descriptor", "inference"),
                               [float(x) for x in b.time_kernels(8)]))}), flush=True)
@@ -723,8 +762,8 @@ def main():
                     help="moves per replica of the plain FP64 statistics runs")
     ap.add_argument("--plain-stat-every", type=int, default=1000)
     ap.add_argument("--real-term", default="auto", choices=["auto", "table", "fit"],
-                    help="real-space term of the batched kernel: the autotuner's pick, the "
-                         "h(u) table or the erfc fit")
+                    help="pair loop of the batched kernel: the autotuner's pick, the shared "
+                         "h(u) table with paired evaluations, or one evaluation at a time")
     ap.add_argument("--only", default=None,
                     choices=[None, "fp32", "fp64", "total", "batch", "chosen", "da", "train",
                              "pressure", "cbmc", "precision", "stats"],
@@ -770,7 +809,8 @@ def main():
     tune = batch.autotune(16)
     if args.real_term != "auto":
         batch.set_real_term(args.real_term == "table")
-    real_term = "table" if batch.real_term() else "erfc fit"
+    real_term = ("shared h(u) table, paired evaluations" if batch.real_term()
+                 else "one evaluation at a time")
     batch.set_groups(args.groups)
     for _ in range(args.warmup):
         batch.run(BS)
@@ -977,7 +1017,7 @@ def main():
                    "l2": "flushed between steps (256 MB write)", "parallelism": "replicas",
                    "autotuned_items": {"pairs_per_item": tune[0], "k_per_tile": tune[1],
                                        "grid": tune[2], "resident_blocks_per_sm": tune[3],
-                                       "real_space_term": real_term},
+                                       "pair_loop": real_term},
                    "step_chains": args.groups},
         "fp64_recompute": recompute,
         "batched_fp32_no_surrogate": {"value": batched32, "unit": "moves/s",

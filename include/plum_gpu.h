@@ -382,18 +382,21 @@ int plum_batch_set_tune(plum_batch* batch, int item_pairs, int k_tile, int grid,
  * candidate, see plum_batch_time_kernels) for item sizes {2048, 4096, 8192,
  * 16384} x k tiles {128, 256, 512, 1024} x grids {2, 3, 4, 6, 8} blocks per
  * SM x register budgets {2, 3, 4} blocks per SM, keeps the fastest (then the
- * real-space term's FP32 erfc fit against the table at those sizes, see
- * plum_batch_set_real_term); out4 (may be NULL) = the chosen {item_pairs,
+ * two pair loops of plum_batch_set_real_term at those sizes); out4 (may be
+ * NULL) = the chosen {item_pairs,
  * k_tile, grid, min_blocks}. */
 int plum_batch_autotune(plum_batch* batch, int steps, int* out4);
-/* The real-space Ewald term of the batched energy change: table = 1 (the
- * default where it applies) evaluates erfc(sqrt(alpha) r)/r as
- * sqrt(alpha) h(alpha r^2) from a table of h(u) = erfc(sqrt u)/sqrt u (cubic
- * pieces, 32 per octave of u, about 1e-7 relative below u = 4), for LJ +
- * Ewald replicas whose real cut-off is at most half the box; table = 0 uses
- * the FP32 erfc fit everywhere. PLUM_ERR_INPUT if a replica's alpha r_c^2 is
- * past the table (2^5). plum_batch_autotune keeps whichever is faster at the
- * sizes it picks; plum_batch_real_term reports the current choice. */
+/* The pair loop of the batched energy change. table = 1 (the default where
+ * it applies): for LJ + Ewald replicas whose real cut-off is at most half
+ * the box, the table of h(u) = erfc(sqrt u)/sqrt u (cubic pieces, 32 per
+ * octave of u, about 1e-7 relative below u = 4; erfc(sqrt(alpha) r)/r =
+ * sqrt(alpha) h(alpha r^2)) staged in shared memory and the trial and current
+ * evaluations of a pair done together, branch-free. table = 0: the loop of
+ * one evaluation at a time, the term from the context's table in global
+ * memory (or the FP32 erfc fit where a cut-off lies past the table).
+ * PLUM_ERR_INPUT for table = 1 if a replica's alpha r_c^2 is past the table
+ * (2^5). plum_batch_autotune keeps whichever is faster at the sizes it picks;
+ * plum_batch_real_term reports the current choice. */
 int plum_batch_set_real_term(plum_batch* batch, int table);
 int plum_batch_real_term(const plum_batch* batch);
 /* The h(u) table itself (host copy, built like the batch's): out[4 b + q] =

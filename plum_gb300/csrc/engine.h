@@ -283,8 +283,9 @@ struct BatchTune {
 // erfc(sqrt(alpha) r) / r = sqrt(alpha) h(alpha r^2) as a function of the
 // dimensionless u = alpha r^2 alone, so one table serves every system. Bins:
 // kH32Per per octave of u for octaves 2^kH32ELo .. 2^(kH32EHi - 1); bin b
-// holds a cubic in y = f - 1/2, f in [0, 1) the bin-local fraction of u
-// (its float mantissa bits below the top five). Built on the host by
+// holds a cubic in v = 1 + f, f in [0, 1) the bin-local fraction of u
+// (its float mantissa bits below the top five).
+// Built on the host by
 // Chebyshev interpolation of std::erfc in double precision (build_h32_table).
 constexpr int kH32ELo = -14, kH32EHi = 5, kH32Per = 32;
 constexpr int kH32Bins = (kH32EHi - kH32ELo) * kH32Per;

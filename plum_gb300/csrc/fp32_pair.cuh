@@ -37,16 +37,16 @@ constexpr int kH32LoBits = (127 + kH32ELo) << 23;  // float bits of 2^kH32ELo
 
 // h(u) = erfc(sqrt u) / sqrt u from the table (in shared memory) at the
 // float bits of u: the exponent and top five mantissa bits pick the bin, the
-// remaining 18 bits are the bin-local fraction f (shifted up into a float of
-// [1, 2), 1 + f exactly), y = f - 1/2. Bins outside
+// remaining 18 bits are the bin-local fraction f, shifted up into a float
+// v = 1 + f of [1, 2) exactly; the bin's cubic is in v. Bins outside
 // the table are clamped (their values are replaced or cut off by the caller).
 __device__ __forceinline__ float h32_tab(const float4* tab, int bits) {
   int idx = (bits >> 18) - ((127 + kH32ELo) << 5);
   idx = min(max(idx, 0), kH32Bins - 1);
   const float4 c = tab[idx];
-  // the 18 bits below the bin index moved to the top of a float in [1, 2)
-  const float y = __int_as_float(((bits << 5) & 0x7FFFFF) | 0x3F800000) - 1.5f;
-  return fmaf(fmaf(fmaf(c.w, y, c.z), y, c.y), y, c.x);
+  // the 18 bits below the bin index moved to the top of a float: v = 1 + f
+  const float v = __int_as_float(((bits << 5) & 0x7FFFFF) | 0x3F800000);
+  return fmaf(fmaf(fmaf(c.w, v, c.z), v, c.y), v, c.x);
 }
 
 // Below the table (u < 2^kH32ELo: r under 1/128 of 1/sqrt(alpha)): the erfc

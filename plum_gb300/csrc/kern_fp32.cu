@@ -317,17 +317,19 @@ __device__ __forceinline__ void pair_sweep(const DevParams& P, const PairConst& 
 // pair_sweep for LJ + Ewald with r_c <= L/2 on every axis, the real-space term
 // from the h(u) table: per (moved u, other j) the trial and current distances
 // share the other bead's load, one LJ pre-test and one charge product, and the
-// cut-off is a select, so a warp runs no divergent erfc. kCubic (equal
-// fixed-point scales on the three axes): r^2 stays in fixed-point units and
-// the box scale is folded into the constants. gn4 staged beads, a multiple of
-// 4 (the padding beads have q = 0 and equal trial and current positions, so
-// they add exactly zero).
+// cut-off is a select, so a warp runs no divergent erfc. Each thread takes two
+// other beads per staged bead, so one load of the staged trial and current
+// entries serves four evaluations. kCubic (equal fixed-point scales on the
+// three axes): r^2 stays in fixed-point units and the box scale is folded
+// into the constants. gn4 staged beads, a multiple of 4; the trial entry's w
+// holds the staged bead's charge (float bits) and the current entry's w its
+// type; the padding beads have q = 0 and equal trial and current positions,
+// so they add exactly zero.
 template <bool kCubic>
 __device__ __forceinline__ void pair_sweep_tab(const DevParams& P, const DevBuffers& B,
-                                               const int4* s_mt, const float* s_mq,
-                                               const float4* s_h, int gn4, int c0, int c1,
-                                               int b_lo, int b_hi, float& acc_lj,
-                                               float& acc_re) {
+                                               const int4* s_mt, const float4* s_h, int gn4,
+                                               int c0, int c1, int b_lo, int b_hi,
+                                               float& acc_lj, float& acc_re) {
   const float sx = P.f_scale[0], sy = P.f_scale[1], sz = P.f_scale[2];
   const float cs = kCubic ? sx * sx : 1.0f;  // real r^2 per unit of r2 below
   const float ics = 1.0f / cs;
@@ -339,43 +341,58 @@ __device__ __forceinline__ void pair_sweep_tab(const DevParams& P, const DevBuff
   const float pref = P.f_lB * P.f_sqrt_alpha;
   const int nt = P.n_type;
   const bool use_pair = P.use_pair;
-  for (int j = c0 + threadIdx.x; j < c1; j += kPairThreads) {
-    if (j >= b_lo && j < b_hi) continue;  // moved pairs: the last item
-    const int4 cj = B.fpos[j];
-    const float qj = B.fq[j] * pref;
+  // one evaluation pair (trial, current) of staged bead (t, c) with other
+  // bead o; ok: o is an other bead of this item (not moved, inside the chunk)
+  auto eval = [&](const int4 t, const int4 c, const int4 o, float qo, bool ok, float& acc) {
+    float x1 = (float)(int)((unsigned)o.x - (unsigned)t.x);
+    float y1 = (float)(int)((unsigned)o.y - (unsigned)t.y);
+    float z1 = (float)(int)((unsigned)o.z - (unsigned)t.z);
+    float x0 = (float)(int)((unsigned)o.x - (unsigned)c.x);
+    float y0 = (float)(int)((unsigned)o.y - (unsigned)c.y);
+    float z0 = (float)(int)((unsigned)o.z - (unsigned)c.z);
+    if (!kCubic) {
+      x1 *= sx, y1 *= sy, z1 *= sz;
+      x0 *= sx, y0 *= sy, z0 *= sz;
+    }
+    const float r1 = fmaf(x1, x1, fmaf(y1, y1, z1 * z1));
+    const float r0 = fmaf(x0, x0, fmaf(y0, y0, z0 * z0));
+    if (use_pair && ok && fminf(r1, r0) < ljlim) {
+      const int k = c.w * nt + o.w;  // trial and current share the type
+      acc_lj += lj32(P, k, r1 * cs) - lj32(P, k, r0 * cs);
+    }
+    const int b1 = __float_as_int(r1 * ua), b0 = __float_as_int(r0 * ua);
+    float h1 = h32_tab(s_h, b1), h0 = h32_tab(s_h, b0);
+    if (min(b1, b0) < kH32LoBits) {
+      if (b1 < kH32LoBits) h1 = h32_small(__int_as_float(b1));
+      if (b0 < kH32LoBits) h0 = h32_small(__int_as_float(b0));
+    }
+    h1 = r1 <= rc2 ? h1 : 0.0f;
+    h0 = r0 <= rc2 ? h0 : 0.0f;
+    acc = fmaf(__int_as_float(t.w) * qo, h1 - h0, acc);
+  };
+  for (int j0 = c0 + threadIdx.x; j0 < c1; j0 += 2 * kPairThreads) {
+    const int j1 = j0 + kPairThreads;
+    const bool ok0 = !(j0 >= b_lo && j0 < b_hi);  // moved pairs: the last item
+    const bool ok1 = j1 < c1 && !(j1 >= b_lo && j1 < b_hi);
+    const int4 o0 = B.fpos[j0];
+    const int4 o1 = j1 < c1 ? B.fpos[j1] : o0;
+    const float q0 = ok0 ? B.fq[j0] * pref : 0.0f;
+    const float q1 = ok1 ? B.fq[j1] * pref : 0.0f;
+    float a0 = 0.0f, a1 = 0.0f;
 #pragma unroll 4
     for (int u = 0; u < gn4; u++) {
       const int4 t = s_mt[u], c = s_mt[kPairGroup + u];
-      float x1 = (float)(int)((unsigned)cj.x - (unsigned)t.x);
-      float y1 = (float)(int)((unsigned)cj.y - (unsigned)t.y);
-      float z1 = (float)(int)((unsigned)cj.z - (unsigned)t.z);
-      float x0 = (float)(int)((unsigned)cj.x - (unsigned)c.x);
-      float y0 = (float)(int)((unsigned)cj.y - (unsigned)c.y);
-      float z0 = (float)(int)((unsigned)cj.z - (unsigned)c.z);
-      if (!kCubic) {
-        x1 *= sx, y1 *= sy, z1 *= sz;
-        x0 *= sx, y0 *= sy, z0 *= sz;
-      }
-      const float r1 = fmaf(x1, x1, fmaf(y1, y1, z1 * z1));
-      const float r0 = fmaf(x0, x0, fmaf(y0, y0, z0 * z0));
-      if (use_pair && fminf(r1, r0) < ljlim)
-        acc_lj += lj32(P, t.w * nt + cj.w, r1 * cs) - lj32(P, c.w * nt + cj.w, r0 * cs);
-      const int b1 = __float_as_int(r1 * ua), b0 = __float_as_int(r0 * ua);
-      float h1 = h32_tab(s_h, b1), h0 = h32_tab(s_h, b0);
-      if (min(b1, b0) < kH32LoBits) {
-        if (b1 < kH32LoBits) h1 = h32_small(__int_as_float(b1));
-        if (b0 < kH32LoBits) h0 = h32_small(__int_as_float(b0));
-      }
-      h1 = r1 <= rc2 ? h1 : 0.0f;
-      h0 = r0 <= rc2 ? h0 : 0.0f;
-      acc_re = fmaf(s_mq[u] * qj, h1 - h0, acc_re);
+      eval(t, c, o0, q0, ok0, a0);
+      eval(t, c, o1, q1, ok1, a1);
     }
+    acc_re += a0 + a1;
   }
 }
 
-// The table (kH32Bins float4): per bin the cubic through h at the four
-// Chebyshev nodes of y in [-1/2, 1/2], h in double precision from std::erfc,
-// the 4 x 4 Vandermonde system solved by Gaussian elimination.
+// The table (kH32Bins float4): per bin the cubic in v = 1 + f (f the
+// bin-local fraction) through h at the four Chebyshev nodes of the bin, h in
+// double precision from std::erfc, the 4 x 4 Vandermonde system solved by
+// Gaussian elimination with partial pivoting.
 void build_h32_table(float4* out) {
   const double kPi = 3.14159265358979323846;
   int i = 0;
@@ -385,11 +402,12 @@ void build_h32_table(float4* out) {
       const double w = std::ldexp(1.0 / kH32Per, e);
       double A[4][5];
       for (int k = 0; k < 4; k++) {
-        const double y = 0.5 * std::cos(kPi * (k + 0.5) / 4.0);
+        const double y = 0.5 * std::cos(kPi * (k + 0.5) / 4.0);  // in [-1/2, 1/2]
         const double u = lo + (y + 0.5) * w;
         const double r = std::sqrt(u);
+        const double v = y + 1.5;  // the kernel's variable, 1 + f
         double p = 1.0;
-        for (int q = 0; q < 4; q++, p *= y) A[k][q] = p;
+        for (int q = 0; q < 4; q++, p *= v) A[k][q] = p;
         A[k][4] = std::erfc(r) / r;
       }
       for (int col = 0; col < 4; col++) {
@@ -505,12 +523,14 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
         __syncthreads();  // the previous item may still read the staging area
         for (int u = threadIdx.x; u < gn4; u += kPairThreads) {
           if (u < gn) {
-            s_mt[u] = B.ftrial[g0 + u];
+            int4 t = B.ftrial[g0 + u];
+            if (tab) t.w = __float_as_int(B.fq[b_lo + g0 + u]);  // the type stays in c.w
+            s_mt[u] = t;
             s_mt[kPairGroup + u] = B.fpos[b_lo + g0 + u];
             s_mq[u] = B.fq[b_lo + g0 + u];
           } else {
             const int4 p = B.fpos[b_lo + g0 + gn - 1];
-            s_mt[u] = p;
+            s_mt[u] = make_int4(p.x, p.y, p.z, __float_as_int(0.0f));
             s_mt[kPairGroup + u] = p;
             s_mq[u] = 0.0f;
           }
@@ -519,11 +539,9 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
         const PairConst K = pair_const(P);
         if (tab) {
           if (P.npbc == 3 && P.f_scale[0] == P.f_scale[1] && P.f_scale[1] == P.f_scale[2])
-            pair_sweep_tab<true>(P, B, s_mt, s_mq, s_h, gn4, c0, c1, b_lo, b_hi, acc_lj,
-                                 acc_re);
+            pair_sweep_tab<true>(P, B, s_mt, s_h, gn4, c0, c1, b_lo, b_hi, acc_lj, acc_re);
           else
-            pair_sweep_tab<false>(P, B, s_mt, s_mq, s_h, gn4, c0, c1, b_lo, b_hi, acc_lj,
-                                  acc_re);
+            pair_sweep_tab<false>(P, B, s_mt, s_h, gn4, c0, c1, b_lo, b_hi, acc_lj, acc_re);
         } else if (P.single_image)
           pair_sweep<true>(P, K, B, s_mt, s_mq, gn, b_lo + g0, c0, c1, b_lo, b_hi, acc_lj,
                            acc_re);

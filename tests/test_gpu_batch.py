@@ -17,7 +17,7 @@ def pg():
 
 
 @pytest.mark.parametrize("tune", [None, (2048, 256, 304, 2), (16384, 64, 1216, 3),
-                                  (4096, 128, 608, 4)])
+                                  (4096, 128, 608, 4), (4096, 1024, 608, 4)])
 def test_uneven_replicas_replay_their_references(pg, tune):
     """Also with other work-item sizes than the defaults (what the autotuner
     may pick): the items only change the order of FP32 partial sums."""
@@ -44,6 +44,24 @@ def test_uneven_replicas_replay_their_references(pg, tune):
         if not g["ewald"][14]:
             fresh = rep.total_energy()[:4].sum()
             assert rel(e, fresh, max(1.0, abs(fresh))) < 1e-4
+
+
+@pytest.mark.parametrize("table", [True, False])
+def test_real_space_term_table_and_fit_replay(pg, table):
+    """Both real-space terms of the batched kernel (the h(u) table and the
+    FP32 erfc fit) replay the reference's bulk fixtures to 1e-4 after 150
+    steps."""
+    cases = [c for c in CASES if not load(c)[1]["ewald"][14]]
+    dirs, gs = zip(*[load(c) for c in cases])
+    b = pg.Batch(list(dirs))
+    b.set_real_term(table)
+    assert b.real_term() == int(table)
+    b.seed(np.array([int(g["run_seed"]) for g in gs], np.uint32))
+    b.run(150)
+    for r, g in enumerate(gs):
+        e = b.replica(r).energies().sum()
+        ref = g["run_etot"][149]
+        assert rel(e, ref, max(1.0, abs(ref))) < 1e-4, (cases[r], table, e, ref)
 
 
 def test_replicas_match_single_system_runs(pg):
@@ -75,7 +93,8 @@ def test_autotune_picks_a_candidate_and_keeps_running(pg):
     b = pg.Batch([d] * 8)
     b.seed(3)
     ip, kt, grid, mb = b.autotune(4)
-    assert ip in (2048, 4096, 8192, 16384) and kt in (128, 256) and grid > 0 and mb in (2, 3, 4)
+    assert ip in (2048, 4096, 8192, 16384) and kt in (128, 256, 512, 1024) and grid > 0
+    assert mb in (2, 3, 4) and b.real_term() in (0, 1)
     assert b.run(100) > 0
 
 

@@ -3,7 +3,7 @@
 
 FP32 (the precision form's pair kernels), (erfc(sqrt(alpha) r)/r = sqrt(alpha) h(alpha r^2)),
 evaluated in float32 exactly as the kernel does (bin from the exponent and top
-five mantissa bits of u, y = bin-local fraction - 1/2, cubic by FMA-free
+five mantissa bits of u, v = 1 + the bin-local fraction, cubic by FMA-free
 Horner) against scipy's erfc in double precision. Bar: 3e-7 relative for
 u < 4 (the FP32 erfc fit it replaces is good to 1.2e-7, and FP32 rounding of
 the result is 6e-8); for 4 <= u < 32, where h is below 1/400 of its value at
@@ -24,7 +24,7 @@ def _eval(tab, u):
     bits = u.view(np.int32)
     idx = np.clip((bits >> 18) - ((127 - 14) << 5), 0, len(tab) - 1)
     c = tab[idx]
-    y = (((bits << 5) & 0x7FFFFF) | 0x3F800000).view(np.float32) - np.float32(1.5)
+    y = (((bits << 5) & 0x7FFFFF) | 0x3F800000).view(np.float32)  # v = 1 + f
     h = c[:, 3]
     for q in (2, 1, 0):
         h = (h * y + c[:, q]).astype(np.float32)
