@@ -399,10 +399,16 @@ int plum_batch_autotune(plum_batch* batch, int steps, int* out4);
  * plum_batch_real_term reports the current choice. */
 int plum_batch_set_real_term(plum_batch* batch, int table);
 int plum_batch_real_term(const plum_batch* batch);
-/* The h(u) table itself (host copy, built like the batch's): out[4 b + q] =
- * coefficient q of bin b, at most cap bins; returns the number of bins. For
- * checks of its accuracy. */
-int plum_h32_table(float* out, int cap);
+/* The h(u) table itself (host copy, built like the batch's): bins of 1/32
+ * octave of the table variable u' = scale u from 2^-14 to 2^5, per bin a
+ * cubic in w = f / 32 (f the bin-local fraction of u'), out[4 b + q] =
+ * coefficient q of bin b, at most cap bins; returns the number of bins.
+ * scale = 1, cut = 0: the universal table. A batch whose replicas share alpha
+ * and r_c stages the cut table, scale = 16 / (alpha r_c^2) and cut = 16: h(u'
+ * / scale) below u' = 16 and zero from there on, so the real-space cut-off is
+ * the table's own. Returns -1 (last error set) for scale <= 0 or cut < 0. For checks of
+ * its accuracy; no reference counterpart. */
+int plum_h32_table(float* out, int cap, double scale, double cut);
 /* The FP64 table every form's FP64 real-space term uses (erfc(sqrt(alpha)
  * r)/r = sqrt(alpha) h(alpha r^2), h(u) = erfc(sqrt u)/sqrt u): 32 bins per
  * octave of u from 2^-12 to 2^5, a degree-8 polynomial in the bin-local

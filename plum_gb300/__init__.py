@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libplumgpu.so")
 
 PLUM_OK = 0
+PLUM_ERR_INPUT = 1
 FORM_FP64 = 0
 FORM_FP32 = 1
 ERRORS = {1: "input", 2: "cuda", 3: "timeout", 4: "nonfinite", 5: "state", 6: "stream"}
@@ -157,7 +158,7 @@ def lib():
         L.plum_time_kernels.argtypes = [C.c_void_p, C.c_int, _dp]
         L.plum_batch_set_real_term.argtypes = [C.c_void_p, C.c_int]
         L.plum_batch_real_term.argtypes = [C.c_void_p]
-        L.plum_h32_table.argtypes = [C.c_void_p, C.c_int]
+        L.plum_h32_table.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double]
         L.plum_h64_table.argtypes = [C.c_void_p, C.c_int]
         L.plum_run_params.argtypes = [C.c_void_p, C.POINTER(RunInfo)]
         L.plum_chain_observables.argtypes = [C.c_void_p, C.c_void_p, C.c_int,
@@ -168,12 +169,16 @@ def lib():
     return _lib
 
 
-def h32_table():
-    """[bins, 4] cubic coefficients of the FP32 h(u) = erfc(sqrt u)/sqrt u
-    table (bins of 1/32 octave from u = 2^-14 to 2^5)."""
-    n = lib().plum_h32_table(None, 0)
+def h32_table(scale=1.0, cut=0.0):
+    """[bins, 4] cubic coefficients (in w = f/32, f the bin-local fraction) of
+    the FP32 table of h(u'/scale), h(u) = erfc(sqrt u)/sqrt u, in bins of 1/32
+    octave of u' from 2^-14 to 2^5; with cut > 0 the bins from u' = cut on
+    are zero (the batch's cut table: scale = 16 / (alpha r_c^2), cut = 16)."""
+    n = lib().plum_h32_table(None, 0, scale, cut)
+    if n < 0:
+        raise PlumError(PLUM_ERR_INPUT, lib().plum_last_error().decode())
     out = np.zeros(4 * n, np.float32)
-    lib().plum_h32_table(_ptr(out), n)
+    lib().plum_h32_table(_ptr(out), n, scale, cut)
     return out.reshape(n, 4)
 
 

@@ -1830,6 +1830,10 @@ struct plum_batch {
   BatchTune tune{4096, 128, 0, 2, 1};
   float4* d_htab = nullptr;  // h(u) table of the real-space term (kH32Bins)
   bool htab_ok = false;      // every replica's alpha r_c^2 lies inside the table
+  // the cut table (variable u' = cut_scale alpha r^2, zero from the cut-off on)
+  // when every replica with the Ewald term has the same alpha and r_c; else
+  // d_htab holds the universal table and cut_scale is 0
+  float cut_scale = 0.0f;
   // per-replica streams
   std::vector<long long> cap, per_step;
   uint32_t** d_states = nullptr;
@@ -1982,7 +1986,8 @@ void chain_enqueue(plum_batch* b, int steps, int r0, int n, double* slots, int* 
   launch_batch_serial(rp, rb, item_off, slots, n, kModeGen, st);
   stage_one();
   for (int i = 0; i < steps; i++) {
-    launch_batch_delta32(rp, rb, n, item_off, slots, b->kt_smem, b->tune, queue, b->d_htab, st);
+    launch_batch_delta32(rp, rb, n, item_off, slots, b->kt_smem, b->tune, queue, b->d_htab,
+                         b->cut_scale, st);
     int mode = kModeFinish | kModeDecide | (i + 1 < steps ? kModeGen : 0);
     launch_batch_serial(rp, rb, item_off, slots, n, mode, st);
     if (i + 1 < steps) stage_one();
@@ -2223,16 +2228,29 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
   {
     // the h(u) table covers u = alpha r^2 < 2^kH32EHi; a replica whose
     // cut-off reaches past it keeps the erfc fit for the whole batch
-    std::vector<float4> h(kH32Bins);
-    build_h32_table(h.data());
-    cudaMemcpy(b->d_htab, h.data(), sizeof(float4) * kH32Bins, cudaMemcpyHostToDevice);
     b->htab_ok = true;
+    bool same = true;  // every Ewald replica has replica e0's alpha and r_c
+    int e0 = -1;
     for (int r = 0; r < n; r++) {
       const DevParams& P = hp[r];
-      if (P.use_ewald && P.sqrt_alpha * P.sqrt_alpha * P.real_cut * P.real_cut >=
-                             std::ldexp(1.0, kH32EHi))
+      if (!P.use_ewald) continue;
+      if (P.sqrt_alpha * P.sqrt_alpha * P.real_cut * P.real_cut >= std::ldexp(1.0, kH32EHi))
         b->htab_ok = false;
+      if (e0 < 0)
+        e0 = r;
+      else if (P.f_sqrt_alpha != hp[e0].f_sqrt_alpha || P.f_real_cut != hp[e0].f_real_cut)
+        same = false;
     }
+    std::vector<float4> h(kH32Bins);
+    b->cut_scale = 0.0f;
+    if (b->htab_ok && same && e0 >= 0) {
+      const double a = hp[e0].f_sqrt_alpha, rcut = hp[e0].f_real_cut;
+      b->cut_scale = (float)(kH32Cut / (a * a * rcut * rcut));
+      build_h32_table(h.data(), (double)b->cut_scale, kH32Cut);
+    } else {
+      build_h32_table(h.data());
+    }
+    cudaMemcpy(b->d_htab, h.data(), sizeof(float4) * kH32Bins, cudaMemcpyHostToDevice);
     b->tune.htab = b->htab_ok ? 1 : 0;
   }
   b->rc_since.resize(n);
@@ -2463,7 +2481,7 @@ int plum_batch_time_kernels(plum_batch* b, int n_steps, double* out4) {
   for (int i = 0; i < n_steps && !rc; i++) {
     rc = timed(0, [&] {
       launch_batch_delta32(b->d_rp, b->d_rb, R, b->d_item_off, b->d_slots, b->kt_smem, b->tune,
-                         b->d_queue, b->d_htab, b->s);
+                         b->d_queue, b->d_htab, b->cut_scale, b->s);
     });
     const int mode = kModeFinish | kModeDecide | (i + 1 < n_steps ? kModeGen : 0);
     if (!rc)
@@ -2640,9 +2658,13 @@ int plum_h64_table(double* out, int cap) {
   return kH64Bins;
 }
 
-int plum_h32_table(float* out, int cap) {
+int plum_h32_table(float* out, int cap, double scale, double cut) {
+  if (!(scale > 0.0) || !(cut >= 0.0)) {
+    fail(PLUM_ERR_INPUT, "table scale must be > 0, cut >= 0");
+    return -1;
+  }
   std::vector<float4> h(kH32Bins);
-  build_h32_table(h.data());
+  build_h32_table(h.data(), scale, cut);
   for (int i = 0; i < std::min(cap, kH32Bins); i++) {
     out[4 * i] = h[i].x;
     out[4 * i + 1] = h[i].y;

@@ -283,13 +283,18 @@ struct BatchTune {
 // erfc(sqrt(alpha) r) / r = sqrt(alpha) h(alpha r^2) as a function of the
 // dimensionless u = alpha r^2 alone, so one table serves every system. Bins:
 // kH32Per per octave of u for octaves 2^kH32ELo .. 2^(kH32EHi - 1); bin b
-// holds a cubic in v = 1 + f, f in [0, 1) the bin-local fraction of u
+// holds a cubic in w = f / 32, f in [0, 1) the bin-local fraction of u
 // (its float mantissa bits below the top five).
 // Built on the host by
 // Chebyshev interpolation of std::erfc in double precision (build_h32_table).
+// A cut table (scale s, cut c) tabulates h(u' / s) in the variable u' = s u
+// and is zero on every bin at or above u' = c, a power of two and so a bin
+// edge: with s = c / (alpha r_c^2) the cut-off of the real-space term is the
+// table's own (the batched pair sweep of replicas sharing alpha and r_c).
 constexpr int kH32ELo = -14, kH32EHi = 5, kH32Per = 32;
 constexpr int kH32Bins = (kH32EHi - kH32ELo) * kH32Per;
-void build_h32_table(float4* out);  // kH32Bins entries
+constexpr double kH32Cut = 16.0;
+void build_h32_table(float4* out, double scale = 1.0, double cut = 0.0);  // kH32Bins entries
 // The FP64 table of h(u): kH64Per bins per octave of u for octaves
 // 2^kH64ELo .. 2^(kH64EHi - 1), a degree-8 polynomial in y = f - 1/2 per bin
 // (kH64Stride doubles per bin, the last zero, for 16-byte loads): Chebyshev
@@ -306,8 +311,11 @@ constexpr int kMinKTile = 64;
 // multiple of the block size); one more item per move takes the pairs among
 // the moved beads.
 constexpr int kPairGroup = 32;
+// Other beads per pair item: item_pairs over the staged group, the group
+// counted as the table loop stages it (padded to a multiple of 4), so that an
+// item of a one-bead move is no longer than a chain move's.
 __host__ __device__ inline int pair_chunk(int m, int item_pairs) {
-  const int g = m < kPairGroup ? (m > 0 ? m : 1) : kPairGroup;
+  const int g = m < kPairGroup ? ((m > 0 ? m : 1) + 3) & ~3 : kPairGroup;
   const int c = (item_pairs / g + kPairThreads - 1) / kPairThreads * kPairThreads;
   return c > kPairThreads ? c : kPairThreads;
 }
@@ -317,9 +325,11 @@ __host__ __device__ inline int pair_item_count(int m, int n_bead, int item_pairs
   return ((m + kPairGroup - 1) / kPairGroup) * ((n_bead + c - 1) / c) + (m > 1 ? 1 : 0);
 }
 // queue: two ints, zero before the first launch (each launch leaves them zero)
+// htab: the universal table (cut_scale 0) or the batch's cut table (scale
+// cut_scale = kH32Cut / (alpha r_c^2), every replica with the same alpha and r_c)
 void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, int* item_off,
                           double* slots, size_t smem, BatchTune tune, int* queue,
-                          const float4* htab, cudaStream_t s);
+                          const float4* htab, float cut_scale, cudaStream_t s);
 void launch_batch_serial(const DevParams* rp, const DevBuffers* rb, const int* item_off,
                          const double* slots, int n_rep, int mode, cudaStream_t s);
 // per replica r: if need[r], shift the unread words [pos[r], len[r]) of out[r]

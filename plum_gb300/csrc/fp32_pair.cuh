@@ -37,16 +37,17 @@ constexpr int kH32LoBits = (127 + kH32ELo) << 23;  // float bits of 2^kH32ELo
 
 // h(u) = erfc(sqrt u) / sqrt u from the table (in shared memory) at the
 // float bits of u: the exponent and top five mantissa bits pick the bin, the
-// remaining 18 bits are the bin-local fraction f, shifted up into a float
-// v = 1 + f of [1, 2) exactly; the bin's cubic is in v. Bins outside
-// the table are clamped (their values are replaced or cut off by the caller).
+// remaining 18 bits are the bin-local fraction f; placed under the exponent
+// of 1 they make the float 1 + f/32 exactly, and w = f/32 is exact too. The
+// bin's cubic is in w. Bins outside the table are clamped to the last one
+// (one unsigned minimum; a u below the table wraps to a huge index): the
+// caller replaces values below the table, and values above it are cut off.
 __device__ __forceinline__ float h32_tab(const float4* tab, int bits) {
-  int idx = (bits >> 18) - ((127 + kH32ELo) << 5);
-  idx = min(max(idx, 0), kH32Bins - 1);
+  const unsigned idx = min((unsigned)((bits >> 18) - ((127 + kH32ELo) << 5)),
+                           (unsigned)(kH32Bins - 1));
   const float4 c = tab[idx];
-  // the 18 bits below the bin index moved to the top of a float: v = 1 + f
-  const float v = __int_as_float(((bits << 5) & 0x7FFFFF) | 0x3F800000);
-  return fmaf(fmaf(fmaf(c.w, v, c.z), v, c.y), v, c.x);
+  const float w = __int_as_float((bits & 0x3FFFF) | 0x3F800000) - 1.0f;
+  return fmaf(fmaf(fmaf(c.w, w, c.z), w, c.y), w, c.x);
 }
 
 // Below the table (u < 2^kH32ELo: r under 1/128 of 1/sqrt(alpha)): the erfc

@@ -384,6 +384,83 @@ __global__ void __launch_bounds__(kTotTile)
   }
 }
 
+// 64-bit fixed-point fraction of the box: frac(x / L) 2^64.
+__device__ __forceinline__ unsigned long long fix64(double x, double inv) {
+  double f = x * inv;
+  f -= floor(f);
+  if (f >= 1.0) f = 0.0;  // a tiny negative x / L rounds up to 1
+  return __double2ull_rn(f * 0x1p64);
+}
+
+// k_total64 for LJ + Ewald in a cubic box periodic on every axis, one image
+// (r_c <= L/2) and one box for both terms: positions as 64-bit fixed-point
+// fractions of the box, staged per tile, so one integer subtraction is the
+// minimum-image difference and its conversion to FP64 the only rounding of
+// the vector (more accurate than x_j - x_i in FP64). r^2 in FP64, in units of
+// (L / 2^64)^2; the cut-off pre-tests in FP32 with a margin, decided in FP64
+// inside; the real-space term sqrt(alpha) h(alpha r^2) from the FP64 table,
+// with lB sqrt(alpha) q_i folded into the thread's charge.
+__global__ void __launch_bounds__(kTotTile)
+    k_total64_fix(const DevParams P, const DevBuffers B, double* out) {
+  __shared__ unsigned long long sx[kTotTile], sy[kTotTile], sz[kTotTile];
+  __shared__ double sq[kTotTile];
+  __shared__ int st[kTotTile];
+  __shared__ double red[2 * (kTotTile / 32)];
+  const int nt = (P.n_bead + kTotTile - 1) / kTotTile;
+  int ta, tb;
+  tri_unrank(blockIdx.x, nt, ta, tb);
+  const int j0 = tb * kTotTile;
+  const int jn = min(kTotTile, P.n_bead - j0);
+  const double inv = P.inv_ebox[0];
+  if (threadIdx.x < jn) {
+    const double4_32a p = B.pos[j0 + threadIdx.x];
+    sx[threadIdx.x] = fix64(p.x, inv);
+    sy[threadIdx.x] = fix64(p.y, inv);
+    sz[threadIdx.x] = fix64(p.z, inv);
+    sq[threadIdx.x] = p.w;
+    st[threadIdx.x] = B.type[j0 + threadIdx.x];
+  }
+  __syncthreads();
+  const double s = P.ebox[0] * 0x1p-64;  // L / 2^64
+  const double s2 = s * s;
+  const double rc2_raw = P.real_cut * P.real_cut / s2;
+  const double lj2_raw = P.lj_max2 / s2;
+  const double ua = P.alpha * s2;
+  // FP32 pre-tests, a little wide: the FP64 tests inside decide
+  const float rc_hi = (float)rc2_raw * 1.0001f, lj_hi = (float)lj2_raw * 1.0001f;
+  double lj = 0.0, re = 0.0;
+  const int i = ta * kTotTile + threadIdx.x;
+  if (i < P.n_bead) {
+    const double4_32a pi = B.pos[i];
+    const unsigned long long ux = fix64(pi.x, inv), uy = fix64(pi.y, inv), uz = fix64(pi.z, inv);
+    const double qi = pi.w * P.lB * P.sqrt_alpha;
+    const int kt = B.type[i] * P.n_type;
+    for (int jj = ta == tb ? (int)threadIdx.x + 1 : 0; jj < jn; jj++) {
+      const double dx = __ll2double_rn((long long)(sx[jj] - ux));
+      const double dy = __ll2double_rn((long long)(sy[jj] - uy));
+      const double dz = __ll2double_rn((long long)(sz[jj] - uz));
+      const double raw = fma(dx, dx, fma(dy, dy, dz * dz));
+      const float rf = __double2float_rn(raw);
+      if (P.use_pair && rf < lj_hi && raw < lj2_raw) lj += lj64(P, kt + st[jj], raw * s2);
+      if (rf <= rc_hi && raw <= rc2_raw && raw > 0.0) {
+        const double qq = qi * sq[jj];
+        if (qq != 0.0) {
+          const long long bits = __double_as_longlong(raw * ua);
+          const double h = bits >= kH64LoBits ? h64_tab(P.htab64, bits)
+                                              : real_term64(P, raw * s2) / P.sqrt_alpha;
+          re = fma(qq, h, re);
+        }
+      }
+    }
+  }
+  const double a = block_sum<kTotTile>(lj, red);
+  const double b = block_sum<kTotTile>(re, red + kTotTile / 32);
+  if (threadIdx.x == 0) {
+    out[2 * blockIdx.x] = a;
+    out[2 * blockIdx.x + 1] = b;
+  }
+}
+
 int total_partials_count(const DevParams& P) {
   long long nt = (P.n_bead + kTotTile - 1) / kTotTile;
   return (int)(nt * (nt + 1) / 2);
@@ -391,7 +468,12 @@ int total_partials_count(const DevParams& P) {
 
 void launch_total64(const DevParams& P, const DevBuffers& B, double* out, int n_part,
                     cudaStream_t s) {
-  k_total64<<<n_part, kTotTile, 0, s>>>(P, B, out);
+  const bool fix = P.use_ewald && P.htab64 && P.same_wrap && P.npbc == 3 && P.single_image &&
+                   P.pair_kind == 0 && P.ebox[0] == P.ebox[1] && P.ebox[1] == P.ebox[2];
+  if (fix)
+    k_total64_fix<<<n_part, kTotTile, 0, s>>>(P, B, out);
+  else
+    k_total64<<<n_part, kTotTile, 0, s>>>(P, B, out);
 }
 
 // S(k) from scratch: block (k tile, bead group) writes a partial; a second

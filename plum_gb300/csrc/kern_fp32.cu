@@ -42,6 +42,31 @@ __device__ __forceinline__ float block_sum32(float v, float* sh) {
   return t;
 }
 
+// Two sums at once (one pair of barriers); each value is added in
+// block_sum32's order, so the results are the same bits as two calls.
+// sh: 2 NT / 32 floats. Valid in thread 0.
+template <int NT>
+__device__ __forceinline__ float2 block_sum32x2(float a, float b, float* sh) {
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) {
+    sh[w] = a;
+    sh[NT / 32 + w] = b;
+  }
+  __syncthreads();
+  float2 t = make_float2(0.0f, 0.0f);
+  if (threadIdx.x == 0)
+    for (int i = 0; i < NT / 32; i++) {
+      t.x += sh[i];
+      t.y += sh[NT / 32 + i];
+    }
+  return t;
+}
+
 __device__ __forceinline__ double block_sum_d(double v, double* sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -316,59 +341,68 @@ __device__ __forceinline__ void pair_sweep(const DevParams& P, const PairConst& 
 // ------------------------------------------------ table-driven real space
 // pair_sweep for LJ + Ewald with r_c <= L/2 on every axis, the real-space term
 // from the h(u) table: per (moved u, other j) the trial and current distances
-// share the other bead's load, one LJ pre-test and one charge product, and the
-// cut-off is a select, so a warp runs no divergent erfc. Each thread takes two
-// other beads per staged bead, so one load of the staged trial and current
-// entries serves four evaluations. kCubic (equal fixed-point scales on the
-// three axes): r^2 stays in fixed-point units and the box scale is folded
-// into the constants. gn4 staged beads, a multiple of 4; the trial entry's w
-// holds the staged bead's charge (float bits) and the current entry's w its
-// type; the padding beads have q = 0 and equal trial and current positions,
-// so they add exactly zero.
-template <bool kCubic>
+// share the other bead's load, one LJ pre-test and the packed (two-lane FP32)
+// arithmetic of r^2 and u, so a warp runs no divergent erfc. Each thread takes
+// two other beads per staged bead, so one load of the staged trial and
+// current entries serves four evaluations; the other bead's charge multiplies
+// its sum once, after the staged beads. kCubic (equal fixed-point scales on
+// the three axes): r^2 stays in fixed-point units and the box scale is folded
+// into the constants. kCut: the table is the batch's cut table (variable
+// u' = cut_scale u, zero from the cut-off on), so the cut-off costs nothing;
+// else the universal table and a select at r_c. gn4 staged beads, a multiple
+// of 4; the trial entry's w holds the staged bead's charge (float bits) and
+// the current entry's w its type; the padding beads have q = 0 and equal
+// trial and current positions, so they add exactly zero.
+template <bool kCubic, bool kCut>
 __device__ __forceinline__ void pair_sweep_tab(const DevParams& P, const DevBuffers& B,
                                                const int4* s_mt, const float4* s_h, int gn4,
                                                int c0, int c1, int b_lo, int b_hi,
-                                               float& acc_lj, float& acc_re) {
+                                               float cut_scale, float& acc_lj, float& acc_re) {
   const float sx = P.f_scale[0], sy = P.f_scale[1], sz = P.f_scale[2];
   const float cs = kCubic ? sx * sx : 1.0f;  // real r^2 per unit of r2 below
   const float ics = 1.0f / cs;
   const float rc2 = P.f_real_cut * P.f_real_cut * ics;
-  const float ua = P.f_sqrt_alpha * P.f_sqrt_alpha * cs;
+  const float ua = P.f_sqrt_alpha * P.f_sqrt_alpha * cs * (kCut ? cut_scale : 1.0f);
+  const float ius = kCut ? 1.0f / cut_scale : 1.0f;  // table variable -> u
   float ljm = 1e-30f;  // r2 = 0 (coincident beads) must reach lj32
   for (int k = 0; k < P.n_type * P.n_type; k++) ljm = fmaxf(ljm, P.f_lj_rc2[k]);
   const float ljlim = ljm * ics;
   const float pref = P.f_lB * P.f_sqrt_alpha;
   const int nt = P.n_type;
   const bool use_pair = P.use_pair;
+  const float2 ua2 = make_float2(ua, ua);
+  const float2 s2x = make_float2(sx, sx), s2y = make_float2(sy, sy), s2z = make_float2(sz, sz);
   // one evaluation pair (trial, current) of staged bead (t, c) with other
   // bead o; ok: o is an other bead of this item (not moved, inside the chunk)
-  auto eval = [&](const int4 t, const int4 c, const int4 o, float qo, bool ok, float& acc) {
-    float x1 = (float)(int)((unsigned)o.x - (unsigned)t.x);
-    float y1 = (float)(int)((unsigned)o.y - (unsigned)t.y);
-    float z1 = (float)(int)((unsigned)o.z - (unsigned)t.z);
-    float x0 = (float)(int)((unsigned)o.x - (unsigned)c.x);
-    float y0 = (float)(int)((unsigned)o.y - (unsigned)c.y);
-    float z0 = (float)(int)((unsigned)o.z - (unsigned)c.z);
+  auto eval = [&](const int4 t, const int4 c, const int4 o, bool ok, float& acc) {
+    float2 dx = make_float2((float)(int)((unsigned)o.x - (unsigned)t.x),
+                            (float)(int)((unsigned)o.x - (unsigned)c.x));
+    float2 dy = make_float2((float)(int)((unsigned)o.y - (unsigned)t.y),
+                            (float)(int)((unsigned)o.y - (unsigned)c.y));
+    float2 dz = make_float2((float)(int)((unsigned)o.z - (unsigned)t.z),
+                            (float)(int)((unsigned)o.z - (unsigned)c.z));
     if (!kCubic) {
-      x1 *= sx, y1 *= sy, z1 *= sz;
-      x0 *= sx, y0 *= sy, z0 *= sz;
+      dx = __fmul2_rn(dx, s2x);
+      dy = __fmul2_rn(dy, s2y);
+      dz = __fmul2_rn(dz, s2z);
     }
-    const float r1 = fmaf(x1, x1, fmaf(y1, y1, z1 * z1));
-    const float r0 = fmaf(x0, x0, fmaf(y0, y0, z0 * z0));
-    if (use_pair && ok && fminf(r1, r0) < ljlim) {
+    const float2 r = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+    if (use_pair && ok && fminf(r.x, r.y) < ljlim) {
       const int k = c.w * nt + o.w;  // trial and current share the type
-      acc_lj += lj32(P, k, r1 * cs) - lj32(P, k, r0 * cs);
+      acc_lj += lj32(P, k, r.x * cs) - lj32(P, k, r.y * cs);
     }
-    const int b1 = __float_as_int(r1 * ua), b0 = __float_as_int(r0 * ua);
+    const float2 u = __fmul2_rn(r, ua2);
+    const int b1 = __float_as_int(u.x), b0 = __float_as_int(u.y);
     float h1 = h32_tab(s_h, b1), h0 = h32_tab(s_h, b0);
     if (min(b1, b0) < kH32LoBits) {
-      if (b1 < kH32LoBits) h1 = h32_small(__int_as_float(b1));
-      if (b0 < kH32LoBits) h0 = h32_small(__int_as_float(b0));
+      if (b1 < kH32LoBits) h1 = h32_small(u.x * ius);
+      if (b0 < kH32LoBits) h0 = h32_small(u.y * ius);
     }
-    h1 = r1 <= rc2 ? h1 : 0.0f;
-    h0 = r0 <= rc2 ? h0 : 0.0f;
-    acc = fmaf(__int_as_float(t.w) * qo, h1 - h0, acc);
+    if (!kCut) {
+      h1 = r.x <= rc2 ? h1 : 0.0f;
+      h0 = r.y <= rc2 ? h0 : 0.0f;
+    }
+    acc = fmaf(__int_as_float(t.w), h1 - h0, acc);
   };
   for (int j0 = c0 + threadIdx.x; j0 < c1; j0 += 2 * kPairThreads) {
     const int j1 = j0 + kPairThreads;
@@ -382,32 +416,37 @@ __device__ __forceinline__ void pair_sweep_tab(const DevParams& P, const DevBuff
 #pragma unroll 4
     for (int u = 0; u < gn4; u++) {
       const int4 t = s_mt[u], c = s_mt[kPairGroup + u];
-      eval(t, c, o0, q0, ok0, a0);
-      eval(t, c, o1, q1, ok1, a1);
+      eval(t, c, o0, ok0, a0);
+      eval(t, c, o1, ok1, a1);
     }
-    acc_re += a0 + a1;
+    acc_re = fmaf(q0, a0, fmaf(q1, a1, acc_re));
   }
 }
 
-// The table (kH32Bins float4): per bin the cubic in v = 1 + f (f the
-// bin-local fraction) through h at the four Chebyshev nodes of the bin, h in
-// double precision from std::erfc, the 4 x 4 Vandermonde system solved by
-// Gaussian elimination with partial pivoting.
-void build_h32_table(float4* out) {
+// The table (kH32Bins float4): per bin the cubic in w = f / 32 (f the
+// bin-local fraction) through h(u' / scale) at the four Chebyshev nodes of the
+// bin, h in double precision from std::erfc; the 4 x 4 Vandermonde system in
+// f solved by Gaussian elimination with partial pivoting, the coefficients
+// then scaled by powers of 32 (exactly) to the kernel's w. With cut > 0 every
+// bin at or above u' = cut is zero.
+void build_h32_table(float4* out, double scale, double cut) {
   const double kPi = 3.14159265358979323846;
   int i = 0;
   for (int e = kH32ELo; e < kH32EHi; e++)
     for (int j = 0; j < kH32Per; j++, i++) {
       const double lo = std::ldexp(1.0 + (double)j / kH32Per, e);
       const double w = std::ldexp(1.0 / kH32Per, e);
+      if (cut > 0.0 && lo >= cut) {
+        out[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        continue;
+      }
       double A[4][5];
       for (int k = 0; k < 4; k++) {
-        const double y = 0.5 * std::cos(kPi * (k + 0.5) / 4.0);  // in [-1/2, 1/2]
-        const double u = lo + (y + 0.5) * w;
+        const double f = 0.5 + 0.5 * std::cos(kPi * (k + 0.5) / 4.0);  // in (0, 1)
+        const double u = (lo + f * w) / scale;
         const double r = std::sqrt(u);
-        const double v = y + 1.5;  // the kernel's variable, 1 + f
         double p = 1.0;
-        for (int q = 0; q < 4; q++, p *= v) A[k][q] = p;
+        for (int q = 0; q < 4; q++, p *= f) A[k][q] = p;
         A[k][4] = std::erfc(r) / r;
       }
       for (int col = 0; col < 4; col++) {
@@ -417,12 +456,13 @@ void build_h32_table(float4* out) {
         for (int q = 0; q < 5; q++) std::swap(A[col][q], A[piv][q]);
         for (int rr = 0; rr < 4; rr++) {
           if (rr == col) continue;
-          const double f = A[rr][col] / A[col][col];
-          for (int q = col; q < 5; q++) A[rr][q] -= f * A[col][q];
+          const double g = A[rr][col] / A[col][col];
+          for (int q = col; q < 5; q++) A[rr][q] -= g * A[col][q];
         }
       }
-      out[i] = make_float4((float)(A[0][4] / A[0][0]), (float)(A[1][4] / A[1][1]),
-                           (float)(A[2][4] / A[2][2]), (float)(A[3][4] / A[3][3]));
+      double c[4];
+      for (int q = 0; q < 4; q++) c[q] = std::ldexp(A[q][4] / A[q][q], 5 * q);  // f^q = 32^q w^q
+      out[i] = make_float4((float)c[0], (float)c[1], (float)c[2], (float)c[3]);
     }
 }
 
@@ -446,7 +486,8 @@ template <int kMinBlocks>
 __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
     k_batch_delta32(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb,
                     int n_rep, int* __restrict__ item_off, double* __restrict__ slots,
-                    BatchTune tune, int* __restrict__ queue, const float4* __restrict__ htab) {
+                    BatchTune tune, int* __restrict__ queue, const float4* __restrict__ htab,
+                    float cut_scale) {
   const int kItemPairs = tune.item_pairs, kKTile32 = tune.k_tile;
   extern __shared__ __align__(16) unsigned char smem_all[];
   // with the h(u) table: the table first, then the staging / k-table area
@@ -454,7 +495,7 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
   unsigned char* smem = smem_all + (htab ? kH32Bins * sizeof(float4) : 0);
   if (htab)
     for (int i = threadIdx.x; i < kH32Bins; i += blockDim.x) s_h[i] = htab[i];
-  __shared__ float red[kPairThreads / 32];
+  __shared__ float red[2 * (kPairThreads / 32)];
   __shared__ int s_pref[kMaxReplicas + 1];
   __shared__ int s_np[kMaxReplicas];
   __shared__ int s_total, s_item;
@@ -520,7 +561,8 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
         // the table path pads the staged beads to a multiple of 4 with the
         // last bead's current position at both places and q = 0
         const int gn4 = tab ? (gn + 3) & ~3 : gn;
-        __syncthreads();  // the previous item may still read the staging area
+        // (the barrier at the top of the item loop: every thread is done
+        // with the previous item's staging area)
         for (int u = threadIdx.x; u < gn4; u += kPairThreads) {
           if (u < gn) {
             int4 t = B.ftrial[g0 + u];
@@ -538,10 +580,22 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
         __syncthreads();
         const PairConst K = pair_const(P);
         if (tab) {
-          if (P.npbc == 3 && P.f_scale[0] == P.f_scale[1] && P.f_scale[1] == P.f_scale[2])
-            pair_sweep_tab<true>(P, B, s_mt, s_h, gn4, c0, c1, b_lo, b_hi, acc_lj, acc_re);
-          else
-            pair_sweep_tab<false>(P, B, s_mt, s_h, gn4, c0, c1, b_lo, b_hi, acc_lj, acc_re);
+          const bool cubic =
+              P.npbc == 3 && P.f_scale[0] == P.f_scale[1] && P.f_scale[1] == P.f_scale[2];
+          if (cut_scale > 0.0f) {
+            if (cubic)
+              pair_sweep_tab<true, true>(P, B, s_mt, s_h, gn4, c0, c1, b_lo, b_hi, cut_scale,
+                                         acc_lj, acc_re);
+            else
+              pair_sweep_tab<false, true>(P, B, s_mt, s_h, gn4, c0, c1, b_lo, b_hi, cut_scale,
+                                          acc_lj, acc_re);
+          } else if (cubic) {
+            pair_sweep_tab<true, false>(P, B, s_mt, s_h, gn4, c0, c1, b_lo, b_hi, 0.0f, acc_lj,
+                                        acc_re);
+          } else {
+            pair_sweep_tab<false, false>(P, B, s_mt, s_h, gn4, c0, c1, b_lo, b_hi, 0.0f, acc_lj,
+                                         acc_re);
+          }
         } else if (P.single_image)
           pair_sweep<true>(P, K, B, s_mt, s_mq, gn, b_lo + g0, c0, c1, b_lo, b_hi, acc_lj,
                            acc_re);
@@ -562,28 +616,39 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
           acc_re += r1 - r0;
         }
       }
-      float a = block_sum32<kPairThreads>(acc_lj, red);
-      float b = block_sum32<kPairThreads>(acc_re, red);
+      const float2 ab = block_sum32x2<kPairThreads>(acc_lj, acc_re, red);
       if (threadIdx.x == 0) {
-        slots[2 * item] = (double)a;
-        slots[2 * item + 1] = (double)b;
+        slots[2 * item] = (double)ab.x;
+        slots[2 * item + 1] = (double)ab.y;
       }
     } else {
       // a k item of up to kMaxKPerThread * kPairThreads vectors: thread t
-      // takes k = tile * k_tile + t + q kPairThreads, so the moved beads'
-      // phase tables, built once per item, serve up to four vectors per thread
+      // takes nq consecutive vectors k = tile * k_tile + t nq + q, so the
+      // moved beads' phase tables, built once per item, serve up to four
+      // vectors per thread, and vectors of one (nx, ny) column (n_z runs
+      // fastest in the k list) share the product e^{i(kx x + ky y)}: the
+      // phase of each is the same cmul(cmul(ex, ey), ez) as phase32's
       const int tile = local - s_np[r];
       const int sk_pend = st->sk_pending, sk_buf = st->sk_buf, cur_buf = st->cur_buf;
+      const int nq = (kKTile32 + kPairThreads - 1) / kPairThreads;
       int kk[kMaxKPerThread];
-      bool mine[kMaxKPerThread];
-      short4 kv[kMaxKPerThread];
+      bool mine[kMaxKPerThread], col[kMaxKPerThread];
+      int ox[kMaxKPerThread], oy[kMaxKPerThread], oz[kMaxKPerThread];
+      bool ny[kMaxKPerThread], nz[kMaxKPerThread];
       float2 ds[kMaxKPerThread];
 #pragma unroll
       for (int q = 0; q < kMaxKPerThread; q++) {
-        const int t = threadIdx.x + q * kPairThreads;
+        const int t = threadIdx.x * nq + q;
         kk[q] = tile * kKTile32 + t;
-        mine[q] = t < kKTile32 && kk[q] < P.n_k;
-        kv[q] = mine[q] ? B.kn[kk[q]] : make_short4(0, 0, 0, 0);
+        mine[q] = q < nq && t < kKTile32 && kk[q] < P.n_k;
+        const short4 kv = mine[q] ? B.kn[kk[q]] : make_short4(0, 0, 0, 0);
+        ox[q] = P.koff[0] + kv.x;
+        oy[q] = P.koff[1] + (kv.y >= 0 ? kv.y : -kv.y);
+        oz[q] = P.koff[2] + (kv.z >= 0 ? kv.z : -kv.z);
+        ny[q] = kv.y < 0;
+        nz[q] = kv.z < 0;
+        // a new (nx, ny) column: recompute the xy product
+        col[q] = q == 0 || ox[q] != ox[q - 1] || oy[q] != oy[q - 1] || ny[q] != ny[q - 1];
         ds[q] = make_float2(0.0f, 0.0f);
       }
       float2* tabs = reinterpret_cast<float2*>(smem);
@@ -597,15 +662,33 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
           table32(P, f, B.fq[c0 + bead], axis, tabs + (bead * 2 + which) * per);
         }
         __syncthreads();
+        if (mine[0])
+          for (int bb = 0; bb < cnt; bb++) {
+            const float2* t1 = tabs + (bb * 2 + 0) * per;
+            const float2* t0 = t1 + per;
+            float2 xy1 = make_float2(0.0f, 0.0f), xy0 = xy1;
 #pragma unroll
-        for (int q = 0; q < kMaxKPerThread; q++)
-          if (mine[q])
-            for (int bb = 0; bb < cnt; bb++) {
-              float2 e1 = phase32(P, tabs + (bb * 2 + 0) * per, kv[q]);
-              float2 e0 = phase32(P, tabs + (bb * 2 + 1) * per, kv[q]);
-              ds[q].x += e1.x - e0.x;
-              ds[q].y += e1.y - e0.y;
-            }
+            for (int q = 0; q < kMaxKPerThread; q++)
+              if (mine[q]) {
+                if (col[q]) {
+                  float2 y1 = t1[oy[q]], y0 = t0[oy[q]];
+                  if (ny[q]) {
+                    y1.y = -y1.y;
+                    y0.y = -y0.y;
+                  }
+                  xy1 = cmul32(t1[ox[q]], y1);
+                  xy0 = cmul32(t0[ox[q]], y0);
+                }
+                float2 z1 = t1[oz[q]], z0 = t0[oz[q]];
+                if (nz[q]) {
+                  z1.y = -z1.y;
+                  z0.y = -z0.y;
+                }
+                const float2 e1 = cmul32(xy1, z1), e0 = cmul32(xy0, z0);
+                ds[q].x += e1.x - e0.x;
+                ds[q].y += e1.y - e0.y;
+              }
+          }
       }
       float e = 0.0f;
 #pragma unroll
@@ -640,7 +723,7 @@ __global__ void __launch_bounds__(kPairThreads, kMinBlocks)
 
 void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, int* item_off,
                           double* slots, size_t smem, BatchTune tune, int* queue,
-                          const float4* htab, cudaStream_t s) {
+                          const float4* htab, float cut_scale, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     const int most = kKTableBytes + 4096 + kH32Bins * (int)sizeof(float4);
@@ -651,16 +734,17 @@ void launch_batch_delta32(const DevParams* rp, const DevBuffers* rb, int n_rep, 
   }
   const int grid = tune.grid > 0 ? tune.grid : pair_grid32();
   if (!tune.htab) htab = nullptr;
+  if (!htab) cut_scale = 0.0f;
   if (htab) smem += kH32Bins * sizeof(float4);
   if (tune.min_blocks == 4)
     k_batch_delta32<4><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune,
-                                                        queue, htab);
+                                                        queue, htab, cut_scale);
   else if (tune.min_blocks == 3)
     k_batch_delta32<3><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune,
-                                                        queue, htab);
+                                                        queue, htab, cut_scale);
   else
     k_batch_delta32<2><<<grid, kPairThreads, smem, s>>>(rp, rb, n_rep, item_off, slots, tune,
-                                                        queue, htab);
+                                                        queue, htab, cut_scale);
 }
 
 __global__ void k_fix_all(const DevParams P, const DevBuffers B) {

@@ -182,9 +182,117 @@ struct GenPlan {
   int end;        // reptation end bead (molecule-relative)
   double s;       // pivot displacement size
   int pivot;      // pivot bead (molecule-relative); -1: generated sequentially
+  int scan;       // pivot: the block locates the beads' draws (pivot_draws)
+  int scan_rel;   // window offset of the first bead's draws
+  int scan_ok;    // every bead's draws lay inside the window
+  int scan_end;   // window offset after the last bead's draws
 };
 
 constexpr int kPivotMax = 512;  // chains up to this length pivot in parallel
+constexpr int kJumpLevels = 9;  // 2^9 >= kPivotMax - 1 beads per pivot
+
+// First window position q >= x of x's parity whose pair (q, q+1) randSphere
+// accepts, kDrawWindow if there is none: the bit scan sphere_scan_bits makes
+// from window offset x, without consuming anything.
+__device__ __forceinline__ int next_accept(const unsigned* accbits, int wlen, int x) {
+  if (x + 1 >= wlen) return kDrawWindow;
+  const unsigned par = (x & 1) ? 0xAAAAAAAAu : 0x55555555u;
+  int w = x >> 5;
+  unsigned m = accbits[w] & par & (0xFFFFFFFFu << (x & 31));
+  while (!m) {
+    if (++w >= kDrawWindow / 32) return kDrawWindow;
+    m = accbits[w] & par;
+  }
+  return (w << 5) + (__ffs(m) - 1);
+}
+
+// Molecule::Pivot's draws for every bead at once. Bead k of the scan order
+// (forward from the pivot, then backward) takes randSphere's accepted pair at
+// p_k and, with the bond potential on, one bond-length draw at p_k + 2, so
+// p_{k+1} = next_accept(p_k + step) with step 2 or 3: thread 0's sequential
+// scan is the chain p_0 = next_accept(rel0), p_k = F^k(p_0). The block tabulates
+// F^(2^l) for every window offset (pointer doubling) and each thread composes
+// the jumps of its bead's rank. Offsets, and therefore results, are those of
+// the sequential scan; plan.scan_ok is cleared when any bead's draws run past
+// the window, and thread 0 then makes the sequential scan instead.
+__device__ __forceinline__ void pivot_draws(const DevParams& P, int wlen, GenPlan& plan,
+                                            int* s_off, int* s_boff,
+                                            short (*jump)[kDrawWindow + 1],
+                                            const unsigned* accbits) {
+  const int step = P.vary_bond ? 3 : 2;
+  const int len = plan.b1 - plan.b0, pv = plan.pivot;
+  const int n = len - 1, nf = len - 1 - pv;
+  int nl = 0;
+  while ((1 << nl) < n) nl++;  // ranks 0 .. n-1 need nl bits
+  for (int x = threadIdx.x; x <= kDrawWindow; x += blockDim.x)
+    jump[0][x] = (short)(x < kDrawWindow ? next_accept(accbits, wlen, x + step) : kDrawWindow);
+  for (int l = 1; l < nl; l++) {
+    __syncthreads();
+    for (int x = threadIdx.x; x <= kDrawWindow; x += blockDim.x)
+      jump[l][x] = jump[l - 1][jump[l - 1][x]];
+  }
+  if (threadIdx.x == 0) {
+    plan.scan_ok = 1;
+    plan.scan_end = plan.scan_rel;
+  }
+  __syncthreads();
+  const int p0 = next_accept(accbits, wlen, plan.scan_rel);
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    int p = p0;
+    for (int l = 0; l < nl; l++)
+      if ((k >> l) & 1) p = jump[l][p];
+    const int i = k < nf ? pv + 1 + k : pv - 1 - (k - nf);
+    if (p >= kDrawWindow || p + step > wlen) {
+      plan.scan_ok = 0;  // every writer stores the same value
+    } else {
+      s_off[i] = p;
+      s_boff[i] = p + 2;
+    }
+    if (k == n - 1) plan.scan_end = p + step;
+  }
+  __syncthreads();
+}
+
+// Thread 0, after the move's own draws: delayed acceptance's stage-one draw,
+// the stream check and the stream position.
+__device__ __forceinline__ void gen_tail(DevState* st, const DevBuffers& B, Draws& d,
+                                         GenPlan& plan) {
+  // Delayed acceptance: a chain move (pivot, crankshaft, reptation) takes
+  // its stage-one draw right after its own draws.
+  if (plan.type >= 2 && st->da_on && B.desc_acc && B.desc_fine) st->da_u1 = d.u();
+  if (d.overrun) {
+    st->error = PLUM_ERR_STREAM_DEV;
+    plan.type = -1;
+  }
+  st->stream_pos = d.pos;
+}
+
+// Thread 0's sequential pivot scan for chains up to kPivotMax beads: records
+// each bead's draw offsets for the block.
+__device__ __forceinline__ void pivot_draws_seq(const DevParams& P, Draws& d, long long wbase,
+                                                int len, int pivot, int* s_off, int* s_boff,
+                                                const unsigned* accbits) {
+  for (int dirn = 0; dirn < 2; dirn++) {
+    int i = dirn == 0 ? pivot + 1 : pivot - 1;
+    for (; dirn == 0 ? i < len : i >= 0; i += dirn == 0 ? 1 : -1) {
+      long long o = sphere_scan_bits(d, accbits);
+      s_off[i] = (int)(o - wbase);
+      if (P.vary_bond) {
+        s_boff[i] = (int)(d.pos - wbase);
+        (void)d.next();
+      }
+      if (d.overrun) break;
+    }
+  }
+}
+
+// The trial position of bead i, and its fixed-point mirror for the precision
+// form's pair sweep.
+__device__ __forceinline__ void put_trial(const DevParams& P, const DevBuffers& B, int b_lo, int i,
+                                          double4_32a t) {
+  B.trial[i] = t;
+  if (P.form) B.ftrial[i - b_lo] = fix_point(P, t, B.type[i]);
+}
 
 // Generates the next step's trial move into `trial` (and the fixed-point
 // mirror for the precision form); thread 0 consumes the draws, the block
@@ -192,11 +300,13 @@ constexpr int kPivotMax = 512;  // chains up to this length pivot in parallel
 __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B, DevState& S,
                                       Draws& d, long long wbase, GenPlan& plan, int* s_off,
                                       int* s_boff, double (*s_w)[kPivotMax],
+                                      short (*jump)[kDrawWindow + 1],
                                       const unsigned* accbits) {
   DevState* const st = &S;
   // ----------------------------------------------------- generate next move
   if (threadIdx.x == 0) {
     plan.type = -1;
+    plan.scan = 0;
     st->step_open = 1;
     (void)d.next();  // simulation.cc:221 (the GC draw)
     const int n_ch = P.n_chain_total, n_io = P.n_ion_total;
@@ -256,18 +366,9 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
           plan.s = s;
           plan.pivot = pivot;
           if (len <= kPivotMax) {
-            for (int dirn = 0; dirn < 2; dirn++) {
-              int i = dirn == 0 ? pivot + 1 : pivot - 1;
-              for (; dirn == 0 ? i < len : i >= 0; i += dirn == 0 ? 1 : -1) {
-                long long o = sphere_scan_bits(d, accbits);
-                s_off[i] = (int)(o - wbase);
-                if (P.vary_bond) {
-                  s_boff[i] = (int)(d.pos - wbase);
-                  (void)d.next();
-                }
-                if (d.overrun) break;
-              }
-            }
+            // the block locates every bead's draws (pivot_draws)
+            plan.scan = 1;
+            plan.scan_rel = (int)(d.pos - wbase);
           } else {
             plan.pivot = -1;
             const double eq = P.bond_len;
@@ -347,22 +448,30 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
         }
       }
     }
-    // Delayed acceptance: a chain move (pivot, crankshaft, reptation) takes
-    // its stage-one draw right after its own draws.
-    if (plan.type >= 2 && st->da_on && B.desc_acc && B.desc_fine) st->da_u1 = d.u();
-    if (d.overrun) {
-      st->error = PLUM_ERR_STREAM_DEV;
-      plan.type = -1;
-    }
-    st->stream_pos = d.pos;
+    if (!plan.scan) gen_tail(st, B, d, plan);
   }
   __syncthreads();
-  // Apply the plan in parallel (pivot already wrote its trial positions).
+  if (plan.scan) {
+    pivot_draws(P, d.wlen, plan, s_off, s_boff, jump, accbits);
+    if (threadIdx.x == 0) {
+      if (plan.scan_ok) {
+        d.pos = wbase + plan.scan_end;
+      } else {
+        d.pos = wbase + plan.scan_rel;
+        pivot_draws_seq(P, d, wbase, plan.b1 - plan.b0, plan.pivot, s_off, s_boff, accbits);
+      }
+      gen_tail(st, B, d, plan);
+    }
+    __syncthreads();
+  }
+  // Apply the plan in parallel (the sequential pivot of a long chain already
+  // wrote its trial positions).
   const GenPlan g = plan;
   if (g.type == 0 || g.type == 1) {
     for (int i = g.b_lo + threadIdx.x; i < g.b_hi; i += blockDim.x) {
       double4_32a o = B.pos[i];
-      B.trial[i] = make_double4_32a(o.x + g.vec[0], o.y + g.vec[1], o.z + g.vec[2], o.w);
+      put_trial(P, B, g.b_lo, i,
+                make_double4_32a(o.x + g.vec[0], o.y + g.vec[1], o.z + g.vec[2], o.w));
     }
   } else if (g.type == 3) {
     const double4_32a pf = B.pos[g.b0 + g.first];
@@ -372,7 +481,7 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
       double r[3];
       for (int a = 0; a < 3; a++)
         r[a] = ((g.R[3 * a] * v[0] + g.R[3 * a + 1] * v[1]) + g.R[3 * a + 2] * v[2]);
-      B.trial[i] = make_double4_32a(r[0] + pf.x, r[1] + pf.y, r[2] + pf.z, o.w);
+      put_trial(P, B, g.b_lo, i, make_double4_32a(r[0] + pf.x, r[1] + pf.y, r[2] + pf.z, o.w));
     }
   } else if (g.type == 2 && g.pivot >= 0) {
     const int len = g.b1 - g.b0, pv = g.pivot;
@@ -417,9 +526,12 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
       const int i = k < nf ? pv + 1 + k : pv - 1 - (k - nf);
       const double q = B.pos[g.b0 + i].w;
-      B.trial[g.b0 + i] =
-          make_double4_32a(pp.x + s_w[0][k], pp.y + s_w[1][k], pp.z + s_w[2][k], q);
+      put_trial(P, B, g.b_lo, g.b0 + i,
+                make_double4_32a(pp.x + s_w[0][k], pp.y + s_w[1][k], pp.z + s_w[2][k], q));
     }
+    // the pivot bead stays where it is (its trial entry equals its position)
+    if (P.form && threadIdx.x == 0)
+      B.ftrial[g.b0 + pv - g.b_lo] = fix_point(P, B.trial[g.b0 + pv], B.type[g.b0 + pv]);
   } else if (g.type == 4) {
     const int len = g.b1 - g.b0;
     for (int i = threadIdx.x; i < len; i += blockDim.x) {
@@ -431,11 +543,11 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
         double4_32a o = B.pos[g.b0 + i + g.dir];
         nw = make_double4_32a(o.x, o.y, o.z, B.pos[g.b0 + i].w);
       }
-      B.trial[g.b0 + i] = nw;
+      put_trial(P, B, g.b_lo, g.b0 + i, nw);
     }
   }
-  if (P.form && g.type >= 0) {
-    // fixed-point trial coordinates for the precision form's pair sweep
+  if (P.form && g.type == 2 && g.pivot < 0) {
+    // fixed-point trial coordinates of the sequential pivot
     __syncthreads();
     for (int i = g.b_lo + threadIdx.x; i < g.b_hi; i += blockDim.x)
       B.ftrial[i - g.b_lo] = fix_point(P, B.trial[i], B.type[i]);
@@ -467,7 +579,10 @@ struct SerialSmem {
   GenPlan plan;
   int s_accept, s_ext_bad;
   int s_off[kPivotMax], s_boff[kPivotMax];  // draw offsets per bead
-  double s_w[3][kPivotMax];                 // pivot bond steps
+  union {
+    short jump[kJumpLevels][kDrawWindow + 1];  // pivot draws: 2^l beads on
+    double s_w[3][kPivotMax];                  // pivot bond steps (used after)
+  };
   // The state lives in shared memory for the step: thread 0's chain of
   // decisions then never waits on global memory for it.
   DevState S;
@@ -491,6 +606,7 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
   int* const s_off = sm.s_off;
   int* const s_boff = sm.s_boff;
   double(*const s_w)[kPivotMax] = sm.s_w;
+  short(*const jump)[kDrawWindow + 1] = sm.jump;
   DevState& S = sm.S;
   {
     const int nw = (int)(sizeof(DevState) / sizeof(int));
@@ -527,14 +643,13 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
   }
   __syncthreads();
   if (mode & kModeGen) {
-    // every window position's randSphere test, 32 positions per thread-word
-    for (int w = threadIdx.x; w < kDrawWindow / 32; w += blockDim.x) {
-      unsigned bits = 0u;
-      for (int k = 0; k < 32; k++) {
-        const int p = w * 32 + k;
-        if (p + 1 < wlen && !sphere_reject(win[p], win[p + 1])) bits |= 1u << k;
-      }
-      accbits[w] = bits;
+    // every window position's randSphere test, one position per thread; a
+    // warp's ballot makes the word of its 32 positions
+    for (int p0 = threadIdx.x & ~31; p0 < kDrawWindow; p0 += blockDim.x) {
+      const int p = p0 + (threadIdx.x & 31);
+      const bool ok = p + 1 < wlen && !sphere_reject(win[p], win[p + 1]);
+      const unsigned bits = __ballot_sync(0xFFFFFFFFu, ok);
+      if ((threadIdx.x & 31) == 0) accbits[p0 >> 5] = bits;
     }
     __syncthreads();
   }
@@ -735,7 +850,7 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
   __syncthreads();
 
   if ((mode & kModeGen) && !S.error)
-    gen_move(P, B, S, d, wbase, plan, s_off, s_boff, s_w, accbits);
+    gen_move(P, B, S, d, wbase, plan, s_off, s_boff, s_w, jump, accbits);
 
   // write the state back
   if (threadIdx.x == 0) S.stream_pos = S.stream_pos > d.pos ? S.stream_pos : d.pos;

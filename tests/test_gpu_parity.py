@@ -111,6 +111,53 @@ def test_medium_system_long_replay_against_oracle(pg, built):
     np.testing.assert_allclose(s.positions(), o.coords(), rtol=0, atol=1e-8)
 
 
+@pytest.mark.parametrize("chain_len,use_bond", [(200, True), (300, True), (300, False),
+                                                (600, True)])
+def test_long_chain_pivots_against_oracle(pg, built, tmp_path, chain_len, use_bond):
+    """Pivots of long chains replay the oracle's draw sequence: the block's
+    parallel scan of the beads' draws (up to 512 beads, with the bond-length
+    draw of the bond potential and without it), its hand-back to thread 0's
+    scan when the draws run past the staged window (300 beads with the bond
+    draw need ~1,050 stream words), and the sequential pivot of chains over
+    512 beads. High temperature (beta = 0.02) so that moves are accepted."""
+    from plum_gb300 import systems
+    d = str(tmp_path / "long")
+    systems.write_bulk(d, systems.BulkSpec(n_chain=2, chain_len=chain_len, n_ion=60, box=30.0,
+                                           move_size=0.15,
+                                           move_prob=(0.1, 0.05, 0.55, 0.15, 0.15),
+                                           use_bond=use_bond), seed=7, beta=0.02)
+    s = pg.System(d)
+    o = built.Oracle(d)
+    stream = built.mt19937(77, 400000)
+    n = 120
+    used, mt, ac, et = s.run_moves(stream, n)
+    used_o, mt_o, ac_o, et_o = o.run_stream(n, stream)
+    assert (np.asarray(mt_o) == 2).sum() > 40
+    assert used == used_o
+    np.testing.assert_array_equal(mt, mt_o)
+    np.testing.assert_array_equal(ac, ac_o)
+    np.testing.assert_allclose(et, et_o, rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(s.positions(), o.coords(), rtol=0, atol=1e-8)
+
+
+@pytest.mark.parametrize("workload", ["bulk_1000_pinned", "bulk_1000"])
+def test_from_scratch_totals_against_oracle(pg, built, tmp_path, workload):
+    """The from-scratch FP64 totals of the 1,000-bead bulk system: with
+    r_c = L/2 (the fixed-point pair kernel: one image, cubic box) and with the
+    reference's automatic r_c = 28 > L/2 (image cells), both forms, against
+    the oracle's at 1e-10."""
+    from plum_gb300 import systems
+    d = str(tmp_path / workload)
+    systems.write_bulk(d, systems.CONFIGS[workload], seed=5)
+    want = built.Oracle(d).energies()
+    for form in (pg.FORM_FP64, pg.FORM_FP32):
+        s = pg.System(d, form=form)
+        got = s.total_energy()[:4]
+        for a, b in zip(got, want):
+            assert abs(a - b) <= 1e-10 * max(1.0, abs(b)), (workload, form, got, want)
+        s.close()
+
+
 def test_stream_exhaustion_reported(pg, built):
     d, _ = load("bulk_small")
     s = pg.System(d)
