@@ -160,14 +160,14 @@ def tau_pooled(X, c=5.0):
     return float(-1.0 / slope), "exponential fit"
 
 
-def paired_check(x, y, k=2.0):
-    """Per-replica means x (chosen form) and y (plain FP64) paired by their
-    starting configuration: the mean difference against k standard errors
-    of the paired differences."""
+def paired_check(x, y, k=2.0, other="plain_fp64"):
+    """Per-replica means x (chosen form) and y (the other arm: plain FP64, or
+    plain Metropolis dynamics) paired by their starting configuration: the
+    mean difference against k standard errors of the paired differences."""
     import numpy as np
     diff = np.asarray(x, np.float64) - np.asarray(y, np.float64)
     se = float(diff.std(ddof=1) / math.sqrt(len(diff)))
-    return {"chosen_mean": float(np.mean(x)), "plain_fp64_mean": float(np.mean(y)),
+    return {"chosen_mean": float(np.mean(x)), other + "_mean": float(np.mean(y)),
             "paired_difference": float(diff.mean()), "standard_error": se,
             "within_2_se": bool(abs(diff.mean()) <= k * se)}
 
@@ -406,10 +406,12 @@ def equilibrium(args, device, sg, tune):
           seeds), sampled every `tau_every` moves: tau_int of the chains'
           Rg^2 (pooled over all chains, Sokal window c = 5, an exponential
           fit when the window does not close) and of the total energy, and
-          the paired check of their per-replica means (same protocol: with
-          the 12 k_BT dead zone stage one only rejects moves Metropolis
-          rejects but for the surrogate's errors, and delayed acceptance
-          keeps the stationary distribution);
+          the paired check of their per-replica means (same protocol;
+          delayed acceptance keeps the stationary distribution, so from
+          equilibrated starts the means agree, while a relaxing system's
+          chosen-form series lags plain Metropolis's, since it accepts fewer
+          moves: starts_equilibrated compares the burn-in's final drift over
+          the series length with the check's standard error);
       (b) plain Metropolis in FP32 and in FP64 from the same starts with the
           same seeds: the two make the same decisions until a flipped one,
           so their trajectories (and Rg^2, exactly) agree until then; the
@@ -487,10 +489,23 @@ def equilibrium(args, device, sg, tune):
     out["series"] = res
     ch, pl = res["chosen_form"], res["plain_dynamics_fp32"]
     out["chosen_vs_plain_dynamics"] = {
-        "energy": paired_check(ch["mean_energy_per_replica"], pl["mean_energy_per_replica"]),
-        "rg2": paired_check(ch["mean_rg2_per_replica"], pl["mean_rg2_per_replica"]),
+        "energy": paired_check(ch["mean_energy_per_replica"], pl["mean_energy_per_replica"],
+                               other="plain_dynamics"),
+        "rg2": paired_check(ch["mean_rg2_per_replica"], pl["mean_rg2_per_replica"],
+                            other="plain_dynamics"),
         "definition": "(a): same starts, same number of moves, different seeds; per-replica "
                       "means, mean paired difference against 2 standard errors"}
+    # Whether the starts are equilibrated: the energy change the burn-in's
+    # final drift would give over the series, against the standard error of
+    # (a). Delayed acceptance keeps the stationary distribution but accepts
+    # fewer moves, so while the system still relaxes its series lags plain
+    # Metropolis's and (a) and (c) measure the relaxation, not a bias.
+    drift = out.get("burn_in_energy_drift_per_1e5_moves")
+    if drift is not None:
+        relax = abs(drift) * args.tau_moves / 1e5
+        se_a = out["chosen_vs_plain_dynamics"]["energy"]["standard_error"]
+        out["relaxation_over_series_kT"] = relax
+        out["starts_equilibrated"] = bool(relax < 2.0 * se_a)
 
     # (b) FP32 and FP64 plain Metropolis, same starts and seeds
     t1 = time.perf_counter()

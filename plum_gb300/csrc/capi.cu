@@ -263,6 +263,10 @@ int enqueue_total(plum_ctx* c, cudaStream_t s, double* drift) {
     launch_fix_all(P, c->B, s);
     k++;
   }
+  if (c->B.fpos64) {
+    launch_fix64_all(P, c->B, s);
+    k++;
+  }
   return k;
 }
 
@@ -659,6 +663,8 @@ static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out) {
       P.htab64 = c->d_htab64;
     }
   }
+  // the plain form's 64-bit position mirror for its fixed-point pair loop
+  if (form == PLUM_FORM_FP64 && fix_pairs(P)) rc |= dalloc(&c->B.fpos64, nb);
   // the precision form's real-space term from the h(u) table where the
   // cut-off lies inside it (alpha r_c^2 < 2^kH32EHi)
   P.htab = nullptr;
@@ -727,7 +733,8 @@ int plum_ctx_destroy(plum_ctx* c) {
                   c->cb_part,    c->cb_u,      c->d_obs_per, c->d_rhoz, c->desc_acc,
                   c->d_rp1,      c->d_rb1,     c->desc_fine, c->cb_part32, c->cb_ticket,
                   c->d_stream,   c->d_mt,      c->d_log_type, c->d_log_acc, c->d_log_e,
-                  c->d_press,    c->d_sk_part, c->d_log_de, c->d_htab, c->d_htab64};
+                  c->d_press,    c->d_sk_part, c->d_log_de, c->d_htab, c->d_htab64,
+                  c->B.fpos64};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (c->h_out) cudaFreeHost(c->h_out);
@@ -857,12 +864,15 @@ int rebuild_system(plum_ctx* c) {
   P.n_mol = in.n_mol;
   P.n_chain_total = (int)chains.size();
   P.n_ion_total = (int)ions.size();
+  const bool mirror64 = B.fpos64 != nullptr;
   void* old[] = {B.pos,      B.trial,      B.type,     B.mol_start, B.chain_ids, B.ion_ids,
                  B.fpos,     B.fq,         B.ftrial,   B.dsk_part,  B.dsk_part32, B.bond_mol,
-                 c->d_tot_part, c->d_obs_per, c->cb_b, c->cb_c,    c->cb_part,  c->cb_u};
+                 c->d_tot_part, c->d_obs_per, c->cb_b, c->cb_c,    c->cb_part,  c->cb_u,
+                 B.fpos64};
   for (void* q : old)
     if (q) cudaFree(q);
   B.pos = B.trial = nullptr;
+  B.fpos64 = nullptr;
   B.type = B.mol_start = B.chain_ids = B.ion_ids = nullptr;
   B.fpos = B.ftrial = nullptr;
   B.fq = nullptr;
@@ -877,6 +887,7 @@ int rebuild_system(plum_ctx* c) {
            dalloc(&B.mol_start, in.n_mol + 1) | dalloc(&B.chain_ids, chains.size()) |
            dalloc(&B.ion_ids, ions.size()) | dalloc(&B.fpos, nb) | dalloc(&B.fq, nb) |
            dalloc(&B.ftrial, c->max_len) | dalloc(&B.bond_mol, in.n_mol);
+  if (mirror64) rc |= dalloc(&B.fpos64, nb);
   const int groups = (c->max_len + std::max(1, P.kchunk_delta) - 1) / std::max(1, P.kchunk_delta);
   rc |= dalloc(&B.dsk_part, (size_t)groups * std::max(1, P.n_k));
   rc |= dalloc(&B.dsk_part32, (size_t)groups * std::max(1, P.n_k));
@@ -1330,6 +1341,7 @@ int plum_ctx_load(plum_ctx* c, const void* buf, long size) {
   std::memcpy(c->drift, p, 4 * sizeof(double));
   std::memcpy(&c->drift_max, p + 4 * sizeof(double), sizeof(double));
   if (c->form == PLUM_FORM_FP32) launch_fix_all(c->P, c->B, c->s);  // the fixed-point mirror
+  launch_fix64_all(c->P, c->B, c->s);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->s));
   c->h_pos_valid = true;
@@ -1944,7 +1956,8 @@ void cells_enqueue(plum_batch* b) {
 // Kernel launches of batch_enqueue(b, steps).
 long batch_kernels(const plum_batch* b, int steps) {
   const bool cells = b->sg && b->cell_moved;
-  const long stage = b->sg ? (cells && b->cells_on ? 3 : 2) + 1 : 0;
+  // descriptor (cell kernel, or the all-pairs kernel), smearing, inference
+  const long stage = b->sg ? 3 : 0;
   const long chains = (b->groups > 1 && b->reps.size() > 1) ? 2 : 1;
   return (cells ? (b->cells_on ? 4 : 1) : 0) + chains * (1 + 2L * steps + steps * stage);
 }
@@ -2284,6 +2297,11 @@ int plum_batch_create(int n, const char* const* dirs, const char* const* runins,
     b->cell_moved = std::max(b->cell_moved, std::min(b->reps[r]->max_len, 512));
     b->max_bead = std::max(b->max_bead, P.n_bead);
   }
+  // the cell kernel also takes the replicas without lists (all pairs): its
+  // grid covers every replica's longest molecule
+  if (b->cell_moved)
+    for (int r = 0; r < n; r++)
+      b->cell_moved = std::max(b->cell_moved, std::min(b->reps[r]->max_len, 512));
   b->h_rp = hp;
   b->h_rb = hb;
   if (b->cell_moved && cells_alloc(b)) {

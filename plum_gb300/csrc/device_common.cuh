@@ -81,6 +81,21 @@ __device__ __forceinline__ int fix_axis(double x, double L, double inv_fix, bool
   return (int)(unsigned int)(unsigned long long)v;
 }
 
+// 64-bit fixed-point fraction of the box: frac(x / L) 2^64.
+__device__ __forceinline__ unsigned long long fix64(double x, double inv) {
+  double f = x * inv;
+  f -= floor(f);
+  if (f >= 1.0) f = 0.0;  // a tiny negative x / L rounds up to 1
+  return __double2ull_rn(f * 0x1p64);
+}
+
+// A bead as the plain form's 64-bit mirror holds it (cubic box).
+__device__ __forceinline__ ulonglong4_32a fix64x4(const DevParams& P, double4_32a p) {
+  const double inv = P.inv_ebox[0];
+  return make_ulonglong4_32a(fix64(p.x, inv), fix64(p.y, inv), fix64(p.z, inv),
+                         (unsigned long long)__double_as_longlong(p.w));
+}
+
 __device__ __forceinline__ int4 fix_point(const DevParams& P, double4_32a p, int type) {
   return make_int4(fix_axis(p.x, P.ebox[0], P.inv_fix[0], true),
                    fix_axis(p.y, P.ebox[1], P.inv_fix[1], true),

@@ -144,6 +144,14 @@ struct DevState {
   int log_n, log_cap;
 };
 
+// The fixed-point pair form of the FP64 kernels (k_delta64, k_total64):
+// LJ + Ewald in a cubic box periodic on every axis, one image (r_c <= L/2),
+// one box for both terms, the FP64 h(u) table.
+__host__ __device__ inline bool fix_pairs(const DevParams& P) {
+  return P.use_ewald && P.htab64 && P.same_wrap && P.npbc == 3 && P.single_image &&
+         P.pair_kind == 0 && P.ebox[0] == P.ebox[1] && P.ebox[1] == P.ebox[2];
+}
+
 struct DevBuffers {  // all pointers: copied word-wise into shared memory by the batch kernels
   double4_32a* pos;
   double4_32a* trial;
@@ -156,6 +164,9 @@ struct DevBuffers {  // all pointers: copied word-wise into shared memory by the
   double2* sk;
   double2* dsk;      // [2][n_k] double-buffered dS(k)
   double* partial;   // [grid][4]
+  // plain form mirror (fix_pairs systems; null otherwise): 64-bit
+  // fixed-point fractions of the box (X, Y, Z) and the charge's bits
+  ulonglong4_32a* fpos64;  // [n_bead] current positions
   // precision form mirrors: 32-bit fixed-point fractions of the Ewald box
   int4* fpos;        // [n_bead] current (X, Y, Z, type)
   float* fq;         // [n_bead] charges
@@ -232,6 +243,8 @@ void launch_rhoz(const DevParams& P, const DevBuffers& B, double res, int n_bins
 // precision form (kern_fp32.cu)
 int pair_grid32();
 void launch_delta_pairs32(const DevParams& P, const DevBuffers& B, cudaStream_t s);
+// the plain form's 64-bit position mirror (B.fpos64), where it has one
+void launch_fix64_all(const DevParams& P, const DevBuffers& B, cudaStream_t s);
 void launch_fix_all(const DevParams& P, const DevBuffers& B, cudaStream_t s);
 void launch_fix_trial(const DevParams& P, const DevBuffers& B, cudaStream_t s);
 

@@ -159,6 +159,48 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return t;  // valid in thread 0
 }
 
+// Constants of the fixed-point pair form: squared distances in units of
+// (L / 2^64)^2 ("raw"). A non-negative double orders like its bit pattern
+// read as an integer, so the cut-off tests are integer compares (off the
+// FP64 pipe).
+struct FixConst {
+  double s2, ua, pref;
+  long long rc2_bits, lj2_bits;  // raw r_c^2 and raw LJ reach, as bits
+};
+__device__ __forceinline__ FixConst fix_const(const DevParams& P) {
+  FixConst F;
+  const double s = P.ebox[0] * 0x1p-64;  // L / 2^64
+  F.s2 = s * s;
+  F.ua = P.alpha * F.s2;
+  F.pref = P.lB * P.sqrt_alpha;
+  F.rc2_bits = __double_as_longlong(P.real_cut * P.real_cut / F.s2);
+  F.lj2_bits = P.use_pair ? __double_as_longlong(P.lj_max2 / F.s2) : 0;
+  return F;
+}
+
+// One pair in the fixed-point form: adds its LJ energy at (k, r^2) to lj and
+// returns h(alpha r^2) inside the real-space cut-off (0 outside, and at
+// r = 0 as the reference's r > 0 test has it); the caller multiplies by the
+// charge product with lB sqrt(alpha) folded in.
+__device__ __forceinline__ double pair_fix(const DevParams& P, const FixConst& F,
+                                           unsigned long long ax, unsigned long long ay,
+                                           unsigned long long az, unsigned long long bx,
+                                           unsigned long long by, unsigned long long bz, int k,
+                                           double& lj) {
+  const double dx = __ll2double_rn((long long)(bx - ax));
+  const double dy = __ll2double_rn((long long)(by - ay));
+  const double dz = __ll2double_rn((long long)(bz - az));
+  const double raw = fma(dx, dx, fma(dy, dy, dz * dz));
+  const long long rb = __double_as_longlong(raw);
+  if (rb < F.lj2_bits) lj += lj64(P, k, raw * F.s2);
+  if (rb > 0 && rb <= F.rc2_bits) {
+    const long long bits = __double_as_longlong(raw * F.ua);
+    return bits >= kH64LoBits ? h64_tab(P.htab64, bits)
+                              : real_term64(P, raw * F.s2) / P.sqrt_alpha;
+  }
+  return 0.0;
+}
+
 // ---------------------------------------------------------------- delta
 // Pair sweep: the m x N (moved, other) pairs are numbered p = i*N + j and dealt
 // to every thread of the grid in turn, so even a one-bead move spreads over
@@ -170,6 +212,9 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 // finish (atomic ticket) adds the groups in order -- deterministic -- and
 // writes dS(k) and the tile's energy change.
 constexpr int kKTile = 128;
+constexpr int kFixStage = 128;  // moved beads the fixed-point pair form stages
+constexpr size_t kFixBytes = kFixStage * (6 * sizeof(unsigned long long) + sizeof(double) +
+                                          sizeof(int));
 
 __global__ void __launch_bounds__(kPairThreads)
     k_delta64(const DevParams P, const DevBuffers B) {
@@ -184,7 +229,55 @@ __global__ void __launch_bounds__(kPairThreads)
   const int N = P.n_bead;
 
   double acc_lj = 0.0, acc_re = 0.0;
-  if (P.use_pair || P.use_ewald) {
+  if (m > 0 && m <= kFixStage && B.fpos64 && fix_pairs(P)) {
+    // Fixed-point pair form: the moved beads (trial and current) are staged
+    // once per block as 64-bit fixed-point fractions of the box, the other
+    // beads come from the context's 64-bit mirror; pairs are dealt over the
+    // grid by the same flat index as below. A moved other bead j pairs once
+    // with each moved bead i < j, both at trial or both at current positions.
+    unsigned long long* fx = reinterpret_cast<unsigned long long*>(smem);  // [6][kFixStage]
+    double* fq = reinterpret_cast<double*>(fx + 6 * kFixStage);
+    int* fk = reinterpret_cast<int*>(fq + kFixStage);
+    const FixConst F = fix_const(P);
+    for (int t = threadIdx.x; t < m; t += blockDim.x) {
+      const ulonglong4_32a a = fix64x4(P, B.trial[b_lo + t]), c = fix64x4(P, B.pos[b_lo + t]);
+      fx[t] = a.x;
+      fx[kFixStage + t] = a.y;
+      fx[2 * kFixStage + t] = a.z;
+      fx[3 * kFixStage + t] = c.x;
+      fx[4 * kFixStage + t] = c.y;
+      fx[5 * kFixStage + t] = c.z;
+      fq[t] = __longlong_as_double((long long)c.w) * F.pref;
+      fk[t] = B.type[b_lo + t] * P.n_type;
+    }
+    __syncthreads();
+    const long long total = (long long)m * N;
+    const long long G = (long long)gridDim.x * blockDim.x;
+    const long long p0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int gq = (int)(G / N), gr = (int)(G % N);
+    int ii = (int)(p0 / N), j = (int)(p0 % N);
+    double lj0 = 0.0;  // LJ at current positions, subtracted at the end
+    for (long long p = p0; p < total; p += G, ii += gq, j += gr) {
+      if (j >= N) {
+        j -= N;
+        ii++;
+      }
+      const bool jm = j >= b_lo && j < b_hi;
+      if (jm && j <= b_lo + ii) continue;
+      const ulonglong4_32a o = B.fpos64[j];
+      const int k = fk[ii] + B.type[j];
+      const double qq = fq[ii] * __longlong_as_double((long long)o.w);
+      const int l = jm ? j - b_lo : 0;
+      const double h1 =
+          pair_fix(P, F, fx[ii], fx[kFixStage + ii], fx[2 * kFixStage + ii],
+                   jm ? fx[l] : o.x, jm ? fx[kFixStage + l] : o.y,
+                   jm ? fx[2 * kFixStage + l] : o.z, k, acc_lj);
+      const double h0 = pair_fix(P, F, fx[3 * kFixStage + ii], fx[4 * kFixStage + ii],
+                                 fx[5 * kFixStage + ii], o.x, o.y, o.z, k, lj0);
+      acc_re = fma(qq, h1 - h0, acc_re);
+    }
+    acc_lj -= lj0;
+  } else if (P.use_pair || P.use_ewald) {
     // pair p = ii * N + j, dealt with stride G; (ii, j) advanced without a
     // division per pair
     const long long total = (long long)m * N;
@@ -322,14 +415,15 @@ int pair_grid() {
 }
 
 static size_t delta_smem(const DevParams& P) {
-  return P.use_ewald ? (size_t)P.kchunk_delta * 2 * P.kper * sizeof(double2) : 0;
+  const size_t k = P.use_ewald ? (size_t)P.kchunk_delta * 2 * P.kper * sizeof(double2) : 0;
+  return fix_pairs(P) ? std::max(k, kFixBytes) : k;
 }
 
 void launch_delta_pairs64(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_delta64, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         kKTableBytes + 4096);
+                         std::max((size_t)kKTableBytes + 4096, kFixBytes));
     attr = true;
   }
   k_delta64<<<pair_grid(), kPairThreads, delta_smem(P), s>>>(P, B);
@@ -384,14 +478,6 @@ __global__ void __launch_bounds__(kTotTile)
   }
 }
 
-// 64-bit fixed-point fraction of the box: frac(x / L) 2^64.
-__device__ __forceinline__ unsigned long long fix64(double x, double inv) {
-  double f = x * inv;
-  f -= floor(f);
-  if (f >= 1.0) f = 0.0;  // a tiny negative x / L rounds up to 1
-  return __double2ull_rn(f * 0x1p64);
-}
-
 // k_total64 for LJ + Ewald in a cubic box periodic on every axis, one image
 // (r_c <= L/2) and one box for both terms: positions as 64-bit fixed-point
 // fractions of the box, staged per tile, so one integer subtraction is the
@@ -421,37 +507,17 @@ __global__ void __launch_bounds__(kTotTile)
     st[threadIdx.x] = B.type[j0 + threadIdx.x];
   }
   __syncthreads();
-  const double s = P.ebox[0] * 0x1p-64;  // L / 2^64
-  const double s2 = s * s;
-  const double rc2_raw = P.real_cut * P.real_cut / s2;
-  const double lj2_raw = P.lj_max2 / s2;
-  const double ua = P.alpha * s2;
-  // FP32 pre-tests, a little wide: the FP64 tests inside decide
-  const float rc_hi = (float)rc2_raw * 1.0001f, lj_hi = (float)lj2_raw * 1.0001f;
+  const FixConst F = fix_const(P);
   double lj = 0.0, re = 0.0;
   const int i = ta * kTotTile + threadIdx.x;
   if (i < P.n_bead) {
     const double4_32a pi = B.pos[i];
     const unsigned long long ux = fix64(pi.x, inv), uy = fix64(pi.y, inv), uz = fix64(pi.z, inv);
-    const double qi = pi.w * P.lB * P.sqrt_alpha;
+    const double qi = pi.w * F.pref;
     const int kt = B.type[i] * P.n_type;
-    for (int jj = ta == tb ? (int)threadIdx.x + 1 : 0; jj < jn; jj++) {
-      const double dx = __ll2double_rn((long long)(sx[jj] - ux));
-      const double dy = __ll2double_rn((long long)(sy[jj] - uy));
-      const double dz = __ll2double_rn((long long)(sz[jj] - uz));
-      const double raw = fma(dx, dx, fma(dy, dy, dz * dz));
-      const float rf = __double2float_rn(raw);
-      if (P.use_pair && rf < lj_hi && raw < lj2_raw) lj += lj64(P, kt + st[jj], raw * s2);
-      if (rf <= rc_hi && raw <= rc2_raw && raw > 0.0) {
-        const double qq = qi * sq[jj];
-        if (qq != 0.0) {
-          const long long bits = __double_as_longlong(raw * ua);
-          const double h = bits >= kH64LoBits ? h64_tab(P.htab64, bits)
-                                              : real_term64(P, raw * s2) / P.sqrt_alpha;
-          re = fma(qq, h, re);
-        }
-      }
-    }
+    for (int jj = ta == tb ? (int)threadIdx.x + 1 : 0; jj < jn; jj++)
+      re = fma(qi * sq[jj], pair_fix(P, F, ux, uy, uz, sx[jj], sy[jj], sz[jj], kt + st[jj], lj),
+               re);
   }
   const double a = block_sum<kTotTile>(lj, red);
   const double b = block_sum<kTotTile>(re, red + kTotTile / 32);
@@ -461,6 +527,16 @@ __global__ void __launch_bounds__(kTotTile)
   }
 }
 
+// The plain form's 64-bit mirror of every bead's position.
+__global__ void k_fix64_all(const DevParams P, const DevBuffers B) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.n_bead; i += gridDim.x * blockDim.x)
+    B.fpos64[i] = fix64x4(P, B.pos[i]);
+}
+
+void launch_fix64_all(const DevParams& P, const DevBuffers& B, cudaStream_t s) {
+  if (B.fpos64 && P.n_bead > 0) k_fix64_all<<<(P.n_bead + 255) / 256, 256, 0, s>>>(P, B);
+}
+
 int total_partials_count(const DevParams& P) {
   long long nt = (P.n_bead + kTotTile - 1) / kTotTile;
   return (int)(nt * (nt + 1) / 2);
@@ -468,9 +544,7 @@ int total_partials_count(const DevParams& P) {
 
 void launch_total64(const DevParams& P, const DevBuffers& B, double* out, int n_part,
                     cudaStream_t s) {
-  const bool fix = P.use_ewald && P.htab64 && P.same_wrap && P.npbc == 3 && P.single_image &&
-                   P.pair_kind == 0 && P.ebox[0] == P.ebox[1] && P.ebox[1] == P.ebox[2];
-  if (fix)
+  if (fix_pairs(P))
     k_total64_fix<<<n_part, kTotTile, 0, s>>>(P, B, out);
   else
     k_total64<<<n_part, kTotTile, 0, s>>>(P, B, out);

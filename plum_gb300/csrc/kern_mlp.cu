@@ -995,13 +995,16 @@ constexpr int kCellWarps = 2 * kCellBeads * kCellSplit;
 // once, at the end). Entries carry the positions, so a candidate costs one
 // load, and the 27 cells' entries form one list spread over the lanes. The
 // same pairs, distances and bins as k_desc.
+// A replica without a valid list (none built, or one that overflowed since
+// the last rebuild) takes every other bead instead of the cells' entries:
+// the same pairs, so the same counts, at all-pairs cost, in this launch.
 __global__ void __launch_bounds__(kCellWarps * 32, 1)
     k_desc_cells(const DevParams* __restrict__ rp, const DevBuffers* __restrict__ rb) {
   const DevParams& P = rp[blockIdx.y];
   const DevBuffers& B = rb[blockIdx.y];
-  if (!P.cell_cap || !B.cell_key) return;
   const DevState* st = B.state;
-  if (!(st->pending && st->da_active && st->cell_ok)) return;
+  if (!(st->pending && st->da_active)) return;
+  const bool cells = P.cell_cap && B.cell_key && st->cell_ok;
   const int b_lo = st->b_lo, m = min(st->b_hi - b_lo, kDescMaxMoved);
   if ((int)blockIdx.x * kCellBeads >= m) return;
   __shared__ unsigned fh[kFineAll];
@@ -1020,7 +1023,7 @@ __global__ void __launch_bounds__(kCellWarps * 32, 1)
     // lane l < 27: neighbour cell l (offsets -1..1 per axis): its first
     // entry and count
     int cbase = 0, cn = 0;
-    if (lane < 27) {
+    if (cells && lane < 27) {
       const int ox = lane % 3 - 1, oy = (lane / 3) % 3 - 1, oz = lane / 9 - 1;
       int x = cell_axis((unsigned)p.x, nx) + ox, y = cell_axis((unsigned)p.y, ny) + oy,
           z = cell_axis((unsigned)p.z, nz) + oz;
@@ -1051,18 +1054,26 @@ __global__ void __launch_bounds__(kCellWarps * 32, 1)
     s_pre[w][lane] = pre;
     s_base[w][lane] = cbase;
     __syncwarp();
-    const int e_lo = part * total / kCellSplit, e_hi = (part + 1) * total / kCellSplit;
+    if (cells) {
+      const int e_lo = part * total / kCellSplit, e_hi = (part + 1) * total / kCellSplit;
 #pragma unroll 4
-    for (int e = e_lo + lane; e < e_hi; e += 32) {
-      int lo = 0, hi = 26;
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (s_pre[w][mid] > e) hi = mid; else lo = mid + 1;
+      for (int e = e_lo + lane; e < e_hi; e += 32) {
+        int lo = 0, hi = 26;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (s_pre[w][mid] > e) hi = mid; else lo = mid + 1;
+        }
+        visit(B.cell_ent[s_base[w][lo] + e - (lo ? s_pre[w][lo - 1] : 0)]);
       }
-      visit(B.cell_ent[s_base[w][lo] + e - (lo ? s_pre[w][lo - 1] : 0)]);
+      const int n_extra = min(B.cell_n[nx * ny * nz], P.cell_cap);
+      for (int e = part * 32 + lane; e < n_extra; e += 32 * kCellSplit) visit(B.cell_extra[e]);
+    } else {
+#pragma unroll 4
+      for (int j = part * 32 + lane; j < P.n_bead; j += 32 * kCellSplit) {
+        const int4 f = B.fpos[j];
+        visit(make_int4(f.x, f.y, f.z, (j << 3) | f.w));
+      }
     }
-    const int n_extra = min(B.cell_n[nx * ny * nz], P.cell_cap);
-    for (int e = part * 32 + lane; e < n_extra; e += 32 * kCellSplit) visit(B.cell_extra[e]);
     for (int q2 = q + 1 + part * 32 + lane; q2 < m; q2 += 32 * kCellSplit) {
       const int4 o = ch ? B.ftrial[q2] : B.fpos[b_lo + q2];
       const float r2 = desc_r2_fix(P, p, o);
@@ -1197,13 +1208,9 @@ void launch_desc_batch(const DevParams* rp, const DevBuffers* rb, int n_rep, uns
   if (cell_moved > 0)
     k_desc_cells<<<dim3((std::min(cell_moved, kDescMaxMoved) + kCellBeads - 1) / kCellBeads,
                         n_rep), kCellWarps * 32, 0, st>>>(rp, rb);
-  if (cell_moved > 0 && form) {
-    // the all-pairs kernel only takes replicas whose cell list overflowed:
-    // usually none, so a small grid (it still has to look at every replica)
-    k_desc<1><<<152, kDescThreads, 0, st>>>(rp, rb, n_rep);
-  } else {
-    launch_desc_counts(rp, rb, n_rep, form, st);
-  }
+  // with cell lists the cell kernel also takes the replicas whose list is
+  // not valid (all pairs); else the all-pairs kernel takes every replica
+  if (!(cell_moved > 0 && form)) launch_desc_counts(rp, rb, n_rep, form, st);
   // programmatic dependent of k_desc (it waits for the counts itself)
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(n_rep);

@@ -786,6 +786,7 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
       for (int i = b_lo + threadIdx.x; i < b_hi; i += blockDim.x) {
         const int4 old_f = P.form ? B.fpos[i] : make_int4(0, 0, 0, 0);
         B.pos[i] = B.trial[i];
+        if (B.fpos64) B.fpos64[i] = fix64x4(P, B.trial[i]);
         if (P.form) B.fpos[i] = B.ftrial[i - b_lo];
         if (P.cell_cap && B.cell_key) {
           // the bead's entry follows it: rewritten in place while it stays in
