@@ -234,18 +234,36 @@ def make_workload(name, seed=20261203):
     return d
 
 
+def _write_brush(job):
+    from plum_gb300 import systems
+    d, spec, seed = job
+    systems.write_brush(d, spec, seed=seed)
+    return d
+
+
 def make_brush_ensemble(n, seed=20261203, only=None):
     """The confined-brush replicas of uneven size (systems.brush_ensemble);
-    `only` picks one replica index."""
+    `only` picks one replica index. Missing ones are written by a process
+    pool (spawned, so it never forks a process that holds a CUDA context)."""
+    import concurrent.futures
+    import multiprocessing
     from plum_gb300 import systems
-    dirs = []
+    dirs, todo = [], []
     for i, spec in enumerate(systems.brush_ensemble(n, seed)):
         if only is not None and i != only:
             continue
         d = os.path.join(tempfile.gettempdir(), "plum_bench_brush_%d_%d" % (seed, i))
         if not os.path.exists(os.path.join(d, "run.in")):
-            systems.write_brush(d, spec, seed=seed + i)
+            todo.append((d, spec, seed + i))
         dirs.append(d)
+    if len(todo) > 1:
+        workers = max(1, min(len(todo), os.cpu_count() or 1, 16))
+        with concurrent.futures.ProcessPoolExecutor(
+                workers, mp_context=multiprocessing.get_context("spawn")) as ex:
+            list(ex.map(_write_brush, todo))
+    else:
+        for job in todo:
+            _write_brush(job)
     return dirs
 
 
@@ -552,6 +570,50 @@ def equilibrium(args, device, sg, tune):
     return out
 
 
+def brush_ensemble_batch(args, local, flush):
+    """The batching form on its own workload: the confined-brush replicas of
+    uneven size (walls with 9-3 LJ and surface sites, slab Ewald with a 3H
+    vacuum gap), one batch, autotuned items, no surrogate, each replica's FP64
+    recompute every 1e4 of its moves inside the timed steps."""
+    import numpy as np
+    import torch
+    import plum_gb300 as pg
+    dirs = make_brush_ensemble(args.brush_replicas)
+    t0 = time.perf_counter()
+    b = pg.Batch(dirs, device=local)
+    setup_s = time.perf_counter() - t0
+    b.seed(np.arange(31000, 31000 + len(dirs), dtype=np.uint32))
+    tune = b.autotune(8)
+    for _ in range(2):
+        b.run(args.batch_steps)
+    ms, n_rc, rc_ms = [], 0, 0.0
+    for _ in range(3):
+        flush.zero_()
+        torch.cuda.synchronize()
+        b.run(args.batch_steps)
+        ms.append(b.last_timing()[0])
+        _, n, t = b.drift()
+        n_rc += n
+        rc_ms += t
+    n_bead = [b.replica(r).n_bead for r in range(len(dirs))]
+    drift_tab, _, _ = b.drift()
+    etot = b.energies().sum(axis=1)
+    kern = b.time_kernels(8)
+    b.close()
+    return {"value": len(dirs) * args.batch_steps / (statistics.mean(ms) / 1e3),
+            "unit": "moves/s", "replicas": len(dirs), "beads_total": int(sum(n_bead)),
+            "beads_min_max": [int(min(n_bead)), int(max(n_bead))],
+            "ms_per_step": statistics.mean(ms), "steps_per_batch": args.batch_steps,
+            "autotuned_items": tune, "setup_s": setup_s,
+            "kernel_ms_per_launch": {"delta": float(kern[0]), "serial": float(kern[1])},
+            "recomputes_in_timed_steps": n_rc,
+            "recompute_share_of_timed_device_time": rc_ms / max(sum(ms), 1e-9),
+            "drift_max_rel_total": float((drift_tab[:, 4] / np.maximum(1.0, np.abs(etot))).max()),
+            "workload": "%d confined brush replicas: H in [30, 60], Lx = Ly = 32, 16-64 grafted "
+                        "chains of 20-80 beads, charge fraction f in [0.1, 1], 9-3 walls with "
+                        "64 LJ sites each, slab Ewald (3H gap)" % len(dirs)}
+
+
 def precision_cases(args, local):
     """precision_on_chain for the three bulk/confined configurations: the
     1,000-particle bulk system (reference Ewald rule: multi-image real
@@ -767,6 +829,9 @@ def main():
     ap.add_argument("--precision-moves", type=int, default=10000,
                     help="proposals per configuration for the FP32-vs-FP64 comparison")
     ap.add_argument("--stats", type=int, default=1, help="0: skip the equilibrium block")
+    ap.add_argument("--brush-replicas", type=int, default=256,
+                    help="replicas of the confined-brush ensemble measured after the "
+                         "headline (0: skip)")
     ap.add_argument("--stat-replicas", type=int, default=16)
     ap.add_argument("--burn", type=int, default=500000,
                     help="burn-in moves per replica (chosen form) before the statistics")
@@ -921,6 +986,12 @@ def main():
     batched32 = R * BS / (statistics.mean(nb_ms) / 1e3)
     kern_ms_nb = nb.time_kernels(32)
     nb.close()
+    brush = None
+    if args.brush_replicas > 0:
+        try:
+            brush = brush_ensemble_batch(args, local, flush)
+        except Exception as e:  # a secondary line: report the failure, keep the headline
+            brush = {"error": "%s: %s" % (type(e).__name__, e)}
 
     # plain FP64 on one system of the workload: moves/s, per-kernel times and
     # an e2e through plum_run_moves (recorded stream in, logs out)
@@ -1038,6 +1109,7 @@ def main():
         "batched_fp32_no_surrogate": {"value": batched32, "unit": "moves/s",
                                       "ms_per_step": statistics.mean(nb_ms),
                                       "autotuned_items": tune_nb},
+        "batched_brush_ensemble": brush,
         "delayed_acceptance": da,
         "kernel_ms_per_launch": {
             "chosen_form": dict(zip(("delta", "serial", "descriptor", "inference"),

@@ -379,8 +379,8 @@ int plum_batch_time_kernels(plum_batch* batch, int n_steps, double* out4);
 int plum_batch_set_tune(plum_batch* batch, int item_pairs, int k_tile, int grid,
                         int min_blocks);
 /* Times the energy-change kernel on these replicas (`steps` steps per
- * candidate, see plum_batch_time_kernels) for item sizes {2048, 4096, 8192,
- * 16384} x k tiles {128, 256, 512, 1024} x grids {2, 3, 4, 6, 8} blocks per
+ * candidate, see plum_batch_time_kernels) for item sizes {4096, 8192, 16384,
+ * 32768} x k tiles {128, 256, 512, 1024} x grids {2, 3, 4, 6, 8} blocks per
  * SM x register budgets {2, 3, 4} blocks per SM, keeps the fastest (then the
  * two pair loops of plum_batch_set_real_term at those sizes); out4 (may be
  * NULL) = the chosen {item_pairs,

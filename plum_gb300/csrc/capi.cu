@@ -645,7 +645,7 @@ static int create_ctx(plum_ctx* c, int form, int device, plum_ctx** out) {
   rc |= dalloc(&B.state, 1);
   c->n_tot_part = total_partials_count(P);
   rc |= dalloc(&c->d_tot_part, 2 * (size_t)c->n_tot_part);
-  rc |= dalloc(&c->d_sk_part, (size_t)sk_full_groups() * std::max(1, P.n_k));
+  rc |= dalloc(&c->d_sk_part, (size_t)sk_full_groups(P) * std::max(1, P.n_k));
   rc |= dalloc(&c->d_out, 64);
   rc |= dalloc(&c->d_obs_per, 5 * (size_t)std::max(1, in.n_mol));
   c->rhoz_bins = (int)std::ceil(in.box[2] / kRhoZRes);
@@ -2615,7 +2615,7 @@ int plum_batch_autotune(plum_batch* b, int steps, int* out4) {
   if (!b || steps <= 0) return fail(PLUM_ERR_INPUT, "bad argument");
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-  const int pairs[] = {2048, 4096, 8192, 16384};
+  const int pairs[] = {4096, 8192, 16384, 32768};
   const int ktiles[] = {128, 256, 512, 1024};
   const int per_sm[] = {2, 3, 4, 6, 8};
   const int occ[] = {2, 3, 4};

@@ -224,7 +224,7 @@ void launch_total64(const DevParams& P, const DevBuffers& B, double* out_partial
 int total_partials_count(const DevParams& P);
 // S(k) from scratch; part: sk_full_groups() * n_k double2 of scratch owned by
 // the caller (one per context, so contexts on different streams never share it)
-int sk_full_groups();
+int sk_full_groups(const DevParams& P);
 void launch_sk_full64(const DevParams& P, const DevBuffers& B, double2* part, cudaStream_t s);
 void launch_misc_total64(const DevParams& P, const DevBuffers& B, double* out6,
                          cudaStream_t s);

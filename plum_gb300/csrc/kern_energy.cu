@@ -552,50 +552,89 @@ void launch_total64(const DevParams& P, const DevBuffers& B, double* out, int n_
 
 // S(k) from scratch: block (k tile, bead group) writes a partial; a second
 // pass adds the groups in order.
-constexpr int kSkGroups = 16;
+// Each thread takes kSkPer consecutive k-vectors (a tile of kSkTile per
+// block); vectors of one (n_x, n_y) column (n_z runs fastest in the k list)
+// share the product e^{i(k_x x + k_y y)} per bead, and each phase is the same
+// cmul(cmul(ex, ey), ez) as phase_from's. Bead groups split the beads so that
+// the grid is one wave of two blocks per SM; a second pass adds the groups in
+// order.
+constexpr int kSkPer = 4;
+constexpr int kSkTile = kSkPer * kPairThreads;
+constexpr int kSkGroupsMax = 512;
+
+int sk_full_groups(const DevParams& P) {
+  const int tiles = std::max(1, (P.n_k + kSkTile - 1) / kSkTile);
+  const int want = (pair_grid() + tiles - 1) / tiles;  // two blocks per SM, one wave
+  return std::max(1, std::min(kSkGroupsMax, want));  // groups past the beads add zero
+}
 
 __global__ void __launch_bounds__(kPairThreads)
-    k_sk64(const DevParams P, const DevBuffers B, double2* part) {
+    k_sk64(const DevParams P, const DevBuffers B, double2* part, int groups) {
   extern __shared__ __align__(32) unsigned char smem[];
   double2* tabs = reinterpret_cast<double2*>(smem);
   const int per = P.kper;
   const int chunk = P.kchunk_sk;
-  const int k = blockIdx.x * kPairThreads + threadIdx.x;
   const int g = blockIdx.y;
-  const int per_g = (P.n_bead + kSkGroups - 1) / kSkGroups;
+  const int per_g = (P.n_bead + groups - 1) / groups;
   const int b0 = g * per_g, b1 = min(P.n_bead, b0 + per_g);
-  short4 kv = make_short4(0, 0, 0, 0);
-  if (k < P.n_k) kv = B.kn[k];
-  double2 s = make_double2(0.0, 0.0);
+  int kk[kSkPer], ox[kSkPer], oy[kSkPer], oz[kSkPer];
+  bool mine[kSkPer], col[kSkPer], ny[kSkPer], nz[kSkPer];
+  double2 s[kSkPer];
+#pragma unroll
+  for (int q = 0; q < kSkPer; q++) {
+    kk[q] = blockIdx.x * kSkTile + threadIdx.x * kSkPer + q;
+    mine[q] = kk[q] < P.n_k;
+    const short4 kv = mine[q] ? B.kn[kk[q]] : make_short4(0, 0, 0, 0);
+    ox[q] = P.koff[0] + kv.x;
+    oy[q] = P.koff[1] + (kv.y >= 0 ? kv.y : -kv.y);
+    oz[q] = P.koff[2] + (kv.z >= 0 ? kv.z : -kv.z);
+    ny[q] = kv.y < 0;
+    nz[q] = kv.z < 0;
+    col[q] = q == 0 || ox[q] != ox[q - 1] || oy[q] != oy[q - 1] || ny[q] != ny[q - 1];
+    s[q] = make_double2(0.0, 0.0);
+  }
   for (int c0 = b0; c0 < b1; c0 += chunk) {
     const int cnt = min(chunk, b1 - c0);
     __syncthreads();
     for (int t = threadIdx.x; t < cnt * 3; t += blockDim.x)
       build_axis_table(P, B.pos[c0 + t / 3], t % 3, tabs + (t / 3) * per);
     __syncthreads();
-    if (k < P.n_k)
+    if (mine[0])
       for (int b = 0; b < cnt; b++) {
-        double2 e = phase_from(P, tabs + b * per, kv);
-        s.x += e.x;
-        s.y += e.y;
+        const double2* tb = tabs + b * per;
+        double2 xy = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int q = 0; q < kSkPer; q++)
+          if (mine[q]) {
+            if (col[q]) {
+              double2 ey = tb[oy[q]];
+              if (ny[q]) ey.y = -ey.y;
+              xy = cmul(tb[ox[q]], ey);
+            }
+            double2 ez = tb[oz[q]];
+            if (nz[q]) ez.y = -ez.y;
+            const double2 e = cmul(xy, ez);
+            s[q].x += e.x;
+            s[q].y += e.y;
+          }
       }
   }
-  if (k < P.n_k) part[(size_t)g * P.n_k + k] = s;
+#pragma unroll
+  for (int q = 0; q < kSkPer; q++)
+    if (mine[q]) part[(size_t)g * P.n_k + kk[q]] = s[q];
 }
 
-__global__ void k_sk_sum(int n_k, const double2* part, double2* sk) {
+__global__ void k_sk_sum(int n_k, int groups, const double2* part, double2* sk) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n_k) return;
   double2 s = make_double2(0.0, 0.0);
-  for (int g = 0; g < kSkGroups; g++) {
+  for (int g = 0; g < groups; g++) {
     double2 p = part[(size_t)g * n_k + k];
     s.x += p.x;
     s.y += p.y;
   }
   sk[k] = s;
 }
-
-int sk_full_groups() { return kSkGroups; }
 
 void launch_sk_full64(const DevParams& P, const DevBuffers& B, double2* part, cudaStream_t s) {
   if (!P.use_ewald || P.n_k == 0) return;
@@ -605,9 +644,10 @@ void launch_sk_full64(const DevParams& P, const DevBuffers& B, double2* part, cu
     attr = true;
   }
   size_t smem = (size_t)P.kchunk_sk * P.kper * sizeof(double2);
-  dim3 grid((P.n_k + kPairThreads - 1) / kPairThreads, kSkGroups);
-  k_sk64<<<grid, kPairThreads, smem, s>>>(P, B, part);
-  k_sk_sum<<<(P.n_k + 255) / 256, 256, 0, s>>>(P.n_k, part, B.sk);
+  const int groups = sk_full_groups(P);
+  dim3 grid((P.n_k + kSkTile - 1) / kSkTile, groups);
+  k_sk64<<<grid, kPairThreads, smem, s>>>(P, B, part, groups);
+  k_sk_sum<<<(P.n_k + 255) / 256, 256, 0, s>>>(P.n_k, groups, part, B.sk);
 }
 
 // Bond energy of molecule m on coordinates p (potential_spring.cc:22-48),

@@ -21,6 +21,7 @@
 #include "engine.h"
 #include "mlp.h"
 #include "device_common.cuh"
+#include "unit_draw.h"
 
 namespace plum {
 
@@ -41,7 +42,7 @@ struct Draws {
     pos++;
     return v;
   }
-  __device__ double u() { return (double)next() / kMtMax; }
+  __device__ double u() { return unit_draw(next()); }
   __device__ uint32_t at(long long o) const {
     long long w = o - wbase;
     return (w >= 0 && w < wlen) ? win[w] : g[o];
@@ -65,8 +66,8 @@ __device__ __forceinline__ bool sphere_reject(uint32_t u1, uint32_t u2) {
   const unsigned long long rhs = M2 - b2;
   const unsigned long long diff = a2 > rhs ? a2 - rhs : rhs - a2;
   if (diff > (1ull << 26)) return a2 > rhs;
-  double r1 = 1.0 - 2.0 * ((double)u1 / kMtMax);
-  double r2 = 1.0 - 2.0 * ((double)u2 / kMtMax);
+  double r1 = 1.0 - 2.0 * unit_draw(u1);
+  double r2 = 1.0 - 2.0 * unit_draw(u2);
   return r1 * r1 + r2 * r2 > 1.0;
 }
 
@@ -107,10 +108,21 @@ __device__ long long sphere_scan_bits(Draws& d, const unsigned* accbits) {
   return sphere_scan(d);
 }
 
+// Metropolis' u < exp(-x) (simulation.cc:324-332), the same decision without
+// the exponential where it is certain: x <= 0 gives exp(-x) >= 1 > u for
+// u < 1; above x = 23, exp(-x) < 1.03e-10 is below every non-zero draw
+// (the least is 1 / (2^32 - 1) = 2.33e-10), so only u = 0 needs it. A NaN x
+// fails both tests and compares false with the exponential, as before.
+__device__ __forceinline__ bool metropolis(double u, double x) {
+  if (x <= 0.0 && u < 1.0) return true;
+  if (x > 23.0) return u == 0.0 && 0.0 < exp(-x);
+  return u < exp(-x);
+}
+
 // The unit vector randSphere returns for an accepted pair.
 __device__ void sphere_vec(uint32_t u1, uint32_t u2, double* v) {
-  double r1 = 1.0 - 2.0 * ((double)u1 / kMtMax);
-  double r2 = 1.0 - 2.0 * ((double)u2 / kMtMax);
+  double r1 = 1.0 - 2.0 * unit_draw(u1);
+  double r2 = 1.0 - 2.0 * unit_draw(u2);
   double rs = r1 * r1 + r2 * r2;
   double ranh = 2.0 * sqrt(1.0 - rs);
   v[0] = r1 * ranh;
@@ -311,14 +323,14 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
     (void)d.next();  // simulation.cc:221 (the GC draw)
     const int n_ch = P.n_chain_total, n_io = P.n_ion_total;
     if (P.n_mol - P.phantom > 0) {
-      int wc = (int)floor((double)d.next() / kMtMax * n_ch);
-      int wi = (int)floor((double)d.next() / kMtMax * n_io);
+      int wc = (int)floor(unit_draw(d.next()) * n_ch);
+      int wi = (int)floor(unit_draw(d.next()) * n_io);
       if (wc == n_ch) wc--;
       if (wi == n_io) wi--;
       int chain_id = (wc >= 0 && wc < n_ch) ? B.chain_ids[wc] : -1;
       int ion_id = (wi >= 0 && wi < n_io) ? B.ion_ids[wi] : -1;
       int mt = 0;
-      double u = (double)d.next() / kMtMax;
+      double u = unit_draw(d.next());
       double cur = P.move_prob[0];
       while (cur < u && mt < 4) {
         mt++;
@@ -386,7 +398,7 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
                 double dy = (p[1] + s * v[1]) - prev[1];
                 double dz = (p[2] + s * v[2]) - prev[2];
                 double bl = eq;
-                if (P.vary_bond) bl += (eq / 5.0) * ((double)d.next() / kMtMax - 0.5);
+                if (P.vary_bond) bl += (eq / 5.0) * (unit_draw(d.next()) - 0.5);
                 double norm = bl / sqrt(dx * dx + dy * dy + dz * dz);
                 double c[3] = {norm * dx + prev[0], norm * dy + prev[1], norm * dz + prev[2]};
                 for (int a = 0; a < 3; a++) {
@@ -412,7 +424,7 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
             for (int a = 0; a < 3; a++) ax[a] /= n;
           }
           const double pi_libm = 3.14159265358979323846;
-          double ang = P.move_size * ((double)d.next() / kMtMax * 2 * pi_libm - pi_libm);
+          double ang = P.move_size * (unit_draw(d.next()) * 2 * pi_libm - pi_libm);
           double sn, cs;
           sincos(ang, &sn, &cs);
           double sa[3] = {sn * ax[0], sn * ax[1], sn * ax[2]};
@@ -433,7 +445,7 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
         } else {
           // Molecule::RandomReptation (molecule.cc:267-312)
           double bl = P.bond_len;
-          if (P.vary_bond) bl += (P.bond_len / 5.0) * ((double)d.next() / kMtMax - 0.5);
+          if (P.vary_bond) bl += (P.bond_len / 5.0) * (unit_draw(d.next()) - 0.5);
           int dir = 1, end = len - 1;
           if (d.next() % 2u == 0u) {
             dir = -1;
@@ -492,7 +504,7 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
       double v[3];
       sphere_vec(d.at(wbase + s_off[i]), d.at(wbase + s_off[i] + 1), v);
       double bl = eq;
-      if (P.vary_bond) bl += (eq / 5.0) * ((double)d.at(wbase + s_boff[i]) / kMtMax - 0.5);
+      if (P.vary_bond) bl += (eq / 5.0) * (unit_draw(d.at(wbase + s_boff[i])) - 0.5);
       const double4_32a oi = B.pos[g.b0 + i], oj = B.pos[g.b0 + j];
       double dx = (oi.x - oj.x) + g.s * v[0];
       double dy = (oi.y - oj.y) + g.s * v[1];
@@ -767,12 +779,12 @@ __device__ __forceinline__ void serial_body(const DevParams& P, const DevBuffers
           // move, min(1, exp(-beta (dE - s))) gives the same ratio
           // exp(-beta dE) of forward to reverse acceptance as Metropolis.
           if (!S.da_skip && !(S.de >= kVeryLarge))
-            acc = d.u() < exp(-P.beta * (S.de - S.da_s));
+            acc = metropolis(d.u(), P.beta * (S.de - S.da_s));
           S.da_n_moves++;
           S.da_n_pass += S.da_skip ? 0 : 1;
           S.da_n_accept += acc;
         } else if (!(S.de >= kVeryLarge)) {
-          acc = d.u() < exp(-P.beta * S.de);  // a NaN dE still draws
+          acc = metropolis(d.u(), P.beta * S.de);  // a NaN dE still draws
         }
         if (d.overrun) S.error = PLUM_ERR_STREAM_DEV;
       } else {

@@ -93,7 +93,7 @@ def test_autotune_picks_a_candidate_and_keeps_running(pg):
     b = pg.Batch([d] * 8)
     b.seed(3)
     ip, kt, grid, mb = b.autotune(4)
-    assert ip in (2048, 4096, 8192, 16384) and kt in (128, 256, 512, 1024) and grid > 0
+    assert ip in (4096, 8192, 16384, 32768) and kt in (128, 256, 512, 1024) and grid > 0
     assert mb in (2, 3, 4) and b.real_term() in (0, 1)
     assert b.run(100) > 0
 
