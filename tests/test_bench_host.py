@@ -1,5 +1,6 @@
 """Host-side measurement helpers of bench.py: the pooled integrated
-autocorrelation time and the paired 2-SE check (CPU only)."""
+autocorrelation time, the paired 2-SE check and its labels, and the pooled
+writer of the brush ensemble (CPU only)."""
 import os
 import sys
 
@@ -34,3 +35,25 @@ def test_paired_check():
     assert ok["standard_error"] < 0.3  # pairing removes the shared spread
     bad = bench.paired_check(x + 10 * ok["standard_error"], y)
     assert not bad["within_2_se"]
+
+
+def test_paired_check_names_the_other_arm():
+    x, y = [1.0, 2.0, 3.0], [1.1, 2.1, 2.9]
+    assert "plain_fp64_mean" in bench.paired_check(x, y)
+    r = bench.paired_check(x, y, other="plain_dynamics")
+    assert "plain_dynamics_mean" in r and "plain_fp64_mean" not in r
+
+
+def test_brush_ensemble_written_by_the_pool_equals_a_sequential_write(tmp_path, monkeypatch):
+    """The process pool writes the same files as a replica written on its own
+    (every replica has its own seed)."""
+    import filecmp
+    monkeypatch.setattr(bench.tempfile, "gettempdir", lambda: str(tmp_path / "pool"))
+    os.makedirs(tmp_path / "pool")
+    dirs = bench.make_brush_ensemble(3, seed=7)
+    monkeypatch.setattr(bench.tempfile, "gettempdir", lambda: str(tmp_path / "one"))
+    os.makedirs(tmp_path / "one")
+    for i, d in enumerate(dirs):
+        (one,) = bench.make_brush_ensemble(3, seed=7, only=i)
+        for f in ("run.in", "input_crd.dat", "input_top.dat"):
+            assert filecmp.cmp(os.path.join(d, f), os.path.join(one, f), shallow=False), (i, f)
