@@ -481,10 +481,11 @@ __global__ void __launch_bounds__(kTotTile)
 // k_total64 for LJ + Ewald in a cubic box periodic on every axis, one image
 // (r_c <= L/2) and one box for both terms: positions as 64-bit fixed-point
 // fractions of the box, staged per tile, so one integer subtraction is the
-// minimum-image difference and its conversion to FP64 the only rounding of
-// the vector (more accurate than x_j - x_i in FP64). r^2 in FP64, in units of
-// (L / 2^64)^2; the cut-off pre-tests in FP32 with a margin, decided in FP64
-// inside; the real-space term sqrt(alpha) h(alpha r^2) from the FP64 table,
+// minimum-image difference (each fraction carries the rounding of x / L, about
+// one ulp of the coordinate, as its FP64 value does; the subtraction is exact
+// and the conversion to FP64 rounds once). r^2 in FP64, in units of
+// (L / 2^64)^2; the cut-off tests as integer compares of the FP64 bit
+// patterns; the real-space term sqrt(alpha) h(alpha r^2) from the FP64 table,
 // with lB sqrt(alpha) q_i folded into the thread's charge.
 __global__ void __launch_bounds__(kTotTile)
     k_total64_fix(const DevParams P, const DevBuffers B, double* out) {
