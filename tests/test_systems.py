@@ -79,3 +79,24 @@ def test_brush_sites_alternate_charge(tmp_path):
     mol, sym, xyz, q, box = read(d)
     qs = q[np.array([s == "S" for s in sym])]
     np.testing.assert_array_equal(qs, np.tile([0.5, -0.5], 6))
+
+
+def test_brush_ensemble_follows_the_batching_workload():
+    """The 256 confined-brush replicas of the batching form: wall gap H in
+    [30, 60], Lx = Ly = 32, 16-64 grafted chains of 20-80 beads, charge
+    fraction in [0.1, 1], 64 surface sites per wall; the draws spread over
+    the ranges and the sizes are uneven."""
+    from plum_gb300 import systems
+    specs = systems.brush_ensemble(256, 20261203)
+    assert len(specs) == 256
+    g = np.array([s.n_graft for s in specs])
+    n = np.array([s.chain_len for s in specs])
+    h = np.array([s.height for s in specs])
+    f = np.array([s.charge_frac for s in specs])
+    assert g.min() >= 16 and g.max() <= 64 and n.min() >= 20 and n.max() <= 80
+    assert h.min() >= 30.0 and h.max() <= 60.0 and f.min() >= 0.1 and f.max() <= 1.0
+    assert all(s.lxy == 32.0 and s.n_sites == 64 for s in specs)
+    assert g.max() - g.min() > 40 and n.max() - n.min() > 50 and h.max() - h.min() > 25
+    beads = g * n
+    assert beads.max() > 5 * beads.min()  # uneven sizes
+    assert systems.brush_ensemble(256, 20261203)[17] == specs[17]  # seeded
