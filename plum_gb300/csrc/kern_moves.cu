@@ -108,17 +108,6 @@ __device__ long long sphere_scan_bits(Draws& d, const unsigned* accbits) {
   return sphere_scan(d);
 }
 
-// Metropolis' u < exp(-x) (simulation.cc:324-332), the same decision without
-// the exponential where it is certain: x <= 0 gives exp(-x) >= 1 > u for
-// u < 1; above x = 23, exp(-x) < 1.03e-10 is below every non-zero draw
-// (the least is 1 / (2^32 - 1) = 2.33e-10), so only u = 0 needs it. A NaN x
-// fails both tests and compares false with the exponential, as before.
-__device__ __forceinline__ bool metropolis(double u, double x) {
-  if (x <= 0.0 && u < 1.0) return true;
-  if (x > 23.0) return u == 0.0 && 0.0 < exp(-x);
-  return u < exp(-x);
-}
-
 // The unit vector randSphere returns for an accepted pair.
 __device__ void sphere_vec(uint32_t u1, uint32_t u2, double* v) {
   double r1 = 1.0 - 2.0 * unit_draw(u1);

@@ -5,9 +5,14 @@
 // from its leading one are known exactly, the rest is non-zero, and rounding
 // them to 53 bits with that rest as a sticky bit is one conversion. Checked
 // against the division for every 32-bit x (tests/test_unit_draw.py).
-// Compiles as CUDA device code and as C (the check).
+// Compiles as CUDA device code and as C (the check). Also the Metropolis
+// test of those draws.
 #pragma once
 #include <stdint.h>
+#ifndef __CUDACC__
+#include <math.h>
+#include <stdbool.h>
+#endif
 
 #ifdef __CUDACC__
 __device__ __forceinline__ double unit_draw(uint32_t x) {
@@ -35,3 +40,20 @@ static inline double unit_draw(uint32_t x) {
   return d;
 }
 #endif
+
+#ifdef __CUDACC__
+#define PLUM_DRAW_FN __device__ __forceinline__
+#else
+#define PLUM_DRAW_FN static inline
+#endif
+
+// Metropolis' u < exp(-x) (simulation.cc:324-332), the same decision without
+// the exponential where it is certain: x <= 0 gives exp(-x) >= 1 > u for
+// u < 1; above x = 23, exp(-x) < 1.03e-10 is below every non-zero draw
+// (the least is 1 / (2^32 - 1) = 2.33e-10), so only u = 0 needs it. A NaN x
+// fails both tests and compares false with the exponential, as before.
+PLUM_DRAW_FN bool metropolis(double u, double x) {
+  if (x <= 0.0 && u < 1.0) return true;
+  if (x > 23.0) return u == 0.0 && 0.0 < exp(-x);
+  return u < exp(-x);
+}
