@@ -351,7 +351,10 @@ __device__ __forceinline__ void gen_move(const DevParams& P, const DevBuffers& B
           for (int a = 0; a < 3; a++) plan.vec[a] = vl * v[a];
           plan.b_hi = b0 + 1;
         } else if (mt == 1) {
-          // Molecule::COMTranslate (molecule.cc:135-151)
+          // Molecule::COMTranslate (molecule.cc:135-151). Here, and in the
+          // pivot and crankshaft picks, the reference multiplies the word
+          // before dividing, so these keep the division (unit_draw is the
+          // quotient of the word alone).
           for (int a = 0; a < 3; a++) plan.vec[a] = 0.5 * P.move_size * (double)d.next() / kMtMax;
           for (int a = 0; a < 3; a++)
             if (d.next() % 2u == 0u) plan.vec[a] = -plan.vec[a];
